@@ -1,0 +1,103 @@
+"""Seeded synthetic structures of the benchmark shapes.
+
+* :func:`cantilever_rollup` — 20 Beam_1 elements (41 nodes, 246 DOF), L = 10 m,
+  E = 210 GPa, nu = 0.3, 0.1 x 0.1 m rectangle, clamped at x = 0, tip moment
+  about z ramped to 2*pi*E*I/L over 20 load steps (the beam rolls into a full
+  circle), residual tolerance 1e-8.
+* :func:`pipe_chain` / :func:`batched_static` — pipe-section Beam_1 chains
+  (Tube De ~ U(0.3, 0.5) m, wall ~ U(0.02, 0.04) m, E = 210 GPa), clamped at
+  one end, tip force ~ N(0, 1e5) N per component, 10 load steps; element
+  counts log-uniform in [50, 2000] from the seed.  The element length is not
+  fixed by the benchmark description; these chains use 1 m elements along +z.
+* :func:`tutorial01` — the reference's tutorial01 deck (5 Beam_1 cantilever,
+  tip force), built programmatically.
+
+Every generator is deterministic in its seed (numpy default_rng).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .model import GF_STATIC, NodalLoad, Solution, Structure, Table
+
+E_STEEL = 210e9
+NU_STEEL = 0.3
+RHO_STEEL = 7850.0
+
+
+def straight_chain(n_el: int, length: float, direction=(1.0, 0.0, 0.0)) -> np.ndarray:
+    d = np.asarray(direction, dtype=np.float64)
+    d = d / np.linalg.norm(d)
+    t = np.linspace(0.0, length, 2 * n_el + 1)
+    return t[:, None] * d[None, :]
+
+
+def cantilever_rollup(n_el: int = 20, steps: int = 20, tol: float = 1e-8) -> Structure:
+    L = 10.0
+    s = Structure(nodes=straight_chain(n_el, L))
+    mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
+    sec = s.add_rectangle(0.1, 0.1)
+    cs_beam = s.add_cs((0.0, 1.0, 0.0), (1.0, 0.0, 0.0))   # E3 along the axis
+    cs_glob = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+    for e in range(n_el):
+        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs_beam))
+    s.clamp(0)
+    I = s.sections[sec][2]  # bending about global z is about the section's E2 axis
+    Mz = 2.0 * math.pi * E_STEEL * I / L
+    s.loads.append(NodalLoad([2 * n_el], cs_glob,
+                             Table(np.array([0.0, 1.0]),
+                                   np.array([[0, 0, 0, 0, 0, 0], [0, 0, 0, 0, 0, Mz]], dtype=float))))
+    dt = 1.0 / steps
+    s.solution = Solution(GF_STATIC, 0.0, 1.0, dt, dt, dt / 1024, 20, 3, 4, 1.0)
+    # No force is applied, so the force criterion falls back to
+    # ForceMinimumReference * tol; 1e4 N puts it (1e-4 N) above the FP64
+    # round-off floor of the axial force residual (~1e-6 N for EA = 2.1e9 N).
+    s.criteria.update(force_tol=tol, moment_tol=tol, force_min=1e4)
+    return s
+
+
+def tutorial01() -> Structure:
+    s = Structure(nodes=np.array([[0.0, 0.0, 0.1 * i] for i in range(11)]))
+    s.nodes[:, 2] = [0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0]
+    mat = s.add_material(1e7, 0.3, 2000)
+    sec = s.add_rectangle(0.1, 0.1)
+    cs = s.add_cs((1, 0, 0), (0, 0, 1))
+    for e in range(5):
+        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    s.clamp(0)
+    s.loads.append(NodalLoad([10], cs, Table(np.array([0.0, 1.0]),
+                                              np.array([[0, 0, 0, 0, 0, 0], [1000, 0, 0, 0, 0, 0]],
+                                                       dtype=float))))
+    s.solution = Solution(GF_STATIC, 0.0, 1.0, 0.1, 0.1, 0.01, 20, 3, 4, 1.0, sample=2)
+    return s
+
+
+def pipe_chain(n_el: int, De: float, wall: float, tip_force, steps: int = 10,
+               element_length: float = 1.0, tol: float = 1e-9) -> Structure:
+    s = Structure(nodes=straight_chain(n_el, n_el * element_length, (0.0, 0.0, 1.0)))
+    mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
+    sec = s.add_tube(De, De - 2.0 * wall)
+    cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+    for e in range(n_el):
+        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    s.clamp(0)
+    f = np.asarray(tip_force, dtype=np.float64)
+    s.loads.append(NodalLoad([2 * n_el], cs, Table(np.array([0.0, 1.0]),
+                                                   np.array([[0.0] * 6, [*f, 0.0, 0.0, 0.0]]))))
+    dt = 1.0 / steps
+    s.solution = Solution(GF_STATIC, 0.0, 1.0, dt, dt, dt / 4096, 30, 3, 4, 1.0)
+    s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol)
+    return s
+
+
+def batched_static(n_chains: int = 512, seed: int = 0, n_min: int = 50, n_max: int = 2000,
+                   steps: int = 10, tol: float = 1e-9) -> list:
+    rng = np.random.default_rng(seed)
+    n_el = np.rint(np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_chains))).astype(int)
+    De = rng.uniform(0.3, 0.5, n_chains)
+    wall = rng.uniform(0.02, 0.04, n_chains)
+    F = rng.normal(0.0, 1e5, (n_chains, 3))
+    return [pipe_chain(int(n), float(d), float(w), F[i], steps=steps, tol=tol)
+            for i, (n, d, w) in enumerate(zip(n_el, De, wall))]

@@ -1,0 +1,391 @@
+"""Structures for the implicit Beam_1 / Shell_1 path.
+
+A :class:`Structure` holds what a GIRAFFE input deck holds for this path
+(nodes, Hooke materials, sections, coordinate systems, Beam_1 / Shell_1
+elements, nodal constraints, nodal loads, shell pressure loads, prescribed
+nodal displacements, one Static or Dynamic solution step and the convergence
+criteria; reference src/IO.cpp:288-657).  It can
+
+* produce the flat C description ``gf_model_desc`` (include/giraffe_model.h)
+  that both the CUDA library and the CPU oracle take, and
+* write itself as a deck in the reference's .inp syntax, which is how the
+  golden fixtures are generated from the reference build.
+
+Indices are 0-based here and 1-based in decks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PI = 3.1415926535897932384626433832795
+
+GF_STATIC, GF_DYNAMIC = 0, 1
+GF_LOAD_NODAL, GF_LOAD_SHELL_PRESSURE = 0, 1
+
+
+# --------------------------------------------------------------------------
+# sections (reference src/SecRectangle.cpp:82-107, src/SecTube.cpp:86-106)
+# --------------------------------------------------------------------------
+def section_rectangle(b: float, h: float) -> tuple:
+    A = b * h
+    I11 = b * h * h * h / 12.0
+    I22 = h * b * b * b / 12.0
+    temp = 0.0
+    for n in range(1, 22, 2):
+        temp += (1.0 / (float(n) ** 5)) * math.tanh(n * PI * h / (2 * b))
+    It = (1.0 / 3.0) * b * b * b * h * (1.0 - 192.0 * b * temp / (PI ** 5 * h))
+    return (A, I11, I22, 0.0, It, I11 + I22)
+
+
+def section_tube(De: float, Di: float) -> tuple:
+    A = (PI / 4.0) * (De * De - Di * Di)
+    I11 = (PI / 64.0) * (De ** 4 - Di ** 4)
+    I33 = (PI / 32.0) * (De ** 4 - Di ** 4)
+    return (A, I11, I11, 0.0, I33, I33)
+
+
+# --------------------------------------------------------------------------
+# ctypes mirror of include/giraffe_model.h
+# --------------------------------------------------------------------------
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class gf_table(C.Structure):
+    _fields_ = [("n_times", C.c_int), ("n_cols", C.c_int), ("times", _dp), ("values", _dp)]
+
+
+class gf_load(C.Structure):
+    _fields_ = [("type", C.c_int), ("n_items", C.c_int), ("items", _ip), ("cs", C.c_int),
+                ("area_update", C.c_int), ("table", gf_table)]
+
+
+class gf_displacement(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("nodes", _ip), ("cs", C.c_int), ("table", gf_table)]
+
+
+class gf_solution(C.Structure):
+    _fields_ = [("type", C.c_int), ("start_time", C.c_double), ("end_time", C.c_double),
+                ("time_step", C.c_double), ("max_time_step", C.c_double),
+                ("min_time_step", C.c_double), ("max_it", C.c_int), ("min_it", C.c_int),
+                ("conv_increase", C.c_int), ("inc_factor", C.c_double), ("beta", C.c_double),
+                ("gamma", C.c_double), ("rayleigh_alpha", C.c_double),
+                ("rayleigh_beta", C.c_double), ("update_rayleigh", C.c_int)]
+
+
+class gf_criteria(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "force_tol", "moment_tol", "force_min", "moment_min", "constraint_min", "disp_tol",
+        "rot_tol", "lag_tol", "disp_min", "rot_min", "lag_min", "divergence_ref")]
+
+
+class gf_model_desc(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("node_xyz", _dp),
+                ("n_materials", C.c_int), ("materials", _dp),
+                ("n_sections", C.c_int), ("sections", _dp),
+                ("n_shell_sections", C.c_int), ("shell_sections", _dp),
+                ("n_cs", C.c_int), ("cs", _dp),
+                ("n_beams", C.c_int), ("beams", _ip),
+                ("n_shells", C.c_int), ("shells", _ip),
+                ("constraints", _ip),
+                ("n_loads", C.c_int), ("loads", C.POINTER(gf_load)),
+                ("n_displacements", C.c_int), ("displacements", C.POINTER(gf_displacement)),
+                ("solution", gf_solution), ("criteria", gf_criteria)]
+
+
+def _r(v):
+    return repr(float(v))
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None and a.size else C.cast(None, t)
+
+
+# --------------------------------------------------------------------------
+@dataclass
+class Table:
+    times: np.ndarray
+    values: np.ndarray  # [n_times][n_cols]
+
+
+@dataclass
+class NodalLoad:
+    nodes: list
+    cs: int
+    table: Table
+
+
+@dataclass
+class PressureLoad:
+    shells: list
+    table: Table
+    area_update: int = 1
+
+
+@dataclass
+class NodalDisplacement:
+    nodes: list
+    cs: int
+    table: Table
+
+
+@dataclass
+class Solution:
+    type: int = GF_STATIC
+    start_time: float = 0.0
+    end_time: float = 1.0
+    time_step: float = 0.1
+    max_time_step: float = 0.1
+    min_time_step: float = 1e-4
+    max_it: int = 20
+    min_it: int = 3
+    conv_increase: int = 4
+    inc_factor: float = 1.0
+    sample: int = 1
+    beta: float = 0.3
+    gamma: float = 0.5
+    rayleigh_alpha: float = 0.0
+    rayleigh_beta: float = 0.0
+    update_rayleigh: int = 0
+
+
+# reference src/ConvergenceCriteria.cpp:15-60
+DEFAULT_CRITERIA = dict(force_tol=1e-4, moment_tol=1e-4, force_min=1e-5, moment_min=1e-5,
+                        constraint_min=1e-7, disp_tol=1e-4, rot_tol=1e-4, lag_tol=1e-4,
+                        disp_min=1e-6, rot_min=1e-6, lag_min=1e-6, divergence_ref=1e15)
+
+
+@dataclass
+class Structure:
+    nodes: np.ndarray                        # [n][3]
+    materials: list = field(default_factory=list)      # (E, nu, rho)
+    sections: list = field(default_factory=list)       # (A, I11, I22, I12, It, I33)
+    section_decks: list = field(default_factory=list)  # deck text of each section
+    shell_sections: list = field(default_factory=list)  # thickness
+    cs: list = field(default_factory=list)             # (E1 xyz, E3 xyz)
+    beams: list = field(default_factory=list)          # (n0, n1, n2, mat, sec, cs)
+    shells: list = field(default_factory=list)         # (6 nodes, mat, shell sec, cs)
+    constraints: np.ndarray | None = None              # [n][6] 0/1
+    loads: list = field(default_factory=list)
+    displacements: list = field(default_factory=list)
+    solution: Solution = field(default_factory=Solution)
+    criteria: dict = field(default_factory=lambda: dict(DEFAULT_CRITERIA))
+
+    # ---- building helpers ----
+    def add_material(self, E, nu, rho):
+        self.materials.append((float(E), float(nu), float(rho)))
+        return len(self.materials) - 1
+
+    def add_rectangle(self, b, h):
+        self.sections.append(section_rectangle(b, h))
+        self.section_decks.append(f"Rectangle\t{len(self.sections)}\tB\t{_r(b)}\tH\t{_r(h)}")
+        return len(self.sections) - 1
+
+    def add_tube(self, De, Di):
+        self.sections.append(section_tube(De, Di))
+        self.section_decks.append(f"Tube\t{len(self.sections)}\tDe\t{_r(De)}\tDi\t{_r(Di)}")
+        return len(self.sections) - 1
+
+    def add_cs(self, e1, e3):
+        self.cs.append(tuple(float(v) for v in (*e1, *e3)))
+        return len(self.cs) - 1
+
+    def clamp(self, node, mask=(1, 1, 1, 1, 1, 1)):
+        if self.constraints is None:
+            self.constraints = np.zeros((len(self.nodes), 6), dtype=np.int32)
+        self.constraints[node] = np.maximum(self.constraints[node], mask)
+
+    @property
+    def n_nodes(self):
+        return len(self.nodes)
+
+    @property
+    def n_free(self):
+        active = np.zeros((self.n_nodes, 6), dtype=bool)
+        for b in self.beams:
+            active[list(b[:3])] = True
+        cons = self.constraints if self.constraints is not None else 0
+        return int((active & (cons == 0)).sum())
+
+    # ---- C description ----
+    def desc(self) -> "DescHandle":
+        return DescHandle(self)
+
+    # ---- deck in the reference's syntax ----
+    def to_inp(self) -> str:
+        o = []
+        s = self.solution
+        o.append("SolutionSteps\t1")
+        if s.type == GF_STATIC:
+            o.append(f"Static\t1\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
+                     f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
+                     f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
+                     f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}")
+        else:
+            o.append(f"Dynamic\t1\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
+                     f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
+                     f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
+                     f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}\n"
+                     f"RayleighDamping\tAlpha\t{_r(s.rayleigh_alpha)}\tBeta\t{_r(s.rayleigh_beta)}"
+                     f"\tUpdate\t{s.update_rayleigh}\n"
+                     f"NewmarkCoefficients\tBeta\t{_r(s.beta)}\tGamma\t{_r(s.gamma)}")
+        o.append(f"Nodes\t{self.n_nodes}")
+        for i, x in enumerate(np.asarray(self.nodes, dtype=np.float64)):
+            o.append(f"Node\t{i + 1}\t{_r(x[0])}\t{_r(x[1])}\t{_r(x[2])}")
+        o.append(f"Elements\t{len(self.beams) + len(self.shells)}")
+        k = 0
+        for b in self.beams:
+            k += 1
+            o.append(f"Beam_1\t{k}\tMat\t{b[3] + 1}\tSec\t{b[4] + 1}\tCS\t{b[5] + 1}\tNodes\t"
+                     f"{b[0] + 1}\t{b[1] + 1}\t{b[2] + 1}")
+        for sh in self.shells:
+            k += 1
+            nodes = "\t".join(str(v + 1) for v in sh[:6])
+            o.append(f"Shell_1\t{k}\tMat\t{sh[6] + 1}\tSec\t{sh[7] + 1}\tCS\t{sh[8] + 1}\tNodes\t{nodes}")
+        o.append(f"Materials\t{len(self.materials)}")
+        for i, (E, nu, rho) in enumerate(self.materials):
+            o.append(f"Hooke\t{i + 1}\tE\t{_r(E)}\tNu\t{_r(nu)}\tRho\t{_r(rho)}")
+        if self.sections:
+            o.append(f"Sections\t{len(self.section_decks)}")
+            o.extend(self.section_decks)
+        if self.shell_sections:
+            o.append(f"ShellSections\t{len(self.shell_sections)}")
+            for i, t in enumerate(self.shell_sections):
+                o.append(f"Homogeneous\t{i + 1}\tThickness\t{_r(t)}")
+        o.append(f"CoordinateSystems\t{len(self.cs)}")
+        for i, c in enumerate(self.cs):
+            o.append(f"CS\t{i + 1}\tE1\t{_r(c[0])}\t{_r(c[1])}\t{_r(c[2])}\tE3\t{_r(c[3])}\t{_r(c[4])}\t{_r(c[5])}")
+        # node sets: one per constrained node group, load and displacement
+        sets, cons_lines, load_lines, disp_lines = [], [], [], []
+
+        def new_set(nodes):
+            sets.append(list(nodes))
+            return len(sets)
+
+        if self.constraints is not None:
+            groups = {}
+            for i, row in enumerate(self.constraints):
+                if row.any():
+                    groups.setdefault(tuple(int(v) for v in row), []).append(i)
+            for mask, nodes in groups.items():
+                ns = new_set(nodes)
+                names = ("UX", "UY", "UZ", "ROTX", "ROTY", "ROTZ")
+                body = "\n".join(f"\t{n}\tBoolTable\t{v}" for n, v in zip(names, mask))
+                cons_lines.append(f"NodalConstraint\t{len(cons_lines) + 1}\tNodeSet\t{ns}\n{body}")
+        for L in self.loads:
+            if isinstance(L, NodalLoad):
+                ns = new_set(L.nodes)
+                rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
+                                 for t, vals in zip(L.table.times, L.table.values))
+                load_lines.append(f"NodalLoad\t{len(load_lines) + 1}\tNodeSet\t{ns}\tCS\t{L.cs + 1}"
+                                  f"\tNTimes\t{len(L.table.times)}\n{rows}")
+            else:
+                rows = "\n".join(f"{_r(float(t))}\t{_r(float(v[0]))}"
+                                 for t, v in zip(L.table.times, L.table.values))
+                load_lines.append(("ShellLoad", L, rows))
+        for D in self.displacements:
+            ns = new_set(D.nodes)
+            rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
+                             for t, vals in zip(D.table.times, D.table.values))
+            disp_lines.append(f"NodalDisplacement\t{len(disp_lines) + 1}\tNodeSet\t{ns}\tCS\t{D.cs + 1}"
+                              f"\tNTimes\t{len(D.table.times)}\n{rows}")
+        if sets:
+            o.append(f"NodeSets\t{len(sets)}")
+            for i, nodes in enumerate(sets):
+                o.append(f"NodeSet\t{i + 1}\tNodes\t{len(nodes)}\tList\t" +
+                         "\t".join(str(n + 1) for n in nodes))
+        if load_lines:
+            o.append(f"Loads\t{len(load_lines)}")
+            o.extend(x for x in load_lines if isinstance(x, str))
+        if disp_lines:
+            o.append(f"Displacements\t{len(disp_lines)}")
+            o.extend(disp_lines)
+        if cons_lines:
+            o.append(f"Constraints\t{len(cons_lines)}")
+            o.extend(cons_lines)
+        c = self.criteria
+        o.append("ConvergenceCriteria\n"
+                 f"ForceTolerance\t{_r(c['force_tol'])}\nMomentTolerance\t{_r(c['moment_tol'])}\n"
+                 f"ForceMinimumReference\t{_r(c['force_min'])}\nMomentMinimumReference\t{_r(c['moment_min'])}\n"
+                 f"ConstraintMinimumReference\t{_r(c['constraint_min'])}\n"
+                 f"DisplacementTolerance\t{_r(c['disp_tol'])}\nRotationTolerance\t{_r(c['rot_tol'])}\n"
+                 f"LagrangeTolerance\t{_r(c['lag_tol'])}\n"
+                 f"DisplacementMinimumReference\t{_r(c['disp_min'])}\n"
+                 f"RotationMinimumReference\t{_r(c['rot_min'])}\n"
+                 f"LagrangeMinimumReference\t{_r(c['lag_min'])}\n"
+                 f"DivergenceReference\t{_r(c['divergence_ref'])}")
+        o.append("SolverOptions\nProcessors\t1\tLinSys\tDirect")
+        return "\n".join(o) + "\n"
+
+
+class DescHandle:
+    """Owns the numpy buffers behind one ``gf_model_desc``."""
+
+    def __init__(self, s: Structure):
+        self.keep = []
+
+        def d(a):
+            a = _d(a)
+            self.keep.append(a)
+            return a
+
+        def i(a):
+            a = _i(a)
+            self.keep.append(a)
+            return a
+
+        nodes = d(np.asarray(s.nodes, dtype=np.float64).reshape(-1, 3))
+        mats = d(np.asarray(s.materials, dtype=np.float64).reshape(-1, 3))
+        secs = d(np.asarray(s.sections, dtype=np.float64).reshape(-1, 6))
+        ssec = d(np.asarray(s.shell_sections, dtype=np.float64).reshape(-1, 1))
+        cs = d(np.asarray(s.cs, dtype=np.float64).reshape(-1, 6))
+        beams = i(np.asarray(s.beams, dtype=np.int32).reshape(-1, 6))
+        shells = i(np.asarray(s.shells, dtype=np.int32).reshape(-1, 9))
+        cons = i(s.constraints) if s.constraints is not None else None
+        loads = (gf_load * max(1, len(s.loads)))()
+        for k, L in enumerate(s.loads):
+            items = i(np.asarray(L.nodes if isinstance(L, NodalLoad) else L.shells))
+            tt = d(L.table.times)
+            tv = d(np.asarray(L.table.values, dtype=np.float64).reshape(len(tt), -1))
+            loads[k].type = GF_LOAD_NODAL if isinstance(L, NodalLoad) else GF_LOAD_SHELL_PRESSURE
+            loads[k].n_items = len(items)
+            loads[k].items = _ptr(items, _ip)
+            loads[k].cs = L.cs if isinstance(L, NodalLoad) else 0
+            loads[k].area_update = getattr(L, "area_update", 0)
+            loads[k].table = gf_table(len(tt), tv.shape[1], _ptr(tt, _dp), _ptr(tv, _dp))
+        disps = (gf_displacement * max(1, len(s.displacements)))()
+        for k, D in enumerate(s.displacements):
+            nd = i(np.asarray(D.nodes))
+            tt = d(D.table.times)
+            tv = d(np.asarray(D.table.values, dtype=np.float64).reshape(len(tt), -1))
+            disps[k].n_nodes = len(nd)
+            disps[k].nodes = _ptr(nd, _ip)
+            disps[k].cs = D.cs
+            disps[k].table = gf_table(len(tt), tv.shape[1], _ptr(tt, _dp), _ptr(tv, _dp))
+        self.keep += [loads, disps]
+        so = s.solution
+        sol = gf_solution(so.type, so.start_time, so.end_time, so.time_step, so.max_time_step,
+                          so.min_time_step, so.max_it, so.min_it, so.conv_increase, so.inc_factor,
+                          so.beta, so.gamma, so.rayleigh_alpha, so.rayleigh_beta, so.update_rayleigh)
+        crit = gf_criteria(**{k: float(v) for k, v in s.criteria.items()})
+        self.desc = gf_model_desc(
+            len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
+            len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
+            len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), loads,
+            len(s.displacements), disps, sol, crit)
+
+    @property
+    def ref(self):
+        return C.byref(self.desc)

@@ -1,0 +1,56 @@
+/*
+ * CPU oracle for the implicit Beam_1 / Shell_1 path.
+ *
+ * TEST INFRASTRUCTURE.  This library restates the reference's algorithm in
+ * plain C so that the CUDA library can be checked against it and so that the
+ * reference's CPU path can be timed on the GPU host, where the reference
+ * itself is not available.  Only the test suite, the smoke check and the
+ * CPU legs of bench.py load it; the product path never does.
+ *
+ * Parity is pinned: tests compare this oracle with the reference's own
+ * sources compiled by oracle/build_ref.py (where the reference tree exists)
+ * and with the golden fixtures generated from that build
+ * (tests/golden/make_golden.py).
+ */
+#ifndef GIRAFFE_ORACLE_H
+#define GIRAFFE_ORACLE_H
+#include "../include/giraffe_model.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Optional per-converged-step record.  nodes receives, per record and node,
+ * copy_coordinates (translation + accumulated Rodrigues vector) followed by
+ * the nodal rotation tensor Q (row-major): 15 doubles.  gp_Q receives, per
+ * record, beam element and Gauss point, the Gauss point's Q_i (row-major). */
+typedef struct oracle_record {
+  int cap;
+  int n;
+  double* time;
+  int* iterations;
+  double* nodes;
+  double* gp_Q;
+} oracle_record;
+
+/* Runs the structure's solution step.  final_nodes (n_nodes x 15, optional)
+ * receives the final nodal state; stats (4 ints, optional) receives converged
+ * steps, Newton iterations, bisections and the aborted flag.  Returns 0 when
+ * the step finished, 1 when it aborted, -1 for an unsupported model. */
+int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats);
+
+/* Independent structures solved concurrently on `threads` host threads.
+ * Returns the number of structures that did not finish. */
+int oracle_solve_batch(int n, const gf_model_desc* models, double** final_nodes, int* stats,
+                       int threads);
+
+/* One Beam_1 element: PreCalc from nodal coordinates (3x3), material
+ * (E, nu, rho), section (A, I11, I22, I12, It, I33) and CS (E1, E3); n_hist
+ * committed increments (each 18 values, nodes x 6) build the Gauss-point
+ * history; then Mount at disp18.  K: 18x18 column-major, f: 18. */
+int oracle_beam_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
+                        int n_hist, const double* hist_disp, const double* disp18, double* K, double* f);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

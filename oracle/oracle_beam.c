@@ -1,0 +1,265 @@
+/*
+ * Beam_1 element, CPU restatement.  TEST INFRASTRUCTURE (oracle): the
+ * checker for the CUDA element kernels and part of the timed CPU baseline.
+ *
+ * Follows reference src/Beam_1.cpp: PreCalc 501-692 (constitutive matrix,
+ * transformation, Gauss points, shape functions), Mount 695-835 (incremental
+ * Rodrigues kinematics, constitutive and geometric stiffness, internal
+ * force), TransformMatrix 1385-1427, SaveLagrange 1494-1506.  The products
+ * DeltaN^T M DeltaN are expanded per 3x3 block instead of through dense
+ * 9x18 matrices; the arithmetic is the same up to rounding order.
+ */
+#include "oracle_beam.h"
+
+#include <string.h>
+
+/* reference src/Beam_1.cpp:501-692 (Hooke material, non-special section) */
+void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec,
+                         const double* cs, ob_const* c, ob_hist* h) {
+  double E = mat[0], nu = mat[1], rho = mat[2];
+  double G = E / (2 * (1 + nu));
+  double sf = 1.0;
+  double A = sec[0], I1 = sec[1], I2 = sec[2], I12 = sec[3], It = sec[4], I33 = sec[5];
+  memset(c, 0, sizeof(*c));
+  c->D[0 * 6 + 0] = sf * G * A;
+  c->D[1 * 6 + 1] = sf * G * A;
+  c->D[2 * 6 + 2] = E * A;
+  c->D[3 * 6 + 3] = E * I1;
+  c->D[4 * 6 + 4] = E * I2;
+  c->D[3 * 6 + 4] = E * I12;
+  c->D[4 * 6 + 3] = E * I12;
+  c->D[5 * 6 + 5] = G * It;
+  c->Mr = rho * A;
+  c->Jr[0] = rho * I1;
+  c->Jr[4] = rho * I2;
+  c->Jr[8] = rho * I33;
+  c->Jr[1] = c->Jr[3] = rho * I12;
+  cs_matrix(c->T3, cs);
+  double e3[3] = {x2[0] - x0[0], x2[1] - x0[1], x2[2] - x0[2]};
+  double len = sqrt(e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2]);
+  double inv = 1.0 / v3_norm(e3);
+  for (int k = 0; k < 3; ++k) e3[k] = inv * e3[k];
+  m3_vec(c->e3r, c->T3, e3);
+  /* no pre-tension: du0 = 0, dz_i = e3 (reference src/Beam_1.cpp:616-621) */
+  c->jac = len / 2.0;
+  for (int g = 0; g < 2; ++g) {
+    double xi = g == 0 ? -0.577350269189626 : +0.577350269189626;
+    c->N[g][0] = 0.5 * xi * (xi - 1.0);
+    c->N[g][1] = 1.0 - xi * xi;
+    c->N[g][2] = 0.5 * xi * (1.0 + xi);
+    c->dN[g][0] = (1.0 / c->jac) * (xi - 0.5);
+    c->dN[g][1] = (1.0 / c->jac) * (-2.0 * xi);
+    c->dN[g][2] = (1.0 / c->jac) * (0.5 + xi);
+  }
+  if (h) {
+    memset(h, 0, sizeof(*h));
+    for (int g = 0; g < 2; ++g) {
+      m3_eye(h->Q[g]);
+      h->dz[g][2] = 1.0;
+    }
+  }
+}
+
+/* Gauss-point kinematics shared by Mount and SaveLagrange
+ * (reference src/Beam_1.cpp:700-786). */
+typedef struct {
+  double alpha[3], dalpha[3], u[3], du[3];
+  double an, g;
+  double A[9], Qd[9], Xi[9], dXi[9], dz[3], dZ[9];
+  double Qt[9]; /* (Q_delta Q_i)^T */
+  double eta[3], kappa[3];
+} gp_kin;
+
+static void beam_gp_kinematics(const ob_const* c, const ob_hist* h, const double* d, int g, gp_kin* k) {
+  double a[3] = {0, 0, 0}, da[3] = {0, 0, 0}, u[3] = {0, 0, 0}, du[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i)
+    for (int n = 0; n < 3; ++n) {
+      const double* dn = d + 6 * n;
+      a[i] += dn[3 + i] * c->N[g][n];
+      da[i] += dn[3 + i] * c->dN[g][n];
+      u[i] += dn[i] * c->N[g][n];
+      du[i] += dn[i] * c->dN[g][n];
+    }
+  m3_vec(k->alpha, c->T3, a);
+  m3_vec(k->dalpha, c->T3, da);
+  m3_vec(k->u, c->T3, u);
+  m3_vec(k->du, c->T3, du);
+  k->an = v3_norm(k->alpha);
+  m3_skew(k->A, k->alpha);
+  k->g = 4.0 / (4.0 + k->an * k->an);
+  double A2[9];
+  m3_mul(A2, k->A, k->A);
+  for (int q = 0; q < 9; ++q) {
+    k->Qd[q] = k->g * (k->A[q] + 0.5 * A2[q]);
+    k->Xi[q] = k->g * 0.5 * k->A[q];
+  }
+  k->Qd[0] += 1.0; k->Qd[4] += 1.0; k->Qd[8] += 1.0;
+  k->Xi[0] += k->g; k->Xi[4] += k->g; k->Xi[8] += k->g;
+  double dA[9];
+  m3_skew(dA, k->dalpha);
+  double ad = v3_dot(k->alpha, k->dalpha);
+  for (int q = 0; q < 9; ++q) k->dXi[q] = -0.5 * k->g * (ad * k->Xi[q] - dA[q]);
+  for (int i = 0; i < 3; ++i) k->dz[i] = k->du[i] + h->dz[g][i];
+  m3_skew(k->dZ, k->dz);
+  double Q[9];
+  m3_mul(Q, k->Qd, h->Q[g]);
+  m3_transpose(k->Qt, Q);
+  m3_vec(k->eta, k->Qt, k->dz);
+  for (int i = 0; i < 3; ++i) k->eta[i] -= c->e3r[i];
+  double t[3];
+  m3_tvec(t, k->Xi, k->dalpha);
+  m3_tvec(k->kappa, h->Q[g], t);
+  for (int i = 0; i < 3; ++i) k->kappa[i] += h->kap[g][i];
+}
+
+/* reference src/Beam_1.cpp:695-835.  d is [3][6] nodal increments (global);
+ * K is 18x18 column-major, f is 18; both are overwritten. */
+void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
+                       double* strain_energy) {
+  double Kl[18 * 18], fl[18];
+  memset(Kl, 0, sizeof(Kl));
+  memset(fl, 0, sizeof(fl));
+  double se = 0.0;
+  for (int g = 0; g < 2; ++g) {
+    gp_kin k;
+    beam_gp_kinematics(c, h, d, g, &k);
+    /* B = B1 B2 (6x9): [[Qt, 0, Qt dZ Xi], [0, Qt Xi, Qt dXi]] */
+    double B[6][9];
+    memset(B, 0, sizeof(B));
+    double t1[9], QdZXi[9], QXi[9], QdXi[9];
+    m3_mul(t1, k.dZ, k.Xi);
+    m3_mul(QdZXi, k.Qt, t1);
+    m3_mul(QXi, k.Qt, k.Xi);
+    m3_mul(QdXi, k.Qt, k.dXi);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        B[i][j] = k.Qt[i * 3 + j];
+        B[i][6 + j] = QdZXi[i * 3 + j];
+        B[3 + i][3 + j] = QXi[i * 3 + j];
+        B[3 + i][6 + j] = QdXi[i * 3 + j];
+      }
+    /* sigma = D eps */
+    double eps[6] = {k.eta[0], k.eta[1], k.eta[2], k.kappa[0], k.kappa[1], k.kappa[2]}, sig[6];
+    for (int i = 0; i < 6; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < 6; ++j) s += c->D[i * 6 + j] * eps[j];
+      sig[i] = s;
+    }
+    /* M = B^T D B + G (9x9, row-major) */
+    double DB[6][9], M[81];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 9; ++j) {
+        double s = 0.0;
+        for (int p = 0; p < 6; ++p) s += c->D[i * 6 + p] * B[p][j];
+        DB[i][j] = s;
+      }
+    for (int i = 0; i < 9; ++i)
+      for (int j = 0; j < 9; ++j) {
+        double s = 0.0;
+        for (int p = 0; p < 6; ++p) s += B[p][i] * DB[p][j];
+        M[i * 9 + j] = s;
+      }
+    /* n = Q n_r, m = Q m_r with Q = Qt^T */
+    double n[3], m[3];
+    m3_tvec(n, k.Qt, sig);
+    m3_tvec(m, k.Qt, sig + 3);
+    double dZn[3], V1[9], V2[9], dV[9], Sn[9], Sm[9];
+    m3_vec(dZn, k.dZ, n);
+    op_V(V1, k.alpha, dZn, k.an);
+    op_V(V2, k.alpha, m, k.an);
+    op_dV(dV, k.alpha, k.dalpha, m, k.an);
+    m3_skew(Sn, n);
+    m3_skew(Sm, m);
+    double Gua[9], Gau[9], Gaa[9], Gda[9], tmp[9], tmp2[9];
+    m3_mul(Gua, Sn, k.Xi);
+    for (int q = 0; q < 9; ++q) Gua[q] = -Gua[q];
+    m3_tmul(Gau, k.Xi, Sn);
+    m3_mul(tmp, k.dZ, Sn);
+    m3_mul(tmp2, tmp, k.Xi);
+    m3_tmul(Gaa, k.Xi, tmp2);
+    m3_mul(tmp, Sm, k.Xi);
+    m3_tmul(tmp2, k.dXi, tmp);
+    for (int q = 0; q < 9; ++q) Gaa[q] = Gaa[q] - V1[q] + dV[q] - tmp2[q];
+    m3_tmul(tmp2, k.Xi, tmp);
+    for (int q = 0; q < 9; ++q) Gda[q] = V2[q] - tmp2[q];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        M[i * 9 + 6 + j] += Gua[i * 3 + j];
+        M[(6 + i) * 9 + j] += Gau[i * 3 + j];
+        M[(6 + i) * 9 + 6 + j] += Gaa[i * 3 + j];
+        M[(3 + i) * 9 + 6 + j] += Gda[i * 3 + j];
+        M[(6 + i) * 9 + 3 + j] += V2[i * 3 + j];
+      }
+    /* K += wJ DeltaN^T M DeltaN; DeltaN maps node I's (u, alpha) to
+     * (u', alpha', alpha) = (dN_I u, dN_I alpha, N_I alpha) */
+    double wJ = 1.0 * c->jac;
+    const double* N = c->N[g];
+    const double* dN = c->dN[g];
+    for (int I = 0; I < 3; ++I)
+      for (int J = 0; J < 3; ++J)
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) {
+            double m00 = M[a * 9 + b], m01 = M[a * 9 + 3 + b], m02 = M[a * 9 + 6 + b];
+            double m10 = M[(3 + a) * 9 + b], m11 = M[(3 + a) * 9 + 3 + b], m12 = M[(3 + a) * 9 + 6 + b];
+            double m20 = M[(6 + a) * 9 + b], m21 = M[(6 + a) * 9 + 3 + b], m22 = M[(6 + a) * 9 + 6 + b];
+            double uu = dN[I] * dN[J] * m00;
+            double ua = dN[I] * (dN[J] * m01 + N[J] * m02);
+            double au = (dN[I] * m10 + N[I] * m20) * dN[J];
+            double aa = dN[I] * dN[J] * m11 + dN[I] * N[J] * m12 + N[I] * dN[J] * m21 + N[I] * N[J] * m22;
+            int r = 6 * I + a, s = 6 * J + b;
+            Kl[r + 18 * s] += wJ * uu;
+            Kl[r + 18 * (s + 3)] += wJ * ua;
+            Kl[(r + 3) + 18 * s] += wJ * au;
+            Kl[(r + 3) + 18 * (s + 3)] += wJ * aa;
+          }
+    /* f += wJ DeltaN^T B^T sigma; B^T sigma = [n; Xi^T m; Xi^T dZ^T n + dXi^T m] */
+    double s0[3] = {n[0], n[1], n[2]}, s1[3], s2[3], a1[3], a2[3];
+    m3_tvec(s1, k.Xi, m);
+    m3_tvec(a1, k.dZ, n);
+    m3_tvec(a2, k.Xi, a1);
+    m3_tvec(a1, k.dXi, m);
+    for (int i = 0; i < 3; ++i) s2[i] = a2[i] + a1[i];
+    for (int I = 0; I < 3; ++I)
+      for (int i = 0; i < 3; ++i) {
+        fl[6 * I + i] += wJ * dN[I] * s0[i];
+        fl[6 * I + 3 + i] += wJ * (dN[I] * s1[i] + N[I] * s2[i]);
+      }
+    double e = 0.0;
+    for (int i = 0; i < 6; ++i) e += sig[i] * eps[i];
+    se += 0.5 * wJ * e;
+  }
+  /* global frame: K <- T^T K T, f <- T^T f (T = blockdiag(T3), reference
+   * src/Beam_1.cpp:833-834) */
+  const double* T = c->T3;
+  for (int bi = 0; bi < 6; ++bi)
+    for (int bj = 0; bj < 6; ++bj) {
+      double blk[9], t2[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) blk[i * 3 + j] = Kl[(3 * bi + i) + 18 * (3 * bj + j)];
+      m3_mul(t2, blk, T);
+      m3_tmul(blk, T, t2);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) K[(3 * bi + i) + 18 * (3 * bj + j)] = blk[i * 3 + j];
+    }
+  for (int bi = 0; bi < 6; ++bi) m3_tvec(f + 3 * bi, T, fl + 3 * bi);
+  if (strain_energy) *strain_energy = se;
+}
+
+/* reference src/Beam_1.cpp:1494-1506 */
+void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d) {
+  for (int g = 0; g < 2; ++g) {
+    gp_kin k;
+    beam_gp_kinematics(c, h, d, g, &k);
+    double Q[9];
+    m3_mul(Q, k.Qd, h->Q[g]);
+    m3_copy(h->Q[g], Q);
+    for (int i = 0; i < 3; ++i) {
+      h->u[g][i] += k.u[i];
+      h->kap[g][i] = k.kappa[i];
+      h->dz[g][i] = k.dz[i];
+    }
+    double an[3];
+    rodrigues_compose(an, k.alpha, h->alpha[g]);
+    memcpy(h->alpha[g], an, sizeof(an));
+  }
+}

@@ -1,0 +1,32 @@
+/* Beam_1 element restatement (oracle; test infrastructure). */
+#ifndef GIRAFFE_ORACLE_BEAM_H
+#define GIRAFFE_ORACLE_BEAM_H
+#include "oracle_common.h"
+
+/* Per-element constants from Beam_1::PreCalc. */
+typedef struct ob_const {
+  double T3[9];    /* transform3: rows E1, E2, E3 of the element CS */
+  double D[36];    /* 6x6 constitutive matrix, row-major */
+  double e3r[3];   /* element axis in the local frame */
+  double jac;      /* L/2 */
+  double N[2][3];  /* shape functions at the two Gauss points */
+  double dN[2][3]; /* their derivatives (divided by the jacobian) */
+  double Mr;       /* mass per unit length */
+  double Jr[9];    /* rotary inertia per unit length */
+} ob_const;
+
+/* Gauss-point history (LagrangeSave, reference src/LagrangeSave.h:11-17). */
+typedef struct ob_hist {
+  double Q[2][9];
+  double dz[2][3];
+  double kap[2][3];
+  double u[2][3];
+  double alpha[2][3];
+} ob_hist;
+
+void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec,
+                         const double* cs, ob_const* c, ob_hist* h);
+void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
+                       double* strain_energy);
+void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);
+#endif

@@ -1,0 +1,498 @@
+/*
+ * Static solution of one structure, CPU restatement.  TEST INFRASTRUCTURE
+ * (oracle): the checker for the CUDA solver and the timed CPU baseline.
+ *
+ * Follows, for Beam_1 structures with nodal loads, constraints and prescribed
+ * displacements:
+ *   reference src/Static.cpp:140-311        load-step and Newton loops
+ *   reference src/Solution.cpp:40-118       free/fixed DOF numbering
+ *   reference src/Solution.cpp:121-224      DOF activation
+ *   reference src/Solution.cpp:390-423      UpdateDisps
+ *   reference src/Solution.cpp:426-575      Save/RestoreConfiguration
+ *   reference src/Solution.cpp:798-849      Zeros, Clear
+ *   reference src/ConvergenceCriteria.cpp:187-618
+ *   reference src/NodalLoad.cpp:230-401     (UpdateforSolutionStep, Mount)
+ *   reference src/NodalDisplacement.cpp:158-208, 327-410 (EulerAngles)
+ *   reference src/Node.cpp:325-370          SaveConfiguration
+ * The linear solve (PARDISO in the reference, src/SparseMatrix.cpp:74-166)
+ * is an FP64 banded LU with partial pivoting on the same K_AA.
+ *
+ * Note on reference src/Static.cpp:214-215: global_X_B is cleared by
+ * Clear() (src/Solution.cpp:841) at the top of every Newton iteration, after
+ * MountDisplacements filled it, so the K_AB X_B correction multiplies a zero
+ * vector; prescribed increments act through the nodal displacements alone.
+ * The oracle therefore omits that product.
+ */
+#include "giraffe_oracle.h"
+
+#include <float.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "band_lu.h"
+#include "oracle_beam.h"
+
+typedef struct {
+  const gf_model_desc* m;
+  int nn, nb;
+  int* GL;       /* [nn][6]: >0 free (1-based), <0 fixed, 0 inactive */
+  int* active;   /* [nn][6] */
+  int* cons;     /* [nn][6] */
+  int n_free, n_fixed, kl, ku, ldab;
+  double* disp;  /* increments in the step (Node::displacements) */
+  double* copy;  /* Node::copy_coordinates */
+  double* Qn;    /* Node::Q */
+  double* vel; double* accel; double* copy_vel; double* copy_accel;
+  ob_const* bc;
+  ob_hist* bh;
+  double* ab; int* ipiv; double* PA;
+  /* criteria state */
+  double force_crit, moment_crit, disp_crit, rot_crit;
+  int n_conv_evaluated;
+  int diverged;
+  /* loads: per nodal load, force/moment multipliers */
+  double (*mult)[6];
+  double last_converged_time, current_time_step;
+} ost;
+
+static void ost_free(ost* s) {
+  free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
+  free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
+  free(s->bc); free(s->bh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
+}
+
+static int ost_init(ost* s, const gf_model_desc* m) {
+  memset(s, 0, sizeof(*s));
+  s->m = m;
+  s->nn = m->n_nodes;
+  s->nb = m->n_beams;
+  int nn = s->nn;
+  s->GL = calloc((size_t)nn * 6, sizeof(int));
+  s->active = calloc((size_t)nn * 6, sizeof(int));
+  s->cons = calloc((size_t)nn * 6, sizeof(int));
+  s->disp = calloc((size_t)nn * 6, sizeof(double));
+  s->copy = calloc((size_t)nn * 6, sizeof(double));
+  s->Qn = calloc((size_t)nn * 9, sizeof(double));
+  s->vel = calloc((size_t)nn * 6, sizeof(double));
+  s->accel = calloc((size_t)nn * 6, sizeof(double));
+  s->copy_vel = calloc((size_t)nn * 6, sizeof(double));
+  s->copy_accel = calloc((size_t)nn * 6, sizeof(double));
+  s->bc = calloc((size_t)(s->nb ? s->nb : 1), sizeof(ob_const));
+  s->bh = calloc((size_t)(s->nb ? s->nb : 1), sizeof(ob_hist));
+  s->mult = calloc((size_t)(m->n_loads ? m->n_loads : 1), sizeof(*s->mult));
+  /* Node::Read sets copy_coordinates to the reference position
+   * (reference src/Node.cpp:160-175); rotations start at zero */
+  for (int i = 0; i < nn; ++i) {
+    m3_eye(s->Qn + 9 * i);
+    for (int k = 0; k < 3; ++k) s->copy[6 * i + k] = m->node_xyz[3 * i + k];
+  }
+  /* Beam_1::PreCalc */
+  for (int e = 0; e < s->nb; ++e) {
+    const int* b = m->beams + 6 * e;
+    oracle_beam_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->materials + 3 * b[3],
+                        m->sections + 6 * b[4], m->cs + 6 * b[5], s->bc + e, s->bh + e);
+  }
+  /* DOFsActive: Beam_1 activates all six DOFs of its nodes */
+  for (int e = 0; e < s->nb; ++e)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 6; ++k) s->active[6 * m->beams[6 * e + j] + k] = 1;
+  if (m->constraints)
+    for (int i = 0; i < nn * 6; ++i) s->cons[i] = m->constraints[i] ? 1 : 0;
+  /* SetGlobalDOFs */
+  int fr = 0, fx = 0;
+  for (int i = 0; i < nn; ++i)
+    for (int k = 0; k < 6; ++k) {
+      if (s->cons[6 * i + k] == 0 && s->active[6 * i + k] == 1) s->GL[6 * i + k] = ++fr;
+      if (s->cons[6 * i + k] == 1 && s->active[6 * i + k] == 1) s->GL[6 * i + k] = -(++fx);
+    }
+  s->n_free = fr;
+  s->n_fixed = fx;
+  /* bandwidth of K_AA under this numbering */
+  int kl = 0;
+  for (int e = 0; e < s->nb; ++e)
+    for (int a = 0; a < 18; ++a)
+      for (int b = 0; b < 18; ++b) {
+        int ga = s->GL[6 * m->beams[6 * e + a / 6] + a % 6], gb = s->GL[6 * m->beams[6 * e + b / 6] + b % 6];
+        if (ga > 0 && gb > 0 && ga - gb > kl) kl = ga - gb;
+      }
+  for (int l = 0; l < m->n_loads; ++l)
+    if (m->loads[l].type == GF_LOAD_NODAL)
+      for (int q = 0; q < m->loads[l].n_items; ++q) {
+        int node = m->loads[l].items[q];
+        for (int a = 3; a < 6; ++a)
+          for (int b = 3; b < 6; ++b) {
+            int ga = s->GL[6 * node + a], gb = s->GL[6 * node + b];
+            if (ga > 0 && gb > 0 && ga - gb > kl) kl = ga - gb;
+          }
+      }
+  s->kl = s->ku = kl;
+  s->ldab = 2 * kl + kl + 1;
+  s->ab = malloc(sizeof(double) * (size_t)s->ldab * (size_t)(fr ? fr : 1));
+  s->ipiv = malloc(sizeof(int) * (size_t)(fr ? fr : 1));
+  s->PA = malloc(sizeof(double) * (size_t)(fr ? fr : 1));
+  /* NodalLoad::UpdateforSolutionStep */
+  for (int l = 0; l < m->n_loads; ++l) {
+    const gf_load* L = m->loads + l;
+    if (L->type != GF_LOAD_NODAL) continue;
+    int cnt[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < L->n_items; ++q)
+      for (int k = 0; k < 6; ++k)
+        if (s->active[6 * L->items[q] + k] != 0) cnt[k]++;
+    for (int k = 0; k < 6; ++k) s->mult[l][k] = 1.0 / cnt[k];
+  }
+  return 0;
+}
+
+/* ---- global assembly ---- */
+static void add_K(ost* s, int ga, int gb, double v) {
+  if (ga > 0 && gb > 0) GB_AT(s->ab, s->ldab, s->kl, s->ku, ga - 1, gb - 1) += v;
+}
+
+static void assemble(ost* s) {
+  const gf_model_desc* m = s->m;
+  memset(s->ab, 0, sizeof(double) * (size_t)s->ldab * (size_t)(s->n_free ? s->n_free : 1));
+  memset(s->PA, 0, sizeof(double) * (size_t)(s->n_free ? s->n_free : 1));
+  double K[324], f[18], d[18];
+  for (int e = 0; e < s->nb; ++e) {
+    const int* b = m->beams + 6 * e;
+    for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
+    oracle_beam_mount(s->bc + e, s->bh + e, d, K, f, NULL);
+    int g[18];
+    for (int a = 0; a < 18; ++a) g[a] = s->GL[6 * b[a / 6] + a % 6];
+    for (int a = 0; a < 18; ++a) {
+      if (g[a] > 0) s->PA[g[a] - 1] += f[a];
+      for (int c = 0; c < 18; ++c) add_K(s, g[a], g[c], K[a + 18 * c]);
+    }
+  }
+  /* NodalLoad::Mount: P_A += -f, -Xi^T m pseudo-moments, K_AA += -V(alpha, Xi^T m) */
+  double time = s->last_converged_time + s->current_time_step;
+  for (int l = 0; l < m->n_loads; ++l) {
+    const gf_load* L = m->loads + l;
+    if (L->type != GF_LOAD_NODAL) continue;
+    double CQ[9];
+    cs_matrix(CQ, m->cs + 6 * L->cs);
+    for (int q = 0; q < L->n_items; ++q) {
+      int node = L->items[q];
+      double fl[3], ml[3], fv[3], mv[3];
+      for (int i = 0; i < 3; ++i) {
+        fl[i] = s->mult[l][i] * table_at(&L->table, time, i);
+        ml[i] = s->mult[l][3 + i] * table_at(&L->table, time, i + 3);
+      }
+      m3_tvec(fv, CQ, fl);
+      m3_tvec(mv, CQ, ml);
+      const double* al = s->disp + 6 * node + 3;
+      double an = v3_norm(al), A[9], Xi[9];
+      double gg = 4.0 / (4.0 + an * an);
+      m3_skew(A, al);
+      for (int k = 0; k < 9; ++k) Xi[k] = gg * 0.5 * A[k];
+      Xi[0] += gg; Xi[4] += gg; Xi[8] += gg;
+      double mm[3], V[9];
+      m3_tvec(mm, Xi, mv);
+      op_V(V, al, mm, an);
+      for (int i = 0; i < 3; ++i) {
+        int gi = s->GL[6 * node + i];
+        if (s->active[6 * node + i] == 1 && gi > 0) s->PA[gi - 1] += -1.0 * fv[i];
+      }
+      for (int i = 0; i < 3; ++i) {
+        int gi = s->GL[6 * node + 3 + i];
+        if (s->active[6 * node + 3 + i] == 1 && gi > 0) s->PA[gi - 1] += -1.0 * mm[i];
+        for (int j = 0; j < 3; ++j)
+          if (s->active[6 * node + 3 + j] == 1) add_K(s, gi, s->GL[6 * node + 3 + j], -1.0 * V[i * 3 + j]);
+      }
+    }
+  }
+  for (int i = 0; i < s->n_free; ++i) s->PA[i] = -1.0 * s->PA[i];
+}
+
+/* ---- convergence criteria (reference src/ConvergenceCriteria.cpp) ---- */
+static int nan_or_huge(double v) { return !(v == v) || v >= 1e300 || v <= -1e300; }
+
+static void establish_residual_criteria(ost* s) {
+  const gf_criteria* c = &s->m->criteria;
+  double mf = 0, mm = 0;
+  for (int i = 0; i < s->nn; ++i)
+    for (int k = 0; k < 6; ++k) {
+      int g = s->GL[6 * i + k];
+      if (g > 0) {
+        double v = fabs(s->PA[g - 1]);
+        if (k < 3 && v > mf) mf = v;
+        if (k >= 3 && v > mm) mm = v;
+      }
+    }
+  double pf = s->force_crit, pm = s->moment_crit;
+  s->force_crit = mf * c->force_tol > c->force_min * c->force_tol ? mf * c->force_tol : c->force_min * c->force_tol;
+  s->moment_crit = mm * c->moment_tol > c->moment_min * c->moment_tol ? mm * c->moment_tol : c->moment_min * c->moment_tol;
+  s->force_crit = (s->n_conv_evaluated * pf + s->force_crit) / (s->n_conv_evaluated + 1);
+  s->moment_crit = (s->n_conv_evaluated * pm + s->moment_crit) / (s->n_conv_evaluated + 1);
+  s->n_conv_evaluated++;
+}
+
+static int check_residual(ost* s) {
+  const gf_criteria* c = &s->m->criteria;
+  double mf = 0, mm = 0;
+  int has_f = 0, has_m = 0;
+  for (int i = 0; i < s->nn; ++i)
+    for (int k = 0; k < 6; ++k) {
+      int g = s->GL[6 * i + k];
+      if (g > 0) {
+        double v = fabs(s->PA[g - 1]);
+        if (nan_or_huge(v)) s->diverged = 1;
+        if (k < 3) { has_f = 1; if (v > mf) mf = v; }
+        else { has_m = 1; if (v > mm) mm = v; }
+      }
+    }
+  if (mf > c->divergence_ref || mm > c->divergence_ref) { s->diverged = 1; return 0; }
+  int ok = 1;
+  if (has_f && mf > s->force_crit) ok = 0;
+  if (has_m && mm > s->moment_crit) ok = 0;
+  return ok;
+}
+
+static int check_gl(ost* s) {
+  const gf_criteria* c = &s->m->criteria;
+  double mdi = 0, mri = 0, mdv = 0, mrv = 0;
+  int has_d = 0, has_r = 0;
+  for (int i = 0; i < s->nn; ++i)
+    for (int k = 0; k < 6; ++k) {
+      int g = s->GL[6 * i + k];
+      if (g > 0) {
+        double inc = fabs(s->PA[g - 1]);
+        if (nan_or_huge(inc)) s->diverged = 1;
+        double val = fabs(s->disp[6 * i + k]);
+        if (k < 3) { has_d = 1; if (inc > mdi) mdi = inc; if (val > mdv) mdv = val; }
+        else { has_r = 1; if (inc > mri) mri = inc; if (val > mrv) mrv = val; }
+      }
+    }
+  s->disp_crit = mdv * c->disp_tol > c->disp_min * c->disp_tol ? c->disp_tol * mdv : c->disp_min * c->disp_tol;
+  s->rot_crit = mrv * c->rot_tol > c->rot_min * c->rot_tol ? c->rot_tol * mrv : c->rot_min * c->rot_tol;
+  if (s->disp_crit > c->divergence_ref || s->rot_crit > c->divergence_ref) { s->diverged = 1; return 0; }
+  int ok = 1;
+  if (has_d && mdi > s->disp_crit) ok = 0;
+  if (has_r && mri > s->rot_crit) ok = 0;
+  return ok;
+}
+
+/* ---- prescribed displacements (reference src/NodalDisplacement.cpp:158-208) ---- */
+static void euler_angles_Q(double* Q, double phi, double th, double psi) {
+  Q[0] = cos(th) * cos(psi);
+  Q[1] = sin(phi) * sin(th) * cos(psi) - cos(phi) * sin(psi);
+  Q[2] = cos(phi) * sin(th) * cos(psi) + sin(phi) * sin(psi);
+  Q[3] = cos(th) * sin(psi);
+  Q[4] = sin(phi) * sin(th) * sin(psi) + cos(phi) * cos(psi);
+  Q[5] = cos(phi) * sin(th) * sin(psi) - sin(phi) * cos(psi);
+  Q[6] = -sin(th);
+  Q[7] = sin(phi) * cos(th);
+  Q[8] = cos(phi) * cos(th);
+}
+
+static void mount_displacements(ost* s) {
+  const gf_model_desc* m = s->m;
+  double time = s->last_converged_time + s->current_time_step, dt = s->current_time_step;
+  for (int l = 0; l < m->n_displacements; ++l) {
+    const gf_displacement* D = m->displacements + l;
+    double CQ[9];
+    cs_matrix(CQ, m->cs + 6 * D->cs);
+    for (int q = 0; q < D->n_nodes; ++q) {
+      int node = D->nodes[q];
+      double dl[3], dg[3];
+      for (int j = 0; j < 3; ++j) dl[j] = table_at(&D->table, time, j) - table_at(&D->table, time - dt, j);
+      m3_tvec(dg, CQ, dl);
+      for (int j = 0; j < 3; ++j)
+        if (s->cons[6 * node + j] == 1 && s->active[6 * node + j] == 1) {
+          s->disp[6 * node + j] = dg[j];
+          s->vel[6 * node + j] = dg[j] / dt;
+          s->accel[6 * node + j] = (s->vel[6 * node + j] - s->copy_vel[6 * node + j]) / dt;
+        }
+      /* rotations: EulerAngles, reference src/NodalDisplacement.cpp:327-410 */
+      double phi = s->cons[6 * node + 3] == 1 ? table_at(&D->table, time, 3) : 0.0;
+      double th = s->cons[6 * node + 4] == 1 ? table_at(&D->table, time, 4) : 0.0;
+      double psi = s->cons[6 * node + 5] == 1 ? table_at(&D->table, time, 5) : 0.0;
+      double Q[9], t[9], Qd[9];
+      euler_angles_Q(Q, phi, th, psi);
+      m3_mul(t, Q, CQ);
+      m3_tmul(Q, CQ, t);
+      m3_mult(Qd, Q, s->Qn + 9 * node);
+      double tr = Qd[0] + Qd[4] + Qd[8];
+      if (tr > 3.0) tr = 3.0;
+      double ax[3] = {0.5 * (Qd[7] - Qd[5]), 0.5 * (Qd[2] - Qd[6]), 0.5 * (Qd[3] - Qd[1])};
+      double theta = 2.0 * asin(sqrt((3.0 - tr) / 4.0));
+      double eu[3] = {0, 0, 0};
+      if (theta != 0.0)
+        for (int k = 0; k < 3; ++k) eu[k] = (theta / sin(theta)) * ax[k];
+      double alpha = 2.0 * sqrt((3.0 - tr) / (1.0 + tr));
+      double rod[3];
+      for (int k = 0; k < 3; ++k) rod[k] = ((4.0 + alpha * alpha) / 4.0) * ax[k];
+      for (int j = 3; j < 6; ++j)
+        if (s->cons[6 * node + j] == 1 && s->active[6 * node + j] == 1) {
+          s->disp[6 * node + j] = rod[j - 3];
+          s->vel[6 * node + j] = eu[j - 3] / dt;
+          s->accel[6 * node + j] = (s->vel[6 * node + j] - s->copy_vel[6 * node + j]) / dt;
+        }
+    }
+  }
+}
+
+/* ---- commit (reference src/Node.cpp:325-370, src/Beam_1.cpp:1494-1506) ---- */
+static void save_configuration(ost* s) {
+  for (int i = 0; i < s->nn; ++i) {
+    double* c = s->copy + 6 * i;
+    const double* d = s->disp + 6 * i;
+    for (int k = 0; k < 3; ++k) c[k] += d[k];
+    double a3[3];
+    rodrigues_compose(a3, d + 3, c + 3);
+    memcpy(c + 3, a3, sizeof(a3));
+    rodrigues_Q(s->Qn + 9 * i, a3);
+    for (int k = 0; k < 6; ++k) {
+      s->copy_accel[6 * i + k] = s->accel[6 * i + k];
+      s->copy_vel[6 * i + k] = s->vel[6 * i + k];
+    }
+  }
+  double d[18];
+  for (int e = 0; e < s->nb; ++e) {
+    const int* b = s->m->beams + 6 * e;
+    for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
+    oracle_beam_commit(s->bc + e, s->bh + e, d);
+  }
+}
+
+static void record(ost* s, oracle_record* rec, double time, int iterations) {
+  if (!rec || rec->n >= rec->cap) return;
+  int r = rec->n++;
+  if (rec->time) rec->time[r] = time;
+  if (rec->iterations) rec->iterations[r] = iterations;
+  if (rec->nodes) {
+    double* o = rec->nodes + (size_t)r * s->nn * 15;
+    for (int i = 0; i < s->nn; ++i) {
+      memcpy(o + 15 * i, s->copy + 6 * i, 6 * sizeof(double));
+      memcpy(o + 15 * i + 6, s->Qn + 9 * i, 9 * sizeof(double));
+    }
+  }
+  if (rec->gp_Q) {
+    double* o = rec->gp_Q + (size_t)r * s->nb * 18;
+    for (int e = 0; e < s->nb; ++e) memcpy(o + 18 * e, s->bh[e].Q, 18 * sizeof(double));
+  }
+}
+
+static int solve_linear(ost* s) {
+  if (s->n_free == 0) return 0;
+  int info = oracle_gbtrf(s->n_free, s->kl, s->ku, s->ab, s->ldab, s->ipiv);
+  if (info) return 1;
+  oracle_gbtrs(s->n_free, s->kl, s->ku, s->ab, s->ldab, s->ipiv, s->PA);
+  for (int i = 0; i < s->n_free; ++i)
+    if (!(s->PA[i] == s->PA[i])) return 1;
+  return 0;
+}
+
+/* reference src/Static.cpp:140-311 */
+static int static_solve(ost* s, oracle_record* rec, int* stats) {
+  const gf_solution* so = &s->m->solution;
+  int aborted = 0, convergence_counter = 0, converged_number = 0, total_it = 0, bisections = 0;
+  s->n_conv_evaluated = 0;
+  s->last_converged_time = so->start_time;
+  record(s, rec, so->start_time, 0);
+  double time_step = so->time_step, time = s->last_converged_time;
+  s->diverged = 0;
+  for (int i = 0; i < s->nn * 6; ++i) s->copy_vel[i] = s->copy_accel[i] = s->vel[i] = s->accel[i] = 0.0;
+  while ((time < so->end_time || s->diverged) && !aborted) {
+    s->last_converged_time = time;
+    time += time_step;
+    if (time > 0.99999999 * so->end_time) {
+      time = so->end_time;
+      time_step = so->end_time - s->last_converged_time;
+    }
+    s->current_time_step = time_step;
+    int it = 1;
+    memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+    mount_displacements(s);
+    int res_conv = 0, gl_conv = 0;
+    s->diverged = 0;
+    while ((!res_conv || !gl_conv) && !s->diverged && !aborted) {
+      assemble(s);
+      if (it == 1) establish_residual_criteria(s);
+      res_conv = check_residual(s);
+      if (getenv("ORACLE_DEBUG")) {
+        double mf = 0; for (int i = 0; i < s->n_free; ++i) if (fabs(s->PA[i]) > mf) mf = fabs(s->PA[i]);
+        fprintf(stderr, "t=%g it=%d maxres=%.6e crit=%.3e\n", time, it, mf, s->force_crit);
+      }
+      int info_fail = 0;
+      if (!(res_conv && gl_conv)) {
+        info_fail = solve_linear(s);
+        res_conv = 0;
+        for (int i = 0; i < s->nn; ++i)
+          for (int k = 0; k < 6; ++k)
+            if (s->cons[6 * i + k] == 0 && s->active[6 * i + k] == 1)
+              s->disp[6 * i + k] += s->PA[s->GL[6 * i + k] - 1];
+        gl_conv = check_gl(s);
+      }
+      if ((it == so->max_it && !(res_conv && gl_conv)) || info_fail) s->diverged = 1;
+      if (time_step < so->min_time_step && time != so->end_time) aborted = 1;
+      it++;
+      total_it++;
+    }
+    if (!s->diverged) {
+      converged_number++;
+      save_configuration(s);
+      convergence_counter++;
+      if (it <= so->min_it || convergence_counter >= so->conv_increase) {
+        time_step = time_step * so->inc_factor;
+        if (time_step > so->max_time_step) time_step = so->max_time_step;
+        convergence_counter = 0;
+      }
+      if (!aborted) record(s, rec, time, it - 1);
+    } else {
+      memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+      for (int i = 0; i < s->nn * 6; ++i) { s->vel[i] = s->copy_vel[i]; s->accel[i] = s->copy_accel[i]; }
+      time -= time_step;
+      time_step = time_step / 2.0;
+      s->diverged = 0;
+      convergence_counter = 0;
+      bisections++;
+    }
+  }
+  if (stats) {
+    stats[0] = converged_number;
+    stats[1] = total_it;
+    stats[2] = bisections;
+    stats[3] = aborted;
+  }
+  return aborted ? 1 : 0;
+}
+
+static void final_state(ost* s, double* out) {
+  if (!out) return;
+  for (int i = 0; i < s->nn; ++i) {
+    memcpy(out + 15 * i, s->copy + 6 * i, 6 * sizeof(double));
+    memcpy(out + 15 * i + 6, s->Qn + 9 * i, 9 * sizeof(double));
+  }
+}
+
+int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
+  if (m->solution.type != GF_STATIC || m->n_shells) return -1;
+  ost s;
+  ost_init(&s, m);
+  int r = static_solve(&s, rec, stats);
+  final_state(&s, final_nodes);
+  ost_free(&s);
+  return r;
+}
+
+int oracle_solve_batch(int n, const gf_model_desc* models, double** final_nodes, int* stats,
+                       int threads) {
+  int fails = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads > 0 ? threads : 1) reduction(+ : fails)
+  for (int i = 0; i < n; ++i)
+    fails += oracle_solve(models + i, NULL, final_nodes ? final_nodes[i] : NULL, stats ? stats + 4 * i : NULL) != 0;
+  return fails;
+}
+
+/* ---- element-level entry points for known-answer tests ---- */
+int oracle_beam_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
+                        int n_hist, const double* hist_disp, const double* disp18, double* K, double* f) {
+  ob_const c;
+  ob_hist h;
+  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, &c, &h);
+  for (int q = 0; q < n_hist; ++q) oracle_beam_commit(&c, &h, hist_disp + 18 * q);
+  oracle_beam_mount(&c, &h, disp18, K, f, NULL);
+  return 0;
+}
