@@ -1,0 +1,317 @@
+// Beam_1 element on the device: Gauss-point kinematics, internal force and
+// tangent, and the Gauss-point commit.
+//
+// Restates reference src/Beam_1.cpp:695-835 (Mount) and 1494-1506
+// (SaveLagrange).  One thread owns one element; the internal force and all
+// rotation updates are FP64, the tangent is computed in TK (double for the
+// plain path, float for the mixed-precision path).  The 9x9 Gauss-point
+// operator M = B^T D B + G is rotated to the global frame block by block
+// (T3^T M_pq T3) before the DeltaN expansion, which is the same linear map as
+// the reference's T^T (DeltaN^T M DeltaN) T on the 18x18 matrix.
+#pragma once
+#include "gf_math.cuh"
+#include "gf_types.h"
+
+namespace gf {
+
+// Interpolated nodal increments at one Gauss point, local frame.
+struct BeamInterp {
+  V3<double> alpha, dalpha, u, du;
+};
+
+// Gauss-point state used by the force and tangent (local frame).
+struct BeamGP {
+  V3<double> alpha, dalpha, dz;
+  double g;
+  M3<double> Xi, dXi, Qt;  // Qt = (Q_delta Q_i)^T
+  double sig[6];           // retro-rotated stress resultants (n_r, m_r)
+};
+
+// reference src/Beam_1.cpp:700-746
+GF_HD BeamInterp beam_interp(const BeamConst& c, const double* d, int g) {
+  const double* N = c.N[g];
+  const double* dN = c.dN[g];
+  V3<double> a, da, u, du;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = d[3 + i] * N[0] + d[9 + i] * N[1] + d[15 + i] * N[2];
+    da[i] = d[3 + i] * dN[0] + d[9 + i] * dN[1] + d[15 + i] * dN[2];
+    u[i] = d[i] * N[0] + d[6 + i] * N[1] + d[12 + i] * N[2];
+    du[i] = d[i] * dN[0] + d[6 + i] * dN[1] + d[12 + i] * dN[2];
+  }
+  M3<double> T;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T[i] = c.T3[i];
+  BeamInterp r;
+  r.alpha = mv(T, a);
+  r.dalpha = mv(T, da);
+  r.u = mv(T, u);
+  r.du = mv(T, du);
+  return r;
+}
+
+// Q_delta and Xi of the incremental rotation (reference src/Beam_1.cpp:748-753)
+GF_HD void beam_rot(const V3<double>& alpha, double& g, M3<double>& Qd, M3<double>& Xi) {
+  double n2 = dot(alpha, alpha);
+  g = 4.0 / (4.0 + n2);
+  M3<double> A = skew(alpha), A2 = mul(A, A);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    Qd[i] = g * (A[i] + 0.5 * A2[i]);
+    Xi[i] = g * 0.5 * A[i];
+  }
+  Qd[0] += 1.0; Qd[4] += 1.0; Qd[8] += 1.0;
+  Xi[0] += g; Xi[4] += g; Xi[8] += g;
+}
+
+// Constitutive product sigma = D eps with D = diag(D00..D55) + D34 (E I12)
+GF_HD void beam_stress(const BeamConst& c, const double* eps, double* sig) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) sig[i] = c.Dd[i] * eps[i];
+  sig[3] += c.D34 * eps[4];
+  sig[4] += c.D34 * eps[3];
+}
+
+// reference src/Beam_1.cpp:748-788
+GF_HD void beam_kinematics(const BeamConst& c, const BeamHist& h, const BeamInterp& ip, int g, BeamGP& k) {
+  k.alpha = ip.alpha;
+  k.dalpha = ip.dalpha;
+  M3<double> Qd;
+  beam_rot(ip.alpha, k.g, Qd, k.Xi);
+  M3<double> dA = skew(ip.dalpha);
+  double ad = dot(ip.alpha, ip.dalpha);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) k.dXi[i] = -0.5 * k.g * (ad * k.Xi[i] - dA[i]);
+  M3<double> Qi;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Qi[i] = h.Q[g][i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) k.dz[i] = ip.du[i] + h.dz[g][i];
+  k.Qt = transpose(mul(Qd, Qi));
+  V3<double> eta = mv(k.Qt, k.dz);
+  V3<double> t = tmv(k.Xi, ip.dalpha);
+  V3<double> kap = tmv(Qi, t);
+  double eps[6];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    eps[i] = eta[i] - c.e3r[i];
+    eps[3 + i] = kap[i] + h.kap[g][i];
+  }
+  beam_stress(c, eps, k.sig);
+}
+
+// Gauss-point operator M = B^T D B + G (9x9 row-major, local frame) in TK.
+// With B = [[Qt, 0, P], [0, R, S]] (P = Qt dZ Xi, R = Qt Xi, S = Qt dXi) and
+// D = diag(Dt, Dr), the blocks are M00 = Qt^T Dt Qt, M02 = Qt^T Dt P,
+// M11 = R^T Dr R, M12 = R^T Dr S, M22 = P^T Dt P + S^T Dr S, M20 = M02^T,
+// M21 = M12^T, M01 = M10 = 0; G is added on top (reference
+// src/Beam_1.cpp:796-822).
+template <typename TK> GF_HD M3<TK> xtdy(const M3<TK>& X, const M3<TK>& DY) { return tmul(X, DY); }
+template <typename TK> GF_HD M3<TK> diag_rows(const M3<TK>& Y, TK d0, TK d1, TK d2) {
+  M3<TK> r;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r[j] = d0 * Y[j];
+    r[3 + j] = d1 * Y[3 + j];
+    r[6 + j] = d2 * Y[6 + j];
+  }
+  return r;
+}
+template <typename TK> GF_HD M3<TK> dr_rows(const M3<TK>& Y, TK d3, TK d4, TK d5, TK d34) {
+  M3<TK> r;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r[j] = d3 * Y[j] + d34 * Y[3 + j];
+    r[3 + j] = d34 * Y[j] + d4 * Y[3 + j];
+    r[6 + j] = d5 * Y[6 + j];
+  }
+  return r;
+}
+
+template <typename TK>
+GF_HD void store_block(TK* M, int ms, int p, int q, const M3<TK>& X, bool add = false, bool transposed = false) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      TK v = transposed ? X[j * 3 + i] : X[i * 3 + j];
+      TK& dst = M[((3 * p + i) * 9 + 3 * q + j) * ms];
+      dst = add ? dst + v : v;
+    }
+}
+
+template <typename TK>
+GF_HD void beam_gp_operator(const BeamConst& c, const BeamGP& k, TK* M, int ms = 1) {
+  const double* sig = k.sig;
+  M3<double> kdZ = skew(k.dz);
+  TK d0 = TK(c.Dd[0]), d1 = TK(c.Dd[1]), d2 = TK(c.Dd[2]);
+  TK d3 = TK(c.Dd[3]), d4 = TK(c.Dd[4]), d5 = TK(c.Dd[5]), d34 = TK(c.D34);
+  M3<TK> Qt = cvt<TK>(k.Qt);
+  M3<TK> Xi = cvt<TK>(k.Xi);
+  M3<TK> Z;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Z[i] = TK(0);
+  store_block(M, ms, 0, 1, Z);
+  store_block(M, ms, 1, 0, Z);
+  store_block(M, ms, 0, 0, tmul(Qt, diag_rows(Qt, d0, d1, d2)));
+  {
+    M3<TK> P = mul(Qt, mul(cvt<TK>(kdZ), Xi));
+    M3<TK> DtP = diag_rows(P, d0, d1, d2);
+    M3<TK> M02 = tmul(Qt, DtP);
+    store_block(M, ms, 0, 2, M02);
+    store_block(M, ms, 2, 0, M02, false, true);
+    store_block(M, ms, 2, 2, tmul(P, DtP));
+  }
+  {
+    M3<TK> R = mul(Qt, Xi);
+    M3<TK> S = mul(Qt, cvt<TK>(k.dXi));
+    M3<TK> DrS = dr_rows(S, d3, d4, d5, d34);
+    store_block(M, ms, 1, 1, tmul(R, dr_rows(R, d3, d4, d5, d34)));
+    M3<TK> M12 = tmul(R, DrS);
+    store_block(M, ms, 1, 2, M12);
+    store_block(M, ms, 2, 1, M12, false, true);
+    store_block(M, ms, 2, 2, tmul(S, DrS), true);
+  }
+  // G (reference src/Beam_1.cpp:796-822)
+  V3<double> nr = {{sig[0], sig[1], sig[2]}}, mr = {{sig[3], sig[4], sig[5]}};
+  V3<TK> n = cvt<TK>(tmv(k.Qt, nr)), m = cvt<TK>(tmv(k.Qt, mr));
+  V3<TK> al = cvt<TK>(k.alpha);
+  TK g = TK(k.g);
+  M3<TK> Sn = skew(n);
+  {
+    M3<TK> Gua = mul(Sn, Xi);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Gua[i] = -Gua[i];
+    store_block(M, ms, 0, 2, Gua, true);
+    store_block(M, ms, 2, 0, tmul(Xi, Sn), true);
+  }
+  M3<TK> V2 = opV(al, m, g);
+  {
+    M3<TK> dZ = cvt<TK>(kdZ);
+    M3<TK> Gaa = tmul(Xi, mul(mul(dZ, Sn), Xi));
+    M3<TK> V1 = opV(al, mv(dZ, n), g);
+    M3<TK> dV = opdV(al, cvt<TK>(k.dalpha), m, g);
+    M3<TK> SmXi = mul(skew(m), Xi);
+    M3<TK> t2 = tmul(cvt<TK>(k.dXi), SmXi);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Gaa[i] = Gaa[i] - V1[i] + dV[i] - t2[i];
+    store_block(M, ms, 2, 2, Gaa, true);
+    M3<TK> t3 = tmul(Xi, SmXi);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) t3[i] = V2[i] - t3[i];
+    store_block(M, ms, 1, 2, t3, true);
+  }
+  store_block(M, ms, 2, 1, V2, true);
+}
+
+// M'_pq = T3^T M_pq T3 for the nine 3x3 blocks, in place.
+template <typename TK> GF_HD void rotate_blocks9(const BeamConst& c, TK* M, int ms = 1) {
+  TK T[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T[i] = TK(c.T3[i]);
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      TK b[9], t[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) b[i * 3 + j] = M[((3 * p + i) * 9 + 3 * q + j) * ms];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[i * 3 + j] = b[i * 3] * T[j] + b[i * 3 + 1] * T[3 + j] + b[i * 3 + 2] * T[6 + j];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          M[((3 * p + i) * 9 + 3 * q + j) * ms] = T[i] * t[j] + T[3 + i] * t[3 + j] + T[6 + i] * t[6 + j];
+    }
+}
+
+// Internal force contribution of one Gauss point, global frame, added to
+// f[i * fs] (reference src/Beam_1.cpp:828).
+GF_HD void beam_gp_force(const BeamConst& c, const BeamGP& k, int g, double* f, int fs = 1) {
+  V3<double> nr = {{k.sig[0], k.sig[1], k.sig[2]}}, mr = {{k.sig[3], k.sig[4], k.sig[5]}};
+  V3<double> n = tmv(k.Qt, nr), m = tmv(k.Qt, mr);
+  V3<double> s1 = tmv(k.Xi, m);
+  V3<double> a1 = tmv(k.Xi, tmv(skew(k.dz), n));
+  V3<double> a2 = tmv(k.dXi, m);
+  V3<double> s2 = {{a1[0] + a2[0], a1[1] + a2[1], a1[2] + a2[2]}};
+  M3<double> T;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T[i] = c.T3[i];
+  V3<double> g0 = tmv(T, n), g1 = tmv(T, s1), g2 = tmv(T, s2);
+  double wJ = c.jac;
+#pragma unroll
+  for (int I = 0; I < 3; ++I) {
+    double dN = c.dN[g][I], N = c.N[g][I];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      f[(6 * I + i) * fs] += wJ * dN * g0[i];
+      f[(6 * I + 3 + i) * fs] += wJ * (dN * g1[i] + N * g2[i]);
+    }
+  }
+}
+
+// K_e entry (row r, column s; 0..17, global frame) from the two rotated
+// Gauss-point operators M0, M1 (row-major 9x9).
+template <typename TK>
+GF_HD TK beam_K_entry(const BeamConst& c, const TK* M0, const TK* M1, int r, int s, int ms = 1) {
+  int I = r / 6, a = r % 6, J = s / 6, b = s % 6;
+  TK acc = TK(0);
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    const TK* M = g ? M1 : M0;
+    TK dNI = TK(c.dN[g][I]), NI = TK(c.N[g][I]), dNJ = TK(c.dN[g][J]), NJ = TK(c.N[g][J]);
+    TK w = TK(c.jac);
+    if (a < 3 && b < 3) {
+      acc += w * dNI * dNJ * M[(a * 9 + b) * ms];
+    } else if (a < 3) {
+      int bb = b - 3;
+      acc += w * dNI * (dNJ * M[(a * 9 + 3 + bb) * ms] + NJ * M[(a * 9 + 6 + bb) * ms]);
+    } else if (b < 3) {
+      int aa = a - 3;
+      acc += w * (dNI * M[((3 + aa) * 9 + b) * ms] + NI * M[((6 + aa) * 9 + b) * ms]) * dNJ;
+    } else {
+      int aa = a - 3, bb = b - 3;
+      acc += w * (dNI * dNJ * M[((3 + aa) * 9 + 3 + bb) * ms] + dNI * NJ * M[((3 + aa) * 9 + 6 + bb) * ms] +
+                  NI * dNJ * M[((6 + aa) * 9 + 3 + bb) * ms] + NI * NJ * M[((6 + aa) * 9 + 6 + bb) * ms]);
+    }
+  }
+  return acc;
+}
+
+// reference src/Beam_1.cpp:1494-1506
+GF_HD void beam_commit(const BeamConst& c, BeamHist& h, BeamHistAux& x, const double* d) {
+#pragma unroll 1
+  for (int g = 0; g < 2; ++g) {
+    BeamInterp ip = beam_interp(c, d, g);
+    BeamGP k;
+    beam_kinematics(c, h, ip, g, k);
+    double gg;
+    M3<double> Qd, Xi;
+    beam_rot(ip.alpha, gg, Qd, Xi);
+    M3<double> Qi;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Qi[i] = h.Q[g][i];
+    M3<double> Q = mul(Qd, Qi);
+    // kappa_r (reference src/Beam_1.cpp:785) recomputed for the history
+    V3<double> t = tmv(Xi, ip.dalpha);
+    V3<double> kap = tmv(Qi, t);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) h.Q[g][i] = Q[i];
+    V3<double> ai = {{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}};
+    V3<double> an = rodrigues_compose(ip.alpha, ai);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      x.u[g][i] += ip.u[i];
+      h.kap[g][i] = kap[i] + h.kap[g][i];
+      h.dz[g][i] = k.dz[i];
+      x.alpha[g][i] = an[i];
+    }
+  }
+}
+
+}  // namespace gf

@@ -1,0 +1,674 @@
+// Host side of the GB300 implicit Beam_1 path: builds device batches from
+// gf_model_desc structures (DOF numbering, colouring, PreCalc constants,
+// loads), drives the device-resident Newton loop, and implements the C ABI
+// declared in include/giraffe_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/giraffe_gpu.h"
+#include "gf_kernels.cuh"
+#include "gf_types.h"
+
+using namespace gf;
+
+struct gf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+};
+
+namespace {
+
+bool set_err(gf_ctx* ctx, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return false;
+}
+
+#define CK(call)                                                                             \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      set_err(ctx, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return GF_ERR_CUDA;                                                                    \
+    }                                                                                        \
+  } while (0)
+
+// ---- host restatements of PreCalc (reference src/Beam_1.cpp:501-692,
+// src/CoordinateSystem.cpp:68-92) ----
+void cs_rows(double* Q, const double* e1e3) {
+  double e1[3] = {e1e3[0], e1e3[1], e1e3[2]}, e3[3] = {e1e3[3], e1e3[4], e1e3[5]};
+  double e2[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+  auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+  double n1 = nrm(e1), n2 = nrm(e2), n3 = nrm(e3);
+  for (int k = 0; k < 3; ++k) {
+    Q[k] = n1 != 1.0 ? e1[k] * (1.0 / n1) : e1[k];
+    Q[3 + k] = n2 != 1.0 ? e2[k] * (1.0 / n2) : e2[k];
+    Q[6 + k] = n3 != 1.0 ? e3[k] * (1.0 / n3) : e3[k];
+  }
+}
+
+void beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec, const double* cs,
+                  BeamConst& c, BeamHist& h, BeamHistAux& x) {
+  std::memset(&c, 0, sizeof(c));
+  std::memset(&h, 0, sizeof(h));
+  std::memset(&x, 0, sizeof(x));
+  double E = mat[0], nu = mat[1], rho = mat[2];
+  double G = E / (2 * (1 + nu));
+  double sf = 1.0;
+  double A = sec[0], I1 = sec[1], I2 = sec[2], I12 = sec[3], It = sec[4], I33 = sec[5];
+  c.Dd[0] = sf * G * A;
+  c.Dd[1] = sf * G * A;
+  c.Dd[2] = E * A;
+  c.Dd[3] = E * I1;
+  c.Dd[4] = E * I2;
+  c.Dd[5] = G * It;
+  c.D34 = E * I12;
+  c.Mr = rho * A;
+  c.Jr[0] = rho * I1;
+  c.Jr[4] = rho * I2;
+  c.Jr[8] = rho * I33;
+  c.Jr[1] = c.Jr[3] = rho * I12;
+  cs_rows(c.T3, cs);
+  double e3[3] = {x2[0] - x0[0], x2[1] - x0[1], x2[2] - x0[2]};
+  double len = std::sqrt(e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2]);
+  double inv = 1.0 / len;
+  for (int k = 0; k < 3; ++k) e3[k] = inv * e3[k];
+  for (int i = 0; i < 3; ++i) c.e3r[i] = c.T3[i * 3] * e3[0] + c.T3[i * 3 + 1] * e3[1] + c.T3[i * 3 + 2] * e3[2];
+  c.jac = len / 2.0;
+  for (int g = 0; g < 2; ++g) {
+    double xi = g == 0 ? -0.577350269189626 : +0.577350269189626;
+    c.N[g][0] = 0.5 * xi * (xi - 1.0);
+    c.N[g][1] = 1.0 - xi * xi;
+    c.N[g][2] = 0.5 * xi * (1.0 + xi);
+    c.dN[g][0] = (1.0 / c.jac) * (xi - 0.5);
+    c.dN[g][1] = (1.0 / c.jac) * (-2.0 * xi);
+    c.dN[g][2] = (1.0 / c.jac) * (0.5 + xi);
+  }
+  for (int g = 0; g < 2; ++g) {
+    h.Q[g][0] = h.Q[g][4] = h.Q[g][8] = 1.0;
+    h.dz[g][2] = 1.0;
+  }
+}
+
+template <typename T> bool dmalloc(gf_ctx* ctx, T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (e != cudaSuccess) return set_err(ctx, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+  return true;
+}
+
+}  // namespace
+
+struct gf_batch {
+  gf_ctx* ctx = nullptr;
+  gf_solve_opts opts{};
+  Batch b{};
+  // host copies needed for results and resets
+  std::vector<StructInfo> info;
+  std::vector<int> kb;  // true half-bandwidth per structure
+  std::vector<void*> allocs;
+  // initial configuration (device) for gf_batch_reset
+  double* copy0 = nullptr;
+  double* Qn0 = nullptr;
+  BeamHist* bhist0 = nullptr;
+  BeamHistAux* baux0 = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long last_launches = 0;
+  int launches_per_pass = 0;
+  int* h_running = nullptr;  // pinned
+};
+
+namespace {
+
+template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
+  if (!dmalloc(B->ctx, p, n)) return false;
+  B->allocs.push_back(*p);
+  return true;
+}
+
+template <typename T> bool upload(gf_batch* B, T** p, const std::vector<T>& v) {
+  if (!balloc(B, p, v.size())) return false;
+  if (!v.empty()) {
+    cudaError_t e = cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return set_err(B->ctx, "upload failed: %s", cudaGetErrorString(e));
+  }
+  return true;
+}
+
+int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
+  gf_ctx* ctx = B->ctx;
+  Batch& b = B->b;
+  std::vector<double> copy, Qn;
+  std::vector<int> gl, cons, node_struct, enodes, estruct, dof_node6, ecolor;
+  std::vector<BeamConst> bconst;
+  std::vector<BeamHist> bhist;
+  std::vector<BeamHistAux> baux;
+  std::vector<StructParams> params;
+  std::vector<LoadEntry> loads;
+  std::vector<DispEntry> disps;
+  std::vector<TableDev> tables;
+  std::vector<double> tdata;
+  int node_off = 0, elem_off = 0, dof_off = 0;
+  int max_color = 0;
+  for (int s = 0; s < n; ++s) {
+    const gf_model_desc& m = models[s];
+    if (m.solution.type != GF_STATIC) { set_err(ctx, "structure %d: only Static solution steps are supported", s); return GF_ERR_ARG; }
+    if (m.n_shells) { set_err(ctx, "structure %d: Shell_1 elements are not supported by this entry point", s); return GF_ERR_ARG; }
+    const int nn = m.n_nodes;
+    std::vector<int> active(nn * 6, 0), c6(nn * 6, 0), g6(nn * 6, -2);
+    for (int e = 0; e < m.n_beams; ++e) {
+      for (int j = 0; j < 3; ++j) {
+        int nd = m.beams[6 * e + j];
+        if (nd < 0 || nd >= nn) { set_err(ctx, "structure %d: beam %d has node %d out of range", s, e, nd); return GF_ERR_ARG; }
+        for (int k = 0; k < 6; ++k) active[6 * nd + k] = 1;
+      }
+      if (m.beams[6 * e + 3] < 0 || m.beams[6 * e + 3] >= m.n_materials || m.beams[6 * e + 4] < 0 ||
+          m.beams[6 * e + 4] >= m.n_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
+        set_err(ctx, "structure %d: beam %d refers to a missing material, section or CS", s, e);
+        return GF_ERR_ARG;
+      }
+    }
+    if (m.constraints)
+      for (int i = 0; i < nn * 6; ++i) c6[i] = m.constraints[i] ? 1 : 0;
+    // SetGlobalDOFs (reference src/Solution.cpp:40-118): node-major numbering
+    int nf = 0;
+    bool has_f = false, has_m = false;
+    for (int i = 0; i < nn; ++i)
+      for (int k = 0; k < 6; ++k) {
+        if (!active[6 * i + k]) continue;
+        if (c6[6 * i + k] == 0) {
+          g6[6 * i + k] = nf++;
+          dof_node6.push_back((node_off + i) * 6 + k);
+          if (k < 3) has_f = true; else has_m = true;
+        } else {
+          g6[6 * i + k] = -1;
+        }
+      }
+    int kbs = 0;
+    for (int e = 0; e < m.n_beams; ++e)
+      for (int a = 0; a < 18; ++a)
+        for (int c = 0; c < 18; ++c) {
+          int ga = g6[6 * m.beams[6 * e + a / 6] + a % 6], gc = g6[6 * m.beams[6 * e + c / 6] + c % 6];
+          if (ga >= 0 && gc >= 0) kbs = std::max(kbs, std::abs(ga - gc));
+        }
+    if (kbs > GF_KB) {
+      set_err(ctx, "structure %d: K_AA half-bandwidth %d exceeds %d (node-major numbering of a chain gives 17)", s, kbs, GF_KB);
+      return GF_ERR_ARG;
+    }
+    B->kb.push_back(kbs);
+    // padding: every structure's DOF range starts at a multiple of 32
+    int nf_pad = (nf + 31) / 32 * 32;
+    for (int q = nf; q < nf_pad; ++q) dof_node6.push_back(-1);
+    StructInfo inf{};
+    inf.node_off = node_off;
+    inf.n_nodes = nn;
+    inf.elem_off = elem_off;
+    inf.n_elem = m.n_beams;
+    inf.dof_off = dof_off;
+    inf.n_free = nf;
+    inf.band_off = (int64_t)dof_off * GF_LDB;
+    inf.has_force = has_f;
+    inf.has_moment = has_m;
+    // nodes
+    for (int i = 0; i < nn; ++i) {
+      for (int k = 0; k < 3; ++k) copy.push_back(m.node_xyz[3 * i + k]);
+      for (int k = 0; k < 3; ++k) copy.push_back(0.0);
+      for (int k = 0; k < 9; ++k) Qn.push_back(k % 4 == 0 ? 1.0 : 0.0);
+      for (int k = 0; k < 6; ++k) { gl.push_back(g6[6 * i + k]); cons.push_back(c6[6 * i + k]); }
+      node_struct.push_back(s);
+    }
+    // elements: PreCalc + greedy colouring by shared nodes
+    std::vector<unsigned> node_colors(nn, 0u);
+    for (int e = 0; e < m.n_beams; ++e) {
+      const int* be = m.beams + 6 * e;
+      BeamConst c;
+      BeamHist h;
+      BeamHistAux x;
+      beam_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.materials + 3 * be[3], m.sections + 6 * be[4],
+                   m.cs + 6 * be[5], c, h, x);
+      bconst.push_back(c);
+      bhist.push_back(h);
+      baux.push_back(x);
+      for (int j = 0; j < 3; ++j) enodes.push_back(node_off + be[j]);
+      estruct.push_back(s);
+      unsigned used = node_colors[be[0]] | node_colors[be[1]] | node_colors[be[2]];
+      int col = 0;
+      while (col < 8 && (used >> col) & 1u) ++col;
+      if (col >= 8) { set_err(ctx, "structure %d: element colouring needs more than 8 colours", s); return GF_ERR_ARG; }
+      for (int j = 0; j < 3; ++j) node_colors[be[j]] |= 1u << col;
+      ecolor.push_back(col);
+      max_color = std::max(max_color, col + 1);
+    }
+    // tables and nodal loads (NodalLoad::UpdateforSolutionStep, reference
+    // src/NodalLoad.cpp:235-263)
+    auto add_table = [&](const gf_table& t) {
+      TableDev d{t.n_times, t.n_cols, (int64_t)tdata.size()};
+      for (int i = 0; i < t.n_times; ++i) tdata.push_back(t.times[i]);
+      for (int i = 0; i < t.n_times * t.n_cols; ++i) tdata.push_back(t.values[i]);
+      tables.push_back(d);
+      return (int)tables.size() - 1;
+    };
+    inf.load_off = (int)loads.size();
+    for (int l = 0; l < m.n_loads; ++l) {
+      const gf_load& L = m.loads[l];
+      if (L.type != GF_LOAD_NODAL) { set_err(ctx, "structure %d: only nodal loads are supported for beams", s); return GF_ERR_ARG; }
+      if (L.table.n_cols < 6) { set_err(ctx, "structure %d: nodal load table needs 6 columns", s); return GF_ERR_ARG; }
+      int cnt[6] = {0, 0, 0, 0, 0, 0};
+      for (int q = 0; q < L.n_items; ++q)
+        for (int k = 0; k < 6; ++k)
+          if (active[6 * L.items[q] + k] != 0) cnt[k]++;
+      int t = add_table(L.table);
+      double CQ[9];
+      cs_rows(CQ, m.cs + 6 * L.cs);
+      for (int q = 0; q < L.n_items; ++q) {
+        LoadEntry le{};
+        le.structure = s;
+        le.node = node_off + L.items[q];
+        le.table = t;
+        std::memcpy(le.CQ, CQ, sizeof(CQ));
+        for (int k = 0; k < 6; ++k) le.mult[k] = 1.0 / cnt[k];
+        loads.push_back(le);
+        // load stiffness couples the node's rotations
+        for (int a = 3; a < 6; ++a)
+          for (int c = 3; c < 6; ++c) {
+            int ga = g6[6 * L.items[q] + a], gc = g6[6 * L.items[q] + c];
+            if (ga >= 0 && gc >= 0 && std::abs(ga - gc) > GF_KB) { set_err(ctx, "load bandwidth"); return GF_ERR_ARG; }
+          }
+      }
+    }
+    inf.n_loads = (int)loads.size() - inf.load_off;
+    for (int l = 0; l < m.n_displacements; ++l) {
+      const gf_displacement& D = m.displacements[l];
+      if (D.table.n_cols < 6) { set_err(ctx, "structure %d: displacement table needs 6 columns", s); return GF_ERR_ARG; }
+      int t = add_table(D.table);
+      double CQ[9];
+      cs_rows(CQ, m.cs + 6 * D.cs);
+      for (int q = 0; q < D.n_nodes; ++q) {
+        DispEntry de{};
+        de.structure = s;
+        de.node = node_off + D.nodes[q];
+        de.table = t;
+        std::memcpy(de.CQ, CQ, sizeof(CQ));
+        disps.push_back(de);
+      }
+    }
+    StructParams p{};
+    const gf_solution& so = m.solution;
+    p.start_time = so.start_time;
+    p.end_time = so.end_time;
+    p.time_step0 = so.time_step;
+    p.max_time_step = so.max_time_step;
+    p.min_time_step = so.min_time_step;
+    p.inc_factor = so.inc_factor;
+    p.max_it = so.max_it;
+    p.min_it = so.min_it;
+    p.conv_increase = so.conv_increase;
+    const gf_criteria& cr = m.criteria;
+    p.force_tol = cr.force_tol;
+    p.moment_tol = cr.moment_tol;
+    p.force_min = cr.force_min;
+    p.moment_min = cr.moment_min;
+    p.disp_tol = cr.disp_tol;
+    p.rot_tol = cr.rot_tol;
+    p.disp_min = cr.disp_min;
+    p.rot_min = cr.rot_min;
+    p.divergence_ref = cr.divergence_ref;
+    params.push_back(p);
+    B->info.push_back(inf);
+    node_off += nn;
+    elem_off += m.n_beams;
+    dof_off += nf_pad;
+  }
+  b.n_struct = n;
+  b.n_nodes = node_off;
+  b.n_elem = elem_off;
+  b.n_free = dof_off;
+  b.n_loads = (int)loads.size();
+  b.n_disps = (int)disps.size();
+  b.n_tables = (int)tables.size();
+  // colour lists
+  std::vector<int> color_elems;
+  b.n_colors = max_color;
+  for (int c = 0; c < max_color; ++c) {
+    b.color_off[c] = (int)color_elems.size();
+    for (int e = 0; e < elem_off; ++e)
+      if (ecolor[e] == c) color_elems.push_back(e);
+  }
+  b.color_off[max_color] = (int)color_elems.size();
+  // device arrays
+  std::vector<double> zeros6((size_t)node_off * 6, 0.0);
+  if (!upload(B, &b.copy, copy) || !upload(B, &b.Qn, Qn) || !upload(B, &b.disp, zeros6) || !upload(B, &b.gl, gl) ||
+      !upload(B, &b.cons, cons) || !upload(B, &b.node_struct, node_struct) || !upload(B, &b.enodes, enodes) ||
+      !upload(B, &b.estruct, estruct) || !upload(B, &b.bconst, bconst) || !upload(B, &b.bhist, bhist) ||
+      !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
+      !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.loads, loads) ||
+      !upload(B, &b.disps, disps) || !upload(B, &b.tables, tables) || !upload(B, &b.table_data, tdata) ||
+      !upload(B, &B->copy0, copy) || !upload(B, &B->Qn0, Qn) || !upload(B, &B->bhist0, bhist) ||
+      !upload(B, &B->baux0, baux))
+    return GF_ERR_CUDA;
+  if (!balloc(B, &b.P, (size_t)dof_off) || !balloc(B, &b.y, (size_t)dof_off) ||
+      !balloc(B, &b.band, (size_t)dof_off * GF_LDB) || !balloc(B, &b.U, (size_t)dof_off * GF_UW) ||
+      !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1))
+    return GF_ERR_CUDA;
+  CK(cudaMemset(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB));
+  CK(cudaMemset(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1)));
+  b.mixed = B->opts.precision == GF_PREC_MIXED;
+  b.max_refine = B->opts.max_refine;
+  return GF_OK;
+}
+
+int batch_reset(gf_batch* B) {
+  gf_ctx* ctx = B->ctx;
+  Batch& b = B->b;
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(b.copy, B->copy0, sizeof(double) * (size_t)b.n_nodes * 6, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(b.Qn, B->Qn0, sizeof(double) * (size_t)b.n_nodes * 9, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(b.bhist, B->bhist0, sizeof(BeamHist) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(b.baux, B->baux0, sizeof(BeamHistAux) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemsetAsync(b.disp, 0, sizeof(double) * (size_t)std::max(b.n_nodes, 1) * 6, st));
+  launch_init_state(b, st);
+  CK(cudaGetLastError());
+  return GF_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+gf_ctx* gf_create(int device) {
+  gf_ctx* ctx = new gf_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return nullptr;
+  }
+  return ctx;
+}
+
+void gf_destroy(gf_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* gf_last_error(const gf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void gf_default_opts(gf_solve_opts* o) {
+  o->precision = GF_PREC_FP64;
+  o->max_refine = 6;
+  o->poll_every = 8;
+  o->use_graph = 1;
+}
+
+gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts) {
+  if (!ctx || n <= 0 || !models) {
+    set_err(ctx, "gf_batch_create: invalid arguments");
+    return nullptr;
+  }
+  cudaSetDevice(ctx->device);
+  gf_batch* B = new gf_batch();
+  B->ctx = ctx;
+  if (opts) B->opts = *opts; else gf_default_opts(&B->opts);
+  if (B->opts.poll_every <= 0) B->opts.poll_every = 8;
+  if (build_batch(B, n, models) != GF_OK || cudaMallocHost(&B->h_running, sizeof(int)) != cudaSuccess ||
+      cudaEventCreate(&B->ev0) != cudaSuccess || cudaEventCreate(&B->ev1) != cudaSuccess) {
+    std::string e = ctx->err;
+    gf_batch_destroy(B);
+    ctx->err = e.empty() ? "gf_batch_create failed" : e;
+    return nullptr;
+  }
+  int colors = 0;
+  for (int c = 0; c < B->b.n_colors; ++c) colors += B->b.color_off[c + 1] > B->b.color_off[c];
+  B->launches_per_pass = 9 + colors;
+  return B;
+}
+
+void gf_batch_destroy(gf_batch* B) {
+  if (!B) return;
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  for (void* p : B->allocs) cudaFree(p);
+  if (B->h_running) cudaFreeHost(B->h_running);
+  if (B->ev0) cudaEventDestroy(B->ev0);
+  if (B->ev1) cudaEventDestroy(B->ev1);
+  delete B;
+}
+
+int gf_batch_reset(gf_batch* B) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  int r = batch_reset(B);
+  if (r != GF_OK) return r;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GF_OK;
+}
+
+int gf_batch_run(gf_batch* B) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  const Batch& b = B->b;
+  if (B->opts.use_graph && !B->graph) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_iteration(b, st);
+    CK(cudaStreamEndCapture(st, &g));
+    CK(cudaGraphInstantiate(&B->graph, g, 0));
+    CK(cudaGraphDestroy(g));
+  }
+  CK(cudaEventRecord(B->ev0, st));
+  long long passes = 0;
+  const long long cap = 4000000;
+  for (;;) {
+    for (int k = 0; k < B->opts.poll_every; ++k) {
+      if (B->graph) {
+        CK(cudaGraphLaunch(B->graph, st));
+      } else {
+        launch_iteration(b, st);
+      }
+      ++passes;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(B->h_running, b.running, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (*B->h_running == 0) break;
+    if (passes > cap) {
+      set_err(ctx, "gf_batch_run: %lld Newton passes without completion", passes);
+      return GF_ERR_TIMEOUT;
+    }
+  }
+  CK(cudaEventRecord(B->ev1, st));
+  CK(cudaEventSynchronize(B->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+  B->last_ms = ms;
+  B->last_launches = passes * B->launches_per_pass;
+  return GF_OK;
+}
+
+double gf_batch_last_ms(const gf_batch* B) { return B ? B->last_ms : 0.0; }
+long long gf_batch_last_launches(const gf_batch* B) { return B ? B->last_launches : 0; }
+
+int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  const Batch& b = B->b;
+  int n = b.n_struct;
+  std::vector<StructState> st(n);
+  CK(cudaMemcpy(st.data(), b.state, sizeof(StructState) * n, cudaMemcpyDeviceToHost));
+  if (stats)
+    for (int s = 0; s < n; ++s) {
+      gf_stats z{};
+      z.converged_steps = st[s].converged_number;
+      z.newton_iterations = st[s].total_it;
+      z.bisections = st[s].bisections;
+      z.aborted = st[s].phase == PH_ABORTED || st[s].aborted;
+      z.fp64_fallback = st[s].fp64_fallback;
+      stats[s] = z;
+    }
+  if (final_nodes) {
+    std::vector<double> copy((size_t)b.n_nodes * 6), Qn((size_t)b.n_nodes * 9);
+    CK(cudaMemcpy(copy.data(), b.copy, sizeof(double) * copy.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(Qn.data(), b.Qn, sizeof(double) * Qn.size(), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < n; ++s) {
+      double* o = final_nodes[s];
+      if (!o) continue;
+      const StructInfo& inf = B->info[s];
+      for (int i = 0; i < inf.n_nodes; ++i) {
+        std::memcpy(o + 15 * i, &copy[(size_t)(inf.node_off + i) * 6], 6 * sizeof(double));
+        std::memcpy(o + 15 * i + 6, &Qn[(size_t)(inf.node_off + i) * 9], 9 * sizeof(double));
+      }
+    }
+  }
+  return GF_OK;
+}
+
+int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
+  if (!B || s < 0 || s >= B->b.n_struct) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  const Batch& b = B->b;
+  const StructInfo& inf = B->info[s];
+  int kb = B->kb[s];
+  if (dims) { dims[0] = inf.n_free; dims[1] = kb; }
+  if (!ab && !PA) return GF_OK;
+  int r = batch_reset(B);
+  if (r != GF_OK) return r;
+  // one partial pass: step start, zero, mount, loads, residual
+  Batch bb = b;
+  launch_iteration_partial(bb, ctx->stream);
+  CK(cudaGetLastError());
+  std::vector<double> band((size_t)inf.n_free * GF_LDB), P(inf.n_free);
+  CK(cudaMemcpyAsync(band.data(), b.band + inf.band_off, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(P.data(), b.P + inf.dof_off, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int ldab = 3 * kb + 1;
+  if (ab) {
+    std::memset(ab, 0, sizeof(double) * (size_t)ldab * inf.n_free);
+    for (int j = 0; j < inf.n_free; ++j)
+      for (int i = std::max(0, j - kb); i <= std::min(inf.n_free - 1, j + kb); ++i)
+        ab[(size_t)(2 * kb + i - j) + (size_t)j * ldab] = band[(size_t)(GF_KB + i - j) + (size_t)j * GF_LDB];
+  }
+  if (PA) std::memcpy(PA, P.data(), sizeof(double) * inf.n_free);
+  return batch_reset(B) == GF_OK ? GF_OK : GF_ERR_CUDA;
+}
+
+int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts, double* const* final_nodes,
+             gf_stats* stats) {
+  gf_batch* B = gf_batch_create(ctx, n, models, opts);
+  if (!B) return GF_ERR_ARG;
+  int r = gf_batch_reset(B);
+  if (r == GF_OK) r = gf_batch_run(B);
+  if (r == GF_OK) r = gf_batch_results(B, final_nodes, stats);
+  gf_batch_destroy(B);
+  return r;
+}
+
+int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec, const double* cs,
+                     int n_hist, const double* hist_disp, const double* disp, double* K, double* f) {
+  if (!ctx || n <= 0) return GF_ERR_ARG;
+  std::vector<BeamConst> c(n);
+  std::vector<BeamHist> h(n);
+  std::vector<BeamHistAux> x(n);
+  for (int e = 0; e < n; ++e)
+    beam_precalc(xyz + 9 * e, xyz + 9 * e + 6, mat + 3 * e, sec + 6 * e, cs + 6 * e, c[e], h[e], x[e]);
+  BeamConst* dc = nullptr;
+  BeamHist* dh = nullptr;
+  BeamHistAux* dx = nullptr;
+  double *dd = nullptr, *dK = nullptr, *df = nullptr;
+  int rc = GF_OK;
+  if (!dmalloc(ctx, &dc, n) || !dmalloc(ctx, &dh, n) || !dmalloc(ctx, &dx, n) || !dmalloc(ctx, &dd, (size_t)n * 18) ||
+      !dmalloc(ctx, &dK, (size_t)n * 324) || !dmalloc(ctx, &df, (size_t)n * 18)) {
+    rc = GF_ERR_CUDA;
+  } else {
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(dc, c.data(), sizeof(BeamConst) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dh, h.data(), sizeof(BeamHist) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dx, x.data(), sizeof(BeamHistAux) * n, cudaMemcpyHostToDevice, st);
+    std::vector<double> step((size_t)n * 18);
+    for (int q = 0; q < n_hist; ++q) {
+      for (int e = 0; e < n; ++e)
+        std::memcpy(&step[(size_t)e * 18], hist_disp + ((size_t)e * n_hist + q) * 18, 18 * sizeof(double));
+      cudaMemcpyAsync(dd, step.data(), sizeof(double) * step.size(), cudaMemcpyHostToDevice, st);
+      launch_beam_commit(n, dc, dh, dx, dd, st);
+      cudaStreamSynchronize(st);
+    }
+    cudaMemcpyAsync(dd, disp, sizeof(double) * (size_t)n * 18, cudaMemcpyHostToDevice, st);
+    launch_beam_elements(n, dc, dh, dd, dK, df, st);
+    cudaMemcpyAsync(K, dK, sizeof(double) * (size_t)n * 324, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(f, df, sizeof(double) * (size_t)n * 18, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_err(ctx, "gf_beam_elements: %s", cudaGetErrorString(e));
+      rc = GF_ERR_CUDA;
+    }
+  }
+  cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dK); cudaFree(df);
+  return rc;
+}
+
+int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info) {
+  if (!ctx || n <= 0 || kl < 0 || ku < 0 || kl > GF_KB || ku > GF_KB || ldab < 2 * kl + ku + 1 || !ab || !b) {
+    set_err(ctx, "gf_band_solve: invalid arguments (kl, ku must be <= %d)", GF_KB);
+    return GF_ERR_ARG;
+  }
+  int npad = (n + 31) / 32 * 32;
+  std::vector<double> band((size_t)npad * GF_LDB, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int i = std::max(0, j - ku); i <= std::min(n - 1, j + kl); ++i)
+      band[(size_t)(GF_KB + i - j) + (size_t)j * GF_LDB] = ab[(size_t)(kl + ku + i - j) + (size_t)j * ldab];
+  Batch bt{};
+  bt.n_struct = 1;
+  StructInfo inf{};
+  inf.n_free = n;
+  StructState st0{};
+  st0.phase = PH_ITER;
+  st0.need_solve = 1;
+  double *dband = nullptr, *dP = nullptr, *dU = nullptr;
+  StructInfo* dinf = nullptr;
+  StructState* dst = nullptr;
+  int rc = GF_OK;
+  if (!dmalloc(ctx, &dband, band.size()) || !dmalloc(ctx, &dP, (size_t)npad) || !dmalloc(ctx, &dU, (size_t)npad * GF_UW) ||
+      !dmalloc(ctx, &dinf, 1) || !dmalloc(ctx, &dst, 1)) {
+    rc = GF_ERR_CUDA;
+  } else {
+    cudaStream_t s = ctx->stream;
+    cudaMemcpyAsync(dband, band.data(), sizeof(double) * band.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dP, b, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dinf, &inf, sizeof(inf), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dst, &st0, sizeof(st0), cudaMemcpyHostToDevice, s);
+    bt.band = dband;
+    bt.P = dP;
+    bt.U = dU;
+    bt.info = dinf;
+    bt.state = dst;
+    launch_band_solve(bt, s);
+    cudaMemcpyAsync(b, dP, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&st0, dst, sizeof(st0), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_err(ctx, "gf_band_solve: %s", cudaGetErrorString(e));
+      rc = GF_ERR_CUDA;
+    }
+    if (info) *info = st0.info_fail;
+  }
+  cudaFree(dband); cudaFree(dP); cudaFree(dU); cudaFree(dinf); cudaFree(dst);
+  return rc;
+}
+
+}  // extern "C"

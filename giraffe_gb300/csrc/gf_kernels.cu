@@ -1,0 +1,671 @@
+// Device-resident Newton loop for batches of Beam_1 structures (see
+// gf_kernels.cuh for the pass structure and the reference lines each kernel
+// follows).
+#include <cuda_runtime.h>
+
+#include "gf_beam.cuh"
+#include "gf_kernels.cuh"
+
+namespace gf {
+
+namespace {
+
+__device__ __forceinline__ bool iterating(const StructState& s) { return s.phase == PH_ITER; }
+
+__device__ __forceinline__ double table_at(const Batch& b, int t, double time, int col) {
+  const TableDev T = b.tables[t];
+  const double* times = b.table_data + T.off;
+  const double* vals = times + T.n_times;
+  if (T.n_times == 0) return 0.0;
+  if (time >= times[T.n_times - 1]) return vals[(T.n_times - 1) * T.n_cols + col];
+  if (time <= times[0]) return vals[col];
+  int idx = 0;
+  while (time >= times[idx]) idx++;
+  double f = (time - times[idx - 1]) / (times[idx] - times[idx - 1]);
+  double a = vals[(idx - 1) * T.n_cols + col], c = vals[idx * T.n_cols + col];
+  return a + f * (c - a);
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_or(int v) { return __any_sync(0xffffffffu, v); }
+
+// Block-wide max of two values and an "any" flag (blockDim.x <= 1024).
+struct Red3 { double a, b; int f; };
+__device__ Red3 block_red(Red3 v) {
+  __shared__ double sa[32], sb[32];
+  __shared__ int sf[32];
+  v.a = warp_max(v.a);
+  v.b = warp_max(v.b);
+  v.f = warp_or(v.f);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sa[w] = v.a; sb[w] = v.b; sf[w] = v.f; }
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  if (w == 0) {
+    v.a = l < nw ? sa[l] : 0.0;
+    v.b = l < nw ? sb[l] : 0.0;
+    v.f = l < nw ? sf[l] : 0;
+    v.a = warp_max(v.a);
+    v.b = warp_max(v.b);
+    v.f = warp_or(v.f);
+    if (l == 0) { sa[0] = v.a; sb[0] = v.b; sf[0] = v.f; }
+  }
+  __syncthreads();
+  Red3 r{sa[0], sb[0], sf[0]};
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ bool nan_or_huge(double v) { return !(v == v) || v >= 1e300 || v <= -1e300; }
+
+// ---------------------------------------------------------------------------
+// initial state: reference src/Static.cpp:140-170
+__global__ void k_init_state(Batch b) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= b.n_struct) return;
+  const StructParams& p = b.params[s];
+  StructState& st = b.state[s];
+  StructState z = {};
+  z.phase = PH_START;
+  z.time = p.start_time;
+  z.time_step = p.time_step0;
+  z.last_converged_time = p.start_time;
+  st = z;
+}
+
+// reference src/Static.cpp:176-197 (+ NodalDisplacement::Mount, EulerAngles)
+__global__ void k_step_begin(Batch b) {
+  int s = blockIdx.x;
+  StructState& st = b.state[s];
+  __shared__ int go;
+  if (threadIdx.x == 0) {
+    if (s == 0) *b.running = 0;
+    go = st.phase == PH_START;
+    if (go) {
+      const StructParams& p = b.params[s];
+      st.last_converged_time = st.time;
+      st.time += st.time_step;
+      if (st.time > 0.99999999 * p.end_time) {
+        st.time = p.end_time;
+        st.time_step = p.end_time - st.last_converged_time;
+      }
+      st.current_time_step = st.time_step;
+      st.it = 1;
+      st.res_conv = 0;
+      st.gl_conv = 0;
+      st.diverged = 0;
+      st.info_fail = 0;
+      st.phase = PH_ITER;
+    }
+  }
+  __syncthreads();
+  if (!go) return;
+  const StructInfo inf = b.info[s];
+  for (int i = threadIdx.x; i < inf.n_nodes * 6; i += blockDim.x) b.disp[(int64_t)inf.node_off * 6 + i] = 0.0;
+  __syncthreads();
+  double time = st.last_converged_time + st.current_time_step, dt = st.current_time_step;
+  for (int e = threadIdx.x; e < b.n_disps; e += blockDim.x) {
+    const DispEntry D = b.disps[e];
+    if (D.structure != s) continue;
+    int node = D.node;
+    const int* cons = b.cons + (int64_t)node * 6;
+    const int* gl = b.gl + (int64_t)node * 6;
+    double dl[3], dg[3];
+    for (int j = 0; j < 3; ++j) dl[j] = table_at(b, D.table, time, j) - table_at(b, D.table, time - dt, j);
+    for (int j = 0; j < 3; ++j) dg[j] = D.CQ[j] * dl[0] + D.CQ[3 + j] * dl[1] + D.CQ[6 + j] * dl[2];
+    for (int j = 0; j < 3; ++j)
+      if (cons[j] == 1 && gl[j] == -1) b.disp[(int64_t)node * 6 + j] = dg[j];
+    double phi = cons[3] == 1 ? table_at(b, D.table, time, 3) : 0.0;
+    double th = cons[4] == 1 ? table_at(b, D.table, time, 4) : 0.0;
+    double psi = cons[5] == 1 ? table_at(b, D.table, time, 5) : 0.0;
+    M3<double> Q;
+    Q[0] = cos(th) * cos(psi);
+    Q[1] = sin(phi) * sin(th) * cos(psi) - cos(phi) * sin(psi);
+    Q[2] = cos(phi) * sin(th) * cos(psi) + sin(phi) * sin(psi);
+    Q[3] = cos(th) * sin(psi);
+    Q[4] = sin(phi) * sin(th) * sin(psi) + cos(phi) * cos(psi);
+    Q[5] = cos(phi) * sin(th) * sin(psi) - sin(phi) * cos(psi);
+    Q[6] = -sin(th);
+    Q[7] = sin(phi) * cos(th);
+    Q[8] = cos(phi) * cos(th);
+    M3<double> CQ, Qi;
+    for (int k = 0; k < 9; ++k) { CQ[k] = D.CQ[k]; Qi[k] = b.Qn[(int64_t)node * 9 + k]; }
+    Q = tmul(CQ, mul(Q, CQ));
+    M3<double> Qd = mul(Q, transpose(Qi));
+    double tr = Qd[0] + Qd[4] + Qd[8];
+    if (tr > 3.0) tr = 3.0;
+    double ax[3] = {0.5 * (Qd[7] - Qd[5]), 0.5 * (Qd[2] - Qd[6]), 0.5 * (Qd[3] - Qd[1])};
+    double al = 2.0 * sqrt((3.0 - tr) / (1.0 + tr));
+    for (int j = 3; j < 6; ++j)
+      if (cons[j] == 1 && gl[j] == -1) b.disp[(int64_t)node * 6 + j] = ((4.0 + al * al) / 4.0) * ax[j - 3];
+  }
+}
+
+// clear band and P of iterating structures
+__global__ void k_zero(Batch b) {
+  int s = blockIdx.y;
+  if (!iterating(b.state[s])) return;
+  const StructInfo inf = b.info[s];
+  int64_t nb = (int64_t)inf.n_free * GF_LDB;
+  double* band = b.band + inf.band_off;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
+    band[i] = 0.0;
+  double* P = b.P + inf.dof_off;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < inf.n_free; i += gridDim.x * blockDim.x) P[i] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Beam_1 Mount + MountElementLoads + MountGlobal for one colour class.
+// One thread per element.  The two rotated Gauss-point operators live in
+// shared memory ([g][entry][thread], conflict-free) while the 18x18 tangent is
+// streamed into the band; elements of one colour share no node, so the
+// scatter needs no atomics and is deterministic.
+constexpr int MOUNT_THREADS = 64;
+constexpr int MOUNT_SMEM = (2 * 81 + 18) * MOUNT_THREADS * (int)sizeof(double);
+
+template <typename TK>
+__global__ void __launch_bounds__(MOUNT_THREADS) k_beam_mount(Batch b, int color) {
+  extern __shared__ unsigned char smem_raw[];
+  TK* sM = reinterpret_cast<TK*>(smem_raw);
+  const int tid = threadIdx.x;
+  int k = b.color_off[color] + blockIdx.x * MOUNT_THREADS + tid;
+  if (k >= b.color_off[color + 1]) return;
+  int e = b.color_elems[k];
+  int s = b.estruct[e];
+  if (!iterating(b.state[s])) return;
+  const StructInfo inf = b.info[s];
+  const BeamConst& c = b.bconst[e];
+  const BeamHist& h = b.bhist[e];
+  int nd[3] = {b.enodes[3 * e], b.enodes[3 * e + 1], b.enodes[3 * e + 2]};
+  double d[18];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) d[6 * j + q] = b.disp[(int64_t)nd[j] * 6 + q];
+  BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
+  double* f = reinterpret_cast<double*>(sM + (size_t)2 * 81 * MOUNT_THREADS) + tid;
+#pragma unroll
+  for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
+#pragma unroll 1
+  for (int g = 0; g < 2; ++g) {
+    BeamGP kin;
+    beam_kinematics(c, h, ip[g], g, kin);
+    beam_gp_force(c, kin, g, f, MOUNT_THREADS);
+    TK* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
+    beam_gp_operator<TK>(c, kin, M, MOUNT_THREADS);
+    rotate_blocks9<TK>(c, M, MOUNT_THREADS);
+  }
+  int gl[18];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) gl[6 * j + q] = b.gl[(int64_t)nd[j] * 6 + q];
+  double* P = b.P + inf.dof_off;
+#pragma unroll
+  for (int r = 0; r < 18; ++r)
+    if (gl[r] >= 0) P[gl[r]] += f[r * MOUNT_THREADS];
+  double* band = b.band + inf.band_off;
+#pragma unroll 1
+  for (int r = 0; r < 18; ++r) {
+    if (gl[r] < 0) continue;
+#pragma unroll 1
+    for (int q2 = 0; q2 < 18; ++q2) {
+      if (gl[q2] < 0) continue;
+      // beam_K_entry reads the operators from shared memory through small
+      // per-thread views
+      int I = r / 6, a = r % 6, J = q2 / 6, bb = q2 % 6;
+      TK acc = TK(0);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const TK* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
+#define MM(i, j) M[((i) * 9 + (j)) * MOUNT_THREADS]
+        TK dNI = TK(c.dN[g][I]), NI = TK(c.N[g][I]), dNJ = TK(c.dN[g][J]), NJ = TK(c.N[g][J]);
+        TK w = TK(c.jac);
+        if (a < 3 && bb < 3) {
+          acc += w * dNI * dNJ * MM(a, bb);
+        } else if (a < 3) {
+          int b3 = bb - 3;
+          acc += w * dNI * (dNJ * MM(a, 3 + b3) + NJ * MM(a, 6 + b3));
+        } else if (bb < 3) {
+          int a3 = a - 3;
+          acc += w * (dNI * MM(3 + a3, bb) + NI * MM(6 + a3, bb)) * dNJ;
+        } else {
+          int a3 = a - 3, b3 = bb - 3;
+          acc += w * (dNI * dNJ * MM(3 + a3, 3 + b3) + dNI * NJ * MM(3 + a3, 6 + b3) +
+                      NI * dNJ * MM(6 + a3, 3 + b3) + NI * NJ * MM(6 + a3, 6 + b3));
+        }
+#undef MM
+      }
+      band[(GF_KB + gl[r] - gl[q2]) + (int64_t)gl[q2] * GF_LDB] += double(acc);
+    }
+  }
+}
+
+// NodalLoad::Mount for every load entry of a structure, in entry order (one
+// thread per structure keeps the accumulation order fixed).
+__global__ void k_loads(Batch b) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= b.n_struct || !iterating(b.state[s])) return;
+  const StructInfo inf = b.info[s];
+  const StructState& st = b.state[s];
+  double time = st.last_converged_time + st.current_time_step;
+  double* P = b.P + inf.dof_off;
+  double* band = b.band + inf.band_off;
+  for (int l = inf.load_off; l < inf.load_off + inf.n_loads; ++l) {
+    const LoadEntry L = b.loads[l];
+    int node = L.node;
+    const int* gl = b.gl + (int64_t)node * 6;
+    V3<double> fl, ml;
+    for (int i = 0; i < 3; ++i) {
+      fl[i] = L.mult[i] * table_at(b, L.table, time, i);
+      ml[i] = L.mult[3 + i] * table_at(b, L.table, time, i + 3);
+    }
+    M3<double> CQ;
+    for (int q = 0; q < 9; ++q) CQ[q] = L.CQ[q];
+    V3<double> fv = tmv(CQ, fl), mvv = tmv(CQ, ml);
+    V3<double> al = {{b.disp[(int64_t)node * 6 + 3], b.disp[(int64_t)node * 6 + 4], b.disp[(int64_t)node * 6 + 5]}};
+    double g = 4.0 / (4.0 + dot(al, al));
+    M3<double> A = skew(al), Xi;
+    for (int q = 0; q < 9; ++q) Xi[q] = g * 0.5 * A[q];
+    Xi[0] += g; Xi[4] += g; Xi[8] += g;
+    V3<double> mm = tmv(Xi, mvv);
+    M3<double> V = opV(al, mm, g);
+    for (int i = 0; i < 3; ++i)
+      if (gl[i] >= 0) P[gl[i]] += -1.0 * fv[i];
+    for (int i = 0; i < 3; ++i) {
+      int gi = gl[3 + i];
+      if (gi >= 0) P[gi] += -1.0 * mm[i];
+      for (int j = 0; j < 3; ++j) {
+        int gj = gl[3 + j];
+        if (gi >= 0 && gj >= 0) band[(GF_KB + gi - gj) + (int64_t)gj * GF_LDB] += -1.0 * V[i * 3 + j];
+      }
+    }
+  }
+}
+
+// P = -P; EstablishResidualCriteria at the first iteration;
+// CheckResidualConvergence (reference src/ConvergenceCriteria.cpp:187-285,
+// 460-598).
+__global__ void k_residual(Batch b) {
+  int s = blockIdx.x;
+  StructState& st = b.state[s];
+  if (!iterating(st)) return;
+  const StructInfo inf = b.info[s];
+  const StructParams& p = b.params[s];
+  double* P = b.P + inf.dof_off;
+  const int* d6 = b.dof_node6 + inf.dof_off;
+  Red3 v{0.0, 0.0, 0};
+  for (int i = threadIdx.x; i < inf.n_free; i += blockDim.x) {
+    double x = -1.0 * P[i];
+    P[i] = x;
+    double a = fabs(x);
+    if (nan_or_huge(a)) v.f = 1;
+    if (d6[i] % 6 < 3) { if (a > v.a) v.a = a; }
+    else { if (a > v.b) v.b = a; }
+  }
+  Red3 r = block_red(v);
+  if (threadIdx.x == 0) {
+    if (st.it == 1) {
+      double pf = st.force_crit, pm = st.moment_crit;
+      double fc = r.a * p.force_tol > p.force_min * p.force_tol ? r.a * p.force_tol : p.force_min * p.force_tol;
+      double mc = r.b * p.moment_tol > p.moment_min * p.moment_tol ? r.b * p.moment_tol : p.moment_min * p.moment_tol;
+      st.force_crit = (st.n_conv_evaluated * pf + fc) / (st.n_conv_evaluated + 1);
+      st.moment_crit = (st.n_conv_evaluated * pm + mc) / (st.n_conv_evaluated + 1);
+      st.n_conv_evaluated++;
+    }
+    if (r.f) st.diverged = 1;
+    int conv = 1;
+    if (r.a > p.divergence_ref || r.b > p.divergence_ref) {
+      st.diverged = 1;
+      conv = 0;
+    } else {
+      if (inf.has_force && r.a > st.force_crit) conv = 0;
+      if (inf.has_moment && r.b > st.moment_crit) conv = 0;
+    }
+    st.res_conv = conv;
+    st.last_res = fmax(r.a, r.b);
+    st.need_solve = !(st.res_conv && st.gl_conv);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Banded LU without pivoting, fused forward substitution, then back
+// substitution, FP64.  One warp per structure.  Columns stream through a
+// 128-column shared-memory ring filled 32 columns at a time, two chunks
+// ahead of the elimination; the warp owns the active 18-column window: lane 0
+// updates the right-hand side, lanes 1..17 the 17 trailing columns.  U rows
+// (pivot first) are written to b.U; the solution overwrites P.
+constexpr int RING = 128;
+constexpr int CHUNK = 32;
+
+template <typename T>
+__device__ __forceinline__ void load_chunk(const T* __restrict__ band, double* __restrict__ rhs, T* ring,
+                                           double* rring, int q, int n, int lane) {
+  int c0 = q * CHUNK;
+  if (c0 >= n) return;
+  int nc = min(CHUNK, n - c0);
+  int slot0 = c0 % RING;
+  const T* src = band + (int64_t)c0 * GF_LDB;
+  T* dst = ring + (int64_t)slot0 * GF_LDB;
+  for (int i = lane; i < nc * GF_LDB; i += 32) dst[i] = src[i];
+  for (int i = lane; i < nc; i += 32) rring[slot0 + i] = rhs[c0 + i];
+}
+
+__global__ void __launch_bounds__(32) k_band_solve(Batch b) {
+  int s = blockIdx.x;
+  StructState& st = b.state[s];
+  if (!iterating(st) || !st.need_solve) return;
+  const StructInfo inf = b.info[s];
+  const int n = inf.n_free;
+  const int lane = threadIdx.x;
+  extern __shared__ unsigned char smem_raw[];
+  double* ring = reinterpret_cast<double*>(smem_raw);
+  double* rring = ring + RING * GF_LDB;
+  const double* band = b.band + inf.band_off;
+  double* rhs = b.P + inf.dof_off;
+  double* U = b.U + (int64_t)inf.dof_off * GF_UW;
+  int fail = 0;
+  load_chunk(band, rhs, ring, rring, 0, n, lane);
+  load_chunk(band, rhs, ring, rring, 1, n, lane);
+  load_chunk(band, rhs, ring, rring, 2, n, lane);
+  __syncwarp();
+  for (int j = 0; j < n; ++j) {
+    if (j % CHUNK == 0 && j > 0) {
+      // chunk j/CHUNK + 2 goes into the slots of chunk j/CHUNK - 2 (finished)
+      load_chunk(band, rhs, ring, rring, j / CHUNK + 2, n, lane);
+      __syncwarp();
+    }
+    const double* pc = ring + (int64_t)(j % RING) * GF_LDB;
+    double piv = pc[GF_KB];
+    if (!(piv != 0.0) || !isfinite(piv)) fail = 1;
+    double inv = 1.0 / piv;
+    if (lane >= 1 && lane <= GF_KB && j + lane < n) {
+      double* cc = ring + (int64_t)((j + lane) % RING) * GF_LDB;
+      double u = cc[GF_KB - lane];
+      U[(int64_t)j * GF_UW + lane] = u;
+      double w = u * inv;
+#pragma unroll
+      for (int r = 1; r <= GF_KB; ++r) cc[GF_KB - lane + r] -= pc[GF_KB + r] * w;
+    } else if (lane == 0) {
+      U[(int64_t)j * GF_UW] = piv;
+      double yj = rring[j % RING];
+      rhs[j] = yj;  // forward-substituted right-hand side
+      double f = yj * inv;
+#pragma unroll
+      for (int r = 1; r <= GF_KB; ++r)
+        if (j + r < n) rring[(j + r) % RING] -= pc[GF_KB + r] * f;
+    } else if (lane > GF_KB && j + lane - GF_KB < n) {
+      // lanes 18..31: nothing to update; keep the warp converged
+    }
+    __syncwarp();
+  }
+  // back substitution: x_j = (y_j - sum_c U(j, j+c) x_{j+c}) / U(j, j)
+  __syncwarp();
+  double xw = 0.0;  // lane c holds x_{j+c}
+  for (int j = n - 1; j >= 0; --j) {
+    double uc = (lane >= 1 && lane <= GF_KB && j + lane < n) ? U[(int64_t)j * GF_UW + lane] : 0.0;
+    double sum = warp_sum(uc * xw);
+    double xj = 0.0;
+    if (lane == 0) xj = (rhs[j] - sum) / U[(int64_t)j * GF_UW];
+    xj = __shfl_sync(0xffffffffu, xj, 0);
+    double up = __shfl_up_sync(0xffffffffu, xw, 1);
+    xw = lane == 1 ? xj : up;
+    if (lane == 0) rhs[j] = xj;
+  }
+  if (lane == 0) st.info_fail = fail;
+}
+
+// UpdateDisps + CheckGLConvergence (reference src/Solution.cpp:390-423,
+// src/ConvergenceCriteria.cpp:289-458)
+__global__ void k_update(Batch b) {
+  int s = blockIdx.x;
+  StructState& st = b.state[s];
+  if (!iterating(st) || !st.need_solve) return;
+  const StructInfo inf = b.info[s];
+  const StructParams& p = b.params[s];
+  const double* P = b.P + inf.dof_off;
+  const int* d6 = b.dof_node6 + inf.dof_off;
+  Red3 inc{0.0, 0.0, 0}, val{0.0, 0.0, 0};
+  for (int i = threadIdx.x; i < inf.n_free; i += blockDim.x) {
+    int q = d6[i];
+    double x = P[i];
+    double nv = b.disp[q] + x;
+    b.disp[q] = nv;
+    double a = fabs(x), v = fabs(nv);
+    if (nan_or_huge(a)) inc.f = 1;
+    if (q % 6 < 3) { if (a > inc.a) inc.a = a; if (v > val.a) val.a = v; }
+    else { if (a > inc.b) inc.b = a; if (v > val.b) val.b = v; }
+  }
+  Red3 ri = block_red(inc);
+  Red3 rv = block_red(val);
+  if (threadIdx.x == 0) {
+    st.res_conv = 0;
+    if (ri.f) st.diverged = 1;
+    st.disp_crit = rv.a * p.disp_tol > p.disp_min * p.disp_tol ? p.disp_tol * rv.a : p.disp_min * p.disp_tol;
+    st.rot_crit = rv.b * p.rot_tol > p.rot_min * p.rot_tol ? p.rot_tol * rv.b : p.rot_min * p.rot_tol;
+    int conv = 1;
+    if (st.disp_crit > p.divergence_ref || st.rot_crit > p.divergence_ref) {
+      st.diverged = 1;
+      conv = 0;
+    } else {
+      if (inf.has_force && ri.a > st.disp_crit) conv = 0;
+      if (inf.has_moment && ri.b > st.rot_crit) conv = 0;
+    }
+    st.gl_conv = conv;
+    st.last_inc = fmax(ri.a, ri.b);
+  }
+}
+
+// Newton-loop end test, divergence, commit or bisection, step growth
+// (reference src/Static.cpp:236-298).
+__global__ void k_control(Batch b) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= b.n_struct) return;
+  StructState& st = b.state[s];
+  st.commit = 0;
+  if (st.phase != PH_ITER) {
+    if (st.phase == PH_START) atomicAdd(b.running, 1);
+    return;
+  }
+  const StructParams& p = b.params[s];
+  int both = st.res_conv && st.gl_conv;
+  if ((st.it == p.max_it && !both) || (st.need_solve && st.info_fail)) st.diverged = 1;
+  if (st.time_step < p.min_time_step && st.time != p.end_time) st.aborted = 1;
+  st.it++;
+  st.total_it++;
+  bool loop = !both && !st.diverged && !st.aborted;
+  if (loop) {
+    atomicAdd(b.running, 1);
+    return;
+  }
+  if (!st.diverged) {
+    st.converged_number++;
+    st.commit = 1;
+    st.convergence_counter++;
+    if (st.it <= p.min_it || st.convergence_counter >= p.conv_increase) {
+      st.time_step = st.time_step * p.inc_factor;
+      if (st.time_step > p.max_time_step) st.time_step = p.max_time_step;
+      st.convergence_counter = 0;
+    }
+  } else {
+    st.time -= st.time_step;
+    st.time_step = st.time_step / 2.0;
+    st.diverged = 0;
+    st.convergence_counter = 0;
+    st.bisections++;
+  }
+  if ((st.time < p.end_time || st.diverged) && !st.aborted) {
+    st.phase = PH_START;
+    atomicAdd(b.running, 1);
+  } else {
+    st.phase = st.aborted ? PH_ABORTED : PH_DONE;
+  }
+}
+
+// SaveConfiguration: element Gauss-point history ...
+__global__ void k_commit_elems(Batch b) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= b.n_elem) return;
+  int s = b.estruct[e];
+  if (!b.state[s].commit) return;
+  double d[18];
+  for (int j = 0; j < 3; ++j) {
+    int nd = b.enodes[3 * e + j];
+    for (int q = 0; q < 6; ++q) d[6 * j + q] = b.disp[(int64_t)nd * 6 + q];
+  }
+  BeamConst c = b.bconst[e];
+  BeamHist h = b.bhist[e];
+  BeamHistAux x = b.baux[e];
+  beam_commit(c, h, x, d);
+  b.bhist[e] = h;
+  b.baux[e] = x;
+}
+
+// ... and nodal configuration (reference src/Node.cpp:325-370)
+__global__ void k_commit_nodes(Batch b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.n_nodes) return;
+  int s = b.node_struct[i];
+  if (!b.state[s].commit) return;
+  double* c = b.copy + (int64_t)i * 6;
+  const double* d = b.disp + (int64_t)i * 6;
+  for (int k = 0; k < 3; ++k) c[k] += d[k];
+  V3<double> a1 = {{c[3], c[4], c[5]}}, a2 = {{d[3], d[4], d[5]}};
+  V3<double> a3 = rodrigues_compose(a2, a1);
+  for (int k = 0; k < 3; ++k) c[3 + k] = a3[k];
+  M3<double> Q = rodrigues(a3);
+  for (int k = 0; k < 9; ++k) b.Qn[(int64_t)i * 9 + k] = Q[k];
+}
+
+// Element-level entry (no batch): tangent and internal force, FP64.
+__global__ void __launch_bounds__(MOUNT_THREADS) k_beam_elements(int n, const BeamConst* cs, const BeamHist* hs,
+                                                                 const double* ds, double* Ks, double* fs) {
+  extern __shared__ unsigned char smem_raw[];
+  double* sM = reinterpret_cast<double*>(smem_raw);
+  const int tid = threadIdx.x;
+  int e = blockIdx.x * blockDim.x + tid;
+  if (e >= n) return;
+  const BeamConst& c = cs[e];
+  const BeamHist& h = hs[e];
+  double d[18];
+  for (int q = 0; q < 18; ++q) d[q] = ds[(int64_t)e * 18 + q];
+  BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
+  double* f = sM + (size_t)2 * 81 * MOUNT_THREADS + tid;
+  for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
+#pragma unroll 1
+  for (int g = 0; g < 2; ++g) {
+    BeamGP kin;
+    beam_kinematics(c, h, ip[g], g, kin);
+    beam_gp_force(c, kin, g, f, MOUNT_THREADS);
+    double* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
+    beam_gp_operator<double>(c, kin, M, MOUNT_THREADS);
+    rotate_blocks9<double>(c, M, MOUNT_THREADS);
+  }
+  double* K = Ks + (int64_t)e * 324;
+#pragma unroll 1
+  for (int r = 0; r < 18; ++r)
+#pragma unroll 1
+    for (int q = 0; q < 18; ++q)
+      K[r + 18 * q] = beam_K_entry<double>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, r, q, MOUNT_THREADS);
+  for (int q = 0; q < 18; ++q) fs[(int64_t)e * 18 + q] = f[q * MOUNT_THREADS];
+}
+
+__global__ void k_beam_commit(int n, const BeamConst* cs, BeamHist* hs, BeamHistAux* xs, const double* ds) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double d[18];
+  for (int q = 0; q < 18; ++q) d[q] = ds[(int64_t)e * 18 + q];
+  BeamHist h = hs[e];
+  BeamHistAux x = xs[e];
+  beam_commit(cs[e], h, x, d);
+  hs[e] = h;
+  xs[e] = x;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+void launch_beam_commit(int n, const BeamConst* c, BeamHist* h, BeamHistAux* x, const double* d, cudaStream_t st) {
+  if (n > 0) k_beam_commit<<<(n + 127) / 128, 128, 0, st>>>(n, c, h, x, d);
+}
+
+void launch_init_state(const Batch& b, cudaStream_t st) {
+  if (b.n_struct == 0) return;
+  k_init_state<<<(b.n_struct + 127) / 128, 128, 0, st>>>(b);
+}
+
+static bool g_attr_set = false;
+
+static void set_attrs();
+
+void launch_iteration_partial(const Batch& b, cudaStream_t st) {
+  set_attrs();
+  int ns = b.n_struct;
+  k_step_begin<<<ns, 256, 0, st>>>(b);
+  k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
+  for (int c = 0; c < b.n_colors; ++c) {
+    int cnt = b.color_off[c + 1] - b.color_off[c];
+    if (cnt <= 0) continue;
+    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b, c);
+  }
+  k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
+  k_residual<<<ns, 256, 0, st>>>(b);
+}
+
+static void set_attrs() {
+  if (!g_attr_set) {
+    cudaFuncSetAttribute(k_beam_mount<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         MOUNT_SMEM);
+    cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (RING * GF_LDB + RING) * (int)sizeof(double));
+    g_attr_set = true;
+  }
+}
+
+void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels) {
+  set_attrs();
+  int ns = b.n_struct;
+  k_step_begin<<<ns, 256, 0, st>>>(b);
+  k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
+  for (int c = 0; c < b.n_colors; ++c) {
+    int cnt = b.color_off[c + 1] - b.color_off[c];
+    if (cnt <= 0) continue;
+    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS,
+                           MOUNT_SMEM, st>>>(b, c);
+  }
+  k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
+  k_residual<<<ns, 256, 0, st>>>(b);
+  launch_band_solve(b, st);
+  k_update<<<ns, 256, 0, st>>>(b);
+  k_control<<<(ns + 127) / 128, 128, 0, st>>>(b);
+  if (commit_kernels) {
+    if (b.n_elem) k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
+    if (b.n_nodes) k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b);
+  }
+}
+
+void launch_band_solve(const Batch& b, cudaStream_t st) {
+  k_band_solve<<<b.n_struct, 32, (RING * GF_LDB + RING) * sizeof(double), st>>>(b);
+}
+
+void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const double* d, double* K,
+                          double* f, cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_beam_elements, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
+    attr = true;
+  }
+  k_beam_elements<<<(n + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(n, c, h, d, K, f);
+}
+
+}  // namespace gf

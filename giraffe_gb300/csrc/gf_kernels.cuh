@@ -1,0 +1,45 @@
+// Kernels of the device-resident Newton loop for batches of Beam_1
+// structures.  One pass of the loop ("iteration") runs, for every structure
+// whose step is in progress:
+//
+//   step_begin   load-step start: time advance, zero increments, prescribed
+//                displacements (reference src/Static.cpp:176-197)
+//   zero         clear K_AA band and P (reference src/Solution.cpp:833-849)
+//   beam_mount   per colour: element tangent + internal force, scattered into
+//                the band and P (reference src/Beam_1.cpp:695-843, 1429-1492)
+//   loads        nodal loads, pseudo-moments, load stiffness
+//                (reference src/NodalLoad.cpp:322-401)
+//   residual     P = -P, criteria at the first iteration, residual check
+//                (reference src/Static.cpp:210-221, ConvergenceCriteria.cpp)
+//   band_solve   K_AA x = P (replaces sparsesystem, src/SparseMatrix.cpp:74-166)
+//   update       UpdateDisps + increment check (src/Solution.cpp:390-423,
+//                src/ConvergenceCriteria.cpp:289-458)
+//   control      divergence, bisection, step growth (src/Static.cpp:236-298)
+//   commit       SaveConfiguration (src/Node.cpp:325-370, Beam_1 1494-1506)
+//
+// Structures that are not iterating skip every kernel, so one launch
+// sequence (captured as a CUDA graph) serves structures at different load
+// steps.
+#pragma once
+#include "gf_types.h"
+
+namespace gf {
+
+void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels = true);
+// First half of a pass (step start, zero, mount, loads, residual): leaves the
+// assembled K_AA and P_A of the first iteration in the batch buffers.
+void launch_iteration_partial(const Batch& b, cudaStream_t st);
+// Commit of n standalone elements with nodal increments d ([n][18]).
+void launch_beam_commit(int n, const BeamConst* c, BeamHist* h, BeamHistAux* x, const double* d, cudaStream_t st);
+void launch_init_state(const Batch& b, cudaStream_t st);
+
+// Element-level entry: tangent (18x18 column-major) and internal force of n
+// elements in the global frame, FP64.  d: [n][18] nodal increments.
+void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const double* d, double* K,
+                          double* f, cudaStream_t st);
+
+// Band factor + solve of independent systems in the batch layout
+// (GF_LDB rows); FP64.  Returns per-system info in state[].info_fail.
+void launch_band_solve(const Batch& b, cudaStream_t st);
+
+}  // namespace gf

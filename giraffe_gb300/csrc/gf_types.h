@@ -1,0 +1,154 @@
+// Device data layout of a batch of structures (shared by host and device
+// code).  A batch holds many independent structures; nodes, elements and free
+// DOFs of each structure are contiguous ranges of the batch-wide arrays.
+//
+// HBM layout (all structure-of-arrays over the batch):
+//   nodes     disp[6], copy[6] (position + accumulated Rodrigues vector),
+//             Qn[9], gl[6] (local free index or -1), node_struct
+//   elements  enodes[3], estruct, BeamConst (PreCalc constants),
+//             BeamHist (Gauss-point history read by Mount), BeamHistAux
+//             (u_i, alpha_i written at commit)
+//   DOFs      dof_node6 (node*6 + k of each free DOF), P (residual, then the
+//             Newton increment), y (forward-substituted right-hand side)
+//   band      per structure, column-major with GF_LDB = 2*GF_KB+1 rows:
+//             entry (i, j) of K_AA at band[(GF_KB + i - j) + j*GF_LDB]
+//             (the reference's BandMatrix GB layout without the kl fill rows,
+//             reference src/BandMatrix.cpp:214,246), FP64 and an FP32 copy
+//   factor    U rows: n_free x (GF_KB+1), [j][c] = U(j, j+c)
+#pragma once
+#include <stdint.h>
+
+#define GF_KB 17
+#define GF_LDB (2 * GF_KB + 1)
+#define GF_UW (GF_KB + 1)
+
+namespace gf {
+
+struct BeamConst {
+  double T3[9];
+  double Dd[6];
+  double D34;
+  double e3r[3];
+  double jac;
+  double N[2][3];
+  double dN[2][3];
+  double Mr;
+  double Jr[9];
+};
+
+struct BeamHist {
+  double Q[2][9];
+  double dz[2][3];
+  double kap[2][3];
+};
+
+struct BeamHistAux {
+  double u[2][3];
+  double alpha[2][3];
+};
+
+enum Phase : int { PH_START = 0, PH_ITER = 1, PH_DONE = 2, PH_ABORTED = 3 };
+
+// Per-structure parameters (Static solution step + ConvergenceCriteria).
+struct StructParams {
+  double start_time, end_time, time_step0, max_time_step, min_time_step, inc_factor;
+  int max_it, min_it, conv_increase, pad0;
+  double force_tol, moment_tol, force_min, moment_min, disp_tol, rot_tol, disp_min, rot_min,
+      divergence_ref;
+};
+
+// Per-structure ranges in the batch arrays.
+struct StructInfo {
+  int node_off, n_nodes;
+  int elem_off, n_elem;
+  int dof_off, n_free;
+  int64_t band_off;  // in entries; band of n_free columns x GF_LDB
+  int has_force, has_moment;  // free translational / rotational DOFs exist
+  int load_off, n_loads;  // nodal load entries of this structure
+};
+
+// Per-structure Newton / load-step control state (reference
+// src/Static.cpp:140-311 as a state machine).
+struct StructState {
+  int phase;
+  int it;
+  int res_conv, gl_conv, diverged, aborted, need_solve, info_fail;
+  int convergence_counter, converged_number, n_conv_evaluated, total_it, bisections;
+  int commit;  // set by control for the commit kernel
+  int solve_sweeps;  // refinement sweeps of the last solve (mixed path)
+  int fp64_fallback;  // mixed path: this structure factors in FP64
+  double time, time_step, last_converged_time, current_time_step;
+  double force_crit, moment_crit, disp_crit, rot_crit;
+  double last_res, last_inc;
+};
+
+// One nodal load entry (one node of a NodalLoad node set).
+struct LoadEntry {
+  int structure;
+  int node;  // batch-wide node index
+  int table;  // index into the table arrays
+  int pad;
+  double CQ[9];  // coordinate system rows (E1, E2, E3)
+  double mult[6];
+};
+
+// One prescribed-displacement node (one node of a NodalDisplacement set).
+struct DispEntry {
+  int structure;
+  int node;
+  int table;
+  int pad;
+  double CQ[9];
+};
+
+struct TableDev {
+  int n_times, n_cols;
+  int64_t off;  // into the batch's table storage: times then values
+};
+
+// Device pointers of a batch.
+struct Batch {
+  int n_struct, n_nodes, n_elem, n_free;
+  int n_loads, n_disps, n_tables;
+  // nodes
+  double* disp;
+  double* copy;
+  double* Qn;
+  int* gl;
+  int* cons;
+  int* node_struct;
+  // elements
+  int* enodes;
+  int* estruct;
+  BeamConst* bconst;
+  BeamHist* bhist;
+  BeamHistAux* baux;
+  int* color_elems;  // elements grouped by colour
+  int color_off[9];  // colour c = color_elems[color_off[c] .. color_off[c+1])
+  int n_colors;
+  // DOFs
+  int* dof_node6;
+  double* P;
+  double* y;
+  double* xr;  // refinement: accumulated solution
+  double* r;   // refinement: residual
+  // band and factor
+  double* band;
+  float* band32;
+  double* U;
+  float* U32;
+  // structures
+  StructInfo* info;
+  StructParams* params;
+  StructState* state;
+  // loads
+  LoadEntry* loads;
+  DispEntry* disps;
+  TableDev* tables;
+  double* table_data;
+  int mixed;  // 1: FP32 factor with FP64 refinement
+  int max_refine;
+  int* running;  // structures still running after the last pass
+};
+
+}  // namespace gf

@@ -1,0 +1,189 @@
+"""ctypes binding of libgiraffe_gpu.so (include/giraffe_gpu.h).
+
+The CUDA library is the only implementation: importing this module loads it
+and raises if it is missing; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .model import Structure, gf_model_desc
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgiraffe_gpu.so")
+
+GF_PREC_FP64, GF_PREC_MIXED = 0, 1
+
+EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_batch_create",
+           "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",
+           "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
+           "gf_beam_elements", "gf_band_solve"]
+
+
+class gf_solve_opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("max_refine", C.c_int), ("poll_every", C.c_int),
+                ("use_graph", C.c_int)]
+
+
+class gf_stats(C.Structure):
+    _fields_ = [("converged_steps", C.c_int), ("newton_iterations", C.c_int), ("bisections", C.c_int),
+                ("aborted", C.c_int), ("linear_solves", C.c_int), ("fp64_fallback", C.c_int),
+                ("pad", C.c_int * 2)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"CUDA library {LIB_PATH} is not built; run giraffe_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+        L.gf_create.restype = vp
+        L.gf_create.argtypes = [C.c_int]
+        L.gf_destroy.argtypes = [vp]
+        L.gf_last_error.restype = C.c_char_p
+        L.gf_last_error.argtypes = [vp]
+        L.gf_default_opts.argtypes = [C.POINTER(gf_solve_opts)]
+        L.gf_batch_create.restype = vp
+        L.gf_batch_create.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts)]
+        L.gf_batch_destroy.argtypes = [vp]
+        L.gf_batch_reset.argtypes = [vp]
+        L.gf_batch_run.argtypes = [vp]
+        L.gf_batch_results.argtypes = [vp, C.POINTER(dp), C.POINTER(gf_stats)]
+        L.gf_batch_last_ms.restype = C.c_double
+        L.gf_batch_last_ms.argtypes = [vp]
+        L.gf_batch_last_launches.restype = C.c_longlong
+        L.gf_batch_last_launches.argtypes = [vp]
+        L.gf_batch_assemble.argtypes = [vp, C.c_int, dp, dp, ip]
+        L.gf_solve.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts),
+                               C.POINTER(dp), C.POINTER(gf_stats)]
+        L.gf_beam_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
+        L.gf_band_solve.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        self.h = self.L.gf_create(device)
+        if not self.h:
+            raise RuntimeError("gf_create failed (no CUDA device?)")
+
+    def close(self):
+        if self.h:
+            self.L.gf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self) -> str:
+        return self.L.gf_last_error(self.h).decode()
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
+
+    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=6):
+        o = gf_solve_opts()
+        self.L.gf_default_opts(C.byref(o))
+        o.precision, o.use_graph, o.poll_every, o.max_refine = precision, int(use_graph), poll_every, max_refine
+        return o
+
+    def beam_elements(self, xyz, mat, sec, cs, hist_disp, disp):
+        n = xyz.shape[0]
+        nh = 0 if hist_disp is None else hist_disp.shape[1]
+        K = np.zeros((n, 324))
+        f = np.zeros((n, 18))
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz, mat, sec, cs, disp)]
+        hd = np.ascontiguousarray(hist_disp if nh else np.zeros((n, 1, 18)), dtype=np.float64)
+        self.check(self.L.gf_beam_elements(self.h, n, _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]), _dp(arrs[3]), nh,
+                                           _dp(hd), _dp(arrs[4]), _dp(K), _dp(f)), "gf_beam_elements")
+        return K.reshape(n, 18, 18).transpose(0, 2, 1), f
+
+    def band_solve(self, ab, kl, ku, b):
+        ab = np.ascontiguousarray(ab, dtype=np.float64)  # [n][ldab] (column j contiguous)
+        n, ldab = ab.shape
+        x = np.ascontiguousarray(b, dtype=np.float64).copy()
+        info = C.c_int(0)
+        self.check(self.L.gf_band_solve(self.h, n, kl, ku, _dp(ab), ldab, _dp(x), C.byref(info)), "gf_band_solve")
+        return x, info.value
+
+
+class BatchSolver:
+    """A device-resident batch of structures (gf_batch_*)."""
+
+    def __init__(self, ctx: Context, structures, opts=None):
+        self.ctx = ctx
+        self.structures = list(structures)
+        self.handles = [s.desc() for s in self.structures]
+        self.descs = (gf_model_desc * len(self.handles))(*[h.desc for h in self.handles])
+        o = opts or ctx.opts()
+        self.h = ctx.L.gf_batch_create(ctx.h, len(self.handles), self.descs, C.byref(o))
+        if not self.h:
+            raise RuntimeError("gf_batch_create failed: " + ctx.error())
+
+    def close(self):
+        if self.h:
+            self.ctx.L.gf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self):
+        self.ctx.check(self.ctx.L.gf_batch_reset(self.h), "gf_batch_reset")
+
+    def run(self):
+        self.ctx.check(self.ctx.L.gf_batch_run(self.h), "gf_batch_run")
+        return self.ctx.L.gf_batch_last_ms(self.h)
+
+    def launches(self):
+        return self.ctx.L.gf_batch_last_launches(self.h)
+
+    def results(self):
+        outs = [np.zeros((s.n_nodes, 15)) for s in self.structures]
+        ptrs = (C.POINTER(C.c_double) * len(outs))(*[_dp(o) for o in outs])
+        stats = (gf_stats * len(outs))()
+        self.ctx.check(self.ctx.L.gf_batch_results(self.h, ptrs, stats), "gf_batch_results")
+        st = np.array([[x.converged_steps, x.newton_iterations, x.bisections, x.aborted] for x in stats])
+        return outs, st
+
+    def assemble(self, s: int):
+        dims = (C.c_int * 2)()
+        self.ctx.check(self.ctx.L.gf_batch_assemble(self.h, s, None, None, dims), "gf_batch_assemble")
+        n, kb = dims[0], dims[1]
+        ab = np.zeros((n, 3 * kb + 1))
+        P = np.zeros(n)
+        self.ctx.check(self.ctx.L.gf_batch_assemble(self.h, s, _dp(ab), _dp(P), dims), "gf_batch_assemble")
+        return ab, P, kb
+
+
+def solve(structures, precision=GF_PREC_FP64, device=0):
+    """Solves every structure's solution step on the GPU; returns final nodal
+    states (n_nodes x 15 each) and stats rows (converged steps, Newton
+    iterations, bisections, aborted)."""
+    ctx = Context(device)
+    b = BatchSolver(ctx, structures, ctx.opts(precision))
+    b.reset()
+    b.run()
+    out = b.results()
+    b.close()
+    ctx.close()
+    return out

@@ -1,0 +1,123 @@
+/*
+ * giraffe_gpu.h — C ABI of the GB300 implementation of GIRAFFE's implicit
+ * Beam_1 finite-element step.
+ *
+ * Every function is extern "C", takes plain pointers and sizes, returns an
+ * int status (0 = success) unless stated otherwise, and records a message
+ * for gf_last_error on failure.  Host arrays are owned by the caller.  A
+ * context owns one CUDA stream on one device; calls on one context must not
+ * overlap.
+ *
+ * Reference interfaces each entry point replaces (paths in the reference
+ * repository alfredogneto/GIRAFFE):
+ *   gf_solve / gf_batch_*   Solution::Solve of a Static solution step for one
+ *                           or many structures: src/Static.cpp:140-311 with
+ *                           Solution::MountLocal/MountGlobal/UpdateDisps/
+ *                           SaveConfiguration/RestoreConfiguration
+ *                           (src/Solution.cpp:227-575) and the
+ *                           ConvergenceCriteria checks
+ *                           (src/ConvergenceCriteria.cpp:187-618)
+ *   gf_beam_elements        Beam_1::PreCalc + SaveLagrange + Mount +
+ *                           MountElementLoads (src/Beam_1.cpp:501-843,
+ *                           1494-1506)
+ *   gf_batch_assemble       MountLocal + MountLoads + MountGlobal +
+ *                           SparseMatrix::Mount into the BandMatrix layout
+ *                           (src/Solution.cpp:227-349, src/SparseMatrix.cpp:58-71,
+ *                           src/BandMatrix.cpp:221-250)
+ *   gf_band_solve           bandsystem (src/BandMatrix.cpp:257-287) and the
+ *                           Newton solve sparsesystem (src/SparseMatrix.cpp:74-166)
+ *                           for banded K_AA
+ */
+#ifndef GIRAFFE_GPU_H
+#define GIRAFFE_GPU_H
+#include <stddef.h>
+
+#include "giraffe_model.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gf_ctx gf_ctx;
+typedef struct gf_batch gf_batch;
+
+enum {
+  GF_OK = 0,
+  GF_ERR_ARG = 1,      /* invalid argument or unsupported model */
+  GF_ERR_CUDA = 2,     /* CUDA runtime error */
+  GF_ERR_SINGULAR = 3, /* zero or non-finite pivot (info_fail = 1 in the reference) */
+  GF_ERR_TIMEOUT = 4   /* a bounded device wait gave up */
+};
+
+enum { GF_PREC_FP64 = 0, GF_PREC_MIXED = 1 };
+
+typedef struct gf_solve_opts {
+  int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED */
+  int max_refine;  /* mixed: FP64 refinement sweeps before falling back to FP64 */
+  int poll_every;  /* Newton passes between host checks for completion */
+  int use_graph;   /* capture one Newton pass as a CUDA graph */
+} gf_solve_opts;
+
+/* Per-structure result of a solution step. */
+typedef struct gf_stats {
+  int converged_steps;    /* converged load steps */
+  int newton_iterations;  /* Newton passes (element mounts) */
+  int bisections;         /* rolled-back steps */
+  int aborted;            /* 1 when the step size fell below MinTimeStep */
+  int linear_solves;      /* linear solves performed */
+  int fp64_fallback;      /* mixed precision: structure switched to FP64 */
+  int pad[2];
+} gf_stats;
+
+/* Context on CUDA device `device`; NULL on failure. */
+gf_ctx* gf_create(int device);
+void gf_destroy(gf_ctx* ctx);
+const char* gf_last_error(const gf_ctx* ctx);
+void gf_default_opts(gf_solve_opts* opts);
+
+/* Uploads n structures (each a Static step of Beam_1 elements with nodal
+ * loads, constraints and prescribed displacements) into one device batch. */
+gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts);
+void gf_batch_destroy(gf_batch* batch);
+/* Restores the initial configuration of every structure (device side). */
+int gf_batch_reset(gf_batch* batch);
+/* Runs every structure's solution step to its end (or abort) on the device. */
+int gf_batch_run(gf_batch* batch);
+/* Final nodal state per structure: final_nodes[s] holds n_nodes x 15 doubles
+ * (copy_coordinates: position and accumulated Rodrigues vector, then the
+ * nodal rotation tensor Q row-major); stats may be NULL. */
+int gf_batch_results(gf_batch* batch, double* const* final_nodes, gf_stats* stats);
+/* Device time of the last gf_batch_run in milliseconds (CUDA events on the
+ * batch's stream), and the number of kernels it launched. */
+double gf_batch_last_ms(const gf_batch* batch);
+long long gf_batch_last_launches(const gf_batch* batch);
+/* First Newton pass of structure s from its initial configuration: K_AA in
+ * the reference's BandMatrix storage (LAPACK GB, ldab = 3*kb + 1 rows, kb =
+ * the structure's half-bandwidth, n_free columns) and P_A after the sign
+ * flip.  dims (optional) receives n_free and kb. */
+int gf_batch_assemble(gf_batch* batch, int s, double* ab, double* PA, int* dims);
+
+/* Convenience: create, run, fetch results and destroy. */
+int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts,
+             double* const* final_nodes, gf_stats* stats);
+
+/* n independent Beam_1 elements: PreCalc from nodal coordinates (n x 9),
+ * material (n x 3: E, nu, rho), section (n x 6: A, I11, I22, I12, It, I33)
+ * and CS (n x 6: E1, E3); n_hist committed increments per element
+ * (n x n_hist x 18) build the Gauss-point history; then Mount at disp
+ * (n x 18).  K: n x 324 (column-major 18x18), f: n x 18 (P_loading). */
+int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
+                     const double* cs, int n_hist, const double* hist_disp, const double* disp, double* K,
+                     double* f);
+
+/* Solves A x = b for a banded matrix given in the reference's BandMatrix
+ * storage (LAPACK GB: entry (i,j) at ab[(kl+ku+i-j) + j*ldab], ldab >=
+ * 2*kl+ku+1), without pivoting, FP64; kl, ku <= 17.  b is overwritten by x.
+ * *info receives 0 or 1 (zero or non-finite pivot), as bandsystem's
+ * info_fail. */
+int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,93 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE: the checker and the timed CPU baseline; never used by
+the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build_oracle.build())
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+        _lib.oracle_solve.argtypes = [C.c_void_p, C.c_void_p, dp, ip]
+        _lib.oracle_solve_batch.argtypes = [C.c_int, C.c_void_p, C.POINTER(dp), ip, C.c_int]
+        _lib.oracle_beam_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
+        _lib.oracle_first_tangent.argtypes = [C.c_void_p, dp, dp, ip]
+    return _lib
+
+
+class Record(C.Structure):
+    _fields_ = [("cap", C.c_int), ("n", C.c_int), ("time", C.POINTER(C.c_double)),
+                ("iterations", C.POINTER(C.c_int)), ("nodes", C.POINTER(C.c_double)),
+                ("gp_Q", C.POINTER(C.c_double))]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def solve(structure, record_cap: int = 0):
+    """Runs one structure.  Returns (final nodes [n_nodes x 15], stats
+    [converged steps, Newton iterations, bisections, aborted], record dict)."""
+    h = structure.desc()
+    final = np.zeros((structure.n_nodes, 15))
+    stats = (C.c_int * 4)()
+    rec = None
+    rd = None
+    if record_cap:
+        t = np.zeros(record_cap)
+        it = np.zeros(record_cap, np.int32)
+        nodes = np.zeros((record_cap, structure.n_nodes, 15))
+        gq = np.zeros((record_cap, max(1, len(structure.beams)), 2, 9))
+        rec = Record(record_cap, 0, _dp(t), it.ctypes.data_as(C.POINTER(C.c_int)), _dp(nodes), _dp(gq))
+    lib().oracle_solve(C.cast(h.ref, C.c_void_p), C.byref(rec) if rec else None, _dp(final), stats)
+    if rec:
+        n = rec.n
+        rd = dict(time=t[:n], iterations=it[:n], nodes=nodes[:n], gp_Q=gq[:n])
+    return final, np.array(list(stats)), rd
+
+
+def solve_batch(structures, threads: int = 1):
+    hs = [s.desc() for s in structures]
+    from giraffe_gb300.model import gf_model_desc
+    arr = (gf_model_desc * len(hs))(*[h.desc for h in hs])
+    finals = [np.zeros((s.n_nodes, 15)) for s in structures]
+    ptrs = (C.POINTER(C.c_double) * len(finals))(*[_dp(f) for f in finals])
+    stats = np.zeros((len(hs), 4), np.int32)
+    fails = lib().oracle_solve_batch(len(hs), C.cast(arr, C.c_void_p), ptrs,
+                                     stats.ctypes.data_as(C.POINTER(C.c_int)), threads)
+    return finals, stats, fails
+
+
+def beam_element(xyz9, mat3, sec6, cs6, hist_disp, disp18):
+    K = np.zeros(324)
+    f = np.zeros(18)
+    hd = np.ascontiguousarray(hist_disp if hist_disp is not None and len(hist_disp) else np.zeros((1, 18)),
+                              dtype=np.float64)
+    nh = 0 if hist_disp is None else len(hist_disp)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz9, mat3, sec6, cs6, disp18)]
+    lib().oracle_beam_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), _dp(args[3]), nh, _dp(hd),
+                              _dp(args[4]), _dp(K), _dp(f))
+    return K.reshape(18, 18).T, f  # row-major [r][s]
+
+
+def first_tangent(structure):
+    h = structure.desc()
+    dims = (C.c_int * 2)()
+    lib().oracle_first_tangent(C.cast(h.ref, C.c_void_p), None, None, dims)
+    n, kl = dims[0], dims[1]
+    ab = np.zeros((n, 3 * kl + 1))
+    P = np.zeros(n)
+    lib().oracle_first_tangent(C.cast(h.ref, C.c_void_p), _dp(ab), _dp(P), dims)
+    return ab, P, kl

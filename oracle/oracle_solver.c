@@ -496,3 +496,24 @@ int oracle_beam_element(const double* xyz9, const double* mat3, const double* se
   oracle_beam_mount(&c, &h, disp18, K, f, NULL);
   return 0;
 }
+
+/* Tangent and residual of the first Newton iteration of the first load step
+ * (all increments zero): K_AA in GB storage (ldab = 3 kl + 1, column-major,
+ * n_free columns) and P_A.  dims receives n_free and kl.  With ab == NULL only
+ * dims is filled. */
+int oracle_first_tangent(const gf_model_desc* m, double* ab, double* PA, int* dims) {
+  ost s;
+  ost_init(&s, m);
+  dims[0] = s.n_free;
+  dims[1] = s.kl;
+  if (ab) {
+    s.last_converged_time = m->solution.start_time;
+    s.current_time_step = m->solution.time_step;
+    mount_displacements(&s);
+    assemble(&s);
+    memcpy(ab, s.ab, sizeof(double) * (size_t)s.ldab * (size_t)s.n_free);
+    memcpy(PA, s.PA, sizeof(double) * (size_t)s.n_free);
+  }
+  ost_free(&s);
+  return 0;
+}

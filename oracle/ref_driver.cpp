@@ -290,8 +290,11 @@ int giraffe_ref_element_mount(int e, double* K, double* P) {
 
 // Commits the current increments as converged (reference
 // src/Solution.cpp:426-530 for nodes and elements) and zeroes them
-// (reference src/Solution.cpp:798-814).
+// (reference src/Solution.cpp:798-814).  SaveLagrange reads the Gauss-point
+// quantities of the last Mount, so every element is mounted at the committed
+// increments first, as the converged Newton iteration does.
 void giraffe_ref_commit() {
+  for (int i = 0; i < db.number_elements; ++i) db.elements[i]->Mount();
   for (int i = 0; i < db.number_nodes; ++i) db.nodes[i]->SaveConfiguration();
   for (int i = 0; i < db.number_elements; ++i) db.elements[i]->SaveLagrange();
   for (int i = 0; i < db.number_nodes; ++i)

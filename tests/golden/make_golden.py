@@ -1,0 +1,192 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own Beam_1 / Static sources, compiled by
+oracle/build_ref.py into oracle/_ref/libgiraffe_ref.so (this needs the
+reference tree, so it runs only where that tree is present), on decks written
+in the reference's .inp syntax by giraffe_gb300.model.Structure.to_inp, and
+stores what the reference computes:
+
+* ref_beam_elements.npz  Beam_1 tangent K (18x18) and unbalanced force P (18)
+                         of single elements with random geometry, section,
+                         coordinate system, committed history and increment
+                         (Beam_1::PreCalc, SaveLagrange, Mount,
+                         MountElementLoads).
+* ref_tutorial01.npz     the reference's tutorial01 cantilever, every
+                         converged configuration the reference writes
+                         (Sample 2) and its Newton solve counts.
+* ref_rollup.npz         20-element roll-up into a circle, every step.
+* ref_chain.npz          a 30-element pipe chain under a tip force, 10 steps.
+
+Node records hold copy_coordinates (position and accumulated Rodrigues
+vector) then the nodal Q (row-major); Gauss-point records hold Q_i
+(row-major).
+
+    python tests/golden/make_golden.py
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from giraffe_gb300 import configs  # noqa: E402
+from giraffe_gb300.model import NodalLoad, Solution, Structure, Table  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "libgiraffe_ref.so")
+
+
+def ref_lib():
+    if not os.path.exists(REF):
+        subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "build_ref.py")], check=True)
+    L = C.CDLL(REF)
+    dp = C.POINTER(C.c_double)
+    L.giraffe_ref_load.argtypes = [C.c_char_p]
+    L.giraffe_ref_solve.argtypes = [C.c_char_p, C.c_char_p]
+    L.giraffe_ref_set_increment.argtypes = [C.c_int, dp]
+    L.giraffe_ref_element_mount.argtypes = [C.c_int, dp, dp]
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def parse_rec(path):
+    recs = []
+    cur = None
+    for line in open(path):
+        p = line.split()
+        if p[0] == "T":
+            cur = {"t": float(p[2]), "N": [], "G": []}
+            recs.append(cur)
+        elif p[0] == "N":
+            v = [float(x) for x in p[2:]]
+            q = np.array(v[6:]).reshape(3, 3).T.ravel()  # column-major -> row-major
+            cur["N"].append(v[:6] + list(q))
+        elif p[0] == "G":
+            v = [float(x) for x in p[3:]]
+            cur["G"].append(list(np.array(v).reshape(3, 3).T.ravel()))
+    times = np.array([r["t"] for r in recs])
+    nodes = np.array([r["N"] for r in recs])
+    gq = np.array([np.array(r["G"]).reshape(-1, 2, 9) for r in recs])
+    return times, nodes, gq
+
+
+def parse_log(path):
+    """Per load step: (time, Newton solves, diverged)."""
+    steps = []
+    for line in open(path):
+        m = re.match(r"Time: ([0-9.eE+-]+)", line)
+        if m:
+            steps.append([float(m.group(1)), 0, 0])
+        elif line.startswith("It.:"):
+            steps[-1][1] += 1
+        elif "diverged" in line:
+            steps[-1][2] = 1
+    return np.array(steps)
+
+
+def run_deck(L, s, tag, tmp):
+    deck = os.path.join(tmp, tag + ".inp")
+    with open(deck, "w") as f:
+        f.write(s.to_inp())
+    assert L.giraffe_ref_load(deck.encode()) == 0, tag
+    rec = os.path.join(tmp, tag + ".rec")
+    log = os.path.join(tmp, tag + ".log")
+    rc = L.giraffe_ref_solve(rec.encode(), log.encode())
+    times, nodes, gq = parse_rec(rec)
+    steps = parse_log(log)
+    return dict(rc=np.array(rc), times=times, nodes=nodes, gp_Q=gq, steps=steps, deck=np.array(s.to_inp()))
+
+
+def element_cases(rng, n):
+    cases = []
+    for k in range(n):
+        # random element geometry along a random axis, CS with E3 on the axis
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        L = rng.uniform(0.2, 2.0)
+        x0 = rng.normal(size=3)
+        xyz = np.array([x0, x0 + 0.5 * L * axis, x0 + L * axis])
+        t = rng.normal(size=3)
+        e1 = t - t.dot(axis) * axis
+        e1 /= np.linalg.norm(e1)
+        if k % 3 == 0:
+            sec = ("rect", rng.uniform(0.05, 0.2), rng.uniform(0.05, 0.2))
+        else:
+            De = rng.uniform(0.2, 0.5)
+            sec = ("tube", De, De - 2 * rng.uniform(0.01, 0.04))
+        mat = (rng.uniform(5e9, 2.5e11), rng.uniform(0.2, 0.4), 7850.0)
+        nh = int(rng.integers(0, 4))
+        scale = np.array([0.02 * L] * 3 + [0.15] * 3)
+        hist = rng.normal(size=(nh, 3, 6)) * scale
+        disp = rng.normal(size=(3, 6)) * scale
+        cases.append(dict(xyz=xyz, e1=e1, e3=axis, sec=sec, mat=mat, hist=hist, disp=disp))
+    return cases
+
+
+def run_elements(L, cases, tmp):
+    out = {k: [] for k in ("xyz", "mat", "sec6", "cs", "hist", "disp", "K", "P")}
+    for i, c in enumerate(cases):
+        s = Structure(nodes=c["xyz"])
+        mat = s.add_material(*c["mat"])
+        sec = s.add_rectangle(c["sec"][1], c["sec"][2]) if c["sec"][0] == "rect" else s.add_tube(c["sec"][1], c["sec"][2])
+        cs = s.add_cs(c["e1"], c["e3"])
+        s.beams.append((0, 1, 2, mat, sec, cs))
+        deck = os.path.join(tmp, f"el{i}.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        L.giraffe_ref_prepare()
+        for h in c["hist"]:
+            for n in range(3):
+                v = np.ascontiguousarray(h[n])
+                L.giraffe_ref_set_increment(n + 1, _dp(v))
+            L.giraffe_ref_commit()
+        for n in range(3):
+            v = np.ascontiguousarray(c["disp"][n])
+            L.giraffe_ref_set_increment(n + 1, _dp(v))
+        K = np.zeros(324)
+        P = np.zeros(18)
+        assert L.giraffe_ref_element_mount(1, _dp(K), _dp(P)) == 18
+        hist = np.zeros((3, 18))
+        hist[: len(c["hist"])] = c["hist"].reshape(-1, 18)
+        out["xyz"].append(c["xyz"].ravel())
+        out["mat"].append(np.array(s.materials[0]))
+        out["sec6"].append(np.array(s.sections[0]))
+        out["cs"].append(np.array(s.cs[0]))
+        out["hist"].append(hist)
+        out["disp"].append(c["disp"].ravel())
+        out["K"].append(K.reshape(18, 18).T)  # row-major [r][s]
+        out["P"].append(P)
+    res = {k: np.array(v) for k, v in out.items()}
+    res["n_hist"] = np.array([len(c["hist"]) for c in cases])
+    return res
+
+
+def small_chain():
+    return configs.pipe_chain(30, 0.4, 0.03, [1.5e5, -1.0e5, 0.8e5], element_length=10.0 / 30)
+
+
+def main():
+    L = ref_lib()
+    rng = np.random.default_rng(20261203)
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, "ref_beam_elements.npz"), **run_elements(L, element_cases(rng, 24), tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_tutorial01.npz"), **run_deck(L, configs.tutorial01(), "t01", tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_rollup.npz"), **run_deck(L, configs.cantilever_rollup(), "roll", tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_chain.npz"), **run_deck(L, small_chain(), "chain", tmp))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

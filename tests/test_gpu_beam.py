@@ -1,0 +1,138 @@
+"""CUDA path (libgiraffe_gpu.so, through its C ABI) against the oracle and
+the reference's golden fixtures.  FP64 throughout: the plain path must match
+the reference's CPU result to 1e-10 relative (stated tolerance); element
+matrices agree to 1e-12."""
+import numpy as np
+import pytest
+
+from giraffe_gb300 import configs
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_beam_elements_match_reference(gpu_ctx, golden):
+    g = golden("ref_beam_elements.npz")
+    n = len(g["K"])
+    # uniform history depth per call: group by n_hist
+    for nh in sorted(set(int(x) for x in g["n_hist"])):
+        idx = [i for i in range(n) if int(g["n_hist"][i]) == nh]
+        hist = np.stack([g["hist"][i][:nh] for i in idx]) if nh else None
+        K, f = gpu_ctx.beam_elements(g["xyz"][idx], g["mat"][idx], g["sec6"][idx], g["cs"][idx], hist, g["disp"][idx])
+        for k, i in enumerate(idx):
+            assert rel(K[k], g["K"][i]) < 1e-12, i
+            assert rel(f[k], g["P"][i]) < 1e-12, i
+
+
+def _band_matrix(rng, n, kl, ku):
+    A = np.zeros((n, n))
+    for i in range(n):
+        for j in range(max(0, i - kl), min(n, i + ku + 1)):
+            A[i, j] = rng.normal()
+        A[i, i] += 4 * (kl + ku + 1)
+    return A
+
+
+def _to_gb(A, kl, ku):
+    n = A.shape[0]
+    ldab = 2 * kl + ku + 1
+    ab = np.zeros((n, ldab))
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            ab[j, kl + ku + i - j] = A[i, j]
+    return ab
+
+
+@pytest.mark.parametrize("n,kl,ku", [(1, 0, 0), (7, 2, 3), (100, 17, 17), (1000, 17, 5), (333, 4, 17)])
+def test_band_solve_matches_dense(gpu_ctx, n, kl, ku):
+    rng = np.random.default_rng(n + 31 * kl + ku)
+    A = _band_matrix(rng, n, kl, ku)
+    b = rng.normal(size=n)
+    x, info = gpu_ctx.band_solve(_to_gb(A, kl, ku), kl, ku, b)
+    assert info == 0
+    assert rel(x, np.linalg.solve(A, b)) < 1e-12
+
+
+def test_band_solve_reports_zero_pivot(gpu_ctx):
+    A = np.diag([1.0, 0.0, 2.0, 3.0])
+    _, info = gpu_ctx.band_solve(_to_gb(A, 1, 1), 1, 1, np.ones(4))
+    assert info == 1
+
+
+def test_first_assembly_matches_oracle(gpu_ctx):
+    from giraffe_gb300 import gpu
+
+    structs = [configs.cantilever_rollup(), configs.tutorial01(), configs.pipe_chain(57, 0.35, 0.025, [1e5, 2e4, -3e4])]
+    b = gpu.BatchSolver(gpu_ctx, structs)
+    for s, st in enumerate(structs):
+        ab, P, kb = b.assemble(s)
+        ab_o, P_o, kl_o = oracle.first_tangent(st)
+        assert kb == kl_o
+        # oracle storage has kl fill rows on top: ldab = 3 kl + 1 in both
+        assert rel(ab, ab_o) < 1e-13
+        assert rel(P, P_o) < 1e-13
+    b.close()
+
+
+def _solve_gpu(ctx, structs, precision=0):
+    from giraffe_gb300 import gpu
+
+    b = gpu.BatchSolver(ctx, structs, ctx.opts(precision))
+    b.reset()
+    b.run()
+    out = b.results()
+    b.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ["ref_tutorial01.npz", "ref_rollup.npz", "ref_chain.npz"])
+def test_static_solve_matches_reference(gpu_ctx, golden, name):
+    from tests.golden.make_golden import small_chain
+
+    s = {"ref_tutorial01.npz": configs.tutorial01, "ref_rollup.npz": configs.cantilever_rollup,
+         "ref_chain.npz": small_chain}[name]()
+    g = golden(name)
+    finals, stats = _solve_gpu(gpu_ctx, [s])
+    ref_final = g["nodes"][-1]
+    scale = np.abs(ref_final[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref_final[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(finals[0][:, 6:] - ref_final[:, 6:]).max() <= 1e-9
+    steps = g["steps"]
+    assert stats[0][0] == int((steps[:, 2] == 0).sum())
+    assert stats[0][3] == 0
+    # same Newton trajectory as the oracle
+    _, ost, _ = oracle.solve(s)
+    assert list(stats[0]) == list(ost)
+
+
+def test_batch_matches_oracle_and_is_order_independent(gpu_ctx):
+    structs = configs.batched_static(24, seed=11, n_min=20, n_max=300)
+    for s in structs:  # short chains of the benchmark family, fixed 10 m length
+        pass
+    finals, stats = _solve_gpu(gpu_ctx, structs)
+    for s, f, st in zip(structs, finals, stats):
+        fo, so, _ = oracle.solve(s)
+        assert list(st) == list(so)
+        scale = np.abs(fo[:, :3]).max()
+        assert np.abs(f[:, :3] - fo[:, :3]).max() <= 1e-10 * scale
+    # each result is the same alone and inside the batch (bit for bit)
+    alone, _ = _solve_gpu(gpu_ctx, [structs[5]])
+    assert np.array_equal(alone[0], finals[5])
+    rev, _ = _solve_gpu(gpu_ctx, structs[::-1])
+    assert np.array_equal(rev[len(structs) - 1 - 5], finals[5])
+
+
+def test_repeat_runs_are_bitwise_identical(gpu_ctx):
+    from giraffe_gb300 import gpu
+
+    structs = configs.batched_static(8, seed=2, n_min=20, n_max=120)
+    b = gpu.BatchSolver(gpu_ctx, structs)
+    b.reset(); b.run(); r1, _ = b.results()
+    b.reset(); b.run(); r2, _ = b.results()
+    b.close()
+    for x, y in zip(r1, r2):
+        assert np.array_equal(x, y)

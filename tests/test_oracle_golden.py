@@ -1,0 +1,83 @@
+"""The CPU oracle against the golden fixtures made by the reference itself
+(tests/golden/make_golden.py) and against known answers."""
+import numpy as np
+import pytest
+
+from giraffe_gb300 import configs
+from oracle import oracle
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_beam_elements_match_reference(golden):
+    g = golden("ref_beam_elements.npz")
+    for i in range(len(g["K"])):
+        nh = int(g["n_hist"][i])
+        K, f = oracle.beam_element(g["xyz"][i], g["mat"][i], g["sec6"][i], g["cs"][i], g["hist"][i][:nh],
+                                   g["disp"][i])
+        assert rel(K, g["K"][i]) < 1e-12, i
+        assert rel(f, g["P"][i]) < 1e-12, i
+
+
+def _check_run(g, s, tol=1e-11):
+    final, stats, rec = oracle.solve(s, record_cap=4096)
+    assert stats[3] == 0 and int(g["rc"]) == 0
+    # every configuration the reference wrote, at the same time
+    for k, t in enumerate(g["times"]):
+        j = int(np.argmin(np.abs(rec["time"] - t)))
+        assert abs(rec["time"][j] - t) < 1e-12
+        ref_nodes = g["nodes"][k]
+        scale = np.abs(ref_nodes[:, :3]).max()
+        assert np.abs(rec["nodes"][j][:, :3] - ref_nodes[:, :3]).max() <= tol * scale, t
+        assert np.abs(rec["nodes"][j][:, 6:] - ref_nodes[:, 6:]).max() <= tol * 10, t
+        assert np.abs(rec["gp_Q"][j] - g["gp_Q"][k]).max() <= tol * 10, t
+    # Newton solves per converged step
+    steps = g["steps"]
+    conv = steps[steps[:, 2] == 0]
+    assert len(conv) == stats[0]
+    assert np.array_equal(rec["iterations"][1:], conv[:, 1].astype(int) + 1)
+    return final, stats, rec
+
+
+def test_tutorial01_matches_reference(golden):
+    _check_run(golden("ref_tutorial01.npz"), configs.tutorial01())
+
+
+def test_rollup_matches_reference(golden):
+    _check_run(golden("ref_rollup.npz"), configs.cantilever_rollup())
+
+
+def test_chain_matches_reference(golden):
+    from tests.golden.make_golden import small_chain
+    _check_run(golden("ref_chain.npz"), small_chain())
+
+
+def test_rollup_known_answer():
+    """An end moment 2 pi E I / L rolls the cantilever into a circle: at load
+    factor t the tip is at (L sin(th)/th, L (1 - cos(th))/th) with th = 2 pi t."""
+    L = 10.0
+    final, stats, rec = oracle.solve(configs.cantilever_rollup(), record_cap=64)
+    assert stats[0] == 20 and stats[2] == 0
+    for t, nodes in zip(rec["time"][1:], rec["nodes"][1:]):
+        th = 2 * np.pi * t
+        ex = np.array([L * np.sin(th) / th, L * (1 - np.cos(th)) / th, 0.0])
+        assert np.abs(nodes[-1][:3] - ex).max() < 1e-6 * L
+    # full circle: tip back at the clamp, tip rotation tensor back to I
+    assert np.abs(final[-1][:3]).max() < 1e-6 * L
+    assert np.abs(final[-1][6:].reshape(3, 3) - np.eye(3)).max() < 1e-6
+
+
+def test_tutorial01_known_small_load_limit():
+    """Small tip force: the linear Timoshenko cantilever deflection
+    F L^3 / (3 E I) + F L / (G A) is recovered."""
+    s = configs.tutorial01()
+    s.loads[0].table.values[1, 0] = 1e-3
+    final, stats, _ = oracle.solve(s)
+    E, nu = 1e7, 0.3
+    A, I = 0.01, 0.1 ** 4 / 12
+    G = E / (2 * (1 + nu))
+    F, L = 1e-3, 1.0
+    ex = F * L ** 3 / (3 * E * I) + F * L / (G * A)
+    assert abs(final[-1][0] - ex) < 1e-9 * max(1, ex / 1e-6) + 1e-3 * ex
