@@ -1,0 +1,317 @@
+"""Benchmark: Newton solves per second of the batched static Beam_1 step.
+
+Workload (one "step" = one complete solve of the batch from its initial
+configuration): 512 independent pipe-section Beam_1 chains, element counts
+log-uniform in [50, 2000] from seed 0, Tube De ~ U(0.3, 0.5) m, wall
+~ U(0.02, 0.04) m, E = 210 GPa, clamped at one end, tip force ~ N(0, 1e5) N
+per component, 10 load steps, each chain 10 m long.  A Newton solve is one
+load step of one structure iterated to convergence (reference
+src/Static.cpp:200-250); the metric counts converged load steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default) runs the CUDA library; --impl reference times the
+reference's CPU algorithm for the path (the oracle restatement, on all host
+threads, on a bounded sample of the same chains).  Under torchrun every rank
+solves its own 512-chain batch (weak scaling, no collective on the data
+path) and rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Newton solves/sec (batched static Beam_1 chains, FP64, converged load steps)"
+UNIT = "Newton solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chains", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=48, help="chains in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl"
+        try:
+            import torch
+
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend, init_method="env://")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "of measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "of fallback"
+
+
+def cpu_baseline(structs, sample_n, rank):
+    """Oracle restatement on all host threads over a bounded, size-stratified
+    sample of the workload's chains."""
+    from oracle import oracle
+
+    order = np.argsort([len(s.beams) for s in structs])
+    idx = order[np.linspace(0, len(order) - 1, min(sample_n, len(order))).astype(int)]
+    sample = [structs[i] for i in idx]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    finals, stats, fails = oracle.solve_batch(sample, threads=threads)
+    dt = time.perf_counter() - t0
+    solves = int(stats[:, 0].sum())
+    return {"value": solves / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} of the {len(structs)} chains (every size stratum), "
+                      f"{solves} Newton solves in {dt:.2f} s on {threads} host threads"}, sample
+
+
+def run_reference(args, rank, world):
+    from giraffe_gb300 import configs
+
+    if rank != 0:
+        return
+    structs = configs.batched_static(args.chains, seed=args.seed)
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info, _ = cpu_baseline(structs, args.cpu_sample, rank)
+        if k >= args.warmup:
+            vals.append(info["value"])
+    value = statistics.median(vals)
+    info["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"batched static: {args.chains} Beam_1 pipe chains, 50-2000 elements "
+                                   f"log-uniform, 10 load steps, seed {args.seed}",
+                       "chains": args.chains, "load_steps": 10, "sample": info["sample"]},
+            "cpu_baseline": info,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import ctypes as C
+
+    from giraffe_gb300 import build, configs, gpu
+
+    build.build()
+    structs = configs.batched_static(args.chains, seed=args.seed + rank)
+    ctx = gpu.Context(0)
+    L = ctx.L
+    b = gpu.BatchSolver(ctx, structs, ctx.opts())
+    # warm-up
+    for _ in range(args.warmup):
+        b.reset()
+        b.run()
+    _, stats = b.results()
+    solves_per_step = int(stats[:, 0].sum())
+    assert stats[:, 3].sum() == 0, "a structure aborted"
+    L.gf_batch_solve_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    ms = C.c_double(0.0)
+    barrier(world)
+    with Clocks() as clk:
+        ctx.check(L.gf_batch_solve_timed(b.h, args.steps, C.byref(ms)), "gf_batch_solve_timed")
+    barrier(world)
+    launches = b.launches()
+    total_ms = max_over_ranks(ms.value, world)
+    total_solves = sum_over_ranks(solves_per_step * args.steps, world)
+    value = total_solves / (total_ms / 1e3)
+    # per-kernel device times (one profiled solve, events around every launch)
+    L.gf_batch_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.gf_kernel_name.restype = C.c_char_p
+    kms = (C.c_double * 12)()
+    kl = (C.c_longlong * 12)()
+    ctx.check(L.gf_batch_profile(b.h, kms, kl), "gf_batch_profile")
+    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(12) if kl[i]}
+    L.gf_batch_work.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
+    lu_f, asm_b, mnt_f = C.c_double(), C.c_double(), C.c_double()
+    ctx.check(L.gf_batch_work(b.h, C.byref(lu_f), C.byref(asm_b), C.byref(mnt_f)), "gf_batch_work")
+    L.gf_device_fp_peaks.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    fp64, fp32 = C.c_double(), C.c_double()
+    ctx.check(L.gf_device_fp_peaks(ctx.h, C.byref(fp64), C.byref(fp32)), "gf_device_fp_peaks")
+    L.gf_batch_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    h2d, d2h = C.c_longlong(), C.c_longlong()
+    L.gf_batch_bytes(b.h, C.byref(h2d), C.byref(d2h))
+    b.close()
+    # e2e through the public C ABI from host descriptors: create (H2D), run, results (D2H)
+    e2e_times = []
+    for k in range(max(1, min(args.steps, 3))):
+        barrier(world)
+        t0 = time.perf_counter()
+        finals, st = gpu.solve(structs)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_t = max_over_ranks(statistics.median(e2e_times), world)
+    e2e_value = sum_over_ranks(int(st[:, 0].sum()), world) / e2e_t
+    # roofline of the dominant kernel
+    peaks, tag = measured_peaks()
+    dom = max(kernels.items(), key=lambda kv: kv[1]["ms"])[0]
+    roof = {"kernel": dom}
+    if dom == "band_solve":
+        t = kernels[dom]["ms"] / 1e3
+        achieved = lu_f.value / t / 1e12
+        roof.update({"bound": "fp64", "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
+                     "frac": achieved / fp64.value, "traffic": None,
+                     "note": "FP64 CUDA-core bound (no HBM or tensor-core bound applies); peak = FP64 FMA "
+                             "throughput measured live by gf_device_fp_peaks; HBM view: "
+                             f"{(lu_f.value / 2 / 17 * 8 * 2) / t / 1e9:.1f} GB/s of "
+                             f"{peaks.get('hbm_gbs')} GB/s {tag}"})
+    elif dom == "beam_mount":
+        t = kernels[dom]["ms"] / 1e3
+        achieved = mnt_f.value / t / 1e12
+        roof.update({"bound": "fp64", "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
+                     "frac": achieved / fp64.value, "traffic": None,
+                     "note": f"assembly bytes {asm_b.value:.3e} -> {asm_b.value / t / 1e9:.1f} GB/s of "
+                             f"{peaks.get('hbm_gbs')} GB/s {tag}"})
+    else:
+        t = kernels[dom]["ms"] / 1e3
+        roof.update({"bound": "hbm", "achieved": asm_b.value / t / 1e9, "peak": peaks.get("hbm_gbs"),
+                     "unit": "GB/s", "frac": asm_b.value / t / 1e9 / peaks.get("hbm_gbs"), "traffic": None})
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, _ = cpu_baseline(structs, args.cpu_sample, rank)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": f"batched static: {args.chains} Beam_1 pipe chains per GPU, "
+                                       f"50-2000 elements log-uniform, 10 load steps, seed {args.seed}",
+                           "chains_per_gpu": args.chains, "load_steps": 10,
+                           "newton_solves_per_step": solves_per_step,
+                           "precision": "plain FP64 (element, band LU, residual)",
+                           "l2": "inputs larger than L2 (K_AA bands ~1 GB per step)",
+                           "parallelism": f"{world} independent batch(es)"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d.value,
+                        "d2h_bytes_per_step": d2h.value},
+                "gpu_launches": launches,
+                "roofline": roof,
+                "kernels_ms_per_solve": {k: round(v["ms"], 3) for k, v in kernels.items()},
+                "peaks_measured": {"fp64_tflops": fp64.value, "fp32_tflops": fp32.value},
+                "clocks": clk.summary(),
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    rank, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -18,6 +18,11 @@
 
 using namespace gf;
 
+// FP64 flops of one Beam_1 Mount on the device (both Gauss points: kinematics,
+// stresses, internal force, B^T D B + G, block rotation and the 18x18
+// expansion), counted from the operation sequence of gf_beam.cuh.
+#define GF_BEAM_MOUNT_FLOPS 9000.0
+
 struct gf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -130,6 +135,7 @@ struct gf_batch {
   long long last_launches = 0;
   int launches_per_pass = 0;
   int* h_running = nullptr;  // pinned
+  long long h2d_bytes = 0;
 };
 
 namespace {
@@ -142,6 +148,7 @@ template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
 
 template <typename T> bool upload(gf_batch* B, T** p, const std::vector<T>& v) {
   if (!balloc(B, p, v.size())) return false;
+  B->h2d_bytes += (long long)(v.size() * sizeof(T));
   if (!v.empty()) {
     cudaError_t e = cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return set_err(B->ctx, "upload failed: %s", cudaGetErrorString(e));
@@ -457,28 +464,35 @@ int gf_batch_reset(gf_batch* B) {
   return GF_OK;
 }
 
-int gf_batch_run(gf_batch* B) {
-  if (!B) return GF_ERR_ARG;
+namespace {
+int ensure_graph(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
   cudaStream_t st = ctx->stream;
-  const Batch& b = B->b;
   if (B->opts.use_graph && !B->graph) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    launch_iteration(b, st);
+    launch_iteration(B->b, st);
     CK(cudaStreamEndCapture(st, &g));
     CK(cudaGraphInstantiate(&B->graph, g, 0));
     CK(cudaGraphDestroy(g));
   }
-  CK(cudaEventRecord(B->ev0, st));
+  return GF_OK;
+}
+
+// Launches Newton passes until no structure is running; polls the device
+// every opts.poll_every passes.
+int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  const Batch& b = B->b;
   long long passes = 0;
   const long long cap = 4000000;
   for (;;) {
     for (int k = 0; k < B->opts.poll_every; ++k) {
-      if (B->graph) {
+      if (B->graph && !prof) {
         CK(cudaGraphLaunch(B->graph, st));
       } else {
-        launch_iteration(b, st);
+        launch_iteration(b, st, true, prof);
       }
       ++passes;
     }
@@ -491,12 +505,146 @@ int gf_batch_run(gf_batch* B) {
       return GF_ERR_TIMEOUT;
     }
   }
+  *passes_out = passes;
+  return GF_OK;
+}
+}  // namespace
+
+int gf_batch_run(gf_batch* B) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  int r = ensure_graph(B);
+  if (r != GF_OK) return r;
+  CK(cudaEventRecord(B->ev0, st));
+  long long passes = 0;
+  r = run_passes(B, &passes);
+  if (r != GF_OK) return r;
   CK(cudaEventRecord(B->ev1, st));
   CK(cudaEventSynchronize(B->ev1));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
   B->last_ms = ms;
   B->last_launches = passes * B->launches_per_pass;
+  return GF_OK;
+}
+
+int gf_batch_solve_timed(gf_batch* B, int steps, double* ms_out) {
+  if (!B || steps <= 0) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  int r = ensure_graph(B);
+  if (r != GF_OK) return r;
+  long long launches = 0;
+  CK(cudaEventRecord(B->ev0, st));
+  for (int k = 0; k < steps; ++k) {
+    r = batch_reset(B);
+    if (r != GF_OK) return r;
+    long long passes = 0;
+    r = run_passes(B, &passes);
+    if (r != GF_OK) return r;
+    launches += passes * B->launches_per_pass + 1;
+  }
+  CK(cudaEventRecord(B->ev1, st));
+  CK(cudaEventSynchronize(B->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+  *ms_out = ms;
+  B->last_ms = ms / steps;
+  B->last_launches = launches;
+  return GF_OK;
+}
+
+int gf_batch_profile(gf_batch* B, double* ms_out, long long* launches_out) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = ctx->stream;
+  int r = batch_reset(B);
+  if (r != GF_OK) return r;
+  const int cap = 1 << 16;
+  std::vector<cudaEvent_t> ev(2 * cap);
+  std::vector<int> cls(cap);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  LaunchProf prof{ev.data(), cls.data(), cap, 0};
+  long long passes = 0;
+  r = run_passes(B, &passes, &prof);
+  CK(cudaStreamSynchronize(st));
+  for (int k = 0; k < GF_N_KERNELS; ++k) { ms_out[k] = 0.0; launches_out[k] = 0; }
+  for (int i = 0; i < prof.n; ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    ms_out[cls[i]] += ms;
+    launches_out[cls[i]] += 1;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (r != GF_OK) return r;
+  if (prof.n >= cap) {
+    set_err(ctx, "gf_batch_profile: more than %d launches", cap);
+    return GF_ERR_ARG;
+  }
+  return GF_OK;
+}
+
+const char* gf_kernel_name(int k) { return kernel_class_name(k); }
+
+int gf_batch_bytes(const gf_batch* B, long long* h2d, long long* d2h) {
+  if (!B) return GF_ERR_ARG;
+  if (h2d) *h2d = B->h2d_bytes;
+  if (d2h) *d2h = (long long)B->b.n_nodes * 15 * (long long)sizeof(double) +
+                  (long long)B->b.n_struct * (long long)sizeof(StructState);
+  return GF_OK;
+}
+
+int gf_batch_work(const gf_batch* B, double* lu_flops, double* asm_bytes, double* mount_flops) {
+  if (!B) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  const Batch& b = B->b;
+  int n = b.n_struct;
+  std::vector<StructState> st(n);
+  CK(cudaMemcpy(st.data(), b.state, sizeof(StructState) * n, cudaMemcpyDeviceToHost));
+  double lu = 0, ab = 0, mf = 0;
+  for (int s = 0; s < n; ++s) {
+    const StructInfo& inf = B->info[s];
+    double nf = inf.n_free, kl = B->kb[s];
+    lu += st[s].n_solves * (2.0 * nf * kl * kl + 2.0 * nf * (kl + kl));
+    ab += st[s].total_it * 8.0 * (6.0 * inf.n_nodes + 80.0 * inf.n_elem + (2 * kl + 1) * nf + nf);
+    mf += st[s].total_it * (double)inf.n_elem * GF_BEAM_MOUNT_FLOPS;
+  }
+  if (lu_flops) *lu_flops = lu;
+  if (asm_bytes) *asm_bytes = ab;
+  if (mount_flops) *mount_flops = mf;
+  return GF_OK;
+}
+
+int gf_device_fp_peaks(gf_ctx* ctx, double* fp64_tflops, double* fp32_tflops) {
+  if (!ctx) return GF_ERR_ARG;
+  cudaStream_t st = ctx->stream;
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  int blocks = sms * 8, threads = 256;
+  void* out = nullptr;
+  CK(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int pass = 0; pass < 2; ++pass) {
+    bool f64 = pass == 0;
+    int iters = f64 ? 2048 : 65536;
+    launch_fp_probe(f64, out, blocks, threads, 64, st);  // warm-up
+    cudaEventRecord(e0, st);
+    launch_fp_probe(f64, out, blocks, threads, iters, st);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    if (f64 && fp64_tflops) *fp64_tflops = tf;
+    if (!f64 && fp32_tflops) *fp32_tflops = tf;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  CK(cudaGetLastError());
   return GF_OK;
 }
 
@@ -518,6 +666,7 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       z.bisections = st[s].bisections;
       z.aborted = st[s].phase == PH_ABORTED || st[s].aborted;
       z.fp64_fallback = st[s].fp64_fallback;
+      z.linear_solves = st[s].n_solves;
       stats[s] = z;
     }
   if (final_nodes) {

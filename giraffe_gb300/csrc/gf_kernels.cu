@@ -338,90 +338,165 @@ __global__ void k_residual(Batch b) {
 }
 
 // ---------------------------------------------------------------------------
-// Banded LU without pivoting, fused forward substitution, then back
-// substitution, FP64.  One warp per structure.  Columns stream through a
-// 128-column shared-memory ring filled 32 columns at a time, two chunks
-// ahead of the elimination; the warp owns the active 18-column window: lane 0
-// updates the right-hand side, lanes 1..17 the 17 trailing columns.  U rows
-// (pivot first) are written to b.U; the solution overwrites P.
+// Banded LU without pivoting, fused forward substitution, back substitution;
+// FP64.  One 4-warp CTA per structure.
+//
+// On this GPU a dependent FP64 operation costs ~64 cycles and an FP64 divide
+// ~640, so the per-column critical path is what bounds a long chain.  The
+// elimination is split so that warp 0 carries only that path with one column
+// of lookahead: at step j it updates column j+1, forms the next pivot's
+// reciprocal (Newton-Raphson iteration r <- r (2 - p r), seeded by the FP32
+// approximate reciprocal, two steps) and the next multipliers, while warps
+// 1-3 apply step j's rank-1 update to columns j+2..j+17 and the right-hand
+// side.  Band columns stream through a 128-column shared-memory ring filled
+// 32 columns at a time, two chunks ahead.  Row j of U (with the pivot
+// reciprocal in place of the pivot) goes to b.U; the forward-substituted
+// right-hand side goes to P, which the back substitution overwrites with x.
 constexpr int RING = 128;
 constexpr int CHUNK = 32;
+constexpr int SOLVE_THREADS = 128;
+
+// Newton-Raphson reciprocal of p, seeded by the hardware FP32 approximation;
+// exact division where the seed is out of FP32 range.
+__device__ __forceinline__ double recip_nr(double p) {
+  float pf = __double2float_rn(p);
+  float af = fabsf(pf);
+  if (!(af > 1e-30f && af < 1e30f)) return 1.0 / p;
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(pf));
+  double r = (double)rf;
+  double e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  return r;
+}
 
 template <typename T>
-__device__ __forceinline__ void load_chunk(const T* __restrict__ band, double* __restrict__ rhs, T* ring,
-                                           double* rring, int q, int n, int lane) {
+__device__ __forceinline__ void load_chunk(const T* __restrict__ band, const double* __restrict__ rhs, T* ring,
+                                           double* rring, int q, int n, int tid, int nthreads) {
   int c0 = q * CHUNK;
   if (c0 >= n) return;
   int nc = min(CHUNK, n - c0);
   int slot0 = c0 % RING;
   const T* src = band + (int64_t)c0 * GF_LDB;
   T* dst = ring + (int64_t)slot0 * GF_LDB;
-  for (int i = lane; i < nc * GF_LDB; i += 32) dst[i] = src[i];
-  for (int i = lane; i < nc; i += 32) rring[slot0 + i] = rhs[c0 + i];
+  for (int i = tid; i < nc * GF_LDB; i += nthreads) dst[i] = src[i];
+  for (int i = tid; i < nc; i += nthreads) rring[slot0 + i] = rhs[c0 + i];
 }
 
-__global__ void __launch_bounds__(32) k_band_solve(Batch b) {
+__global__ void __launch_bounds__(SOLVE_THREADS) k_band_solve(Batch b) {
   int s = blockIdx.x;
   StructState& st = b.state[s];
   if (!iterating(st) || !st.need_solve) return;
   const StructInfo inf = b.info[s];
   const int n = inf.n_free;
-  const int lane = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   extern __shared__ unsigned char smem_raw[];
   double* ring = reinterpret_cast<double*>(smem_raw);
   double* rring = ring + RING * GF_LDB;
+  __shared__ double lbuf[2][GF_KB + 1];
+  __shared__ double invb[2];
+  __shared__ int sfail;
   const double* band = b.band + inf.band_off;
   double* rhs = b.P + inf.dof_off;
   double* U = b.U + (int64_t)inf.dof_off * GF_UW;
-  int fail = 0;
-  load_chunk(band, rhs, ring, rring, 0, n, lane);
-  load_chunk(band, rhs, ring, rring, 1, n, lane);
-  load_chunk(band, rhs, ring, rring, 2, n, lane);
-  __syncwarp();
+  if (tid == 0) sfail = 0;
+  load_chunk(band, rhs, ring, rring, 0, n, tid, SOLVE_THREADS);
+  load_chunk(band, rhs, ring, rring, 1, n, tid, SOLVE_THREADS);
+  load_chunk(band, rhs, ring, rring, 2, n, tid, SOLVE_THREADS);
+  __syncthreads();
+  // step 0 multipliers
+  if (warp == 0) {
+    double p = ring[GF_KB];
+    double inv = recip_nr(p);
+    if (lane >= 1 && lane <= GF_KB) lbuf[0][lane] = (lane < n) ? ring[GF_KB + lane] * inv : 0.0;
+    if (lane == 0) {
+      invb[0] = inv;
+      if (!(p != 0.0) || !isfinite(p)) sfail = 1;
+    }
+  }
+  __syncthreads();
   for (int j = 0; j < n; ++j) {
-    if (j % CHUNK == 0 && j > 0) {
-      // chunk j/CHUNK + 2 goes into the slots of chunk j/CHUNK - 2 (finished)
-      load_chunk(band, rhs, ring, rring, j / CHUNK + 2, n, lane);
-      __syncwarp();
+    const int cur = j & 1;
+    if (j % CHUNK == 0 && j > 0) load_chunk(band, rhs, ring, rring, j / CHUNK + 2, n, tid, SOLVE_THREADS);
+    if (warp > 0) {
+      // rank-1 update of columns j+2..j+17 (16 x 17 entries) and the rhs (17)
+      for (int k = tid - 32; k < 16 * GF_KB + GF_KB; k += SOLVE_THREADS - 32) {
+        if (k < 16 * GF_KB) {
+          int r = k / 16 + 1, c = k % 16 + 2;
+          int J = j + c;
+          if (J < n) {
+            double* col = ring + (int64_t)(J % RING) * GF_LDB;
+            col[GF_KB + r - c] -= lbuf[cur][r] * col[GF_KB - c];
+          }
+        } else {
+          int r = k - 16 * GF_KB + 1;
+          if (j + r < n) rring[(j + r) % RING] -= lbuf[cur][r] * rring[j % RING];
+        }
+      }
+    } else {
+      // U row j (reciprocal pivot first), y_j
+      if (lane >= 1 && lane <= GF_KB) {
+        int J = j + lane;
+        U[(int64_t)j * GF_UW + lane] = J < n ? ring[(int64_t)(J % RING) * GF_LDB + GF_KB - lane] : 0.0;
+      } else if (lane == 0) {
+        U[(int64_t)j * GF_UW] = invb[cur];
+        rhs[j] = rring[j % RING];
+      }
+      if (j + 1 < n) {
+        double* c1 = ring + (int64_t)((j + 1) % RING) * GF_LDB;
+        if (lane >= 1 && lane <= GF_KB) c1[GF_KB + lane - 1] -= lbuf[cur][lane] * c1[GF_KB - 1];
+        __syncwarp();
+        double p = c1[GF_KB];
+        double inv = recip_nr(p);
+        if (lane >= 1 && lane <= GF_KB) lbuf[cur ^ 1][lane] = (j + 1 + lane < n) ? c1[GF_KB + lane] * inv : 0.0;
+        if (lane == 0) {
+          invb[cur ^ 1] = inv;
+          if (!(p != 0.0) || !isfinite(p)) sfail = 1;
+        }
+      }
     }
-    const double* pc = ring + (int64_t)(j % RING) * GF_LDB;
-    double piv = pc[GF_KB];
-    if (!(piv != 0.0) || !isfinite(piv)) fail = 1;
-    double inv = 1.0 / piv;
-    if (lane >= 1 && lane <= GF_KB && j + lane < n) {
-      double* cc = ring + (int64_t)((j + lane) % RING) * GF_LDB;
-      double u = cc[GF_KB - lane];
-      U[(int64_t)j * GF_UW + lane] = u;
-      double w = u * inv;
-#pragma unroll
-      for (int r = 1; r <= GF_KB; ++r) cc[GF_KB - lane + r] -= pc[GF_KB + r] * w;
-    } else if (lane == 0) {
-      U[(int64_t)j * GF_UW] = piv;
-      double yj = rring[j % RING];
-      rhs[j] = yj;  // forward-substituted right-hand side
-      double f = yj * inv;
-#pragma unroll
-      for (int r = 1; r <= GF_KB; ++r)
-        if (j + r < n) rring[(j + r) % RING] -= pc[GF_KB + r] * f;
-    } else if (lane > GF_KB && j + lane - GF_KB < n) {
-      // lanes 18..31: nothing to update; keep the warp converged
+    __syncthreads();
+  }
+  // back substitution, column oriented, warp 0: lane t (1..17) holds
+  // y'_{j-t}; x_j = y'_j / u_jj, then y'_{j-t} -= U(j-t, j) x_j.
+  if (warp == 0) {
+    double yv = 0.0;  // lane 0: y'_j; lane t: y'_{j-t}
+    {
+      int i = n - 1 - lane;
+      if (lane <= GF_KB && i >= 0) yv = rhs[i];
     }
-    __syncwarp();
+    for (int j0 = n - 1; j0 >= 0; j0 -= CHUNK) {
+      // per-chunk operands: lane t needs U(j - t, t) for j in the chunk, lane 0
+      // the reciprocal pivots, lane 17 the y entering at j - 18
+      double uo[CHUNK];
+#pragma unroll
+      for (int q = 0; q < CHUNK; ++q) {
+        int j = j0 - q;
+        double v = 0.0;
+        if (j >= 0) {
+          if (lane == 0) v = U[(int64_t)j * GF_UW];
+          else if (lane <= GF_KB && j - lane >= 0) v = U[(int64_t)(j - lane) * GF_UW + lane];
+          else if (lane == GF_KB + 1 && j - GF_KB - 1 >= 0) v = rhs[j - GF_KB - 1];
+        }
+        uo[q] = v;
+      }
+#pragma unroll
+      for (int q = 0; q < CHUNK; ++q) {
+        int j = j0 - q;
+        if (j < 0) break;
+        double xj = __shfl_sync(0xffffffffu, yv * uo[q], 0);
+        if (lane == 0) rhs[j] = xj;
+        if (lane >= 1 && lane <= GF_KB) yv = fma(-uo[q], xj, yv);
+        // shift the window: lane t takes lane t+1's value; lane 17 takes y_{j-18}
+        double nx = __shfl_down_sync(0xffffffffu, yv, 1);
+        double ent = __shfl_sync(0xffffffffu, uo[q], GF_KB + 1);
+        yv = lane < GF_KB ? nx : (lane == GF_KB ? ent : 0.0);
+      }
+    }
   }
-  // back substitution: x_j = (y_j - sum_c U(j, j+c) x_{j+c}) / U(j, j)
-  __syncwarp();
-  double xw = 0.0;  // lane c holds x_{j+c}
-  for (int j = n - 1; j >= 0; --j) {
-    double uc = (lane >= 1 && lane <= GF_KB && j + lane < n) ? U[(int64_t)j * GF_UW + lane] : 0.0;
-    double sum = warp_sum(uc * xw);
-    double xj = 0.0;
-    if (lane == 0) xj = (rhs[j] - sum) / U[(int64_t)j * GF_UW];
-    xj = __shfl_sync(0xffffffffu, xj, 0);
-    double up = __shfl_up_sync(0xffffffffu, xw, 1);
-    xw = lane == 1 ? xj : up;
-    if (lane == 0) rhs[j] = xj;
-  }
-  if (lane == 0) st.info_fail = fail;
+  if (tid == 0) st.info_fail = sfail;
 }
 
 // UpdateDisps + CheckGLConvergence (reference src/Solution.cpp:390-423,
@@ -482,6 +557,7 @@ __global__ void k_control(Batch b) {
   if (st.time_step < p.min_time_step && st.time != p.end_time) st.aborted = 1;
   st.it++;
   st.total_it++;
+  if (st.need_solve) st.n_solves++;
   bool loop = !both && !st.diverged && !st.aborted;
   if (loop) {
     atomicAdd(b.running, 1);
@@ -631,30 +707,73 @@ static void set_attrs() {
   }
 }
 
-void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels) {
+const char* kernel_class_name(int k) {
+  static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_mount", "loads", "residual", "band_solve",
+                                        "update", "control", "commit_elems", "commit_nodes", "init_state", "other"};
+  return k >= 0 && k < KC_COUNT ? names[k] : "?";
+}
+
+namespace {
+struct ProfScope {
+  LaunchProf* p;
+  cudaStream_t st;
+  int idx;
+  ProfScope(LaunchProf* p_, cudaStream_t s, int k) : p(p_), st(s), idx(-1) {
+    if (p && p->n < p->cap) {
+      idx = p->n++;
+      p->cls[idx] = k;
+      cudaEventRecord(p->ev[2 * idx], st);
+    }
+  }
+  ~ProfScope() {
+    if (idx >= 0) cudaEventRecord(p->ev[2 * idx + 1], st);
+  }
+};
+}  // namespace
+
+void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, LaunchProf* prof) {
   set_attrs();
   int ns = b.n_struct;
-  k_step_begin<<<ns, 256, 0, st>>>(b);
-  k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
+  { ProfScope q(prof, st, KC_STEP_BEGIN); k_step_begin<<<ns, 256, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_ZERO); k_zero<<<dim3(8, ns), 256, 0, st>>>(b); }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];
     if (cnt <= 0) continue;
-    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS,
-                           MOUNT_SMEM, st>>>(b, c);
+    ProfScope q(prof, st, KC_MOUNT);
+    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b, c);
   }
-  k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
-  k_residual<<<ns, 256, 0, st>>>(b);
-  launch_band_solve(b, st);
-  k_update<<<ns, 256, 0, st>>>(b);
-  k_control<<<(ns + 127) / 128, 128, 0, st>>>(b);
+  { ProfScope q(prof, st, KC_LOADS); k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
+  { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {
-    if (b.n_elem) k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
-    if (b.n_nodes) k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b);
+    if (b.n_elem) { ProfScope q(prof, st, KC_COMMIT_ELEMS); k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b); }
+    if (b.n_nodes) { ProfScope q(prof, st, KC_COMMIT_NODES); k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b); }
   }
 }
 
+namespace {
+template <typename T> __global__ void k_fp_probe(T* out, int iters, T a, T c) {
+  T x0 = threadIdx.x, x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3), x4 = x0 + T(4), x5 = x0 + T(5),
+    x6 = x0 + T(6), x7 = x0 + T(7);
+  for (int i = 0; i < iters; ++i) {
+    x0 = x0 * a + c; x1 = x1 * a + c; x2 = x2 * a + c; x3 = x3 * a + c;
+    x4 = x4 * a + c; x5 = x5 * a + c; x6 = x6 * a + c; x7 = x7 * a + c;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+
+void launch_fp_probe(bool fp64, void* out, int blocks, int threads, int iters, cudaStream_t st) {
+  if (fp64)
+    k_fp_probe<double><<<blocks, threads, 0, st>>>(static_cast<double*>(out), iters, 0.999, 0.001);
+  else
+    k_fp_probe<float><<<blocks, threads, 0, st>>>(static_cast<float*>(out), iters, 0.999f, 0.001f);
+}
+
 void launch_band_solve(const Batch& b, cudaStream_t st) {
-  k_band_solve<<<b.n_struct, 32, (RING * GF_LDB + RING) * sizeof(double), st>>>(b);
+  k_band_solve<<<b.n_struct, SOLVE_THREADS, (RING * GF_LDB + RING) * sizeof(double), st>>>(b);
 }
 
 void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const double* d, double* K,

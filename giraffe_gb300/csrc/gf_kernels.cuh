@@ -25,7 +25,23 @@
 
 namespace gf {
 
-void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels = true);
+// Optional per-kernel timing: when non-null, every launch of kernel class k
+// is bracketed by events ev[2*i], ev[2*i+1] and recorded in cls[i].
+struct LaunchProf {
+  cudaEvent_t* ev;
+  int* cls;
+  int cap;
+  int n;
+};
+enum KernelClass {
+  KC_STEP_BEGIN = 0, KC_ZERO, KC_MOUNT, KC_LOADS, KC_RESIDUAL, KC_SOLVE, KC_UPDATE, KC_CONTROL,
+  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_INIT, KC_OTHER, KC_COUNT
+};
+const char* kernel_class_name(int k);
+
+void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels = true, LaunchProf* prof = nullptr);
+// FMA throughput probe: 8 independent chains per thread, `iters` steps.
+void launch_fp_probe(bool fp64, void* out, int blocks, int threads, int iters, cudaStream_t st);
 // First half of a pass (step start, zero, mount, loads, residual): leaves the
 // assembled K_AA and P_A of the first iteration in the batch buffers.
 void launch_iteration_partial(const Batch& b, cudaStream_t st);

@@ -75,6 +75,7 @@ struct StructState {
   int res_conv, gl_conv, diverged, aborted, need_solve, info_fail;
   int convergence_counter, converged_number, n_conv_evaluated, total_it, bisections;
   int commit;  // set by control for the commit kernel
+  int n_solves;  // linear solves performed
   int solve_sweeps;  // refinement sweeps of the last solve (mixed path)
   int fp64_fallback;  // mixed path: this structure factors in FP64
   double time, time_step, last_converged_time, current_time_step;

@@ -97,6 +97,28 @@ long long gf_batch_last_launches(const gf_batch* batch);
  * flip.  dims (optional) receives n_free and kb. */
 int gf_batch_assemble(gf_batch* batch, int s, double* ab, double* PA, int* dims);
 
+/* Runs `steps` complete solves of the batch (each: reset to the initial
+ * configuration, then run to the end) back to back and returns their total
+ * device time in milliseconds through *ms (CUDA events on the batch's
+ * stream). */
+int gf_batch_solve_timed(gf_batch* batch, int steps, double* ms);
+/* One reset + run without graph capture, with CUDA events around every
+ * kernel; per kernel class k (0 <= k < GF_N_KERNELS, names from
+ * gf_kernel_name) *ms_out[k] receives the summed device time and
+ * launches_out[k] the launch count. */
+enum { GF_N_KERNELS = 12 };
+int gf_batch_profile(gf_batch* batch, double* ms_out, long long* launches_out);
+const char* gf_kernel_name(int k);
+/* Bytes the batch moved host->device when it was created, and bytes
+ * gf_batch_results moves device->host. */
+int gf_batch_bytes(const gf_batch* batch, long long* h2d, long long* d2h);
+/* Algorithmic work of the last run: per-structure Newton passes summed into
+ * the factor/solve flop count 2 n kl ku + 2 n (kl + ku) and the assembly
+ * bytes 8 [6 N_nodes + 80 N_e + 35 n + n] per pass (see DESIGN). */
+int gf_batch_work(const gf_batch* batch, double* lu_flops, double* asm_bytes, double* mount_flops);
+/* Measured FP64 and FP32 FMA throughput of the device (TFLOP/s). */
+int gf_device_fp_peaks(gf_ctx* ctx, double* fp64_tflops, double* fp32_tflops);
+
 /* Convenience: create, run, fetch results and destroy. */
 int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts,
              double* const* final_nodes, gf_stats* stats);
