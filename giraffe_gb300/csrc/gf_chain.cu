@@ -1,0 +1,375 @@
+// Chain solver kernels (see gf_chain.cuh).  One thread per item (element or
+// corner): every FP64 warp instruction carries 32 independent items, which is
+// what the FP64 unit's throughput needs; the 6x19 augmented matrices of the
+// small dense solves are staged in shared memory.
+#include <cuda_runtime.h>
+
+#include "gf_chain.cuh"
+#include "gf_math.cuh"
+
+namespace gf {
+
+namespace {
+
+constexpr int CT = 64;   // threads per block
+constexpr int NC = 19;   // augmented columns: 6 (matrix) + 13 (right-hand sides)
+
+__device__ __forceinline__ bool solving(const Batch& b, int s) {
+  const StructState& st = b.state[s];
+  return st.phase == PH_ITER && st.need_solve;
+}
+
+__device__ __forceinline__ double band_at(const double* band, int r, int c) {
+  return band[(GF_KB + r - c) + (int64_t)c * GF_LDB];
+}
+
+// Newton-Raphson reciprocal seeded by the FP32 hardware approximation (two
+// steps r <- r + r (1 - p r)); exact division outside the FP32 range.
+__device__ __forceinline__ double recip(double p) {
+  float pf = __double2float_rn(p);
+  float af = fabsf(pf);
+  if (!(af > 1e-30f && af < 1e30f)) return 1.0 / p;
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(pf));
+  double r = (double)rf;
+  double e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  return r;
+}
+
+// Gauss-Jordan on a thread's 6 x ncols augmented matrix A (row-major, entry
+// (r, c) at A[(r * NC + c) * CT]): on return columns 6.. hold D^{-1} RHS.
+// No pivoting; returns false on a zero or non-finite pivot.
+__device__ bool gauss_jordan6(double* A, int ncols) {
+  bool ok = true;
+#pragma unroll 1
+  for (int k = 0; k < 6; ++k) {
+    double p = A[(k * NC + k) * CT];
+    if (!(p != 0.0) || !isfinite(p)) ok = false;
+    double inv = recip(p);
+#pragma unroll 1
+    for (int c = k + 1; c < ncols; ++c) A[(k * NC + c) * CT] *= inv;
+#pragma unroll 1
+    for (int i = 0; i < 6; ++i) {
+      if (i == k) continue;
+      double m = A[(i * NC + k) * CT];
+#pragma unroll 1
+      for (int c = k + 1; c < ncols; ++c) A[(i * NC + c) * CT] = fma(-m, A[(k * NC + c) * CT], A[(i * NC + c) * CT]);
+    }
+  }
+  return ok;
+}
+
+// ---- 1. condensation of the midside node of every chain element ----
+__global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
+  extern __shared__ double smem[];
+  int t = blockIdx.x * CT + threadIdx.x;
+  if (t >= c.n_chain_elems) return;
+  int e = c.elem_list[t];
+  int s = b.estruct[e];
+  if (!solving(b, s)) return;
+  const StructInfo inf = b.info[s];
+  const double* band = b.band + inf.band_off;
+  const double* P = b.P + inf.dof_off;
+  double* A = smem + threadIdx.x;
+  int nm = b.enodes[3 * e + 1], na = b.enodes[3 * e], nb = b.enodes[3 * e + 2];
+  bool fa = c.elem_corner_a[t] >= 0, fb = c.elem_corner_b[t] >= 0;
+  int gm[6], ga[6], gb[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    gm[i] = b.gl[(int64_t)nm * 6 + i];
+    ga[i] = b.gl[(int64_t)na * 6 + i];
+    gb[i] = b.gl[(int64_t)nb * 6 + i];
+  }
+#pragma unroll 1
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {
+      A[(i * NC + j) * CT] = band_at(band, gm[i], gm[j]);
+      A[(i * NC + 7 + j) * CT] = fa ? band_at(band, gm[i], ga[j]) : 0.0;
+      A[(i * NC + 13 + j) * CT] = fb ? band_at(band, gm[i], gb[j]) : 0.0;
+    }
+    A[(i * NC + 6) * CT] = P[gm[i]];
+  }
+  if (!gauss_jordan6(A, NC)) b.state[s].info_fail = 1;
+  double* ez = c.ez + (int64_t)t * 78;
+#pragma unroll 1
+  for (int i = 0; i < 6; ++i)
+#pragma unroll 1
+    for (int q = 0; q < 13; ++q) ez[i * 13 + q] = A[(i * NC + 6 + q) * CT];
+  // -A_as Z and -A_bs Z (6 x 13 each)
+  double* ec = c.ec + (int64_t)t * 156;
+#pragma unroll 1
+  for (int side = 0; side < 2; ++side) {
+    bool free_side = side ? fb : fa;
+    const int* gx = side ? gb : ga;
+#pragma unroll 1
+    for (int i = 0; i < 6; ++i) {
+      double row[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) row[j] = free_side ? band_at(band, gx[i], gm[j]) : 0.0;
+#pragma unroll 1
+      for (int q = 0; q < 13; ++q) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc = fma(row[j], A[(j * NC + 6 + q) * CT], acc);
+        ec[i * 26 + side * 13 + q] = -acc;
+      }
+    }
+  }
+}
+
+// ---- 2. corner system ----
+__global__ void k_corner_system(Batch b, ChainData c) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n_corners) return;
+  int s = c.corner_struct[k];
+  if (!solving(b, s)) return;
+  const StructInfo inf = b.info[s];
+  const double* band = b.band + inf.band_off;
+  const double* P = b.P + inf.dof_off;
+  int node = c.corner_node[k];
+  int eL = c.corner_left[k], eR = c.corner_right[k];
+  int kp = c.corner_prev[k], kn = c.corner_next[k];
+  int g[6], gp[6], gn[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    g[i] = b.gl[(int64_t)node * 6 + i];
+    gp[i] = kp >= 0 ? b.gl[(int64_t)c.corner_node[kp] * 6 + i] : -1;
+    gn[i] = kn >= 0 ? b.gl[(int64_t)c.corner_node[kn] * 6 + i] : -1;
+  }
+  const double* cl = eL >= 0 ? c.ec + (int64_t)eL * 156 : nullptr;
+  const double* cr = eR >= 0 ? c.ec + (int64_t)eR * 156 : nullptr;
+  double* D = c.cD + (int64_t)k * 36;
+  double* L = c.cL + (int64_t)k * 36;
+  double* U = c.cU + (int64_t)k * 36;
+  double* bb = c.cb + (int64_t)k * 6;
+  for (int i = 0; i < 6; ++i) {
+    for (int j = 0; j < 6; ++j) {
+      double d = band_at(band, g[i], g[j]);
+      if (cl) d += cl[i * 26 + 13 + 7 + j];  // -A_bs Z_b of the left element
+      if (cr) d += cr[i * 26 + 1 + j];       // -A_as Z_a of the right element
+      D[i * 6 + j] = d;
+      U[i * 6 + j] = kn >= 0 ? band_at(band, g[i], gn[j]) + (cr ? cr[i * 26 + 7 + j] : 0.0) : 0.0;
+      L[i * 6 + j] = kp >= 0 ? band_at(band, g[i], gp[j]) + (cl ? cl[i * 26 + 13 + 1 + j] : 0.0) : 0.0;
+    }
+    double r = P[g[i]];
+    if (cl) r += cl[i * 26 + 13];
+    if (cr) r += cr[i * 26];
+    bb[i] = r;
+  }
+}
+
+// ---- 3. cyclic reduction: eliminate odd positions ----
+__global__ void __launch_bounds__(CT) k_cr_eliminate(Batch b, ChainData c, int lo, int hi) {
+  extern __shared__ double smem[];
+  int t = lo + blockIdx.x * CT + threadIdx.x;
+  if (t >= hi) return;
+  CrItem it = c.odd[t];
+  if (!solving(b, it.structure)) return;
+  int k = it.corner;
+  double* A = smem + threadIdx.x;
+  const double* D = c.cD + (int64_t)k * 36;
+  const double* L = c.cL + (int64_t)k * 36;
+  const double* U = c.cU + (int64_t)k * 36;
+  const double* bb = c.cb + (int64_t)k * 6;
+#pragma unroll 1
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      A[(i * NC + j) * CT] = D[i * 6 + j];
+      A[(i * NC + 7 + j) * CT] = it.prev >= 0 ? L[i * 6 + j] : 0.0;
+      A[(i * NC + 13 + j) * CT] = it.next >= 0 ? U[i * 6 + j] : 0.0;
+    }
+    A[(i * NC + 6) * CT] = bb[i];
+  }
+  if (!gauss_jordan6(A, NC)) b.state[it.structure].info_fail = 1;
+  double* z = c.cz + (int64_t)k * 78;
+#pragma unroll 1
+  for (int i = 0; i < 6; ++i)
+#pragma unroll 1
+    for (int q = 0; q < 13; ++q) z[i * 13 + q] = A[(i * NC + 6 + q) * CT];
+}
+
+// ---- 3b. cyclic reduction: surviving positions absorb their neighbours ----
+// D -= U ZL(next) + L ZU(prev);  b -= U Zb(next) + L Zb(prev);
+// U <- -U ZU(next);  L <- -L ZL(prev)
+__global__ void k_cr_update(Batch b, ChainData c, int lo, int hi) {
+  int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= hi) return;
+  CrItem it = c.even[t];
+  if (!solving(b, it.structure)) return;
+  int k = it.corner;
+  double* D = c.cD + (int64_t)k * 36;
+  double* L = c.cL + (int64_t)k * 36;
+  double* U = c.cU + (int64_t)k * 36;
+  double* bb = c.cb + (int64_t)k * 6;
+  const double* zn = it.next >= 0 ? c.cz + (int64_t)it.next * 78 : nullptr;
+  const double* zp = it.prev >= 0 ? c.cz + (int64_t)it.prev * 78 : nullptr;
+#pragma unroll 1
+  for (int i = 0; i < 6; ++i) {
+    double u[6], l[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      u[j] = U[i * 6 + j];
+      l[j] = L[i * 6 + j];
+    }
+    double nb = bb[i], nD[6], nU[6], nL[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      nD[q] = D[i * 6 + q];
+      nU[q] = 0.0;
+      nL[q] = 0.0;
+    }
+    if (zn) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        nb = fma(-u[j], zn[j * 13], nb);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          nD[q] = fma(-u[j], zn[j * 13 + 1 + q], nD[q]);
+          nU[q] = fma(-u[j], zn[j * 13 + 7 + q], nU[q]);
+        }
+      }
+    }
+    if (zp) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        nb = fma(-l[j], zp[j * 13], nb);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          nD[q] = fma(-l[j], zp[j * 13 + 7 + q], nD[q]);
+          nL[q] = fma(-l[j], zp[j * 13 + 1 + q], nL[q]);
+        }
+      }
+    }
+    bb[i] = nb;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      D[i * 6 + q] = nD[q];
+      U[i * 6 + q] = nU[q];
+      L[i * 6 + q] = nL[q];
+    }
+  }
+}
+
+// ---- 3c. the last position of each chain ----
+__global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
+  extern __shared__ double smem[];
+  int t = blockIdx.x * CT + threadIdx.x;
+  if (t >= c.n_roots) return;
+  int k = c.roots[t];
+  int s = c.corner_struct[k];
+  if (!solving(b, s)) return;
+  double* A = smem + threadIdx.x;
+  const double* D = c.cD + (int64_t)k * 36;
+  const double* bb = c.cb + (int64_t)k * 6;
+  for (int i = 0; i < 6; ++i) {
+    for (int j = 0; j < 6; ++j) A[(i * NC + j) * CT] = D[i * 6 + j];
+    A[(i * NC + 6) * CT] = bb[i];
+  }
+  if (!gauss_jordan6(A, 7)) b.state[s].info_fail = 1;
+  for (int i = 0; i < 6; ++i) c.cx[(int64_t)k * 6 + i] = A[(i * NC + 6) * CT];
+}
+
+// ---- 4. back substitution: x = Zb - ZL x_prev - ZU x_next ----
+__global__ void k_cr_back(Batch b, ChainData c, int lo, int hi) {
+  int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= hi) return;
+  CrItem it = c.odd[t];
+  if (!solving(b, it.structure)) return;
+  const double* z = c.cz + (int64_t)it.corner * 78;
+  double xp[6], xn[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    xp[j] = it.prev >= 0 ? c.cx[(int64_t)it.prev * 6 + j] : 0.0;
+    xn[j] = it.next >= 0 ? c.cx[(int64_t)it.next * 6 + j] : 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double x = z[i * 13];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      x = fma(-z[i * 13 + 1 + j], xp[j], x);
+      x = fma(-z[i * 13 + 7 + j], xn[j], x);
+    }
+    c.cx[(int64_t)it.corner * 6 + i] = x;
+  }
+}
+
+// ---- 4b. midside nodes, and the solution into P ----
+__global__ void k_chain_scatter(Batch b, ChainData c) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= c.n_chain_elems) return;
+  int e = c.elem_list[t];
+  int s = b.estruct[e];
+  if (!solving(b, s)) return;
+  const StructInfo inf = b.info[s];
+  double* P = b.P + inf.dof_off;
+  int ka = c.elem_corner_a[t], kb = c.elem_corner_b[t];
+  const double* z = c.ez + (int64_t)t * 78;
+  double xa[6], xb[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    xa[j] = ka >= 0 ? c.cx[(int64_t)ka * 6 + j] : 0.0;
+    xb[j] = kb >= 0 ? c.cx[(int64_t)kb * 6 + j] : 0.0;
+  }
+  int nm = b.enodes[3 * e + 1];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double x = z[i * 13];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      x = fma(-z[i * 13 + 1 + j], xa[j], x);
+      x = fma(-z[i * 13 + 7 + j], xb[j], x);
+    }
+    P[b.gl[(int64_t)nm * 6 + i]] = x;
+  }
+}
+
+__global__ void k_corner_scatter(Batch b, ChainData c) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n_corners) return;
+  int s = c.corner_struct[k];
+  if (!solving(b, s)) return;
+  const StructInfo inf = b.info[s];
+  double* P = b.P + inf.dof_off;
+  int node = c.corner_node[k];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) P[b.gl[(int64_t)node * 6 + i]] = c.cx[(int64_t)k * 6 + i];
+}
+
+}  // namespace
+
+void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
+  if (c.n_chain_elems == 0) return;
+  static bool attr = false;
+  const int smem = 6 * NC * CT * (int)sizeof(double);
+  if (!attr) {
+    cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_cr_eliminate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_cr_root, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  k_condense<<<(c.n_chain_elems + CT - 1) / CT, CT, smem, st>>>(b, c);
+  if (c.n_corners > 0) {
+    k_corner_system<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);
+    for (int l = 0; l < c.n_levels; ++l) {
+      int lo = c.odd_off[l], hi = c.odd_off[l + 1];
+      if (hi > lo) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, smem, st>>>(b, c, lo, hi);
+      int elo = c.even_off[l], ehi = c.even_off[l + 1];
+      if (ehi > elo) k_cr_update<<<(ehi - elo + 127) / 128, 128, 0, st>>>(b, c, elo, ehi);
+    }
+    k_cr_root<<<(c.n_roots + CT - 1) / CT, CT, smem, st>>>(b, c);
+    for (int l = c.n_levels - 1; l >= 0; --l) {
+      int lo = c.odd_off[l], hi = c.odd_off[l + 1];
+      if (hi > lo) k_cr_back<<<(hi - lo + 127) / 128, 128, 0, st>>>(b, c, lo, hi);
+    }
+    k_corner_scatter<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);
+  }
+  k_chain_scatter<<<(c.n_chain_elems + 127) / 128, 128, 0, st>>>(b, c);
+}
+
+}  // namespace gf

@@ -171,6 +171,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   std::vector<double> tdata;
   int node_off = 0, elem_off = 0, dof_off = 0;
   int max_color = 0;
+  std::vector<int> chain_flags;
+  std::vector<std::vector<char>> chain_free;
   for (int s = 0; s < n; ++s) {
     const gf_model_desc& m = models[s];
     if (m.solution.type != GF_STATIC) { set_err(ctx, "structure %d: only Static solution steps are supported", s); return GF_ERR_ARG; }
@@ -217,6 +219,22 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       return GF_ERR_ARG;
     }
     B->kb.push_back(kbs);
+    // chain structure: elements on nodes (2e, 2e+1, 2e+2), every node fully
+    // free or fully fixed, midside and interior corner nodes free
+    bool chain = m.n_beams > 0 && nn == 2 * m.n_beams + 1;
+    for (int e = 0; chain && e < m.n_beams; ++e)
+      chain = m.beams[6 * e] == 2 * e && m.beams[6 * e + 1] == 2 * e + 1 && m.beams[6 * e + 2] == 2 * e + 2;
+    std::vector<char> node_free(nn, 0);
+    for (int i = 0; chain && i < nn; ++i) {
+      int f = 0;
+      for (int k = 0; k < 6; ++k) f += g6[6 * i + k] >= 0;
+      if (f != 0 && f != 6) chain = false;
+      node_free[i] = f == 6;
+      bool interior = i > 0 && i < nn - 1;
+      if (interior && !node_free[i]) chain = false;
+    }
+    chain_flags.push_back(chain ? 1 : 0);
+    chain_free.push_back(node_free);
     // padding: every structure's DOF range starts at a multiple of 32
     int nf_pad = (nf + 31) / 32 * 32;
     for (int q = nf; q < nf_pad; ++q) dof_node6.push_back(-1);
@@ -230,6 +248,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     inf.band_off = (int64_t)dof_off * GF_LDB;
     inf.has_force = has_f;
     inf.has_moment = has_m;
+    inf.is_chain = chain_flags.back();
     // nodes
     for (int i = 0; i < nn; ++i) {
       for (int k = 0; k < 3; ++k) copy.push_back(m.node_xyz[3 * i + k]);
@@ -347,6 +366,76 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.n_loads = (int)loads.size();
   b.n_disps = (int)disps.size();
   b.n_tables = (int)tables.size();
+  // chain solver data
+  {
+    ChainData& cd = b.chain;
+    std::vector<int> elem_list, eca, ecb, cnode, cstruct, cleft, cright, cprev, cnext, roots;
+    std::vector<std::vector<CrItem>> odd_l(CR_MAX_LEVELS), even_l(CR_MAX_LEVELS);
+    int n_levels = 0;
+    for (int s = 0; s < n; ++s) {
+      if (!chain_flags[s]) continue;
+      const StructInfo& inf = B->info[s];
+      int mm = inf.n_elem;
+      const std::vector<char>& fr = chain_free[s];
+      int cbase = (int)cnode.size(), tbase = (int)elem_list.size();
+      std::vector<int> pos(mm + 1, -1);
+      int M = 0;
+      for (int ci = 0; ci <= mm; ++ci)
+        if (fr[2 * ci]) pos[ci] = M++;
+      for (int e = 0; e < mm; ++e) {
+        elem_list.push_back(inf.elem_off + e);
+        eca.push_back(pos[e] >= 0 ? cbase + pos[e] : -1);
+        ecb.push_back(pos[e + 1] >= 0 ? cbase + pos[e + 1] : -1);
+      }
+      for (int ci = 0; ci <= mm; ++ci) {
+        if (pos[ci] < 0) continue;
+        int k = pos[ci];
+        cnode.push_back(inf.node_off + 2 * ci);
+        cstruct.push_back(s);
+        cleft.push_back(ci >= 1 ? tbase + ci - 1 : -1);
+        cright.push_back(ci < mm ? tbase + ci : -1);
+        cprev.push_back(k > 0 ? cbase + k - 1 : -1);
+        cnext.push_back(k + 1 < M ? cbase + k + 1 : -1);
+      }
+      if (M >= 1) roots.push_back(cbase);
+      int l = 0;
+      for (int h = 1; h < M; h *= 2, ++l) {
+        if (l >= CR_MAX_LEVELS) { set_err(ctx, "chain too long for %d reduction levels", CR_MAX_LEVELS); return GF_ERR_ARG; }
+        for (int kp = h; kp < M; kp += 2 * h)
+          odd_l[l].push_back(CrItem{cbase + kp, cbase + kp - h, kp + h < M ? cbase + kp + h : -1, s});
+        for (int kp = 0; kp < M; kp += 2 * h) {
+          bool hp = kp - h >= 0, hn = kp + h < M;
+          if (hp || hn) even_l[l].push_back(CrItem{cbase + kp, hp ? cbase + kp - h : -1, hn ? cbase + kp + h : -1, s});
+        }
+      }
+      n_levels = std::max(n_levels, l);
+    }
+    std::vector<CrItem> odd, even;
+    for (int l = 0; l <= CR_MAX_LEVELS; ++l) {
+      cd.odd_off[l] = (int)odd.size();
+      cd.even_off[l] = (int)even.size();
+      if (l < CR_MAX_LEVELS) {
+        odd.insert(odd.end(), odd_l[l].begin(), odd_l[l].end());
+        even.insert(even.end(), even_l[l].begin(), even_l[l].end());
+      }
+    }
+    cd.n_chain_elems = (int)elem_list.size();
+    cd.n_corners = (int)cnode.size();
+    cd.n_levels = n_levels;
+    cd.n_roots = (int)roots.size();
+    if (cd.n_chain_elems) {
+      size_t ne = elem_list.size(), nc = std::max<size_t>(cnode.size(), 1);
+      if (!upload(B, &cd.elem_list, elem_list) || !upload(B, &cd.elem_corner_a, eca) ||
+          !upload(B, &cd.elem_corner_b, ecb) || !upload(B, &cd.corner_node, cnode) ||
+          !upload(B, &cd.corner_struct, cstruct) || !upload(B, &cd.corner_left, cleft) ||
+          !upload(B, &cd.corner_right, cright) || !upload(B, &cd.corner_prev, cprev) ||
+          !upload(B, &cd.corner_next, cnext) || !upload(B, &cd.odd, odd) || !upload(B, &cd.even, even) ||
+          !upload(B, &cd.roots, roots) || !balloc(B, &cd.ez, ne * 78) || !balloc(B, &cd.ec, ne * 156) ||
+          !balloc(B, &cd.cD, nc * 36) || !balloc(B, &cd.cL, nc * 36) || !balloc(B, &cd.cU, nc * 36) ||
+          !balloc(B, &cd.cb, nc * 6) || !balloc(B, &cd.cz, nc * 78) || !balloc(B, &cd.cx, nc * 6))
+        return GF_ERR_CUDA;
+    }
+  }
   // colour lists
   std::vector<int> color_elems;
   b.n_colors = max_color;
@@ -441,7 +530,17 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
   }
   int colors = 0;
   for (int c = 0; c < B->b.n_colors; ++c) colors += B->b.color_off[c + 1] > B->b.color_off[c];
-  B->launches_per_pass = 9 + colors;
+  const ChainData& cd = B->b.chain;
+  int chain_launches = 0;
+  if (cd.n_chain_elems) {
+    chain_launches = 2;
+    if (cd.n_corners) {
+      chain_launches += 3;
+      for (int l = 0; l < cd.n_levels; ++l)
+        chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
+    }
+  }
+  B->launches_per_pass = 9 + colors + chain_launches;
   return B;
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "gf_beam.cuh"
+#include "gf_chain.cuh"
 #include "gf_kernels.cuh"
 
 namespace gf {
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_band_solve(Batch b) {
   StructState& st = b.state[s];
   if (!iterating(st) || !st.need_solve) return;
   const StructInfo inf = b.info[s];
+  if (inf.is_chain) return;
   const int n = inf.n_free;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   extern __shared__ unsigned char smem_raw[];
@@ -745,6 +747,7 @@ void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, Laun
   { ProfScope q(prof, st, KC_LOADS); k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
+  if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_OTHER); launch_chain_solve(b, b.chain, st); }
   { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {

@@ -65,6 +65,7 @@ struct StructInfo {
   int64_t band_off;  // in entries; band of n_free columns x GF_LDB
   int has_force, has_moment;  // free translational / rotational DOFs exist
   int load_off, n_loads;  // nodal load entries of this structure
+  int is_chain;  // solved by the chain solver (else by the band LU)
 };
 
 // Per-structure Newton / load-step control state (reference
@@ -105,6 +106,47 @@ struct DispEntry {
 struct TableDev {
   int n_times, n_cols;
   int64_t off;  // into the batch's table storage: times then values
+};
+
+// Chain solver data (see gf_chain.cuh).
+#define CR_MAX_LEVELS 24
+
+// One cyclic-reduction item: a corner position with its neighbours at the
+// item's level (-1 when absent).
+struct CrItem {
+  int corner;  // batch-wide corner index
+  int prev;
+  int next;
+  int structure;
+};
+
+struct ChainData {
+  int n_chain_elems;   // elements of chain structures
+  int n_corners;       // free corners of chain structures
+  int n_levels;
+  int* elem_list;      // batch element ids of chain elements
+  int* elem_corner_a;  // corner index of the element's first corner (-1 if fixed)
+  int* elem_corner_b;  // corner index of the element's last corner (-1 if fixed)
+  int* corner_node;    // batch node id of each free corner
+  int* corner_struct;
+  int* corner_left;    // chain element to the left (-1 if none)
+  int* corner_right;   // chain element to the right (-1 if none)
+  int* corner_prev;    // previous free corner of the same chain (-1 if none)
+  int* corner_next;    // next free corner (-1 if none)
+  double* ez;          // [chain elem][6][13]  Z_s = A_ss^{-1}[b_s | A_sa | A_sb]
+  double* ec;          // [chain elem][6][26]  -A_as Z_s (13 cols), -A_bs Z_s (13 cols)
+  double* cD;          // [corner][36] (row-major 6x6)
+  double* cL;          // [corner][36]
+  double* cU;          // [corner][36]
+  double* cb;          // [corner][6]
+  double* cz;          // [corner][6][13]  Z = D^{-1}[b | L | U] of an eliminated corner
+  double* cx;          // [corner][6]  solution
+  CrItem* odd;         // per level: eliminated positions
+  int odd_off[CR_MAX_LEVELS + 1];
+  CrItem* even;        // per level: surviving positions with at least one eliminated neighbour
+  int even_off[CR_MAX_LEVELS + 1];
+  int* roots;          // per chain structure: the corner left after all levels
+  int n_roots;
 };
 
 // Device pointers of a batch.
@@ -150,6 +192,7 @@ struct Batch {
   int mixed;  // 1: FP32 factor with FP64 refinement
   int max_refine;
   int* running;  // structures still running after the last pass
+  ChainData chain;
 };
 
 }  // namespace gf

@@ -126,6 +126,47 @@ def test_batch_matches_oracle_and_is_order_independent(gpu_ctx):
     assert np.array_equal(rev[len(structs) - 1 - 5], finals[5])
 
 
+def _beam_variant(kind):
+    """Chain variants that exercise both linear solvers: clamped-clamped and
+    end-clamped chains go through the chain solver; pinned ends (only the
+    translations fixed) and a reversed node order go through the band LU."""
+    from giraffe_gb300.model import NodalLoad, Table
+
+    s = configs.pipe_chain(40, 0.3, 0.02, [0.0, 0.0, 0.0], element_length=0.25)
+    n = s.n_nodes
+    s.constraints[:] = 0
+    s.loads = []
+    mid = n // 2
+    if kind == "clamped-clamped":
+        s.clamp(0)
+        s.clamp(n - 1)
+    elif kind == "clamped-top":
+        s.clamp(n - 1)
+        mid = 0
+    elif kind == "pinned":
+        s.clamp(0, (1, 1, 1, 0, 0, 0))
+        s.clamp(n - 1, (1, 1, 1, 1, 0, 0))
+    elif kind == "reversed":
+        s.beams = [(b[2], b[1], b[0], *b[3:]) for b in s.beams]
+        s.clamp(0)
+        mid = n - 1
+    scale = 1e-2 if kind == "pinned" else 1.0
+    s.loads.append(NodalLoad([mid], 0, Table(np.array([0.0, 1.0]),
+                                             scale * np.array([[0.0] * 6, [4e5, -2e5, 1e5, 2e4, 0.0, -1e4]]))))
+    return s
+
+
+@pytest.mark.parametrize("kind", ["clamped-clamped", "clamped-top", "pinned", "reversed"])
+def test_solver_variants_match_oracle(gpu_ctx, kind):
+    s = _beam_variant(kind)
+    finals, stats = _solve_gpu(gpu_ctx, [s])
+    fo, so, _ = oracle.solve(s)
+    assert so[3] == 0
+    assert list(stats[0]) == list(so)
+    scale = np.abs(fo[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - fo[:, :3]).max() <= 1e-10 * scale
+
+
 def test_repeat_runs_are_bitwise_identical(gpu_ctx):
     from giraffe_gb300 import gpu
 
