@@ -145,12 +145,12 @@ def _beam_variant(kind):
         mid = 0
     elif kind == "pinned":
         s.clamp(0, (1, 1, 1, 0, 0, 0))
-        s.clamp(n - 1, (1, 1, 1, 1, 0, 0))
+        s.clamp(n - 1, (1, 1, 1, 0, 0, 1))  # torsion about the axis (z) restrained
     elif kind == "reversed":
         s.beams = [(b[2], b[1], b[0], *b[3:]) for b in s.beams]
         s.clamp(0)
         mid = n - 1
-    scale = 1e-2 if kind == "pinned" else 1.0
+    scale = 1.0
     s.loads.append(NodalLoad([mid], 0, Table(np.array([0.0, 1.0]),
                                              scale * np.array([[0.0] * 6, [4e5, -2e5, 1e5, 2e4, 0.0, -1e4]]))))
     return s
