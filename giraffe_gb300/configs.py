@@ -15,6 +15,13 @@
   Newton/bisection control either.
 * :func:`tutorial01` — the reference's tutorial01 deck (5 Beam_1 cantilever,
   tip force), built programmatically.
+* :func:`riser_chain` / :func:`batched_dynamic` — implicit dynamics: pipe
+  chains of 100-1000 elements (uniform from the seed), rho = 7850 kg/m^3,
+  Newmark beta = 0.25, gamma = 0.5, dt = 0.01 s, 1000 steps, the top node
+  driven laterally by u(t) = A sin(2 pi t / T) with A ~ U(0.5, 2) m and
+  T ~ U(5, 15) s (tabulated at every time step, so exact at step times), its
+  rotations held; bottom free.  E = 210 GPa and 0.5 m elements (chains of
+  50-500 m) are this generator's choices; the description fixes neither.
 
 Every generator is deterministic in its seed (numpy default_rng).
 """
@@ -24,7 +31,7 @@ import math
 
 import numpy as np
 
-from .model import GF_STATIC, NodalLoad, Solution, Structure, Table
+from .model import GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, Solution, Structure, Table
 
 E_STEEL = 210e9
 NU_STEEL = 0.3
@@ -78,6 +85,27 @@ def tutorial01() -> Structure:
     return s
 
 
+def tutorial10() -> Structure:
+    """The reference's tutorial10 deck: 5 Beam_1 elements, Dynamic step with a
+    prescribed base motion (translations and an Euler-angle rotation about z),
+    Newmark beta = 0.3, gamma = 0.5."""
+    s = Structure(nodes=np.array([[0.0, 0.0, 0.1 * i] for i in range(11)]))
+    s.nodes[:, 2] = [0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0]
+    mat = s.add_material(1e7, 0.3, 2000)
+    sec = s.add_rectangle(0.1, 0.1)
+    cs = s.add_cs((1, 0, 0), (0, 0, 1))
+    for e in range(5):
+        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    s.clamp(0)
+    s.displacements.append(NodalDisplacement([0], cs, Table(
+        np.array([0.0, 2.5, 5.0, 7.5, 10.0]),
+        np.array([[0, 0, 0, 0, 0, 0], [0, 0.5, 0.25, 0, 0, 0], [0, 0, 0, 0, 0, 3.14],
+                  [0, -0.5, -0.25, 0, 0, 0], [0, 0, 0, 0, 0, 0]], dtype=float))))
+    s.solution = Solution(GF_DYNAMIC, 0.0, 10.0, 0.005, 0.005, 0.001, 20, 3, 4, 1.0, sample=10,
+                          beta=0.3, gamma=0.5)
+    return s
+
+
 def pipe_chain(n_el: int, De: float, wall: float, tip_force, steps: int = 10,
                element_length: float = 1.0, tol: float = 1e-8) -> Structure:
     s = Structure(nodes=straight_chain(n_el, n_el * element_length, (0.0, 0.0, 1.0)))
@@ -109,3 +137,35 @@ def batched_static(n_chains: int = 512, seed: int = 0, n_min: int = 50, n_max: i
     return [pipe_chain(int(n), float(d), float(w), F[i], steps=steps, tol=tol,
                        element_length=chain_length / int(n))
             for i, (n, d, w) in enumerate(zip(n_el, De, wall))]
+
+
+def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, steps: int = 1000,
+                dt: float = 0.01, element_length: float = 0.5, tol: float = 1e-8) -> Structure:
+    L = n_el * element_length
+    s = Structure(nodes=straight_chain(n_el, L, (0.0, 0.0, 1.0)))
+    mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
+    sec = s.add_tube(De, De - 2.0 * wall)
+    cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+    for e in range(n_el):
+        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    top = 2 * n_el
+    s.clamp(top)
+    t = np.arange(steps + 1) * dt
+    vals = np.zeros((steps + 1, 6))
+    vals[:, 0] = amp * np.sin(2.0 * math.pi * t / period)
+    s.displacements.append(NodalDisplacement([top], cs, Table(t, vals)))
+    s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 64, 20, 3, 4, 1.0, beta=0.25, gamma=0.5)
+    s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, force_min=1.0, moment_min=1.0)
+    return s
+
+
+def batched_dynamic(n_chains: int = 256, seed: int = 0, n_min: int = 100, n_max: int = 1000,
+                    steps: int = 1000, tol: float = 1e-8) -> list:
+    rng = np.random.default_rng(seed)
+    n_el = rng.integers(n_min, n_max + 1, n_chains)
+    De = rng.uniform(0.3, 0.5, n_chains)
+    wall = rng.uniform(0.02, 0.04, n_chains)
+    amp = rng.uniform(0.5, 2.0, n_chains)
+    per = rng.uniform(5.0, 15.0, n_chains)
+    return [riser_chain(int(n), float(d), float(w), float(a), float(p), steps=steps, tol=tol)
+            for n, d, w, a, p in zip(n_el, De, wall, amp, per)]

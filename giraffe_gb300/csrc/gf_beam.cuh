@@ -283,6 +283,102 @@ GF_HD TK beam_K_entry(const BeamConst& c, const TK* M0, const TK* M1, int r, int
   return acc;
 }
 
+// Inertial contribution of one Gauss point (Beam_1::MountMass, reference
+// src/Beam_1.cpp:1564-1638, Hooke sections: no offset of the mass centre).
+// In the element frame, with Newmark coefficients a[0..5] = a1..a6:
+//   dT_u = Mr (a1 du - a2 v_i - a3 acc_i)
+//   dT_a = Xi(da) h,  h = J_i w2 + w1 x J_i w1,  J_i = Q(alpha_i) Jr Q(alpha_i)^T,
+//   w1 = a4 da + a5 w_i + a6 dw_i,  w2 = a1 da - a2 w_i - a3 dw_i
+// (Newmark in the tangent space transported by Q_delta, and Xi^T Q_delta = Xi
+// for Rodrigues parameters), and the exact tangent
+//   d dT_u/d du = a1 Mr I,
+//   d dT_a/d da = Xi (a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)))
+//                 - g^2/2 (h + da x h / 2) da^T - g/2 skew(h).
+// Adds wJ N_I dT (global frame) to f[(6I+i)*fs] and returns the rotated
+// rotational tangent T3^T (d dT_a/d da) T3 in Daa[q * ds]; the translational
+// tangent is a1 Mr I in every frame.
+GF_HD void beam_gp_inertia(const BeamConst& c, const BeamHistAux& x, const BeamInterp& ip, const double* vel,
+                           const double* acc, const double* a, int g, double* f, int fs, double* Daa, int ds) {
+  const double* N = c.N[g];
+  M3<double> T;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T[i] = c.T3[i];
+  V3<double> wi, dwi, vi, ai;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    wi[i] = vel[3 + i] * N[0] + vel[9 + i] * N[1] + vel[15 + i] * N[2];
+    dwi[i] = acc[3 + i] * N[0] + acc[9 + i] * N[1] + acc[15 + i] * N[2];
+    vi[i] = vel[i] * N[0] + vel[6 + i] * N[1] + vel[12 + i] * N[2];
+    ai[i] = acc[i] * N[0] + acc[6 + i] * N[1] + acc[12 + i] * N[2];
+  }
+  wi = mv(T, wi);
+  dwi = mv(T, dwi);
+  vi = mv(T, vi);
+  ai = mv(T, ai);
+  const double a1 = a[0], a2 = a[1], a3 = a[2], a4 = a[3], a5 = a[4], a6 = a[5];
+  V3<double> fu;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) fu[i] = c.Mr * (a1 * ip.u[i] - a2 * vi[i] - a3 * ai[i]);
+  V3<double> al = {{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}};
+  M3<double> Qi = rodrigues(al), Jr;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Jr[i] = c.Jr[i];
+  M3<double> Ji = mul(mul(Qi, Jr), transpose(Qi));
+  V3<double> w1, w2;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    w1[i] = a4 * ip.alpha[i] + a5 * wi[i] + a6 * dwi[i];
+    w2[i] = a1 * ip.alpha[i] - a2 * wi[i] - a3 * dwi[i];
+  }
+  V3<double> Jw1 = mv(Ji, w1), Jw2 = mv(Ji, w2), cr = cross(w1, Jw1), h;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) h[i] = Jw2[i] + cr[i];
+  double gg;
+  M3<double> Qd, Xi;
+  beam_rot(ip.alpha, gg, Qd, Xi);
+  V3<double> m = mv(Xi, h);
+  M3<double> t = mul(skew(w1), Ji), SJw1 = skew(Jw1), Dh;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) Dh[q] = a1 * Ji[q] + a4 * (t[q] - SJw1[q]);
+  M3<double> D = mul(Xi, Dh);
+  V3<double> axh = cross(ip.alpha, h);
+  M3<double> Sh = skew(h);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      D[i * 3 + j] += -0.5 * gg * gg * (h[i] + 0.5 * axh[i]) * ip.alpha[j] - 0.5 * gg * Sh[i * 3 + j];
+  M3<double> Dg = tmul(T, mul(D, T));
+#pragma unroll
+  for (int q = 0; q < 9; ++q) Daa[q * ds] = Dg[q];
+  V3<double> gu = tmv(T, fu), ga = tmv(T, m);
+  double wJ = c.jac;
+#pragma unroll
+  for (int I = 0; I < 3; ++I)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      f[(6 * I + i) * fs] += wJ * N[I] * gu[i];
+      f[(6 * I + 3 + i) * fs] += wJ * N[I] * ga[i];
+    }
+}
+
+// Inertial tangent entry (row r, column s of the 18x18, global frame).
+GF_HD double beam_M_entry(const BeamConst& c, const double* D0, const double* D1, int ds, double a1Mr, int r, int s) {
+  int I = r / 6, a = r % 6, J = s / 6, b = s % 6;
+  double acc = 0.0;
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    double w = c.jac * c.N[g][I] * c.N[g][J];
+    if (a < 3 && b < 3) {
+      if (a == b) acc += w * a1Mr;
+    } else if (a >= 3 && b >= 3) {
+      const double* D = g ? D1 : D0;
+      acc += w * D[((a - 3) * 3 + (b - 3)) * ds];
+    }
+  }
+  return acc;
+}
+
 // reference src/Beam_1.cpp:1494-1506
 GF_HD void beam_commit(const BeamConst& c, BeamHist& h, BeamHistAux& x, const double* d) {
 #pragma unroll 1

@@ -39,24 +39,30 @@ __device__ __forceinline__ double recip(double p) {
   return r;
 }
 
-// Gauss-Jordan on a thread's 6 x ncols augmented matrix A (row-major, entry
+// Gauss-Jordan on a thread's 6 x NCOLS augmented matrix A (row-major, entry
 // (r, c) at A[(r * NC + c) * CT]): on return columns 6.. hold D^{-1} RHS.
-// No pivoting; returns false on a zero or non-finite pivot.
-__device__ bool gauss_jordan6(double* A, int ncols) {
+// No pivoting; returns false on a zero or non-finite pivot.  Fully unrolled
+// so that the independent column updates of one pivot step overlap.
+template <int NCOLS>
+__device__ bool gauss_jordan6(double* A) {
   bool ok = true;
-#pragma unroll 1
+#pragma unroll
   for (int k = 0; k < 6; ++k) {
     double p = A[(k * NC + k) * CT];
     if (!(p != 0.0) || !isfinite(p)) ok = false;
     double inv = recip(p);
-#pragma unroll 1
-    for (int c = k + 1; c < ncols; ++c) A[(k * NC + c) * CT] *= inv;
-#pragma unroll 1
+    double rk[NCOLS];
+#pragma unroll
+    for (int c = k + 1; c < NCOLS; ++c) {
+      rk[c] = A[(k * NC + c) * CT] * inv;
+      A[(k * NC + c) * CT] = rk[c];
+    }
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
       if (i == k) continue;
       double m = A[(i * NC + k) * CT];
-#pragma unroll 1
-      for (int c = k + 1; c < ncols; ++c) A[(i * NC + c) * CT] = fma(-m, A[(k * NC + c) * CT], A[(i * NC + c) * CT]);
+#pragma unroll
+      for (int c = k + 1; c < NCOLS; ++c) A[(i * NC + c) * CT] = fma(-m, rk[c], A[(i * NC + c) * CT]);
     }
   }
   return ok;
@@ -93,7 +99,7 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
     }
     A[(i * NC + 6) * CT] = P[gm[i]];
   }
-  if (!gauss_jordan6(A, NC)) b.state[s].info_fail = 1;
+  if (!gauss_jordan6<NC>(A)) b.state[s].info_fail = 1;
   double* ez = c.ez + (int64_t)t * 78;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
@@ -185,7 +191,7 @@ __global__ void __launch_bounds__(CT) k_cr_eliminate(Batch b, ChainData c, int l
     }
     A[(i * NC + 6) * CT] = bb[i];
   }
-  if (!gauss_jordan6(A, NC)) b.state[it.structure].info_fail = 1;
+  if (!gauss_jordan6<NC>(A)) b.state[it.structure].info_fail = 1;
   double* z = c.cz + (int64_t)k * 78;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
     for (int j = 0; j < 6; ++j) A[(i * NC + j) * CT] = D[i * 6 + j];
     A[(i * NC + 6) * CT] = bb[i];
   }
-  if (!gauss_jordan6(A, 7)) b.state[s].info_fail = 1;
+  if (!gauss_jordan6<7>(A)) b.state[s].info_fail = 1;
   for (int i = 0; i < 6; ++i) c.cx[(int64_t)k * 6 + i] = A[(i * NC + 6) * CT];
 }
 

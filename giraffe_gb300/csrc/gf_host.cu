@@ -175,7 +175,11 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   std::vector<std::vector<char>> chain_free;
   for (int s = 0; s < n; ++s) {
     const gf_model_desc& m = models[s];
-    if (m.solution.type != GF_STATIC) { set_err(ctx, "structure %d: only Static solution steps are supported", s); return GF_ERR_ARG; }
+    if (m.solution.type != GF_STATIC && m.solution.type != GF_DYNAMIC) { set_err(ctx, "structure %d: unknown solution type", s); return GF_ERR_ARG; }
+    if (m.solution.type == GF_DYNAMIC && (m.solution.rayleigh_alpha != 0.0 || m.solution.rayleigh_beta != 0.0)) {
+      set_err(ctx, "structure %d: Rayleigh damping is not supported (alpha = beta = 0 required)", s);
+      return GF_ERR_ARG;
+    }
     if (m.n_shells) { set_err(ctx, "structure %d: Shell_1 elements are not supported by this entry point", s); return GF_ERR_ARG; }
     const int nn = m.n_nodes;
     std::vector<int> active(nn * 6, 0), c6(nn * 6, 0), g6(nn * 6, -2);
@@ -219,6 +223,14 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       return GF_ERR_ARG;
     }
     B->kb.push_back(kbs);
+    if (m.solution.type == GF_DYNAMIC)
+      for (int i = 0; i < nn; ++i) {
+        int fr = (g6[6 * i + 3] >= 0) + (g6[6 * i + 4] >= 0) + (g6[6 * i + 5] >= 0);
+        if (fr != 0 && fr != 3) {
+          set_err(ctx, "structure %d: dynamic nodes need all rotations free or all fixed (node %d)", s, i);
+          return GF_ERR_ARG;
+        }
+      }
     // chain structure: elements on nodes (2e, 2e+1, 2e+2), every node fully
     // free or fully fixed, midside and interior corner nodes free
     bool chain = m.n_beams > 0 && nn == 2 * m.n_beams + 1;
@@ -343,6 +355,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     p.max_it = so.max_it;
     p.min_it = so.min_it;
     p.conv_increase = so.conv_increase;
+    p.dynamic = so.type == GF_DYNAMIC;
+    p.beta = so.beta;
+    p.gamma = so.gamma;
     const gf_criteria& cr = m.criteria;
     p.force_tol = cr.force_tol;
     p.moment_tol = cr.moment_tol;
@@ -448,6 +463,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   // device arrays
   std::vector<double> zeros6((size_t)node_off * 6, 0.0);
   if (!upload(B, &b.copy, copy) || !upload(B, &b.Qn, Qn) || !upload(B, &b.disp, zeros6) || !upload(B, &b.gl, gl) ||
+      !upload(B, &b.vel, zeros6) || !upload(B, &b.accel, zeros6) || !upload(B, &b.copy_vel, zeros6) ||
+      !upload(B, &b.copy_accel, zeros6) ||
       !upload(B, &b.cons, cons) || !upload(B, &b.node_struct, node_struct) || !upload(B, &b.enodes, enodes) ||
       !upload(B, &b.estruct, estruct) || !upload(B, &b.bconst, bconst) || !upload(B, &b.bhist, bhist) ||
       !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
@@ -458,7 +475,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     return GF_ERR_CUDA;
   if (!balloc(B, &b.P, (size_t)dof_off) || !balloc(B, &b.y, (size_t)dof_off) ||
       !balloc(B, &b.band, (size_t)dof_off * GF_LDB) || !balloc(B, &b.U, (size_t)dof_off * GF_UW) ||
-      !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1))
+      !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
+      !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18))
     return GF_ERR_CUDA;
   CK(cudaMemset(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB));
   CK(cudaMemset(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1)));
@@ -475,7 +493,12 @@ int batch_reset(gf_batch* B) {
   CK(cudaMemcpyAsync(b.Qn, B->Qn0, sizeof(double) * (size_t)b.n_nodes * 9, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.bhist, B->bhist0, sizeof(BeamHist) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.baux, B->baux0, sizeof(BeamHistAux) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
-  CK(cudaMemsetAsync(b.disp, 0, sizeof(double) * (size_t)std::max(b.n_nodes, 1) * 6, st));
+  const size_t n6 = sizeof(double) * (size_t)std::max(b.n_nodes, 1) * 6;
+  CK(cudaMemsetAsync(b.disp, 0, n6, st));
+  CK(cudaMemsetAsync(b.vel, 0, n6, st));
+  CK(cudaMemsetAsync(b.accel, 0, n6, st));
+  CK(cudaMemsetAsync(b.copy_vel, 0, n6, st));
+  CK(cudaMemsetAsync(b.copy_accel, 0, n6, st));
   launch_init_state(b, st);
   CK(cudaGetLastError());
   return GF_OK;
@@ -540,7 +563,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
         chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
     }
   }
-  B->launches_per_pass = 9 + colors + chain_launches;
+  B->launches_per_pass = 10 + colors + chain_launches;
   return B;
 }
 
@@ -866,6 +889,59 @@ int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, c
     }
   }
   cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dK); cudaFree(df);
+  return rc;
+}
+
+int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
+                             const double* cs, int n_hist, const double* hist_disp, const double* disp,
+                             const double* vel, const double* acc, double dt, double beta, double gamma, double* M,
+                             double* F) {
+  if (!ctx || n <= 0 || !(dt > 0.0) || !(beta > 0.0)) return GF_ERR_ARG;
+  std::vector<BeamConst> c(n);
+  std::vector<BeamHist> h(n);
+  std::vector<BeamHistAux> x(n);
+  for (int e = 0; e < n; ++e)
+    beam_precalc(xyz + 9 * e, xyz + 9 * e + 6, mat + 3 * e, sec + 6 * e, cs + 6 * e, c[e], h[e], x[e]);
+  double a[6] = {1.0 / (dt * dt * beta), 1.0 / (dt * beta), 1.0 / (2.0 * beta) - 1.0, gamma / (dt * beta),
+                 1.0 - gamma / beta, dt * (1.0 - gamma / (2.0 * beta))};
+  BeamConst* dc = nullptr;
+  BeamHist* dh = nullptr;
+  BeamHistAux* dx = nullptr;
+  double *dd = nullptr, *dv = nullptr, *da = nullptr, *dA = nullptr, *dM = nullptr, *dF = nullptr;
+  int rc = GF_OK;
+  if (!dmalloc(ctx, &dc, n) || !dmalloc(ctx, &dh, n) || !dmalloc(ctx, &dx, n) || !dmalloc(ctx, &dd, (size_t)n * 18) ||
+      !dmalloc(ctx, &dv, (size_t)n * 18) || !dmalloc(ctx, &da, (size_t)n * 18) || !dmalloc(ctx, &dA, 6) ||
+      !dmalloc(ctx, &dM, (size_t)n * 324) || !dmalloc(ctx, &dF, (size_t)n * 18)) {
+    rc = GF_ERR_CUDA;
+  } else {
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(dc, c.data(), sizeof(BeamConst) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dh, h.data(), sizeof(BeamHist) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dx, x.data(), sizeof(BeamHistAux) * n, cudaMemcpyHostToDevice, st);
+    std::vector<double> step((size_t)n * 18);
+    for (int q = 0; q < n_hist; ++q) {
+      for (int e = 0; e < n; ++e)
+        std::memcpy(&step[(size_t)e * 18], hist_disp + ((size_t)e * n_hist + q) * 18, 18 * sizeof(double));
+      cudaMemcpyAsync(dd, step.data(), sizeof(double) * step.size(), cudaMemcpyHostToDevice, st);
+      launch_beam_commit(n, dc, dh, dx, dd, st);
+      cudaStreamSynchronize(st);
+    }
+    cudaMemcpyAsync(dd, disp, sizeof(double) * (size_t)n * 18, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dv, vel, sizeof(double) * (size_t)n * 18, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(da, acc, sizeof(double) * (size_t)n * 18, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dA, a, sizeof(a), cudaMemcpyHostToDevice, st);
+    launch_beam_inertia(n, dc, dx, dd, dv, da, dA, dM, dF, st);
+    cudaMemcpyAsync(M, dM, sizeof(double) * (size_t)n * 324, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(F, dF, sizeof(double) * (size_t)n * 18, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_err(ctx, "gf_beam_inertia_elements: %s", cudaGetErrorString(e));
+      rc = GF_ERR_CUDA;
+    }
+  }
+  cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dv); cudaFree(da); cudaFree(dA);
+  cudaFree(dM); cudaFree(dF);
   return rc;
 }
 

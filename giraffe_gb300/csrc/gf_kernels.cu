@@ -68,6 +68,37 @@ __device__ Red3 block_red(Red3 v) {
 
 __device__ __forceinline__ bool nan_or_huge(double v) { return !(v == v) || v >= 1e300 || v <= -1e300; }
 
+// UpdateDyn for one node (reference src/Dynamic.cpp:480-580): Newmark
+// velocity and acceleration of the free DOFs; the rotational ones are
+// transported by Q_delta.  Nodes have all rotations free or all fixed
+// (checked on the host), so the rotational vectors are complete.
+__device__ void update_dyn_node(const Batch& b, const double* a, int node) {
+  const int64_t o = (int64_t)node * 6;
+  const int* gl = b.gl + o;
+  const double* d = b.disp + o;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    if (gl[j] >= 0) {
+      b.vel[o + j] = d[j] * a[3] + b.copy_vel[o + j] * a[4] + b.copy_accel[o + j] * a[5];
+      b.accel[o + j] = d[j] * a[0] - b.copy_vel[o + j] * a[1] - b.copy_accel[o + j] * a[2];
+    }
+  if (gl[3] >= 0 || gl[4] >= 0 || gl[5] >= 0) {
+    V3<double> al = {{d[3], d[4], d[5]}}, va, aa;
+    for (int j = 0; j < 3; ++j) {
+      va[j] = d[3 + j] * a[3] + b.copy_vel[o + 3 + j] * a[4] + b.copy_accel[o + 3 + j] * a[5];
+      aa[j] = d[3 + j] * a[0] - b.copy_vel[o + 3 + j] * a[1] - b.copy_accel[o + 3 + j] * a[2];
+    }
+    M3<double> Qd = rodrigues(al);
+    va = mv(Qd, va);
+    aa = mv(Qd, aa);
+    for (int j = 0; j < 3; ++j)
+      if (gl[3 + j] >= 0) {
+        b.vel[o + 3 + j] = va[j];
+        b.accel[o + 3 + j] = aa[j];
+      }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // initial state: reference src/Static.cpp:140-170
 __global__ void k_init_state(Batch b) {
@@ -100,6 +131,16 @@ __global__ void k_step_begin(Batch b) {
         st.time_step = p.end_time - st.last_converged_time;
       }
       st.current_time_step = st.time_step;
+      if (p.dynamic) {
+        // reference src/Dynamic.cpp:582-590
+        double dt = st.time_step;
+        st.a[0] = 1.0 / (dt * dt * p.beta);
+        st.a[1] = 1.0 / (dt * p.beta);
+        st.a[2] = 1.0 / (2.0 * p.beta) - 1.0;
+        st.a[3] = p.gamma / (dt * p.beta);
+        st.a[4] = 1.0 - p.gamma / p.beta;
+        st.a[5] = dt * (1.0 - p.gamma / (2.0 * p.beta));
+      }
       st.it = 1;
       st.res_conv = 0;
       st.gl_conv = 0;
@@ -111,7 +152,15 @@ __global__ void k_step_begin(Batch b) {
   __syncthreads();
   if (!go) return;
   const StructInfo inf = b.info[s];
-  for (int i = threadIdx.x; i < inf.n_nodes * 6; i += blockDim.x) b.disp[(int64_t)inf.node_off * 6 + i] = 0.0;
+  const bool dyn = b.params[s].dynamic;
+  for (int i = threadIdx.x; i < inf.n_nodes * 6; i += blockDim.x) {
+    int64_t q = (int64_t)inf.node_off * 6 + i;
+    b.disp[q] = 0.0;
+    if (dyn) {  // back to the converged velocities (a no-op after a commit)
+      b.vel[q] = b.copy_vel[q];
+      b.accel[q] = b.copy_accel[q];
+    }
+  }
   __syncthreads();
   double time = st.last_converged_time + st.current_time_step, dt = st.current_time_step;
   for (int e = threadIdx.x; e < b.n_disps; e += blockDim.x) {
@@ -124,7 +173,14 @@ __global__ void k_step_begin(Batch b) {
     for (int j = 0; j < 3; ++j) dl[j] = table_at(b, D.table, time, j) - table_at(b, D.table, time - dt, j);
     for (int j = 0; j < 3; ++j) dg[j] = D.CQ[j] * dl[0] + D.CQ[3 + j] * dl[1] + D.CQ[6 + j] * dl[2];
     for (int j = 0; j < 3; ++j)
-      if (cons[j] == 1 && gl[j] == -1) b.disp[(int64_t)node * 6 + j] = dg[j];
+      if (cons[j] == 1 && gl[j] == -1) {
+        int64_t q = (int64_t)node * 6 + j;
+        b.disp[q] = dg[j];
+        if (dyn) {
+          b.vel[q] = dg[j] / dt;
+          b.accel[q] = (b.vel[q] - b.copy_vel[q]) / dt;
+        }
+      }
     double phi = cons[3] == 1 ? table_at(b, D.table, time, 3) : 0.0;
     double th = cons[4] == 1 ? table_at(b, D.table, time, 4) : 0.0;
     double psi = cons[5] == 1 ? table_at(b, D.table, time, 5) : 0.0;
@@ -146,8 +202,21 @@ __global__ void k_step_begin(Batch b) {
     if (tr > 3.0) tr = 3.0;
     double ax[3] = {0.5 * (Qd[7] - Qd[5]), 0.5 * (Qd[2] - Qd[6]), 0.5 * (Qd[3] - Qd[1])};
     double al = 2.0 * sqrt((3.0 - tr) / (1.0 + tr));
+    double theta = 2.0 * asin(sqrt((3.0 - tr) / 4.0));
+    double eu = theta != 0.0 ? theta / sin(theta) : 0.0;
     for (int j = 3; j < 6; ++j)
-      if (cons[j] == 1 && gl[j] == -1) b.disp[(int64_t)node * 6 + j] = ((4.0 + al * al) / 4.0) * ax[j - 3];
+      if (cons[j] == 1 && gl[j] == -1) {
+        int64_t q = (int64_t)node * 6 + j;
+        b.disp[q] = ((4.0 + al * al) / 4.0) * ax[j - 3];
+        if (dyn) {
+          b.vel[q] = eu * ax[j - 3] / dt;
+          b.accel[q] = (b.vel[q] - b.copy_vel[q]) / dt;
+        }
+      }
+  }
+  if (dyn) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < inf.n_nodes; i += blockDim.x) update_dyn_node(b, st.a, inf.node_off + i);
   }
 }
 
@@ -165,25 +234,31 @@ __global__ void k_zero(Batch b) {
 }
 
 // ---------------------------------------------------------------------------
-// Beam_1 Mount + MountElementLoads + MountGlobal for one colour class.
-// One thread per element.  The two rotated Gauss-point operators live in
-// shared memory ([g][entry][thread], conflict-free) while the 18x18 tangent is
-// streamed into the band; elements of one colour share no node, so the
-// scatter needs no atomics and is deterministic.
+// Beam_1 Mount + MountElementLoads (k_beam_tangent) and MountGlobal
+// (k_beam_scatter).
+//
+// k_beam_tangent: one thread per element, every element of every iterating
+// structure.  The two rotated Gauss-point operators live in shared memory
+// ([g][entry][thread], conflict-free); the 18x18 tangent (column-major) and
+// the 18 internal forces go to per-element scratch.  Keeping the band
+// read-modify-write out of this FP64-bound kernel keeps global-load latency
+// off its dependency chains.
+// k_beam_scatter: one warp per element of one colour class; lanes walk the
+// 324 tangent entries in column order, so the band updates of a column are
+// contiguous.  Elements of one colour share no node, so the scatter needs no
+// atomics and is deterministic.
 constexpr int MOUNT_THREADS = 64;
-constexpr int MOUNT_SMEM = (2 * 81 + 18) * MOUNT_THREADS * (int)sizeof(double);
+constexpr int MOUNT_SMEM = (2 * 81 + 18 + 18) * MOUNT_THREADS * (int)sizeof(double);
 
 template <typename TK>
-__global__ void __launch_bounds__(MOUNT_THREADS) k_beam_mount(Batch b, int color) {
+__global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
   extern __shared__ unsigned char smem_raw[];
   TK* sM = reinterpret_cast<TK*>(smem_raw);
   const int tid = threadIdx.x;
-  int k = b.color_off[color] + blockIdx.x * MOUNT_THREADS + tid;
-  if (k >= b.color_off[color + 1]) return;
-  int e = b.color_elems[k];
+  int e = blockIdx.x * MOUNT_THREADS + tid;
+  if (e >= b.n_elem) return;
   int s = b.estruct[e];
   if (!iterating(b.state[s])) return;
-  const StructInfo inf = b.info[s];
   const BeamConst& c = b.bconst[e];
   const BeamHist& h = b.bhist[e];
   int nd[3] = {b.enodes[3 * e], b.enodes[3 * e + 1], b.enodes[3 * e + 2]};
@@ -194,8 +269,12 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_mount(Batch b, int color
     for (int q = 0; q < 6; ++q) d[6 * j + q] = b.disp[(int64_t)nd[j] * 6 + q];
   BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
   double* f = reinterpret_cast<double*>(sM + (size_t)2 * 81 * MOUNT_THREADS) + tid;
+  double* Dm = f + 18 * MOUNT_THREADS;  // inertial rotational tangents, 2 x 9
 #pragma unroll
   for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
+  const StructParams& pr = b.params[s];
+  const bool dyn = pr.dynamic;
+  const double* an = b.state[s].a;
 #pragma unroll 1
   for (int g = 0; g < 2; ++g) {
     BeamGP kin;
@@ -205,50 +284,61 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_mount(Batch b, int color
     beam_gp_operator<TK>(c, kin, M, MOUNT_THREADS);
     rotate_blocks9<TK>(c, M, MOUNT_THREADS);
   }
-  int gl[18];
+  double a1Mr = 0.0;
+  if (dyn) {
+    // MountMass + MountDyn: inertial force and mass/gyroscopic tangent
+    double vel[18], acc[18];
 #pragma unroll
-  for (int j = 0; j < 3; ++j)
+    for (int j = 0; j < 3; ++j)
 #pragma unroll
-    for (int q = 0; q < 6; ++q) gl[6 * j + q] = b.gl[(int64_t)nd[j] * 6 + q];
-  double* P = b.P + inf.dof_off;
-#pragma unroll
-  for (int r = 0; r < 18; ++r)
-    if (gl[r] >= 0) P[gl[r]] += f[r * MOUNT_THREADS];
-  double* band = b.band + inf.band_off;
-#pragma unroll 1
-  for (int r = 0; r < 18; ++r) {
-    if (gl[r] < 0) continue;
-#pragma unroll 1
-    for (int q2 = 0; q2 < 18; ++q2) {
-      if (gl[q2] < 0) continue;
-      // beam_K_entry reads the operators from shared memory through small
-      // per-thread views
-      int I = r / 6, a = r % 6, J = q2 / 6, bb = q2 % 6;
-      TK acc = TK(0);
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const TK* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
-#define MM(i, j) M[((i) * 9 + (j)) * MOUNT_THREADS]
-        TK dNI = TK(c.dN[g][I]), NI = TK(c.N[g][I]), dNJ = TK(c.dN[g][J]), NJ = TK(c.N[g][J]);
-        TK w = TK(c.jac);
-        if (a < 3 && bb < 3) {
-          acc += w * dNI * dNJ * MM(a, bb);
-        } else if (a < 3) {
-          int b3 = bb - 3;
-          acc += w * dNI * (dNJ * MM(a, 3 + b3) + NJ * MM(a, 6 + b3));
-        } else if (bb < 3) {
-          int a3 = a - 3;
-          acc += w * (dNI * MM(3 + a3, bb) + NI * MM(6 + a3, bb)) * dNJ;
-        } else {
-          int a3 = a - 3, b3 = bb - 3;
-          acc += w * (dNI * dNJ * MM(3 + a3, 3 + b3) + dNI * NJ * MM(3 + a3, 6 + b3) +
-                      NI * dNJ * MM(6 + a3, 3 + b3) + NI * NJ * MM(6 + a3, 6 + b3));
-        }
-#undef MM
+      for (int q = 0; q < 6; ++q) {
+        vel[6 * j + q] = b.copy_vel[(int64_t)nd[j] * 6 + q];
+        acc[6 * j + q] = b.copy_accel[(int64_t)nd[j] * 6 + q];
       }
-      band[(GF_KB + gl[r] - gl[q2]) + (int64_t)gl[q2] * GF_LDB] += double(acc);
-    }
+    double a6[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) a6[q] = an[q];
+    const BeamHistAux& x = b.baux[e];
+#pragma unroll 1
+    for (int g = 0; g < 2; ++g)
+      beam_gp_inertia(c, x, ip[g], vel, acc, a6, g, f, MOUNT_THREADS, Dm + (size_t)g * 9 * MOUNT_THREADS, MOUNT_THREADS);
+    a1Mr = a6[0] * c.Mr;
   }
+  double* Ke = b.Ke + (int64_t)e * 324;
+#pragma unroll 1
+  for (int q2 = 0; q2 < 18; ++q2)
+#pragma unroll 1
+    for (int r = 0; r < 18; ++r) {
+      double k = double(beam_K_entry<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, r, q2, MOUNT_THREADS));
+      if (dyn) k += beam_M_entry(c, Dm, Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, r, q2);
+      Ke[r + 18 * q2] = k;
+    }
+  double* Fe = b.Fe + (int64_t)e * 18;
+#pragma unroll
+  for (int q = 0; q < 18; ++q) Fe[q] = f[q * MOUNT_THREADS];
+}
+
+__global__ void k_beam_scatter(Batch b, int color) {
+  int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  int k = b.color_off[color] + w;
+  if (k >= b.color_off[color + 1]) return;
+  int e = b.color_elems[k];
+  int s = b.estruct[e];
+  if (!iterating(b.state[s])) return;
+  const StructInfo inf = b.info[s];
+  int myg = -1;
+  if (lane < 18) myg = b.gl[(int64_t)b.enodes[3 * e + lane / 6] * 6 + lane % 6];
+  const double* Ke = b.Ke + (int64_t)e * 324;
+  double* band = b.band + inf.band_off;
+  for (int idx = lane; idx < 324; idx += 32) {
+    int r = idx % 18, q = idx / 18;
+    int gr = __shfl_sync(0xffffffffu, myg, r);
+    int gq = __shfl_sync(0xffffffffu, myg, q);
+    double v = Ke[idx];
+    if (gr >= 0 && gq >= 0) band[(GF_KB + gr - gq) + (int64_t)gq * GF_LDB] += v;
+  }
+  if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)e * 18 + lane];
 }
 
 // NodalLoad::Mount for every load entry of a structure, in entry order (one
@@ -524,6 +614,8 @@ __global__ void k_update(Batch b) {
   }
   Red3 ri = block_red(inc);
   Red3 rv = block_red(val);
+  if (b.params[s].dynamic)
+    for (int i = threadIdx.x; i < inf.n_nodes; i += blockDim.x) update_dyn_node(b, st.a, inf.node_off + i);
   if (threadIdx.x == 0) {
     st.res_conv = 0;
     if (ri.f) st.diverged = 1;
@@ -622,6 +714,11 @@ __global__ void k_commit_nodes(Batch b) {
   for (int k = 0; k < 3; ++k) c[3 + k] = a3[k];
   M3<double> Q = rodrigues(a3);
   for (int k = 0; k < 9; ++k) b.Qn[(int64_t)i * 9 + k] = Q[k];
+  if (b.params[s].dynamic)
+    for (int k = 0; k < 6; ++k) {
+      b.copy_vel[(int64_t)i * 6 + k] = b.vel[(int64_t)i * 6 + k];
+      b.copy_accel[(int64_t)i * 6 + k] = b.accel[(int64_t)i * 6 + k];
+    }
 }
 
 // Element-level entry (no batch): tangent and internal force, FP64.
@@ -657,6 +754,31 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_elements(int n, const Be
   for (int q = 0; q < 18; ++q) fs[(int64_t)e * 18 + q] = f[q * MOUNT_THREADS];
 }
 
+// Element-level inertia (no batch): M (18x18 column-major, global) and F.
+__global__ void k_beam_inertia_elements(int n, const BeamConst* cs, const BeamHistAux* xs, const double* ds,
+                                        const double* vs, const double* as, const double* a, double* Ms,
+                                        double* Fs) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const BeamConst& c = cs[e];
+  double d[18], vel[18], acc[18], f[18], D[18];
+  for (int q = 0; q < 18; ++q) {
+    d[q] = ds[(int64_t)e * 18 + q];
+    vel[q] = vs[(int64_t)e * 18 + q];
+    acc[q] = as[(int64_t)e * 18 + q];
+    f[q] = 0.0;
+  }
+  double an[6];
+  for (int q = 0; q < 6; ++q) an[q] = a[q];
+  for (int g = 0; g < 2; ++g) {
+    BeamInterp ip = beam_interp(c, d, g);
+    beam_gp_inertia(c, xs[e], ip, vel, acc, an, g, f, 1, D + 9 * g, 1);
+  }
+  for (int r = 0; r < 18; ++r)
+    for (int q = 0; q < 18; ++q) Ms[(int64_t)e * 324 + r + 18 * q] = beam_M_entry(c, D, D + 9, 1, an[0] * c.Mr, r, q);
+  for (int q = 0; q < 18; ++q) Fs[(int64_t)e * 18 + q] = f[q];
+}
+
 __global__ void k_beam_commit(int n, const BeamConst* cs, BeamHist* hs, BeamHistAux* xs, const double* ds) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
@@ -672,6 +794,11 @@ __global__ void k_beam_commit(int n, const BeamConst* cs, BeamHist* hs, BeamHist
 }  // namespace
 
 // ---------------------------------------------------------------------------
+void launch_beam_inertia(int n, const BeamConst* c, const BeamHistAux* x, const double* d, const double* v,
+                         const double* a_acc, const double* a, double* M, double* F, cudaStream_t st) {
+  if (n > 0) k_beam_inertia_elements<<<(n + 63) / 64, 64, 0, st>>>(n, c, x, d, v, a_acc, a, M, F);
+}
+
 void launch_beam_commit(int n, const BeamConst* c, BeamHist* h, BeamHistAux* x, const double* d, cudaStream_t st) {
   if (n > 0) k_beam_commit<<<(n + 127) / 128, 128, 0, st>>>(n, c, h, x, d);
 }
@@ -685,24 +812,24 @@ static bool g_attr_set = false;
 
 static void set_attrs();
 
+namespace {
+struct ProfScope;
+}
+static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof);
+
 void launch_iteration_partial(const Batch& b, cudaStream_t st) {
   set_attrs();
   int ns = b.n_struct;
   k_step_begin<<<ns, 256, 0, st>>>(b);
   k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
-  for (int c = 0; c < b.n_colors; ++c) {
-    int cnt = b.color_off[c + 1] - b.color_off[c];
-    if (cnt <= 0) continue;
-    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b, c);
-  }
+  launch_mount(b, st, nullptr);
   k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
   k_residual<<<ns, 256, 0, st>>>(b);
 }
 
 static void set_attrs() {
   if (!g_attr_set) {
-    cudaFuncSetAttribute(k_beam_mount<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         MOUNT_SMEM);
+    cudaFuncSetAttribute(k_beam_tangent<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
     cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (RING * GF_LDB + RING) * (int)sizeof(double));
     g_attr_set = true;
@@ -710,8 +837,8 @@ static void set_attrs() {
 }
 
 const char* kernel_class_name(int k) {
-  static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_mount", "loads", "residual", "band_solve",
-                                        "update", "control", "commit_elems", "commit_nodes", "init_state", "other"};
+  static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_tangent", "loads", "residual", "band_solve",
+                                        "update", "control", "commit_elems", "commit_nodes", "chain_solve", "scatter"};
   return k >= 0 && k < KC_COUNT ? names[k] : "?";
 }
 
@@ -733,21 +860,30 @@ struct ProfScope {
 };
 }  // namespace
 
+static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
+  if (b.n_elem == 0) return;
+  {
+    ProfScope q(prof, st, KC_MOUNT);
+    k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+  }
+  for (int c = 0; c < b.n_colors; ++c) {
+    int cnt = b.color_off[c + 1] - b.color_off[c];
+    if (cnt <= 0) continue;
+    ProfScope q(prof, st, KC_SCATTER);
+    k_beam_scatter<<<(cnt + 3) / 4, 128, 0, st>>>(b, c);
+  }
+}
+
 void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, LaunchProf* prof) {
   set_attrs();
   int ns = b.n_struct;
   { ProfScope q(prof, st, KC_STEP_BEGIN); k_step_begin<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_ZERO); k_zero<<<dim3(8, ns), 256, 0, st>>>(b); }
-  for (int c = 0; c < b.n_colors; ++c) {
-    int cnt = b.color_off[c + 1] - b.color_off[c];
-    if (cnt <= 0) continue;
-    ProfScope q(prof, st, KC_MOUNT);
-    k_beam_mount<double><<<(cnt + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b, c);
-  }
+  launch_mount(b, st, prof);
   { ProfScope q(prof, st, KC_LOADS); k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
-  if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_OTHER); launch_chain_solve(b, b.chain, st); }
+  if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_CHAIN); launch_chain_solve(b, b.chain, st); }
   { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {

@@ -35,7 +35,7 @@ struct LaunchProf {
 };
 enum KernelClass {
   KC_STEP_BEGIN = 0, KC_ZERO, KC_MOUNT, KC_LOADS, KC_RESIDUAL, KC_SOLVE, KC_UPDATE, KC_CONTROL,
-  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_INIT, KC_OTHER, KC_COUNT
+  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_COUNT
 };
 const char* kernel_class_name(int k);
 
@@ -48,6 +48,10 @@ void launch_iteration_partial(const Batch& b, cudaStream_t st);
 // Commit of n standalone elements with nodal increments d ([n][18]).
 void launch_beam_commit(int n, const BeamConst* c, BeamHist* h, BeamHistAux* x, const double* d, cudaStream_t st);
 void launch_init_state(const Batch& b, cudaStream_t st);
+// Inertial force and tangent of n standalone elements; a: 6 Newmark
+// coefficients in device memory.
+void launch_beam_inertia(int n, const BeamConst* c, const BeamHistAux* x, const double* d, const double* v,
+                         const double* a_acc, const double* a, double* M, double* F, cudaStream_t st);
 
 // Element-level entry: tangent (18x18 column-major) and internal force of n
 // elements in the global frame, FP64.  d: [n][18] nodal increments.

@@ -52,7 +52,8 @@ enum Phase : int { PH_START = 0, PH_ITER = 1, PH_DONE = 2, PH_ABORTED = 3 };
 // Per-structure parameters (Static solution step + ConvergenceCriteria).
 struct StructParams {
   double start_time, end_time, time_step0, max_time_step, min_time_step, inc_factor;
-  int max_it, min_it, conv_increase, pad0;
+  int max_it, min_it, conv_increase, dynamic;  // dynamic: Newmark step (Dynamic::Solve)
+  double beta, gamma;  // Newmark parameters
   double force_tol, moment_tol, force_min, moment_min, disp_tol, rot_tol, disp_min, rot_min,
       divergence_ref;
 };
@@ -82,6 +83,7 @@ struct StructState {
   double time, time_step, last_converged_time, current_time_step;
   double force_crit, moment_crit, disp_crit, rot_crit;
   double last_res, last_inc;
+  double a[6];  // Newmark coefficients of the current step
 };
 
 // One nodal load entry (one node of a NodalLoad node set).
@@ -157,6 +159,10 @@ struct Batch {
   double* disp;
   double* copy;
   double* Qn;
+  double* vel;         // Newmark velocities (dynamic structures)
+  double* accel;
+  double* copy_vel;    // converged velocities / accelerations
+  double* copy_accel;
   int* gl;
   int* cons;
   int* node_struct;
@@ -176,6 +182,8 @@ struct Batch {
   double* xr;  // refinement: accumulated solution
   double* r;   // refinement: residual
   // band and factor
+  double* Ke;  // per-element tangent scratch (18x18 column-major)
+  double* Fe;  // per-element internal force scratch
   double* band;
   float* band32;
   double* U;

@@ -19,7 +19,9 @@ GF_PREC_FP64, GF_PREC_MIXED = 0, 1
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_batch_create",
            "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
-           "gf_beam_elements", "gf_band_solve"]
+           "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
+           "gf_kernel_name", "gf_batch_bytes", "gf_batch_work", "gf_device_fp_peaks",
+           "gf_beam_inertia_elements"]
 
 
 class gf_solve_opts(C.Structure):
@@ -64,6 +66,8 @@ def lib():
                                C.POINTER(dp), C.POINTER(gf_stats)]
         L.gf_beam_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         L.gf_band_solve.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
+        L.gf_beam_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
+                                               C.c_double, C.c_double, dp, dp]
         _lib = L
     return _lib
 
@@ -113,6 +117,18 @@ class Context:
         self.check(self.L.gf_beam_elements(self.h, n, _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]), _dp(arrs[3]), nh,
                                            _dp(hd), _dp(arrs[4]), _dp(K), _dp(f)), "gf_beam_elements")
         return K.reshape(n, 18, 18).transpose(0, 2, 1), f
+
+    def beam_inertia(self, xyz, mat, sec, cs, hist_disp, disp, vel, acc, dt, beta, gamma):
+        n = xyz.shape[0]
+        nh = 0 if hist_disp is None else hist_disp.shape[1]
+        M = np.zeros((n, 324))
+        F = np.zeros((n, 18))
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz, mat, sec, cs, disp, vel, acc)]
+        hd = np.ascontiguousarray(hist_disp if nh else np.zeros((n, 1, 18)), dtype=np.float64)
+        self.check(self.L.gf_beam_inertia_elements(self.h, n, *[_dp(a) for a in arrs[:4]], nh, _dp(hd), _dp(arrs[4]),
+                                                   _dp(arrs[5]), _dp(arrs[6]), dt, beta, gamma, _dp(M), _dp(F)),
+                   "gf_beam_inertia_elements")
+        return M.reshape(n, 18, 18).transpose(0, 2, 1), F
 
     def band_solve(self, ab, kl, ku, b):
         ab = np.ascontiguousarray(ab, dtype=np.float64)  # [n][ldab] (column j contiguous)

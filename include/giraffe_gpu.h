@@ -10,13 +10,15 @@
  *
  * Reference interfaces each entry point replaces (paths in the reference
  * repository alfredogneto/GIRAFFE):
- *   gf_solve / gf_batch_*   Solution::Solve of a Static solution step for one
- *                           or many structures: src/Static.cpp:140-311 with
+ *   gf_solve / gf_batch_*   Solution::Solve of a Static or Dynamic solution
+ *                           step for one or many structures:
+ *                           src/Static.cpp:140-311, src/Dynamic.cpp:255-590 with
  *                           Solution::MountLocal/MountGlobal/UpdateDisps/
  *                           SaveConfiguration/RestoreConfiguration
  *                           (src/Solution.cpp:227-575) and the
  *                           ConvergenceCriteria checks
  *                           (src/ConvergenceCriteria.cpp:187-618)
+ *   gf_beam_inertia_elements Beam_1::MountMass (src/Beam_1.cpp:1564-1638)
  *   gf_beam_elements        Beam_1::PreCalc + SaveLagrange + Mount +
  *                           MountElementLoads (src/Beam_1.cpp:501-843,
  *                           1494-1506)
@@ -131,6 +133,17 @@ int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opt
 int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
                      const double* cs, int n_hist, const double* hist_disp, const double* disp, double* K,
                      double* f);
+
+/* Inertial contributions of n independent Beam_1 elements (replaces
+ * Beam_1::MountMass, reference src/Beam_1.cpp:1564-1638, for Hooke
+ * sections): geometry, history and increments as gf_beam_elements, plus the
+ * converged nodal velocities and accelerations (n x 18 each) and the Newmark
+ * step (dt, beta, gamma; reference src/Dynamic.cpp:582-590).  M: n x 324
+ * mass/gyroscopic tangent (column-major), F: n x 18 inertial force. */
+int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
+                             const double* cs, int n_hist, const double* hist_disp, const double* disp,
+                             const double* vel, const double* acc, double dt, double beta, double gamma,
+                             double* M, double* F);
 
 /* Solves A x = b for a banded matrix given in the reference's BandMatrix
  * storage (LAPACK GB: entry (i,j) at ab[(kl+ku+i-j) + j*ldab], ldab >=

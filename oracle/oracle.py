@@ -24,6 +24,8 @@ def lib():
         _lib.oracle_solve_batch.argtypes = [C.c_int, C.c_void_p, C.POINTER(dp), ip, C.c_int]
         _lib.oracle_beam_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         _lib.oracle_first_tangent.argtypes = [C.c_void_p, dp, dp, ip]
+        _lib.oracle_beam_inertia_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double,
+                                                     C.c_double, dp, dp, dp]
     return _lib
 
 
@@ -91,3 +93,16 @@ def first_tangent(structure):
     P = np.zeros(n)
     lib().oracle_first_tangent(C.cast(h.ref, C.c_void_p), _dp(ab), _dp(P), dims)
     return ab, P, kl
+
+
+def beam_inertia(xyz9, mat3, sec6, cs6, hist_disp, disp18, vel18, acc18, dt, beta, gamma):
+    M = np.zeros(324)
+    F = np.zeros(18)
+    ke = np.zeros(1)
+    nh = 0 if hist_disp is None else len(hist_disp)
+    hd = np.ascontiguousarray(hist_disp if nh else np.zeros((1, 18)), dtype=np.float64)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz9, mat3, sec6, cs6, disp18, vel18, acc18)]
+    lib().oracle_beam_inertia_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), _dp(args[3]), nh, _dp(hd),
+                                      _dp(args[4]), _dp(args[5]), _dp(args[6]), dt, beta, gamma, _dp(M), _dp(F),
+                                      _dp(ke))
+    return M.reshape(18, 18).T, F, ke[0]

@@ -263,3 +263,127 @@ void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d) {
     memcpy(h->alpha[g], an, sizeof(an));
   }
 }
+
+/* Beam_1::MountMass (reference src/Beam_1.cpp:1564-1638) for Hooke sections
+ * (no offset of the mass centre).  At each Gauss point, in the element frame:
+ *   translation  dT_u = Mr (a1 du - a2 v_i - a3 acc_i)
+ *   rotation     omega = Q_d w1, omega_dot = Q_d w2 with w1 = a4 da + c1,
+ *                w2 = a1 da + c2, c1 = a5 w_i + a6 dw_i, c2 = -a2 w_i - a3 dw_i
+ *                (Newmark in the tangent space, transported by Q_d as in
+ *                reference src/Dynamic.cpp:513-551); spatial inertia
+ *                J = Q J_r Q^T, Q = Q_d Q(alpha_i);
+ *                m = J omega_dot + omega x J omega;  dT_a = Xi(da)^T m.
+ * Since Xi^T Q_d = Xi for Rodrigues parameters, dT_a = Xi(da) h with
+ * h = J_i w2 + w1 x J_i w1, J_i = Q(alpha_i) J_r Q(alpha_i)^T.  The tangent is
+ * its exact derivative:
+ *   d dT_u / d du = a1 Mr I
+ *   d dT_a / d da = Xi (a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)))
+ *                   - g^2/2 (h + da x h / 2) da^T - g/2 skew(h).
+ * The element sums wJ N^T dT and wJ N^T DdT N and turns them to the global
+ * frame. */
+void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, const double* vel,
+                         const double* acc, const double* a, double* K, double* f, double* kinetic) {
+  double Kl[18 * 18], fl[18];
+  memset(Kl, 0, sizeof(Kl));
+  memset(fl, 0, sizeof(fl));
+  double ke = 0.0;
+  const double a1 = a[0], a2 = a[1], a3 = a[2], a4 = a[3], a5 = a[4], a6 = a[5];
+  for (int g = 0; g < 2; ++g) {
+    const double* N = c->N[g];
+    double da[3] = {0, 0, 0}, du[3] = {0, 0, 0}, wi[3] = {0, 0, 0}, dwi[3] = {0, 0, 0}, vi[3] = {0, 0, 0},
+           ai[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int n = 0; n < 3; ++n) {
+        da[i] += d[6 * n + 3 + i] * N[n];
+        du[i] += d[6 * n + i] * N[n];
+        wi[i] += vel[6 * n + 3 + i] * N[n];
+        dwi[i] += acc[6 * n + 3 + i] * N[n];
+        vi[i] += vel[6 * n + i] * N[n];
+        ai[i] += acc[6 * n + i] * N[n];
+      }
+    m3_vec(da, c->T3, da);
+    m3_vec(du, c->T3, du);
+    m3_vec(wi, c->T3, wi);
+    m3_vec(dwi, c->T3, dwi);
+    m3_vec(vi, c->T3, vi);
+    m3_vec(ai, c->T3, ai);
+    double dT[6], DdT[36];
+    memset(DdT, 0, sizeof(DdT));
+    for (int i = 0; i < 3; ++i) {
+      dT[i] = c->Mr * (a1 * du[i] - a2 * vi[i] - a3 * ai[i]);
+      DdT[i * 6 + i] = a1 * c->Mr;
+    }
+    double Qi[9], Ji[9], t[9];
+    rodrigues_Q(Qi, h->alpha[g]);
+    m3_mul(t, Qi, c->Jr);
+    m3_mult(Ji, t, Qi);
+    double w1[3], w2[3], Jw1[3], Jw2[3], cr[3], hv[3];
+    for (int i = 0; i < 3; ++i) {
+      w1[i] = a4 * da[i] + a5 * wi[i] + a6 * dwi[i];
+      w2[i] = a1 * da[i] - a2 * wi[i] - a3 * dwi[i];
+    }
+    m3_vec(Jw1, Ji, w1);
+    m3_vec(Jw2, Ji, w2);
+    v3_cross(cr, w1, Jw1);
+    for (int i = 0; i < 3; ++i) hv[i] = Jw2[i] + cr[i];
+    double n2 = v3_dot(da, da);
+    double gg = 4.0 / (4.0 + n2);
+    double A[9], Xi[9];
+    m3_skew(A, da);
+    for (int q = 0; q < 9; ++q) Xi[q] = gg * 0.5 * A[q];
+    Xi[0] += gg; Xi[4] += gg; Xi[8] += gg;
+    double m[3];
+    m3_vec(m, Xi, hv);
+    for (int i = 0; i < 3; ++i) dT[3 + i] = m[i];
+    /* dh/dda = a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)) */
+    double Sw1[9], SJw1[9], Dh[9];
+    m3_skew(Sw1, w1);
+    m3_skew(SJw1, Jw1);
+    m3_mul(t, Sw1, Ji);
+    for (int q = 0; q < 9; ++q) Dh[q] = a1 * Ji[q] + a4 * (t[q] - SJw1[q]);
+    double XDh[9], axh[3], hh[3], Sh[9];
+    m3_mul(XDh, Xi, Dh);
+    v3_cross(axh, da, hv);
+    for (int i = 0; i < 3; ++i) hh[i] = hv[i] + 0.5 * axh[i];
+    m3_skew(Sh, hv);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        DdT[(3 + i) * 6 + 3 + j] = XDh[i * 3 + j] - 0.5 * gg * gg * hh[i] * da[j] - 0.5 * gg * Sh[i * 3 + j];
+    double wJ = 1.0 * c->jac;
+    for (int I = 0; I < 3; ++I) {
+      for (int i = 0; i < 6; ++i) fl[6 * I + i] += wJ * N[I] * dT[i];
+      for (int J = 0; J < 3; ++J)
+        for (int i = 0; i < 6; ++i)
+          for (int j = 0; j < 6; ++j) Kl[(6 * I + i) + 18 * (6 * J + j)] += wJ * N[I] * N[J] * DdT[i * 6 + j];
+    }
+    /* kinetic energy of the Gauss point at the end of the step */
+    double v1[3], om[3], Qd[9], Jom[3];
+    for (int i = 0; i < 3; ++i) v1[i] = a4 * du[i] + a5 * vi[i] + a6 * ai[i];
+    rodrigues_Q(Qd, da);
+    m3_vec(om, Qd, w1);
+    double Q[9];
+    m3_mul(Q, Qd, Qi);
+    m3_mul(t, Q, c->Jr);
+    double J[9];
+    m3_mult(J, t, Q);
+    m3_vec(Jom, J, om);
+    ke += wJ * (0.5 * c->Mr * v3_dot(v1, v1) + 0.5 * v3_dot(om, Jom));
+  }
+  const double* T = c->T3;
+  for (int bi = 0; bi < 6; ++bi)
+    for (int bj = 0; bj < 6; ++bj) {
+      double blk[9], t2[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) blk[i * 3 + j] = Kl[(3 * bi + i) + 18 * (3 * bj + j)];
+      m3_mul(t2, blk, T);
+      m3_tmul(blk, T, t2);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) K[(3 * bi + i) + 18 * (3 * bj + j)] += blk[i * 3 + j];
+    }
+  for (int bi = 0; bi < 6; ++bi) {
+    double t3[3];
+    m3_tvec(t3, T, fl + 3 * bi);
+    for (int i = 0; i < 3; ++i) f[3 * bi + i] += t3[i];
+  }
+  if (kinetic) *kinetic = ke;
+}

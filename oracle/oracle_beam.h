@@ -29,4 +29,9 @@ void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, 
 void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
                        double* strain_energy);
 void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);
+/* Inertial force and its tangent (MountMass, Newmark coefficients a[6]);
+ * vel/acc: [3][6] converged nodal velocities and accelerations. Adds to K
+ * (18x18 column-major, global frame) and f. */
+void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, const double* vel,
+                         const double* acc, const double* a, double* K, double* f, double* kinetic);
 #endif

@@ -33,6 +33,8 @@
 #include "band_lu.h"
 #include "oracle_beam.h"
 
+static void newmark_coeff(double dt, double beta, double gamma, double* a);
+
 typedef struct {
   const gf_model_desc* m;
   int nn, nb;
@@ -54,6 +56,8 @@ typedef struct {
   /* loads: per nodal load, force/moment multipliers */
   double (*mult)[6];
   double last_converged_time, current_time_step;
+  int dynamic;
+  double a[6];  /* Newmark coefficients of the current step */
 } ost;
 
 static void ost_free(ost* s) {
@@ -158,6 +162,15 @@ static void assemble(ost* s) {
     const int* b = m->beams + 6 * e;
     for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
     oracle_beam_mount(s->bc + e, s->bh + e, d, K, f, NULL);
+    if (s->dynamic) {
+      /* MountMass + MountDyn (reference src/Beam_1.cpp:1564-1638, 1668-1673) */
+      double v[18], ac[18];
+      for (int j = 0; j < 3; ++j) {
+        memcpy(v + 6 * j, s->copy_vel + 6 * b[j], 6 * sizeof(double));
+        memcpy(ac + 6 * j, s->copy_accel + 6 * b[j], 6 * sizeof(double));
+      }
+      oracle_beam_inertia(s->bc + e, s->bh + e, d, v, ac, s->a, K, f, NULL);
+    }
     int g[18];
     for (int a = 0; a < 18; ++a) g[a] = s->GL[6 * b[a / 6] + a % 6];
     for (int a = 0; a < 18; ++a) {
@@ -459,6 +472,115 @@ static int static_solve(ost* s, oracle_record* rec, int* stats) {
   return aborted ? 1 : 0;
 }
 
+/* UpdateDyn (reference src/Dynamic.cpp:480-580): Newmark velocities and
+ * accelerations of the free DOFs; rotational ones transported by Q_delta.
+ * The rotational scratch vectors persist across nodes within one call, as in
+ * the reference (it only matters for nodes with some rotations fixed). */
+static void update_dyn(ost* s) {
+  const double* a = s->a;
+  double vaux[3] = {0, 0, 0}, aaux[3] = {0, 0, 0};
+  for (int i = 0; i < s->nn; ++i) {
+    const double* d = s->disp + 6 * i;
+    for (int j = 0; j < 3; ++j)
+      if (s->GL[6 * i + j] > 0) {
+        s->vel[6 * i + j] = d[j] * a[3] + s->copy_vel[6 * i + j] * a[4] + s->copy_accel[6 * i + j] * a[5];
+        s->accel[6 * i + j] = d[j] * a[0] - s->copy_vel[6 * i + j] * a[1] - s->copy_accel[6 * i + j] * a[2];
+      }
+    double Qd[9];
+    rodrigues_Q(Qd, d + 3);
+    for (int j = 3; j < 6; ++j)
+      if (s->GL[6 * i + j] > 0) {
+        vaux[j - 3] = d[j] * a[3] + s->copy_vel[6 * i + j] * a[4] + s->copy_accel[6 * i + j] * a[5];
+        aaux[j - 3] = d[j] * a[0] - s->copy_vel[6 * i + j] * a[1] - s->copy_accel[6 * i + j] * a[2];
+      }
+    m3_vec(vaux, Qd, vaux);
+    m3_vec(aaux, Qd, aaux);
+    for (int j = 3; j < 6; ++j)
+      if (s->GL[6 * i + j] > 0) {
+        s->vel[6 * i + j] = vaux[j - 3];
+        s->accel[6 * i + j] = aaux[j - 3];
+      }
+  }
+}
+
+/* reference src/Dynamic.cpp:255-468 (no contact, no special constraints,
+ * Rayleigh alpha = beta = 0, zero initial conditions) */
+static int dynamic_solve(ost* s, oracle_record* rec, int* stats) {
+  const gf_solution* so = &s->m->solution;
+  int aborted = 0, convergence_counter = 0, converged_number = 0, total_it = 0, bisections = 0;
+  s->n_conv_evaluated = 0;
+  s->last_converged_time = so->start_time;
+  record(s, rec, so->start_time, 0);
+  double time_step = so->time_step, time = s->last_converged_time;
+  /* ComputeInitialConditions with zero initial conditions: Zeros() and a
+   * SaveConfiguration that leaves every node unchanged */
+  memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+  for (int i = 0; i < s->nn * 6; ++i) { s->copy_vel[i] = s->vel[i]; s->copy_accel[i] = s->accel[i]; }
+  s->diverged = 0;
+  while ((time < so->end_time || s->diverged) && !aborted) {
+    s->last_converged_time = time;
+    time += time_step;
+    if (time > 0.99999999 * so->end_time) {
+      time = so->end_time;
+      time_step = so->end_time - s->last_converged_time;
+    }
+    s->current_time_step = time_step;
+    newmark_coeff(time_step, so->beta, so->gamma, s->a);
+    int it = 1;
+    memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+    mount_displacements(s);
+    update_dyn(s);
+    int res_conv = 0, gl_conv = 0;
+    s->diverged = 0;
+    while ((!res_conv || !gl_conv) && !s->diverged && !aborted) {
+      assemble(s);
+      if (it == 1) establish_residual_criteria(s);
+      res_conv = check_residual(s);
+      int info_fail = 0;
+      if (!(res_conv && gl_conv)) {
+        info_fail = solve_linear(s);
+        res_conv = 0;
+        for (int i = 0; i < s->nn; ++i)
+          for (int k = 0; k < 6; ++k)
+            if (s->cons[6 * i + k] == 0 && s->active[6 * i + k] == 1)
+              s->disp[6 * i + k] += s->PA[s->GL[6 * i + k] - 1];
+        update_dyn(s);
+        gl_conv = check_gl(s);
+      }
+      if ((it == so->max_it && !(res_conv && gl_conv)) || info_fail) s->diverged = 1;
+      if (time_step < so->min_time_step && time != so->end_time) aborted = 1;
+      it++;
+      total_it++;
+    }
+    if (!s->diverged) {
+      converged_number++;
+      save_configuration(s);
+      convergence_counter++;
+      if (!aborted) record(s, rec, time, it - 1);
+      if (it <= so->min_it || convergence_counter >= so->conv_increase) {
+        time_step = time_step * so->inc_factor;
+        if (time_step > so->max_time_step) time_step = so->max_time_step;
+        convergence_counter = 0;
+      }
+    } else {
+      memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+      for (int i = 0; i < s->nn * 6; ++i) { s->vel[i] = s->copy_vel[i]; s->accel[i] = s->copy_accel[i]; }
+      time -= time_step;
+      time_step = time_step / 2.0;
+      s->diverged = 0;
+      convergence_counter = 0;
+      bisections++;
+    }
+  }
+  if (stats) {
+    stats[0] = converged_number;
+    stats[1] = total_it;
+    stats[2] = bisections;
+    stats[3] = aborted;
+  }
+  return aborted ? 1 : 0;
+}
+
 static void final_state(ost* s, double* out) {
   if (!out) return;
   for (int i = 0; i < s->nn; ++i) {
@@ -468,10 +590,12 @@ static void final_state(ost* s, double* out) {
 }
 
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
-  if (m->solution.type != GF_STATIC || m->n_shells) return -1;
+  if (m->n_shells) return -1;
+  if (m->solution.type == GF_DYNAMIC && (m->solution.rayleigh_alpha != 0.0 || m->solution.rayleigh_beta != 0.0)) return -1;
   ost s;
   ost_init(&s, m);
-  int r = static_solve(&s, rec, stats);
+  s.dynamic = m->solution.type == GF_DYNAMIC;
+  int r = s.dynamic ? dynamic_solve(&s, rec, stats) : static_solve(&s, rec, stats);
   final_state(&s, final_nodes);
   ost_free(&s);
   return r;
@@ -515,5 +639,31 @@ int oracle_first_tangent(const gf_model_desc* m, double* ab, double* PA, int* di
     memcpy(PA, s.PA, sizeof(double) * (size_t)s.n_free);
   }
   ost_free(&s);
+  return 0;
+}
+
+/* Newmark coefficients (reference src/Dynamic.cpp:582-590). */
+static void newmark_coeff(double dt, double beta, double gamma, double* a) {
+  a[0] = 1.0 / (dt * dt * beta);
+  a[1] = 1.0 / (dt * beta);
+  a[2] = 1.0 / (2.0 * beta) - 1.0;
+  a[3] = gamma / (dt * beta);
+  a[4] = 1.0 - gamma / beta;
+  a[5] = dt * (1.0 - gamma / (2.0 * beta));
+}
+
+int oracle_beam_inertia_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
+                                int n_hist, const double* hist_disp, const double* disp18, const double* vel18,
+                                const double* acc18, double dt, double beta, double gamma, double* M, double* F,
+                                double* ke) {
+  ob_const c;
+  ob_hist h;
+  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, &c, &h);
+  for (int q = 0; q < n_hist; ++q) oracle_beam_commit(&c, &h, hist_disp + 18 * q);
+  double a[6];
+  newmark_coeff(dt, beta, gamma, a);
+  memset(M, 0, sizeof(double) * 324);
+  memset(F, 0, sizeof(double) * 18);
+  oracle_beam_inertia(&c, &h, disp18, vel18, acc18, a, M, F, ke);
   return 0;
 }

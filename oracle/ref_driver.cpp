@@ -288,6 +288,35 @@ int giraffe_ref_element_mount(int e, double* K, double* P) {
   return n;
 }
 
+// Converged nodal velocities and accelerations (Node::copy_vel / copy_accel).
+void giraffe_ref_set_vel_accel(int node, const double* vel6, const double* accel6) {
+  for (int k = 0; k < 6; ++k) {
+    db.nodes[node - 1]->copy_vel[k] = vel6[k];
+    db.nodes[node - 1]->copy_accel[k] = accel6[k];
+  }
+}
+
+// Beam_1 inertial contributions of the first solution step, which must be
+// Dynamic: Newmark coefficients for time step dt
+// (reference src/Dynamic.cpp:582-590), then Mount (Gauss-point increments)
+// and MountMass (reference src/Beam_1.cpp:1564-1638).  M: 18x18 column-major
+// mass/gyroscopic tangent, F: inertial_loading, *ke: kinetic energy.
+int giraffe_ref_beam_inertia(int e, double dt, double* M, double* F, double* ke) {
+  if (typeid(*db.solution[0]) != typeid(Dynamic)) return 0;
+  Dynamic* d = static_cast<Dynamic*>(db.solution[0]);
+  d->CalculateNewmarkCoeff(dt);
+  db.current_solution_number = 1;
+  Element* el = db.elements[e - 1];
+  if (typeid(*el) != typeid(Beam_1)) return 0;
+  Beam_1* b = static_cast<Beam_1*>(el);
+  b->Mount();
+  b->MountMass();
+  memcpy(M, b->mass->getMatrix(), sizeof(double) * 324);
+  memcpy(F, b->inertial_loading->getMatrix(), sizeof(double) * 18);
+  *ke = b->kinetic_energy;
+  return 18;
+}
+
 // Commits the current increments as converged (reference
 // src/Solution.cpp:426-530 for nodes and elements) and zeroes them
 // (reference src/Solution.cpp:798-814).  SaveLagrange reads the Gauss-point

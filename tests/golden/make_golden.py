@@ -16,6 +16,12 @@ stores what the reference computes:
                          (Sample 2) and its Newton solve counts.
 * ref_rollup.npz         20-element roll-up into a circle, every step.
 * ref_chain.npz          a 30-element pipe chain under a tip force, 10 steps.
+* ref_tutorial10.npz     the reference's tutorial10: Dynamic step (Newmark),
+                         prescribed base translation and rotation, 2000 steps
+                         (every 10th configuration, as the deck's Sample).
+* ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
+                         single elements (Beam_1::MountMass) with random
+                         history, increments, nodal velocities/accelerations.
 
 Node records hold copy_coordinates (position and accumulated Rodrigues
 vector) then the nodal Q (row-major); Gauss-point records hold Q_i
@@ -171,6 +177,52 @@ def run_elements(L, cases, tmp):
     return res
 
 
+def run_inertia(L, cases, tmp, rng):
+    dp = C.POINTER(C.c_double)
+    L.giraffe_ref_set_vel_accel.argtypes = [C.c_int, dp, dp]
+    L.giraffe_ref_beam_inertia.argtypes = [C.c_int, C.c_double, dp, dp, dp]
+    out = {k: [] for k in ("xyz", "mat", "sec6", "cs", "hist", "disp", "vel", "acc", "dt", "beta", "gamma",
+                           "M", "F", "ke")}
+    nh_list = []
+    for i, c in enumerate(cases):
+        s = Structure(nodes=c["xyz"])
+        mat = s.add_material(*c["mat"])
+        sec = s.add_rectangle(c["sec"][1], c["sec"][2]) if c["sec"][0] == "rect" else s.add_tube(c["sec"][1], c["sec"][2])
+        cs = s.add_cs(c["e1"], c["e3"])
+        s.beams.append((0, 1, 2, mat, sec, cs))
+        beta, gamma, dt = rng.uniform(0.25, 0.35), rng.uniform(0.5, 0.6), rng.uniform(1e-3, 2e-2)
+        s.solution = Solution(1, 0.0, 1.0, dt, dt, dt / 100, 20, 3, 4, 1.0, beta=beta, gamma=gamma)
+        deck = os.path.join(tmp, f"in{i}.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        L.giraffe_ref_prepare()
+        for h in c["hist"]:
+            for n in range(3):
+                L.giraffe_ref_set_increment(n + 1, _dp(np.ascontiguousarray(h[n])))
+            L.giraffe_ref_commit()
+        vel = rng.normal(size=(3, 6))
+        acc = rng.normal(size=(3, 6)) * 5
+        for n in range(3):
+            L.giraffe_ref_set_vel_accel(n + 1, _dp(np.ascontiguousarray(vel[n])), _dp(np.ascontiguousarray(acc[n])))
+            L.giraffe_ref_set_increment(n + 1, _dp(np.ascontiguousarray(c["disp"][n])))
+        M = np.zeros(324)
+        F = np.zeros(18)
+        ke = np.zeros(1)
+        assert L.giraffe_ref_beam_inertia(1, dt, _dp(M), _dp(F), _dp(ke)) == 18
+        hist = np.zeros((3, 18))
+        hist[: len(c["hist"])] = c["hist"].reshape(-1, 18)
+        for k, v in (("xyz", c["xyz"].ravel()), ("mat", np.array(s.materials[0])), ("sec6", np.array(s.sections[0])),
+                     ("cs", np.array(s.cs[0])), ("hist", hist), ("disp", c["disp"].ravel()), ("vel", vel.ravel()),
+                     ("acc", acc.ravel()), ("dt", dt), ("beta", beta), ("gamma", gamma), ("M", M.reshape(18, 18).T),
+                     ("F", F), ("ke", ke[0])):
+            out[k].append(v)
+        nh_list.append(len(c["hist"]))
+    res = {k: np.array(v) for k, v in out.items()}
+    res["n_hist"] = np.array(nh_list)
+    return res
+
+
 def small_chain():
     return configs.pipe_chain(30, 0.4, 0.03, [1.5e5, -1.0e5, 0.8e5], element_length=10.0 / 30)
 
@@ -183,6 +235,9 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_tutorial01.npz"), **run_deck(L, configs.tutorial01(), "t01", tmp))
         np.savez_compressed(os.path.join(HERE, "ref_rollup.npz"), **run_deck(L, configs.cantilever_rollup(), "roll", tmp))
         np.savez_compressed(os.path.join(HERE, "ref_chain.npz"), **run_deck(L, small_chain(), "chain", tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_tutorial10.npz"), **run_deck(L, configs.tutorial10(), "t10", tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_beam_inertia.npz"),
+                            **run_inertia(L, element_cases(rng, 16), tmp, rng))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

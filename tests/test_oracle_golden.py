@@ -21,6 +21,18 @@ def test_beam_elements_match_reference(golden):
         assert rel(f, g["P"][i]) < 1e-12, i
 
 
+def test_beam_inertia_matches_reference(golden):
+    g = golden("ref_beam_inertia.npz")
+    for i in range(len(g["M"])):
+        nh = int(g["n_hist"][i])
+        M, F, ke = oracle.beam_inertia(g["xyz"][i], g["mat"][i], g["sec6"][i], g["cs"][i], g["hist"][i][:nh],
+                                       g["disp"][i], g["vel"][i], g["acc"][i], float(g["dt"][i]),
+                                       float(g["beta"][i]), float(g["gamma"][i]))
+        assert rel(M, g["M"][i]) < 1e-12, i
+        assert rel(F, g["F"][i]) < 1e-12, i
+        assert abs(ke - g["ke"][i]) <= 1e-12 * abs(g["ke"][i]), i
+
+
 def _check_run(g, s, tol=1e-11):
     final, stats, rec = oracle.solve(s, record_cap=4096)
     assert stats[3] == 0 and int(g["rc"]) == 0
@@ -52,6 +64,10 @@ def test_rollup_matches_reference(golden):
 def test_chain_matches_reference(golden):
     from tests.golden.make_golden import small_chain
     _check_run(golden("ref_chain.npz"), small_chain())
+
+
+def test_tutorial10_dynamics_matches_reference(golden):
+    _check_run(golden("ref_tutorial10.npz"), configs.tutorial10(), tol=1e-10)
 
 
 def test_rollup_known_answer():
