@@ -331,12 +331,14 @@ __global__ void k_beam_scatter(Batch b, int color) {
   if (lane < 18) myg = b.gl[(int64_t)b.enodes[3 * e + lane / 6] * 6 + lane % 6];
   const double* Ke = b.Ke + (int64_t)e * 324;
   double* band = b.band + inf.band_off;
-  for (int idx = lane; idx < 324; idx += 32) {
-    int r = idx % 18, q = idx / 18;
+  // uniform trip count: every lane takes part in every shuffle
+  for (int base = 0; base < 324; base += 32) {
+    int idx = base + lane;
+    bool valid = idx < 324;
+    int r = valid ? idx % 18 : 0, q = valid ? idx / 18 : 0;
     int gr = __shfl_sync(0xffffffffu, myg, r);
     int gq = __shfl_sync(0xffffffffu, myg, q);
-    double v = Ke[idx];
-    if (gr >= 0 && gq >= 0) band[(GF_KB + gr - gq) + (int64_t)gq * GF_LDB] += v;
+    if (valid && gr >= 0 && gq >= 0) band[(GF_KB + gr - gq) + (int64_t)gq * GF_LDB] += Ke[idx];
   }
   if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)e * 18 + lane];
 }
