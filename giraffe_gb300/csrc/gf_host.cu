@@ -996,3 +996,110 @@ int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab
 }
 
 }  // extern "C"
+
+// ---- gf_band_solve_noalloc: the banded solve staged through static device
+// scratch instead of per-call buffers ----
+namespace {
+constexpr size_t round256(size_t doubles) { return (doubles + 31) / 32 * 32; }
+constexpr size_t NA_BAND = (size_t)GF_NOALLOC_MAX_N * GF_LDB;  // band, GF layout
+constexpr size_t NA_P = NA_BAND;                                // right-hand side / solution
+constexpr size_t NA_U = NA_P + round256(GF_NOALLOC_MAX_N);      // U rows
+constexpr size_t NA_INFO = NA_U + round256((size_t)GF_NOALLOC_MAX_N * GF_UW);
+constexpr size_t NA_STATE = NA_INFO + round256((sizeof(StructInfo) + 7) / 8);
+constexpr size_t NA_TOTAL = NA_STATE + round256((sizeof(StructState) + 7) / 8);
+constexpr int NA_MAX_DEVICES = 64;
+void* g_noalloc_base[NA_MAX_DEVICES] = {};
+
+struct DeviceGuard {
+  int prev = -1;
+  bool switched = false;
+  ~DeviceGuard() {
+    if (switched) cudaSetDevice(prev);
+  }
+};
+}  // namespace
+
+// about 7 MB per device: GF_NOALLOC_MAX_N x (GF_LDB + 1 + GF_UW) doubles
+static __device__ __align__(256) double g_noalloc_scratch[NA_TOTAL];
+
+// Zeroes every scratch band entry that is not a stored entry of the caller's
+// matrix: rows outside the kl/ku band and the triangle corners (i < 0 or
+// i >= n), whatever an earlier call or the caller's unreferenced GB entries
+// left there.
+__global__ void k_noalloc_band_clean(double* band, int n, int kl, int ku) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * GF_LDB) return;
+  int j = (int)(t / GF_LDB), r = (int)(t % GF_LDB);
+  int i = j + r - GF_KB;
+  if (r < GF_KB - ku || r > GF_KB + kl || i < 0 || i >= n) band[t] = 0.0;
+}
+
+extern "C" int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b,
+                                     int* info) {
+  if (!ctx) return GF_ERR_ARG;
+  if (n <= 0 || kl < 0 || ku < 0 || kl > GF_KB || ku > GF_KB || ldab < 2 * kl + ku + 1 || !ab || !b) {
+    set_err(ctx, "gf_band_solve_noalloc: invalid arguments (kl, ku must be <= %d)", GF_KB);
+    return GF_ERR_ARG;
+  }
+  if (n > GF_NOALLOC_MAX_N) {
+    set_err(ctx, "gf_band_solve_noalloc: n = %d exceeds the static scratch limit GF_NOALLOC_MAX_N = %d; "
+                 "use gf_band_solve", n, (int)GF_NOALLOC_MAX_N);
+    return GF_ERR_ARG;
+  }
+  if (ctx->device < 0 || ctx->device >= NA_MAX_DEVICES) {
+    set_err(ctx, "gf_band_solve_noalloc: device %d out of range", ctx->device);
+    return GF_ERR_ARG;
+  }
+  DeviceGuard guard;
+  CK(cudaGetDevice(&guard.prev));
+  if (guard.prev != ctx->device) {
+    CK(cudaSetDevice(ctx->device));
+    guard.switched = true;
+  }
+  double* base = static_cast<double*>(g_noalloc_base[ctx->device]);
+  if (!base) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_err(ctx, "gf_band_solve_noalloc: cudaGetSymbolAddress of the static scratch failed: %s",
+              cudaGetErrorString(e));
+      return GF_ERR_CUDA;
+    }
+    g_noalloc_base[ctx->device] = p;
+    base = static_cast<double*>(p);
+  }
+  double* dband = base;
+  double* dP = base + NA_P;
+  double* dU = base + NA_U;
+  StructInfo* dinf = reinterpret_cast<StructInfo*>(base + NA_INFO);
+  StructState* dst = reinterpret_cast<StructState*>(base + NA_STATE);
+  StructInfo inf{};
+  inf.n_free = n;
+  StructState st0{};
+  st0.phase = PH_ITER;
+  st0.need_solve = 1;
+  cudaStream_t s = ctx->stream;
+  // column j's stored rows kl .. 2kl+ku of ab land on band rows GF_KB-ku .. GF_KB+kl
+  CK(cudaMemcpy2DAsync(dband + (GF_KB - ku), sizeof(double) * GF_LDB, ab + kl, sizeof(double) * (size_t)ldab,
+                       sizeof(double) * (size_t)(kl + ku + 1), (size_t)n, cudaMemcpyHostToDevice, s));
+  int64_t cells = (int64_t)n * GF_LDB;
+  k_noalloc_band_clean<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(dband, n, kl, ku);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(dP, b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dinf, &inf, sizeof(inf), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dst, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
+  Batch bt{};
+  bt.n_struct = 1;
+  bt.band = dband;
+  bt.P = dP;
+  bt.U = dU;
+  bt.info = dinf;
+  bt.state = dst;
+  launch_band_solve(bt, s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(b, dP, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&st0, dst, sizeof(st0), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (info) *info = st0.info_fail;
+  return GF_OK;
+}

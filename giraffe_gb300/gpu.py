@@ -21,7 +21,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
            "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
            "gf_kernel_name", "gf_batch_bytes", "gf_batch_work", "gf_device_fp_peaks",
-           "gf_beam_inertia_elements"]
+           "gf_beam_inertia_elements", "gf_band_solve_noalloc"]
 
 
 class gf_solve_opts(C.Structure):
@@ -66,6 +66,7 @@ def lib():
                                C.POINTER(dp), C.POINTER(gf_stats)]
         L.gf_beam_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         L.gf_band_solve.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
+        L.gf_band_solve_noalloc.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
         L.gf_beam_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
                                                C.c_double, C.c_double, dp, dp]
         _lib = L
@@ -136,6 +137,16 @@ class Context:
         x = np.ascontiguousarray(b, dtype=np.float64).copy()
         info = C.c_int(0)
         self.check(self.L.gf_band_solve(self.h, n, kl, ku, _dp(ab), ldab, _dp(x), C.byref(info)), "gf_band_solve")
+        return x, info.value
+
+    def band_solve_noalloc(self, ab, kl, ku, b):
+        """gf_band_solve_noalloc: band_solve through the static device scratch."""
+        ab = np.ascontiguousarray(ab, dtype=np.float64)
+        n, ldab = ab.shape
+        x = np.ascontiguousarray(b, dtype=np.float64).copy()
+        info = C.c_int(0)
+        self.check(self.L.gf_band_solve_noalloc(self.h, n, kl, ku, _dp(ab), ldab, _dp(x), C.byref(info)),
+                   "gf_band_solve_noalloc")
         return x, info.value
 
 

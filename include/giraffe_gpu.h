@@ -152,6 +152,20 @@ int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double
  * info_fail. */
 int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
 
+/* No counterpart in the reference.  The same solve as gf_band_solve, same
+ * arguments and results, for callers that must not allocate device memory
+ * per call: a host loop that runs under another allocator's budget, or one
+ * that cannot afford cudaMalloc/cudaFree, which synchronise the whole device.
+ * Work arrays live in one static device array per device sized for
+ * GF_NOALLOC_MAX_N unknowns (about 7 MB); no cudaMalloc, cudaFree or other
+ * allocating routine is called.  n > GF_NOALLOC_MAX_N returns GF_ERR_ARG
+ * (use gf_band_solve).  The first call on each device looks up the array's
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Every context on a device shares the array: overlapping calls on
+ * one device, from two threads or two contexts, race. */
+enum { GF_NOALLOC_MAX_N = 16384 };
+int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
+
 #ifdef __cplusplus
 }
 #endif
