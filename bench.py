@@ -32,6 +32,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "Newton solves/sec (batched static Beam_1 chains, FP64, converged load steps)"
 UNIT = "Newton solves/s"
+# DRAM bytes per element mount of k_beam_tangent, from one ncu capture on 128
+# chains: (57.3 MB read + 182.9 MB written) / 79,322 elements
+TANGENT_DRAM_BYTES_PER_ELEMENT = (57.312768e6 + 182.872576e6) / 79322
 
 
 def parse():
@@ -267,8 +270,14 @@ def run_ours(args, rank, world):
     elif dom in ("beam_tangent", "beam_mount"):
         t = kernels[dom]["ms"] / 1e3
         achieved = mnt_f.value / t / 1e12
+        mounts_per_launch = mnt_f.value / 9000.0 / max(kernels[dom]["launches"], 1)
         roof.update({"bound": "fp64", "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
-                     "frac": achieved / fp64.value, "traffic": None,
+                     "frac": achieved / fp64.value,
+                     "traffic": TANGENT_DRAM_BYTES_PER_ELEMENT * mounts_per_launch,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_beam_tangent "
+                                       "launch on 128 chains (profiles/k_beam_tangent_128chains.md): "
+                                       f"{TANGENT_DRAM_BYTES_PER_ELEMENT:.0f} B per element, scaled by the "
+                                       f"{mounts_per_launch:.0f} element mounts of an average launch here",
                      "note": "FP64 CUDA-core bound; achieved counts 9000 FP64 flops per Beam_1 Mount "
                              "(both Gauss points); peak = FP64 FMA throughput measured live (of measured); "
                              f"HBM view: assembly bytes {asm_b.value:.3e} -> {asm_b.value / t / 1e9:.1f} GB/s of "
