@@ -47,6 +47,12 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=512, help="chains in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=32,
+                    help="chains solved one at a time for the plain single-structure leg")
+    ap.add_argument("--serve-requests", type=int, default=400,
+                    help="requests in the served-stream leg (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate of the served stream (1/s)")
+    ap.add_argument("--serve-budget-gb", type=int, default=16, help="device-memory budget of the server")
     return ap.parse_args()
 
 
@@ -200,6 +206,54 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def plain_leg(ctx, structs, sample_n):
+    """The plain FP64 path one structure at a time (a batch of one per
+    gf_batch_run, as a caller replacing Static::Solve per structure would run
+    it) over a size-stratified sample of the same chains; device time of each
+    run after one warm-up run of the same structure."""
+    from giraffe_gb300 import gpu
+
+    order = np.argsort([len(s.beams) for s in structs])
+    idx = order[np.linspace(0, len(order) - 1, min(sample_n, len(order))).astype(int)]
+    ms, solves = 0.0, 0
+    for i in idx:
+        b = gpu.BatchSolver(ctx, [structs[i]])
+        b.reset()
+        b.run()
+        b.reset()
+        ms += b.run()
+        solves += int(b.results()[1][0, 0])
+        b.close()
+    return {"value": solves / (ms / 1e3), "unit": UNIT,
+            "sample": f"{len(idx)} of the {len(structs)} chains (every size stratum), one structure per solve, "
+                      f"{solves} Newton solves in {ms:.1f} ms of device time"}
+
+
+def served_leg(ctx, args, rank):
+    """Continuous batching of a Poisson stream of static pipe-chain requests
+    (1k-50k DOF log-uniform) through gf_server_*: admitted by the device
+    budget as they arrive; latency = result returned - scheduled arrival."""
+    from giraffe_gb300 import configs, serve
+
+    reqs = configs.served_chains(args.serve_requests, seed=args.seed + 1000 + rank)
+    arrivals = serve.poisson_arrivals(len(reqs), args.serve_rate, seed=args.seed + 1000 + rank)
+    srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30)
+    warm = configs.served_chains(8, seed=args.seed + 2000 + rank)  # first-use costs out of the stream
+    serve.run_stream(srv, warm, np.zeros(len(warm)))
+    st0 = srv.status()
+    out = serve.run_stream(srv, reqs, arrivals)
+    st1 = srv.status()
+    srv.close()
+    res = out["results"]
+    return {"workload": f"{len(reqs)} static Beam_1 pipe chains, 1k-50k free DOF log-uniform, 10 load steps, "
+                        f"Poisson arrivals at {args.serve_rate:g}/s (seeded); Shell_1 plates not included",
+            "requests": len(reqs), "p50_latency_ms": out["p50_ms"], "p99_latency_ms": out["p99_ms"],
+            "solves_per_s": out["solves_per_s"], "requests_per_s": out["requests_per_s"], "wall_s": out["wall_s"],
+            "aborted": int(sum(r.stats[3] for r in res)), "budget_gb": args.serve_budget_gb,
+            "gpu_launches": st1["launches"] - st0["launches"],
+            "mean_queued_ms": float(np.mean([r.queued_ms for r in res]))}
+
+
 def run_ours(args, rank, world):
     import ctypes as C
 
@@ -286,6 +340,11 @@ def run_ours(args, rank, world):
         t = kernels[dom]["ms"] / 1e3
         roof.update({"bound": "hbm", "achieved": asm_b.value / t / 1e9, "peak": peaks.get("hbm_gbs"),
                      "unit": "GB/s", "frac": asm_b.value / t / 1e9 / peaks.get("hbm_gbs"), "traffic": None})
+    plain = plain_leg(ctx, structs, args.plain_sample)
+    plain["batched_over_plain"] = value / plain["value"]
+    serving = None
+    if args.serve_requests > 0:
+        serving = served_leg(ctx, args, rank)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(structs, args.cpu_sample, rank)
@@ -307,6 +366,8 @@ def run_ours(args, rank, world):
                 "kernels_ms_per_solve": {k: round(v["ms"], 3) for k, v in kernels.items()},
                 "peaks_measured": {"fp64_tflops": fp64.value, "fp32_tflops": fp32.value},
                 "clocks": clk.summary(),
+                "plain_single_structure": plain,
+                "serving": serving,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     ctx.close()

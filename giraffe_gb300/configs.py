@@ -139,6 +139,22 @@ def batched_static(n_chains: int = 512, seed: int = 0, n_min: int = 50, n_max: i
             for i, (n, d, w) in enumerate(zip(n_el, De, wall))]
 
 
+def served_chains(n_requests: int, seed: int = 0, dof_min: int = 1000, dof_max: int = 50000,
+                  steps: int = 10, tol: float = 1e-8, chain_length: float = 10.0) -> list:
+    """Static pipe-chain requests of the mixed served stream: free-DOF counts
+    log-uniform in [dof_min, dof_max] (n_e = (DOF/6 - 1)/2 elements), section
+    and tip force drawn as in batched_static."""
+    rng = np.random.default_rng(seed)
+    dof = np.exp(rng.uniform(math.log(dof_min), math.log(dof_max), n_requests))
+    n_el = np.maximum(1, np.rint((dof / 6.0 - 1.0) / 2.0)).astype(int)
+    De = rng.uniform(0.3, 0.5, n_requests)
+    wall = rng.uniform(0.02, 0.04, n_requests)
+    F = rng.normal(0.0, 1e5, (n_requests, 3))
+    return [pipe_chain(int(n), float(d), float(w), F[i], steps=steps, tol=tol,
+                       element_length=chain_length / int(n))
+            for i, (n, d, w) in enumerate(zip(n_el, De, wall))]
+
+
 def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, steps: int = 1000,
                 dt: float = 0.01, element_length: float = 0.5, tol: float = 1e-8) -> Structure:
     L = n_el * element_length

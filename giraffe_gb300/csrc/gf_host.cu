@@ -9,27 +9,25 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
 #include "../../include/giraffe_gpu.h"
+#include "gf_host_internal.h"
 #include "gf_kernels.cuh"
 #include "gf_types.h"
 
 using namespace gf;
+using namespace gfh;
 
 // FP64 flops of one Beam_1 Mount on the device (both Gauss points: kinematics,
 // stresses, internal force, B^T D B + G, block rotation and the 18x18
 // expansion), counted from the operation sequence of gf_beam.cuh.
 #define GF_BEAM_MOUNT_FLOPS 9000.0
 
-struct gf_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-};
 
-namespace {
+namespace gfh {
 
 bool set_err(gf_ctx* ctx, const char* fmt, ...) {
   char buf[512];
@@ -114,34 +112,25 @@ template <typename T> bool dmalloc(gf_ctx* ctx, T** p, size_t n) {
   return true;
 }
 
-}  // namespace
+}  // namespace gfh
 
-struct gf_batch {
-  gf_ctx* ctx = nullptr;
-  gf_solve_opts opts{};
-  Batch b{};
-  // host copies needed for results and resets
-  std::vector<StructInfo> info;
-  std::vector<int> kb;  // true half-bandwidth per structure
-  std::vector<void*> allocs;
-  // initial configuration (device) for gf_batch_reset
-  double* copy0 = nullptr;
-  double* Qn0 = nullptr;
-  BeamHist* bhist0 = nullptr;
-  BeamHistAux* baux0 = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double last_ms = 0.0;
-  long long last_launches = 0;
-  int launches_per_pass = 0;
-  int* h_running = nullptr;  // pinned
-  long long h2d_bytes = 0;
-};
-
-namespace {
+namespace gfh {
 
 template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
-  if (!dmalloc(B->ctx, p, n)) return false;
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  if (B->count_only) {
+    B->counted_bytes += (bytes + 255) / 256 * 256;
+    *p = nullptr;
+    return true;
+  }
+  if (B->arena) {
+    void* q = B->arena->alloc(bytes);
+    if (!q) return set_err(B->ctx, "device budget exhausted (%zu bytes requested, %zu free in the largest block)",
+                           bytes, B->arena->largest_free());
+    *p = static_cast<T*>(q);
+  } else if (!dmalloc(B->ctx, p, n)) {
+    return false;
+  }
   B->allocs.push_back(*p);
   return true;
 }
@@ -149,8 +138,9 @@ template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
 template <typename T> bool upload(gf_batch* B, T** p, const std::vector<T>& v) {
   if (!balloc(B, p, v.size())) return false;
   B->h2d_bytes += (long long)(v.size() * sizeof(T));
-  if (!v.empty()) {
-    cudaError_t e = cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (!v.empty() && !B->count_only) {
+    // pageable source: staged before return, ordered on the batch's stream
+    cudaError_t e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, B->stream);
     if (e != cudaSuccess) return set_err(B->ctx, "upload failed: %s", cudaGetErrorString(e));
   }
   return true;
@@ -478,17 +468,34 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
       !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18))
     return GF_ERR_CUDA;
-  CK(cudaMemset(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB));
-  CK(cudaMemset(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1)));
+  if (B->count_only) return GF_OK;
+  CK(cudaMemsetAsync(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB, B->stream));
+  CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
   b.max_refine = B->opts.max_refine;
   return GF_OK;
 }
 
+int count_launches_per_pass(const gf_batch* B) {
+  int colors = 0;
+  for (int c = 0; c < B->b.n_colors; ++c) colors += B->b.color_off[c + 1] > B->b.color_off[c];
+  const ChainData& cd = B->b.chain;
+  int chain_launches = 0;
+  if (cd.n_chain_elems) {
+    chain_launches = 2;
+    if (cd.n_corners) {
+      chain_launches += 3;
+      for (int l = 0; l < cd.n_levels; ++l)
+        chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
+    }
+  }
+  return 10 + colors + chain_launches;
+}
+
 int batch_reset(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
   Batch& b = B->b;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   CK(cudaMemcpyAsync(b.copy, B->copy0, sizeof(double) * (size_t)b.n_nodes * 6, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.Qn, B->Qn0, sizeof(double) * (size_t)b.n_nodes * 9, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.bhist, B->bhist0, sizeof(BeamHist) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
@@ -542,6 +549,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
   cudaSetDevice(ctx->device);
   gf_batch* B = new gf_batch();
   B->ctx = ctx;
+  B->stream = ctx->stream;
   if (opts) B->opts = *opts; else gf_default_opts(&B->opts);
   if (B->opts.poll_every <= 0) B->opts.poll_every = 8;
   if (build_batch(B, n, models) != GF_OK || cudaMallocHost(&B->h_running, sizeof(int)) != cudaSuccess ||
@@ -551,26 +559,17 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
     ctx->err = e.empty() ? "gf_batch_create failed" : e;
     return nullptr;
   }
-  int colors = 0;
-  for (int c = 0; c < B->b.n_colors; ++c) colors += B->b.color_off[c + 1] > B->b.color_off[c];
-  const ChainData& cd = B->b.chain;
-  int chain_launches = 0;
-  if (cd.n_chain_elems) {
-    chain_launches = 2;
-    if (cd.n_corners) {
-      chain_launches += 3;
-      for (int l = 0; l < cd.n_levels; ++l)
-        chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
-    }
-  }
-  B->launches_per_pass = 10 + colors + chain_launches;
+  B->launches_per_pass = count_launches_per_pass(B);
   return B;
 }
 
 void gf_batch_destroy(gf_batch* B) {
   if (!B) return;
   if (B->graph) cudaGraphExecDestroy(B->graph);
-  for (void* p : B->allocs) cudaFree(p);
+  for (void* p : B->allocs) {
+    if (B->arena) B->arena->release(p);
+    else cudaFree(p);
+  }
   if (B->h_running) cudaFreeHost(B->h_running);
   if (B->ev0) cudaEventDestroy(B->ev0);
   if (B->ev1) cudaEventDestroy(B->ev1);
@@ -582,14 +581,16 @@ int gf_batch_reset(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
   int r = batch_reset(B);
   if (r != GF_OK) return r;
-  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamSynchronize(B->stream));
   return GF_OK;
 }
 
-namespace {
+}  // extern "C"
+
+namespace gfh {
 int ensure_graph(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   if (B->opts.use_graph && !B->graph) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -605,7 +606,7 @@ int ensure_graph(gf_batch* B) {
 // every opts.poll_every passes.
 int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
   gf_ctx* ctx = B->ctx;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   const Batch& b = B->b;
   long long passes = 0;
   const long long cap = 4000000;
@@ -630,12 +631,14 @@ int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
   *passes_out = passes;
   return GF_OK;
 }
-}  // namespace
+}  // namespace gfh
+
+extern "C" {
 
 int gf_batch_run(gf_batch* B) {
   if (!B) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   int r = ensure_graph(B);
   if (r != GF_OK) return r;
   CK(cudaEventRecord(B->ev0, st));
@@ -654,7 +657,7 @@ int gf_batch_run(gf_batch* B) {
 int gf_batch_solve_timed(gf_batch* B, int steps, double* ms_out) {
   if (!B || steps <= 0) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   int r = ensure_graph(B);
   if (r != GF_OK) return r;
   long long launches = 0;
@@ -680,7 +683,7 @@ int gf_batch_solve_timed(gf_batch* B, int steps, double* ms_out) {
 int gf_batch_profile(gf_batch* B, double* ms_out, long long* launches_out) {
   if (!B) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = B->stream;
   int r = batch_reset(B);
   if (r != GF_OK) return r;
   const int cap = 1 << 16;
@@ -820,12 +823,12 @@ int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
   if (r != GF_OK) return r;
   // one partial pass: step start, zero, mount, loads, residual
   Batch bb = b;
-  launch_iteration_partial(bb, ctx->stream);
+  launch_iteration_partial(bb, B->stream);
   CK(cudaGetLastError());
   std::vector<double> band((size_t)inf.n_free * GF_LDB), P(inf.n_free);
-  CK(cudaMemcpyAsync(band.data(), b.band + inf.band_off, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(P.data(), b.P + inf.dof_off, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpyAsync(band.data(), b.band + inf.band_off, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, B->stream));
+  CK(cudaMemcpyAsync(P.data(), b.P + inf.dof_off, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, B->stream));
+  CK(cudaStreamSynchronize(B->stream));
   int ldab = 3 * kb + 1;
   if (ab) {
     std::memset(ab, 0, sizeof(double) * (size_t)ldab * inf.n_free);
@@ -1101,5 +1104,20 @@ extern "C" int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const d
   CK(cudaMemcpyAsync(&st0, dst, sizeof(st0), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (info) *info = st0.info_fail;
+  return GF_OK;
+}
+
+extern "C" int gf_batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, size_t* bytes) {
+  if (n <= 0 || !models || !bytes) {
+    set_err(ctx, "gf_batch_device_bytes: invalid arguments");
+    return GF_ERR_ARG;
+  }
+  gf_batch B;
+  B.ctx = ctx;
+  B.count_only = true;
+  gf_default_opts(&B.opts);
+  int r = build_batch(&B, n, models);
+  if (r != GF_OK) return r;
+  *bytes = B.counted_bytes;
   return GF_OK;
 }

@@ -1,0 +1,123 @@
+// Internal host types of libgiraffe_gpu.so shared by the batch path
+// (gf_host.cu) and the served path (gf_server.cu).  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/giraffe_gpu.h"
+#include "gf_types.h"
+
+struct gf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+};
+
+// First-fit sub-allocator over one device allocation: the served path's HBM
+// budget.  Blocks are 256-byte aligned; freeing merges neighbours.
+struct DevArena {
+  char* base = nullptr;
+  size_t size = 0;
+  std::map<size_t, size_t> free_blocks;  // offset -> bytes
+  std::map<size_t, size_t> used;         // offset -> bytes
+  size_t in_use = 0;
+  void init(void* p, size_t n) {
+    base = static_cast<char*>(p);
+    size = n;
+    free_blocks.clear();
+    used.clear();
+    in_use = 0;
+    if (n) free_blocks[0] = n;
+  }
+  void* alloc(size_t n) {
+    n = (std::max<size_t>(n, 1) + 255) / 256 * 256;
+    for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+      if (it->second < n) continue;
+      size_t off = it->first, rest = it->second - n;
+      free_blocks.erase(it);
+      if (rest) free_blocks[off + n] = rest;
+      used[off] = n;
+      in_use += n;
+      return base + off;
+    }
+    return nullptr;
+  }
+  void release(void* p) {
+    auto it = used.find(static_cast<size_t>(static_cast<char*>(p) - base));
+    if (it == used.end()) return;
+    size_t off = it->first, n = it->second;
+    used.erase(it);
+    in_use -= n;
+    auto nx = free_blocks.lower_bound(off);
+    if (nx != free_blocks.end() && nx->first == off + n) {
+      n += nx->second;
+      free_blocks.erase(nx);
+    }
+    auto pv = free_blocks.lower_bound(off);
+    if (pv != free_blocks.begin()) {
+      --pv;
+      if (pv->first + pv->second == off) {
+        pv->second += n;
+        return;
+      }
+    }
+    free_blocks[off] = n;
+  }
+  size_t largest_free() const {
+    size_t m = 0;
+    for (const auto& f : free_blocks) m = std::max(m, f.second);
+    return m;
+  }
+};
+
+struct gf_batch {
+  gf_ctx* ctx = nullptr;
+  gf_solve_opts opts{};
+  gf::Batch b{};
+  cudaStream_t stream = nullptr;  // the context's stream, or a served wave's own
+  DevArena* arena = nullptr;      // served waves: allocations come from the server's budget
+  bool count_only = false;        // size the batch without touching the device
+  size_t counted_bytes = 0;
+  // host copies needed for results and resets
+  std::vector<gf::StructInfo> info;
+  std::vector<int> kb;  // true half-bandwidth per structure
+  std::vector<void*> allocs;
+  // initial configuration (device) for gf_batch_reset
+  double* copy0 = nullptr;
+  double* Qn0 = nullptr;
+  gf::BeamHist* bhist0 = nullptr;
+  gf::BeamHistAux* baux0 = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long last_launches = 0;
+  int launches_per_pass = 0;
+  int* h_running = nullptr;  // pinned
+  long long h2d_bytes = 0;
+};
+
+namespace gfh {
+bool set_err(gf_ctx* ctx, const char* fmt, ...);
+// Builds the device batch of n structures (or, with B->count_only, only
+// counts its device bytes).
+int build_batch(gf_batch* B, int n, const gf_model_desc* models);
+// Initial configuration and step state, enqueued on B->stream.
+int batch_reset(gf_batch* B);
+// Captures one Newton pass as a CUDA graph on B->stream (opts.use_graph).
+int ensure_graph(gf_batch* B);
+// Kernel launches of one Newton pass.
+int count_launches_per_pass(const gf_batch* B);
+}  // namespace gfh
+
+#define GF_CK(call)                                                                          \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      gfh::set_err(ctx, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return GF_ERR_CUDA;                                                                    \
+    }                                                                                        \
+  } while (0)

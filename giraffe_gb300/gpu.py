@@ -21,7 +21,9 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
            "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
            "gf_kernel_name", "gf_batch_bytes", "gf_batch_work", "gf_device_fp_peaks",
-           "gf_beam_inertia_elements", "gf_band_solve_noalloc"]
+           "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_batch_device_bytes",
+           "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
+           "gf_server_poll", "gf_server_get_status"]
 
 
 class gf_solve_opts(C.Structure):
@@ -33,6 +35,22 @@ class gf_stats(C.Structure):
     _fields_ = [("converged_steps", C.c_int), ("newton_iterations", C.c_int), ("bisections", C.c_int),
                 ("aborted", C.c_int), ("linear_solves", C.c_int), ("fp64_fallback", C.c_int),
                 ("pad", C.c_int * 2)]
+
+
+class gf_server_opts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_waves", C.c_int), ("max_wave_structs", C.c_int),
+                ("passes_per_chunk", C.c_int), ("pad", C.c_int)]
+
+
+class gf_server_result(C.Structure):
+    _fields_ = [("tag", C.c_longlong), ("status", C.c_int), ("pad", C.c_int), ("stats", gf_stats),
+                ("queued_ms", C.c_double), ("total_ms", C.c_double)]
+
+
+class gf_server_status(C.Structure):
+    _fields_ = [("queued", C.c_int), ("waves", C.c_int), ("structures", C.c_int), ("pad", C.c_int),
+                ("budget_in_use", C.c_size_t), ("passes", C.c_longlong), ("launches", C.c_longlong),
+                ("reported", C.c_longlong)]
 
 
 _lib = None
@@ -69,8 +87,29 @@ def lib():
         L.gf_band_solve_noalloc.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
         L.gf_beam_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
                                                C.c_double, C.c_double, dp, dp]
+        L.gf_batch_device_bytes.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(C.c_size_t)]
+        L.gf_server_default_opts.argtypes = [C.POINTER(gf_server_opts)]
+        L.gf_server_create.restype = vp
+        L.gf_server_create.argtypes = [vp, C.POINTER(gf_server_opts)]
+        L.gf_server_destroy.argtypes = [vp]
+        L.gf_server_submit.argtypes = [vp, C.POINTER(gf_model_desc), dp, C.c_longlong]
+        L.gf_server_poll.argtypes = [vp, C.POINTER(gf_server_result), C.c_int, ip]
+        L.gf_server_get_status.argtypes = [vp, C.POINTER(gf_server_status)]
         _lib = L
     return _lib
+
+
+def device_bytes(structures) -> int:
+    """Device bytes one batch of these structures holds (gf_batch_device_bytes;
+    needs no GPU)."""
+    L = lib()
+    handles = [s.desc() for s in structures]
+    descs = (gf_model_desc * len(handles))(*[h.desc for h in handles])
+    n = C.c_size_t(0)
+    rc = L.gf_batch_device_bytes(None, len(handles), descs, C.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"gf_batch_device_bytes failed ({rc})")
+    return n.value
 
 
 def _dp(a):

@@ -152,6 +152,68 @@ int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double
  * info_fail. */
 int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
 
+/* Device bytes a batch of these n structures holds (gf_batch_create's
+ * allocations, each rounded to 256 bytes); checks the descriptions as
+ * gf_batch_create does.  Needs no device; ctx may be NULL. */
+int gf_batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, size_t* bytes);
+
+/* ---- Served path: continuous batching under a device-memory budget ----
+ * No counterpart in the reference, which solves one input deck per process.
+ * A server owns one device allocation of hbm_budget bytes.  Submitted
+ * structures queue until there is room; each admission takes every queued
+ * structure that fits (first come, first served, up to max_wave_structs) into
+ * a new device batch, a "wave", on its own stream, so waves admitted while
+ * others run overlap on the device.  Every structure keeps its state on the
+ * device for all its load steps; its result is reported as soon as it
+ * finishes, and its wave's memory returns to the budget when the wave's last
+ * structure finishes.  Results equal those of gf_solve on the structure
+ * alone.  All progress happens inside gf_server_poll; calls on one server
+ * must not overlap. */
+typedef struct gf_server gf_server;
+
+typedef struct gf_server_opts {
+  size_t hbm_budget;     /* bytes of device memory for structures */
+  int max_waves;         /* batches in flight at once (each its own stream) */
+  int max_wave_structs;  /* structures per batch */
+  int passes_per_chunk;  /* Newton passes enqueued between two state reads */
+  int pad;
+} gf_server_opts;
+
+typedef struct gf_server_result {
+  long long tag;             /* as given to gf_server_submit */
+  int status;                /* GF_OK, or GF_ERR_TIMEOUT / GF_ERR_CUDA */
+  int pad;
+  gf_stats stats;
+  double queued_ms;          /* submit -> admission */
+  double total_ms;           /* submit -> result reported */
+} gf_server_result;
+
+typedef struct gf_server_status {
+  int queued;                /* submitted, not admitted */
+  int waves;                 /* batches on the device */
+  int structures;            /* admitted, not yet reported */
+  int pad;
+  size_t budget_in_use;      /* bytes of the budget held by waves */
+  long long passes;          /* Newton passes launched so far */
+  long long launches;        /* kernels launched so far */
+  long long reported;        /* results reported so far */
+} gf_server_status;
+
+void gf_server_default_opts(gf_server_opts* opts);
+gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts);
+void gf_server_destroy(gf_server* srv);
+/* Queues one structure.  The arrays model points to and final_nodes
+ * (n_nodes x 15 doubles, as gf_batch_results) must stay valid until its
+ * result is reported.  GF_ERR_ARG if the model is invalid or needs more than
+ * the whole budget. */
+int gf_server_submit(gf_server* srv, const gf_model_desc* model, double* final_nodes, long long tag);
+/* Reads finished work, retires finished waves, admits queued structures and
+ * keeps two chunks of passes in flight per wave; returns at once.  Up to
+ * max_results finished structures go to results (*n_results of them); the
+ * rest wait for the next call. */
+int gf_server_poll(gf_server* srv, gf_server_result* results, int max_results, int* n_results);
+int gf_server_get_status(const gf_server* srv, gf_server_status* status);
+
 /* No counterpart in the reference.  The same solve as gf_band_solve, same
  * arguments and results, for callers that must not allocate device memory
  * per call: a host loop that runs under another allocator's budget, or one
