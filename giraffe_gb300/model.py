@@ -198,6 +198,10 @@ class Structure:
         self.section_decks.append(f"Tube\t{len(self.sections)}\tDe\t{_r(De)}\tDi\t{_r(Di)}")
         return len(self.sections) - 1
 
+    def add_shell_section(self, thickness):
+        self.shell_sections.append(float(thickness))
+        return len(self.shell_sections) - 1
+
     def add_cs(self, e1, e3):
         self.cs.append(tuple(float(v) for v in (*e1, *e3)))
         return len(self.cs) - 1
@@ -268,7 +272,7 @@ class Structure:
         for i, c in enumerate(self.cs):
             o.append(f"CS\t{i + 1}\tE1\t{_r(c[0])}\t{_r(c[1])}\t{_r(c[2])}\tE3\t{_r(c[3])}\t{_r(c[4])}\t{_r(c[5])}")
         # node sets: one per constrained node group, load and displacement
-        sets, cons_lines, load_lines, disp_lines = [], [], [], []
+        sets, elem_sets, cons_lines, load_lines, disp_lines = [], [], [], [], []
 
         def new_set(nodes):
             sets.append(list(nodes))
@@ -294,7 +298,9 @@ class Structure:
             else:
                 rows = "\n".join(f"{_r(float(t))}\t{_r(float(v[0]))}"
                                  for t, v in zip(L.table.times, L.table.values))
-                load_lines.append(("ShellLoad", L, rows))
+                elem_sets.append([len(self.beams) + e for e in L.shells])
+                load_lines.append(f"ShellLoad\t{len(load_lines) + 1}\tElementSet\t{len(elem_sets)}"
+                                  f"\tAreaUpdate\t{int(L.area_update)}\tNTimes\t{len(L.table.times)}\n{rows}")
         for D in self.displacements:
             ns = new_set(D.nodes)
             rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
@@ -306,9 +312,14 @@ class Structure:
             for i, nodes in enumerate(sets):
                 o.append(f"NodeSet\t{i + 1}\tNodes\t{len(nodes)}\tList\t" +
                          "\t".join(str(n + 1) for n in nodes))
+        if elem_sets:
+            o.append(f"ElementSets\t{len(elem_sets)}")
+            for i, els in enumerate(elem_sets):
+                o.append(f"ElementSet\t{i + 1}\tElements\t{len(els)}\tList\t" +
+                         "\t".join(str(e + 1) for e in els))
         if load_lines:
             o.append(f"Loads\t{len(load_lines)}")
-            o.extend(x for x in load_lines if isinstance(x, str))
+            o.extend(load_lines)
         if disp_lines:
             o.append(f"Displacements\t{len(disp_lines)}")
             o.extend(disp_lines)

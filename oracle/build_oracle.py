@@ -9,7 +9,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["oracle_beam.c", "oracle_solver.c"]
+SOURCES = ["oracle_beam.c", "oracle_shell.c", "oracle_solver.c"]
 LIB = os.path.join(HERE, "liboracle.so")
 
 

@@ -29,7 +29,7 @@ OBJ = os.path.join(OUT, "obj")
 SOURCES = [
     "Matrix", "Beam_1", "Shell_1", "Node", "LagrangeSave", "Hooke", "SecTube", "SecRectangle",
     "ShellSectionHomogeneous", "CoordinateSystem", "Table", "Static", "Dynamic", "Solution",
-    "ConvergenceCriteria", "NodalLoad", "NodalConstraint", "NodeSet", "BoolTable", "Load",
+    "ConvergenceCriteria", "NodalLoad", "NodalConstraint", "NodeSet", "ElementSet", "BoolTable", "Load",
     "Element", "NodalDisplacement", "ShellLoad", "SolverOptions", "SolidSection",
 ]
 

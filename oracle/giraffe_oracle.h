@@ -50,6 +50,16 @@ int oracle_solve_batch(int n, const gf_model_desc* models, double** final_nodes,
 int oracle_beam_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
                         int n_hist, const double* hist_disp, const double* disp18, double* K, double* f);
 
+/* One Shell_1 element: PreCalc from nodal coordinates (6x3), material
+ * (E, nu, rho) and thickness; n_hist committed increments (each 27 values in
+ * element DOF order: translations of nodes 1..6, rotations of nodes 4..6)
+ * build the Gauss-point history; then Mount at disp27, and with
+ * with_pressure the follower pressure at the current configuration.
+ * K: 27x27 column-major, f: 27 (P_loading). */
+int oracle_shell_element(const double* xyz18, const double* mat3, double thickness, int n_hist,
+                         const double* hist_disp, const double* disp27, int with_pressure, double pressure,
+                         int area_update, double* K, double* f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,7 @@
 #include "SecRectangle.h"
 #include "SecTube.h"
 #include "Shell_1.h"
+#include "ElementSet.h"
 #include "ShellLoad.h"
 #include "ShellSectionHomogeneous.h"
 #include "SolverOptions.h"
@@ -185,6 +186,16 @@ int giraffe_ref_load(const char* path) {
         ok = db.node_sets[i]->Read(f);
       }
       db.node_sets_exist = true;
+    } else if (!strcmp(s, "ElementSets")) {
+      if (fscanf(f, "%999s", s) != 1) { ok = false; break; }
+      db.number_element_sets = atoi(s);
+      db.element_sets = new ElementSet*[db.number_element_sets];
+      for (int i = 0; i < db.number_element_sets && ok; ++i) {
+        db.element_sets[i] = new ElementSet();
+        TryComment(f);
+        ok = db.element_sets[i]->Read(f);
+      }
+      db.element_sets_exist = true;
     } else if (!strcmp(s, "Loads")) {
       ok = read_block<Load>(f, db.number_loads, db.loads, [](const char* t) -> Load* {
         if (!strcmp(t, "NodalLoad")) return new NodalLoad();
@@ -329,4 +340,21 @@ void giraffe_ref_commit() {
   for (int i = 0; i < db.number_nodes; ++i)
     for (int k = 0; k < 6; ++k) db.nodes[i]->displacements[k] = 0.0;
 }
+}
+
+// Shell_1 Mount + MountElementLoads + MountShellSpecialLoads of load number
+// l (1-based) with the load evaluated at time t (reference
+// src/Shell_1.cpp:1392-1467).  K: 27x27 column-major, P: P_loading.
+extern "C" int giraffe_ref_shell_pressure(int e, int l, double t, double* K, double* P) {
+  Element* el = db.elements[e - 1];
+  if (typeid(*el) != typeid(Shell_1)) return 0;
+  db.last_converged_time = t;
+  db.current_time_step = 0.0;
+  Shell_1* s = static_cast<Shell_1*>(el);
+  s->Mount();
+  s->MountElementLoads();
+  s->MountShellSpecialLoads(l);
+  memcpy(K, s->stiffness->getMatrix(), sizeof(double) * 27 * 27);
+  memcpy(P, s->P_loading->getMatrix(), sizeof(double) * 27);
+  return 27;
 }
