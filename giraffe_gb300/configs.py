@@ -31,7 +31,8 @@ import math
 
 import numpy as np
 
-from .model import GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, Solution, Structure, Table
+from .model import (GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PressureLoad, Solution, Structure,
+                    Table)
 
 E_STEEL = 210e9
 NU_STEEL = 0.3
@@ -185,3 +186,45 @@ def batched_dynamic(n_chains: int = 256, seed: int = 0, n_min: int = 100, n_max:
     per = rng.uniform(5.0, 15.0, n_chains)
     return [riser_chain(int(n), float(d), float(w), float(a), float(p), steps=steps, tol=tol)
             for n, d, w, a, p in zip(n_el, De, wall, amp, per)]
+
+
+def square_plate(n: int = 64, side: float = 1.0, thickness: float = 0.01, E: float = 70e9, nu: float = 0.33,
+                 pressure: float = 1e5, steps: int = 20, area_update: int = 1, tol: float = 1e-8) -> Structure:
+    """Square plate in the x-y plane meshed into n x n squares, each split
+    into two six-node Shell_1 triangles ((2n+1)^2 grid nodes: corners at even
+    grid indices, midside nodes elsewhere), all four edges clamped, uniform
+    follower pressure ramped linearly to `pressure` over `steps` load steps."""
+    m = 2 * n + 1
+    h = side / (2 * n)
+    gx, gy = np.meshgrid(np.arange(m) * h, np.arange(m) * h, indexing="xy")
+    s = Structure(nodes=np.stack([gx.ravel(), gy.ravel(), np.zeros(m * m)], axis=1))
+    mat = s.add_material(E, nu, 2700.0)
+    sec = s.add_shell_section(thickness)
+    cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+
+    def node(i, j):
+        return j * m + i
+
+    for j in range(n):
+        for i in range(n):
+            a, b = node(2 * i, 2 * j), node(2 * i + 2, 2 * j)
+            c, d = node(2 * i + 2, 2 * j + 2), node(2 * i, 2 * j + 2)
+            ab, bc, cd, da = node(2 * i + 1, 2 * j), node(2 * i + 2, 2 * j + 1), node(2 * i + 1, 2 * j + 2), \
+                node(2 * i, 2 * j + 1)
+            ac = node(2 * i + 1, 2 * j + 1)
+            s.shells.append((a, b, c, ab, bc, ac, mat, sec, cs))
+            s.shells.append((a, c, d, ac, cd, da, mat, sec, cs))
+    for j in range(m):
+        for i in range(m):
+            if i in (0, m - 1) or j in (0, m - 1):
+                s.clamp(node(i, j))
+    s.loads.append(PressureLoad(list(range(len(s.shells))), Table(np.array([0.0, 1.0]),
+                                                                  np.array([[0.0], [pressure]])),
+                                area_update=area_update))
+    dt = 1.0 / steps
+    s.solution = Solution(GF_STATIC, 0.0, 1.0, dt, dt, dt / 4096, 30, 3, 4, 1.0)
+    # No moment is applied, so the moment criterion falls back to
+    # MomentMinimumReference * tol; 1 N m keeps it above the FP64 round-off
+    # floor of the rotational residual.
+    s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, moment_min=1.0)
+    return s

@@ -220,6 +220,9 @@ class Structure:
         active = np.zeros((self.n_nodes, 6), dtype=bool)
         for b in self.beams:
             active[list(b[:3])] = True
+        for sh in self.shells:
+            active[list(sh[:3]), :3] = True
+            active[list(sh[3:6])] = True
         cons = self.constraints if self.constraints is not None else 0
         return int((active & (cons == 0)).sum())
 

@@ -24,6 +24,8 @@ def lib():
         _lib.oracle_solve_batch.argtypes = [C.c_int, C.c_void_p, C.POINTER(dp), ip, C.c_int]
         _lib.oracle_beam_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         _lib.oracle_first_tangent.argtypes = [C.c_void_p, dp, dp, ip]
+        _lib.oracle_shell_element.argtypes = [dp, dp, C.c_double, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int,
+                                              dp, dp]
         _lib.oracle_beam_inertia_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double,
                                                      C.c_double, dp, dp, dp]
     return _lib
@@ -82,6 +84,20 @@ def beam_element(xyz9, mat3, sec6, cs6, hist_disp, disp18):
     lib().oracle_beam_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), _dp(args[3]), nh, _dp(hd),
                               _dp(args[4]), _dp(K), _dp(f))
     return K.reshape(18, 18).T, f  # row-major [r][s]
+
+
+def shell_element(xyz18, mat3, thickness, hist_disp, disp27, pressure=None, area_update=1):
+    """One Shell_1 element (oracle_shell_element): K row-major [r][s], f."""
+    K = np.zeros(729)
+    f = np.zeros(27)
+    nh = 0 if hist_disp is None else len(hist_disp)
+    hd = np.ascontiguousarray(hist_disp if nh else np.zeros((1, 27)), dtype=np.float64)
+    x = np.ascontiguousarray(xyz18, dtype=np.float64)
+    m = np.ascontiguousarray(mat3, dtype=np.float64)
+    d = np.ascontiguousarray(disp27, dtype=np.float64)
+    lib().oracle_shell_element(_dp(x), _dp(m), float(thickness), nh, _dp(hd), _dp(d), int(pressure is not None),
+                               float(pressure or 0.0), int(area_update), _dp(K), _dp(f))
+    return K.reshape(27, 27).T, f
 
 
 def first_tangent(structure):

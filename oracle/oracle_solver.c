@@ -32,6 +32,7 @@
 
 #include "band_lu.h"
 #include "oracle_beam.h"
+#include "oracle_shell.h"
 
 static void newmark_coeff(double dt, double beta, double gamma, double* a);
 
@@ -48,6 +49,9 @@ typedef struct {
   double* vel; double* accel; double* copy_vel; double* copy_accel;
   ob_const* bc;
   ob_hist* bh;
+  int ns;
+  os_const* sc;
+  os_hist* sh;
   double* ab; int* ipiv; double* PA;
   /* criteria state */
   double force_crit, moment_crit, disp_crit, rot_crit;
@@ -63,7 +67,22 @@ typedef struct {
 static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
-  free(s->bc); free(s->bh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
+  free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
+}
+
+/* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
+ * nodes 1..6, then rotations of nodes 4..6 (reference
+ * src/Shell_1.cpp:1513-1560) */
+static void shell_dofs(const ost* s, int e, int* g) {
+  const int* q = s->m->shells + 9 * e;
+  for (int a = 0; a < 18; ++a) g[a] = s->GL[6 * q[a / 3] + a % 3];
+  for (int a = 0; a < 9; ++a) g[18 + a] = s->GL[6 * q[3 + a / 3] + 3 + a % 3];
+}
+
+static void shell_increments(const ost* s, int e, double* d) {
+  const int* q = s->m->shells + 9 * e;
+  for (int a = 0; a < 18; ++a) d[a] = s->disp[6 * q[a / 3] + a % 3];
+  for (int a = 0; a < 9; ++a) d[18 + a] = s->disp[6 * q[3 + a / 3] + 3 + a % 3];
 }
 
 static int ost_init(ost* s, const gf_model_desc* m) {
@@ -84,6 +103,9 @@ static int ost_init(ost* s, const gf_model_desc* m) {
   s->copy_accel = calloc((size_t)nn * 6, sizeof(double));
   s->bc = calloc((size_t)(s->nb ? s->nb : 1), sizeof(ob_const));
   s->bh = calloc((size_t)(s->nb ? s->nb : 1), sizeof(ob_hist));
+  s->ns = m->n_shells;
+  s->sc = calloc((size_t)(s->ns ? s->ns : 1), sizeof(os_const));
+  s->sh = calloc((size_t)(s->ns ? s->ns : 1), sizeof(os_hist));
   s->mult = calloc((size_t)(m->n_loads ? m->n_loads : 1), sizeof(*s->mult));
   /* Node::Read sets copy_coordinates to the reference position
    * (reference src/Node.cpp:160-175); rotations start at zero */
@@ -97,10 +119,22 @@ static int ost_init(ost* s, const gf_model_desc* m) {
     oracle_beam_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->materials + 3 * b[3],
                         m->sections + 6 * b[4], m->cs + 6 * b[5], s->bc + e, s->bh + e);
   }
-  /* DOFsActive: Beam_1 activates all six DOFs of its nodes */
+  /* Shell_1::PreCalc */
+  for (int e = 0; e < s->ns; ++e) {
+    const int* q = m->shells + 9 * e;
+    double xyz[18];
+    for (int j = 0; j < 6; ++j) memcpy(xyz + 3 * j, m->node_xyz + 3 * q[j], 3 * sizeof(double));
+    oracle_shell_precalc(xyz, m->materials + 3 * q[6], m->shell_sections[q[7]], s->sc + e, s->sh + e);
+  }
+  /* DOFsActive: Beam_1 activates all six DOFs of its nodes; Shell_1 the
+   * translations of its six nodes and the rotations of its midside nodes
+   * (reference src/Beam_1.cpp:39-57, src/Shell_1.cpp:51-68) */
   for (int e = 0; e < s->nb; ++e)
     for (int j = 0; j < 3; ++j)
       for (int k = 0; k < 6; ++k) s->active[6 * m->beams[6 * e + j] + k] = 1;
+  for (int e = 0; e < s->ns; ++e)
+    for (int j = 0; j < 6; ++j)
+      for (int k = 0; k < (j < 3 ? 3 : 6); ++k) s->active[6 * m->shells[9 * e + j] + k] = 1;
   if (m->constraints)
     for (int i = 0; i < nn * 6; ++i) s->cons[i] = m->constraints[i] ? 1 : 0;
   /* SetGlobalDOFs */
@@ -120,6 +154,13 @@ static int ost_init(ost* s, const gf_model_desc* m) {
         int ga = s->GL[6 * m->beams[6 * e + a / 6] + a % 6], gb = s->GL[6 * m->beams[6 * e + b / 6] + b % 6];
         if (ga > 0 && gb > 0 && ga - gb > kl) kl = ga - gb;
       }
+  for (int e = 0; e < s->ns; ++e) {
+    int g[27];
+    shell_dofs(s, e, g);
+    for (int a = 0; a < 27; ++a)
+      for (int b = 0; b < 27; ++b)
+        if (g[a] > 0 && g[b] > 0 && g[a] - g[b] > kl) kl = g[a] - g[b];
+  }
   for (int l = 0; l < m->n_loads; ++l)
     if (m->loads[l].type == GF_LOAD_NODAL)
       for (int q = 0; q < m->loads[l].n_items; ++q) {
@@ -178,8 +219,36 @@ static void assemble(ost* s) {
       for (int c = 0; c < 18; ++c) add_K(s, g[a], g[c], K[a + 18 * c]);
     }
   }
-  /* NodalLoad::Mount: P_A += -f, -Xi^T m pseudo-moments, K_AA += -V(alpha, Xi^T m) */
   double time = s->last_converged_time + s->current_time_step;
+  /* Shell_1: Mount + MountElementLoads, then the ShellLoads acting on the
+   * element (MountLoads, reference src/ShellLoad.cpp:133-148), then
+   * MountGlobal */
+  double Ks[729], fs[27], ds[27];
+  for (int e = 0; e < s->ns; ++e) {
+    shell_increments(s, e, ds);
+    oracle_shell_mount(s->sc + e, s->sh + e, ds, Ks, fs, NULL);
+    for (int l = 0; l < m->n_loads; ++l) {
+      const gf_load* L = m->loads + l;
+      if (L->type != GF_LOAD_SHELL_PRESSURE) continue;
+      for (int q = 0; q < L->n_items; ++q) {
+        if (L->items[q] != e) continue;
+        double pu[18];
+        const int* nd = m->shells + 9 * e;
+        for (int a = 0; a < 18; ++a) {
+          int node = nd[a / 3], k = a % 3;
+          pu[a] = s->copy[6 * node + k] - m->node_xyz[3 * node + k] + s->disp[6 * node + k];
+        }
+        oracle_shell_pressure(s->sc + e, pu, table_at(&L->table, time, 0), L->area_update, Ks, fs);
+      }
+    }
+    int g[27];
+    shell_dofs(s, e, g);
+    for (int a = 0; a < 27; ++a) {
+      if (g[a] > 0) s->PA[g[a] - 1] += fs[a];
+      for (int c = 0; c < 27; ++c) add_K(s, g[a], g[c], Ks[a + 27 * c]);
+    }
+  }
+  /* NodalLoad::Mount: P_A += -f, -Xi^T m pseudo-moments, K_AA += -V(alpha, Xi^T m) */
   for (int l = 0; l < m->n_loads; ++l) {
     const gf_load* L = m->loads + l;
     if (L->type != GF_LOAD_NODAL) continue;
@@ -366,6 +435,11 @@ static void save_configuration(ost* s) {
     const int* b = s->m->beams + 6 * e;
     for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
     oracle_beam_commit(s->bc + e, s->bh + e, d);
+  }
+  double ds[27];
+  for (int e = 0; e < s->ns; ++e) {
+    shell_increments(s, e, ds);
+    oracle_shell_commit(s->sc + e, s->sh + e, ds);
   }
 }
 
@@ -590,7 +664,7 @@ static void final_state(ost* s, double* out) {
 }
 
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
-  if (m->n_shells) return -1;
+  if (m->n_shells && m->solution.type == GF_DYNAMIC) return -1;
   if (m->solution.type == GF_DYNAMIC && (m->solution.rayleigh_alpha != 0.0 || m->solution.rayleigh_beta != 0.0)) return -1;
   ost s;
   ost_init(&s, m);

@@ -22,12 +22,22 @@ stores what the reference computes:
 * ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
                          single elements (Beam_1::MountMass) with random
                          history, increments, nodal velocities/accelerations.
+* ref_shell_elements.npz Shell_1 tangent K (27x27) and unbalanced force P (27)
+                         of single elements with random geometry, material,
+                         thickness, committed history and increment, half of
+                         them with a follower pressure (Shell_1::PreCalc,
+                         SaveLagrange, Mount, MountElementLoads,
+                         MountShellSpecialLoads; both AreaUpdate modes).
+* ref_plate.npz          a clamped 4x4x2 Shell_1 plate under follower
+                         pressure (AreaUpdate 1), 20 steps, every step.
+* ref_plate_fixed_area.npz  a clamped 3x3x2 plate, AreaUpdate 0, 10 steps.
 
 Node records hold copy_coordinates (position and accumulated Rodrigues
 vector) then the nodal Q (row-major); Gauss-point records hold Q_i
 (row-major).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py <fixture>  # one (elements | ref_*.npz)
 """
 import ctypes as C
 import os
@@ -43,7 +53,7 @@ ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, ROOT)
 
 from giraffe_gb300 import configs  # noqa: E402
-from giraffe_gb300.model import NodalLoad, Solution, Structure, Table  # noqa: E402
+from giraffe_gb300.model import NodalLoad, PressureLoad, Solution, Structure, Table  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "libgiraffe_ref.so")
 
@@ -57,6 +67,7 @@ def ref_lib():
     L.giraffe_ref_solve.argtypes = [C.c_char_p, C.c_char_p]
     L.giraffe_ref_set_increment.argtypes = [C.c_int, dp]
     L.giraffe_ref_element_mount.argtypes = [C.c_int, dp, dp]
+    L.giraffe_ref_shell_pressure.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp]
     return L
 
 
@@ -223,21 +234,103 @@ def run_inertia(L, cases, tmp, rng):
     return res
 
 
+def run_shell_elements(L, rng, n, tmp):
+    out = {k: [] for k in ("xyz", "mat", "thick", "hist", "disp", "pressure", "area_update", "K", "P")}
+    nh_list = []
+    for i in range(n):
+        c = rng.normal(size=(3, 3))
+        if i % 4 == 0:
+            c[:, 2] = 0.0  # in the x-y plane
+        xyz = np.vstack([c, 0.5 * (c[0] + c[1]), 0.5 * (c[1] + c[2]), 0.5 * (c[2] + c[0])])
+        s = Structure(nodes=xyz)
+        matv = (rng.uniform(5e10, 2.1e11), rng.uniform(0.2, 0.4), 7850.0)
+        mat = s.add_material(*matv)
+        t = rng.uniform(0.005, 0.05)
+        sec = s.add_shell_section(t)
+        cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+        s.shells.append((0, 1, 2, 3, 4, 5, mat, sec, cs))
+        press = i % 2 == 1
+        area_update = int(i % 4 == 3)
+        p = rng.uniform(-1e5, 1e5)
+        if press:
+            s.loads.append(PressureLoad([0], Table(np.array([0.0, 10.0]), np.array([[p], [p]])),
+                                        area_update=area_update))
+        deck = os.path.join(tmp, f"sh{i}.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        L.giraffe_ref_prepare()
+        nh = int(rng.integers(0, 4))
+        scale = np.array([0.01] * 3 + [0.1] * 3)
+        hist = np.zeros((3, 27))
+        for q in range(nh + 1):
+            dn = rng.normal(size=(6, 6)) * scale
+            dn[:3, 3:] = 0.0  # corner nodes carry no rotation
+            for nd in range(6):
+                L.giraffe_ref_set_increment(nd + 1, _dp(np.ascontiguousarray(dn[nd])))
+            d27 = np.concatenate([dn[:, :3].ravel(), dn[3:, 3:].ravel()])
+            if q < nh:
+                L.giraffe_ref_commit()
+                hist[q] = d27
+        K = np.zeros(729)
+        P = np.zeros(27)
+        if press:
+            assert L.giraffe_ref_shell_pressure(1, 1, 1.0, _dp(K), _dp(P)) == 27
+        else:
+            assert L.giraffe_ref_element_mount(1, _dp(K), _dp(P)) == 27
+        for k, v in (("xyz", xyz.ravel()), ("mat", np.array(matv)), ("thick", t), ("hist", hist), ("disp", d27),
+                     ("pressure", p if press else np.nan), ("area_update", area_update),
+                     ("K", K.reshape(27, 27).T), ("P", P)):
+            out[k].append(v)
+        nh_list.append(nh)
+    res = {k: np.array(v) for k, v in out.items()}
+    res["n_hist"] = np.array(nh_list)
+    return res
+
+
 def small_chain():
     return configs.pipe_chain(30, 0.4, 0.03, [1.5e5, -1.0e5, 0.8e5], element_length=10.0 / 30)
 
 
-def main():
+DECKS = {
+    "ref_tutorial01.npz": configs.tutorial01,
+    "ref_rollup.npz": configs.cantilever_rollup,
+    "ref_chain.npz": small_chain,
+    "ref_tutorial10.npz": configs.tutorial10,
+    "ref_plate.npz": lambda: configs.square_plate(4, steps=20),
+    "ref_plate_fixed_area.npz": lambda: configs.square_plate(3, steps=10, area_update=0),
+}
+
+
+def make_elements():
     L = ref_lib()
     rng = np.random.default_rng(20261203)
     with tempfile.TemporaryDirectory() as tmp:
         np.savez_compressed(os.path.join(HERE, "ref_beam_elements.npz"), **run_elements(L, element_cases(rng, 24), tmp))
-        np.savez_compressed(os.path.join(HERE, "ref_tutorial01.npz"), **run_deck(L, configs.tutorial01(), "t01", tmp))
-        np.savez_compressed(os.path.join(HERE, "ref_rollup.npz"), **run_deck(L, configs.cantilever_rollup(), "roll", tmp))
-        np.savez_compressed(os.path.join(HERE, "ref_chain.npz"), **run_deck(L, small_chain(), "chain", tmp))
-        np.savez_compressed(os.path.join(HERE, "ref_tutorial10.npz"), **run_deck(L, configs.tutorial10(), "t10", tmp))
         np.savez_compressed(os.path.join(HERE, "ref_beam_inertia.npz"),
                             **run_inertia(L, element_cases(rng, 16), tmp, rng))
+        np.savez_compressed(os.path.join(HERE, "ref_shell_elements.npz"), **run_shell_elements(L, rng, 24, tmp))
+
+
+def make_deck(name):
+    L = ref_lib()
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, name), **run_deck(L, DECKS[name](), name.split(".")[0], tmp))
+
+
+def main():
+    """Each deck runs in a process of its own: the reference keeps its
+    database in one global object, which a second deck does not fully
+    reset."""
+    if len(sys.argv) > 1:
+        if sys.argv[1] == "elements":
+            make_elements()
+        else:
+            make_deck(sys.argv[1])
+        return
+    ref_lib()
+    for job in ["elements"] + list(DECKS):
+        subprocess.run([sys.executable, os.path.abspath(__file__), job], check=True)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
