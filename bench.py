@@ -284,10 +284,10 @@ def run_ours(args, rank, world):
     # per-kernel device times (one profiled solve, events around every launch)
     L.gf_batch_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.gf_kernel_name.restype = C.c_char_p
-    kms = (C.c_double * 12)()
-    kl = (C.c_longlong * 12)()
+    kms = (C.c_double * 14)()
+    kl = (C.c_longlong * 14)()
     ctx.check(L.gf_batch_profile(b.h, kms, kl), "gf_batch_profile")
-    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(12) if kl[i]}
+    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(14) if kl[i]}
     L.gf_batch_work.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
     lu_f, asm_b, mnt_f = C.c_double(), C.c_double(), C.c_double()
     ctx.check(L.gf_batch_work(b.h, C.byref(lu_f), C.byref(asm_b), C.byref(mnt_f)), "gf_batch_work")

@@ -112,6 +112,150 @@ template <typename T> bool dmalloc(gf_ctx* ctx, T** p, size_t n) {
   return true;
 }
 
+
+// ---- host restatement of Shell_1::PreCalc (reference
+// src/Shell_1.cpp:1666-2365, homogeneous section, Hooke material) ----
+static double tri_area2(const double* a, const double* b, const double* c) {
+  double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, v[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+  double w[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+  return 0.5 * std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+}
+
+static void shell_shapes(const double* L, const double* L1, const double* L2, double* N, double* N1, double* N2) {
+  N[0] = (2 * L[0] - 1) * L[0];
+  N[1] = (2 * L[1] - 1) * L[1];
+  N[2] = (2 * L[2] - 1) * L[2];
+  N[3] = 4 * L[0] * L[1];
+  N[4] = 4 * L[1] * L[2];
+  N[5] = 4 * L[2] * L[0];
+  const double* D[2] = {L1, L2};
+  double* O[2] = {N1, N2};
+  for (int q = 0; q < 2; ++q) {
+    const double* Ld = D[q];
+    O[q][0] = 4 * Ld[0] * L[0] - Ld[0];
+    O[q][1] = 4 * Ld[1] * L[1] - Ld[1];
+    O[q][2] = 4 * Ld[2] * L[2] - Ld[2];
+    O[q][3] = 4 * Ld[0] * L[1] + 4 * L[0] * Ld[1];
+    O[q][4] = 4 * Ld[1] * L[2] + 4 * L[1] * Ld[2];
+    O[q][5] = 4 * Ld[2] * L[0] + 4 * L[2] * Ld[0];
+  }
+}
+
+void shell_precalc(const double* xyz, const double* mat, double thick, ShellConst& c, ShellHist& h, ShellHistAux& x) {
+  std::memset(&c, 0, sizeof(c));
+  std::memset(&h, 0, sizeof(h));
+  std::memset(&x, 0, sizeof(x));
+  const double *x1 = xyz, *x2 = xyz + 3, *x3 = xyz + 6;
+  double a[3], b[3];
+  for (int k = 0; k < 3; ++k) { a[k] = x2[k] - x1[k]; b[k] = x3[k] - x1[k]; }
+  double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  double A = 0.5 * nn;
+  double e3[3], e1[3], e2[3];
+  for (int k = 0; k < 3; ++k) e3[k] = (1.0 / nn) * n[k];
+  double eg[3] = {1.0, 0.0, 0.0};
+  if (std::fabs(e3[0]) >= 1.0 - 1e-4) { eg[0] = 0.0; eg[1] = 1.0; }
+  double dd = eg[0] * e3[0] + eg[1] * e3[1] + eg[2] * e3[2];
+  for (int k = 0; k < 3; ++k) e1[k] = eg[k] - dd * e3[k];
+  double n1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+  for (int k = 0; k < 3; ++k) e1[k] = (1.0 / n1) * e1[k];
+  e2[0] = e3[1] * e1[2] - e3[2] * e1[1];
+  e2[1] = e3[2] * e1[0] - e3[0] * e1[2];
+  e2[2] = e3[0] * e1[1] - e3[1] * e1[0];
+  for (int k = 0; k < 3; ++k) { c.T3[k] = e1[k]; c.T3[3 + k] = e2[k]; c.T3[6 + k] = e3[k]; }
+  double E = mat[0], nu = mat[1];
+  c.mu = E / (2.0 * (1 + nu));
+  c.lambda = 2.0 * c.mu * nu / (1 - 2.0 * nu);
+  c.stiff_drill = E * thick * thick * thick;
+  c.thick = thick;
+  auto dotv = [](const double* p, const double* q) { return p[0] * q[0] + p[1] * q[1] + p[2] * q[2]; };
+  double d23[3], d31[3], d12[3], d32[3], d13[3], d21[3];
+  for (int k = 0; k < 3; ++k) {
+    d23[k] = x2[k] - x3[k]; d31[k] = x3[k] - x1[k]; d12[k] = x1[k] - x2[k];
+    d32[k] = x3[k] - x2[k]; d13[k] = x1[k] - x3[k]; d21[k] = x2[k] - x1[k];
+  }
+  double Lx1[3] = {0.5 * dotv(d23, e2) / A, 0.5 * dotv(d31, e2) / A, 0.5 * dotv(d12, e2) / A};
+  double Lx2[3] = {0.5 * dotv(d32, e1) / A, 0.5 * dotv(d13, e1) / A, 0.5 * dotv(d21, e1) / A};
+  for (int g = 0; g < 3; ++g) {
+    const double* xp = xyz + 3 * (3 + g);
+    double L[3] = {tri_area2(xp, x2, x3) / A, tri_area2(xp, x3, x1) / A, tri_area2(xp, x1, x2) / A};
+    shell_shapes(L, Lx1, Lx2, c.Nu[g], c.Nu1[g], c.Nu2[g]);
+    c.Na[g][0] = 1 - 2 * L[2]; c.Na[g][1] = 1 - 2 * L[0]; c.Na[g][2] = 1 - 2 * L[1];
+    c.Na1[g][0] = -2 * Lx1[2]; c.Na1[g][1] = -2 * Lx1[0]; c.Na1[g][2] = -2 * Lx1[1];
+    c.Na2[g][0] = -2 * Lx2[2]; c.Na2[g][1] = -2 * Lx2[0]; c.Na2[g][2] = -2 * Lx2[1];
+  }
+  // six-point surface rule of Cowper (1973)
+  const double pa = 0.816847572980459, pb = 0.091576213509771, pc = 0.108103018168070, pd = 0.445948490915965;
+  const double wa = 0.109951743655322, wb = 0.223381589678011;
+  const double Lc[6][3] = {{pa, pb, pb}, {pb, pa, pb}, {pb, pb, pa}, {pc, pd, pd}, {pd, pc, pd}, {pd, pd, pc}};
+  for (int k = 0; k < 6; ++k) {
+    c.w4[k] = A * (k < 3 ? wa : wb);
+    shell_shapes(Lc[k], Lx1, Lx2, c.N4[k], c.N41[k], c.N42[k]);
+  }
+  c.alpha1 = A / 3.0;
+  for (int g = 0; g < 3; ++g) {
+    h.Q[g][0] = h.Q[g][4] = h.Q[g][8] = 1.0;
+    h.z1[g][0] = 1.0;
+    h.z2[g][1] = 1.0;
+  }
+}
+
+// Reverse Cuthill-McKee order of the nodes of one structure (node graph:
+// nodes that share an element).  Each connected component starts from a
+// pseudo-peripheral node (repeated breadth-first search from a node of
+// minimum degree in the last level); neighbours are visited by increasing
+// degree; the final order is reversed.  Nodes without elements keep their
+// place at the end.
+std::vector<int> rcm_order(int nn, const std::vector<std::vector<int>>& adj) {
+  std::vector<int> deg(nn), order;
+  order.reserve(nn);
+  for (int i = 0; i < nn; ++i) deg[i] = (int)adj[i].size();
+  std::vector<char> seen(nn, 0);
+  std::vector<int> level(nn, -1);
+  auto bfs_last = [&](int r, int* ecc) {
+    std::vector<int> q{r};
+    std::fill(level.begin(), level.end(), -1);
+    level[r] = 0;
+    for (size_t h = 0; h < q.size(); ++h)
+      for (int v : adj[q[h]])
+        if (level[v] < 0) { level[v] = level[q[h]] + 1; q.push_back(v); }
+    int last = level[q.back()];
+    *ecc = last;
+    int best = q.back();
+    for (int v : q)
+      if (level[v] == last && deg[v] < deg[best]) best = v;
+    return best;
+  };
+  for (;;) {
+    int start = -1;
+    for (int i = 0; i < nn; ++i)
+      if (!seen[i] && deg[i] > 0 && (start < 0 || deg[i] < deg[start])) start = i;
+    if (start < 0) break;
+    int ecc = 0, e2 = 0;
+    int cand = bfs_last(start, &ecc);
+    for (int it = 0; it < 8; ++it) {
+      int nxt = bfs_last(cand, &e2);
+      if (e2 <= ecc) break;
+      start = cand;
+      ecc = e2;
+      cand = nxt;
+    }
+    std::vector<int> q{start};
+    seen[start] = 1;
+    for (size_t h = 0; h < q.size(); ++h) {
+      std::vector<int> nb;
+      for (int v : adj[q[h]])
+        if (!seen[v]) nb.push_back(v);
+      std::sort(nb.begin(), nb.end(), [&](int x, int y) { return deg[x] != deg[y] ? deg[x] < deg[y] : x < y; });
+      for (int v : nb) { seen[v] = 1; q.push_back(v); }
+    }
+    order.insert(order.end(), q.rbegin(), q.rend());
+  }
+  for (int i = 0; i < nn; ++i)
+    if (!seen[i]) order.push_back(i);
+  return order;
+}
+
 }  // namespace gfh
 
 namespace gfh {
@@ -163,6 +307,16 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   int max_color = 0;
   std::vector<int> chain_flags;
   std::vector<std::vector<char>> chain_free;
+  // Shell_1 elements
+  std::vector<int> snodes, sstruct, spress, sarea, scolor;
+  std::vector<ShellConst> sconst;
+  std::vector<ShellHist> shist;
+  std::vector<ShellHistAux> saux;
+  int shell_off = 0, max_scolor = 0;
+  std::vector<int> wide_structs;
+  int64_t wb_total = 0;
+  int max_panels = 0, max_wkl = 0;
+  B->perm.clear();
   for (int s = 0; s < n; ++s) {
     const gf_model_desc& m = models[s];
     if (m.solution.type != GF_STATIC && m.solution.type != GF_DYNAMIC) { set_err(ctx, "structure %d: unknown solution type", s); return GF_ERR_ARG; }
@@ -170,9 +324,30 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       set_err(ctx, "structure %d: Rayleigh damping is not supported (alpha = beta = 0 required)", s);
       return GF_ERR_ARG;
     }
-    if (m.n_shells) { set_err(ctx, "structure %d: Shell_1 elements are not supported by this entry point", s); return GF_ERR_ARG; }
+    if (m.n_shells && m.n_beams) {
+      set_err(ctx, "structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
+      return GF_ERR_ARG;
+    }
+    if (m.n_shells && m.solution.type == GF_DYNAMIC) {
+      set_err(ctx, "structure %d: Shell_1 structures are supported in Static steps only", s);
+      return GF_ERR_ARG;
+    }
     const int nn = m.n_nodes;
+    const bool wide = m.n_shells > 0;
     std::vector<int> active(nn * 6, 0), c6(nn * 6, 0), g6(nn * 6, -2);
+    for (int e = 0; e < m.n_shells; ++e) {
+      const int* q = m.shells + 9 * e;
+      for (int j = 0; j < 6; ++j) {
+        if (q[j] < 0 || q[j] >= nn) { set_err(ctx, "structure %d: shell %d has node %d out of range", s, e, q[j]); return GF_ERR_ARG; }
+        // Shell_1 activates translations everywhere, rotations on the
+        // midside nodes (reference src/Shell_1.cpp:51-68)
+        for (int k = 0; k < (j < 3 ? 3 : 6); ++k) active[6 * q[j] + k] = 1;
+      }
+      if (q[6] < 0 || q[6] >= m.n_materials || q[7] < 0 || q[7] >= m.n_shell_sections) {
+        set_err(ctx, "structure %d: shell %d refers to a missing material or shell section", s, e);
+        return GF_ERR_ARG;
+      }
+    }
     for (int e = 0; e < m.n_beams; ++e) {
       for (int j = 0; j < 3; ++j) {
         int nd = m.beams[6 * e + j];
@@ -187,10 +362,51 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     }
     if (m.constraints)
       for (int i = 0; i < nn * 6; ++i) c6[i] = m.constraints[i] ? 1 : 0;
-    // SetGlobalDOFs (reference src/Solution.cpp:40-118): node-major numbering
+    // SetGlobalDOFs (reference src/Solution.cpp:40-118): node-major
+    // numbering.  Shell structures number their free DOFs in reverse
+    // Cuthill-McKee node order instead (the solver's numbering; results are
+    // reported per node, and gf_batch_assemble maps back to the reference's
+    // numbering through perm).
+    std::vector<int> node_order(nn);
+    for (int i = 0; i < nn; ++i) node_order[i] = i;
+    std::vector<int> g_nat(nn * 6, -2);
+    {
+      int q = 0;
+      for (int i = 0; i < nn; ++i)
+        for (int k = 0; k < 6; ++k)
+          if (active[6 * i + k]) g_nat[6 * i + k] = c6[6 * i + k] == 0 ? q++ : -1;
+    }
+    auto shell_band = [&](const std::vector<int>& g) {
+      int kl = 0;
+      for (int e = 0; e < m.n_shells; ++e) {
+        const int* q = m.shells + 9 * e;
+        int d[27];
+        for (int a = 0; a < 18; ++a) d[a] = g[6 * q[a / 3] + a % 3];
+        for (int a = 0; a < 9; ++a) d[18 + a] = g[6 * q[3 + a / 3] + 3 + a % 3];
+        for (int a = 0; a < 27; ++a)
+          for (int c = 0; c < 27; ++c)
+            if (d[a] >= 0 && d[c] >= 0) kl = std::max(kl, std::abs(d[a] - d[c]));
+      }
+      return kl;
+    };
+    int kl_nat = wide ? shell_band(g_nat) : 0;
+    if (wide) {
+      std::vector<std::vector<int>> adj(nn);
+      for (int e = 0; e < m.n_shells; ++e) {
+        const int* q = m.shells + 9 * e;
+        for (int a = 0; a < 6; ++a)
+          for (int c = 0; c < 6; ++c)
+            if (a != c) adj[q[a]].push_back(q[c]);
+      }
+      for (auto& v : adj) {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+      }
+      node_order = rcm_order(nn, adj);
+    }
     int nf = 0;
     bool has_f = false, has_m = false;
-    for (int i = 0; i < nn; ++i)
+    for (int i : node_order)
       for (int k = 0; k < 6; ++k) {
         if (!active[6 * i + k]) continue;
         if (c6[6 * i + k] == 0) {
@@ -201,6 +417,26 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
           g6[6 * i + k] = -1;
         }
       }
+    int wkl = 0;
+    if (wide) {
+      wkl = shell_band(g6);
+      if (wkl > kl_nat) {  // keep the natural numbering when it is narrower
+        node_order.resize(nn);
+        for (int i = 0; i < nn; ++i) node_order[i] = i;
+        dof_node6.resize(dof_node6.size() - nf);
+        g6 = g_nat;
+        for (int i = 0; i < nn; ++i)
+          for (int k = 0; k < 6; ++k)
+            if (g6[6 * i + k] >= 0) dof_node6.push_back((node_off + i) * 6 + k);
+        wkl = kl_nat;
+      }
+      std::vector<int> perm(nf);
+      for (int i = 0; i < nn * 6; ++i)
+        if (g_nat[i] >= 0) perm[g_nat[i]] = g6[i];
+      B->perm.push_back(perm);
+    } else {
+      B->perm.push_back(std::vector<int>());
+    }
     int kbs = 0;
     for (int e = 0; e < m.n_beams; ++e)
       for (int a = 0; a < 18; ++a)
@@ -212,7 +448,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       set_err(ctx, "structure %d: K_AA half-bandwidth %d exceeds %d (node-major numbering of a chain gives 17)", s, kbs, GF_KB);
       return GF_ERR_ARG;
     }
-    B->kb.push_back(kbs);
+    B->kb.push_back(wide ? kl_nat : kbs);
     if (m.solution.type == GF_DYNAMIC)
       for (int i = 0; i < nn; ++i) {
         int fr = (g6[6 * i + 3] >= 0) + (g6[6 * i + 4] >= 0) + (g6[6 * i + 5] >= 0);
@@ -251,6 +487,16 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     inf.has_force = has_f;
     inf.has_moment = has_m;
     inf.is_chain = chain_flags.back();
+    if (wide) {
+      inf.wide = 1;
+      inf.wkl = std::max(wkl, 1);
+      inf.n_panels = (nf + GF_WB_NB - 1) / GF_WB_NB;
+      inf.wb_off = wb_total;
+      wb_total += (int64_t)std::max(nf, 1) * (2 * inf.wkl + 1);
+      wide_structs.push_back(s);
+      max_panels = std::max(max_panels, inf.n_panels);
+      max_wkl = std::max(max_wkl, inf.wkl);
+    }
     // nodes
     for (int i = 0; i < nn; ++i) {
       for (int k = 0; k < 3; ++k) copy.push_back(m.node_xyz[3 * i + k]);
@@ -281,6 +527,32 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       ecolor.push_back(col);
       max_color = std::max(max_color, col + 1);
     }
+    // Shell_1 PreCalc and greedy colouring (up to 16 colours)
+    for (int e = 0; e < m.n_shells; ++e) {
+      const int* q = m.shells + 9 * e;
+      double xyz[18];
+      for (int j = 0; j < 6; ++j)
+        for (int k = 0; k < 3; ++k) xyz[3 * j + k] = m.node_xyz[3 * q[j] + k];
+      ShellConst c;
+      ShellHist h;
+      ShellHistAux x;
+      shell_precalc(xyz, m.materials + 3 * q[6], m.shell_sections[q[7]], c, h, x);
+      sconst.push_back(c);
+      shist.push_back(h);
+      saux.push_back(x);
+      for (int j = 0; j < 6; ++j) snodes.push_back(node_off + q[j]);
+      sstruct.push_back(s);
+      spress.push_back(-1);
+      sarea.push_back(0);
+      unsigned used = 0;
+      for (int j = 0; j < 6; ++j) used |= node_colors[q[j]];
+      int col = 0;
+      while (col < 16 && (used >> col) & 1u) ++col;
+      if (col >= 16) { set_err(ctx, "structure %d: shell colouring needs more than 16 colours", s); return GF_ERR_ARG; }
+      for (int j = 0; j < 6; ++j) node_colors[q[j]] |= 1u << col;
+      scolor.push_back(col);
+      max_scolor = std::max(max_scolor, col + 1);
+    }
     // tables and nodal loads (NodalLoad::UpdateforSolutionStep, reference
     // src/NodalLoad.cpp:235-263)
     auto add_table = [&](const gf_table& t) {
@@ -293,7 +565,24 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     inf.load_off = (int)loads.size();
     for (int l = 0; l < m.n_loads; ++l) {
       const gf_load& L = m.loads[l];
-      if (L.type != GF_LOAD_NODAL) { set_err(ctx, "structure %d: only nodal loads are supported for beams", s); return GF_ERR_ARG; }
+      if (L.type == GF_LOAD_SHELL_PRESSURE) {
+        // ShellLoad (reference src/ShellLoad.cpp:133-148): one follower
+        // pressure per element
+        if (L.table.n_cols < 1) { set_err(ctx, "structure %d: pressure table needs 1 column", s); return GF_ERR_ARG; }
+        int t = add_table(L.table);
+        for (int q = 0; q < L.n_items; ++q) {
+          int e = L.items[q];
+          if (e < 0 || e >= m.n_shells) { set_err(ctx, "structure %d: pressure on missing shell %d", s, e); return GF_ERR_ARG; }
+          if (spress[shell_off + e] >= 0) {
+            set_err(ctx, "structure %d: shell %d carries more than one pressure load", s, e);
+            return GF_ERR_ARG;
+          }
+          spress[shell_off + e] = t;
+          sarea[shell_off + e] = L.area_update ? 1 : 0;
+        }
+        continue;
+      }
+      if (L.type != GF_LOAD_NODAL) { set_err(ctx, "structure %d: unknown load type", s); return GF_ERR_ARG; }
       if (L.table.n_cols < 6) { set_err(ctx, "structure %d: nodal load table needs 6 columns", s); return GF_ERR_ARG; }
       int cnt[6] = {0, 0, 0, 0, 0, 0};
       for (int q = 0; q < L.n_items; ++q)
@@ -362,6 +651,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     B->info.push_back(inf);
     node_off += nn;
     elem_off += m.n_beams;
+    shell_off += m.n_shells;
     dof_off += nf_pad;
   }
   b.n_struct = n;
@@ -450,6 +740,31 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       if (ecolor[e] == c) color_elems.push_back(e);
   }
   b.color_off[max_color] = (int)color_elems.size();
+  // Shell_1 arrays, colour lists and the wide band
+  ShellData& sd = b.sh;
+  sd.n_shells = shell_off;
+  sd.n_wide = (int)wide_structs.size();
+  sd.max_panels = max_panels;
+  sd.max_kl = max_wkl;
+  sd.n_colors = max_scolor;
+  std::vector<int> scolor_elems;
+  for (int c = 0; c < max_scolor; ++c) {
+    sd.color_off[c] = (int)scolor_elems.size();
+    for (int e = 0; e < shell_off; ++e)
+      if (scolor[e] == c) scolor_elems.push_back(e);
+  }
+  sd.color_off[max_scolor] = (int)scolor_elems.size();
+  if (shell_off) {
+    if (!upload(B, &sd.snodes, snodes) || !upload(B, &sd.sstruct, sstruct) || !upload(B, &sd.spress, spress) ||
+        !upload(B, &sd.sarea, sarea) || !upload(B, &sd.sconst, sconst) || !upload(B, &sd.shist, shist) ||
+        !upload(B, &sd.saux, saux) || !upload(B, &B->shist0, shist) || !upload(B, &B->saux0, saux) ||
+        !upload(B, &sd.color_elems, scolor_elems) || !balloc(B, &sd.Ke, (size_t)shell_off * 729) ||
+        !balloc(B, &sd.Fe, (size_t)shell_off * 27))
+      return GF_ERR_CUDA;
+  }
+  if (!wide_structs.empty()) {
+    if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total)) return GF_ERR_CUDA;
+  }
   // device arrays
   std::vector<double> zeros6((size_t)node_off * 6, 0.0);
   if (!upload(B, &b.copy, copy) || !upload(B, &b.Qn, Qn) || !upload(B, &b.disp, zeros6) || !upload(B, &b.gl, gl) ||
@@ -468,6 +783,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
       !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18))
     return GF_ERR_CUDA;
+  b.xref = B->copy0;
   if (B->count_only) return GF_OK;
   CK(cudaMemsetAsync(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB, B->stream));
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
@@ -489,7 +805,7 @@ int count_launches_per_pass(const gf_batch* B) {
         chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
     }
   }
-  return 10 + colors + chain_launches;
+  return 10 + colors + chain_launches + shell_launches_per_pass(B->b);
 }
 
 int batch_reset(gf_batch* B) {
@@ -500,6 +816,10 @@ int batch_reset(gf_batch* B) {
   CK(cudaMemcpyAsync(b.Qn, B->Qn0, sizeof(double) * (size_t)b.n_nodes * 9, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.bhist, B->bhist0, sizeof(BeamHist) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(b.baux, B->baux0, sizeof(BeamHistAux) * (size_t)b.n_elem, cudaMemcpyDeviceToDevice, st));
+  if (b.sh.n_shells) {
+    CK(cudaMemcpyAsync(b.sh.shist, B->shist0, sizeof(ShellHist) * (size_t)b.sh.n_shells, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(b.sh.saux, B->saux0, sizeof(ShellHistAux) * (size_t)b.sh.n_shells, cudaMemcpyDeviceToDevice, st));
+  }
   const size_t n6 = sizeof(double) * (size_t)std::max(b.n_nodes, 1) * 6;
   CK(cudaMemsetAsync(b.disp, 0, n6, st));
   CK(cudaMemsetAsync(b.vel, 0, n6, st));
@@ -731,6 +1051,7 @@ int gf_batch_work(const gf_batch* B, double* lu_flops, double* asm_bytes, double
   for (int s = 0; s < n; ++s) {
     const StructInfo& inf = B->info[s];
     double nf = inf.n_free, kl = B->kb[s];
+    if (inf.wide) kl = inf.wkl;
     lu += st[s].n_solves * (2.0 * nf * kl * kl + 2.0 * nf * (kl + kl));
     ab += st[s].total_it * 8.0 * (6.0 * inf.n_nodes + 80.0 * inf.n_elem + (2 * kl + 1) * nf + nf);
     mf += st[s].total_it * (double)inf.n_elem * GF_BEAM_MOUNT_FLOPS;
@@ -825,18 +1146,30 @@ int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
   Batch bb = b;
   launch_iteration_partial(bb, B->stream);
   CK(cudaGetLastError());
-  std::vector<double> band((size_t)inf.n_free * GF_LDB), P(inf.n_free);
-  CK(cudaMemcpyAsync(band.data(), b.band + inf.band_off, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, B->stream));
+  const int nf = inf.n_free;
+  const int64_t W = inf.wide ? 2 * (int64_t)inf.wkl + 1 : GF_LDB;
+  std::vector<double> band((size_t)nf * W), P(nf);
+  const double* src = inf.wide ? b.sh.wband + inf.wb_off : b.band + inf.band_off;
+  CK(cudaMemcpyAsync(band.data(), src, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, B->stream));
   CK(cudaMemcpyAsync(P.data(), b.P + inf.dof_off, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, B->stream));
   CK(cudaStreamSynchronize(B->stream));
+  // the reference's numbering: identity, or back from the solver's
+  // reverse Cuthill-McKee numbering for wide structures
+  const std::vector<int>& perm = B->perm[s];
+  auto pm = [&](int i) { return perm.empty() ? i : perm[i]; };
+  const int64_t kw = inf.wide ? inf.wkl : GF_KB;
   int ldab = 3 * kb + 1;
   if (ab) {
-    std::memset(ab, 0, sizeof(double) * (size_t)ldab * inf.n_free);
-    for (int j = 0; j < inf.n_free; ++j)
-      for (int i = std::max(0, j - kb); i <= std::min(inf.n_free - 1, j + kb); ++i)
-        ab[(size_t)(2 * kb + i - j) + (size_t)j * ldab] = band[(size_t)(GF_KB + i - j) + (size_t)j * GF_LDB];
+    std::memset(ab, 0, sizeof(double) * (size_t)ldab * nf);
+    for (int j = 0; j < nf; ++j)
+      for (int i = std::max(0, j - kb); i <= std::min(nf - 1, j + kb); ++i) {
+        int64_t pi = pm(i), pj = pm(j);
+        if (std::llabs(pi - pj) > kw) continue;
+        ab[(size_t)(2 * kb + i - j) + (size_t)j * ldab] = band[(size_t)(kw + pi - pj) + (size_t)pj * W];
+      }
   }
-  if (PA) std::memcpy(PA, P.data(), sizeof(double) * inf.n_free);
+  if (PA)
+    for (int i = 0; i < nf; ++i) PA[i] = P[pm(i)];
   return batch_reset(B) == GF_OK ? GF_OK : GF_ERR_CUDA;
 }
 
@@ -892,6 +1225,65 @@ int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, c
     }
   }
   cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dK); cudaFree(df);
+  return rc;
+}
+
+int gf_shell_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick, int n_hist,
+                      const double* hist_disp, const double* disp, const double* pressure, int area_update, double* K,
+                      double* f) {
+  if (!ctx || n <= 0 || !xyz || !mat || !thick || !disp || !K || !f || n_hist < 0 || (n_hist && !hist_disp)) {
+    set_err(ctx, "gf_shell_elements: invalid arguments");
+    return GF_ERR_ARG;
+  }
+  std::vector<ShellConst> c(n);
+  std::vector<ShellHist> h(n);
+  std::vector<ShellHistAux> x(n);
+  std::vector<double> pu((size_t)n * 18, 0.0), p(n, std::nan(""));
+  for (int e = 0; e < n; ++e) {
+    shell_precalc(xyz + 18 * (size_t)e, mat + 3 * (size_t)e, thick[e], c[e], h[e], x[e]);
+    for (int a = 0; a < 18; ++a) {
+      double v = disp[(size_t)e * 27 + a];
+      for (int q = 0; q < n_hist; ++q) v += hist_disp[((size_t)e * n_hist + q) * 27 + a];
+      pu[(size_t)e * 18 + a] = v;
+    }
+    if (pressure) p[e] = pressure[e];
+  }
+  ShellConst* dc = nullptr;
+  ShellHist* dh = nullptr;
+  ShellHistAux* dx = nullptr;
+  double *dd = nullptr, *dpu = nullptr, *dp = nullptr, *dK = nullptr, *df = nullptr;
+  int rc = GF_OK;
+  if (!dmalloc(ctx, &dc, n) || !dmalloc(ctx, &dh, n) || !dmalloc(ctx, &dx, n) || !dmalloc(ctx, &dd, (size_t)n * 27) ||
+      !dmalloc(ctx, &dpu, (size_t)n * 18) || !dmalloc(ctx, &dp, (size_t)n) || !dmalloc(ctx, &dK, (size_t)n * 729) ||
+      !dmalloc(ctx, &df, (size_t)n * 27)) {
+    rc = GF_ERR_CUDA;
+  } else {
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(dc, c.data(), sizeof(ShellConst) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dh, h.data(), sizeof(ShellHist) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dx, x.data(), sizeof(ShellHistAux) * n, cudaMemcpyHostToDevice, st);
+    std::vector<double> step((size_t)n * 27);
+    for (int q = 0; q < n_hist; ++q) {
+      for (int e = 0; e < n; ++e)
+        std::memcpy(&step[(size_t)e * 27], hist_disp + ((size_t)e * n_hist + q) * 27, 27 * sizeof(double));
+      cudaMemcpyAsync(dd, step.data(), sizeof(double) * step.size(), cudaMemcpyHostToDevice, st);
+      launch_shell_commit_elements(n, dc, dh, dx, dd, st);
+      cudaStreamSynchronize(st);
+    }
+    cudaMemcpyAsync(dd, disp, sizeof(double) * (size_t)n * 27, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dpu, pu.data(), sizeof(double) * pu.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dp, p.data(), sizeof(double) * p.size(), cudaMemcpyHostToDevice, st);
+    launch_shell_elements(n, dc, dh, dd, dpu, dp, area_update, dK, df, st);
+    cudaMemcpyAsync(K, dK, sizeof(double) * (size_t)n * 729, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(f, df, sizeof(double) * (size_t)n * 27, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_err(ctx, "gf_shell_elements: %s", cudaGetErrorString(e));
+      rc = GF_ERR_CUDA;
+    }
+  }
+  cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dpu); cudaFree(dp); cudaFree(dK); cudaFree(df);
   return rc;
 }
 

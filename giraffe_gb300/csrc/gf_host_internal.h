@@ -91,6 +91,11 @@ struct gf_batch {
   double* Qn0 = nullptr;
   gf::BeamHist* bhist0 = nullptr;
   gf::BeamHistAux* baux0 = nullptr;
+  gf::ShellHist* shist0 = nullptr;
+  gf::ShellHistAux* saux0 = nullptr;
+  // wide (Shell_1) structures: the reference's free-DOF index -> the
+  // solver's (reverse Cuthill-McKee) index; empty for the others
+  std::vector<std::vector<int>> perm;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;

@@ -225,7 +225,7 @@ __global__ void k_zero(Batch b) {
   int s = blockIdx.y;
   if (!iterating(b.state[s])) return;
   const StructInfo inf = b.info[s];
-  int64_t nb = (int64_t)inf.n_free * GF_LDB;
+  int64_t nb = inf.wide ? 0 : (int64_t)inf.n_free * GF_LDB;  // wide structures: k_wb_zero
   double* band = b.band + inf.band_off;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
     band[i] = 0.0;
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_band_solve(Batch b) {
   StructState& st = b.state[s];
   if (!iterating(st) || !st.need_solve) return;
   const StructInfo inf = b.info[s];
-  if (inf.is_chain) return;
+  if (inf.is_chain || inf.wide) return;
   const int n = inf.n_free;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   extern __shared__ unsigned char smem_raw[];
@@ -824,7 +824,9 @@ void launch_iteration_partial(const Batch& b, cudaStream_t st) {
   int ns = b.n_struct;
   k_step_begin<<<ns, 256, 0, st>>>(b);
   k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
+  launch_wide_zero(b, st);
   launch_mount(b, st, nullptr);
+  launch_shell_mount(b, st);
   k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
   k_residual<<<ns, 256, 0, st>>>(b);
 }
@@ -840,7 +842,8 @@ static void set_attrs() {
 
 const char* kernel_class_name(int k) {
   static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_tangent", "loads", "residual", "band_solve",
-                                        "update", "control", "commit_elems", "commit_nodes", "chain_solve", "scatter"};
+                                        "update", "control", "commit_elems", "commit_nodes", "chain_solve", "scatter",
+                                        "shell_mount", "wide_solve"};
   return k >= 0 && k < KC_COUNT ? names[k] : "?";
 }
 
@@ -881,15 +884,19 @@ void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, Laun
   int ns = b.n_struct;
   { ProfScope q(prof, st, KC_STEP_BEGIN); k_step_begin<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_ZERO); k_zero<<<dim3(8, ns), 256, 0, st>>>(b); }
+  if (b.sh.n_wide) { ProfScope q(prof, st, KC_ZERO); launch_wide_zero(b, st); }
   launch_mount(b, st, prof);
+  if (b.sh.n_shells) { ProfScope q(prof, st, KC_SHELL); launch_shell_mount(b, st); }
   { ProfScope q(prof, st, KC_LOADS); k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
   if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_CHAIN); launch_chain_solve(b, b.chain, st); }
+  if (b.sh.n_wide) { ProfScope q(prof, st, KC_WIDE); launch_wide_solve(b, st); }
   { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {
     if (b.n_elem) { ProfScope q(prof, st, KC_COMMIT_ELEMS); k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b); }
+    if (b.sh.n_shells) { ProfScope q(prof, st, KC_COMMIT_ELEMS); launch_shell_commit(b, st); }
     if (b.n_nodes) { ProfScope q(prof, st, KC_COMMIT_NODES); k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b); }
   }
 }

@@ -35,7 +35,7 @@ struct LaunchProf {
 };
 enum KernelClass {
   KC_STEP_BEGIN = 0, KC_ZERO, KC_MOUNT, KC_LOADS, KC_RESIDUAL, KC_SOLVE, KC_UPDATE, KC_CONTROL,
-  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_COUNT
+  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_SHELL, KC_WIDE, KC_COUNT
 };
 const char* kernel_class_name(int k);
 
@@ -57,6 +57,22 @@ void launch_beam_inertia(int n, const BeamConst* c, const BeamHistAux* x, const 
 // elements in the global frame, FP64.  d: [n][18] nodal increments.
 void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const double* d, double* K,
                           double* f, cudaStream_t st);
+
+// Shell_1 structures (gf_shell.cu): element tangent + follower pressure and
+// the colour scatter into the wide band; zeroing of the wide band; the
+// wide-band LU and triangular solves; SaveLagrange.
+void launch_shell_mount(const Batch& b, cudaStream_t st);
+void launch_wide_zero(const Batch& b, cudaStream_t st);
+void launch_wide_solve(const Batch& b, cudaStream_t st);
+void launch_shell_commit(const Batch& b, cudaStream_t st);
+// Standalone Shell_1 elements (gf_shell_elements): d [n][27], pu [n][18],
+// p [n] (NaN: no pressure); K [n][729] column-major, f [n][27].
+void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const double* d, const double* pu,
+                           const double* p, int area_update, double* K, double* f, cudaStream_t st);
+void launch_shell_commit_elements(int n, const ShellConst* c, ShellHist* h, ShellHistAux* x, const double* d,
+                                  cudaStream_t st);
+// Kernel launches of one pass of the shell and wide-band kernels.
+int shell_launches_per_pass(const Batch& b);
 
 // Band factor + solve of independent systems in the batch layout
 // (GF_LDB rows); FP64.  Returns per-system info in state[].info_fail.

@@ -1,0 +1,953 @@
+// Shell_1 structures on the device: element tangent and internal force with
+// the follower pressure (k_shell_tangent), colour scatter into the wide band
+// (k_shell_scatter), SaveLagrange (k_shell_commit), and the wide-band LU with
+// its triangular solves for the K_AA of those structures.
+//
+// Element math restates reference src/Shell_1.cpp:
+//   899-1332   Mount: incremental Rodrigues kinematics at the three midside
+//              Gauss points, thickness integration (3 points) of the
+//              compressible neo-Hookean law, generalized constitutive matrix
+//              D (12x12), Psi (12x15), geometric part G (15x15),
+//              K = T^T sum_g w (dN^T (Psi^T D Psi + G) dN) T
+//   1392-1467  MountShellSpecialLoads: follower pressure and its tangent
+//   1650-1664  SaveLagrange
+// dN is block-sparse (each 3x3 block a scalar times I), so the products run
+// over the 3x3 blocks that are not zero.
+//
+// Wide band: K_AA of a structure with free-DOF half-bandwidth kl is stored
+// column-major with 2 kl + 1 rows.  No pivoting (the reference's tangent
+// operators here are near-symmetric positive definite; a zero or non-finite
+// pivot sets info_fail, which the step control treats like the reference's
+// solver failure).  Right-looking blocked LU, GF_WB_NB columns per panel:
+//   k_wb_diag    LU of the panel's diagonal block (one CTA per structure)
+//   k_wb_trsm    L21 = A21 U11^-1 (row-parallel) and U12 = L11^-1 A12
+//                (column-parallel), many CTAs
+//   k_wb_update  A22 -= L21 U12, 64x64 tiles (the only dense contraction:
+//                2 n kl^2 FP64 flops per factorization)
+// and the solves k_wb_fwd (y = L^-1 b, b in P, y in y) and k_wb_bwd
+// (x = U^-1 y into P), one launch per panel each.
+#include <cuda_runtime.h>
+
+#include "gf_kernels.cuh"
+#include "gf_math.cuh"
+#include "gf_types.h"
+
+namespace gf {
+
+namespace {
+
+__device__ __forceinline__ bool iterating_s(const StructState& s) { return s.phase == PH_ITER; }
+
+// 1/p by two Newton-Raphson steps from the FP32 hardware approximation;
+// exact division where the seed is out of FP32 range.
+__device__ __forceinline__ double wb_recip(double p) {
+  float pf = __double2float_rn(p);
+  float af = fabsf(pf);
+  if (!(af > 1e-30f && af < 1e30f)) return 1.0 / p;
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(pf));
+  double r = (double)rf;
+  double e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-p, r, 1.0);
+  return fma(r, e, r);
+}
+
+typedef V3<double> v3;
+typedef M3<double> m3;
+
+struct SGp {
+  v3 u, u1, u2, al, al1, al2;
+  double g;
+  m3 Xi, Xi1, Xi2, Q;
+  v3 z1, z2, eta1, eta2, k1, k2;
+};
+
+// Gauss-point kinematics of the increment d (27, element DOF order, global).
+__device__ void shell_gp(const ShellConst& c, const ShellHist& h, const double* d, int g, SGp& k) {
+  v3 ug = {{0, 0, 0}}, u1g = {{0, 0, 0}}, u2g = {{0, 0, 0}}, ag = {{0, 0, 0}}, a1g = {{0, 0, 0}},
+     a2g = {{0, 0, 0}};
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      ug[j] += d[3 * n + j] * c.Nu[g][n];
+      u1g[j] += d[3 * n + j] * c.Nu1[g][n];
+      u2g[j] += d[3 * n + j] * c.Nu2[g][n];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      ag[j] += d[18 + 3 * m + j] * c.Na[g][m];
+      a1g[j] += d[18 + 3 * m + j] * c.Na1[g][m];
+      a2g[j] += d[18 + 3 * m + j] * c.Na2[g][m];
+    }
+  }
+  m3 T;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) T[q] = c.T3[q];
+  k.u = mv(T, ug);
+  k.u1 = mv(T, u1g);
+  k.u2 = mv(T, u2g);
+  k.al = mv(T, ag);
+  k.al1 = mv(T, a1g);
+  k.al2 = mv(T, a2g);
+  double an2 = dot(k.al, k.al);
+  k.g = 4.0 / (4.0 + an2);
+  m3 A = skew(k.al), A2 = mul(A, A), Qd;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    Qd[q] = k.g * (A[q] + 0.5 * A2[q]);
+    k.Xi[q] = k.g * 0.5 * A[q];
+  }
+  Qd[0] += 1.0; Qd[4] += 1.0; Qd[8] += 1.0;
+  k.Xi[0] += k.g; k.Xi[4] += k.g; k.Xi[8] += k.g;
+  m3 S1 = skew(k.al1), S2 = skew(k.al2);
+  double p1 = dot(k.al, k.al1), p2 = dot(k.al, k.al2);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    k.Xi1[q] = -0.5 * k.g * (p1 * k.Xi[q] - S1[q]);
+    k.Xi2[q] = -0.5 * k.g * (p2 * k.Xi[q] - S2[q]);
+  }
+  m3 Qi;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) Qi[q] = h.Q[g][q];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    k.z1[j] = k.u1[j] + h.z1[g][j];
+    k.z2[j] = k.u2[j] + h.z2[g][j];
+  }
+  k.Q = mul(Qd, Qi);
+  k.eta1 = tmv(k.Q, k.z1);
+  k.eta2 = tmv(k.Q, k.z2);
+  k.eta1[0] -= 1.0;
+  k.eta2[1] -= 1.0;
+  m3 XQ = mul(k.Xi, Qi);
+  k.k1 = tmv(XQ, k.al1);
+  k.k2 = tmv(XQ, k.al2);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    k.k1[j] += h.k1[g][j];
+    k.k2[j] += h.k2[g][j];
+  }
+}
+
+__device__ __forceinline__ void gather_d(const Batch& b, int e, double* d) {
+  const int* nd = b.sh.snodes + 6 * e;
+#pragma unroll
+  for (int a = 0; a < 18; ++a) d[a] = b.disp[(int64_t)nd[a / 3] * 6 + a % 3];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) d[18 + a] = b.disp[(int64_t)nd[3 + a / 3] * 6 + 3 + a % 3];
+}
+
+__device__ __forceinline__ m3 ld3(const double* p) {
+  m3 r;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) r[q] = p[q];
+  return r;
+}
+
+// Table::GetValueAt (reference src/Table.cpp:73-102), first column:
+// clamped outside the table, linear between the rows that bracket time.
+__device__ __forceinline__ double table_value(const Batch& b, int t, double time) {
+  const TableDev T = b.tables[t];
+  const double* times = b.table_data + T.off;
+  const double* vals = times + T.n_times;
+  if (T.n_times == 0) return 0.0;
+  if (time >= times[T.n_times - 1]) return vals[(int64_t)(T.n_times - 1) * T.n_cols];
+  if (time <= times[0]) return vals[0];
+  int idx = 0;
+  while (time >= times[idx]) idx++;
+  double f = (time - times[idx - 1]) / (times[idx] - times[idx - 1]);
+  double a = vals[(int64_t)(idx - 1) * T.n_cols], c = vals[(int64_t)idx * T.n_cols];
+  return a + f * (c - a);
+}
+
+}  // namespace
+
+// Mount of one element at increment d: K (27x27 column-major, global
+// frame; written from zero) and f (internal force, global frame).
+__device__ void shell_mount(const ShellConst& c, const ShellHist& h, const double* d, double* K, double* f) {
+  for (int q = 0; q < 729; ++q) K[q] = 0.0;
+  double fl[27];
+#pragma unroll
+  for (int q = 0; q < 27; ++q) fl[q] = 0.0;
+  const double mu = c.mu, la = c.lambda;
+  const double csi[3] = {-0.77459666924148337703585307995648, 0.0, 0.77459666924148337703585307995648};
+  const double wt[3] = {0.55555555555555555555555555555556, 0.88888888888888888888888888888889,
+                        0.55555555555555555555555555555556};
+  for (int g = 0; g < 3; ++g) {
+    SGp k;
+    shell_gp(c, h, d, g, k);
+    // thickness integration: D blocks [row group (n1, m1, n2, m2)][column
+    // group (eta1, kappa1, eta2, kappa2)] and the generalized stresses
+    m3 D[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int x = 0; x < 9; ++x) D[r][q][x] = 0.0;
+    v3 nr1 = {{0, 0, 0}}, nr2 = {{0, 0, 0}}, mr1 = {{0, 0, 0}}, mr2 = {{0, 0, 0}};
+    const double jac = c.thick / 2.0;
+    for (int q = 0; q < 3; ++q) {
+      double zeta = c.thick * csi[q] / 2.0;
+      double w = wt[q] * jac;
+      double g11 = k.eta1[0] + zeta * k.k1[1], g12 = k.eta1[1] - zeta * k.k1[0], g13 = k.eta1[2];
+      double g21 = k.eta2[0] + zeta * k.k2[1], g22 = k.eta2[1] - zeta * k.k2[0], g23 = k.eta2[2];
+      double jb = (1.0 + g11) * (1.0 + g22) - g12 * g21;
+      double v = (la * (jb * jb * jb - 1.0) + 2.0 * mu * (jb - 1.0)) / (la * jb * jb * jb + 2.0 * mu * jb);
+      double den = la * jb * jb + 2.0 * mu;
+      double dv = ((la + 2.0 * mu) * (3.0 * la * jb * jb + 2.0 * mu)) / (jb * jb * den * den);
+      v3 t1 = {{mu * v * (1.0 + g22) + mu * (g11 - g22), mu * v * (-g21) + mu * (g12 + g21), mu * g13}};
+      v3 t2 = {{mu * v * (-g12) + mu * (g12 + g21), mu * v * (1.0 + g11) + mu * (g22 - g11), mu * g23}};
+      m3 C11 = {{mu * ((1.0 + g22) * (1.0 + g22) * dv + 1.0), -mu * (1.0 + g22) * g21 * dv, 0,
+                 -mu * (1.0 + g22) * g21 * dv, mu * (g21 * g21 * dv + 1.0), 0, 0, 0, mu}};
+      m3 C22 = {{mu * (g12 * g12 * dv + 1.0), -mu * ((1.0 + g11) * g12 * dv), 0,
+                 -mu * ((1.0 + g11) * g12 * dv), mu * ((1.0 + g11) * (1.0 + g11) * dv + 1.0), 0, 0, 0, mu}};
+      m3 C12 = {{-mu * ((1.0 + g22) * g12 * dv), mu * (v - 1.0 + (1.0 + g11) * (1.0 + g22) * dv), 0,
+                 mu * (1.0 - v + g12 * g21 * dv), -mu * ((1.0 + g11) * g21 * dv), 0, 0, 0, 0}};
+      m3 C21 = transpose(C12);
+      // with E3r = skew(e3): C E3r, E3r C, E3r C E3r in closed form
+      const m3* Cs[2][2] = {{&C11, &C12}, {&C21, &C22}};
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int bq = 0; bq < 2; ++bq) {
+          const m3& C = *Cs[a][bq];
+          m3 CE, EC, ECE;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            CE[i * 3 + 0] = C[i * 3 + 1];
+            CE[i * 3 + 1] = -C[i * 3 + 0];
+            CE[i * 3 + 2] = 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            EC[0 * 3 + j] = -C[1 * 3 + j];
+            EC[1 * 3 + j] = C[0 * 3 + j];
+            EC[2 * 3 + j] = 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            ECE[0 * 3 + j] = -CE[1 * 3 + j];
+            ECE[1 * 3 + j] = CE[0 * 3 + j];
+            ECE[2 * 3 + j] = 0.0;
+          }
+          // rows: n_a (group 2a), m_a (group 2a+1); columns: eta_b (2b), kappa_b (2b+1)
+#pragma unroll
+          for (int x = 0; x < 9; ++x) {
+            D[2 * a][2 * bq][x] += w * C[x];
+            D[2 * a][2 * bq + 1][x] -= w * zeta * CE[x];
+            D[2 * a + 1][2 * bq][x] += w * zeta * EC[x];
+            D[2 * a + 1][2 * bq + 1][x] -= w * zeta * zeta * ECE[x];
+          }
+        }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        nr1[j] += w * t1[j];
+        nr2[j] += w * t2[j];
+      }
+      mr1[0] += w * zeta * (-t1[1]);
+      mr1[1] += w * zeta * t1[0];
+      mr2[0] += w * zeta * (-t2[1]);
+      mr2[1] += w * zeta * t2[0];
+    }
+    D[1][1][8] = c.stiff_drill;
+    D[3][3][8] = c.stiff_drill;
+    mr1[2] = c.stiff_drill * k.k1[2];
+    mr2[2] = c.stiff_drill * k.k2[2];
+    // Psi blocks: P[r][r] (r = 0..3) and P[r][4]
+    m3 Qt = transpose(k.Q);
+    m3 QX = mul(Qt, k.Xi);
+    m3 Z1 = skew(k.z1), Z2 = skew(k.z2);
+    m3 Pd[4] = {Qt, QX, Qt, QX};
+    m3 P4[4] = {mul(mul(Qt, Z1), k.Xi), mul(Qt, k.Xi1), mul(mul(Qt, Z2), k.Xi), mul(Qt, k.Xi2)};
+    // M = Psi^T D Psi + G, 5x5 blocks
+    m3 M[5][5];
+    m3 DP4[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      m3 acc;
+#pragma unroll
+      for (int x = 0; x < 9; ++x) acc[x] = 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        m3 t = mul(D[r][q], P4[q]);
+#pragma unroll
+        for (int x = 0; x < 9; ++x) acc[x] += t[x];
+      }
+      DP4[r] = acc;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) M[a][q] = mul(tmul(Pd[a], D[a][q]), Pd[q]);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) M[a][4] = tmul(Pd[a], DP4[a]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      m3 acc;
+#pragma unroll
+      for (int x = 0; x < 9; ++x) acc[x] = 0.0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        m3 t = tmul(P4[r], D[r][q]);
+#pragma unroll
+        for (int x = 0; x < 9; ++x) acc[x] += t[x];
+      }
+      M[4][q] = mul(acc, Pd[q]);
+    }
+    {
+      m3 acc;
+#pragma unroll
+      for (int x = 0; x < 9; ++x) acc[x] = 0.0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        m3 t = tmul(P4[r], DP4[r]);
+#pragma unroll
+        for (int x = 0; x < 9; ++x) acc[x] += t[x];
+      }
+      M[4][4] = acc;
+    }
+    // geometric part G
+    v3 n1 = mv(k.Q, nr1), n2 = mv(k.Q, nr2), m1 = mv(k.Q, mr1), m2 = mv(k.Q, mr2);
+    m3 Xi = k.Xi;
+    m3 Gdua1 = mul(skew(n1), Xi), Gdua2 = mul(skew(n2), Xi);
+#pragma unroll
+    for (int x = 0; x < 9; ++x) { Gdua1[x] = -Gdua1[x]; Gdua2[x] = -Gdua2[x]; }
+    m3 Vm1 = opV(k.al, m1, k.g), Vm2 = opV(k.al, m2, k.g);
+    m3 Gaa;
+    {
+      m3 a1 = tmul(Xi, mul(mul(Z1, skew(n1)), Xi));
+      m3 a2 = opV(k.al, mv(Z1, n1), k.g);
+      m3 a3 = opdV(k.al, k.al1, m1, k.g);
+      m3 a4 = tmul(k.Xi1, mul(skew(m1), Xi));
+      m3 b1 = tmul(Xi, mul(mul(Z2, skew(n2)), Xi));
+      m3 b2 = opV(k.al, mv(Z2, n2), k.g);
+      m3 b3 = opdV(k.al, k.al2, m2, k.g);
+      m3 b4 = tmul(k.Xi2, mul(skew(m2), Xi));
+#pragma unroll
+      for (int x = 0; x < 9; ++x) Gaa[x] = (a1[x] - a2[x] + a3[x] - a4[x]) + (b1[x] - b2[x] + b3[x] - b4[x]);
+    }
+    m3 Vm1t = transpose(Vm1), Vm2t = transpose(Vm2), Gdua1t = transpose(Gdua1), Gdua2t = transpose(Gdua2);
+#pragma unroll
+    for (int x = 0; x < 9; ++x) {
+      M[0][4][x] += Gdua1[x];
+      M[1][4][x] += Vm1t[x];
+      M[2][4][x] += Gdua2[x];
+      M[3][4][x] += Vm2t[x];
+      M[4][0][x] += Gdua1t[x];
+      M[4][1][x] += Vm1[x];
+      M[4][2][x] += Gdua2t[x];
+      M[4][3][x] += Vm2[x];
+      M[4][4][x] += Gaa[x];
+    }
+    // generalized internal force q = Psi^T sigma
+    v3 sg[4] = {nr1, mr1, nr2, mr2};
+    v3 qv[5];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) qv[r] = tmv(Pd[r], sg[r]);
+    {
+      v3 acc = {{0, 0, 0}};
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        v3 t = tmv(P4[r], sg[r]);
+        acc[0] += t[0]; acc[1] += t[1]; acc[2] += t[2];
+      }
+      qv[4] = acc;
+    }
+    // dN coefficients: translation node a (0..5) sits in row blocks 0 (x1)
+    // and 2 (x2); midside rotation node m in blocks 1 (x1), 3 (x2), 4
+    const double a1w = c.alpha1;
+    for (int a = 0; a < 9; ++a) {
+      int ra[3];
+      double ca[3];
+      int na;
+      if (a < 6) { ra[0] = 0; ca[0] = c.Nu1[g][a]; ra[1] = 2; ca[1] = c.Nu2[g][a]; na = 2; }
+      else {
+        int m = a - 6;
+        ra[0] = 1; ca[0] = c.Na1[g][m]; ra[1] = 3; ca[1] = c.Na2[g][m]; ra[2] = 4; ca[2] = c.Na[g][m]; na = 3;
+      }
+      for (int i = 0; i < na; ++i)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) fl[3 * a + x] += a1w * ca[i] * qv[ra[i]][x];
+      for (int bb = 0; bb < 9; ++bb) {
+        int rb[3];
+        double cb[3];
+        int nbq;
+        if (bb < 6) { rb[0] = 0; cb[0] = c.Nu1[g][bb]; rb[1] = 2; cb[1] = c.Nu2[g][bb]; nbq = 2; }
+        else {
+          int m = bb - 6;
+          rb[0] = 1; cb[0] = c.Na1[g][m]; rb[1] = 3; cb[1] = c.Na2[g][m]; rb[2] = 4; cb[2] = c.Na[g][m]; nbq = 3;
+        }
+        double blk[9];
+#pragma unroll
+        for (int x = 0; x < 9; ++x) blk[x] = 0.0;
+        for (int i = 0; i < na; ++i)
+          for (int j = 0; j < nbq; ++j) {
+            double w = a1w * ca[i] * cb[j];
+            const m3& Mb = M[ra[i]][rb[j]];
+#pragma unroll
+            for (int x = 0; x < 9; ++x) blk[x] += w * Mb[x];
+          }
+        // local-frame block (3a.., 3bb..), column-major 27x27
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) K[(3 * a + i) + 27 * (3 * bb + j)] += blk[i * 3 + j];
+      }
+    }
+  }
+  // to the global frame: every 3x3 block B -> T3^T B T3, in place
+  m3 T;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) T[q] = c.T3[q];
+  for (int a = 0; a < 9; ++a)
+    for (int bb = 0; bb < 9; ++bb) {
+      m3 blk;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) blk[i * 3 + j] = K[(3 * a + i) + 27 * (3 * bb + j)];
+      m3 o = tmul(T, mul(blk, T));
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) K[(3 * a + i) + 27 * (3 * bb + j)] = o[i * 3 + j];
+    }
+  for (int a = 0; a < 9; ++a) {
+    v3 x = {{fl[3 * a], fl[3 * a + 1], fl[3 * a + 2]}};
+    v3 y = tmv(T, x);
+    f[3 * a] = y[0]; f[3 * a + 1] = y[1]; f[3 * a + 2] = y[2];
+  }
+}
+
+// Follower pressure p at the current configuration (pu: displacements of
+// the six nodes from the reference position, global): P_loading -= the
+// consistent nodal load, K += its tangent.
+__device__ void shell_pressure(const ShellConst& c, const double* pu, double p, bool area_update, double* K,
+                               double* f) {
+  {
+    v3 e1 = {{c.T3[0], c.T3[1], c.T3[2]}}, e2 = {{c.T3[3], c.T3[4], c.T3[5]}};
+    for (int kq = 0; kq < 6; ++kq) {
+      v3 t1, t2;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+        for (int n = 0; n < 6; ++n) {
+          s1 += c.N41[kq][n] * pu[3 * n + j];
+          s2 += c.N42[kq][n] * pu[3 * n + j];
+        }
+        t1[j] = e1[j] + s1;
+        t2[j] = e2[j] + s2;
+      }
+      v3 cr = cross(t1, t2);
+      double nc = sqrt(dot(cr, cr));
+      v3 np = {{(1.0 / nc) * cr[0], (1.0 / nc) * cr[1], (1.0 / nc) * cr[2]}};
+      v3 qp = {{-p * np[0], -p * np[1], -p * np[2]}};
+      double fac = area_update ? c.w4[kq] * nc : c.w4[kq];
+#pragma unroll
+      for (int n = 0; n < 6; ++n)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f[3 * n + j] -= fac * c.N4[kq][n] * qp[j];
+      m3 S1 = skew(t1), S2 = skew(t2), Pm;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          Pm[i * 3 + j] = area_update ? (i == j ? 1.0 : 0.0) : (1.0 / nc) * ((i == j ? 1.0 : 0.0) - np[i] * np[j]);
+      for (int bb = 0; bb < 6; ++bb) {
+        m3 Bb;
+#pragma unroll
+        for (int x = 0; x < 9; ++x) Bb[x] = S1[x] * c.N42[kq][bb] - S2[x] * c.N41[kq][bb];
+        m3 Kb = area_update ? Bb : mul(Pm, Bb);
+        for (int a = 0; a < 6; ++a) {
+          double w = c.w4[kq] * p * c.N4[kq][a];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) K[(3 * a + i) + 27 * (3 * bb + j)] += w * Kb[i * 3 + j];
+        }
+      }
+    }
+  }
+}
+
+// One thread per Shell_1 element of an iterating structure: Mount +
+// MountElementLoads + the element's ShellLoad at the step's time; K (27x27,
+// column-major, global frame) and f (P_loading) go to the element scratch.
+__global__ void __launch_bounds__(64) k_shell_tangent(Batch b) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= b.sh.n_shells) return;
+  int s = b.sh.sstruct[e];
+  const StructState& st = b.state[s];
+  if (!iterating_s(st)) return;
+  double* K = b.sh.Ke + (int64_t)e * 729;
+  double d[27], f[27];
+  gather_d(b, e, d);
+  shell_mount(b.sh.sconst[e], b.sh.shist[e], d, K, f);
+  int pt = b.sh.spress[e];
+  if (pt >= 0) {
+    const int* nd = b.sh.snodes + 6 * e;
+    double pu[18];
+    for (int a = 0; a < 18; ++a) {
+      int64_t q = (int64_t)nd[a / 3] * 6 + a % 3;
+      pu[a] = b.copy[q] - b.xref[q] + d[a];  // xref: reference positions, 6 per node
+    }
+    shell_pressure(b.sh.sconst[e], pu, table_value(b, pt, st.time), b.sh.sarea[e] != 0, K, f);
+  }
+  double* F = b.sh.Fe + (int64_t)e * 27;
+#pragma unroll
+  for (int a = 0; a < 27; ++a) F[a] = f[a];
+}
+
+// Standalone elements (gf_shell_elements): n elements with their own
+// constants, history and increments d ([n][27]); with pressure p[e] (NaN:
+// none) at the displacement pu ([n][18]).
+__global__ void __launch_bounds__(64) k_shell_elements(int n, const ShellConst* cs, const ShellHist* hs,
+                                                       const double* ds, const double* pus, const double* ps,
+                                                       int area_update, double* Ks, double* fs) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double d[27], f[27];
+  for (int a = 0; a < 27; ++a) d[a] = ds[(int64_t)e * 27 + a];
+  double* K = Ks + (int64_t)e * 729;
+  shell_mount(cs[e], hs[e], d, K, f);
+  double p = ps[e];
+  if (p == p) {
+    double pu[18];
+    for (int a = 0; a < 18; ++a) pu[a] = pus[(int64_t)e * 18 + a];
+    shell_pressure(cs[e], pu, p, area_update != 0, K, f);
+  }
+  for (int a = 0; a < 27; ++a) fs[(int64_t)e * 27 + a] = f[a];
+}
+
+// MountGlobal: one warp per element of one colour (no two elements of a
+// colour share a node, so no two writers meet).  The element's free DOFs
+// (structure-local, in the structure's reverse Cuthill-McKee numbering) go
+// to the wide band and to P.
+__global__ void k_shell_scatter(Batch b, int color) {
+  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int lo = b.sh.color_off[color], hi = b.sh.color_off[color + 1];
+  if (lo + w >= hi) return;
+  int e = b.sh.color_elems[lo + w];
+  int s = b.sh.sstruct[e];
+  if (!iterating_s(b.state[s])) return;
+  const StructInfo& inf = b.info[s];
+  const int* nd = b.sh.snodes + 6 * e;
+  int myg = -1;
+  if (lane < 27) {
+    int node = lane < 18 ? nd[lane / 3] : nd[3 + (lane - 18) / 3];
+    int k = lane < 18 ? lane % 3 : 3 + (lane - 18) % 3;
+    myg = b.gl[(int64_t)node * 6 + k];
+  }
+  const double* K = b.sh.Ke + (int64_t)e * 729;
+  const double* F = b.sh.Fe + (int64_t)e * 27;
+  double* band = b.sh.wband + inf.wb_off;
+  const int kl = inf.wkl;
+  const int64_t W = 2 * kl + 1;
+  if (lane < 27 && myg >= 0) b.P[inf.dof_off + myg] += F[lane];
+  for (int base = 0; base < 729; base += 32) {
+    int idx = base + lane;
+    bool valid = idx < 729;
+    int r = valid ? idx % 27 : 0, q = valid ? idx / 27 : 0;
+    int gr = __shfl_sync(0xffffffffu, myg, r);
+    int gq = __shfl_sync(0xffffffffu, myg, q);
+    if (valid && gr >= 0 && gq >= 0) band[(kl + gr - gq) + (int64_t)gq * W] += K[idx];
+  }
+}
+
+// SaveLagrange at the converged increment d.
+__device__ void shell_commit(const ShellConst& c, ShellHist& h, ShellHistAux& x, const double* d) {
+  for (int g = 0; g < 3; ++g) {
+    SGp k;
+    shell_gp(c, h, d, g, k);
+    v3 ai = {{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}};
+    v3 an = rodrigues_compose(k.al, ai);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      h.k1[g][j] = k.k1[j];
+      h.k2[g][j] = k.k2[j];
+      h.z1[g][j] = k.z1[j];
+      h.z2[g][j] = k.z2[j];
+      x.u[g][j] += k.u[j];
+      x.alpha[g][j] = an[j];
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) h.Q[g][q] = k.Q[q];
+  }
+}
+
+// SaveLagrange of the structures that converged this pass.
+__global__ void k_shell_commit(Batch b) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= b.sh.n_shells) return;
+  int s = b.sh.sstruct[e];
+  if (!b.state[s].commit) return;
+  ShellHist h = b.sh.shist[e];
+  ShellHistAux x = b.sh.saux[e];
+  double d[27];
+  gather_d(b, e, d);
+  shell_commit(b.sh.sconst[e], h, x, d);
+  b.sh.shist[e] = h;
+  b.sh.saux[e] = x;
+}
+
+__global__ void k_shell_commit_elements(int n, const ShellConst* cs, ShellHist* hs, ShellHistAux* xs,
+                                        const double* ds) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  ShellHist h = hs[e];
+  ShellHistAux x = xs[e];
+  double d[27];
+  for (int a = 0; a < 27; ++a) d[a] = ds[(int64_t)e * 27 + a];
+  shell_commit(cs[e], h, x, d);
+  hs[e] = h;
+  xs[e] = x;
+}
+
+// ---------------------------------------------------------------------------
+// Wide-band LU.  Band pointer and geometry of wide structure w.
+namespace {
+struct WB {
+  double* a;
+  int n, kl;
+  int64_t W;
+  __device__ __forceinline__ double& at(int i, int j) const { return a[(kl + i - j) + (int64_t)j * W]; }
+};
+
+__device__ __forceinline__ bool wide_active(const Batch& b, int s) {
+  const StructState& st = b.state[s];
+  return iterating_s(st) && st.need_solve;
+}
+
+__device__ __forceinline__ WB wb_of(const Batch& b, const StructInfo& inf) {
+  WB w;
+  w.a = b.sh.wband + inf.wb_off;
+  w.n = inf.n_free;
+  w.kl = inf.wkl;
+  w.W = 2 * (int64_t)inf.wkl + 1;
+  return w;
+}
+constexpr int NB = GF_WB_NB;
+}  // namespace
+
+// zero the wide band of iterating structures
+__global__ void k_wb_zero(Batch b) {
+  int s = b.sh.wide_structs[blockIdx.y];
+  if (!iterating_s(b.state[s])) return;
+  const StructInfo& inf = b.info[s];
+  int64_t n = (int64_t)inf.n_free * (2 * (int64_t)inf.wkl + 1);
+  double* a = b.sh.wband + inf.wb_off;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = 0.0;
+}
+
+// LU (no pivoting) of the diagonal block of panel p, in place.
+__global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
+  int s = b.sh.wide_structs[blockIdx.x];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  __shared__ double A[NB][NB + 1];
+  __shared__ int fail;
+  const int tid = threadIdx.x;
+  if (tid == 0) fail = 0;
+  for (int x = tid; x < NB * NB; x += blockDim.x) {
+    int i = x % NB, j = x / NB;
+    double v = 0.0;
+    if (i < nb && j < nb && abs(i - j) <= w.kl) v = w.at(j0 + i, j0 + j);
+    A[i][j] = v;
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    double piv = A[k][k];
+    if (tid == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
+    double r = wb_recip(piv);
+    __syncthreads();
+    for (int i = k + 1 + tid; i < nb; i += blockDim.x) A[i][k] *= r;
+    __syncthreads();
+    int m = nb - k - 1;
+    for (int x = tid; x < m * m; x += blockDim.x) {
+      int i = k + 1 + x % m, j = k + 1 + x / m;
+      A[i][j] -= A[i][k] * A[k][j];
+    }
+    __syncthreads();
+  }
+  for (int x = tid; x < nb * nb; x += blockDim.x) {
+    int i = x % nb, j = x / nb;
+    if (abs(i - j) <= w.kl) w.at(j0 + i, j0 + j) = A[i][j];
+  }
+  if (tid == 0 && fail) b.state[s].info_fail = 1;
+}
+
+// L21 = A21 U11^-1 (row blocks) and U12 = L11^-1 A12 (column blocks) of
+// panel p.  16 rows (or columns) per CTA, 16 threads each splitting the
+// panel width; blockIdx.x < nrb: L21 row block, else U12 column block.
+__global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
+  int s = b.sh.wide_structs[blockIdx.y];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);  // rows below / columns right of the panel
+  if (m <= 0) return;
+  const int nrb = (m + 15) / 16;
+  const bool lower = blockIdx.x < nrb;
+  const int blk = lower ? blockIdx.x : blockIdx.x - nrb;
+  if (blk >= nrb) return;
+  __shared__ double T[NB][NB + 1];  // the diagonal block's LU
+  __shared__ double X[16][NB + 1];
+  __shared__ double rd[NB];         // reciprocals of U11's diagonal
+  const int tid = threadIdx.x;
+  for (int x = tid; x < NB * NB; x += blockDim.x) {
+    int i = x % NB, j = x / NB;
+    T[i][j] = (i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
+  }
+  if (tid < nb) rd[tid] = wb_recip(w.at(j0 + tid, j0 + tid));
+  const int r = tid >> 4, c = tid & 15;  // row (or column) r of the block, lane c of its 16
+  const int g = j0 + nb + blk * 16 + r;  // global row (lower) or column (upper)
+  const bool live = g < j0 + nb + m;
+  for (int k = c; k < NB; k += 16) {
+    double v = 0.0;
+    if (live && k < nb) {
+      if (lower) { if (g - (j0 + k) <= w.kl) v = w.at(g, j0 + k); }
+      else { if (g - (j0 + k) <= w.kl) v = w.at(j0 + k, g); }
+    }
+    X[r][k] = v;
+  }
+  __syncthreads();
+  const unsigned gm = 0xffffu << (16 * ((tid >> 4) & 1));
+  if (lower) {
+    // x U11 = a: x_k = a_k / u_kk, then a_j -= x_k u_kj (j > k)
+    for (int k = 0; k < nb; ++k) {
+      double xk = X[r][k] * rd[k];
+      __syncwarp(gm);
+      for (int j = k + 1 + c; j < nb; j += 16) X[r][j] -= xk * T[k][j];
+      if (c == 0) X[r][k] = xk;
+      __syncwarp(gm);
+    }
+  } else {
+    // L11 y = a (unit lower): y_k = a_k, then a_i -= l_ik y_k (i > k)
+    for (int k = 0; k < nb; ++k) {
+      double yk = X[r][k];
+      __syncwarp(gm);
+      for (int i = k + 1 + c; i < nb; i += 16) X[r][i] -= T[i][k] * yk;
+      __syncwarp(gm);
+    }
+  }
+  __syncthreads();
+  for (int k = c; k < nb; k += 16) {
+    if (!live || g - (j0 + k) > w.kl) continue;
+    if (lower) w.at(g, j0 + k) = X[r][k];
+    else w.at(j0 + k, g) = X[r][k];
+  }
+}
+
+// A22 -= L21 U12 over the (m x m) trailing window of panel p, 64x64 tiles,
+// each of 256 threads a 4x4 block of outputs.
+__global__ void __launch_bounds__(256) k_wb_update(Batch b, int p) {
+  int s = b.sh.wide_structs[blockIdx.z];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);
+  if (m <= 0) return;
+  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  if (r0 >= m || c0 >= m) return;
+  constexpr int KC = 32;               // panel columns per shared-memory stage
+  __shared__ double Ls[KC][64 + 1];  // [k][row]
+  __shared__ double Us[KC][64 + 1];  // [k][col]
+  const int tid = threadIdx.x;
+  const int base = j0 + nb;
+  const int ty = tid >> 4, tx = tid & 15;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int k0 = 0; k0 < nb; k0 += KC) {
+    for (int x = tid; x < KC * 64; x += blockDim.x) {
+      int i = x % 64, k = x / 64;
+      int gk = j0 + k0 + k;
+      int gi = base + r0 + i;
+      Ls[k][i] = (k0 + k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
+      int gj = base + c0 + i;
+      Us[k][i] = (k0 + k < nb && c0 + i < m && gj - gk <= w.kl) ? w.at(gk, gj) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < KC; ++k) {
+      double a[4], bq[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = Ls[k][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bq[j] = Us[k][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bq[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    int cj = c0 + tx + 16 * j;
+    if (cj >= m) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int ri = r0 + ty + 16 * i;
+      if (ri >= m) continue;
+      w.at(base + ri, base + cj) -= acc[i][j];
+    }
+  }
+}
+
+// Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
+// below the panel: P_i -= L21(i, :) y_p.  Every CTA solves the small
+// triangle redundantly; CTA 0 writes y_p.
+__global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
+  int s = b.sh.wide_structs[blockIdx.y];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);
+  double* P = b.P + inf.dof_off;
+  double* Y = b.y + inf.dof_off;
+  __shared__ double ys[NB];
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    // lanes hold entries k = lane and lane + 32
+    double v0 = tid < nb ? P[j0 + tid] : 0.0, v1 = tid + 32 < nb ? P[j0 + tid + 32] : 0.0;
+    for (int k = 0; k < nb; ++k) {
+      double yk = __shfl_sync(0xffffffffu, k < 32 ? v0 : v1, k & 31);
+      int i0 = tid, i1 = tid + 32;
+      if (i0 > k && i0 < nb && i0 - k <= w.kl) v0 -= w.at(j0 + i0, j0 + k) * yk;
+      if (i1 > k && i1 < nb && i1 - k <= w.kl) v1 -= w.at(j0 + i1, j0 + k) * yk;
+    }
+    ys[tid] = v0;
+    ys[tid + 32] = v1;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int k = tid; k < nb; k += blockDim.x) Y[j0 + k] = ys[k];
+  int i = nb + blockIdx.x * blockDim.x + tid;  // row offset from j0
+  if (i < nb + m && j0 + i < w.n) {
+    double acc = 0.0;
+    for (int k = 0; k < nb; ++k)
+      if (i - k <= w.kl) acc = fma(w.at(j0 + i, j0 + k), ys[k], acc);
+    P[j0 + i] -= acc;
+  }
+}
+
+// Backward substitution for panel p (last panel first): x_p = U11^-1 y_p into
+// P; then the rows above the panel: y_i -= U(i, panel) x_p.
+__global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
+  int s = b.sh.wide_structs[blockIdx.y];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  double* P = b.P + inf.dof_off;
+  double* Y = b.y + inf.dof_off;
+  __shared__ double xs[NB];
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    double v0 = tid < nb ? Y[j0 + tid] : 0.0, v1 = tid + 32 < nb ? Y[j0 + tid + 32] : 0.0;
+    for (int k = nb - 1; k >= 0; --k) {
+      double rp = wb_recip(w.at(j0 + k, j0 + k));
+      double mine = k < 32 ? v0 : v1;
+      double xk = __shfl_sync(0xffffffffu, mine, k & 31) * rp;
+      if (k < 32) { if (tid == k) v0 = xk; }
+      else { if (tid + 32 == k) v1 = xk; }
+      int i0 = tid, i1 = tid + 32;
+      if (i0 < k && k - i0 <= w.kl) v0 -= w.at(j0 + i0, j0 + k) * xk;
+      if (i1 < k && k - i1 <= w.kl) v1 -= w.at(j0 + i1, j0 + k) * xk;
+    }
+    xs[tid] = v0;
+    xs[tid + 32] = v1;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int k = tid; k < nb; k += blockDim.x) P[j0 + k] = xs[k];
+  const int top = max(0, j0 - w.kl);
+  int i = top + blockIdx.x * blockDim.x + tid;
+  if (i < j0) {
+    double acc = 0.0;
+    for (int k = 0; k < nb; ++k)
+      if (j0 + k - i <= w.kl) acc = fma(w.at(i, j0 + k), xs[k], acc);
+    Y[i] -= acc;
+  }
+}
+
+void launch_shell_mount(const Batch& b, cudaStream_t st) {
+  if (b.sh.n_shells == 0) return;
+  k_shell_tangent<<<(b.sh.n_shells + 63) / 64, 64, 0, st>>>(b);
+  for (int c = 0; c < b.sh.n_colors; ++c) {
+    int cnt = b.sh.color_off[c + 1] - b.sh.color_off[c];
+    if (cnt <= 0) continue;
+    k_shell_scatter<<<(cnt + 3) / 4, 128, 0, st>>>(b, c);
+  }
+}
+
+void launch_wide_zero(const Batch& b, cudaStream_t st) {
+  if (b.sh.n_wide == 0) return;
+  k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
+}
+
+void launch_wide_solve(const Batch& b, cudaStream_t st) {
+  if (b.sh.n_wide == 0) return;
+  const int nw = b.sh.n_wide;
+  const int mr = b.sh.max_kl;  // largest kl over the wide structures
+  const int tiles = (mr + 63) / 64;
+  const int nrb = (mr + 15) / 16;
+  for (int p = 0; p < b.sh.max_panels; ++p) {
+    k_wb_diag<<<nw, 256, 0, st>>>(b, p);
+    k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, st>>>(b, p);
+    k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p);
+  }
+  const int rb = (mr + 255) / 256;
+  for (int p = 0; p < b.sh.max_panels; ++p) k_wb_fwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
+  for (int p = b.sh.max_panels - 1; p >= 0; --p) k_wb_bwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
+}
+
+void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const double* d, const double* pu,
+                           const double* p, int area_update, double* K, double* f, cudaStream_t st) {
+  if (n <= 0) return;
+  k_shell_elements<<<(n + 63) / 64, 64, 0, st>>>(n, c, h, d, pu, p, area_update, K, f);
+}
+
+void launch_shell_commit_elements(int n, const ShellConst* c, ShellHist* h, ShellHistAux* x, const double* d,
+                                  cudaStream_t st) {
+  if (n <= 0) return;
+  k_shell_commit_elements<<<(n + 127) / 128, 128, 0, st>>>(n, c, h, x, d);
+}
+
+void launch_shell_commit(const Batch& b, cudaStream_t st) {
+  if (b.sh.n_shells == 0) return;
+  k_shell_commit<<<(b.sh.n_shells + 127) / 128, 128, 0, st>>>(b);
+}
+
+}  // namespace gf
+
+namespace gf {
+int shell_launches_per_pass(const Batch& b) {
+  int n = 0;
+  if (b.sh.n_shells) {
+    n += 2;  // tangent + commit
+    for (int c = 0; c < b.sh.n_colors; ++c) n += b.sh.color_off[c + 1] > b.sh.color_off[c];
+  }
+  if (b.sh.n_wide) n += 1 + 5 * b.sh.max_panels;
+  return n;
+}
+}  // namespace gf

@@ -47,6 +47,38 @@ struct BeamHistAux {
   double alpha[2][3];
 };
 
+// Shell_1 PreCalc constants (reference src/Shell_1.cpp:1666-2365): local
+// frame rows e1r, e2r, e3r; Lame constants and drilling stiffness; shape
+// functions at the three midside Gauss points (translations Nu of the six
+// nodes, rotations Na of the three midside nodes, with x1 / x2 derivatives);
+// the six-point surface rule (weights w4, translation shape functions and
+// derivatives) used by the follower pressure.
+struct ShellConst {
+  double T3[9];
+  double mu, lambda, stiff_drill, thick, alpha1;
+  double Nu[3][6], Nu1[3][6], Nu2[3][6];
+  double Na[3][3], Na1[3][3], Na2[3][3];
+  double w4[6];
+  double N4[6][6], N41[6][6], N42[6][6];
+};
+
+// Shell_1 Gauss-point history read by Mount: Q_i, kappa_r1_i, kappa_r2_i,
+// z_x1_i, z_x2_i (reference src/Shell_1.cpp:1650-1664).
+struct ShellHist {
+  double Q[3][9];
+  double k1[3][3], k2[3][3];
+  double z1[3][3], z2[3][3];
+};
+
+// Written at commit only: u_i and alpha_i.
+struct ShellHistAux {
+  double u[3][3];
+  double alpha[3][3];
+};
+
+// Wide-band LU panel width (columns per panel).
+#define GF_WB_NB 64
+
 enum Phase : int { PH_START = 0, PH_ITER = 1, PH_DONE = 2, PH_ABORTED = 3 };
 
 // Per-structure parameters (Static solution step + ConvergenceCriteria).
@@ -67,6 +99,15 @@ struct StructInfo {
   int has_force, has_moment;  // free translational / rotational DOFs exist
   int load_off, n_loads;  // nodal load entries of this structure
   int is_chain;  // solved by the chain solver (else by the band LU)
+  // wide-band structures (Shell_1): K_AA column-major with 2 wkl + 1 rows,
+  // entry (i, j) at wband[wb_off + (wkl + i - j) + j (2 wkl + 1)]; the free
+  // DOFs are numbered in reverse Cuthill-McKee node order
+  int wide;
+  int wkl;
+  int n_panels;  // ceil(n_free / GF_WB_NB)
+  int pad_w;
+  int64_t wb_off;    // into ShellData::wband
+  int64_t winv_off;  // into ShellData::winv: n_panels x 2 x NB x NB
 };
 
 // Per-structure Newton / load-step control state (reference
@@ -151,6 +192,29 @@ struct ChainData {
   int n_roots;
 };
 
+// Shell_1 elements and the wide-band storage of their structures.
+struct ShellData {
+  int n_shells;
+  int n_wide;       // structures solved by the wide-band LU
+  int max_panels;   // over those structures
+  int max_kl;       // over those structures
+  int* wide_structs;  // [n_wide] structure indices
+  int* snodes;      // [n_shells][6] batch node ids
+  int* sstruct;
+  int* spress;      // table index of the follower pressure on the element, or -1
+  int* sarea;       // AreaUpdate flag of that pressure
+  ShellConst* sconst;
+  ShellHist* shist;
+  ShellHistAux* saux;
+  double* Ke;       // [n_shells][27 x 27] column-major (global frame)
+  double* Fe;       // [n_shells][27]
+  int* color_elems;
+  int color_off[17];
+  int n_colors;
+  double* wband;
+  double* winv;
+};
+
 // Device pointers of a batch.
 struct Batch {
   int n_struct, n_nodes, n_elem, n_free;
@@ -158,6 +222,7 @@ struct Batch {
   // nodes
   double* disp;
   double* copy;
+  double* xref;        // reference positions (initial copy: 6 per node)
   double* Qn;
   double* vel;         // Newmark velocities (dynamic structures)
   double* accel;
@@ -201,6 +266,7 @@ struct Batch {
   int max_refine;
   int* running;  // structures still running after the last pass
   ChainData chain;
+  ShellData sh;
 };
 
 }  // namespace gf

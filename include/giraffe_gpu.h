@@ -19,6 +19,9 @@
  *                           ConvergenceCriteria checks
  *                           (src/ConvergenceCriteria.cpp:187-618)
  *   gf_beam_inertia_elements Beam_1::MountMass (src/Beam_1.cpp:1564-1638)
+ *   gf_shell_elements       Shell_1::PreCalc + SaveLagrange + Mount +
+ *                           MountElementLoads + MountShellSpecialLoads
+ *                           (src/Shell_1.cpp:899-1467, 1650-2365)
  *   gf_beam_elements        Beam_1::PreCalc + SaveLagrange + Mount +
  *                           MountElementLoads (src/Beam_1.cpp:501-843,
  *                           1494-1506)
@@ -77,8 +80,11 @@ void gf_destroy(gf_ctx* ctx);
 const char* gf_last_error(const gf_ctx* ctx);
 void gf_default_opts(gf_solve_opts* opts);
 
-/* Uploads n structures (each a Static step of Beam_1 elements with nodal
- * loads, constraints and prescribed displacements) into one device batch. */
+/* Uploads n structures into one device batch: each a Static or Dynamic
+ * step of Beam_1 elements, or a Static step of Shell_1 elements with
+ * follower pressures, with nodal loads, constraints and prescribed
+ * displacements.  Shell_1 structures are solved by the wide-band LU on
+ * their reverse Cuthill-McKee numbering. */
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts);
 void gf_batch_destroy(gf_batch* batch);
 /* Restores the initial configuration of every structure (device side). */
@@ -108,7 +114,7 @@ int gf_batch_solve_timed(gf_batch* batch, int steps, double* ms);
  * kernel; per kernel class k (0 <= k < GF_N_KERNELS, names from
  * gf_kernel_name) *ms_out[k] receives the summed device time and
  * launches_out[k] the launch count. */
-enum { GF_N_KERNELS = 12 };
+enum { GF_N_KERNELS = 14 };
 int gf_batch_profile(gf_batch* batch, double* ms_out, long long* launches_out);
 const char* gf_kernel_name(int k);
 /* Bytes the batch moved host->device when it was created, and bytes
@@ -133,6 +139,21 @@ int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opt
 int gf_beam_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
                      const double* cs, int n_hist, const double* hist_disp, const double* disp, double* K,
                      double* f);
+
+/* n independent Shell_1 elements (replaces Shell_1::PreCalc + SaveLagrange +
+ * Mount + MountElementLoads + MountShellSpecialLoads, reference
+ * src/Shell_1.cpp:1666-2365, 1650-1664, 899-1332, 1384-1467; homogeneous
+ * section, Hooke material): PreCalc from the six nodal coordinates (n x 18),
+ * material (n x 3: E, nu, rho) and thickness (n); n_hist committed
+ * increments per element (n x n_hist x 27, element DOF order: translations
+ * of nodes 1..6, then rotations of nodes 4..6) build the Gauss-point
+ * history; then Mount at disp (n x 27).  pressure (n, may be NULL; NaN =
+ * none) adds the follower pressure at the displaced configuration (history
+ * plus disp) with the reference's AreaUpdate flag area_update.  K: n x 729
+ * (column-major 27x27), f: n x 27 (P_loading). */
+int gf_shell_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick, int n_hist,
+                      const double* hist_disp, const double* disp, const double* pressure, int area_update, double* K,
+                      double* f);
 
 /* Inertial contributions of n independent Beam_1 elements (replaces
  * Beam_1::MountMass, reference src/Beam_1.cpp:1564-1638, for Hooke
