@@ -749,8 +749,10 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
   }
 }
 
-// A22 -= L21 U12 over the (m x m) trailing window of panel p, 64x64 tiles,
-// each of 256 threads a 4x4 block of outputs.
+// A22 -= L21 U12 over the (m x m) trailing window of panel p, 32x32 tiles
+// (small tiles keep the FP64 work even across the SMs), each of 256
+// threads a 2x2 block of outputs.
+constexpr int UT = 32;
 __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p) {
   int s = b.sh.wide_structs[blockIdx.z];
   if (!wide_active(b, s)) return;
@@ -760,54 +762,36 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p) {
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);
   if (m <= 0) return;
-  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int r0 = blockIdx.x * UT, c0 = blockIdx.y * UT;
   if (r0 >= m || c0 >= m) return;
-  constexpr int KC = 32;               // panel columns per shared-memory stage
-  __shared__ double Ls[KC][64 + 1];  // [k][row]
-  __shared__ double Us[KC][64 + 1];  // [k][col]
+  __shared__ double Ls[NB][UT + 1];  // [k][row]
+  __shared__ double Us[NB][UT + 1];  // [k][col]
   const int tid = threadIdx.x;
   const int base = j0 + nb;
+  for (int x = tid; x < NB * UT; x += blockDim.x) {
+    int i = x % UT, k = x / UT;
+    int gk = j0 + k;
+    int gi = base + r0 + i;
+    Ls[k][i] = (k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
+    int gj = base + c0 + i;
+    Us[k][i] = (k < nb && c0 + i < m && gj - gk <= w.kl) ? w.at(gk, gj) : 0.0;
+  }
+  __syncthreads();
   const int ty = tid >> 4, tx = tid & 15;
-  double acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-  for (int k0 = 0; k0 < nb; k0 += KC) {
-    for (int x = tid; x < KC * 64; x += blockDim.x) {
-      int i = x % 64, k = x / 64;
-      int gk = j0 + k0 + k;
-      int gi = base + r0 + i;
-      Ls[k][i] = (k0 + k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
-      int gj = base + c0 + i;
-      Us[k][i] = (k0 + k < nb && c0 + i < m && gj - gk <= w.kl) ? w.at(gk, gj) : 0.0;
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int k = 0; k < KC; ++k) {
-      double a[4], bq[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = Ls[k][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) bq[j] = Us[k][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bq[j], acc[i][j]);
-    }
-    __syncthreads();
+  double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+#pragma unroll 8
+  for (int k = 0; k < NB; ++k) {
+    double l0 = Ls[k][ty], l1 = Ls[k][ty + 16], u0 = Us[k][tx], u1 = Us[k][tx + 16];
+    a00 = fma(l0, u0, a00);
+    a01 = fma(l0, u1, a01);
+    a10 = fma(l1, u0, a10);
+    a11 = fma(l1, u1, a11);
   }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    int cj = c0 + tx + 16 * j;
-    if (cj >= m) continue;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      int ri = r0 + ty + 16 * i;
-      if (ri >= m) continue;
-      w.at(base + ri, base + cj) -= acc[i][j];
-    }
-  }
+  const int ri0 = r0 + ty, ri1 = r0 + ty + 16, cj0 = c0 + tx, cj1 = c0 + tx + 16;
+  if (ri0 < m && cj0 < m) w.at(base + ri0, base + cj0) -= a00;
+  if (ri0 < m && cj1 < m) w.at(base + ri0, base + cj1) -= a01;
+  if (ri1 < m && cj0 < m) w.at(base + ri1, base + cj0) -= a10;
+  if (ri1 < m && cj1 < m) w.at(base + ri1, base + cj1) -= a11;
 }
 
 // Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
@@ -823,16 +807,21 @@ __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
   const int m = min(w.kl, w.n - j0 - nb);
   double* P = b.P + inf.dof_off;
   double* Y = b.y + inf.dof_off;
+  __shared__ double T[NB][NB + 1];  // the panel's diagonal block (L11 below the diagonal)
   __shared__ double ys[NB];
   const int tid = threadIdx.x;
+  for (int x = tid; x < NB * NB; x += blockDim.x) {
+    int i = x % NB, j = x / NB;
+    T[i][j] = (i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
+  }
+  __syncthreads();
   if (tid < 32) {
     // lanes hold entries k = lane and lane + 32
     double v0 = tid < nb ? P[j0 + tid] : 0.0, v1 = tid + 32 < nb ? P[j0 + tid + 32] : 0.0;
     for (int k = 0; k < nb; ++k) {
       double yk = __shfl_sync(0xffffffffu, k < 32 ? v0 : v1, k & 31);
-      int i0 = tid, i1 = tid + 32;
-      if (i0 > k && i0 < nb && i0 - k <= w.kl) v0 -= w.at(j0 + i0, j0 + k) * yk;
-      if (i1 > k && i1 < nb && i1 - k <= w.kl) v1 -= w.at(j0 + i1, j0 + k) * yk;
+      if (tid > k) v0 -= T[tid][k] * yk;
+      if (tid + 32 > k) v1 -= T[tid + 32][k] * yk;
     }
     ys[tid] = v0;
     ys[tid + 32] = v1;
@@ -860,19 +849,26 @@ __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   double* P = b.P + inf.dof_off;
   double* Y = b.y + inf.dof_off;
+  __shared__ double T[NB][NB + 1];  // the panel's diagonal block (U11 on and above the diagonal)
+  __shared__ double rdiag[NB];
   __shared__ double xs[NB];
   const int tid = threadIdx.x;
+  for (int x = tid; x < NB * NB; x += blockDim.x) {
+    int i = x % NB, j = x / NB;
+    T[i][j] = (i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
+  }
+  __syncthreads();
+  if (tid < nb) rdiag[tid] = wb_recip(T[tid][tid]);
+  __syncthreads();
   if (tid < 32) {
     double v0 = tid < nb ? Y[j0 + tid] : 0.0, v1 = tid + 32 < nb ? Y[j0 + tid + 32] : 0.0;
     for (int k = nb - 1; k >= 0; --k) {
-      double rp = wb_recip(w.at(j0 + k, j0 + k));
       double mine = k < 32 ? v0 : v1;
-      double xk = __shfl_sync(0xffffffffu, mine, k & 31) * rp;
+      double xk = __shfl_sync(0xffffffffu, mine, k & 31) * rdiag[k];
       if (k < 32) { if (tid == k) v0 = xk; }
       else { if (tid + 32 == k) v1 = xk; }
-      int i0 = tid, i1 = tid + 32;
-      if (i0 < k && k - i0 <= w.kl) v0 -= w.at(j0 + i0, j0 + k) * xk;
-      if (i1 < k && k - i1 <= w.kl) v1 -= w.at(j0 + i1, j0 + k) * xk;
+      if (tid < k) v0 -= T[tid][k] * xk;
+      if (tid + 32 < k) v1 -= T[tid + 32][k] * xk;
     }
     xs[tid] = v0;
     xs[tid + 32] = v1;
@@ -909,7 +905,7 @@ void launch_wide_solve(const Batch& b, cudaStream_t st) {
   if (b.sh.n_wide == 0) return;
   const int nw = b.sh.n_wide;
   const int mr = b.sh.max_kl;  // largest kl over the wide structures
-  const int tiles = (mr + 63) / 64;
+  const int tiles = (mr + UT - 1) / UT;
   const int nrb = (mr + 15) / 16;
   for (int p = 0; p < b.sh.max_panels; ++p) {
     k_wb_diag<<<nw, 256, 0, st>>>(b, p);
