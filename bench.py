@@ -53,6 +53,10 @@ def parse():
                     help="requests in the served-stream leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="device-memory budget of the server")
+    ap.add_argument("--shell-steps", type=int, default=2,
+                    help="load steps (of 20) of the 64x64x2 Shell_1 plate leg (0 = skip)")
+    ap.add_argument("--dyn-steps", type=int, default=50,
+                    help="time steps (of 1000) of the batched-dynamics leg (0 = skip)")
     return ap.parse_args()
 
 
@@ -229,6 +233,78 @@ def plain_leg(ctx, structs, sample_n):
                       f"{solves} Newton solves in {ms:.1f} ms of device time"}
 
 
+def shell_leg(ctx, args, fp64_peak):
+    """The Shell_1 plate (64x64 squares x 2 six-node triangles, 84,867 free
+    DOFs, clamped edges, follower pressure ramped to 1e5 Pa over 20 load
+    steps): the first `shell_steps` load steps, device-timed, with the
+    wide-band LU's FP64 rate; and an 8x8 plate solved completely by the GPU
+    and by the oracle on the host cores, like for like."""
+    import ctypes as C
+
+    from giraffe_gb300 import configs, gpu
+    from oracle import oracle
+
+    L = ctx.L
+    s = configs.square_plate(64, steps=20)
+    s.solution.end_time = args.shell_steps / 20.0
+    b = gpu.BatchSolver(ctx, [s])
+    b.reset()
+    ms = b.run()
+    fin, st = b.results()
+    lu, ab, mf = C.c_double(), C.c_double(), C.c_double()
+    L.gf_batch_work(b.h, C.byref(lu), C.byref(ab), C.byref(mf))
+    dims = (C.c_int * 2)()
+    L.gf_batch_assemble(b.h, 0, None, None, dims)
+    launches = b.launches()
+    b.close()
+    small = configs.square_plate(8, steps=20)
+    bs = gpu.BatchSolver(ctx, [small])
+    bs.reset()
+    bs.run()
+    bs.reset()
+    ms_small = bs.run()
+    st_small = bs.results()[1][0]
+    bs.close()
+    t0 = time.perf_counter()
+    _, so, _ = oracle.solve(small, 0)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"Shell_1 plate 64x64x2, {dims[0]} free DOFs, natural numbering half-bandwidth "
+                        f"{dims[1]}, first {args.shell_steps} of 20 load steps",
+            "newton_solves": int(st[0][0]), "newton_passes": int(st[0][1]), "ms": ms,
+            "solves_per_s": st[0][0] / (ms / 1e3), "ms_per_pass": ms / max(1, st[0][1]),
+            "wide_lu_tflops": lu.value / (ms / 1e3) / 1e12, "fp64_peak_tflops": fp64_peak,
+            "wide_lu_frac_of_measured_fp64": lu.value / (ms / 1e3) / 1e12 / fp64_peak,
+            "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
+            "plate8": {"workload": "Shell_1 plate 8x8x2 (1,203 free DOFs), all 20 load steps",
+                        "gpu_solves_per_s": st_small[0] / (ms_small / 1e3), "gpu_ms": ms_small,
+                        "cpu_oracle_solves_per_s": so[0] / cpu_s, "cpu_cores": 1,
+                        "same_counts": bool(tuple(st_small) == tuple(so))}}
+
+
+def dynamics_leg(ctx, args):
+    """Batched implicit dynamics (256 pipe Beam_1 chains of 100-1000
+    elements, Newmark beta 0.25 gamma 0.5, dt 0.01 s, sinusoidal top
+    displacement): the first `dyn_steps` of the 1000 time steps,
+    device-timed after one warm-up run."""
+    from giraffe_gb300 import configs, gpu
+
+    structs = configs.batched_dynamic(256, seed=args.seed)
+    for s in structs:
+        s.solution.end_time = args.dyn_steps * 0.01
+    b = gpu.BatchSolver(ctx, structs)
+    b.reset()
+    b.run()
+    b.reset()
+    ms = b.run()
+    _, st = b.results()
+    launches = b.launches()
+    b.close()
+    solves = int(st[:, 0].sum())
+    return {"workload": f"256 pipe chains, 100-1000 elements uniform (seed {args.seed}), Newmark, first "
+                        f"{args.dyn_steps} of 1000 time steps", "newton_solves": solves, "ms": ms,
+            "solves_per_s": solves / (ms / 1e3), "aborted": int(st[:, 3].sum()), "gpu_launches": launches}
+
+
 def served_leg(ctx, args, rank):
     """Continuous batching of a Poisson stream of static pipe-chain requests
     (1k-50k DOF log-uniform) through gf_server_*: admitted by the device
@@ -284,10 +360,10 @@ def run_ours(args, rank, world):
     # per-kernel device times (one profiled solve, events around every launch)
     L.gf_batch_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.gf_kernel_name.restype = C.c_char_p
-    kms = (C.c_double * 14)()
-    kl = (C.c_longlong * 14)()
+    kms = (C.c_double * 17)()
+    kl = (C.c_longlong * 17)()
     ctx.check(L.gf_batch_profile(b.h, kms, kl), "gf_batch_profile")
-    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(14) if kl[i]}
+    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(17) if kl[i]}
     L.gf_batch_work.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
     lu_f, asm_b, mnt_f = C.c_double(), C.c_double(), C.c_double()
     ctx.check(L.gf_batch_work(b.h, C.byref(lu_f), C.byref(asm_b), C.byref(mnt_f)), "gf_batch_work")
@@ -342,6 +418,8 @@ def run_ours(args, rank, world):
                      "unit": "GB/s", "frac": asm_b.value / t / 1e9 / peaks.get("hbm_gbs"), "traffic": None})
     plain = plain_leg(ctx, structs, args.plain_sample)
     plain["batched_over_plain"] = value / plain["value"]
+    shell = shell_leg(ctx, args, fp64.value) if args.shell_steps > 0 else None
+    dyn = dynamics_leg(ctx, args) if args.dyn_steps > 0 else None
     serving = None
     if args.serve_requests > 0:
         serving = served_leg(ctx, args, rank)
@@ -367,6 +445,8 @@ def run_ours(args, rank, world):
                 "peaks_measured": {"fp64_tflops": fp64.value, "fp32_tflops": fp32.value},
                 "clocks": clk.summary(),
                 "plain_single_structure": plain,
+                "shell_plate": shell,
+                "dynamics": dyn,
                 "serving": serving,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)

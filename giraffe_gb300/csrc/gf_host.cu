@@ -764,6 +764,10 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   }
   if (!wide_structs.empty()) {
     if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total)) return GF_ERR_CUDA;
+    if (!B->count_only) {
+      for (auto& a : sd.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+      for (auto& e : sd.evt) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
   }
   // device arrays
   std::vector<double> zeros6((size_t)node_off * 6, 0.0);
@@ -886,6 +890,10 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
 void gf_batch_destroy(gf_batch* B) {
   if (!B) return;
   if (B->graph) cudaGraphExecDestroy(B->graph);
+  for (auto& a : B->b.sh.aux)
+    if (a) cudaStreamDestroy(a);
+  for (auto& e : B->b.sh.evt)
+    if (e) cudaEventDestroy(e);
   for (void* p : B->allocs) {
     if (B->arena) B->arena->release(p);
     else cudaFree(p);

@@ -814,9 +814,6 @@ static bool g_attr_set = false;
 
 static void set_attrs();
 
-namespace {
-struct ProfScope;
-}
 static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof);
 
 void launch_iteration_partial(const Batch& b, cudaStream_t st) {
@@ -843,27 +840,10 @@ static void set_attrs() {
 const char* kernel_class_name(int k) {
   static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_tangent", "loads", "residual", "band_solve",
                                         "update", "control", "commit_elems", "commit_nodes", "chain_solve", "scatter",
-                                        "shell_mount", "wide_solve"};
+                                        "shell_mount", "wide_diag", "wide_trsm", "wide_update", "wide_subst"};
   return k >= 0 && k < KC_COUNT ? names[k] : "?";
 }
 
-namespace {
-struct ProfScope {
-  LaunchProf* p;
-  cudaStream_t st;
-  int idx;
-  ProfScope(LaunchProf* p_, cudaStream_t s, int k) : p(p_), st(s), idx(-1) {
-    if (p && p->n < p->cap) {
-      idx = p->n++;
-      p->cls[idx] = k;
-      cudaEventRecord(p->ev[2 * idx], st);
-    }
-  }
-  ~ProfScope() {
-    if (idx >= 0) cudaEventRecord(p->ev[2 * idx + 1], st);
-  }
-};
-}  // namespace
 
 static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   if (b.n_elem == 0) return;
@@ -891,7 +871,7 @@ void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, Laun
   { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
   if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_CHAIN); launch_chain_solve(b, b.chain, st); }
-  if (b.sh.n_wide) { ProfScope q(prof, st, KC_WIDE); launch_wide_solve(b, st); }
+  if (b.sh.n_wide) launch_wide_solve(b, st, prof);
   { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {

@@ -35,9 +35,27 @@ struct LaunchProf {
 };
 enum KernelClass {
   KC_STEP_BEGIN = 0, KC_ZERO, KC_MOUNT, KC_LOADS, KC_RESIDUAL, KC_SOLVE, KC_UPDATE, KC_CONTROL,
-  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_SHELL, KC_WIDE, KC_COUNT
+  KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_SHELL, KC_WIDE_DIAG, KC_WIDE_TRSM, KC_WIDE_UPDATE,
+  KC_WIDE_SUBST, KC_COUNT
 };
 const char* kernel_class_name(int k);
+
+// Brackets one launch with profiling events (no-op when p is null).
+struct ProfScope {
+  LaunchProf* p;
+  cudaStream_t st;
+  int idx;
+  ProfScope(LaunchProf* p_, cudaStream_t s, int k) : p(p_), st(s), idx(-1) {
+    if (p && p->n < p->cap) {
+      idx = p->n++;
+      p->cls[idx] = k;
+      cudaEventRecord(p->ev[2 * idx], st);
+    }
+  }
+  ~ProfScope() {
+    if (idx >= 0) cudaEventRecord(p->ev[2 * idx + 1], st);
+  }
+};
 
 void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels = true, LaunchProf* prof = nullptr);
 // FMA throughput probe: 8 independent chains per thread, `iters` steps.
@@ -63,7 +81,7 @@ void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const do
 // wide-band LU and triangular solves; SaveLagrange.
 void launch_shell_mount(const Batch& b, cudaStream_t st);
 void launch_wide_zero(const Batch& b, cudaStream_t st);
-void launch_wide_solve(const Batch& b, cudaStream_t st);
+void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof = nullptr);
 void launch_shell_commit(const Batch& b, cudaStream_t st);
 // Standalone Shell_1 elements (gf_shell_elements): d [n][27], pu [n][18],
 // p [n] (NaN: no pressure); K [n][729] column-major, f [n][27].

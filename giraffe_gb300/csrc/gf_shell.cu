@@ -753,7 +753,9 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
 // (small tiles keep the FP64 work even across the SMs), each of 256
 // threads a 2x2 block of outputs.
 constexpr int UT = 32;
-__global__ void __launch_bounds__(256) k_wb_update(Batch b, int p) {
+// part: 0 every tile, 1 only the tiles of the next panel's diagonal block
+// (the first NB rows and columns of the window), 2 every other tile.
+__global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
   int s = b.sh.wide_structs[blockIdx.z];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -764,6 +766,8 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p) {
   if (m <= 0) return;
   const int r0 = blockIdx.x * UT, c0 = blockIdx.y * UT;
   if (r0 >= m || c0 >= m) return;
+  const bool corner = r0 < NB && c0 < NB;
+  if ((part == 1 && !corner) || (part == 2 && corner)) return;
   __shared__ double Ls[NB][UT + 1];  // [k][row]
   __shared__ double Us[NB][UT + 1];  // [k][col]
   const int tid = threadIdx.x;
@@ -901,20 +905,53 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
   k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
 }
 
-void launch_wide_solve(const Batch& b, cudaStream_t st) {
+// Panel loop with lookahead on two helper streams (fork / join by events,
+// so a captured pass keeps the same dependencies):
+//   main   trsm(p) -> update corner(p) -> update rest(p) -> [join diag(p+1)]
+//   s2     [after corner(p)] diag(p+1)
+//   s3     [after trsm(p)]   forward substitution of panel p
+// The next panel's diagonal LU and the forward substitution run while the
+// bulk of the trailing update occupies the SMs; the backward substitution
+// follows the last panel.
+void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   if (b.sh.n_wide == 0) return;
-  const int nw = b.sh.n_wide;
-  const int mr = b.sh.max_kl;  // largest kl over the wide structures
+  const ShellData& sd = b.sh;
+  const int nw = sd.n_wide;
+  const int mr = sd.max_kl;  // largest kl over the wide structures
   const int tiles = (mr + UT - 1) / UT;
+  const int ct = (NB + UT - 1) / UT;
   const int nrb = (mr + 15) / 16;
-  for (int p = 0; p < b.sh.max_panels; ++p) {
-    k_wb_diag<<<nw, 256, 0, st>>>(b, p);
-    k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, st>>>(b, p);
-    k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p);
-  }
   const int rb = (mr + 255) / 256;
-  for (int p = 0; p < b.sh.max_panels; ++p) k_wb_fwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
-  for (int p = b.sh.max_panels - 1; p >= 0; --p) k_wb_bwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
+  cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1];
+  // the helpers fork from the main stream at their first wait and join it
+  // again before the backward substitution
+  cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
+  { ProfScope q(prof, st, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, st>>>(b, 0); }
+  for (int p = 0; p < sd.max_panels; ++p) {
+    { ProfScope q(prof, st, KC_WIDE_TRSM); k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, st>>>(b, p); }
+    cudaEventRecord(e_trsm, st);
+    cudaStreamWaitEvent(s3, e_trsm, 0);
+    { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
+    bool next = p + 1 < sd.max_panels;
+    if (next) {
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(ct, ct, nw), 256, 0, st>>>(b, p, 1); }
+      cudaEventRecord(e_corner, st);
+      cudaStreamWaitEvent(s2, e_corner, 0);
+      { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, s2>>>(b, p + 1); }
+      cudaEventRecord(e_diag, s2);
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p, 2); }
+      cudaStreamWaitEvent(st, e_diag, 0);
+    } else {
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p, 0); }
+    }
+  }
+  // join: every forward step is done before the backward substitution
+  cudaEventRecord(e_fwd, s3);
+  cudaStreamWaitEvent(st, e_fwd, 0);
+  for (int p = sd.max_panels - 1; p >= 0; --p) {
+    ProfScope q(prof, st, KC_WIDE_SUBST);
+    k_wb_bwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
+  }
 }
 
 void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const double* d, const double* pu,
@@ -943,7 +980,7 @@ int shell_launches_per_pass(const Batch& b) {
     n += 2;  // tangent + commit
     for (int c = 0; c < b.sh.n_colors; ++c) n += b.sh.color_off[c + 1] > b.sh.color_off[c];
   }
-  if (b.sh.n_wide) n += 1 + 5 * b.sh.max_panels;
+  if (b.sh.n_wide) n += 1 + 6 * b.sh.max_panels;
   return n;
 }
 }  // namespace gf

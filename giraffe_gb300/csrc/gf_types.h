@@ -16,6 +16,7 @@
 //             reference src/BandMatrix.cpp:214,246), FP64 and an FP32 copy
 //   factor    U rows: n_free x (GF_KB+1), [j][c] = U(j, j+c)
 #pragma once
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 #define GF_KB 17
@@ -107,7 +108,6 @@ struct StructInfo {
   int n_panels;  // ceil(n_free / GF_WB_NB)
   int pad_w;
   int64_t wb_off;    // into ShellData::wband
-  int64_t winv_off;  // into ShellData::winv: n_panels x 2 x NB x NB
 };
 
 // Per-structure Newton / load-step control state (reference
@@ -212,7 +212,10 @@ struct ShellData {
   int color_off[17];
   int n_colors;
   double* wband;
-  double* winv;
+  // host handles of the wide-band lookahead: two helper streams and the
+  // events that fork from and join into the pass's stream
+  cudaStream_t aux[2];
+  cudaEvent_t evt[5];  // [1] after trsm, [2] after the corner update, [3] after diag, [4] end of forward
 };
 
 // Device pointers of a batch.

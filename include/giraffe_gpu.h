@@ -114,7 +114,7 @@ int gf_batch_solve_timed(gf_batch* batch, int steps, double* ms);
  * kernel; per kernel class k (0 <= k < GF_N_KERNELS, names from
  * gf_kernel_name) *ms_out[k] receives the summed device time and
  * launches_out[k] the launch count. */
-enum { GF_N_KERNELS = 14 };
+enum { GF_N_KERNELS = 17 };
 int gf_batch_profile(gf_batch* batch, double* ms_out, long long* launches_out);
 const char* gf_kernel_name(int k);
 /* Bytes the batch moved host->device when it was created, and bytes
