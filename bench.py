@@ -53,6 +53,10 @@ def parse():
                     help="requests in the served-stream leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate of the served stream (1/s)")
     ap.add_argument("--serve-budget-gb", type=int, default=16, help="device-memory budget of the server")
+    ap.add_argument("--serve-mixed-requests", type=int, default=60,
+                    help="requests in the mixed chain/plate served leg (0 = skip)")
+    ap.add_argument("--serve-plate-max-dof", type=int, default=20000,
+                    help="largest plate (free DOFs) in the mixed served leg")
     ap.add_argument("--shell-steps", type=int, default=2,
                     help="load steps (of 20) of the 64x64x2 Shell_1 plate leg (0 = skip)")
     ap.add_argument("--dyn-steps", type=int, default=50,
@@ -330,6 +334,33 @@ def served_leg(ctx, args, rank):
             "mean_queued_ms": float(np.mean([r.queued_ms for r in res]))}
 
 
+def served_mixed_leg(ctx, args, rank):
+    """The mixed served stream: 70 % pipe chains (1k-50k DOF), 30 % Shell_1
+    plates (10k DOF up to --serve-plate-max-dof), Poisson arrivals."""
+    from giraffe_gb300 import configs, serve
+
+    seed = args.seed + 3000 + rank
+    reqs = configs.served_mixed(args.serve_mixed_requests, seed=seed,
+                                plate_dof=(10000, max(10001, args.serve_plate_max_dof)))
+    arrivals = serve.poisson_arrivals(len(reqs), args.serve_rate, seed=seed)
+    srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30)
+    out = serve.run_stream(srv, reqs, arrivals)
+    st = srv.status()
+    srv.close()
+    res = out["results"]
+    is_plate = np.array([bool(s.shells) for s in reqs])
+    lat = out["latency_ms"]
+    return {"workload": f"{len(reqs)} requests: {int((~is_plate).sum())} pipe chains 1k-50k DOF and "
+                        f"{int(is_plate.sum())} Shell_1 plates 10k-{args.serve_plate_max_dof} DOF (of the 10k-200k "
+                        f"range), 10 load steps each, Poisson arrivals at {args.serve_rate:g}/s; plates run in "
+                        f"waves of their own",
+            "p50_latency_ms": out["p50_ms"], "p99_latency_ms": out["p99_ms"],
+            "chain_p50_ms": float(np.percentile(lat[~is_plate], 50)) if (~is_plate).any() else None,
+            "plate_p50_ms": float(np.percentile(lat[is_plate], 50)) if is_plate.any() else None,
+            "solves_per_s": out["solves_per_s"], "requests_per_s": out["requests_per_s"], "wall_s": out["wall_s"],
+            "aborted": int(sum(r.stats[3] for r in res)), "gpu_launches": st["launches"]}
+
+
 def run_ours(args, rank, world):
     import ctypes as C
 
@@ -416,13 +447,16 @@ def run_ours(args, rank, world):
         t = kernels[dom]["ms"] / 1e3
         roof.update({"bound": "hbm", "achieved": asm_b.value / t / 1e9, "peak": peaks.get("hbm_gbs"),
                      "unit": "GB/s", "frac": asm_b.value / t / 1e9 / peaks.get("hbm_gbs"), "traffic": None})
-    plain = plain_leg(ctx, structs, args.plain_sample)
-    plain["batched_over_plain"] = value / plain["value"]
+    plain = None
+    if args.plain_sample > 0:
+        plain = plain_leg(ctx, structs, args.plain_sample)
+        plain["batched_over_plain"] = value / plain["value"]
     shell = shell_leg(ctx, args, fp64.value) if args.shell_steps > 0 else None
     dyn = dynamics_leg(ctx, args) if args.dyn_steps > 0 else None
     serving = None
     if args.serve_requests > 0:
         serving = served_leg(ctx, args, rank)
+    serving_mixed = served_mixed_leg(ctx, args, rank) if args.serve_mixed_requests > 0 else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(structs, args.cpu_sample, rank)
@@ -448,6 +482,7 @@ def run_ours(args, rank, world):
                 "shell_plate": shell,
                 "dynamics": dyn,
                 "serving": serving,
+                "serving_mixed": serving_mixed,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     ctx.close()

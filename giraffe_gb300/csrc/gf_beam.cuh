@@ -255,32 +255,55 @@ GF_HD void beam_gp_force(const BeamConst& c, const BeamGP& k, int g, double* f, 
   }
 }
 
-// K_e entry (row r, column s; 0..17, global frame) from the two rotated
-// Gauss-point operators M0, M1 (row-major 9x9).
+GF_HD double beam_M_entry(const BeamConst& c, const double* D0, const double* D1, int ds, double a1Mr, int r, int s);
+
+// The 6x6 block (I, J) of K_e (global frame) from the two rotated
+// Gauss-point operators, written to K (column-major 18x18, leading
+// dimension 18).  The products of the Gauss weight and shape-function values
+// and derivatives are formed once per block (cdd = w N'_I N'_J, cdn = w N'_I
+// N_J, cnd = w N_I N'_J, cnn = w N_I N_J), so each entry is a short FMA chain
+// over the operator blocks: translation rows/columns couple through N' only,
+// rotation rows/columns through N' (curvature) and N (the alpha terms).  With
+// dyn, the inertial blocks of beam_M_entry are added.
 template <typename TK>
-GF_HD TK beam_K_entry(const BeamConst& c, const TK* M0, const TK* M1, int r, int s, int ms = 1) {
-  int I = r / 6, a = r % 6, J = s / 6, b = s % 6;
-  TK acc = TK(0);
+GF_HD void beam_K_block(const BeamConst& c, const TK* M0, const TK* M1, int I, int J, int ms, double* K,
+                        bool dyn = false, const double* D0 = nullptr, const double* D1 = nullptr, int ds = 1,
+                        double a1Mr = 0.0) {
+  TK cdd[2], cdn[2], cnd[2], cnn[2];
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
-    const TK* M = g ? M1 : M0;
-    TK dNI = TK(c.dN[g][I]), NI = TK(c.N[g][I]), dNJ = TK(c.dN[g][J]), NJ = TK(c.N[g][J]);
-    TK w = TK(c.jac);
-    if (a < 3 && b < 3) {
-      acc += w * dNI * dNJ * M[(a * 9 + b) * ms];
-    } else if (a < 3) {
-      int bb = b - 3;
-      acc += w * dNI * (dNJ * M[(a * 9 + 3 + bb) * ms] + NJ * M[(a * 9 + 6 + bb) * ms]);
-    } else if (b < 3) {
-      int aa = a - 3;
-      acc += w * (dNI * M[((3 + aa) * 9 + b) * ms] + NI * M[((6 + aa) * 9 + b) * ms]) * dNJ;
-    } else {
-      int aa = a - 3, bb = b - 3;
-      acc += w * (dNI * dNJ * M[((3 + aa) * 9 + 3 + bb) * ms] + dNI * NJ * M[((3 + aa) * 9 + 6 + bb) * ms] +
-                  NI * dNJ * M[((6 + aa) * 9 + 3 + bb) * ms] + NI * NJ * M[((6 + aa) * 9 + 6 + bb) * ms]);
-    }
+    TK w = TK(c.jac), dNI = TK(c.dN[g][I]), NI = TK(c.N[g][I]), dNJ = TK(c.dN[g][J]), NJ = TK(c.N[g][J]);
+    cdd[g] = w * dNI * dNJ;
+    cdn[g] = w * dNI * NJ;
+    cnd[g] = w * NI * dNJ;
+    cnn[g] = w * NI * NJ;
   }
-  return acc;
+#pragma unroll 1
+  for (int b = 0; b < 6; ++b)
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      TK acc = TK(0);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const TK* M = g ? M1 : M0;
+        if (a < 3 && b < 3) {
+          acc += cdd[g] * M[(a * 9 + b) * ms];
+        } else if (a < 3) {
+          int bb = b - 3;
+          acc += cdd[g] * M[(a * 9 + 3 + bb) * ms] + cdn[g] * M[(a * 9 + 6 + bb) * ms];
+        } else if (b < 3) {
+          int aa = a - 3;
+          acc += cdd[g] * M[((3 + aa) * 9 + b) * ms] + cnd[g] * M[((6 + aa) * 9 + b) * ms];
+        } else {
+          int aa = a - 3, bb = b - 3;
+          acc += cdd[g] * M[((3 + aa) * 9 + 3 + bb) * ms] + cdn[g] * M[((3 + aa) * 9 + 6 + bb) * ms] +
+                 cnd[g] * M[((6 + aa) * 9 + 3 + bb) * ms] + cnn[g] * M[((6 + aa) * 9 + 6 + bb) * ms];
+        }
+      }
+      double k = double(acc);
+      if (dyn) k += beam_M_entry(c, D0, D1, ds, a1Mr, 6 * I + a, 6 * J + b);
+      K[(6 * I + a) + 18 * (6 * J + b)] = k;
+    }
 }
 
 // Inertial contribution of one Gauss point (Beam_1::MountMass, reference

@@ -306,13 +306,11 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
   }
   double* Ke = b.Ke + (int64_t)e * 324;
 #pragma unroll 1
-  for (int q2 = 0; q2 < 18; ++q2)
+  for (int J = 0; J < 3; ++J)
 #pragma unroll 1
-    for (int r = 0; r < 18; ++r) {
-      double k = double(beam_K_entry<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, r, q2, MOUNT_THREADS));
-      if (dyn) k += beam_M_entry(c, Dm, Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, r, q2);
-      Ke[r + 18 * q2] = k;
-    }
+    for (int I = 0; I < 3; ++I)
+      beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
+                       Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr);
   double* Fe = b.Fe + (int64_t)e * 18;
 #pragma unroll
   for (int q = 0; q < 18; ++q) Fe[q] = f[q * MOUNT_THREADS];
@@ -749,10 +747,9 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_elements(int n, const Be
   }
   double* K = Ks + (int64_t)e * 324;
 #pragma unroll 1
-  for (int r = 0; r < 18; ++r)
+  for (int J = 0; J < 3; ++J)
 #pragma unroll 1
-    for (int q = 0; q < 18; ++q)
-      K[r + 18 * q] = beam_K_entry<double>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, r, q, MOUNT_THREADS);
+    for (int I = 0; I < 3; ++I) beam_K_block<double>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, K);
   for (int q = 0; q < 18; ++q) fs[(int64_t)e * 18 + q] = f[q * MOUNT_THREADS];
 }
 

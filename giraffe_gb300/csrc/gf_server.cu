@@ -36,6 +36,7 @@ double now_ms() {
 
 struct Request {
   gf_model_desc model;
+  bool wide = false;  // Shell_1 structure (wide-band solver)
   double* out = nullptr;
   long long tag = 0;
   size_t bytes = 0;
@@ -81,6 +82,13 @@ struct gf_server {
 };
 
 namespace {
+
+// Slot kinds: with more than one slot, the upper half (at least one slot)
+// takes Shell_1 waves and the rest beam waves.
+bool slot_for_wide(const gf_server* S, int i) {
+  int W = S->o.max_waves;
+  return W > 1 && i >= W - W / 2;
+}
 
 StructState* state_buf(gf_server* S, int slot, int k) {
   return S->pin_state + ((size_t)slot * 2 + k) * S->o.max_wave_structs;
@@ -184,27 +192,43 @@ void retire(gf_server* S, size_t i) {
   S->waves.erase(S->waves.begin() + (long)i);
 }
 
-// Forms one wave from the head of the queue, if a slot and the budget allow.
-int admit(gf_server* S, bool* admitted) {
+// Forms one wave of one kind of structure, if a slot of that kind and the
+// budget allow.  A wave holds structures of one kind (beam structures, or
+// Shell_1 structures, whose pass is the long wide-band solve), taken in
+// arrival order while they fit the free budget.
+int admit_kind(gf_server* S, bool kind, bool* admitted) {
   gf_ctx* ctx = S->ctx;
   *admitted = false;
-  if (S->queue.empty()) return GF_OK;
+  bool any = false, wide_queued = false;
+  for (const Request& r : S->queue) {
+    any |= r.wide == kind;
+    wide_queued |= r.wide;
+  }
+  if (!any) return GF_OK;
+  // Shell_1 waves take the Shell_1 slots; beam waves take the beam slots,
+  // and the Shell_1 slots too while no Shell_1 structure waits
   int slot = -1;
-  for (int i = 0; i < S->o.max_waves; ++i)
-    if (!S->slot_busy[i]) { slot = i; break; }
+  for (int i = 0; i < S->o.max_waves && slot < 0; ++i) {
+    if (S->slot_busy[i]) continue;
+    bool ok = S->o.max_waves == 1 || (kind ? slot_for_wide(S, i) : (!slot_for_wide(S, i) || !wide_queued));
+    if (ok) slot = i;
+  }
   if (slot < 0) return GF_OK;
   size_t free_bytes = S->arena.size - S->arena.in_use;
   size_t total = kWaveSlack;
-  int take = 0;
-  while (take < (int)S->queue.size() && take < S->o.max_wave_structs &&
-         total + S->queue[take].bytes <= free_bytes) {
-    total += S->queue[take].bytes;
-    ++take;
+  std::vector<int> pick;
+  for (int i = 0; i < (int)S->queue.size() && (int)pick.size() < S->o.max_wave_structs; ++i) {
+    const Request& r = S->queue[i];
+    if (r.wide != kind) continue;
+    if (total + r.bytes > free_bytes) break;
+    total += r.bytes;
+    pick.push_back(i);
   }
+  const int take = (int)pick.size();
   if (take == 0) return GF_OK;
   Wave* w = new Wave();
   w->slot = slot;
-  w->reqs.assign(S->queue.begin(), S->queue.begin() + take);
+  for (int i : pick) w->reqs.push_back(S->queue[i]);
   w->reported.assign(take, 0);
   std::vector<gf_model_desc> models(take);
   double t = now_ms();
@@ -241,12 +265,20 @@ int admit(gf_server* S, bool* admitted) {
     return r;
   }
   w->B = B;
-  S->queue.erase(S->queue.begin(), S->queue.begin() + take);
+  for (int k = take - 1; k >= 0; --k) S->queue.erase(S->queue.begin() + pick[k]);
   S->slot_busy[slot] = 1;
   S->in_flight_structs += take;
   S->waves.push_back(w);
   *admitted = true;
   return GF_OK;
+}
+
+int admit(gf_server* S, bool* admitted) {
+  bool a = false, b = false;
+  int r = admit_kind(S, false, &a);
+  if (r == GF_OK) r = admit_kind(S, true, &b);
+  *admitted = a || b;
+  return r;
 }
 
 }  // namespace
@@ -277,7 +309,13 @@ gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts) {
   S->streams.assign(W, nullptr);
   S->slot_busy.assign(W, 0);
   S->events.assign(2 * W, nullptr);
-  for (int i = 0; ok && i < W; ++i) ok = cudaStreamCreateWithFlags(&S->streams[i], cudaStreamNonBlocking) == cudaSuccess;
+  // beam waves run on high-priority streams, Shell_1 waves (long wide-band
+  // passes) on low-priority ones, so chains keep their latency beside plates
+  int prio_low = 0, prio_high = 0;
+  if (ok) ok = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) == cudaSuccess;
+  for (int i = 0; ok && i < W; ++i)
+    ok = cudaStreamCreateWithPriority(&S->streams[i], cudaStreamNonBlocking,
+                                      slot_for_wide(S, i) ? prio_low : prio_high) == cudaSuccess;
   for (int i = 0; ok && i < 2 * W; ++i)
     ok = cudaEventCreateWithFlags(&S->events[i], cudaEventDisableTiming) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking) == cudaSuccess &&
@@ -325,6 +363,7 @@ int gf_server_submit(gf_server* S, const gf_model_desc* model, double* final_nod
   q.out = final_nodes;
   q.tag = tag;
   q.bytes = bytes;
+  q.wide = model->n_shells > 0;
   q.t_submit = now_ms();
   S->queue.push_back(q);
   return GF_OK;

@@ -176,14 +176,15 @@ struct ChainData {
   int* corner_right;   // chain element to the right (-1 if none)
   int* corner_prev;    // previous free corner of the same chain (-1 if none)
   int* corner_next;    // next free corner (-1 if none)
-  double* ez;          // [chain elem][6][13]  Z_s = A_ss^{-1}[b_s | A_sa | A_sb]
-  double* ec;          // [chain elem][6][26]  -A_as Z_s (13 cols), -A_bs Z_s (13 cols)
-  double* cD;          // [corner][36] (row-major 6x6)
-  double* cL;          // [corner][36]
-  double* cU;          // [corner][36]
-  double* cb;          // [corner][6]
-  double* cz;          // [corner][6][13]  Z = D^{-1}[b | L | U] of an eliminated corner
-  double* cx;          // [corner][6]  solution
+  // scratch below is structure-of-arrays: entry x of item i at [x * n_items + i]
+  double* ez;          // [6*13][chain elem]  Z_s = A_ss^{-1}[b_s | A_sa | A_sb]
+  double* ec;          // [6*26][chain elem]  -A_as Z_s (13 cols), -A_bs Z_s (13 cols)
+  double* cD;          // [36][corner] (row-major 6x6 per corner)
+  double* cL;          // [36][corner]
+  double* cU;          // [36][corner]
+  double* cb;          // [6][corner]
+  double* cz;          // [6*13][corner]  Z = D^{-1}[b | L | U] of an eliminated corner
+  double* cx;          // [6][corner]  solution
   CrItem* odd;         // per level: eliminated positions
   int odd_off[CR_MAX_LEVELS + 1];
   CrItem* even;        // per level: surviving positions with at least one eliminated neighbour
