@@ -12,6 +12,12 @@ namespace gf {
 namespace {
 
 constexpr int CT = 64;   // threads per block
+
+// Scratch arrays are structure-of-arrays: entry x of chain element t at
+// [x * n_chain_elems + t], entry x of corner k at [x * n_corners + k], so
+// that the threads of a warp (consecutive items) touch consecutive addresses.
+#define ELM(arr, t, x) (arr)[(int64_t)(x) * c.n_chain_elems + (t)]
+#define CRN(arr, k, x) (arr)[(int64_t)(x) * c.n_corners + (k)]
 constexpr int NC = 19;   // augmented columns: 6 (matrix) + 13 (right-hand sides)
 
 __device__ __forceinline__ bool solving(const Batch& b, int s) {
@@ -100,13 +106,11 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
     A[(i * NC + 6) * CT] = P[gm[i]];
   }
   if (!gauss_jordan6<NC>(A)) b.state[s].info_fail = 1;
-  double* ez = c.ez + (int64_t)t * 78;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
 #pragma unroll 1
-    for (int q = 0; q < 13; ++q) ez[i * 13 + q] = A[(i * NC + 6 + q) * CT];
+    for (int q = 0; q < 13; ++q) ELM(c.ez, t, i * 13 + q) = A[(i * NC + 6 + q) * CT];
   // -A_as Z and -A_bs Z (6 x 13 each)
-  double* ec = c.ec + (int64_t)t * 156;
 #pragma unroll 1
   for (int side = 0; side < 2; ++side) {
     bool free_side = side ? fb : fa;
@@ -121,7 +125,7 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
         double acc = 0.0;
 #pragma unroll
         for (int j = 0; j < 6; ++j) acc = fma(row[j], A[(j * NC + 6 + q) * CT], acc);
-        ec[i * 26 + side * 13 + q] = -acc;
+        ELM(c.ec, t, i * 26 + side * 13 + q) = -acc;
       }
     }
   }
@@ -146,25 +150,21 @@ __global__ void k_corner_system(Batch b, ChainData c) {
     gp[i] = kp >= 0 ? b.gl[(int64_t)c.corner_node[kp] * 6 + i] : -1;
     gn[i] = kn >= 0 ? b.gl[(int64_t)c.corner_node[kn] * 6 + i] : -1;
   }
-  const double* cl = eL >= 0 ? c.ec + (int64_t)eL * 156 : nullptr;
-  const double* cr = eR >= 0 ? c.ec + (int64_t)eR * 156 : nullptr;
-  double* D = c.cD + (int64_t)k * 36;
-  double* L = c.cL + (int64_t)k * 36;
-  double* U = c.cU + (int64_t)k * 36;
-  double* bb = c.cb + (int64_t)k * 6;
   for (int i = 0; i < 6; ++i) {
     for (int j = 0; j < 6; ++j) {
       double d = band_at(band, g[i], g[j]);
-      if (cl) d += cl[i * 26 + 13 + 7 + j];  // -A_bs Z_b of the left element
-      if (cr) d += cr[i * 26 + 1 + j];       // -A_as Z_a of the right element
-      D[i * 6 + j] = d;
-      U[i * 6 + j] = kn >= 0 ? band_at(band, g[i], gn[j]) + (cr ? cr[i * 26 + 7 + j] : 0.0) : 0.0;
-      L[i * 6 + j] = kp >= 0 ? band_at(band, g[i], gp[j]) + (cl ? cl[i * 26 + 13 + 1 + j] : 0.0) : 0.0;
+      if (eL >= 0) d += ELM(c.ec, eL, i * 26 + 13 + 7 + j);  // -A_bs Z_b of the left element
+      if (eR >= 0) d += ELM(c.ec, eR, i * 26 + 1 + j);       // -A_as Z_a of the right element
+      CRN(c.cD, k, i * 6 + j) = d;
+      CRN(c.cU, k, i * 6 + j) =
+          kn >= 0 ? band_at(band, g[i], gn[j]) + (eR >= 0 ? ELM(c.ec, eR, i * 26 + 7 + j) : 0.0) : 0.0;
+      CRN(c.cL, k, i * 6 + j) =
+          kp >= 0 ? band_at(band, g[i], gp[j]) + (eL >= 0 ? ELM(c.ec, eL, i * 26 + 13 + 1 + j) : 0.0) : 0.0;
     }
     double r = P[g[i]];
-    if (cl) r += cl[i * 26 + 13];
-    if (cr) r += cr[i * 26];
-    bb[i] = r;
+    if (eL >= 0) r += ELM(c.ec, eL, i * 26 + 13);
+    if (eR >= 0) r += ELM(c.ec, eR, i * 26);
+    CRN(c.cb, k, i) = r;
   }
 }
 
@@ -177,88 +177,140 @@ __global__ void __launch_bounds__(CT) k_cr_eliminate(Batch b, ChainData c, int l
   if (!solving(b, it.structure)) return;
   int k = it.corner;
   double* A = smem + threadIdx.x;
-  const double* D = c.cD + (int64_t)k * 36;
-  const double* L = c.cL + (int64_t)k * 36;
-  const double* U = c.cU + (int64_t)k * 36;
-  const double* bb = c.cb + (int64_t)k * 6;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      A[(i * NC + j) * CT] = D[i * 6 + j];
-      A[(i * NC + 7 + j) * CT] = it.prev >= 0 ? L[i * 6 + j] : 0.0;
-      A[(i * NC + 13 + j) * CT] = it.next >= 0 ? U[i * 6 + j] : 0.0;
+      A[(i * NC + j) * CT] = CRN(c.cD, k, i * 6 + j);
+      A[(i * NC + 7 + j) * CT] = it.prev >= 0 ? CRN(c.cL, k, i * 6 + j) : 0.0;
+      A[(i * NC + 13 + j) * CT] = it.next >= 0 ? CRN(c.cU, k, i * 6 + j) : 0.0;
     }
-    A[(i * NC + 6) * CT] = bb[i];
+    A[(i * NC + 6) * CT] = CRN(c.cb, k, i);
   }
   if (!gauss_jordan6<NC>(A)) b.state[it.structure].info_fail = 1;
-  double* z = c.cz + (int64_t)k * 78;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
 #pragma unroll 1
-    for (int q = 0; q < 13; ++q) z[i * 13 + q] = A[(i * NC + 6 + q) * CT];
+    for (int q = 0; q < 13; ++q) CRN(c.cz, k, i * 13 + q) = A[(i * NC + 6 + q) * CT];
+}
+
+// Warp-per-item form of k_cr_eliminate for the small levels near the top of
+// the reduction, where one item per thread would leave most of the FP64
+// units idle: lane q holds column q of the augmented 6 x 19 matrix
+// [D | b | L | U] in registers and the pivot column is broadcast by shuffle.
+// The arithmetic is the same sequence as gauss_jordan6 (same products and
+// FMAs on every entry), so both forms give the same bits.
+__global__ void k_cr_eliminate_w(Batch b, ChainData c, int lo, int hi) {
+  const int lane = threadIdx.x & 31;
+  const int t = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (t >= hi) return;
+  CrItem it = c.odd[t];
+  if (!solving(b, it.structure)) return;
+  const int k = it.corner;
+  double col[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double v = 0.0;
+    if (lane < 6) v = CRN(c.cD, k, i * 6 + lane);
+    else if (lane == 6) v = CRN(c.cb, k, i);
+    else if (lane < 13) v = it.prev >= 0 ? CRN(c.cL, k, i * 6 + lane - 7) : 0.0;
+    else if (lane < NC) v = it.next >= 0 ? CRN(c.cU, k, i * 6 + lane - 13) : 0.0;
+    col[i] = v;
+  }
+  bool ok = true;
+#pragma unroll
+  for (int kk = 0; kk < 6; ++kk) {
+    double p = __shfl_sync(0xffffffffu, col[kk], kk);
+    if (!(p != 0.0) || !isfinite(p)) ok = false;
+    double inv = recip(p);
+    double m[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) m[i] = __shfl_sync(0xffffffffu, col[i], kk);
+    if (lane > kk && lane < NC) {
+      double rk = col[kk] * inv;
+      col[kk] = rk;
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+        if (i != kk) col[i] = fma(-m[i], rk, col[i]);
+    }
+  }
+  if (!ok && lane == 0) b.state[it.structure].info_fail = 1;
+  if (lane >= 6 && lane < NC)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) CRN(c.cz, k, i * 13 + lane - 6) = col[i];
 }
 
 // ---- 3b. cyclic reduction: surviving positions absorb their neighbours ----
 // D -= U ZL(next) + L ZU(prev);  b -= U Zb(next) + L Zb(prev);
 // U <- -U ZU(next);  L <- -L ZL(prev)
+__device__ __forceinline__ void cr_update_row(const ChainData& c, const CrItem& it, int i) {
+  const int k = it.corner;
+  const int zn = it.next, zp = it.prev;
+  {
+    double u[6], l[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      u[j] = CRN(c.cU, k, i * 6 + j);
+      l[j] = CRN(c.cL, k, i * 6 + j);
+    }
+    double nb = CRN(c.cb, k, i), nD[6], nU[6], nL[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      nD[q] = CRN(c.cD, k, i * 6 + q);
+      nU[q] = 0.0;
+      nL[q] = 0.0;
+    }
+    if (zn >= 0) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        nb = fma(-u[j], CRN(c.cz, zn, j * 13), nb);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          nD[q] = fma(-u[j], CRN(c.cz, zn, j * 13 + 1 + q), nD[q]);
+          nU[q] = fma(-u[j], CRN(c.cz, zn, j * 13 + 7 + q), nU[q]);
+        }
+      }
+    }
+    if (zp >= 0) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        nb = fma(-l[j], CRN(c.cz, zp, j * 13), nb);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          nD[q] = fma(-l[j], CRN(c.cz, zp, j * 13 + 7 + q), nD[q]);
+          nL[q] = fma(-l[j], CRN(c.cz, zp, j * 13 + 1 + q), nL[q]);
+        }
+      }
+    }
+    CRN(c.cb, k, i) = nb;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      CRN(c.cD, k, i * 6 + q) = nD[q];
+      CRN(c.cU, k, i * 6 + q) = nU[q];
+      CRN(c.cL, k, i * 6 + q) = nL[q];
+    }
+  }
+}
+
 __global__ void k_cr_update(Batch b, ChainData c, int lo, int hi) {
   int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= hi) return;
   CrItem it = c.even[t];
   if (!solving(b, it.structure)) return;
-  int k = it.corner;
-  double* D = c.cD + (int64_t)k * 36;
-  double* L = c.cL + (int64_t)k * 36;
-  double* U = c.cU + (int64_t)k * 36;
-  double* bb = c.cb + (int64_t)k * 6;
-  const double* zn = it.next >= 0 ? c.cz + (int64_t)it.next * 78 : nullptr;
-  const double* zp = it.prev >= 0 ? c.cz + (int64_t)it.prev * 78 : nullptr;
 #pragma unroll 1
-  for (int i = 0; i < 6; ++i) {
-    double u[6], l[6];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      u[j] = U[i * 6 + j];
-      l[j] = L[i * 6 + j];
-    }
-    double nb = bb[i], nD[6], nU[6], nL[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      nD[q] = D[i * 6 + q];
-      nU[q] = 0.0;
-      nL[q] = 0.0;
-    }
-    if (zn) {
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        nb = fma(-u[j], zn[j * 13], nb);
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          nD[q] = fma(-u[j], zn[j * 13 + 1 + q], nD[q]);
-          nU[q] = fma(-u[j], zn[j * 13 + 7 + q], nU[q]);
-        }
-      }
-    }
-    if (zp) {
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        nb = fma(-l[j], zp[j * 13], nb);
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          nD[q] = fma(-l[j], zp[j * 13 + 7 + q], nD[q]);
-          nL[q] = fma(-l[j], zp[j * 13 + 1 + q], nL[q]);
-        }
-      }
-    }
-    bb[i] = nb;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      D[i * 6 + q] = nD[q];
-      U[i * 6 + q] = nU[q];
-      L[i * 6 + q] = nL[q];
-    }
-  }
+  for (int i = 0; i < 6; ++i) cr_update_row(c, it, i);
+}
+
+// Row-per-lane form for the small levels: six lanes per item (rows of the
+// 6x6 blocks are independent), five items per warp.
+__global__ void k_cr_update_w(Batch b, ChainData c, int lo, int hi) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= 30) return;
+  const int t = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 5 + lane / 6;
+  if (t >= hi) return;
+  CrItem it = c.even[t];
+  if (!solving(b, it.structure)) return;
+  cr_update_row(c, it, lane % 6);
 }
 
 // ---- 3c. the last position of each chain ----
@@ -270,14 +322,12 @@ __global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
   int s = c.corner_struct[k];
   if (!solving(b, s)) return;
   double* A = smem + threadIdx.x;
-  const double* D = c.cD + (int64_t)k * 36;
-  const double* bb = c.cb + (int64_t)k * 6;
   for (int i = 0; i < 6; ++i) {
-    for (int j = 0; j < 6; ++j) A[(i * NC + j) * CT] = D[i * 6 + j];
-    A[(i * NC + 6) * CT] = bb[i];
+    for (int j = 0; j < 6; ++j) A[(i * NC + j) * CT] = CRN(c.cD, k, i * 6 + j);
+    A[(i * NC + 6) * CT] = CRN(c.cb, k, i);
   }
   if (!gauss_jordan6<7>(A)) b.state[s].info_fail = 1;
-  for (int i = 0; i < 6; ++i) c.cx[(int64_t)k * 6 + i] = A[(i * NC + 6) * CT];
+  for (int i = 0; i < 6; ++i) CRN(c.cx, k, i) = A[(i * NC + 6) * CT];
 }
 
 // ---- 4. back substitution: x = Zb - ZL x_prev - ZU x_next ----
@@ -286,22 +336,22 @@ __global__ void k_cr_back(Batch b, ChainData c, int lo, int hi) {
   if (t >= hi) return;
   CrItem it = c.odd[t];
   if (!solving(b, it.structure)) return;
-  const double* z = c.cz + (int64_t)it.corner * 78;
+  const int k = it.corner;
   double xp[6], xn[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    xp[j] = it.prev >= 0 ? c.cx[(int64_t)it.prev * 6 + j] : 0.0;
-    xn[j] = it.next >= 0 ? c.cx[(int64_t)it.next * 6 + j] : 0.0;
+    xp[j] = it.prev >= 0 ? CRN(c.cx, it.prev, j) : 0.0;
+    xn[j] = it.next >= 0 ? CRN(c.cx, it.next, j) : 0.0;
   }
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    double x = z[i * 13];
+    double x = CRN(c.cz, k, i * 13);
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      x = fma(-z[i * 13 + 1 + j], xp[j], x);
-      x = fma(-z[i * 13 + 7 + j], xn[j], x);
+      x = fma(-CRN(c.cz, k, i * 13 + 1 + j), xp[j], x);
+      x = fma(-CRN(c.cz, k, i * 13 + 7 + j), xn[j], x);
     }
-    c.cx[(int64_t)it.corner * 6 + i] = x;
+    CRN(c.cx, k, i) = x;
   }
 }
 
@@ -315,21 +365,20 @@ __global__ void k_chain_scatter(Batch b, ChainData c) {
   const StructInfo inf = b.info[s];
   double* P = b.P + inf.dof_off;
   int ka = c.elem_corner_a[t], kb = c.elem_corner_b[t];
-  const double* z = c.ez + (int64_t)t * 78;
   double xa[6], xb[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    xa[j] = ka >= 0 ? c.cx[(int64_t)ka * 6 + j] : 0.0;
-    xb[j] = kb >= 0 ? c.cx[(int64_t)kb * 6 + j] : 0.0;
+    xa[j] = ka >= 0 ? CRN(c.cx, ka, j) : 0.0;
+    xb[j] = kb >= 0 ? CRN(c.cx, kb, j) : 0.0;
   }
   int nm = b.enodes[3 * e + 1];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    double x = z[i * 13];
+    double x = ELM(c.ez, t, i * 13);
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      x = fma(-z[i * 13 + 1 + j], xa[j], x);
-      x = fma(-z[i * 13 + 7 + j], xb[j], x);
+      x = fma(-ELM(c.ez, t, i * 13 + 1 + j), xa[j], x);
+      x = fma(-ELM(c.ez, t, i * 13 + 7 + j), xb[j], x);
     }
     P[b.gl[(int64_t)nm * 6 + i]] = x;
   }
@@ -344,7 +393,7 @@ __global__ void k_corner_scatter(Batch b, ChainData c) {
   double* P = b.P + inf.dof_off;
   int node = c.corner_node[k];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) P[b.gl[(int64_t)node * 6 + i]] = c.cx[(int64_t)k * 6 + i];
+  for (int i = 0; i < 6; ++i) P[b.gl[(int64_t)node * 6 + i]] = CRN(c.cx, k, i);
 }
 
 }  // namespace
@@ -362,11 +411,16 @@ void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
   k_condense<<<(c.n_chain_elems + CT - 1) / CT, CT, smem, st>>>(b, c);
   if (c.n_corners > 0) {
     k_corner_system<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);
+    // levels with fewer items than ~8 per FP64 unit take the lane-parallel
+    // forms (same results, shorter per-item instruction chains)
+    const int small = 152 * 4 * 8;
     for (int l = 0; l < c.n_levels; ++l) {
       int lo = c.odd_off[l], hi = c.odd_off[l + 1];
-      if (hi > lo) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, smem, st>>>(b, c, lo, hi);
+      if (hi - lo >= small) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, smem, st>>>(b, c, lo, hi);
+      else if (hi > lo) k_cr_eliminate_w<<<(hi - lo + 3) / 4, 128, 0, st>>>(b, c, lo, hi);
       int elo = c.even_off[l], ehi = c.even_off[l + 1];
-      if (ehi > elo) k_cr_update<<<(ehi - elo + 127) / 128, 128, 0, st>>>(b, c, elo, ehi);
+      if (ehi - elo >= small) k_cr_update<<<(ehi - elo + 127) / 128, 128, 0, st>>>(b, c, elo, ehi);
+      else if (ehi > elo) k_cr_update_w<<<(ehi - elo + 19) / 20, 128, 0, st>>>(b, c, elo, ehi);
     }
     k_cr_root<<<(c.n_roots + CT - 1) / CT, CT, smem, st>>>(b, c);
     for (int l = c.n_levels - 1; l >= 0; --l) {
