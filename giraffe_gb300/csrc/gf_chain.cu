@@ -292,17 +292,8 @@ __device__ __forceinline__ void cr_update_row(const ChainData& c, const CrItem& 
   }
 }
 
-__global__ void k_cr_update(Batch b, ChainData c, int lo, int hi) {
-  int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= hi) return;
-  CrItem it = c.even[t];
-  if (!solving(b, it.structure)) return;
-#pragma unroll 1
-  for (int i = 0; i < 6; ++i) cr_update_row(c, it, i);
-}
-
-// Row-per-lane form for the small levels: six lanes per item (rows of the
-// 6x6 blocks are independent), five items per warp.
+// Row per lane: six lanes per item (rows of the 6x6 blocks are
+// independent), five items per warp.
 __global__ void k_cr_update_w(Batch b, ChainData c, int lo, int hi) {
   const int lane = threadIdx.x & 31;
   if (lane >= 30) return;
@@ -331,28 +322,24 @@ __global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
 }
 
 // ---- 4. back substitution: x = Zb - ZL x_prev - ZU x_next ----
+// Row per lane: six lanes per item, five items per warp.
 __global__ void k_cr_back(Batch b, ChainData c, int lo, int hi) {
-  int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (lane >= 30) return;
+  const int t = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 5 + lane / 6;
   if (t >= hi) return;
   CrItem it = c.odd[t];
   if (!solving(b, it.structure)) return;
-  const int k = it.corner;
-  double xp[6], xn[6];
+  const int k = it.corner, i = lane % 6;
+  double x = CRN(c.cz, k, i * 13);
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    xp[j] = it.prev >= 0 ? CRN(c.cx, it.prev, j) : 0.0;
-    xn[j] = it.next >= 0 ? CRN(c.cx, it.next, j) : 0.0;
+    double xp = it.prev >= 0 ? CRN(c.cx, it.prev, j) : 0.0;
+    double xn = it.next >= 0 ? CRN(c.cx, it.next, j) : 0.0;
+    x = fma(-CRN(c.cz, k, i * 13 + 1 + j), xp, x);
+    x = fma(-CRN(c.cz, k, i * 13 + 7 + j), xn, x);
   }
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    double x = CRN(c.cz, k, i * 13);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      x = fma(-CRN(c.cz, k, i * 13 + 1 + j), xp[j], x);
-      x = fma(-CRN(c.cz, k, i * 13 + 7 + j), xn[j], x);
-    }
-    CRN(c.cx, k, i) = x;
-  }
+  CRN(c.cx, k, i) = x;
 }
 
 // ---- 4b. midside nodes, and the solution into P ----
@@ -418,14 +405,15 @@ void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
       int lo = c.odd_off[l], hi = c.odd_off[l + 1];
       if (hi - lo >= small) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, smem, st>>>(b, c, lo, hi);
       else if (hi > lo) k_cr_eliminate_w<<<(hi - lo + 3) / 4, 128, 0, st>>>(b, c, lo, hi);
+      // the update runs row-per-lane at every level: the same FP64
+      // instruction count as one item per thread, six times the warps
       int elo = c.even_off[l], ehi = c.even_off[l + 1];
-      if (ehi - elo >= small) k_cr_update<<<(ehi - elo + 127) / 128, 128, 0, st>>>(b, c, elo, ehi);
-      else if (ehi > elo) k_cr_update_w<<<(ehi - elo + 19) / 20, 128, 0, st>>>(b, c, elo, ehi);
+      if (ehi > elo) k_cr_update_w<<<(ehi - elo + 19) / 20, 128, 0, st>>>(b, c, elo, ehi);
     }
     k_cr_root<<<(c.n_roots + CT - 1) / CT, CT, smem, st>>>(b, c);
     for (int l = c.n_levels - 1; l >= 0; --l) {
       int lo = c.odd_off[l], hi = c.odd_off[l + 1];
-      if (hi > lo) k_cr_back<<<(hi - lo + 127) / 128, 128, 0, st>>>(b, c, lo, hi);
+      if (hi > lo) k_cr_back<<<(hi - lo + 19) / 20, 128, 0, st>>>(b, c, lo, hi);
     }
     k_corner_scatter<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);
   }
