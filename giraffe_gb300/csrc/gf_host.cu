@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -649,6 +650,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     p.divergence_ref = cr.divergence_ref;
     params.push_back(p);
     B->info.push_back(inf);
+    B->shell_off.push_back(shell_off);
     node_off += nn;
     elem_off += m.n_beams;
     shell_off += m.n_shells;
@@ -789,6 +791,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     return GF_ERR_CUDA;
   b.xref = B->copy0;
   if (B->count_only) return GF_OK;
+  B->h_gl = gl;
+  B->h_enodes = enodes;
+  B->h_snodes = snodes;
   CK(cudaMemsetAsync(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB, B->stream));
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
@@ -1140,14 +1145,17 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
   return GF_OK;
 }
 
-int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
-  if (!B || s < 0 || s >= B->b.n_struct) return GF_ERR_ARG;
+}  // extern "C"
+
+namespace {
+// The first Newton pass of structure s from its initial configuration, read
+// back: K_AA in the solver's band layout (leading dimension W, half
+// bandwidth kw) and P_A, both in the solver's numbering.
+int first_pass_band(gf_batch* B, int s, std::vector<double>& band, std::vector<double>& P, int64_t& W,
+                    int64_t& kw) {
   gf_ctx* ctx = B->ctx;
   const Batch& b = B->b;
   const StructInfo& inf = B->info[s];
-  int kb = B->kb[s];
-  if (dims) { dims[0] = inf.n_free; dims[1] = kb; }
-  if (!ab && !PA) return GF_OK;
   int r = batch_reset(B);
   if (r != GF_OK) return r;
   // one partial pass: step start, zero, mount, loads, residual
@@ -1155,17 +1163,35 @@ int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
   launch_iteration_partial(bb, B->stream);
   CK(cudaGetLastError());
   const int nf = inf.n_free;
-  const int64_t W = inf.wide ? 2 * (int64_t)inf.wkl + 1 : GF_LDB;
-  std::vector<double> band((size_t)nf * W), P(nf);
+  W = inf.wide ? 2 * (int64_t)inf.wkl + 1 : GF_LDB;
+  kw = inf.wide ? inf.wkl : GF_KB;
+  band.assign((size_t)nf * W, 0.0);
+  P.assign(nf, 0.0);
   const double* src = inf.wide ? b.sh.wband + inf.wb_off : b.band + inf.band_off;
   CK(cudaMemcpyAsync(band.data(), src, sizeof(double) * band.size(), cudaMemcpyDeviceToHost, B->stream));
   CK(cudaMemcpyAsync(P.data(), b.P + inf.dof_off, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, B->stream));
   CK(cudaStreamSynchronize(B->stream));
+  return batch_reset(B) == GF_OK ? GF_OK : GF_ERR_CUDA;
+}
+}  // namespace
+
+extern "C" {
+
+int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
+  if (!B || s < 0 || s >= B->b.n_struct) return GF_ERR_ARG;
+  const StructInfo& inf = B->info[s];
+  int kb = B->kb[s];
+  if (dims) { dims[0] = inf.n_free; dims[1] = kb; }
+  if (!ab && !PA) return GF_OK;
+  std::vector<double> band, P;
+  int64_t W = 0, kw = 0;
+  int r = first_pass_band(B, s, band, P, W, kw);
+  if (r != GF_OK) return r;
+  const int nf = inf.n_free;
   // the reference's numbering: identity, or back from the solver's
   // reverse Cuthill-McKee numbering for wide structures
   const std::vector<int>& perm = B->perm[s];
   auto pm = [&](int i) { return perm.empty() ? i : perm[i]; };
-  const int64_t kw = inf.wide ? inf.wkl : GF_KB;
   int ldab = 3 * kb + 1;
   if (ab) {
     std::memset(ab, 0, sizeof(double) * (size_t)ldab * nf);
@@ -1178,7 +1204,75 @@ int gf_batch_assemble(gf_batch* B, int s, double* ab, double* PA, int* dims) {
   }
   if (PA)
     for (int i = 0; i < nf; ++i) PA[i] = P[pm(i)];
-  return batch_reset(B) == GF_OK ? GF_OK : GF_ERR_CUDA;
+  return GF_OK;
+}
+
+int gf_batch_assemble_csr(gf_batch* B, int s, int* row_ptr, int* col_idx, double* val, double* PA, int* dims) {
+  if (!B || s < 0 || s >= B->b.n_struct) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  if (B->h_gl.empty()) {
+    set_err(ctx, "gf_batch_assemble_csr: the batch keeps no host numbering");
+    return GF_ERR_ARG;
+  }
+  const StructInfo& inf = B->info[s];
+  const int nf = inf.n_free;
+  const std::vector<int>& perm = B->perm[s];
+  std::vector<int> inv(nf);  // solver index -> the reference's index
+  for (int i = 0; i < nf; ++i) inv[perm.empty() ? i : perm[i]] = i;
+  // pattern: the union of the element patterns over free DOF pairs
+  // (SparseMatrix::setValue of every element entry, summed by setFromTriplets)
+  std::vector<std::vector<int>> rows(nf);
+  auto add_elem = [&](const int* dofs, int nd) {
+    for (int a = 0; a < nd; ++a) {
+      if (dofs[a] < 0) continue;
+      for (int c = 0; c < nd; ++c)
+        if (dofs[c] >= 0) rows[inv[dofs[a]]].push_back(inv[dofs[c]]);
+    }
+  };
+  for (int e = inf.elem_off; e < inf.elem_off + inf.n_elem; ++e) {
+    int d[18];
+    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_enodes[3 * e + a / 6] * 6 + a % 6];
+    add_elem(d, 18);
+  }
+  int s_lo = B->shell_off[s];
+  int s_hi = s + 1 < (int)B->shell_off.size() ? B->shell_off[s + 1] : B->b.sh.n_shells;
+  for (int e = s_lo; e < s_hi; ++e) {
+    int d[27];
+    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_snodes[6 * e + a / 3] * 6 + a % 3];
+    for (int a = 0; a < 9; ++a) d[18 + a] = B->h_gl[(size_t)B->h_snodes[6 * e + 3 + a / 3] * 6 + 3 + a % 3];
+    add_elem(d, 27);
+  }
+  int64_t nnz = 0;
+  for (auto& r : rows) {
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    nnz += (int64_t)r.size();
+  }
+  if (nnz > INT32_MAX) {
+    set_err(ctx, "gf_batch_assemble_csr: %lld nonzeros exceed 32-bit CSR indices", (long long)nnz);
+    return GF_ERR_ARG;
+  }
+  if (dims) { dims[0] = nf; dims[1] = (int)nnz; }
+  if (!row_ptr && !col_idx && !val && !PA) return GF_OK;
+  std::vector<double> band, P;
+  int64_t W = 0, kw = 0;
+  int r = first_pass_band(B, s, band, P, W, kw);
+  if (r != GF_OK) return r;
+  int64_t q = 0;
+  for (int i = 0; i < nf; ++i) {
+    if (row_ptr) row_ptr[i] = (int)q;
+    int64_t pi = perm.empty() ? i : perm[i];
+    for (int j : rows[i]) {
+      int64_t pj = perm.empty() ? j : perm[j];
+      if (col_idx) col_idx[q] = j;
+      if (val) val[q] = std::llabs(pi - pj) <= kw ? band[(size_t)(kw + pi - pj) + (size_t)pj * W] : 0.0;
+      ++q;
+    }
+  }
+  if (row_ptr) row_ptr[nf] = (int)q;
+  if (PA)
+    for (int i = 0; i < nf; ++i) PA[i] = P[perm.empty() ? i : perm[i]];
+  return GF_OK;
 }
 
 int gf_solve(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts, double* const* final_nodes,

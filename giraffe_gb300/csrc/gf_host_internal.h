@@ -96,6 +96,11 @@ struct gf_batch {
   // wide (Shell_1) structures: the reference's free-DOF index -> the
   // solver's (reverse Cuthill-McKee) index; empty for the others
   std::vector<std::vector<int>> perm;
+  // host copies for the CSR view of K_AA (gf_batch_assemble_csr): free index
+  // (solver numbering) of every node DOF, element nodes, per-structure shell
+  // offsets
+  std::vector<int> h_gl, h_enodes, h_snodes;
+  std::vector<int> shell_off;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;

@@ -23,7 +23,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_kernel_name", "gf_batch_bytes", "gf_batch_work", "gf_device_fp_peaks",
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
-           "gf_server_poll", "gf_server_get_status", "gf_shell_elements"]
+           "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr"]
 
 
 class gf_solve_opts(C.Structure):
@@ -87,6 +87,7 @@ def lib():
         L.gf_band_solve_noalloc.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
         L.gf_beam_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
                                                C.c_double, C.c_double, dp, dp]
+        L.gf_batch_assemble_csr.argtypes = [vp, C.c_int, ip, ip, dp, dp, ip]
         L.gf_shell_elements.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int, dp, dp, dp, C.c_int, dp, dp]
         L.gf_batch_device_bytes.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(C.c_size_t)]
         L.gf_server_default_opts.argtypes = [C.POINTER(gf_server_opts)]
@@ -254,6 +255,21 @@ class BatchSolver:
         P = np.zeros(n)
         self.ctx.check(self.ctx.L.gf_batch_assemble(self.h, s, _dp(ab), _dp(P), dims), "gf_batch_assemble")
         return ab, P, kb
+
+    def assemble_csr(self, s: int):
+        """First-pass K_AA of structure s in CSR (row_ptr, col_idx, val) and P_A."""
+        L = self.ctx.L
+        dims = (C.c_int * 2)()
+        self.ctx.check(L.gf_batch_assemble_csr(self.h, s, None, None, None, None, dims), "gf_batch_assemble_csr")
+        n, nnz = dims[0], dims[1]
+        rp = np.zeros(n + 1, dtype=np.int32)
+        ci = np.zeros(nnz, dtype=np.int32)
+        v = np.zeros(nnz)
+        P = np.zeros(n)
+        ip = C.POINTER(C.c_int)
+        self.ctx.check(L.gf_batch_assemble_csr(self.h, s, rp.ctypes.data_as(ip), ci.ctypes.data_as(ip), _dp(v),
+                                               _dp(P), dims), "gf_batch_assemble_csr")
+        return rp, ci, v, P
 
 
 def solve(structures, precision=GF_PREC_FP64, device=0):

@@ -29,6 +29,8 @@
  *                           SparseMatrix::Mount into the BandMatrix layout
  *                           (src/Solution.cpp:227-349, src/SparseMatrix.cpp:58-71,
  *                           src/BandMatrix.cpp:221-250)
+ *   gf_batch_assemble_csr   the same into the SparseMatrix CSR layout
+ *                           (src/SparseMatrix.cpp:58-71)
  *   gf_band_solve           bandsystem (src/BandMatrix.cpp:257-287) and the
  *                           Newton solve sparsesystem (src/SparseMatrix.cpp:74-166)
  *                           for banded K_AA
@@ -104,6 +106,13 @@ long long gf_batch_last_launches(const gf_batch* batch);
  * the structure's half-bandwidth, n_free columns) and P_A after the sign
  * flip.  dims (optional) receives n_free and kb. */
 int gf_batch_assemble(gf_batch* batch, int s, double* ab, double* PA, int* dims);
+/* The same first-pass K_AA in the reference's SparseMatrix layout
+ * (src/SparseMatrix.cpp:58-71: Eigen RowMajor CSR, 0-based, the union of
+ * every element's free-DOF pattern with duplicates summed, zeros kept):
+ * row_ptr (n_free + 1), col_idx and val (nnz), P_A (n_free), all in the
+ * reference's DOF numbering.  dims receives n_free and nnz; call with NULL
+ * arrays first to size them. */
+int gf_batch_assemble_csr(gf_batch* batch, int s, int* row_ptr, int* col_idx, double* val, double* PA, int* dims);
 
 /* Runs `steps` complete solves of the batch (each: reset to the initial
  * configuration, then run to the end) back to back and returns their total

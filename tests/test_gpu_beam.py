@@ -177,3 +177,62 @@ def test_repeat_runs_are_bitwise_identical(gpu_ctx):
     b.close()
     for x, y in zip(r1, r2):
         assert np.array_equal(x, y)
+
+
+def _element_pattern(s):
+    """Union of the element free-DOF patterns in the reference's numbering."""
+    nn = s.n_nodes
+    act = np.zeros((nn, 6), bool)
+    for b in s.beams:
+        act[list(b[:3])] = True
+    for sh in s.shells:
+        act[list(sh[:3]), :3] = True
+        act[list(sh[3:6])] = True
+    cons = s.constraints if s.constraints is not None else np.zeros((nn, 6), int)
+    g = -np.ones((nn, 6), int)
+    q = 0
+    for i in range(nn):
+        for k in range(6):
+            if act[i, k] and cons[i, k] == 0:
+                g[i, k] = q
+                q += 1
+    pat = set()
+    elems = [np.concatenate([g[list(b[:3])].ravel()]) for b in s.beams]
+    elems += [np.concatenate([g[list(sh[:6]), :3].ravel(), g[list(sh[3:6]), 3:].ravel()]) for sh in s.shells]
+    for d in elems:
+        d = d[d >= 0]
+        for a in d:
+            for c in d:
+                pat.add((int(a), int(c)))
+    return q, pat
+
+
+def test_assembly_csr_matches_oracle(gpu_ctx):
+    """gf_batch_assemble_csr: the reference's SparseMatrix layout (row-major
+    CSR, 0-based, union of element patterns, zeros kept) with the values of
+    the oracle's first tangent (1e-13)."""
+    from giraffe_gb300 import gpu
+
+    structs = [configs.tutorial01(), configs.pipe_chain(25, 0.35, 0.025, [1e5, 2e4, -3e4]),
+               configs.square_plate(3, steps=10)]
+    b = gpu.BatchSolver(gpu_ctx, structs)
+    for s_i, st in enumerate(structs):
+        rp, ci, v, P = b.assemble_csr(s_i)
+        ab_o, P_o, kl = oracle.first_tangent(st)
+        n, pat = _element_pattern(st)
+        assert len(rp) == n + 1 and rp[-1] == len(pat)
+        got = {(i, int(ci[q])) for i in range(n) for q in range(rp[i], rp[i + 1])}
+        assert got == pat
+        for i in range(n):
+            assert np.all(np.diff(ci[rp[i]:rp[i + 1]]) > 0)
+        dense = np.zeros((n, n))
+        for i in range(n):
+            dense[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        ref = np.zeros((n, n))
+        ldab = 3 * kl + 1
+        for j in range(n):
+            for i in range(max(0, j - kl), min(n, j + kl + 1)):
+                ref[i, j] = ab_o[j, 2 * kl + i - j]
+        assert rel(dense, ref) < 1e-13
+        assert rel(P, P_o) < 1e-13
+    b.close()
