@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "gf_beam.cuh"
+#include "gf_df64.cuh"
 #include "gf_chain.cuh"
 #include "gf_kernels.cuh"
 
@@ -828,6 +829,7 @@ void launch_iteration_partial(const Batch& b, cudaStream_t st) {
 static void set_attrs() {
   if (!g_attr_set) {
     cudaFuncSetAttribute(k_beam_tangent<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
+    cudaFuncSetAttribute(k_beam_tangent<f2>, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
     cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (RING * GF_LDB + RING) * (int)sizeof(double));
     g_attr_set = true;
@@ -846,7 +848,12 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   if (b.n_elem == 0) return;
   {
     ProfScope q(prof, st, KC_MOUNT);
-    k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+    // mixed precision: the tangent operator in FP32-pair arithmetic on the
+    // FP32 pipe; kinematics, internal force and everything after stay FP64
+    if (b.mixed)
+      k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+    else
+      k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
   }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];
