@@ -25,10 +25,6 @@ __device__ __forceinline__ bool solving(const Batch& b, int s) {
   return st.phase == PH_ITER && st.need_solve;
 }
 
-__device__ __forceinline__ double band_at(const double* band, int r, int c) {
-  return band[(GF_KB + r - c) + (int64_t)c * GF_LDB];
-}
-
 // Newton-Raphson reciprocal seeded by the FP32 hardware approximation (two
 // steps r <- r + r (1 - p r)); exact division outside the FP32 range.
 __device__ __forceinline__ double recip(double p) {
@@ -83,25 +79,28 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   int s = b.estruct[e];
   if (!solving(b, s)) return;
   const StructInfo inf = b.info[s];
-  const double* band = b.band + inf.band_off;
   const double* P = b.P + inf.dof_off;
   double* A = smem + threadIdx.x;
-  int nm = b.enodes[3 * e + 1], na = b.enodes[3 * e], nb = b.enodes[3 * e + 2];
+  // K of the chain comes from the element tangents (column-major 18x18,
+  // DOFs of the first corner, the midside node, the last corner) plus the
+  // nodal load stiffness of the midside node: the midside rows belong to
+  // this element alone
+  const double* K = b.Ke + (int64_t)e * 324;
+  const double* nk = b.nodeK + (int64_t)b.enodes[3 * e + 1] * 9;
+  int nm = b.enodes[3 * e + 1];
   bool fa = c.elem_corner_a[t] >= 0, fb = c.elem_corner_b[t] >= 0;
-  int gm[6], ga[6], gb[6];
+  int gm[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    gm[i] = b.gl[(int64_t)nm * 6 + i];
-    ga[i] = b.gl[(int64_t)na * 6 + i];
-    gb[i] = b.gl[(int64_t)nb * 6 + i];
-  }
+  for (int i = 0; i < 6; ++i) gm[i] = b.gl[(int64_t)nm * 6 + i];
 #pragma unroll 1
   for (int i = 0; i < 6; ++i) {
 #pragma unroll 1
     for (int j = 0; j < 6; ++j) {
-      A[(i * NC + j) * CT] = band_at(band, gm[i], gm[j]);
-      A[(i * NC + 7 + j) * CT] = fa ? band_at(band, gm[i], ga[j]) : 0.0;
-      A[(i * NC + 13 + j) * CT] = fb ? band_at(band, gm[i], gb[j]) : 0.0;
+      double kmm = K[(6 + i) + 18 * (6 + j)];
+      if (i >= 3 && j >= 3) kmm += nk[(i - 3) * 3 + j - 3];
+      A[(i * NC + j) * CT] = kmm;
+      A[(i * NC + 7 + j) * CT] = fa ? K[(6 + i) + 18 * j] : 0.0;
+      A[(i * NC + 13 + j) * CT] = fb ? K[(6 + i) + 18 * (12 + j)] : 0.0;
     }
     A[(i * NC + 6) * CT] = P[gm[i]];
   }
@@ -114,12 +113,12 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
 #pragma unroll 1
   for (int side = 0; side < 2; ++side) {
     bool free_side = side ? fb : fa;
-    const int* gx = side ? gb : ga;
+    const int r0 = side ? 12 : 0;
 #pragma unroll 1
     for (int i = 0; i < 6; ++i) {
       double row[6];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) row[j] = free_side ? band_at(band, gx[i], gm[j]) : 0.0;
+      for (int j = 0; j < 6; ++j) row[j] = free_side ? K[(r0 + i) + 18 * (6 + j)] : 0.0;
 #pragma unroll 1
       for (int q = 0; q < 13; ++q) {
         double acc = 0.0;
@@ -138,28 +137,32 @@ __global__ void k_corner_system(Batch b, ChainData c) {
   int s = c.corner_struct[k];
   if (!solving(b, s)) return;
   const StructInfo inf = b.info[s];
-  const double* band = b.band + inf.band_off;
   const double* P = b.P + inf.dof_off;
   int node = c.corner_node[k];
   int eL = c.corner_left[k], eR = c.corner_right[k];
   int kp = c.corner_prev[k], kn = c.corner_next[k];
-  int g[6], gp[6], gn[6];
+  int g[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    g[i] = b.gl[(int64_t)node * 6 + i];
-    gp[i] = kp >= 0 ? b.gl[(int64_t)c.corner_node[kp] * 6 + i] : -1;
-    gn[i] = kn >= 0 ? b.gl[(int64_t)c.corner_node[kn] * 6 + i] : -1;
-  }
+  for (int i = 0; i < 6; ++i) g[i] = b.gl[(int64_t)node * 6 + i];
+  // K blocks from the element tangents: the corner is the last node of the
+  // element on its left and the first of the one on its right (two terms,
+  // so the sum does not depend on their order), then the nodal load
+  // stiffness, as the band held them
+  const double* KL = eL >= 0 ? b.Ke + (int64_t)c.elem_list[eL] * 324 : nullptr;
+  const double* KR = eR >= 0 ? b.Ke + (int64_t)c.elem_list[eR] * 324 : nullptr;
+  const double* nk = b.nodeK + (int64_t)node * 9;
   for (int i = 0; i < 6; ++i) {
     for (int j = 0; j < 6; ++j) {
-      double d = band_at(band, g[i], g[j]);
+      double kl = KL ? KL[(12 + i) + 18 * (12 + j)] : 0.0;
+      double kr = KR ? KR[i + 18 * j] : 0.0;
+      double d = kl + kr;
+      if (i >= 3 && j >= 3) d += nk[(i - 3) * 3 + j - 3];
       if (eL >= 0) d += ELM(c.ec, eL, i * 26 + 13 + 7 + j);  // -A_bs Z_b of the left element
       if (eR >= 0) d += ELM(c.ec, eR, i * 26 + 1 + j);       // -A_as Z_a of the right element
       CRN(c.cD, k, i * 6 + j) = d;
-      CRN(c.cU, k, i * 6 + j) =
-          kn >= 0 ? band_at(band, g[i], gn[j]) + (eR >= 0 ? ELM(c.ec, eR, i * 26 + 7 + j) : 0.0) : 0.0;
+      CRN(c.cU, k, i * 6 + j) = kn >= 0 ? KR[i + 18 * (12 + j)] + (eR >= 0 ? ELM(c.ec, eR, i * 26 + 7 + j) : 0.0) : 0.0;
       CRN(c.cL, k, i * 6 + j) =
-          kp >= 0 ? band_at(band, g[i], gp[j]) + (eL >= 0 ? ELM(c.ec, eL, i * 26 + 13 + 1 + j) : 0.0) : 0.0;
+          kp >= 0 ? KL[(12 + i) + 18 * j] + (eL >= 0 ? ELM(c.ec, eL, i * 26 + 13 + 1 + j) : 0.0) : 0.0;
     }
     double r = P[g[i]];
     if (eL >= 0) r += ELM(c.ec, eL, i * 26 + 13);

@@ -787,8 +787,10 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   if (!balloc(B, &b.P, (size_t)dof_off) || !balloc(B, &b.y, (size_t)dof_off) ||
       !balloc(B, &b.band, (size_t)dof_off * GF_LDB) || !balloc(B, &b.U, (size_t)dof_off * GF_UW) ||
       !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
-      !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18))
+      !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18) ||
+      !balloc(B, &b.nodeK, (size_t)std::max(node_off, 1) * 9))
     return GF_ERR_CUDA;
+  b.full_band = 0;
   b.xref = B->copy0;
   if (B->count_only) return GF_OK;
   B->h_gl = gl;
@@ -796,6 +798,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   B->h_snodes = snodes;
   CK(cudaMemsetAsync(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB, B->stream));
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
+  CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
   b.max_refine = B->opts.max_refine;
   return GF_OK;

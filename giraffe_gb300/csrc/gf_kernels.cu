@@ -226,7 +226,13 @@ __global__ void k_zero(Batch b) {
   int s = blockIdx.y;
   if (!iterating(b.state[s])) return;
   const StructInfo inf = b.info[s];
-  int64_t nb = inf.wide ? 0 : (int64_t)inf.n_free * GF_LDB;  // wide structures: k_wb_zero
+  // wide structures: k_wb_zero; chain structures keep no band (nodeK instead)
+  const bool chain_only = inf.is_chain && !b.full_band;
+  int64_t nb = (inf.wide || chain_only) ? 0 : (int64_t)inf.n_free * GF_LDB;
+  if (inf.is_chain) {
+    double* nk = b.nodeK + (int64_t)inf.node_off * 9;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < inf.n_nodes * 9; i += gridDim.x * blockDim.x) nk[i] = 0.0;
+  }
   double* band = b.band + inf.band_off;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
     band[i] = 0.0;
@@ -328,6 +334,11 @@ __global__ void k_beam_scatter(Batch b, int color) {
   const StructInfo inf = b.info[s];
   int myg = -1;
   if (lane < 18) myg = b.gl[(int64_t)b.enodes[3 * e + lane / 6] * 6 + lane % 6];
+  if (inf.is_chain && !b.full_band) {
+    // the chain solver reads K_e directly; only the residual is assembled
+    if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)e * 18 + lane];
+    return;
+  }
   const double* Ke = b.Ke + (int64_t)e * 324;
   double* band = b.band + inf.band_off;
   // uniform trip count: every lane takes part in every shuffle
@@ -352,6 +363,7 @@ __global__ void k_loads(Batch b) {
   double time = st.last_converged_time + st.current_time_step;
   double* P = b.P + inf.dof_off;
   double* band = b.band + inf.band_off;
+  const bool to_nodeK = inf.is_chain && !b.full_band;
   for (int l = inf.load_off; l < inf.load_off + inf.n_loads; ++l) {
     const LoadEntry L = b.loads[l];
     int node = L.node;
@@ -378,7 +390,10 @@ __global__ void k_loads(Batch b) {
       if (gi >= 0) P[gi] += -1.0 * mm[i];
       for (int j = 0; j < 3; ++j) {
         int gj = gl[3 + j];
-        if (gi >= 0 && gj >= 0) band[(GF_KB + gi - gj) + (int64_t)gj * GF_LDB] += -1.0 * V[i * 3 + j];
+        if (gi < 0 || gj < 0) continue;
+        if (to_nodeK) b.nodeK[(int64_t)node * 9 + i * 3 + j] += -1.0 * V[i * 3 + j];
+        else if (inf.wide) b.sh.wband[inf.wb_off + (inf.wkl + gi - gj) + (int64_t)gj * (2 * inf.wkl + 1)] += -1.0 * V[i * 3 + j];
+        else band[(GF_KB + gi - gj) + (int64_t)gj * GF_LDB] += -1.0 * V[i * 3 + j];
       }
     }
   }
@@ -814,8 +829,10 @@ static void set_attrs();
 
 static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof);
 
-void launch_iteration_partial(const Batch& b, cudaStream_t st) {
+void launch_iteration_partial(const Batch& b_in, cudaStream_t st) {
   set_attrs();
+  Batch b = b_in;
+  b.full_band = 1;  // the assembly view: every structure's band is filled
   int ns = b.n_struct;
   k_step_begin<<<ns, 256, 0, st>>>(b);
   k_zero<<<dim3(8, ns), 256, 0, st>>>(b);

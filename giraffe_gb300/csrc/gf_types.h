@@ -266,7 +266,14 @@ struct Batch {
   DispEntry* disps;
   TableDev* tables;
   double* table_data;
-  int mixed;  // 1: FP32 factor with FP64 refinement
+  // chain structures: the nodal load stiffness (rotation block, row-major
+  // 3x3 per node); their solver reads K from the element tangents and this,
+  // so their band is neither cleared nor filled -- unless full_band (the
+  // assembly view of gf_batch_assemble), which fills the band for every
+  // structure
+  double* nodeK;
+  int full_band;
+  int mixed;  // 1: Beam_1 tangent operator in FP32-pair arithmetic
   int max_refine;
   int* running;  // structures still running after the last pass
   ChainData chain;
