@@ -85,7 +85,9 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   // DOFs of the first corner, the midside node, the last corner) plus the
   // nodal load stiffness of the midside node: the midside rows belong to
   // this element alone
-  const double* K = b.Ke + (int64_t)e * 324;
+  const double* Kb = b.Ke + e;  // structure-of-arrays: entry x at Kb[x * n_elem]
+  const int64_t ne = b.n_elem;
+#define K(x) Kb[(int64_t)(x) * ne]
   const double* nk = b.nodeK + (int64_t)b.enodes[3 * e + 1] * 9;
   int nm = b.enodes[3 * e + 1];
   bool fa = c.elem_corner_a[t] >= 0, fb = c.elem_corner_b[t] >= 0;
@@ -96,11 +98,11 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   for (int i = 0; i < 6; ++i) {
 #pragma unroll 1
     for (int j = 0; j < 6; ++j) {
-      double kmm = K[(6 + i) + 18 * (6 + j)];
+      double kmm = K((6 + i) + 18 * (6 + j));
       if (i >= 3 && j >= 3) kmm += nk[(i - 3) * 3 + j - 3];
       A[(i * NC + j) * CT] = kmm;
-      A[(i * NC + 7 + j) * CT] = fa ? K[(6 + i) + 18 * j] : 0.0;
-      A[(i * NC + 13 + j) * CT] = fb ? K[(6 + i) + 18 * (12 + j)] : 0.0;
+      A[(i * NC + 7 + j) * CT] = fa ? K((6 + i) + 18 * j) : 0.0;
+      A[(i * NC + 13 + j) * CT] = fb ? K((6 + i) + 18 * (12 + j)) : 0.0;
     }
     A[(i * NC + 6) * CT] = P[gm[i]];
   }
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
     for (int i = 0; i < 6; ++i) {
       double row[6];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) row[j] = free_side ? K[(r0 + i) + 18 * (6 + j)] : 0.0;
+      for (int j = 0; j < 6; ++j) row[j] = free_side ? K((r0 + i) + 18 * (6 + j)) : 0.0;
 #pragma unroll 1
       for (int q = 0; q < 13; ++q) {
         double acc = 0.0;
@@ -129,6 +131,8 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
     }
   }
 }
+
+#undef K
 
 // ---- 2. corner system ----
 __global__ void k_corner_system(Batch b, ChainData c) {
@@ -148,21 +152,23 @@ __global__ void k_corner_system(Batch b, ChainData c) {
   // element on its left and the first of the one on its right (two terms,
   // so the sum does not depend on their order), then the nodal load
   // stiffness, as the band held them
-  const double* KL = eL >= 0 ? b.Ke + (int64_t)c.elem_list[eL] * 324 : nullptr;
-  const double* KR = eR >= 0 ? b.Ke + (int64_t)c.elem_list[eR] * 324 : nullptr;
+  const int64_t ne = b.n_elem;  // element scratch: entry x of element e at [x * n_elem + e]
+  const double* KL = eL >= 0 ? b.Ke + c.elem_list[eL] : nullptr;
+  const double* KR = eR >= 0 ? b.Ke + c.elem_list[eR] : nullptr;
   const double* nk = b.nodeK + (int64_t)node * 9;
   for (int i = 0; i < 6; ++i) {
     for (int j = 0; j < 6; ++j) {
-      double kl = KL ? KL[(12 + i) + 18 * (12 + j)] : 0.0;
-      double kr = KR ? KR[i + 18 * j] : 0.0;
+      double kl = KL ? KL[((12 + i) + 18 * (12 + j)) * ne] : 0.0;
+      double kr = KR ? KR[(i + 18 * j) * ne] : 0.0;
       double d = kl + kr;
       if (i >= 3 && j >= 3) d += nk[(i - 3) * 3 + j - 3];
       if (eL >= 0) d += ELM(c.ec, eL, i * 26 + 13 + 7 + j);  // -A_bs Z_b of the left element
       if (eR >= 0) d += ELM(c.ec, eR, i * 26 + 1 + j);       // -A_as Z_a of the right element
       CRN(c.cD, k, i * 6 + j) = d;
-      CRN(c.cU, k, i * 6 + j) = kn >= 0 ? KR[i + 18 * (12 + j)] + (eR >= 0 ? ELM(c.ec, eR, i * 26 + 7 + j) : 0.0) : 0.0;
+      CRN(c.cU, k, i * 6 + j) =
+          kn >= 0 ? KR[(i + 18 * (12 + j)) * ne] + (eR >= 0 ? ELM(c.ec, eR, i * 26 + 7 + j) : 0.0) : 0.0;
       CRN(c.cL, k, i * 6 + j) =
-          kp >= 0 ? KL[(12 + i) + 18 * j] + (eL >= 0 ? ELM(c.ec, eL, i * 26 + 13 + 1 + j) : 0.0) : 0.0;
+          kp >= 0 ? KL[((12 + i) + 18 * j) * ne] + (eL >= 0 ? ELM(c.ec, eL, i * 26 + 13 + 1 + j) : 0.0) : 0.0;
     }
     double r = P[g[i]];
     if (eL >= 0) r += ELM(c.ec, eL, i * 26 + 13);

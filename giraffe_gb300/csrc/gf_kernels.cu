@@ -311,16 +311,19 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
       beam_gp_inertia(c, x, ip[g], vel, acc, a6, g, f, MOUNT_THREADS, Dm + (size_t)g * 9 * MOUNT_THREADS, MOUNT_THREADS);
     a1Mr = a6[0] * c.Mr;
   }
-  double* Ke = b.Ke + (int64_t)e * 324;
+  // element scratch is structure-of-arrays (entry x of element e at
+  // [x * n_elem + e]): the writes of a warp and the per-item reads of the
+  // chain solver are coalesced
+  double* Ke = b.Ke + e;
+  const int64_t ne = b.n_elem;
 #pragma unroll 1
   for (int J = 0; J < 3; ++J)
 #pragma unroll 1
     for (int I = 0; I < 3; ++I)
       beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
-                       Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr);
-  double* Fe = b.Fe + (int64_t)e * 18;
+                       Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, ne);
 #pragma unroll
-  for (int q = 0; q < 18; ++q) Fe[q] = f[q * MOUNT_THREADS];
+  for (int q = 0; q < 18; ++q) b.Fe[q * ne + e] = f[q * MOUNT_THREADS];
 }
 
 __global__ void k_beam_scatter(Batch b, int color) {
@@ -336,10 +339,11 @@ __global__ void k_beam_scatter(Batch b, int color) {
   if (lane < 18) myg = b.gl[(int64_t)b.enodes[3 * e + lane / 6] * 6 + lane % 6];
   if (inf.is_chain && !b.full_band) {
     // the chain solver reads K_e directly; only the residual is assembled
-    if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)e * 18 + lane];
+    if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)lane * b.n_elem + e];
     return;
   }
-  const double* Ke = b.Ke + (int64_t)e * 324;
+  const double* Ke = b.Ke + e;
+  const int64_t ne = b.n_elem;
   double* band = b.band + inf.band_off;
   // uniform trip count: every lane takes part in every shuffle
   for (int base = 0; base < 324; base += 32) {
@@ -348,9 +352,9 @@ __global__ void k_beam_scatter(Batch b, int color) {
     int r = valid ? idx % 18 : 0, q = valid ? idx / 18 : 0;
     int gr = __shfl_sync(0xffffffffu, myg, r);
     int gq = __shfl_sync(0xffffffffu, myg, q);
-    if (valid && gr >= 0 && gq >= 0) band[(GF_KB + gr - gq) + (int64_t)gq * GF_LDB] += Ke[idx];
+    if (valid && gr >= 0 && gq >= 0) band[(GF_KB + gr - gq) + (int64_t)gq * GF_LDB] += Ke[idx * ne];
   }
-  if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)e * 18 + lane];
+  if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)lane * ne + e];
 }
 
 // NodalLoad::Mount for every load entry of a structure, in entry order (one
