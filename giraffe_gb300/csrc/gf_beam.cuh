@@ -204,7 +204,8 @@ GF_HD void beam_gp_operator(const BeamConst& c, const BeamGP& k, TK* M, int ms =
   store_block(M, ms, 2, 1, V2, true);
 }
 
-// M'_pq = T3^T M_pq T3 for the nine 3x3 blocks, in place.
+// M'_pq = T3^T M_pq T3 for the 3x3 blocks, in place; M01 = M10 = 0 stay
+// zero and are skipped.
 template <typename TK> GF_HD void rotate_blocks9(const BeamConst& c, TK* M, int ms = 1) {
   TK T[9];
 #pragma unroll
@@ -213,6 +214,7 @@ template <typename TK> GF_HD void rotate_blocks9(const BeamConst& c, TK* M, int 
   for (int p = 0; p < 3; ++p)
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
+      if ((p == 0 && q == 1) || (p == 1 && q == 0)) continue;
       TK b[9], t[9];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -259,7 +261,7 @@ GF_HD double beam_M_entry(const BeamConst& c, const double* D0, const double* D1
 
 // The 6x6 block (I, J) of K_e (global frame) from the two rotated
 // Gauss-point operators, written to K (column-major 18x18, leading
-// dimension 18).  The products of the Gauss weight and shape-function values
+// dimension 18, entries ks apart).  The products of the Gauss weight and shape-function values
 // and derivatives are formed once per block (cdd = w N'_I N'_J, cdn = w N'_I
 // N_J, cnd = w N_I N'_J, cnn = w N_I N_J), so each entry is a short FMA chain
 // over the operator blocks: translation rows/columns couple through N' only,
@@ -268,7 +270,7 @@ GF_HD double beam_M_entry(const BeamConst& c, const double* D0, const double* D1
 template <typename TK>
 GF_HD void beam_K_block(const BeamConst& c, const TK* M0, const TK* M1, int I, int J, int ms, double* K,
                         bool dyn = false, const double* D0 = nullptr, const double* D1 = nullptr, int ds = 1,
-                        double a1Mr = 0.0) {
+                        double a1Mr = 0.0, int64_t ks = 1) {
   TK cdd[2], cdn[2], cnd[2], cnn[2];
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
@@ -289,11 +291,13 @@ GF_HD void beam_K_block(const BeamConst& c, const TK* M0, const TK* M1, int I, i
         if (a < 3 && b < 3) {
           acc += cdd[g] * M[(a * 9 + b) * ms];
         } else if (a < 3) {
+          // the operator's block (0, 1) is zero
           int bb = b - 3;
-          acc += cdd[g] * M[(a * 9 + 3 + bb) * ms] + cdn[g] * M[(a * 9 + 6 + bb) * ms];
+          acc += cdn[g] * M[(a * 9 + 6 + bb) * ms];
         } else if (b < 3) {
+          // the operator's block (1, 0) is zero
           int aa = a - 3;
-          acc += cdd[g] * M[((3 + aa) * 9 + b) * ms] + cnd[g] * M[((6 + aa) * 9 + b) * ms];
+          acc += cnd[g] * M[((6 + aa) * 9 + b) * ms];
         } else {
           int aa = a - 3, bb = b - 3;
           acc += cdd[g] * M[((3 + aa) * 9 + 3 + bb) * ms] + cdn[g] * M[((3 + aa) * 9 + 6 + bb) * ms] +
@@ -302,7 +306,7 @@ GF_HD void beam_K_block(const BeamConst& c, const TK* M0, const TK* M1, int I, i
       }
       double k = double(acc);
       if (dyn) k += beam_M_entry(c, D0, D1, ds, a1Mr, 6 * I + a, 6 * J + b);
-      K[(6 * I + a) + 18 * (6 * J + b)] = k;
+      K[((6 * I + a) + 18 * (6 * J + b)) * ks] = k;
     }
 }
 
