@@ -33,8 +33,8 @@ import numpy as np  # noqa: E402
 METRIC = "Newton solves/sec (batched static Beam_1 chains, FP64, converged load steps)"
 UNIT = "Newton solves/s"
 # DRAM bytes per element mount of k_beam_tangent, from one ncu capture on 128
-# chains: (57.3 MB read + 182.9 MB written) / 79,322 elements
-TANGENT_DRAM_BYTES_PER_ELEMENT = (57.312768e6 + 182.872576e6) / 79322
+# chains: (54.9 MB read + 173.1 MB written) / 79,322 elements
+TANGENT_DRAM_BYTES_PER_ELEMENT = (54.875648e6 + 173.070848e6) / 79322
 
 
 def parse():
