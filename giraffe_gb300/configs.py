@@ -228,3 +228,28 @@ def square_plate(n: int = 64, side: float = 1.0, thickness: float = 0.01, E: flo
     # floor of the rotational residual.
     s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, moment_min=1.0)
     return s
+
+
+def served_mixed(n_requests: int, seed: int = 0, plate_share: float = 0.3, chain_dof=(1000, 50000),
+                 plate_dof=(10000, 200000), steps: int = 10, tol: float = 1e-8) -> list:
+    """The mixed served stream: each request is a pipe chain (free DOFs
+    log-uniform in chain_dof, drawn as in served_chains) or, with probability
+    plate_share, a clamped square Shell_1 plate (free DOFs log-uniform in
+    plate_dof; an n x n x 2 mesh has about 20.7 n^2 free DOFs) under a
+    follower pressure drawn from U(5e4, 1e5) Pa, ramped over `steps` load
+    steps."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_requests):
+        if rng.random() < plate_share:
+            dof = math.exp(rng.uniform(math.log(plate_dof[0]), math.log(plate_dof[1])))
+            n = max(2, int(round(math.sqrt(dof / 20.7))))
+            out.append(square_plate(n, pressure=float(rng.uniform(5e4, 1e5)), steps=steps, tol=tol))
+        else:
+            dof = math.exp(rng.uniform(math.log(chain_dof[0]), math.log(chain_dof[1])))
+            n_el = max(1, int(round((dof / 6.0 - 1.0) / 2.0)))
+            De, wall = rng.uniform(0.3, 0.5), rng.uniform(0.02, 0.04)
+            F = rng.normal(0.0, 1e5, 3)
+            out.append(pipe_chain(n_el, float(De), float(wall), F, steps=steps, tol=tol,
+                                  element_length=10.0 / n_el))
+    return out

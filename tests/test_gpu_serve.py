@@ -106,3 +106,26 @@ def test_poisson_stream_latency(gpu_ctx):
     assert all(r.status == 0 and r.stats[3] == 0 for r in out["results"])
     assert np.all(out["latency_ms"] > 0)
     assert out["p99_ms"] >= out["p50_ms"] > 0
+
+
+def test_mixed_chains_and_plates_equal_alone(gpu_ctx):
+    """Shell_1 plates and beam chains in one stream: plates go to their own
+    waves (the wide-band pass is long), every result equals its structure
+    solved alone."""
+    structs = configs.served_mixed(12, seed=21, plate_share=0.4, chain_dof=(600, 6000), plate_dof=(200, 1500))
+    assert any(s.shells for s in structs) and any(s.beams for s in structs)
+    srv = serve.Server(gpu_ctx, hbm_budget=1 << 30, max_waves=4, max_wave_structs=3, passes_per_chunk=2)
+    results = {}
+    t0 = time.perf_counter()
+    for i, s in enumerate(structs):
+        srv.submit(s, tag=i)
+        for r in srv.poll():
+            results[r.tag] = r
+        if i % 4 == 3:
+            time.sleep(0.002)
+    while len(results) < len(structs):
+        for r in srv.poll():
+            results[r.tag] = r
+        assert time.perf_counter() - t0 < 300
+    srv.close()
+    _check_same_as_alone(gpu_ctx, structs, results)

@@ -36,3 +36,14 @@ def test_served_chains_span_the_dof_range():
     dof = np.array([x.n_free for x in s])
     assert dof.min() >= 900 and dof.max() <= 50100
     assert np.median(dof) > 3000 and np.median(dof) < 15000
+
+
+def test_served_mixed_stream_shares_and_sizes():
+    s = configs.served_mixed(120, seed=4, plate_dof=(10000, 40000))
+    plates = [x for x in s if x.shells]
+    chains = [x for x in s if x.beams]
+    assert len(plates) + len(chains) == 120
+    assert 0.18 < len(plates) / 120 < 0.42
+    pd = np.array([x.n_free for x in plates])
+    assert pd.min() > 7000 and pd.max() < 46000
+    assert [x.n_free for x in s][:20] == [x.n_free for x in configs.served_mixed(20, seed=4, plate_dof=(10000, 40000))]
