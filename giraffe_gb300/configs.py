@@ -46,6 +46,13 @@ def straight_chain(n_el: int, length: float, direction=(1.0, 0.0, 0.0)) -> np.nd
     return t[:, None] * d[None, :]
 
 
+def _chain_beams(s: Structure, n_el: int, mat: int, sec: int, cs: int) -> None:
+    """Beam_1 elements (2e, 2e+1, 2e+2) along a straight chain of 2 n_el + 1 nodes."""
+    e = np.arange(n_el)
+    s.beams.extend(np.stack([2 * e, 2 * e + 1, 2 * e + 2, np.full(n_el, mat), np.full(n_el, sec),
+                             np.full(n_el, cs)], axis=1))
+
+
 def cantilever_rollup(n_el: int = 20, steps: int = 20, tol: float = 1e-8) -> Structure:
     L = 10.0
     s = Structure(nodes=straight_chain(n_el, L))
@@ -53,8 +60,7 @@ def cantilever_rollup(n_el: int = 20, steps: int = 20, tol: float = 1e-8) -> Str
     sec = s.add_rectangle(0.1, 0.1)
     cs_beam = s.add_cs((0.0, 1.0, 0.0), (1.0, 0.0, 0.0))   # E3 along the axis
     cs_glob = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
-    for e in range(n_el):
-        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs_beam))
+    _chain_beams(s, n_el, mat, sec, cs_beam)
     s.clamp(0)
     I = s.sections[sec][2]  # bending about global z is about the section's E2 axis
     Mz = 2.0 * math.pi * E_STEEL * I / L
@@ -113,8 +119,7 @@ def pipe_chain(n_el: int, De: float, wall: float, tip_force, steps: int = 10,
     mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
     sec = s.add_tube(De, De - 2.0 * wall)
     cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
-    for e in range(n_el):
-        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    _chain_beams(s, n_el, mat, sec, cs)
     s.clamp(0)
     f = np.asarray(tip_force, dtype=np.float64)
     s.loads.append(NodalLoad([2 * n_el], cs, Table(np.array([0.0, 1.0]),
@@ -163,8 +168,7 @@ def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, st
     mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
     sec = s.add_tube(De, De - 2.0 * wall)
     cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
-    for e in range(n_el):
-        s.beams.append((2 * e, 2 * e + 1, 2 * e + 2, mat, sec, cs))
+    _chain_beams(s, n_el, mat, sec, cs)
     top = 2 * n_el
     s.clamp(top)
     t = np.arange(steps + 1) * dt

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -12,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/giraffe_gpu.h"
@@ -261,6 +264,10 @@ std::vector<int> rcm_order(int nn, const std::vector<std::vector<int>>& adj) {
 
 namespace gfh {
 
+double host_now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
   size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
   if (B->count_only) {
@@ -268,6 +275,11 @@ template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
     *p = nullptr;
     return true;
   }
+  struct Clock {
+    double* acc;
+    double t0;
+    ~Clock() { *acc += host_now_ms() - t0; }
+  } clock{&B->host_ms[1], host_now_ms()};
   if (B->arena) {
     void* q = B->arena->alloc(bytes);
     if (!q) return set_err(B->ctx, "device budget exhausted (%zu bytes requested, %zu free in the largest block)",
@@ -280,13 +292,256 @@ template <typename T> bool balloc(gf_batch* B, T** p, size_t n) {
   return true;
 }
 
-template <typename T> bool upload(gf_batch* B, T** p, const std::vector<T>& v) {
+template <typename T, typename A> bool upload(gf_batch* B, T** p, const std::vector<T, A>& v) {
   if (!balloc(B, p, v.size())) return false;
   B->h2d_bytes += (long long)(v.size() * sizeof(T));
   if (!v.empty() && !B->count_only) {
     // pageable source: staged before return, ordered on the batch's stream
+    const double t0 = host_now_ms();
     cudaError_t e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, B->stream);
+    B->host_ms[2] += host_now_ms() - t0;
     if (e != cudaSuccess) return set_err(B->ctx, "upload failed: %s", cudaGetErrorString(e));
+  }
+  return true;
+}
+
+namespace {
+
+std::string strf(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return buf;
+}
+
+// Runs f(s) for s in [0, n) on up to 16 host threads, structures handed out
+// one at a time; inline when the batch is small (work: nodes + elements).
+template <typename F> void parallel_structures(int n, size_t work, F f) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int T = (int)std::min<unsigned>(hw ? hw : 1u, 16u);
+  if (work < 50000) T = 1;
+  T = std::min(T, n);
+  if (T <= 1) {
+    for (int s = 0; s < n; ++s) f(s);
+    return;
+  }
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    for (int s; (s = next.fetch_add(1)) < n;) f(s);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < T; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+}
+
+// One structure after the numbering pass.
+struct StructPlan {
+  std::string err;                  // non-empty: the structure is rejected
+  std::vector<int> active, c6, g6;  // per node DOF: element-activated, constrained, free index (-1 fixed, -2 inactive)
+  std::vector<int> dofs;            // local node DOF (6 node + k) of each free index, in the solver's order
+  std::vector<int> perm;            // wide structures: the reference's free index -> the solver's
+  std::vector<char> node_free;      // chain structures: node fully free
+  int nf = 0, kb = 0, kl_nat = 0, wkl = 0;
+  bool has_f = false, has_m = false, wide = false, chain = false;
+  int n_colors = 0, n_scolors = 0;  // set by the fill pass
+};
+
+// Checks, activation and DOF numbering of one structure (SetGlobalDOFs,
+// reference src/Solution.cpp:40-118), its half-bandwidth and whether it is a
+// chain.
+void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
+  if (m.solution.type != GF_STATIC && m.solution.type != GF_DYNAMIC) {
+    P.err = strf("structure %d: unknown solution type", s);
+    return;
+  }
+  if (m.solution.type == GF_DYNAMIC && (m.solution.rayleigh_alpha != 0.0 || m.solution.rayleigh_beta != 0.0)) {
+    P.err = strf("structure %d: Rayleigh damping is not supported (alpha = beta = 0 required)", s);
+    return;
+  }
+  if (m.n_shells && m.n_beams) {
+    P.err = strf("structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
+    return;
+  }
+  if (m.n_shells && m.solution.type == GF_DYNAMIC) {
+    P.err = strf("structure %d: Shell_1 structures are supported in Static steps only", s);
+    return;
+  }
+  const int nn = m.n_nodes;
+  const bool wide = m.n_shells > 0;
+  P.wide = wide;
+  std::vector<int>& active = P.active;
+  std::vector<int>& c6 = P.c6;
+  std::vector<int>& g6 = P.g6;
+  active.assign((size_t)nn * 6, 0);
+  c6.assign((size_t)nn * 6, 0);
+  g6.assign((size_t)nn * 6, -2);
+  for (int e = 0; e < m.n_shells; ++e) {
+    const int* q = m.shells + 9 * e;
+    for (int j = 0; j < 6; ++j) {
+      if (q[j] < 0 || q[j] >= nn) {
+        P.err = strf("structure %d: shell %d has node %d out of range", s, e, q[j]);
+        return;
+      }
+      // Shell_1 activates translations everywhere, rotations on the
+      // midside nodes (reference src/Shell_1.cpp:51-68)
+      for (int k = 0; k < (j < 3 ? 3 : 6); ++k) active[6 * q[j] + k] = 1;
+    }
+    if (q[6] < 0 || q[6] >= m.n_materials || q[7] < 0 || q[7] >= m.n_shell_sections) {
+      P.err = strf("structure %d: shell %d refers to a missing material or shell section", s, e);
+      return;
+    }
+  }
+  for (int e = 0; e < m.n_beams; ++e) {
+    for (int j = 0; j < 3; ++j) {
+      int nd = m.beams[6 * e + j];
+      if (nd < 0 || nd >= nn) {
+        P.err = strf("structure %d: beam %d has node %d out of range", s, e, nd);
+        return;
+      }
+      for (int k = 0; k < 6; ++k) active[6 * nd + k] = 1;
+    }
+    if (m.beams[6 * e + 3] < 0 || m.beams[6 * e + 3] >= m.n_materials || m.beams[6 * e + 4] < 0 ||
+        m.beams[6 * e + 4] >= m.n_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
+      P.err = strf("structure %d: beam %d refers to a missing material, section or CS", s, e);
+      return;
+    }
+  }
+  if (m.constraints)
+    for (int i = 0; i < nn * 6; ++i) c6[i] = m.constraints[i] ? 1 : 0;
+  // Node-major numbering.  Shell structures number their free DOFs in
+  // reverse Cuthill-McKee node order instead when that gives the narrower
+  // band (the solver's numbering; results are reported per node, and
+  // gf_batch_assemble maps back to the reference's numbering through perm).
+  std::vector<int> g_nat;
+  auto number = [&](const std::vector<int>& order, std::vector<int>& g, std::vector<int>* dofs) {
+    int q = 0;
+    for (int i : order)
+      for (int k = 0; k < 6; ++k) {
+        if (!active[6 * i + k]) continue;
+        if (c6[6 * i + k] == 0) {
+          g[6 * i + k] = q++;
+          if (dofs) dofs->push_back(6 * i + k);
+        } else {
+          g[6 * i + k] = -1;
+        }
+      }
+    return q;
+  };
+  auto shell_band = [&](const std::vector<int>& g) {
+    int kl = 0;
+    for (int e = 0; e < m.n_shells; ++e) {
+      const int* q = m.shells + 9 * e;
+      int lo = INT_MAX, hi = -1;
+      for (int a = 0; a < 27; ++a) {
+        int d = a < 18 ? g[6 * q[a / 3] + a % 3] : g[6 * q[3 + (a - 18) / 3] + 3 + (a - 18) % 3];
+        if (d >= 0) { lo = std::min(lo, d); hi = std::max(hi, d); }
+      }
+      if (hi >= 0) kl = std::max(kl, hi - lo);
+    }
+    return kl;
+  };
+  std::vector<int> natural(nn);
+  for (int i = 0; i < nn; ++i) natural[i] = i;
+  int nf = 0;
+  if (wide) {
+    g_nat.assign((size_t)nn * 6, -2);
+    number(natural, g_nat, nullptr);
+    P.kl_nat = shell_band(g_nat);
+    std::vector<std::vector<int>> adj(nn);
+    for (int e = 0; e < m.n_shells; ++e) {
+      const int* q = m.shells + 9 * e;
+      for (int a = 0; a < 6; ++a)
+        for (int c = 0; c < 6; ++c)
+          if (a != c) adj[q[a]].push_back(q[c]);
+    }
+    for (auto& v : adj) {
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    nf = number(rcm_order(nn, adj), g6, &P.dofs);
+    P.wkl = shell_band(g6);
+    if (P.wkl > P.kl_nat) {  // keep the natural numbering when it is narrower
+      g6 = g_nat;
+      P.dofs.clear();
+      for (int i = 0; i < nn * 6; ++i)
+        if (g6[i] >= 0) P.dofs.push_back(i);
+      P.wkl = P.kl_nat;
+    }
+    P.perm.assign(nf, 0);
+    for (int i = 0; i < nn * 6; ++i)
+      if (g_nat[i] >= 0) P.perm[g_nat[i]] = g6[i];
+  } else {
+    P.dofs.reserve((size_t)nn * 6);
+    nf = number(natural, g6, &P.dofs);
+  }
+  P.nf = nf;
+  for (int d : P.dofs) {
+    if (d % 6 < 3) P.has_f = true; else P.has_m = true;
+  }
+  // half-bandwidth: the widest spread of free indices within one element
+  int kbs = 0;
+  for (int e = 0; e < m.n_beams; ++e) {
+    int lo = INT_MAX, hi = -1;
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 6; ++k) {
+        int g = g6[6 * m.beams[6 * e + j] + k];
+        if (g >= 0) { lo = std::min(lo, g); hi = std::max(hi, g); }
+      }
+    if (hi >= 0) kbs = std::max(kbs, hi - lo);
+  }
+  if (kbs > GF_KB) {
+    P.err = strf("structure %d: K_AA half-bandwidth %d exceeds %d (node-major numbering of a chain gives 17)", s, kbs,
+                 GF_KB);
+    return;
+  }
+  P.kb = wide ? P.kl_nat : kbs;
+  if (m.solution.type == GF_DYNAMIC)
+    for (int i = 0; i < nn; ++i) {
+      int fr = (g6[6 * i + 3] >= 0) + (g6[6 * i + 4] >= 0) + (g6[6 * i + 5] >= 0);
+      if (fr != 0 && fr != 3) {
+        P.err = strf("structure %d: dynamic nodes need all rotations free or all fixed (node %d)", s, i);
+        return;
+      }
+    }
+  // chain structure: elements on nodes (2e, 2e+1, 2e+2), every node fully
+  // free or fully fixed, midside and interior corner nodes free
+  bool chain = m.n_beams > 0 && nn == 2 * m.n_beams + 1;
+  for (int e = 0; chain && e < m.n_beams; ++e)
+    chain = m.beams[6 * e] == 2 * e && m.beams[6 * e + 1] == 2 * e + 1 && m.beams[6 * e + 2] == 2 * e + 2;
+  P.node_free.assign(nn, 0);
+  for (int i = 0; chain && i < nn; ++i) {
+    int f = 0;
+    for (int k = 0; k < 6; ++k) f += g6[6 * i + k] >= 0;
+    if (f != 0 && f != 6) chain = false;
+    P.node_free[i] = f == 6;
+    bool interior = i > 0 && i < nn - 1;
+    if (interior && !P.node_free[i]) chain = false;
+  }
+  P.chain = chain;
+}
+
+}  // namespace
+
+// A device array initialised from another device array of the batch (the
+// initial states kept for gf_batch_reset).
+template <typename T> bool dup(gf_batch* B, T** p, const T* src, size_t n) {
+  if (!balloc(B, p, n)) return false;
+  if (n && !B->count_only) {
+    cudaError_t e = cudaMemcpyAsync(*p, src, n * sizeof(T), cudaMemcpyDeviceToDevice, B->stream);
+    if (e != cudaSuccess) return set_err(B->ctx, "device copy failed: %s", cudaGetErrorString(e));
+  }
+  return true;
+}
+
+// A zero-filled device array.
+template <typename T> bool zeroed(gf_batch* B, T** p, size_t n) {
+  if (!balloc(B, p, n)) return false;
+  if (!B->count_only) {
+    cudaError_t e = cudaMemsetAsync(*p, 0, std::max<size_t>(n, 1) * sizeof(T), B->stream);
+    if (e != cudaSuccess) return set_err(B->ctx, "device memset failed: %s", cudaGetErrorString(e));
   }
   return true;
 }
@@ -294,239 +549,113 @@ template <typename T> bool upload(gf_batch* B, T** p, const std::vector<T>& v) {
 int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   gf_ctx* ctx = B->ctx;
   Batch& b = B->b;
-  std::vector<double> copy, Qn;
-  std::vector<int> gl, cons, node_struct, enodes, estruct, dof_node6, ecolor;
-  std::vector<BeamConst> bconst;
-  std::vector<BeamHist> bhist;
-  std::vector<BeamHistAux> baux;
-  std::vector<StructParams> params;
-  std::vector<LoadEntry> loads;
-  std::vector<DispEntry> disps;
-  std::vector<TableDev> tables;
-  std::vector<double> tdata;
-  int node_off = 0, elem_off = 0, dof_off = 0;
-  int max_color = 0;
-  std::vector<int> chain_flags;
-  std::vector<std::vector<char>> chain_free;
-  // Shell_1 elements
-  std::vector<int> snodes, sstruct, spress, sarea, scolor;
-  std::vector<ShellConst> sconst;
-  std::vector<ShellHist> shist;
-  std::vector<ShellHistAux> saux;
-  int shell_off = 0, max_scolor = 0;
+  // ---- numbering pass (parallel over structures) ----
+  std::vector<StructPlan> plan(n);
+  size_t work = 0;
+  for (int s = 0; s < n; ++s) work += (size_t)std::max(models[s].n_nodes, 0) + std::max(models[s].n_beams, 0) +
+                                      std::max(models[s].n_shells, 0);
+  parallel_structures(n, work, [&](int s) { plan_structure(models[s], s, plan[s]); });
+  for (int s = 0; s < n; ++s)
+    if (!plan[s].err.empty()) {
+      set_err(ctx, "%s", plan[s].err.c_str());
+      return GF_ERR_ARG;
+    }
+  // ---- offsets (serial) ----
+  std::vector<int> node_offs(n), elem_offs(n), shell_offs(n), dof_offs(n);
+  int node_off = 0, elem_off = 0, dof_off = 0, shell_off = 0;
   std::vector<int> wide_structs;
   int64_t wb_total = 0;
   int max_panels = 0, max_wkl = 0;
-  B->perm.clear();
+  B->perm.assign(n, std::vector<int>());
+  B->info.assign(n, StructInfo{});
+  B->kb.assign(n, 0);
+  B->shell_off.assign(n, 0);
   for (int s = 0; s < n; ++s) {
     const gf_model_desc& m = models[s];
-    if (m.solution.type != GF_STATIC && m.solution.type != GF_DYNAMIC) { set_err(ctx, "structure %d: unknown solution type", s); return GF_ERR_ARG; }
-    if (m.solution.type == GF_DYNAMIC && (m.solution.rayleigh_alpha != 0.0 || m.solution.rayleigh_beta != 0.0)) {
-      set_err(ctx, "structure %d: Rayleigh damping is not supported (alpha = beta = 0 required)", s);
-      return GF_ERR_ARG;
-    }
-    if (m.n_shells && m.n_beams) {
-      set_err(ctx, "structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
-      return GF_ERR_ARG;
-    }
-    if (m.n_shells && m.solution.type == GF_DYNAMIC) {
-      set_err(ctx, "structure %d: Shell_1 structures are supported in Static steps only", s);
-      return GF_ERR_ARG;
-    }
-    const int nn = m.n_nodes;
-    const bool wide = m.n_shells > 0;
-    std::vector<int> active(nn * 6, 0), c6(nn * 6, 0), g6(nn * 6, -2);
-    for (int e = 0; e < m.n_shells; ++e) {
-      const int* q = m.shells + 9 * e;
-      for (int j = 0; j < 6; ++j) {
-        if (q[j] < 0 || q[j] >= nn) { set_err(ctx, "structure %d: shell %d has node %d out of range", s, e, q[j]); return GF_ERR_ARG; }
-        // Shell_1 activates translations everywhere, rotations on the
-        // midside nodes (reference src/Shell_1.cpp:51-68)
-        for (int k = 0; k < (j < 3 ? 3 : 6); ++k) active[6 * q[j] + k] = 1;
-      }
-      if (q[6] < 0 || q[6] >= m.n_materials || q[7] < 0 || q[7] >= m.n_shell_sections) {
-        set_err(ctx, "structure %d: shell %d refers to a missing material or shell section", s, e);
-        return GF_ERR_ARG;
-      }
-    }
-    for (int e = 0; e < m.n_beams; ++e) {
-      for (int j = 0; j < 3; ++j) {
-        int nd = m.beams[6 * e + j];
-        if (nd < 0 || nd >= nn) { set_err(ctx, "structure %d: beam %d has node %d out of range", s, e, nd); return GF_ERR_ARG; }
-        for (int k = 0; k < 6; ++k) active[6 * nd + k] = 1;
-      }
-      if (m.beams[6 * e + 3] < 0 || m.beams[6 * e + 3] >= m.n_materials || m.beams[6 * e + 4] < 0 ||
-          m.beams[6 * e + 4] >= m.n_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
-        set_err(ctx, "structure %d: beam %d refers to a missing material, section or CS", s, e);
-        return GF_ERR_ARG;
-      }
-    }
-    if (m.constraints)
-      for (int i = 0; i < nn * 6; ++i) c6[i] = m.constraints[i] ? 1 : 0;
-    // SetGlobalDOFs (reference src/Solution.cpp:40-118): node-major
-    // numbering.  Shell structures number their free DOFs in reverse
-    // Cuthill-McKee node order instead (the solver's numbering; results are
-    // reported per node, and gf_batch_assemble maps back to the reference's
-    // numbering through perm).
-    std::vector<int> node_order(nn);
-    for (int i = 0; i < nn; ++i) node_order[i] = i;
-    std::vector<int> g_nat(nn * 6, -2);
-    {
-      int q = 0;
-      for (int i = 0; i < nn; ++i)
-        for (int k = 0; k < 6; ++k)
-          if (active[6 * i + k]) g_nat[6 * i + k] = c6[6 * i + k] == 0 ? q++ : -1;
-    }
-    auto shell_band = [&](const std::vector<int>& g) {
-      int kl = 0;
-      for (int e = 0; e < m.n_shells; ++e) {
-        const int* q = m.shells + 9 * e;
-        int d[27];
-        for (int a = 0; a < 18; ++a) d[a] = g[6 * q[a / 3] + a % 3];
-        for (int a = 0; a < 9; ++a) d[18 + a] = g[6 * q[3 + a / 3] + 3 + a % 3];
-        for (int a = 0; a < 27; ++a)
-          for (int c = 0; c < 27; ++c)
-            if (d[a] >= 0 && d[c] >= 0) kl = std::max(kl, std::abs(d[a] - d[c]));
-      }
-      return kl;
-    };
-    int kl_nat = wide ? shell_band(g_nat) : 0;
-    if (wide) {
-      std::vector<std::vector<int>> adj(nn);
-      for (int e = 0; e < m.n_shells; ++e) {
-        const int* q = m.shells + 9 * e;
-        for (int a = 0; a < 6; ++a)
-          for (int c = 0; c < 6; ++c)
-            if (a != c) adj[q[a]].push_back(q[c]);
-      }
-      for (auto& v : adj) {
-        std::sort(v.begin(), v.end());
-        v.erase(std::unique(v.begin(), v.end()), v.end());
-      }
-      node_order = rcm_order(nn, adj);
-    }
-    int nf = 0;
-    bool has_f = false, has_m = false;
-    for (int i : node_order)
-      for (int k = 0; k < 6; ++k) {
-        if (!active[6 * i + k]) continue;
-        if (c6[6 * i + k] == 0) {
-          g6[6 * i + k] = nf++;
-          dof_node6.push_back((node_off + i) * 6 + k);
-          if (k < 3) has_f = true; else has_m = true;
-        } else {
-          g6[6 * i + k] = -1;
-        }
-      }
-    int wkl = 0;
-    if (wide) {
-      wkl = shell_band(g6);
-      if (wkl > kl_nat) {  // keep the natural numbering when it is narrower
-        node_order.resize(nn);
-        for (int i = 0; i < nn; ++i) node_order[i] = i;
-        dof_node6.resize(dof_node6.size() - nf);
-        g6 = g_nat;
-        for (int i = 0; i < nn; ++i)
-          for (int k = 0; k < 6; ++k)
-            if (g6[6 * i + k] >= 0) dof_node6.push_back((node_off + i) * 6 + k);
-        wkl = kl_nat;
-      }
-      std::vector<int> perm(nf);
-      for (int i = 0; i < nn * 6; ++i)
-        if (g_nat[i] >= 0) perm[g_nat[i]] = g6[i];
-      B->perm.push_back(perm);
-    } else {
-      B->perm.push_back(std::vector<int>());
-    }
-    int kbs = 0;
-    for (int e = 0; e < m.n_beams; ++e)
-      for (int a = 0; a < 18; ++a)
-        for (int c = 0; c < 18; ++c) {
-          int ga = g6[6 * m.beams[6 * e + a / 6] + a % 6], gc = g6[6 * m.beams[6 * e + c / 6] + c % 6];
-          if (ga >= 0 && gc >= 0) kbs = std::max(kbs, std::abs(ga - gc));
-        }
-    if (kbs > GF_KB) {
-      set_err(ctx, "structure %d: K_AA half-bandwidth %d exceeds %d (node-major numbering of a chain gives 17)", s, kbs, GF_KB);
-      return GF_ERR_ARG;
-    }
-    B->kb.push_back(wide ? kl_nat : kbs);
-    if (m.solution.type == GF_DYNAMIC)
-      for (int i = 0; i < nn; ++i) {
-        int fr = (g6[6 * i + 3] >= 0) + (g6[6 * i + 4] >= 0) + (g6[6 * i + 5] >= 0);
-        if (fr != 0 && fr != 3) {
-          set_err(ctx, "structure %d: dynamic nodes need all rotations free or all fixed (node %d)", s, i);
-          return GF_ERR_ARG;
-        }
-      }
-    // chain structure: elements on nodes (2e, 2e+1, 2e+2), every node fully
-    // free or fully fixed, midside and interior corner nodes free
-    bool chain = m.n_beams > 0 && nn == 2 * m.n_beams + 1;
-    for (int e = 0; chain && e < m.n_beams; ++e)
-      chain = m.beams[6 * e] == 2 * e && m.beams[6 * e + 1] == 2 * e + 1 && m.beams[6 * e + 2] == 2 * e + 2;
-    std::vector<char> node_free(nn, 0);
-    for (int i = 0; chain && i < nn; ++i) {
-      int f = 0;
-      for (int k = 0; k < 6; ++k) f += g6[6 * i + k] >= 0;
-      if (f != 0 && f != 6) chain = false;
-      node_free[i] = f == 6;
-      bool interior = i > 0 && i < nn - 1;
-      if (interior && !node_free[i]) chain = false;
-    }
-    chain_flags.push_back(chain ? 1 : 0);
-    chain_free.push_back(node_free);
-    // padding: every structure's DOF range starts at a multiple of 32
-    int nf_pad = (nf + 31) / 32 * 32;
-    for (int q = nf; q < nf_pad; ++q) dof_node6.push_back(-1);
-    StructInfo inf{};
+    StructPlan& P = plan[s];
+    node_offs[s] = node_off;
+    elem_offs[s] = elem_off;
+    shell_offs[s] = shell_off;
+    dof_offs[s] = dof_off;
+    StructInfo& inf = B->info[s];
     inf.node_off = node_off;
-    inf.n_nodes = nn;
+    inf.n_nodes = m.n_nodes;
     inf.elem_off = elem_off;
     inf.n_elem = m.n_beams;
     inf.dof_off = dof_off;
-    inf.n_free = nf;
+    inf.n_free = P.nf;
     inf.band_off = (int64_t)dof_off * GF_LDB;
-    inf.has_force = has_f;
-    inf.has_moment = has_m;
-    inf.is_chain = chain_flags.back();
-    if (wide) {
+    inf.has_force = P.has_f;
+    inf.has_moment = P.has_m;
+    inf.is_chain = P.chain ? 1 : 0;
+    if (P.wide) {
       inf.wide = 1;
-      inf.wkl = std::max(wkl, 1);
-      inf.n_panels = (nf + GF_WB_NB - 1) / GF_WB_NB;
+      inf.wkl = std::max(P.wkl, 1);
+      inf.n_panels = (P.nf + GF_WB_NB - 1) / GF_WB_NB;
       inf.wb_off = wb_total;
-      wb_total += (int64_t)std::max(nf, 1) * (2 * inf.wkl + 1);
+      wb_total += (int64_t)std::max(P.nf, 1) * (2 * inf.wkl + 1);
       wide_structs.push_back(s);
       max_panels = std::max(max_panels, inf.n_panels);
       max_wkl = std::max(max_wkl, inf.wkl);
+      B->perm[s] = std::move(P.perm);
     }
-    // nodes
+    B->kb[s] = P.kb;
+    B->shell_off[s] = shell_off;
+    node_off += m.n_nodes;
+    elem_off += m.n_beams;
+    shell_off += m.n_shells;
+    // padding: every structure's DOF range starts at a multiple of 32
+    dof_off += (P.nf + 31) / 32 * 32;
+  }
+  // ---- fill pass (parallel over structures): nodes, DOF map, PreCalc and
+  // colouring of the elements ----
+  hvec<double> copy((size_t)node_off * 6), Qn((size_t)node_off * 9);
+  hvec<int> gl((size_t)node_off * 6), cons((size_t)node_off * 6), node_struct(node_off);
+  hvec<int> dof_node6(dof_off);
+  hvec<BeamConst> bconst(elem_off);
+  hvec<BeamHist> bhist(elem_off);
+  hvec<BeamHistAux> baux(elem_off);
+  hvec<int> enodes((size_t)elem_off * 3), estruct(elem_off), ecolor(elem_off);
+  hvec<ShellConst> sconst(shell_off);
+  hvec<ShellHist> shist(shell_off);
+  hvec<ShellHistAux> saux(shell_off);
+  hvec<int> snodes((size_t)shell_off * 6), sstruct(shell_off), spress(shell_off), sarea(shell_off), scolor(shell_off);
+  parallel_structures(n, work, [&](int s) {
+    const gf_model_desc& m = models[s];
+    StructPlan& P = plan[s];
+    const int nn = m.n_nodes, no = node_offs[s], eo = elem_offs[s], so = shell_offs[s];
+    const int dof_end = s + 1 < n ? dof_offs[s + 1] : dof_off;
     for (int i = 0; i < nn; ++i) {
-      for (int k = 0; k < 3; ++k) copy.push_back(m.node_xyz[3 * i + k]);
-      for (int k = 0; k < 3; ++k) copy.push_back(0.0);
-      for (int k = 0; k < 9; ++k) Qn.push_back(k % 4 == 0 ? 1.0 : 0.0);
-      for (int k = 0; k < 6; ++k) { gl.push_back(g6[6 * i + k]); cons.push_back(c6[6 * i + k]); }
-      node_struct.push_back(s);
+      double* x = &copy[(size_t)(no + i) * 6];
+      for (int k = 0; k < 3; ++k) { x[k] = m.node_xyz[3 * i + k]; x[3 + k] = 0.0; }
+      double* q = &Qn[(size_t)(no + i) * 9];
+      for (int k = 0; k < 9; ++k) q[k] = k % 4 == 0 ? 1.0 : 0.0;
+      for (int k = 0; k < 6; ++k) {
+        gl[(size_t)(no + i) * 6 + k] = P.g6[6 * i + k];
+        cons[(size_t)(no + i) * 6 + k] = P.c6[6 * i + k];
+      }
+      node_struct[no + i] = s;
     }
+    for (int q = 0; q < P.nf; ++q) dof_node6[dof_offs[s] + q] = no * 6 + P.dofs[q];
+    for (int q = dof_offs[s] + P.nf; q < dof_end; ++q) dof_node6[q] = -1;  // padding
     // elements: PreCalc + greedy colouring by shared nodes
     std::vector<unsigned> node_colors(nn, 0u);
     for (int e = 0; e < m.n_beams; ++e) {
       const int* be = m.beams + 6 * e;
-      BeamConst c;
-      BeamHist h;
-      BeamHistAux x;
       beam_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.materials + 3 * be[3], m.sections + 6 * be[4],
-                   m.cs + 6 * be[5], c, h, x);
-      bconst.push_back(c);
-      bhist.push_back(h);
-      baux.push_back(x);
-      for (int j = 0; j < 3; ++j) enodes.push_back(node_off + be[j]);
-      estruct.push_back(s);
+                   m.cs + 6 * be[5], bconst[eo + e], bhist[eo + e], baux[eo + e]);
+      for (int j = 0; j < 3; ++j) enodes[(size_t)(eo + e) * 3 + j] = no + be[j];
+      estruct[eo + e] = s;
       unsigned used = node_colors[be[0]] | node_colors[be[1]] | node_colors[be[2]];
       int col = 0;
       while (col < 8 && (used >> col) & 1u) ++col;
-      if (col >= 8) { set_err(ctx, "structure %d: element colouring needs more than 8 colours", s); return GF_ERR_ARG; }
+      if (col >= 8) {
+        P.err = strf("structure %d: element colouring needs more than 8 colours", s);
+        return;
+      }
       for (int j = 0; j < 3; ++j) node_colors[be[j]] |= 1u << col;
-      ecolor.push_back(col);
-      max_color = std::max(max_color, col + 1);
+      ecolor[eo + e] = col;
+      P.n_colors = std::max(P.n_colors, col + 1);
     }
     // Shell_1 PreCalc and greedy colouring (up to 16 colours)
     for (int e = 0; e < m.n_shells; ++e) {
@@ -534,26 +663,46 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       double xyz[18];
       for (int j = 0; j < 6; ++j)
         for (int k = 0; k < 3; ++k) xyz[3 * j + k] = m.node_xyz[3 * q[j] + k];
-      ShellConst c;
-      ShellHist h;
-      ShellHistAux x;
-      shell_precalc(xyz, m.materials + 3 * q[6], m.shell_sections[q[7]], c, h, x);
-      sconst.push_back(c);
-      shist.push_back(h);
-      saux.push_back(x);
-      for (int j = 0; j < 6; ++j) snodes.push_back(node_off + q[j]);
-      sstruct.push_back(s);
-      spress.push_back(-1);
-      sarea.push_back(0);
+      shell_precalc(xyz, m.materials + 3 * q[6], m.shell_sections[q[7]], sconst[so + e], shist[so + e], saux[so + e]);
+      for (int j = 0; j < 6; ++j) snodes[(size_t)(so + e) * 6 + j] = no + q[j];
+      sstruct[so + e] = s;
+      spress[so + e] = -1;  // set by the pressure loads below
+      sarea[so + e] = 0;
       unsigned used = 0;
       for (int j = 0; j < 6; ++j) used |= node_colors[q[j]];
       int col = 0;
       while (col < 16 && (used >> col) & 1u) ++col;
-      if (col >= 16) { set_err(ctx, "structure %d: shell colouring needs more than 16 colours", s); return GF_ERR_ARG; }
+      if (col >= 16) {
+        P.err = strf("structure %d: shell colouring needs more than 16 colours", s);
+        return;
+      }
       for (int j = 0; j < 6; ++j) node_colors[q[j]] |= 1u << col;
-      scolor.push_back(col);
-      max_scolor = std::max(max_scolor, col + 1);
+      scolor[so + e] = col;
+      P.n_scolors = std::max(P.n_scolors, col + 1);
     }
+  });
+  int max_color = 0, max_scolor = 0;
+  for (int s = 0; s < n; ++s) {
+    if (!plan[s].err.empty()) {
+      set_err(ctx, "%s", plan[s].err.c_str());
+      return GF_ERR_ARG;
+    }
+    max_color = std::max(max_color, plan[s].n_colors);
+    max_scolor = std::max(max_scolor, plan[s].n_scolors);
+  }
+  // ---- tables, loads, prescribed displacements, step parameters (serial) ----
+  std::vector<StructParams> params(n);
+  std::vector<LoadEntry> loads;
+  std::vector<DispEntry> disps;
+  std::vector<TableDev> tables;
+  std::vector<double> tdata;
+  for (int s = 0; s < n; ++s) {
+    const gf_model_desc& m = models[s];
+    const StructPlan& P = plan[s];
+    const std::vector<int>& active = P.active;
+    const std::vector<int>& g6 = P.g6;
+    const int node_off = node_offs[s], shell_off = shell_offs[s];
+    StructInfo& inf = B->info[s];
     // tables and nodal loads (NodalLoad::UpdateforSolutionStep, reference
     // src/NodalLoad.cpp:235-263)
     auto add_table = [&](const gf_table& t) {
@@ -624,7 +773,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
         disps.push_back(de);
       }
     }
-    StructParams p{};
+    StructParams& p = params[s];
     const gf_solution& so = m.solution;
     p.start_time = so.start_time;
     p.end_time = so.end_time;
@@ -648,13 +797,6 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     p.disp_min = cr.disp_min;
     p.rot_min = cr.rot_min;
     p.divergence_ref = cr.divergence_ref;
-    params.push_back(p);
-    B->info.push_back(inf);
-    B->shell_off.push_back(shell_off);
-    node_off += nn;
-    elem_off += m.n_beams;
-    shell_off += m.n_shells;
-    dof_off += nf_pad;
   }
   b.n_struct = n;
   b.n_nodes = node_off;
@@ -663,59 +805,82 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.n_loads = (int)loads.size();
   b.n_disps = (int)disps.size();
   b.n_tables = (int)tables.size();
-  // chain solver data
+  // chain solver data: sizes and offsets per structure (serial), then the
+  // tables of each structure filled in parallel
   {
     ChainData& cd = b.chain;
-    std::vector<int> elem_list, eca, ecb, cnode, cstruct, cleft, cright, cprev, cnext, roots;
-    std::vector<std::vector<CrItem>> odd_l(CR_MAX_LEVELS), even_l(CR_MAX_LEVELS);
-    int n_levels = 0;
+    const int NL = CR_MAX_LEVELS;
+    std::vector<int> Mc(n, 0), tb(n, 0), cb(n, 0), rpos(n, -1);
+    std::vector<int> opos((size_t)n * NL, 0), epos((size_t)n * NL, 0);
+    std::vector<int> ocnt(NL, 0), ecnt(NL, 0);
+    int n_t = 0, n_c = 0, n_levels = 0, n_roots = 0;
     for (int s = 0; s < n; ++s) {
-      if (!chain_flags[s]) continue;
-      const StructInfo& inf = B->info[s];
-      int mm = inf.n_elem;
-      const std::vector<char>& fr = chain_free[s];
-      int cbase = (int)cnode.size(), tbase = (int)elem_list.size();
-      std::vector<int> pos(mm + 1, -1);
+      if (!plan[s].chain) continue;
+      const int mm = B->info[s].n_elem;
+      const std::vector<char>& fr = plan[s].node_free;
       int M = 0;
-      for (int ci = 0; ci <= mm; ++ci)
-        if (fr[2 * ci]) pos[ci] = M++;
-      for (int e = 0; e < mm; ++e) {
-        elem_list.push_back(inf.elem_off + e);
-        eca.push_back(pos[e] >= 0 ? cbase + pos[e] : -1);
-        ecb.push_back(pos[e + 1] >= 0 ? cbase + pos[e + 1] : -1);
-      }
-      for (int ci = 0; ci <= mm; ++ci) {
-        if (pos[ci] < 0) continue;
-        int k = pos[ci];
-        cnode.push_back(inf.node_off + 2 * ci);
-        cstruct.push_back(s);
-        cleft.push_back(ci >= 1 ? tbase + ci - 1 : -1);
-        cright.push_back(ci < mm ? tbase + ci : -1);
-        cprev.push_back(k > 0 ? cbase + k - 1 : -1);
-        cnext.push_back(k + 1 < M ? cbase + k + 1 : -1);
-      }
-      if (M >= 1) roots.push_back(cbase);
+      for (int ci = 0; ci <= mm; ++ci) M += fr[2 * ci] != 0;
+      Mc[s] = M;
+      tb[s] = n_t;
+      cb[s] = n_c;
+      n_t += mm;
+      n_c += M;
+      if (M >= 1) rpos[s] = n_roots++;
       int l = 0;
       for (int h = 1; h < M; h *= 2, ++l) {
-        if (l >= CR_MAX_LEVELS) { set_err(ctx, "chain too long for %d reduction levels", CR_MAX_LEVELS); return GF_ERR_ARG; }
-        for (int kp = h; kp < M; kp += 2 * h)
-          odd_l[l].push_back(CrItem{cbase + kp, cbase + kp - h, kp + h < M ? cbase + kp + h : -1, s});
-        for (int kp = 0; kp < M; kp += 2 * h) {
-          bool hp = kp - h >= 0, hn = kp + h < M;
-          if (hp || hn) even_l[l].push_back(CrItem{cbase + kp, hp ? cbase + kp - h : -1, hn ? cbase + kp + h : -1, s});
-        }
+        if (l >= NL) { set_err(ctx, "chain too long for %d reduction levels", NL); return GF_ERR_ARG; }
+        // odd items kp = h, 3h, 5h, ... < M; even items kp = 0, 2h, 4h, ... < M
+        opos[(size_t)s * NL + l] = ocnt[l];
+        ocnt[l] += (M - h - 1) / (2 * h) + 1;
+        epos[(size_t)s * NL + l] = ecnt[l];
+        ecnt[l] += (M + 2 * h - 1) / (2 * h);
       }
       n_levels = std::max(n_levels, l);
     }
-    std::vector<CrItem> odd, even;
-    for (int l = 0; l <= CR_MAX_LEVELS; ++l) {
-      cd.odd_off[l] = (int)odd.size();
-      cd.even_off[l] = (int)even.size();
-      if (l < CR_MAX_LEVELS) {
-        odd.insert(odd.end(), odd_l[l].begin(), odd_l[l].end());
-        even.insert(even.end(), even_l[l].begin(), even_l[l].end());
-      }
+    for (int l = 0, o = 0, e = 0; l <= NL; ++l) {
+      cd.odd_off[l] = o;
+      cd.even_off[l] = e;
+      if (l < NL) { o += ocnt[l]; e += ecnt[l]; }
     }
+    hvec<int> elem_list(n_t), eca(n_t), ecb(n_t), cnode(n_c), cstruct(n_c), cleft(n_c), cright(n_c), cprev(n_c),
+        cnext(n_c), roots(n_roots);
+    hvec<CrItem> odd(cd.odd_off[NL]), even(cd.even_off[NL]);
+    parallel_structures(n, work, [&](int s) {
+      if (!plan[s].chain) return;
+      const StructInfo& inf = B->info[s];
+      const int mm = inf.n_elem, M = Mc[s], cbase = cb[s], tbase = tb[s];
+      const std::vector<char>& fr = plan[s].node_free;
+      std::vector<int> pos(mm + 1, -1);
+      for (int ci = 0, k = 0; ci <= mm; ++ci)
+        if (fr[2 * ci]) pos[ci] = k++;
+      for (int e = 0; e < mm; ++e) {
+        elem_list[tbase + e] = inf.elem_off + e;
+        eca[tbase + e] = pos[e] >= 0 ? cbase + pos[e] : -1;
+        ecb[tbase + e] = pos[e + 1] >= 0 ? cbase + pos[e + 1] : -1;
+      }
+      for (int ci = 0; ci <= mm; ++ci) {
+        if (pos[ci] < 0) continue;
+        const int k = pos[ci], c = cbase + k;
+        cnode[c] = inf.node_off + 2 * ci;
+        cstruct[c] = s;
+        cleft[c] = ci >= 1 ? tbase + ci - 1 : -1;
+        cright[c] = ci < mm ? tbase + ci : -1;
+        cprev[c] = k > 0 ? cbase + k - 1 : -1;
+        cnext[c] = k + 1 < M ? cbase + k + 1 : -1;
+      }
+      if (rpos[s] >= 0) roots[rpos[s]] = cbase;
+      int l = 0;
+      for (int h = 1; h < M; h *= 2, ++l) {
+        CrItem* o = &odd[cd.odd_off[l] + opos[(size_t)s * NL + l]];
+        for (int kp = h; kp < M; kp += 2 * h)
+          *o++ = CrItem{cbase + kp, cbase + kp - h, kp + h < M ? cbase + kp + h : -1, s};
+        CrItem* v = &even[cd.even_off[l] + epos[(size_t)s * NL + l]];
+        for (int kp = 0; kp < M; kp += 2 * h) {
+          bool hp = kp - h >= 0, hn = kp + h < M;
+          *v++ = CrItem{cbase + kp, hp ? cbase + kp - h : -1, hn ? cbase + kp + h : -1, s};
+        }
+      }
+    });
     cd.n_chain_elems = (int)elem_list.size();
     cd.n_corners = (int)cnode.size();
     cd.n_levels = n_levels;
@@ -759,7 +924,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   if (shell_off) {
     if (!upload(B, &sd.snodes, snodes) || !upload(B, &sd.sstruct, sstruct) || !upload(B, &sd.spress, spress) ||
         !upload(B, &sd.sarea, sarea) || !upload(B, &sd.sconst, sconst) || !upload(B, &sd.shist, shist) ||
-        !upload(B, &sd.saux, saux) || !upload(B, &B->shist0, shist) || !upload(B, &B->saux0, saux) ||
+        !upload(B, &sd.saux, saux) || !dup(B, &B->shist0, sd.shist, shist.size()) ||
+        !dup(B, &B->saux0, sd.saux, saux.size()) ||
         !upload(B, &sd.color_elems, scolor_elems) || !balloc(B, &sd.Ke, (size_t)shell_off * 729) ||
         !balloc(B, &sd.Fe, (size_t)shell_off * 27))
       return GF_ERR_CUDA;
@@ -772,17 +938,17 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     }
   }
   // device arrays
-  std::vector<double> zeros6((size_t)node_off * 6, 0.0);
-  if (!upload(B, &b.copy, copy) || !upload(B, &b.Qn, Qn) || !upload(B, &b.disp, zeros6) || !upload(B, &b.gl, gl) ||
-      !upload(B, &b.vel, zeros6) || !upload(B, &b.accel, zeros6) || !upload(B, &b.copy_vel, zeros6) ||
-      !upload(B, &b.copy_accel, zeros6) ||
+  const size_t n6 = (size_t)node_off * 6;
+  if (!upload(B, &b.copy, copy) || !upload(B, &b.Qn, Qn) || !zeroed(B, &b.disp, n6) || !upload(B, &b.gl, gl) ||
+      !zeroed(B, &b.vel, n6) || !zeroed(B, &b.accel, n6) || !zeroed(B, &b.copy_vel, n6) ||
+      !zeroed(B, &b.copy_accel, n6) ||
       !upload(B, &b.cons, cons) || !upload(B, &b.node_struct, node_struct) || !upload(B, &b.enodes, enodes) ||
       !upload(B, &b.estruct, estruct) || !upload(B, &b.bconst, bconst) || !upload(B, &b.bhist, bhist) ||
       !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
       !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.loads, loads) ||
       !upload(B, &b.disps, disps) || !upload(B, &b.tables, tables) || !upload(B, &b.table_data, tdata) ||
-      !upload(B, &B->copy0, copy) || !upload(B, &B->Qn0, Qn) || !upload(B, &B->bhist0, bhist) ||
-      !upload(B, &B->baux0, baux))
+      !dup(B, &B->copy0, b.copy, copy.size()) || !dup(B, &B->Qn0, b.Qn, Qn.size()) ||
+      !dup(B, &B->bhist0, b.bhist, bhist.size()) || !dup(B, &B->baux0, b.baux, baux.size()))
     return GF_ERR_CUDA;
   if (!balloc(B, &b.P, (size_t)dof_off) || !balloc(B, &b.y, (size_t)dof_off) ||
       !balloc(B, &b.band, (size_t)dof_off * GF_LDB) || !balloc(B, &b.U, (size_t)dof_off * GF_UW) ||
@@ -793,9 +959,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.full_band = 0;
   b.xref = B->copy0;
   if (B->count_only) return GF_OK;
-  B->h_gl = gl;
-  B->h_enodes = enodes;
-  B->h_snodes = snodes;
+  B->h_gl = std::move(gl);
+  B->h_enodes = std::move(enodes);
+  B->h_snodes = std::move(snodes);
   CK(cudaMemsetAsync(b.band, 0, sizeof(double) * (size_t)std::max(dof_off, 1) * GF_LDB, B->stream));
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
@@ -884,6 +1050,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
   B->stream = ctx->stream;
   if (opts) B->opts = *opts; else gf_default_opts(&B->opts);
   if (B->opts.poll_every <= 0) B->opts.poll_every = 8;
+  const double t0 = host_now_ms();
   if (build_batch(B, n, models) != GF_OK || cudaMallocHost(&B->h_running, sizeof(int)) != cudaSuccess ||
       cudaEventCreate(&B->ev0) != cudaSuccess || cudaEventCreate(&B->ev1) != cudaSuccess) {
     std::string e = ctx->err;
@@ -892,6 +1059,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
     return nullptr;
   }
   B->launches_per_pass = count_launches_per_pass(B);
+  B->host_ms[0] = host_now_ms() - t0 - B->host_ms[1] - B->host_ms[2];
   return B;
 }
 
@@ -928,12 +1096,14 @@ int ensure_graph(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
   cudaStream_t st = B->stream;
   if (B->opts.use_graph && !B->graph) {
+    const double t0 = host_now_ms();
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     launch_iteration(B->b, st);
     CK(cudaStreamEndCapture(st, &g));
     CK(cudaGraphInstantiate(&B->graph, g, 0));
     CK(cudaGraphDestroy(g));
+    B->host_ms[3] = host_now_ms() - t0;
   }
   return GF_OK;
 }
@@ -1117,6 +1287,7 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
   if (!B) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
   const Batch& b = B->b;
+  const double t0 = host_now_ms();
   int n = b.n_struct;
   std::vector<StructState> st(n);
   CK(cudaMemcpy(st.data(), b.state, sizeof(StructState) * n, cudaMemcpyDeviceToHost));
@@ -1145,6 +1316,13 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       }
     }
   }
+  B->host_ms[4] = host_now_ms() - t0;
+  return GF_OK;
+}
+
+int gf_batch_host_ms(const gf_batch* B, double* ms, int n) {
+  if (!B || !ms || n < 0) return GF_ERR_ARG;
+  for (int i = 0; i < n && i < 5; ++i) ms[i] = B->host_ms[i];
   return GF_OK;
 }
 

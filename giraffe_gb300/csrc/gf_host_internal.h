@@ -5,7 +5,9 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/giraffe_gpu.h"
@@ -74,6 +76,20 @@ struct DevArena {
   }
 };
 
+// Host arrays whose elements are default-initialised (left unset for plain
+// types): the batch build writes every element itself, from several threads,
+// so the pages are first touched in parallel instead of by one zero fill.
+template <typename T> struct DefaultInitAlloc : std::allocator<T> {
+  template <typename U> struct rebind { using other = DefaultInitAlloc<U>; };
+  DefaultInitAlloc() = default;
+  template <typename U> DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+  template <typename U> void construct(U* p) noexcept { ::new (static_cast<void*>(p)) U; }
+  template <typename U, typename... A> void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <typename T> using hvec = std::vector<T, DefaultInitAlloc<T>>;
+
 struct gf_batch {
   gf_ctx* ctx = nullptr;
   gf_solve_opts opts{};
@@ -99,7 +115,7 @@ struct gf_batch {
   // host copies for the CSR view of K_AA (gf_batch_assemble_csr): free index
   // (solver numbering) of every node DOF, element nodes, per-structure shell
   // offsets
-  std::vector<int> h_gl, h_enodes, h_snodes;
+  hvec<int> h_gl, h_enodes, h_snodes;
   std::vector<int> shell_off;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -108,6 +124,11 @@ struct gf_batch {
   int launches_per_pass = 0;
   int* h_running = nullptr;  // pinned
   long long h2d_bytes = 0;
+  // host wall time (ms) of gf_batch_create, split into model work (checks,
+  // numbering, PreCalc, colouring, chain tables), device allocation and
+  // host->device uploads; CUDA-graph capture + instantiation of the first
+  // gf_batch_run; the last gf_batch_results
+  double host_ms[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 };
 
 namespace gfh {
@@ -121,6 +142,8 @@ int batch_reset(gf_batch* B);
 int ensure_graph(gf_batch* B);
 // Kernel launches of one Newton pass.
 int count_launches_per_pass(const gf_batch* B);
+// Host wall clock in milliseconds.
+double host_now_ms();
 }  // namespace gfh
 
 #define GF_CK(call)                                                                          \

@@ -20,7 +20,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
            "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
-           "gf_kernel_name", "gf_batch_bytes", "gf_batch_work", "gf_device_fp_peaks",
+           "gf_kernel_name", "gf_batch_bytes", "gf_batch_host_ms", "gf_batch_work", "gf_device_fp_peaks",
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
            "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr"]

@@ -55,17 +55,23 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
+# Pointer members are declared as void* here (same size and alignment as the
+# typed pointers of the C header) so that numpy buffer addresses are stored
+# without a ctypes pointer object per array.
+_vp = C.c_void_p
+
+
 class gf_table(C.Structure):
-    _fields_ = [("n_times", C.c_int), ("n_cols", C.c_int), ("times", _dp), ("values", _dp)]
+    _fields_ = [("n_times", C.c_int), ("n_cols", C.c_int), ("times", _vp), ("values", _vp)]
 
 
 class gf_load(C.Structure):
-    _fields_ = [("type", C.c_int), ("n_items", C.c_int), ("items", _ip), ("cs", C.c_int),
+    _fields_ = [("type", C.c_int), ("n_items", C.c_int), ("items", _vp), ("cs", C.c_int),
                 ("area_update", C.c_int), ("table", gf_table)]
 
 
 class gf_displacement(C.Structure):
-    _fields_ = [("n_nodes", C.c_int), ("nodes", _ip), ("cs", C.c_int), ("table", gf_table)]
+    _fields_ = [("n_nodes", C.c_int), ("nodes", _vp), ("cs", C.c_int), ("table", gf_table)]
 
 
 class gf_solution(C.Structure):
@@ -84,16 +90,16 @@ class gf_criteria(C.Structure):
 
 
 class gf_model_desc(C.Structure):
-    _fields_ = [("n_nodes", C.c_int), ("node_xyz", _dp),
-                ("n_materials", C.c_int), ("materials", _dp),
-                ("n_sections", C.c_int), ("sections", _dp),
-                ("n_shell_sections", C.c_int), ("shell_sections", _dp),
-                ("n_cs", C.c_int), ("cs", _dp),
-                ("n_beams", C.c_int), ("beams", _ip),
-                ("n_shells", C.c_int), ("shells", _ip),
-                ("constraints", _ip),
-                ("n_loads", C.c_int), ("loads", C.POINTER(gf_load)),
-                ("n_displacements", C.c_int), ("displacements", C.POINTER(gf_displacement)),
+    _fields_ = [("n_nodes", C.c_int), ("node_xyz", _vp),
+                ("n_materials", C.c_int), ("materials", _vp),
+                ("n_sections", C.c_int), ("sections", _vp),
+                ("n_shell_sections", C.c_int), ("shell_sections", _vp),
+                ("n_cs", C.c_int), ("cs", _vp),
+                ("n_beams", C.c_int), ("beams", _vp),
+                ("n_shells", C.c_int), ("shells", _vp),
+                ("constraints", _vp),
+                ("n_loads", C.c_int), ("loads", _vp),
+                ("n_displacements", C.c_int), ("displacements", _vp),
                 ("solution", gf_solution), ("criteria", gf_criteria)]
 
 
@@ -109,8 +115,69 @@ def _i(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
-def _ptr(a, t):
-    return a.ctypes.data_as(t) if a is not None and a.size else C.cast(None, t)
+def _ptr(a, t=None):
+    """Address of a numpy buffer for a void* member (None when empty)."""
+    return a.__array_interface__["data"][0] if a is not None and a.size else None
+
+
+class ElementTable:
+    """Element rows (node indices, then material, section and frame indices)
+    kept in one growing int32 array, so that handing a structure to the C ABI
+    passes that array as it is.  Behaves as a list of tuples: append, extend,
+    indexing, assignment of a row, iteration, len."""
+
+    def __init__(self, width: int, rows=()):
+        self.width = width
+        self._a = np.zeros((16, width), dtype=np.int32)
+        self._n = 0
+        self.extend(rows)
+
+    def _reserve(self, n):
+        if n > len(self._a):
+            a = np.zeros((max(n, 2 * len(self._a)), self.width), dtype=np.int32)
+            a[:self._n] = self._a[:self._n]
+            self._a = a
+
+    def append(self, row):
+        self._reserve(self._n + 1)
+        self._a[self._n] = row
+        self._n += 1
+
+    def extend(self, rows):
+        rows = np.asarray(rows if not isinstance(rows, ElementTable) else rows.array(), dtype=np.int32)
+        if rows.size == 0:
+            return
+        rows = rows.reshape(-1, self.width)
+        self._reserve(self._n + len(rows))
+        self._a[self._n:self._n + len(rows)] = rows
+        self._n += len(rows)
+
+    def array(self) -> np.ndarray:
+        """The rows as an [n][width] int32 view (no copy)."""
+        return self._a[:self._n]
+
+    def __len__(self):
+        return self._n
+
+    def __bool__(self):
+        return self._n > 0
+
+    def __iter__(self):
+        return iter([tuple(r) for r in self.array().tolist()])
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return [tuple(r) for r in self.array()[k].tolist()]
+        return tuple(self.array()[k].tolist())
+
+    def __setitem__(self, k, row):
+        self.array()[k] = row
+
+    def __eq__(self, other):
+        return list(self) == list(other)
+
+    def __repr__(self):
+        return f"ElementTable({list(self)!r})"
 
 
 # --------------------------------------------------------------------------
@@ -175,13 +242,19 @@ class Structure:
     section_decks: list = field(default_factory=list)  # deck text of each section
     shell_sections: list = field(default_factory=list)  # thickness
     cs: list = field(default_factory=list)             # (E1 xyz, E3 xyz)
-    beams: list = field(default_factory=list)          # (n0, n1, n2, mat, sec, cs)
-    shells: list = field(default_factory=list)         # (6 nodes, mat, shell sec, cs)
+    beams: ElementTable = field(default_factory=lambda: ElementTable(6))   # (n0, n1, n2, mat, sec, cs)
+    shells: ElementTable = field(default_factory=lambda: ElementTable(9))  # (6 nodes, mat, shell sec, cs)
     constraints: np.ndarray | None = None              # [n][6] 0/1
     loads: list = field(default_factory=list)
     displacements: list = field(default_factory=list)
     solution: Solution = field(default_factory=Solution)
     criteria: dict = field(default_factory=lambda: dict(DEFAULT_CRITERIA))
+
+    def __setattr__(self, name, value):
+        # element rows assigned as lists become ElementTables
+        if name in ("beams", "shells") and not isinstance(value, ElementTable):
+            value = ElementTable(6 if name == "beams" else 9, value)
+        object.__setattr__(self, name, value)
 
     # ---- building helpers ----
     def add_material(self, E, nu, rho):
@@ -218,11 +291,9 @@ class Structure:
     @property
     def n_free(self):
         active = np.zeros((self.n_nodes, 6), dtype=bool)
-        for b in self.beams:
-            active[list(b[:3])] = True
-        for sh in self.shells:
-            active[list(sh[:3]), :3] = True
-            active[list(sh[3:6])] = True
+        active[self.beams.array()[:, :3].ravel()] = True
+        active[self.shells.array()[:, :3].ravel(), :3] = True
+        active[self.shells.array()[:, 3:6].ravel()] = True
         cons = self.constraints if self.constraints is not None else 0
         return int((active & (cons == 0)).sum())
 
@@ -365,8 +436,8 @@ class DescHandle:
         secs = d(np.asarray(s.sections, dtype=np.float64).reshape(-1, 6))
         ssec = d(np.asarray(s.shell_sections, dtype=np.float64).reshape(-1, 1))
         cs = d(np.asarray(s.cs, dtype=np.float64).reshape(-1, 6))
-        beams = i(np.asarray(s.beams, dtype=np.int32).reshape(-1, 6))
-        shells = i(np.asarray(s.shells, dtype=np.int32).reshape(-1, 9))
+        beams = i(s.beams.array())
+        shells = i(s.shells.array())
         cons = i(s.constraints) if s.constraints is not None else None
         loads = (gf_load * max(1, len(s.loads)))()
         for k, L in enumerate(s.loads):
@@ -397,8 +468,8 @@ class DescHandle:
         self.desc = gf_model_desc(
             len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
             len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
-            len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), loads,
-            len(s.displacements), disps, sol, crit)
+            len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), C.addressof(loads),
+            len(s.displacements), C.addressof(disps), sol, crit)
 
     @property
     def ref(self):

@@ -131,8 +131,16 @@ const char* gf_kernel_name(int k);
 int gf_batch_bytes(const gf_batch* batch, long long* h2d, long long* d2h);
 /* Algorithmic work of the last run: per-structure Newton passes summed into
  * the factor/solve flop count 2 n kl ku + 2 n (kl + ku) and the assembly
- * bytes 8 [6 N_nodes + 80 N_e + 35 n + n] per pass (see DESIGN). */
+ * bytes 8 [6 N_nodes + 80 N_e + 35 n + n] per pass (nodal state, element
+ * constants and history, band and right-hand side); mount_flops counts 9000
+ * FP64 flops per Beam_1 element mount. */
 int gf_batch_work(const gf_batch* batch, double* lu_flops, double* asm_bytes, double* mount_flops);
+/* Host wall time in ms: ms[0] model work of gf_batch_create (checks,
+ * numbering, PreCalc, colouring, chain tables), ms[1] its device
+ * allocations, ms[2] its host->device uploads, ms[3] CUDA-graph capture and
+ * instantiation in the first gf_batch_run, ms[4] the last gf_batch_results.
+ * Writes min(n, 5) values. */
+int gf_batch_host_ms(const gf_batch* batch, double* ms, int n);
 /* Measured FP64 and FP32 FMA throughput of the device (TFLOP/s). */
 int gf_device_fp_peaks(gf_ctx* ctx, double* fp64_tflops, double* fp32_tflops);
 
