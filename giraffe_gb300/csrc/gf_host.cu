@@ -1303,18 +1303,20 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       stats[s] = z;
     }
   if (final_nodes) {
-    std::vector<double> copy((size_t)b.n_nodes * 6), Qn((size_t)b.n_nodes * 9);
+    hvec<double> copy((size_t)b.n_nodes * 6), Qn((size_t)b.n_nodes * 9);
     CK(cudaMemcpy(copy.data(), b.copy, sizeof(double) * copy.size(), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(Qn.data(), b.Qn, sizeof(double) * Qn.size(), cudaMemcpyDeviceToHost));
-    for (int s = 0; s < n; ++s) {
+    parallel_structures(n, (size_t)b.n_nodes, [&](int s) {
       double* o = final_nodes[s];
-      if (!o) continue;
+      if (!o) return;
       const StructInfo& inf = B->info[s];
+      const double* x = &copy[(size_t)inf.node_off * 6];
+      const double* q = &Qn[(size_t)inf.node_off * 9];
       for (int i = 0; i < inf.n_nodes; ++i) {
-        std::memcpy(o + 15 * i, &copy[(size_t)(inf.node_off + i) * 6], 6 * sizeof(double));
-        std::memcpy(o + 15 * i + 6, &Qn[(size_t)(inf.node_off + i) * 9], 9 * sizeof(double));
+        for (int k = 0; k < 6; ++k) o[15 * i + k] = x[6 * i + k];
+        for (int k = 0; k < 9; ++k) o[15 * i + 6 + k] = q[9 * i + k];
       }
-    }
+    });
   }
   B->host_ms[4] = host_now_ms() - t0;
   return GF_OK;
@@ -1624,10 +1626,11 @@ int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double
 }
 
 int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info) {
-  if (!ctx || n <= 0 || kl < 0 || ku < 0 || kl > GF_KB || ku > GF_KB || ldab < 2 * kl + ku + 1 || !ab || !b) {
-    set_err(ctx, "gf_band_solve: invalid arguments (kl, ku must be <= %d)", GF_KB);
+  if (!ctx || n <= 0 || kl < 0 || ku < 0 || ldab < 2 * kl + ku + 1 || !ab || !b) {
+    set_err(ctx, "gf_band_solve: invalid arguments");
     return GF_ERR_ARG;
   }
+  if (kl > GF_KB || ku > GF_KB) return wide_band_solve(ctx, n, kl, ku, ab, ldab, b, info);
   int npad = (n + 31) / 32 * 32;
   std::vector<double> band((size_t)npad * GF_LDB, 0.0);
   for (int j = 0; j < n; ++j)

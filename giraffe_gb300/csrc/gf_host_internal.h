@@ -144,6 +144,12 @@ int ensure_graph(gf_batch* B);
 int count_launches_per_pass(const gf_batch* B);
 // Host wall clock in milliseconds.
 double host_now_ms();
+// Reverse Cuthill-McKee order of a graph given by adjacency lists
+// (order[k] = the vertex placed k-th).
+std::vector<int> rcm_order(int nn, const std::vector<std::vector<int>>& adj);
+// gf_band_solve for half-bandwidths above 17: the blocked wide-band LU on a
+// one-structure batch (gf_sparse.cu).
+int wide_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
 }  // namespace gfh
 
 #define GF_CK(call)                                                                          \

@@ -21,7 +21,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
            "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
            "gf_kernel_name", "gf_batch_bytes", "gf_batch_host_ms", "gf_batch_work", "gf_device_fp_peaks",
-           "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_batch_device_bytes",
+           "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_sparse_solve", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
            "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr"]
 
@@ -79,12 +79,14 @@ def lib():
         L.gf_batch_last_ms.argtypes = [vp]
         L.gf_batch_last_launches.restype = C.c_longlong
         L.gf_batch_last_launches.argtypes = [vp]
+        L.gf_batch_host_ms.argtypes = [vp, dp, C.c_int]
         L.gf_batch_assemble.argtypes = [vp, C.c_int, dp, dp, ip]
         L.gf_solve.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts),
                                C.POINTER(dp), C.POINTER(gf_stats)]
         L.gf_beam_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         L.gf_band_solve.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
         L.gf_band_solve_noalloc.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, ip]
+        L.gf_sparse_solve.argtypes = [vp, C.c_int, ip, ip, dp, dp, ip]
         L.gf_beam_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
                                                C.c_double, C.c_double, dp, dp]
         L.gf_batch_assemble_csr.argtypes = [vp, C.c_int, ip, ip, dp, dp, ip]
@@ -194,6 +196,22 @@ class Context:
         self.check(self.L.gf_band_solve(self.h, n, kl, ku, _dp(ab), ldab, _dp(x), C.byref(info)), "gf_band_solve")
         return x, info.value
 
+    def sparse_solve(self, row_ptr, col_idx, val, b):
+        """gf_sparse_solve: K x = b for K in 0-based row-major CSR; returns
+        (x, info)."""
+        n = len(b)
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+        ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        if len(rp) != n + 1 or len(ci) != rp[-1] or len(v) != rp[-1]:
+            raise ValueError("CSR arrays do not match n and nnz")
+        x = np.ascontiguousarray(b, dtype=np.float64).copy()
+        info = C.c_int(0)
+        ip = C.POINTER(C.c_int)
+        self.check(self.L.gf_sparse_solve(self.h, n, rp.ctypes.data_as(ip), ci.ctypes.data_as(ip), _dp(v), _dp(x),
+                                          C.byref(info)), "gf_sparse_solve")
+        return x, info.value
+
     def band_solve_noalloc(self, ab, kl, ku, b):
         """gf_band_solve_noalloc: band_solve through the static device scratch."""
         ab = np.ascontiguousarray(ab, dtype=np.float64)
@@ -236,11 +254,18 @@ class BatchSolver:
         self.ctx.check(self.ctx.L.gf_batch_run(self.h), "gf_batch_run")
         return self.ctx.L.gf_batch_last_ms(self.h)
 
+    def host_ms(self):
+        """Host wall time (ms) of the batch: model work, device allocation and
+        uploads of gf_batch_create, graph capture, the last results read."""
+        ms = (C.c_double * 5)()
+        self.ctx.check(self.ctx.L.gf_batch_host_ms(self.h, ms, 5), "gf_batch_host_ms")
+        return dict(zip(("build", "alloc", "upload", "graph", "results"), list(ms)))
+
     def launches(self):
         return self.ctx.L.gf_batch_last_launches(self.h)
 
     def results(self):
-        outs = [np.zeros((s.n_nodes, 15)) for s in self.structures]
+        outs = [np.empty((s.n_nodes, 15)) for s in self.structures]
         ptrs = (C.POINTER(C.c_double) * len(outs))(*[_dp(o) for o in outs])
         stats = (gf_stats * len(outs))()
         self.ctx.check(self.ctx.L.gf_batch_results(self.h, ptrs, stats), "gf_batch_results")
@@ -272,15 +297,19 @@ class BatchSolver:
         return rp, ci, v, P
 
 
-def solve(structures, precision=GF_PREC_FP64, device=0):
+def solve(structures, precision=GF_PREC_FP64, device=0, timings=None):
     """Solves every structure's solution step on the GPU; returns final nodal
     states (n_nodes x 15 each) and stats rows (converged steps, Newton
-    iterations, bisections, aborted)."""
+    iterations, bisections, aborted).  A dict passed as `timings` receives
+    the device time of the run and the host-time split of gf_batch_host_ms
+    (ms)."""
     ctx = Context(device)
     b = BatchSolver(ctx, structures, ctx.opts(precision))
     b.reset()
-    b.run()
+    dev_ms = b.run()
     out = b.results()
+    if timings is not None:
+        timings.update(b.host_ms(), device_run=dev_ms)
     b.close()
     ctx.close()
     return out

@@ -31,9 +31,9 @@
  *                           src/BandMatrix.cpp:221-250)
  *   gf_batch_assemble_csr   the same into the SparseMatrix CSR layout
  *                           (src/SparseMatrix.cpp:58-71)
- *   gf_band_solve           bandsystem (src/BandMatrix.cpp:257-287) and the
- *                           Newton solve sparsesystem (src/SparseMatrix.cpp:74-166)
- *                           for banded K_AA
+ *   gf_band_solve           bandsystem (src/BandMatrix.cpp:257-287)
+ *   gf_sparse_solve         the Newton solve sparsesystem
+ *                           (src/SparseMatrix.cpp:74-166) on SparseMatrix's CSR
  */
 #ifndef GIRAFFE_GPU_H
 #define GIRAFFE_GPU_H
@@ -185,10 +185,23 @@ int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double
 
 /* Solves A x = b for a banded matrix given in the reference's BandMatrix
  * storage (LAPACK GB: entry (i,j) at ab[(kl+ku+i-j) + j*ldab], ldab >=
- * 2*kl+ku+1), without pivoting, FP64; kl, ku <= 17.  b is overwritten by x.
- * *info receives 0 or 1 (zero or non-finite pivot), as bandsystem's
- * info_fail. */
+ * 2*kl+ku+1), without pivoting, FP64.  kl, ku <= 17 run on the 35-row band
+ * solver; wider bands on the blocked wide-band LU with half-bandwidth
+ * max(kl, ku).  b is overwritten by x.  *info receives 0 or 1 (zero or
+ * non-finite pivot), as bandsystem's info_fail. */
 int gf_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
+
+/* Replaces sparsesystem (src/SparseMatrix.cpp:74-166, the Newton step's
+ * solve) for one system K x = b, K in SparseMatrix's layout: Eigen
+ * row-major CSR, 0-based (row_ptr[n+1], col_idx[nnz], val[nnz]; entries
+ * repeated within a row are summed).  The unknowns are ordered by the
+ * narrower of their natural order and reverse Cuthill-McKee on the
+ * symmetrised pattern; the factorization is the no-pivot banded LU of
+ * gf_band_solve on the GPU, FP64.  b (n) is overwritten by x.  *info
+ * receives 0 or 1 (zero or non-finite pivot), as sparsesystem's info_fail;
+ * the return value reports argument and CUDA errors. */
+int gf_sparse_solve(gf_ctx* ctx, int n, const int* row_ptr, const int* col_idx, const double* val, double* b,
+                    int* info);
 
 /* Device bytes a batch of these n structures holds (gf_batch_create's
  * allocations, each rounded to 256 bytes); checks the descriptions as
