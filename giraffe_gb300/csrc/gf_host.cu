@@ -296,9 +296,20 @@ template <typename T, typename A> bool upload(gf_batch* B, T** p, const std::vec
   if (!balloc(B, p, v.size())) return false;
   B->h2d_bytes += (long long)(v.size() * sizeof(T));
   if (!v.empty() && !B->count_only) {
-    // pageable source: staged before return, ordered on the batch's stream
+    // through pinned staging when the batch has some (the copy then does not
+    // wait for other streams' work); else from the pageable source, staged
+    // by the driver before return; ordered on the batch's stream
     const double t0 = host_now_ms();
-    cudaError_t e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, B->stream);
+    const size_t bytes = v.size() * sizeof(T);
+    void* src = const_cast<T*>(v.data());
+    if (B->host_stage) {
+      if (void* h = B->host_stage->alloc(bytes)) {
+        std::memcpy(h, v.data(), bytes);
+        B->staged.push_back(h);
+        src = h;
+      }
+    }
+    cudaError_t e = cudaMemcpyAsync(*p, src, bytes, cudaMemcpyHostToDevice, B->stream);
     B->host_ms[2] += host_now_ms() - t0;
     if (e != cudaSuccess) return set_err(B->ctx, "upload failed: %s", cudaGetErrorString(e));
   }
@@ -931,7 +942,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       return GF_ERR_CUDA;
   }
   if (!wide_structs.empty()) {
-    if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total)) return GF_ERR_CUDA;
+    if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total) ||
+        !balloc(B, &sd.panel, 1))
+      return GF_ERR_CUDA;
     if (!B->count_only) {
       for (auto& a : sd.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
       for (auto& e : sd.evt) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

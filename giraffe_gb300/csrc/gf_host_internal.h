@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -19,15 +20,19 @@ struct gf_ctx {
   std::string err;
 };
 
-// First-fit sub-allocator over one device allocation: the served path's HBM
-// budget.  Blocks are 256-byte aligned; freeing merges neighbours.
+// First-fit sub-allocator over one allocation (the served path's device
+// budget, or its pinned host staging).  Blocks are 256-byte aligned;
+// freeing merges neighbours.  Thread-safe: the served path's builder thread
+// allocates while the polling thread frees.
 struct DevArena {
   char* base = nullptr;
   size_t size = 0;
   std::map<size_t, size_t> free_blocks;  // offset -> bytes
   std::map<size_t, size_t> used;         // offset -> bytes
   size_t in_use = 0;
+  mutable std::mutex mu;
   void init(void* p, size_t n) {
+    std::lock_guard<std::mutex> g(mu);
     base = static_cast<char*>(p);
     size = n;
     free_blocks.clear();
@@ -36,6 +41,7 @@ struct DevArena {
     if (n) free_blocks[0] = n;
   }
   void* alloc(size_t n) {
+    std::lock_guard<std::mutex> g(mu);
     n = (std::max<size_t>(n, 1) + 255) / 256 * 256;
     for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
       if (it->second < n) continue;
@@ -49,6 +55,7 @@ struct DevArena {
     return nullptr;
   }
   void release(void* p) {
+    std::lock_guard<std::mutex> g(mu);
     auto it = used.find(static_cast<size_t>(static_cast<char*>(p) - base));
     if (it == used.end()) return;
     size_t off = it->first, n = it->second;
@@ -70,9 +77,14 @@ struct DevArena {
     free_blocks[off] = n;
   }
   size_t largest_free() const {
+    std::lock_guard<std::mutex> g(mu);
     size_t m = 0;
     for (const auto& f : free_blocks) m = std::max(m, f.second);
     return m;
+  }
+  size_t bytes_in_use() const {
+    std::lock_guard<std::mutex> g(mu);
+    return in_use;
   }
 };
 
@@ -96,6 +108,8 @@ struct gf_batch {
   gf::Batch b{};
   cudaStream_t stream = nullptr;  // the context's stream, or a served wave's own
   DevArena* arena = nullptr;      // served waves: allocations come from the server's budget
+  DevArena* host_stage = nullptr; // served waves: pinned staging for the uploads
+  std::vector<void*> staged;      // staging blocks in use until the uploads land
   bool count_only = false;        // size the batch without touching the device
   size_t counted_bytes = 0;
   // host copies needed for results and resets

@@ -9,14 +9,23 @@
 // an event after each chunk.  Two chunks stay in flight per wave, so the
 // device works while the host reads the older chunk's state.  A structure
 // whose state reads DONE or ABORTED has its nodal result copied out on a
-// separate stream (no kernel writes a finished structure's nodes again) and
-// is reported at once; the wave's memory returns to the budget when its last
-// structure is done and no chunk of it is in flight.
+// separate stream (no kernel writes a finished structure's nodes again) into
+// pinned staging, and is reported once that copy has landed; the wave's
+// memory returns to the budget when its last structure is reported and no
+// chunk of it is in flight.  Every host<->device copy of the served path
+// goes through the pinned staging pool, because copies to or from pageable
+// memory block the host until the device's other work lets them through,
+// which stalls the polling loop behind long Shell_1 passes.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/giraffe_gpu.h"
@@ -47,7 +56,11 @@ struct Wave {
   gf_batch* B = nullptr;
   int slot = -1;
   std::vector<Request> reqs;
-  std::vector<char> reported;
+  std::vector<char> reported;  // 0 running, 1 reported, 2 result copy pending
+  int pending = 0;             // result copies not yet landed
+  size_t reserved = 0;         // budget bytes set aside at admission
+  int build_status = GF_OK;    // set by the builder thread
+  std::string build_err;
   int inflight = 0;  // chunks enqueued and not yet read (0..2)
   int head = 0;      // buffer (0/1) of the oldest in-flight chunk
   bool finishing = false;
@@ -59,6 +72,32 @@ struct Wave {
 constexpr long long kMaxWavePasses = 4000000;
 // Slack added to each wave's size: the batch's own 256-byte roundings.
 constexpr size_t kWaveSlack = 1 << 16;
+// Pinned host staging shared by the uploads of new waves and the result
+// copies; a copy that finds no room waits (results) or goes through
+// pageable memory (uploads).
+constexpr size_t kHostStage = (size_t)256 << 20;
+
+// Handles of a retired Shell_1 wave kept until the device is idle:
+// destroying an executable graph with conditional nodes waits for the
+// device's other work, which would stall the polling loop behind the
+// running waves.
+struct Parked {
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t evt[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+// Parked handles beyond this many are destroyed at once, waiting or not.
+constexpr size_t kMaxParked = 64;
+
+// A finished structure's nodal result on its way to the caller: issued
+// (host != nullptr) once staging room is free, reported when ev completes.
+struct PendingResult {
+  Wave* w = nullptr;
+  int s = 0;
+  StructState st{};
+  char* host = nullptr;
+  cudaEvent_t ev = nullptr;
+};
 
 }  // namespace
 
@@ -74,6 +113,23 @@ struct gf_server {
   int* pin_running = nullptr;         // [slot][2], pinned
   cudaStream_t copy_stream = nullptr;
   cudaStream_t capture_stream = nullptr;
+  void* stage_mem = nullptr;  // pinned, kHostStage bytes
+  DevArena stage;             // first-fit over stage_mem
+  std::deque<PendingResult> pending;
+  std::vector<Parked> parked;
+  // Builder thread: builds admitted waves (batch build, uploads, graph
+  // capture and instantiation, reset), so that the polling thread never
+  // waits on them.  Instantiating a Shell_1 pass graph of thousands of
+  // launches can take hundreds of milliseconds while other waves run.
+  gf_ctx build_ctx;           // the builder's error text
+  std::thread builder;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Wave*> jobs;     // admitted, to build
+  std::vector<Wave*> built;   // built (or failed), to pick up
+  bool stop = false;
+  int building = 0;           // admitted waves not yet picked up (polling thread)
+  size_t reserved = 0;        // their budget bytes (polling thread)
   std::deque<Request> queue;
   std::vector<Wave*> waves;
   std::deque<gf_server_result> done;
@@ -83,11 +139,13 @@ struct gf_server {
 
 namespace {
 
-// Slot kinds: with more than one slot, the upper half (at least one slot)
-// takes Shell_1 waves and the rest beam waves.
+// Slot kinds: with more than one slot, the upper third (at least one slot)
+// takes Shell_1 waves and the rest beam waves.  A Shell_1 wave holds many
+// plates at once (its LU kernels run them side by side) for seconds; beam
+// waves are short and many.
 bool slot_for_wide(const gf_server* S, int i) {
   int W = S->o.max_waves;
-  return W > 1 && i >= W - W / 2;
+  return W > 1 && i >= W - std::max(1, W / 3);
 }
 
 StructState* state_buf(gf_server* S, int slot, int k) {
@@ -118,19 +176,70 @@ void report(gf_server* S, Wave& w, int s, const StructState* st, int status) {
   S->reported++;
 }
 
-// Copies structure s's final nodal state (position + rotation vector, then
-// Q row-major: 15 doubles per node) into the caller's array.
-int copy_result(gf_server* S, Wave& w, int s) {
+// Queues structure s's nodal result for copying out (its final state st).
+void start_result(gf_server* S, Wave& w, int s, const StructState& st) {
+  PendingResult p;
+  p.w = &w;
+  p.s = s;
+  p.st = st;
+  w.reported[s] = 2;
+  w.pending++;
+  S->pending.push_back(p);
+}
+
+// Issues the D->H copies of queued results while staging room lasts: the
+// structure's nodes (position + rotation vector, 6 doubles each) and Q (9
+// each) into pinned memory, then an event.
+int issue_results(gf_server* S) {
   gf_ctx* ctx = S->ctx;
-  const StructInfo& inf = w.B->info[s];
-  double* out = w.reqs[s].out;
-  if (!out || inf.n_nodes == 0) return GF_OK;
-  const Batch& b = w.B->b;
-  GF_CK(cudaMemcpy2DAsync(out, 15 * sizeof(double), b.copy + (size_t)inf.node_off * 6, 6 * sizeof(double),
-                          6 * sizeof(double), (size_t)inf.n_nodes, cudaMemcpyDeviceToHost, S->copy_stream));
-  GF_CK(cudaMemcpy2DAsync(out + 6, 15 * sizeof(double), b.Qn + (size_t)inf.node_off * 9, 9 * sizeof(double),
-                          9 * sizeof(double), (size_t)inf.n_nodes, cudaMemcpyDeviceToHost, S->copy_stream));
-  GF_CK(cudaStreamSynchronize(S->copy_stream));
+  for (PendingResult& p : S->pending) {
+    if (p.host) continue;
+    const StructInfo& inf = p.w->B->info[p.s];
+    const size_t nn = (size_t)inf.n_nodes;
+    if (!p.w->reqs[p.s].out || nn == 0) continue;  // nothing to copy; completed below
+    char* h = static_cast<char*>(S->stage.alloc(sizeof(double) * 15 * nn));
+    if (!h) break;  // keep arrival order: wait for room
+    p.host = h;
+    const Batch& b = p.w->B->b;
+    double* hd = reinterpret_cast<double*>(h);
+    GF_CK(cudaMemcpyAsync(hd, b.copy + (size_t)inf.node_off * 6, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost,
+                          S->copy_stream));
+    GF_CK(cudaMemcpyAsync(hd + 6 * nn, b.Qn + (size_t)inf.node_off * 9, sizeof(double) * 9 * nn,
+                          cudaMemcpyDeviceToHost, S->copy_stream));
+    GF_CK(cudaEventCreateWithFlags(&p.ev, cudaEventDisableTiming));
+    GF_CK(cudaEventRecord(p.ev, S->copy_stream));
+  }
+  return GF_OK;
+}
+
+// Reports the results whose copies have landed (in order), interleaving
+// them into the caller's arrays (15 doubles per node).
+int complete_results(gf_server* S) {
+  gf_ctx* ctx = S->ctx;
+  while (!S->pending.empty()) {
+    PendingResult& p = S->pending.front();
+    Wave& w = *p.w;
+    const Request& r = w.reqs[p.s];
+    const size_t nn = (size_t)w.B->info[p.s].n_nodes;
+    const bool copy = r.out && nn > 0;
+    if (copy) {
+      if (!p.host) break;
+      cudaError_t q = cudaEventQuery(p.ev);
+      if (q == cudaErrorNotReady) break;
+      GF_CK(q);
+      const double* x = reinterpret_cast<const double*>(p.host);
+      const double* Q = x + 6 * nn;
+      for (size_t i = 0; i < nn; ++i) {
+        std::memcpy(r.out + 15 * i, x + 6 * i, 6 * sizeof(double));
+        std::memcpy(r.out + 15 * i + 6, Q + 9 * i, 9 * sizeof(double));
+      }
+      S->stage.release(p.host);
+      cudaEventDestroy(p.ev);
+    }
+    report(S, w, p.s, &p.st, GF_OK);
+    w.pending--;
+    S->pending.pop_front();
+  }
   return GF_OK;
 }
 
@@ -139,7 +248,14 @@ int enqueue_chunk(gf_server* S, Wave& w) {
   cudaStream_t st = S->streams[w.slot];
   const int k = (w.head + w.inflight) & 1;
   const Batch& b = w.B->b;
-  for (int p = 0; p < S->o.passes_per_chunk; ++p) GF_CK(cudaGraphLaunch(w.B->graph, st));
+  for (int p = 0; p < S->o.passes_per_chunk; ++p) {
+    if (w.B->graph) {
+      GF_CK(cudaGraphLaunch(w.B->graph, st));
+    } else {
+      launch_iteration(b, st);
+      GF_CK(cudaGetLastError());
+    }
+  }
   GF_CK(cudaMemcpyAsync(running_buf(S, w.slot, k), b.running, sizeof(int), cudaMemcpyDeviceToHost, st));
   GF_CK(cudaMemcpyAsync(state_buf(S, w.slot, k), b.state, sizeof(StructState) * (size_t)b.n_struct,
                         cudaMemcpyDeviceToHost, st));
@@ -164,11 +280,7 @@ int read_chunk(gf_server* S, Wave& w, bool* progressed) {
   const int running = *running_buf(S, w.slot, k);
   for (int s = 0; s < (int)w.reqs.size(); ++s) {
     if (w.reported[s]) continue;
-    if (st[s].phase == PH_DONE || st[s].phase == PH_ABORTED) {
-      int r = copy_result(S, w, s);
-      if (r != GF_OK) return r;
-      report(S, w, s, &st[s], GF_OK);
-    }
+    if (st[s].phase == PH_DONE || st[s].phase == PH_ABORTED) start_result(S, w, s, st[s]);
   }
   w.head ^= 1;
   w.inflight--;
@@ -182,11 +294,37 @@ int read_chunk(gf_server* S, Wave& w, bool* progressed) {
   return GF_OK;
 }
 
+void destroy_parked(Parked& p) {
+  if (p.graph) cudaGraphExecDestroy(p.graph);
+  for (auto& a : p.aux)
+    if (a) cudaStreamDestroy(a);
+  for (auto& e : p.evt)
+    if (e) cudaEventDestroy(e);
+}
+
+// Destroys the parked handles (the device is idle, or too many wait).
+void reap(gf_server* S) {
+  for (Parked& p : S->parked) destroy_parked(p);
+  S->parked.clear();
+}
+
 void retire(gf_server* S, size_t i) {
   Wave* w = S->waves[i];
   for (int s = 0; s < (int)w->reqs.size(); ++s)
     if (!w->reported[s]) report(S, *w, s, nullptr, GF_ERR_TIMEOUT);
-  gf_batch_destroy(w->B);  // returns its arena blocks
+  gf_batch* B = w->B;
+  if (B->b.sh.loops_in_graph) {
+    Parked p;
+    std::swap(p.graph, B->graph);
+    for (int k = 0; k < 3; ++k) std::swap(p.aux[k], B->b.sh.aux[k]);
+    for (int k = 0; k < 5; ++k) std::swap(p.evt[k], B->b.sh.evt[k]);
+    S->parked.push_back(p);
+    if (S->parked.size() > kMaxParked) {
+      destroy_parked(S->parked.front());
+      S->parked.erase(S->parked.begin());
+    }
+  }
+  gf_batch_destroy(B);  // returns its arena blocks
   S->slot_busy[w->slot] = 0;
   delete w;
   S->waves.erase(S->waves.begin() + (long)i);
@@ -214,7 +352,8 @@ int admit_kind(gf_server* S, bool kind, bool* admitted) {
     if (ok) slot = i;
   }
   if (slot < 0) return GF_OK;
-  size_t free_bytes = S->arena.size - S->arena.in_use;
+  const size_t used = S->arena.bytes_in_use() + S->reserved;
+  const size_t free_bytes = used < S->arena.size ? S->arena.size - used : 0;
   size_t total = kWaveSlack;
   std::vector<int> pick;
   for (int i = 0; i < (int)S->queue.size() && (int)pick.size() < S->o.max_wave_structs; ++i) {
@@ -228,49 +367,110 @@ int admit_kind(gf_server* S, bool kind, bool* admitted) {
   if (take == 0) return GF_OK;
   Wave* w = new Wave();
   w->slot = slot;
-  for (int i : pick) w->reqs.push_back(S->queue[i]);
-  w->reported.assign(take, 0);
-  std::vector<gf_model_desc> models(take);
-  double t = now_ms();
-  for (int i = 0; i < take; ++i) {
-    models[i] = w->reqs[i].model;
-    w->reqs[i].t_admit = t;
+  w->reserved = total;
+  const double t = now_ms();
+  for (int i : pick) {
+    w->reqs.push_back(S->queue[i]);
+    w->reqs.back().t_admit = t;
   }
+  w->reported.assign(take, 0);
+  for (int k = take - 1; k >= 0; --k) S->queue.erase(S->queue.begin() + pick[k]);
+  S->slot_busy[slot] = 1;
+  S->in_flight_structs += take;
+  S->reserved += total;
+  S->building++;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    S->jobs.push_back(w);
+  }
+  S->cv.notify_one();
+  *admitted = true;
+  return GF_OK;
+}
+
+// Builder thread: the device batch of one admitted wave, built and captured
+// on the capture stream, reset on the wave's slot stream.
+void build_wave(gf_server* S, Wave& w) {
+  const int take = (int)w.reqs.size();
+  std::vector<gf_model_desc> models(take);
+  for (int i = 0; i < take; ++i) models[i] = w.reqs[i].model;
   gf_batch* B = new gf_batch();
-  B->ctx = ctx;
+  B->ctx = &S->build_ctx;
   gf_default_opts(&B->opts);
   B->opts.use_graph = 1;
   B->arena = &S->arena;
-  // build and capture on the idle capture stream, then run on the slot's
+  B->host_stage = &S->stage;
   B->stream = S->capture_stream;
   int r = build_batch(B, take, models.data());
-  // the uploads must land before the blocks are reused or the wave runs
+  B->b.sh.loops_in_graph = 1;
+  // the uploads must land before the staging blocks are reused
   if (cudaStreamSynchronize(S->capture_stream) != cudaSuccess && r == GF_OK) r = GF_ERR_CUDA;
+  for (void* h : B->staged) S->stage.release(h);
+  B->staged.clear();
+  B->host_stage = nullptr;
   if (r == GF_OK) {
     B->launches_per_pass = count_launches_per_pass(B);
     r = ensure_graph(B);
   }
-  if (r != GF_OK) {
-    gf_batch_destroy(B);
-    delete w;
-    // out of contiguous room: leave the queue as it is and retry when a
-    // wave retires; anything else is an error of the submitted structures
-    return S->waves.empty() ? r : GF_OK;
+  if (r == GF_OK) {
+    B->stream = S->streams[w.slot];
+    r = batch_reset(B);
   }
-  B->stream = S->streams[slot];
-  r = batch_reset(B);
   if (r != GF_OK) {
+    w.build_err = S->build_ctx.err;
     gf_batch_destroy(B);
-    delete w;
-    return r;
+    w.build_status = r;
+    return;
   }
-  w->B = B;
-  for (int k = take - 1; k >= 0; --k) S->queue.erase(S->queue.begin() + pick[k]);
-  S->slot_busy[slot] = 1;
-  S->in_flight_structs += take;
-  S->waves.push_back(w);
-  *admitted = true;
-  return GF_OK;
+  w.B = B;
+}
+
+void builder_main(gf_server* S) {
+  cudaSetDevice(S->ctx->device);
+  for (;;) {
+    Wave* w = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv.wait(lk, [S] { return S->stop || !S->jobs.empty(); });
+      if (S->stop) return;
+      w = S->jobs.front();
+      S->jobs.pop_front();
+    }
+    build_wave(S, *w);
+    std::lock_guard<std::mutex> g(S->mu);
+    S->built.push_back(w);
+  }
+}
+
+// Takes over the waves the builder has finished: built ones start running;
+// a failed one returns its structures to the head of the queue.  Running out
+// of contiguous room is retried once a wave retires; with nothing running or
+// building, the failure is the submitted structures' own and is returned.
+int pickup(gf_server* S) {
+  std::vector<Wave*> got;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    got.swap(S->built);
+  }
+  int r = GF_OK;
+  for (Wave* w : got) {
+    S->building--;
+    S->reserved -= w->reserved;
+    if (w->build_status == GF_OK) {
+      w->B->ctx = S->ctx;
+      S->waves.push_back(w);
+      continue;
+    }
+    for (int k = (int)w->reqs.size() - 1; k >= 0; --k) S->queue.push_front(w->reqs[k]);
+    S->slot_busy[w->slot] = 0;
+    S->in_flight_structs -= (int)w->reqs.size();
+    if (r == GF_OK && S->waves.empty() && S->building == 0) {
+      S->ctx->err = w->build_err;
+      r = w->build_status;
+    }
+    delete w;
+  }
+  return r;
 }
 
 int admit(gf_server* S, bool* admitted) {
@@ -321,21 +521,44 @@ gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts) {
   ok = ok && cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking) == cudaSuccess &&
        cudaStreamCreateWithFlags(&S->capture_stream, cudaStreamNonBlocking) == cudaSuccess &&
        cudaMallocHost(&S->pin_state, sizeof(StructState) * 2 * (size_t)W * S->o.max_wave_structs) == cudaSuccess &&
-       cudaMallocHost(&S->pin_running, sizeof(int) * 2 * (size_t)W) == cudaSuccess;
+       cudaMallocHost(&S->pin_running, sizeof(int) * 2 * (size_t)W) == cudaSuccess &&
+       cudaMallocHost(&S->stage_mem, kHostStage) == cudaSuccess;
+  if (ok) S->stage.init(S->stage_mem, kHostStage);
   if (!ok) {
     set_err(ctx, "gf_server_create: device set-up failed (budget %zu bytes): %s", S->o.hbm_budget,
             cudaGetErrorString(cudaGetLastError()));
     gf_server_destroy(S);
     return nullptr;
   }
+  S->build_ctx.device = ctx->device;
+  S->build_ctx.stream = S->capture_stream;
+  S->builder = std::thread(builder_main, S);
   return S;
 }
 
 void gf_server_destroy(gf_server* S) {
   if (!S) return;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    S->stop = true;
+  }
+  S->cv.notify_all();
+  if (S->builder.joinable()) S->builder.join();
+  for (Wave* w : S->jobs) delete w;
+  S->jobs.clear();
+  for (Wave* w : S->built) {
+    if (w->B) gf_batch_destroy(w->B);
+    delete w;
+  }
+  S->built.clear();
   for (cudaStream_t s : S->streams)
     if (s) cudaStreamSynchronize(s);
+  if (S->copy_stream) cudaStreamSynchronize(S->copy_stream);
+  for (PendingResult& p : S->pending)
+    if (p.ev) cudaEventDestroy(p.ev);
+  S->pending.clear();
   while (!S->waves.empty()) retire(S, S->waves.size() - 1);
+  reap(S);
   for (cudaStream_t s : S->streams)
     if (s) cudaStreamDestroy(s);
   for (cudaEvent_t e : S->events)
@@ -344,6 +567,7 @@ void gf_server_destroy(gf_server* S) {
   if (S->capture_stream) cudaStreamDestroy(S->capture_stream);
   if (S->pin_state) cudaFreeHost(S->pin_state);
   if (S->pin_running) cudaFreeHost(S->pin_running);
+  if (S->stage_mem) cudaFreeHost(S->stage_mem);
   if (S->arena_mem) cudaFree(S->arena_mem);
   delete S;
 }
@@ -371,14 +595,21 @@ int gf_server_submit(gf_server* S, const gf_model_desc* model, double* final_nod
 
 int gf_server_poll(gf_server* S, gf_server_result* results, int max_results, int* n_results) {
   if (!S) return GF_ERR_ARG;
-  int r = GF_OK;
-  // read finished chunks (every ready one), retire finished waves
-  for (size_t i = 0; i < S->waves.size();) {
+  int r = pickup(S);
+  if (r != GF_OK) return r;
+  if ((r = complete_results(S)) != GF_OK) return r;
+  // read finished chunks (every ready one), copy out finished structures,
+  // retire waves whose structures are all reported
+  for (size_t i = 0; i < S->waves.size(); ++i) {
     Wave& w = *S->waves[i];
     bool progressed = true;
     while (progressed && r == GF_OK) r = read_chunk(S, w, &progressed);
     if (r != GF_OK) return r;
-    if (w.finishing && w.inflight == 0) {
+  }
+  if ((r = issue_results(S)) != GF_OK || (r = complete_results(S)) != GF_OK) return r;
+  for (size_t i = 0; i < S->waves.size();) {
+    Wave& w = *S->waves[i];
+    if (w.finishing && w.inflight == 0 && w.pending == 0) {
       retire(S, i);
       continue;
     }
@@ -389,12 +620,14 @@ int gf_server_poll(gf_server* S, gf_server_result* results, int max_results, int
     r = admit(S, &admitted);
     if (r != GF_OK) return r;
   }
+  if ((r = pickup(S)) != GF_OK) return r;
   // keep two chunks in flight per running wave
   for (Wave* w : S->waves)
     while (!w->finishing && w->inflight < 2) {
       r = enqueue_chunk(S, *w);
       if (r != GF_OK) return r;
     }
+  if (S->waves.empty() && S->building == 0 && !S->parked.empty()) reap(S);
   int n = 0;
   while (results && n < max_results && !S->done.empty()) {
     results[n++] = S->done.front();
@@ -408,9 +641,9 @@ int gf_server_get_status(const gf_server* S, gf_server_status* st) {
   if (!S || !st) return GF_ERR_ARG;
   std::memset(st, 0, sizeof(*st));
   st->queued = (int)S->queue.size();
-  st->waves = (int)S->waves.size();
+  st->waves = (int)S->waves.size() + S->building;
   st->structures = S->in_flight_structs;
-  st->budget_in_use = S->arena.in_use;
+  st->budget_in_use = S->arena.bytes_in_use();
   st->passes = S->passes;
   st->launches = S->launches;
   st->reported = S->reported;

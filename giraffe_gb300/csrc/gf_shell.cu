@@ -28,6 +28,8 @@
 // (x = U^-1 y into P), one launch per panel each.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "gf_kernels.cuh"
 #include "gf_math.cuh"
 #include "gf_types.h"
@@ -632,6 +634,10 @@ __device__ __forceinline__ WB wb_of(const Batch& b, const StructInfo& inf) {
   return w;
 }
 constexpr int NB = GF_WB_NB;
+
+// Panel index of a wide-band kernel: p >= 0 as given; inside a captured
+// panel loop p = -1 - d, meaning the device counter plus d.
+__device__ __forceinline__ int wb_panel(const Batch& b, int p) { return p >= 0 ? p : *b.sh.panel + (-1 - p); }
 }  // namespace
 
 // zero the wide band of iterating structures
@@ -647,6 +653,8 @@ __global__ void k_wb_zero(Batch b) {
 
 // LU (no pivoting) of the diagonal block of panel p, in place.
 __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.x];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -689,6 +697,8 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
 // panel p.  16 rows (or columns) per CTA, 16 threads each splitting the
 // panel width; blockIdx.x < nrb: L21 row block, else U12 column block.
 __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -756,6 +766,8 @@ constexpr int UT = 32;
 // part: 0 every tile, 1 only the tiles of the next panel's diagonal block
 // (the first NB rows and columns of the window), 2 every other tile.
 __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.z];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -802,6 +814,8 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 // below the panel: P_i -= L21(i, :) y_p.  Every CTA solves the small
 // triangle redundantly; CTA 0 writes y_p.
 __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -845,6 +859,8 @@ __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
 // Backward substitution for panel p (last panel first): x_p = U11^-1 y_p into
 // P; then the rows above the panel: y_i -= U(i, panel) x_p.
 __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
   if (!wide_active(b, s)) return;
   const StructInfo& inf = b.info[s];
@@ -913,8 +929,102 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
 // The next panel's diagonal LU and the forward substitution run while the
 // bulk of the trailing update occupies the SMs; the backward substitution
 // follows the last panel.
+// Panel-loop control inside a captured pass: the counter's start value,
+// and the step at the end of each loop body, which also sets the loop's
+// condition (continue while the counter stays in [0, limit)).
+__global__ void k_wb_loop_set(int* counter, int v) { *counter = v; }
+__global__ void k_wb_loop_step(int* counter, int step, int limit, cudaGraphConditionalHandle h) {
+  const int c = *counter + step;
+  *counter = c;
+  cudaGraphSetConditional(h, (c >= 0 && c < limit) ? 1u : 0u);
+}
+
+namespace {
+// Appends a WHILE conditional node to the capture of st (its condition
+// starts at 1 on every launch) and returns its body graph, into which the
+// caller captures one loop iteration.
+cudaError_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+  if ((e = cudaGraphConditionalHandleCreate(h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = *h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, g, dv.data(), nullptr, dv.size(), &np)) != cudaSuccess) return e;
+  *body = np.conditional.phGraph_out[0];
+  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+}  // namespace
+
+// The panel loops as two graph-resident WHILE loops (forward: factor and
+// forward substitution, one panel per iteration; backward substitution, last
+// panel first), used when a served wave's pass is captured: the pass graph
+// then holds a dozen nodes whatever the panel count, instead of six launches
+// per panel, and instantiates in a millisecond even while other waves run
+// (a graph of thousands of launches took hundreds of milliseconds then, and
+// held up the server's other CUDA calls).  One iteration keeps the
+// lookahead of the launched form (next panel's diagonal LU and this panel's
+// forward step beside the trailing update); it ends with the counter step.
+// Each iteration costs a few microseconds more than the unrolled panel
+// sequence, so the batch path, which captures once on an idle device, keeps
+// the unrolled form.
+static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
+  const ShellData& sd = b.sh;
+  const int nw = sd.n_wide, mr = sd.max_kl, P = sd.max_panels;
+  const int tiles = (mr + UT - 1) / UT, ct = (NB + UT - 1) / UT, nrb = (mr + 15) / 16, rb = (mr + 255) / 256;
+  cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1];
+  cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
+  if (P <= 0) return cudaSuccess;
+  cudaError_t e;
+  cudaGraphConditionalHandle h;
+  cudaGraph_t body, done;
+  k_wb_loop_set<<<1, 1, 0, st>>>(sd.panel, 0);
+  k_wb_diag<<<nw, 256, 0, st>>>(b, 0);
+  if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
+  if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return e;
+  k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, sb>>>(b, -1);
+  cudaEventRecord(e_trsm, sb);
+  cudaStreamWaitEvent(s3, e_trsm, 0);
+  k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
+  cudaEventRecord(e_fwd, s3);
+  k_wb_update<<<dim3(ct, ct, nw), 256, 0, sb>>>(b, -1, 1);
+  cudaEventRecord(e_corner, sb);
+  cudaStreamWaitEvent(s2, e_corner, 0);
+  k_wb_diag<<<nw, 256, 0, s2>>>(b, -2);
+  cudaEventRecord(e_diag, s2);
+  k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, sb>>>(b, -1, 2);
+  cudaStreamWaitEvent(sb, e_diag, 0);
+  cudaStreamWaitEvent(sb, e_fwd, 0);
+  k_wb_loop_step<<<1, 1, 0, sb>>>(sd.panel, 1, P, h);
+  if ((e = cudaStreamEndCapture(sb, &done)) != cudaSuccess) return e;
+  k_wb_loop_set<<<1, 1, 0, st>>>(sd.panel, P - 1);
+  if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
+  if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return e;
+  k_wb_bwd<<<dim3(rb, nw), 256, 0, sb>>>(b, -1);
+  k_wb_loop_step<<<1, 1, 0, sb>>>(sd.panel, -1, P, h);
+  return cudaStreamEndCapture(sb, &done);
+}
+
 void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   if (b.sh.n_wide == 0) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!prof && b.sh.loops_in_graph && b.sh.panel && cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
+      cs == cudaStreamCaptureStatusActive) {
+    // an error here invalidates the capture, which the caller's end of
+    // capture reports
+    capture_wide_loops(b, st);
+    return;
+  }
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide;
   const int mr = sd.max_kl;  // largest kl over the wide structures
@@ -980,7 +1090,11 @@ int shell_launches_per_pass(const Batch& b) {
     n += 2;  // tangent + commit
     for (int c = 0; c < b.sh.n_colors; ++c) n += b.sh.color_off[c + 1] > b.sh.color_off[c];
   }
-  if (b.sh.n_wide) n += 1 + 6 * b.sh.max_panels;
+  // unrolled: the first diagonal LU, then per panel trsm, forward step,
+  // update corner + next diagonal + update rest (or one update for the
+  // last), backward step; graph loops: two loop-control kernels, the first
+  // diagonal LU, six kernels per forward iteration and two per backward one
+  if (b.sh.n_wide) n += b.sh.loops_in_graph ? 3 + 8 * b.sh.max_panels : 1 + 6 * b.sh.max_panels;
   return n;
 }
 }  // namespace gf

@@ -74,7 +74,7 @@ struct DevBufs {
 // Helper streams and events of the wide LU's lookahead; destroyed on scope
 // exit.
 struct Helpers {
-  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t evt[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   ~Helpers() {
     for (auto& a : aux)
@@ -127,7 +127,7 @@ struct WideBatch {
     sd.max_panels = inf.n_panels;
     sd.max_kl = w;
     sd.wband = wband;
-    for (int k = 0; k < 2; ++k) sd.aux[k] = hl.aux[k];
+    for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
     for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
     return true;
   }

@@ -213,9 +213,12 @@ struct ShellData {
   int color_off[17];
   int n_colors;
   double* wband;
+  int* panel;       // device panel counter of the captured panel loops
+  int loops_in_graph;  // capture the panel loops as graph WHILE loops (served waves)
   // host handles of the wide-band lookahead: two helper streams and the
-  // events that fork from and join into the pass's stream
-  cudaStream_t aux[2];
+  // events that fork from and join into the pass's stream; aux[2] roots the
+  // captured panel-loop bodies
+  cudaStream_t aux[3];
   cudaEvent_t evt[5];  // [1] after trsm, [2] after the corner update, [3] after diag, [4] end of forward
 };
 
