@@ -969,6 +969,20 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18) ||
       !balloc(B, &b.nodeK, (size_t)std::max(node_off, 1) * 9))
     return GF_ERR_CUDA;
+  // reduction chunks of k_residual / k_update
+  {
+    std::vector<int> cs, c0;
+    for (int s = 0; s < n; ++s) {
+      const int nf = B->info[s].n_free, nch = nf > 0 ? (nf + GF_RED_CHUNK - 1) / GF_RED_CHUNK : 1;
+      for (int k = 0; k < nch; ++k) {
+        cs.push_back(s);
+        c0.push_back(k * GF_RED_CHUNK);
+      }
+    }
+    b.n_chunks = (int)cs.size();
+    if (!upload(B, &b.chunk_struct, cs) || !upload(B, &b.chunk_start, c0) || !zeroed(B, &b.red, (size_t)n))
+      return GF_ERR_CUDA;
+  }
   b.full_band = 0;
   b.xref = B->copy0;
   if (B->count_only) return GF_OK;

@@ -69,6 +69,31 @@ __device__ Red3 block_red(Red3 v) {
 
 __device__ __forceinline__ bool nan_or_huge(double v) { return !(v == v) || v >= 1e300 || v <= -1e300; }
 
+// ---- reductions of one structure spread over several CTAs ----
+__device__ __forceinline__ int red_chunks(const StructInfo& inf) {
+  return inf.n_free > 0 ? (inf.n_free + GF_RED_CHUNK - 1) / GF_RED_CHUNK : 1;
+}
+// Max of non-negative doubles through their bit patterns (exact, so the
+// result does not depend on the order in which CTAs arrive).
+__device__ __forceinline__ void red_max(unsigned long long* p, double v) {
+  atomicMax(p, (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ double red_value(const unsigned long long* p) {
+  return __longlong_as_double((long long)*(volatile const unsigned long long*)p);
+}
+// Counts this CTA in; true in every thread of the CTA that arrives last, to
+// which the other CTAs' global writes are then visible (each thread fences
+// its own writes before the count).
+__device__ bool red_arrive(RedScratch& r, int n_chunks) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&r.ticket, 1) == n_chunks - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
 // UpdateDyn for one node (reference src/Dynamic.cpp:480-580): Newmark
 // velocity and acceleration of the free DOFs; the rotational ones are
 // transported by Q_delta.  Nodes have all rotations free or all fixed
@@ -407,15 +432,16 @@ __global__ void k_loads(Batch b) {
 // CheckResidualConvergence (reference src/ConvergenceCriteria.cpp:187-285,
 // 460-598).
 __global__ void k_residual(Batch b) {
-  int s = blockIdx.x;
+  const int s = b.chunk_struct[blockIdx.x];
   StructState& st = b.state[s];
   if (!iterating(st)) return;
   const StructInfo inf = b.info[s];
   const StructParams& p = b.params[s];
   double* P = b.P + inf.dof_off;
   const int* d6 = b.dof_node6 + inf.dof_off;
+  const int i1 = min(inf.n_free, b.chunk_start[blockIdx.x] + GF_RED_CHUNK);
   Red3 v{0.0, 0.0, 0};
-  for (int i = threadIdx.x; i < inf.n_free; i += blockDim.x) {
+  for (int i = b.chunk_start[blockIdx.x] + threadIdx.x; i < i1; i += blockDim.x) {
     double x = -1.0 * P[i];
     P[i] = x;
     double a = fabs(x);
@@ -424,6 +450,19 @@ __global__ void k_residual(Batch b) {
     else { if (a > v.b) v.b = a; }
   }
   Red3 r = block_red(v);
+  RedScratch& R = b.red[s];
+  if (threadIdx.x == 0) {
+    red_max(&R.a, r.a);
+    red_max(&R.b, r.b);
+    if (r.f) atomicOr(&R.f, 1);
+  }
+  if (!red_arrive(R, red_chunks(inf))) return;
+  if (threadIdx.x == 0) {
+    r.a = red_value(&R.a);
+    r.b = red_value(&R.b);
+    r.f = *(volatile int*)&R.f;
+    R = RedScratch{0ull, 0ull, 0ull, 0ull, 0, 0};
+  }
   if (threadIdx.x == 0) {
     if (st.it == 1) {
       double pf = st.force_crit, pm = st.moment_crit;
@@ -614,15 +653,16 @@ __global__ void __launch_bounds__(SOLVE_THREADS) k_band_solve(Batch b) {
 // UpdateDisps + CheckGLConvergence (reference src/Solution.cpp:390-423,
 // src/ConvergenceCriteria.cpp:289-458)
 __global__ void k_update(Batch b) {
-  int s = blockIdx.x;
+  const int s = b.chunk_struct[blockIdx.x];
   StructState& st = b.state[s];
   if (!iterating(st) || !st.need_solve) return;
   const StructInfo inf = b.info[s];
   const StructParams& p = b.params[s];
   const double* P = b.P + inf.dof_off;
   const int* d6 = b.dof_node6 + inf.dof_off;
+  const int i1 = min(inf.n_free, b.chunk_start[blockIdx.x] + GF_RED_CHUNK);
   Red3 inc{0.0, 0.0, 0}, val{0.0, 0.0, 0};
-  for (int i = threadIdx.x; i < inf.n_free; i += blockDim.x) {
+  for (int i = b.chunk_start[blockIdx.x] + threadIdx.x; i < i1; i += blockDim.x) {
     int q = d6[i];
     double x = P[i];
     double nv = b.disp[q] + x;
@@ -634,8 +674,26 @@ __global__ void k_update(Batch b) {
   }
   Red3 ri = block_red(inc);
   Red3 rv = block_red(val);
+  RedScratch& R = b.red[s];
+  if (threadIdx.x == 0) {
+    red_max(&R.a, ri.a);
+    red_max(&R.b, ri.b);
+    red_max(&R.va, rv.a);
+    red_max(&R.vb, rv.b);
+    if (ri.f) atomicOr(&R.f, 1);
+  }
+  if (!red_arrive(R, red_chunks(inf))) return;
+  // the last CTA: every increment of the structure is in place
   if (b.params[s].dynamic)
     for (int i = threadIdx.x; i < inf.n_nodes; i += blockDim.x) update_dyn_node(b, st.a, inf.node_off + i);
+  if (threadIdx.x == 0) {
+    ri.a = red_value(&R.a);
+    ri.b = red_value(&R.b);
+    rv.a = red_value(&R.va);
+    rv.b = red_value(&R.vb);
+    ri.f = *(volatile int*)&R.f;
+    R = RedScratch{0ull, 0ull, 0ull, 0ull, 0, 0};
+  }
   if (threadIdx.x == 0) {
     st.res_conv = 0;
     if (ri.f) st.diverged = 1;
@@ -844,7 +902,7 @@ void launch_iteration_partial(const Batch& b_in, cudaStream_t st) {
   launch_mount(b, st, nullptr);
   launch_shell_mount(b, st);
   k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
-  k_residual<<<ns, 256, 0, st>>>(b);
+  k_residual<<<b.n_chunks, 256, 0, st>>>(b);
 }
 
 static void set_attrs() {
@@ -893,11 +951,11 @@ void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, Laun
   launch_mount(b, st, prof);
   if (b.sh.n_shells) { ProfScope q(prof, st, KC_SHELL); launch_shell_mount(b, st); }
   { ProfScope q(prof, st, KC_LOADS); k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b); }
-  { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<ns, 256, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_RESIDUAL); k_residual<<<b.n_chunks, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_SOLVE); launch_band_solve(b, st); }
   if (b.chain.n_chain_elems) { ProfScope q(prof, st, KC_CHAIN); launch_chain_solve(b, b.chain, st); }
   if (b.sh.n_wide) launch_wide_solve(b, st, prof);
-  { ProfScope q(prof, st, KC_UPDATE); k_update<<<ns, 256, 0, st>>>(b); }
+  { ProfScope q(prof, st, KC_UPDATE); k_update<<<b.n_chunks, 256, 0, st>>>(b); }
   { ProfScope q(prof, st, KC_CONTROL); k_control<<<(ns + 127) / 128, 128, 0, st>>>(b); }
   if (commit_kernels) {
     if (b.n_elem) { ProfScope q(prof, st, KC_COMMIT_ELEMS); k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b); }

@@ -112,6 +112,19 @@ struct StructInfo {
 
 // Per-structure Newton / load-step control state (reference
 // src/Static.cpp:140-311 as a state machine).
+// DOFs per CTA of the residual and update reductions (k_residual,
+// k_update): a structure's free DOFs are split into chunks of this size,
+// at least one per structure.
+#define GF_RED_CHUNK 2048
+
+// Per-structure partial results of those reductions across their CTAs:
+// maxima of non-negative values as the bit patterns of the doubles (which
+// order as unsigned integers), the NaN flag, and the count of CTAs done.
+struct RedScratch {
+  unsigned long long a, b, va, vb;
+  int f, ticket;
+};
+
 struct StructState {
   int phase;
   int it;
@@ -279,6 +292,12 @@ struct Batch {
   int mixed;  // 1: Beam_1 tangent operator in FP32-pair arithmetic
   int max_refine;
   int* running;  // structures still running after the last pass
+  // reduction chunks: chunk k covers free DOFs [chunk_start[k],
+  // chunk_start[k] + GF_RED_CHUNK) of structure chunk_struct[k]
+  int n_chunks;
+  int* chunk_struct;
+  int* chunk_start;
+  RedScratch* red;  // [n_struct], zero between kernels
   ChainData chain;
   ShellData sh;
 };
