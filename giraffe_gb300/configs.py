@@ -92,10 +92,12 @@ def tutorial01() -> Structure:
     return s
 
 
-def tutorial10() -> Structure:
+def tutorial10(rayleigh_alpha: float = 0.0, rayleigh_beta: float = 0.0, update_rayleigh: int = 0) -> Structure:
     """The reference's tutorial10 deck: 5 Beam_1 elements, Dynamic step with a
     prescribed base motion (translations and an Euler-angle rotation about z),
-    Newmark beta = 0.3, gamma = 0.5."""
+    Newmark beta = 0.3, gamma = 0.5; optionally with Rayleigh damping
+    C = alpha M + beta K (formed once, or at every iteration with
+    update_rayleigh = 1)."""
     s = Structure(nodes=np.array([[0.0, 0.0, 0.1 * i] for i in range(11)]))
     s.nodes[:, 2] = [0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0]
     mat = s.add_material(1e7, 0.3, 2000)
@@ -109,7 +111,8 @@ def tutorial10() -> Structure:
         np.array([[0, 0, 0, 0, 0, 0], [0, 0.5, 0.25, 0, 0, 0], [0, 0, 0, 0, 0, 3.14],
                   [0, -0.5, -0.25, 0, 0, 0], [0, 0, 0, 0, 0, 0]], dtype=float))))
     s.solution = Solution(GF_DYNAMIC, 0.0, 10.0, 0.005, 0.005, 0.001, 20, 3, 4, 1.0, sample=10,
-                          beta=0.3, gamma=0.5)
+                          beta=0.3, gamma=0.5, rayleigh_alpha=rayleigh_alpha, rayleigh_beta=rayleigh_beta,
+                          update_rayleigh=update_rayleigh)
     return s
 
 
@@ -162,7 +165,8 @@ def served_chains(n_requests: int, seed: int = 0, dof_min: int = 1000, dof_max: 
 
 
 def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, steps: int = 1000,
-                dt: float = 0.01, element_length: float = 0.5, tol: float = 1e-8) -> Structure:
+                dt: float = 0.01, element_length: float = 0.5, tol: float = 1e-8, rayleigh_alpha: float = 0.0,
+                rayleigh_beta: float = 0.0, update_rayleigh: int = 0) -> Structure:
     L = n_el * element_length
     s = Structure(nodes=straight_chain(n_el, L, (0.0, 0.0, 1.0)))
     mat = s.add_material(E_STEEL, NU_STEEL, RHO_STEEL)
@@ -175,7 +179,8 @@ def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, st
     vals = np.zeros((steps + 1, 6))
     vals[:, 0] = amp * np.sin(2.0 * math.pi * t / period)
     s.displacements.append(NodalDisplacement([top], cs, Table(t, vals)))
-    s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 64, 20, 3, 4, 1.0, beta=0.25, gamma=0.5)
+    s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 64, 20, 3, 4, 1.0, beta=0.25, gamma=0.5,
+                          rayleigh_alpha=rayleigh_alpha, rayleigh_beta=rayleigh_beta, update_rayleigh=update_rayleigh)
     s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, force_min=1.0, moment_min=1.0)
     return s
 

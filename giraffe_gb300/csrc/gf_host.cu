@@ -368,10 +368,6 @@ void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
     P.err = strf("structure %d: unknown solution type", s);
     return;
   }
-  if (m.solution.type == GF_DYNAMIC && (m.solution.rayleigh_alpha != 0.0 || m.solution.rayleigh_beta != 0.0)) {
-    P.err = strf("structure %d: Rayleigh damping is not supported (alpha = beta = 0 required)", s);
-    return;
-  }
   if (m.n_shells && m.n_beams) {
     P.err = strf("structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
     return;
@@ -808,6 +804,13 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     p.disp_min = cr.disp_min;
     p.rot_min = cr.rot_min;
     p.divergence_ref = cr.divergence_ref;
+    if (so.type == GF_DYNAMIC && (so.rayleigh_alpha != 0.0 || so.rayleigh_beta != 0.0)) {
+      p.ray_on = 1;
+      p.ray_alpha = so.rayleigh_alpha;
+      p.ray_beta = so.rayleigh_beta;
+      p.ray_update = so.update_rayleigh ? 1 : 0;
+      b.any_rayleigh = 1;
+    }
   }
   b.n_struct = n;
   b.n_nodes = node_off;
@@ -967,7 +970,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !balloc(B, &b.band, (size_t)dof_off * GF_LDB) || !balloc(B, &b.U, (size_t)dof_off * GF_UW) ||
       !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
       !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18) ||
-      !balloc(B, &b.nodeK, (size_t)std::max(node_off, 1) * 9))
+      !balloc(B, &b.nodeK, (size_t)std::max(node_off, 1) * 9) ||
+      !balloc(B, &b.RD, b.any_rayleigh ? (size_t)elem_off * 324 : 1))
     return GF_ERR_CUDA;
   // reduction chunks of k_residual / k_update
   {
@@ -1010,7 +1014,7 @@ int count_launches_per_pass(const gf_batch* B) {
         chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
     }
   }
-  return 10 + colors + chain_launches + shell_launches_per_pass(B->b);
+  return 10 + colors + chain_launches + shell_launches_per_pass(B->b) + (B->b.any_rayleigh ? 1 : 0);
 }
 
 int batch_reset(gf_batch* B) {

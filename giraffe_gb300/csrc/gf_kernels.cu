@@ -347,8 +347,129 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     for (int I = 0; I < 3; ++I)
       beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
                        Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, ne);
+  // Rayleigh damping: on the iterations that form C_e, the stiffness part
+  // of K_e alone (no inertial terms) goes to the damping scratch, where
+  // k_beam_rayleigh turns it into C_e = alpha M_modal + beta K_e
+  if (dyn && pr.ray_on && (pr.ray_update || !b.state[s].ray_init)) {
+    double* Ce = b.RD + e;
+#pragma unroll 1
+    for (int J = 0; J < 3; ++J)
+#pragma unroll 1
+      for (int I = 0; I < 3; ++I)
+        beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ce, false, Dm,
+                         Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, 0.0, ne);
+  }
 #pragma unroll
   for (int q = 0; q < 18; ++q) b.Fe[q * ne + e] = f[q * MOUNT_THREADS];
+}
+
+// MountDamping and the damping part of MountDyn (reference
+// src/Beam_1.cpp:1641-1673).  On the iterations that form it (the step's
+// first, or every one with Update 1), C_e = alpha M_modal + beta K_e; the
+// modal mass is MountMassModal (src/Beam_1.cpp:1538-1553) with the
+// EvaluateMassModal operator (src/Beam_1.cpp:1681-1774) of a section
+// without a first moment of mass, blockdiag(Q Mr Q^T, Q Jr Q^T) with
+// Q = Q(alpha_i) at each Gauss point, summed as wJ N^T D N (w = 1) and
+// turned to the global frame block by block (T3^T B T3).  Every iteration
+// then adds a4 C_e to K_e and C_e v to f_e, v the nodes' current
+// velocities.  One thread per element; C_e is structure-of-arrays like K_e.
+__global__ void k_beam_rayleigh(Batch b) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= b.n_elem) return;
+  const int s = b.estruct[e];
+  const StructState& st = b.state[s];
+  if (!iterating(st)) return;
+  const StructParams& p = b.params[s];
+  if (!p.dynamic || !p.ray_on) return;
+  const int64_t ne = b.n_elem;
+  double* C = b.RD + e;
+  if (p.ray_update || !st.ray_init) {
+    const BeamConst& c = b.bconst[e];
+    const BeamHistAux& x = b.baux[e];
+    double D[2][2][9];  // [Gauss point][translation, rotation][3x3 row-major]
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      M3<double> Q = rodrigues(V3<double>{{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}});
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double mt = 0.0, jt = 0.0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            double qm = 0.0, qj = 0.0;
+#pragma unroll
+            for (int l = 0; l < 3; ++l) {
+              qm += Q[i * 3 + l] * (l == k ? c.Mr : 0.0);
+              qj += Q[i * 3 + l] * c.Jr[l * 3 + k];
+            }
+            mt += qm * Q[j * 3 + k];
+            jt += qj * Q[j * 3 + k];
+          }
+          D[g][0][i * 3 + j] = mt;
+          D[g][1][i * 3 + j] = jt;
+        }
+    }
+    const double* T = c.T3;
+#pragma unroll 1
+    for (int I = 0; I < 3; ++I)
+#pragma unroll 1
+      for (int J = 0; J < 3; ++J)
+#pragma unroll 1
+        for (int bi = 0; bi < 2; ++bi)
+#pragma unroll 1
+          for (int bj = 0; bj < 2; ++bj) {
+            double m[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) m[q] = 0.0;
+            if (bi == bj) {
+              double loc[9];
+#pragma unroll
+              for (int q = 0; q < 9; ++q) {
+                loc[q] = 0.0;
+#pragma unroll
+                for (int g = 0; g < 2; ++g) loc[q] += ((c.jac * c.N[g][I]) * D[g][bi][q]) * c.N[g][J];
+              }
+              double t2[9];  // loc T, then T^T (loc T)
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  t2[i * 3 + j] = loc[i * 3] * T[j] + loc[i * 3 + 1] * T[3 + j] + loc[i * 3 + 2] * T[6 + j];
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  m[i * 3 + j] = T[i] * t2[j] + T[3 + i] * t2[3 + j] + T[6 + i] * t2[6 + j];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int j = 0; j < 3; ++j) {
+                const int64_t xi = (6 * I + 3 * bi + i) + 18 * (6 * J + 3 * bj + j);
+                C[xi * ne] = p.ray_alpha * m[i * 3 + j] + p.ray_beta * C[xi * ne];
+              }
+          }
+  }
+  const double a4 = st.a[3];
+  double v[18];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const int64_t nd = b.enodes[3 * e + j];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) v[6 * j + q] = b.vel[nd * 6 + q];
+  }
+#pragma unroll 1
+  for (int q = 0; q < 18; ++q) {
+    double acc = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < 18; ++k) {
+      const double cq = C[(int64_t)(q + 18 * k) * ne];
+      acc += cq * v[k];
+      b.Ke[(int64_t)(q + 18 * k) * ne + e] += a4 * cq;
+    }
+    b.Fe[(int64_t)q * ne + e] += acc;
+  }
 }
 
 __global__ void k_beam_scatter(Batch b, int color) {
@@ -724,6 +845,7 @@ __global__ void k_control(Batch b) {
     return;
   }
   const StructParams& p = b.params[s];
+  if (p.ray_on) st.ray_init = 1;  // the step's first iteration has formed C
   int both = st.res_conv && st.gl_conv;
   if ((st.it == p.max_it && !both) || (st.need_solve && st.info_fail)) st.diverged = 1;
   if (st.time_step < p.min_time_step && st.time != p.end_time) st.aborted = 1;
@@ -933,6 +1055,7 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
       k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
     else
       k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+    if (b.any_rayleigh) k_beam_rayleigh<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
   }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];

@@ -89,6 +89,11 @@ struct StructParams {
   double beta, gamma;  // Newmark parameters
   double force_tol, moment_tol, force_min, moment_min, disp_tol, rot_tol, disp_min, rot_min,
       divergence_ref;
+  // Rayleigh damping of a Dynamic step (Beam_1::MountDamping): C_e = alpha
+  // M_modal + beta K_e, formed at the first Newton iteration of the step
+  // (or at every iteration with ray_update)
+  double ray_alpha, ray_beta;
+  int ray_on, ray_update;
 };
 
 // Per-structure ranges in the batch arrays.
@@ -134,6 +139,7 @@ struct StructState {
   int n_solves;  // linear solves performed
   int solve_sweeps;  // refinement sweeps of the last solve (mixed path)
   int fp64_fallback;  // mixed path: this structure factors in FP64
+  int ray_init;       // Rayleigh matrices formed (after the step's first iteration)
   double time, time_step, last_converged_time, current_time_step;
   double force_crit, moment_crit, disp_crit, rot_crit;
   double last_res, last_inc;
@@ -292,6 +298,10 @@ struct Batch {
   int mixed;  // 1: Beam_1 tangent operator in FP32-pair arithmetic
   int max_refine;
   int* running;  // structures still running after the last pass
+  // Rayleigh damping matrix per element (18x18, structure-of-arrays: entry
+  // x of element e at [x * n_elem + e]); allocated when any_rayleigh
+  double* RD;
+  int any_rayleigh;
   // reduction chunks: chunk k covers free DOFs [chunk_start[k],
   // chunk_start[k] + GF_RED_CHUNK) of structure chunk_struct[k]
   int n_chunks;

@@ -387,3 +387,46 @@ void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, c
   }
   if (kinetic) *kinetic = ke;
 }
+
+/* Beam_1::MountMassModal (reference src/Beam_1.cpp:1538-1553) for sections
+ * without a first moment of mass (br = 0: Hooke rectangles and tubes): at
+ * each Gauss point EvaluateMassModal (src/Beam_1.cpp:1681-1774) gives the
+ * 6x6 operator blockdiag(Q Mr Q^T, Q Jr Q^T), Q = Q(alpha_i) the Rodrigues
+ * rotation of the Gauss point's committed rotation vector and Mr = rho A I;
+ * the element sums wJ N^T D N (w = 1) and turns the 18x18 to the global
+ * frame as transform^T M transform.  M: 18x18 column-major. */
+void oracle_beam_modal_mass(const ob_const* c, const ob_hist* h, double* M) {
+  double Ml[18 * 18];
+  memset(Ml, 0, sizeof(Ml));
+  for (int g = 0; g < 2; ++g) {
+    double Q[9], t[9], Mt[9], Jt[9], Mr[9] = {c->Mr, 0, 0, 0, c->Mr, 0, 0, 0, c->Mr};
+    rodrigues_Q(Q, h->alpha[g]);
+    m3_mul(t, Q, Mr);
+    m3_mult(Mt, t, Q);
+    m3_mul(t, Q, c->Jr);
+    m3_mult(Jt, t, Q);
+    double D[36];
+    memset(D, 0, sizeof(D));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        D[i * 6 + j] = Mt[i * 3 + j];
+        D[(3 + i) * 6 + 3 + j] = Jt[i * 3 + j];
+      }
+    const double* N = c->N[g];
+    for (int I = 0; I < 3; ++I)
+      for (int J = 0; J < 3; ++J)
+        for (int i = 0; i < 6; ++i)
+          for (int j = 0; j < 6; ++j) Ml[(6 * I + i) + 18 * (6 * J + j)] += ((c->jac * N[I]) * D[i * 6 + j]) * N[J];
+  }
+  const double* T = c->T3;
+  for (int bi = 0; bi < 6; ++bi)
+    for (int bj = 0; bj < 6; ++bj) {
+      double blk[9], t2[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) blk[i * 3 + j] = Ml[(3 * bi + i) + 18 * (3 * bj + j)];
+      m3_mul(t2, blk, T);
+      m3_tmul(blk, T, t2);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[(3 * bi + i) + 18 * (3 * bj + j)] = blk[i * 3 + j];
+    }
+}

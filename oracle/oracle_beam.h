@@ -34,4 +34,7 @@ void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);
  * (18x18 column-major, global frame) and f. */
 void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, const double* vel,
                          const double* acc, const double* a, double* K, double* f, double* kinetic);
+/* Modal mass (MountMassModal) in the global frame, 18x18 column-major:
+ * the alpha term of Rayleigh damping. */
+void oracle_beam_modal_mass(const ob_const* c, const ob_hist* h, double* M);
 #endif

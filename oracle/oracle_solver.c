@@ -62,12 +62,20 @@ typedef struct {
   double last_converged_time, current_time_step;
   int dynamic;
   double a[6];  /* Newmark coefficients of the current step */
+  /* Rayleigh damping (Beam_1::MountDamping, reference
+   * src/Beam_1.cpp:1641-1665): C_e = alpha M_modal + beta K_e per element,
+   * formed at the first Newton iteration of the step (the Dynamic::Solve
+   * flag `first`) or at every iteration with Update 1 */
+  int ray, ray_update, ray_init;
+  double ray_alpha, ray_beta;
+  double* rd;   /* [nb][18x18] column-major */
 } ost;
 
 static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
   free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
+  free(s->rd);
 }
 
 /* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
@@ -204,13 +212,30 @@ static void assemble(ost* s) {
     for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
     oracle_beam_mount(s->bc + e, s->bh + e, d, K, f, NULL);
     if (s->dynamic) {
-      /* MountMass + MountDyn (reference src/Beam_1.cpp:1564-1638, 1668-1673) */
+      /* MountMass + MountDamping + MountDyn (reference
+       * src/Beam_1.cpp:1564-1673): K += M (+ a4 C), f += f_inertial (+ C v) */
       double v[18], ac[18];
       for (int j = 0; j < 3; ++j) {
         memcpy(v + 6 * j, s->copy_vel + 6 * b[j], 6 * sizeof(double));
         memcpy(ac + 6 * j, s->copy_accel + 6 * b[j], 6 * sizeof(double));
       }
+      double* rd = s->ray ? s->rd + (size_t)324 * e : NULL;
+      if (rd && (s->ray_update || !s->ray_init)) {
+        double Mm[324];
+        oracle_beam_modal_mass(s->bc + e, s->bh + e, Mm);
+        for (int x = 0; x < 324; ++x) rd[x] = s->ray_alpha * Mm[x] + s->ray_beta * K[x];
+      }
       oracle_beam_inertia(s->bc + e, s->bh + e, d, v, ac, s->a, K, f, NULL);
+      if (rd) {
+        double vi[18];
+        for (int j = 0; j < 3; ++j) memcpy(vi + 6 * j, s->vel + 6 * b[j], 6 * sizeof(double));
+        for (int x = 0; x < 324; ++x) K[x] += s->a[3] * rd[x];
+        for (int q = 0; q < 18; ++q) {
+          double acc = 0.0;
+          for (int k = 0; k < 18; ++k) acc += rd[q + 18 * k] * vi[k];
+          f[q] += acc;
+        }
+      }
     }
     int g[18];
     for (int a = 0; a < 18; ++a) g[a] = s->GL[6 * b[a / 6] + a % 6];
@@ -608,6 +633,7 @@ static int dynamic_solve(ost* s, oracle_record* rec, int* stats) {
     s->diverged = 0;
     while ((!res_conv || !gl_conv) && !s->diverged && !aborted) {
       assemble(s);
+      s->ray_init = 1;
       if (it == 1) establish_residual_criteria(s);
       res_conv = check_residual(s);
       int info_fail = 0;
@@ -665,10 +691,16 @@ static void final_state(ost* s, double* out) {
 
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
   if (m->n_shells && m->solution.type == GF_DYNAMIC) return -1;
-  if (m->solution.type == GF_DYNAMIC && (m->solution.rayleigh_alpha != 0.0 || m->solution.rayleigh_beta != 0.0)) return -1;
   ost s;
   ost_init(&s, m);
   s.dynamic = m->solution.type == GF_DYNAMIC;
+  if (s.dynamic && (m->solution.rayleigh_alpha != 0.0 || m->solution.rayleigh_beta != 0.0)) {
+    s.ray = 1;
+    s.ray_alpha = m->solution.rayleigh_alpha;
+    s.ray_beta = m->solution.rayleigh_beta;
+    s.ray_update = m->solution.update_rayleigh;
+    s.rd = calloc((size_t)324 * (s.nb ? s.nb : 1), sizeof(double));
+  }
   int r = s.dynamic ? dynamic_solve(&s, rec, stats) : static_solve(&s, rec, stats);
   final_state(&s, final_nodes);
   ost_free(&s);

@@ -19,6 +19,13 @@ stores what the reference computes:
 * ref_tutorial10.npz     the reference's tutorial10: Dynamic step (Newmark),
                          prescribed base translation and rotation, 2000 steps
                          (every 10th configuration, as the deck's Sample).
+* ref_tutorial10_rayleigh.npz, ref_tutorial10_rayleigh_update.npz
+                         tutorial10 with Rayleigh damping (alpha 0.2 1/s,
+                         beta 0.002 s): C formed at the first iteration
+                         (Update 0), and at every iteration (Update 1).
+* ref_riser_rayleigh.npz a 12-element riser under a prescribed top motion
+                         with Rayleigh damping (alpha 0.3, beta 0.004,
+                         Update 1), 120 steps.
 * ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
                          single elements (Beam_1::MountMass) with random
                          history, increments, nodal velocities/accelerations.
@@ -299,6 +306,11 @@ DECKS = {
     "ref_tutorial10.npz": configs.tutorial10,
     "ref_plate.npz": lambda: configs.square_plate(4, steps=20),
     "ref_plate_fixed_area.npz": lambda: configs.square_plate(3, steps=10, area_update=0),
+    "ref_tutorial10_rayleigh.npz": lambda: configs.tutorial10(0.2, 0.002, 0),
+    "ref_tutorial10_rayleigh_update.npz": lambda: configs.tutorial10(0.2, 0.002, 1),
+    "ref_riser_rayleigh.npz": lambda: configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0,
+                                                          rayleigh_alpha=0.3, rayleigh_beta=0.004,
+                                                          update_rayleigh=1),
 }
 
 

@@ -90,6 +90,23 @@ def test_tutorial10_dynamics_matches_reference(golden):
     _check_run(golden("ref_tutorial10.npz"), configs.tutorial10(), tol=1e-10)
 
 
+@pytest.mark.parametrize("name,update", [("ref_tutorial10_rayleigh.npz", 0), ("ref_tutorial10_rayleigh_update.npz", 1)])
+def test_tutorial10_rayleigh_matches_reference(golden, name, update):
+    """Rayleigh damping C = alpha M_modal + beta K (MountDamping), formed at
+    the first iteration (Update 0) or at every iteration (Update 1); the
+    damped motion differs from the undamped one by far more than the
+    tolerance."""
+    final, _, _ = _check_run(golden(name), configs.tutorial10(0.2, 0.002, update), tol=1e-10)
+    undamped = golden("ref_tutorial10.npz")["nodes"][-1]
+    assert np.abs(final[:, :3] - undamped[:, :3]).max() > 1e-4 * np.abs(undamped[:, :3]).max()
+
+
+def test_riser_rayleigh_matches_reference(golden):
+    _check_run(golden("ref_riser_rayleigh.npz"),
+               configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0, rayleigh_alpha=0.3,
+                                   rayleigh_beta=0.004, update_rayleigh=1), tol=1e-10)
+
+
 def test_rollup_known_answer():
     """An end moment 2 pi E I / L rolls the cantilever into a circle: at load
     factor t the tip is at (L sin(th)/th, L (1 - cos(th))/th) with th = 2 pi t."""
