@@ -302,6 +302,13 @@ class Structure:
         return DescHandle(self)
 
     # ---- deck in the reference's syntax ----
+    @staticmethod
+    def from_inp(text: str, step: int = 1) -> "Structure":
+        """The structure and solution step of a deck in the reference's .inp
+        syntax (giraffe_gb300.deck.read_deck)."""
+        from .deck import read_deck
+        return read_deck(text, step)
+
     def to_inp(self) -> str:
         o = []
         s = self.solution

@@ -1,0 +1,104 @@
+"""The .inp reader (giraffe_gb300.deck) against the writer and, where the
+reference tree is present, against the reference's own tutorial decks read
+as text.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from giraffe_gb300 import configs
+from giraffe_gb300.deck import DeckError, read_deck, read_deck_file
+from giraffe_gb300.model import NodalLoad
+
+REF_INPUTS = "/root/reference/inputs"
+
+
+def same_structure(a, b):
+    assert np.array_equal(np.asarray(a.nodes), np.asarray(b.nodes))
+    assert a.materials == b.materials
+    assert a.sections == b.sections
+    assert a.shell_sections == b.shell_sections
+    assert a.cs == b.cs
+    assert np.array_equal(a.beams.array(), b.beams.array())
+    assert np.array_equal(a.shells.array(), b.shells.array())
+    if a.constraints is None or b.constraints is None:
+        assert a.constraints is None and b.constraints is None or \
+            not np.asarray(a.constraints if a.constraints is not None else b.constraints).any()
+    else:
+        assert np.array_equal(np.asarray(a.constraints), np.asarray(b.constraints))
+    assert len(a.loads) == len(b.loads)
+    for x, y in zip(a.loads, b.loads):
+        assert type(x) is type(y)
+        if isinstance(x, NodalLoad):
+            assert list(x.nodes) == list(y.nodes) and x.cs == y.cs
+        else:
+            assert list(x.shells) == list(y.shells) and int(x.area_update) == int(y.area_update)
+        assert np.array_equal(x.table.times, y.table.times)
+        assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
+    assert len(a.displacements) == len(b.displacements)
+    for x, y in zip(a.displacements, b.displacements):
+        assert list(x.nodes) == list(y.nodes) and x.cs == y.cs
+        assert np.array_equal(x.table.times, y.table.times)
+        assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
+    assert a.solution == b.solution
+    assert {k: float(v) for k, v in a.criteria.items()} == {k: float(v) for k, v in b.criteria.items()}
+
+
+@pytest.mark.parametrize("make", [
+    configs.tutorial01, configs.cantilever_rollup, lambda: configs.tutorial10(0.2, 0.002, 1),
+    lambda: configs.pipe_chain(25, 0.4, 0.03, [1e5, -2e4, 3e4]),
+    lambda: configs.riser_chain(15, 0.35, 0.025, 1.0, 6.0, steps=30),
+    lambda: configs.square_plate(3, steps=10, area_update=0), lambda: configs.square_plate(4, steps=20),
+])
+def test_written_deck_reads_back_the_same(make):
+    s = make()
+    same_structure(read_deck(s.to_inp()), s)
+
+
+def test_sets_by_sequence_comments_and_skipped_blocks():
+    s = configs.pipe_chain(4, 0.4, 0.03, [1e5, 0.0, 0.0])
+    text = s.to_inp()
+    # a node set written as a sequence, comments, and output blocks
+    first = text.splitlines()
+    k = next(i for i, ln in enumerate(first) if ln.startswith("NodeSet\t1\t"))
+    first[k] = "NodeSet\t1\tNodes\t1\tSequence\tInitial\t1\tIncrement\t1   // the clamped end"
+    text = "// header comment\n" + "\n".join(first) + "\nMonitor\tSample\t1\nMonitorNodes\t1\t9\n" \
+        "PostFiles\nMagFactor\t1\nWriteMesh\t1\nContacts\t0\n"
+    same_structure(read_deck(text), s)
+
+
+def test_unsupported_content_is_refused():
+    base = configs.pipe_chain(4, 0.4, 0.03, [1e5, 0.0, 0.0]).to_inp()
+    with pytest.raises(DeckError, match="Pipe_1"):
+        read_deck(base.replace("Beam_1\t2\t", "Pipe_1\t2\t"))
+    with pytest.raises(DeckError, match="Contacts"):
+        read_deck(base + "Contacts\t1\nNSSS\t1\n")
+    with pytest.raises(DeckError, match="solution step"):
+        read_deck(base, step=2)
+
+
+def _ref_deck(name):
+    path = os.path.join(REF_INPUTS, name, name + ".inp")
+    if not os.path.exists(path):
+        pytest.skip("reference decks not present")
+    return path
+
+
+def test_reference_tutorial01_reads_as_the_built_config():
+    same_structure(read_deck_file(_ref_deck("tutorial01")), configs.tutorial01())
+
+
+def test_reference_tutorial10_reads_as_the_built_config():
+    same_structure(read_deck_file(_ref_deck("tutorial10")), configs.tutorial10())
+
+
+def test_reference_tutorial05_first_step():
+    """A Shell_1 plate with a nodal load: the Static first step reads; the
+    Dynamic second step would start from the first one's end state."""
+    path = _ref_deck("tutorial05")
+    s = read_deck_file(path)
+    assert len(s.shells) == 400 and len(s.beams) == 0 and s.n_nodes == 861
+    assert s.solution.type == 0 and s.solution.end_time == 1.0
+    assert int(np.asarray(s.constraints).sum()) == 21 * 6
+    with pytest.raises(DeckError, match="first solution step"):
+        read_deck_file(path, step=2)
