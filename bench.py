@@ -285,6 +285,12 @@ def shell_leg(ctx, args, fp64_peak):
     L = ctx.L
     s = configs.square_plate(64, steps=20)
     s.solution.end_time = args.shell_steps / 20.0
+    # the same steps with the trailing update in FP64 FMA, for comparison
+    bf = gpu.BatchSolver(ctx, [s], ctx.opts(wide_update=gpu.GF_WIDE_FP64))
+    bf.reset()
+    ms_fp64 = bf.run()
+    st_fp64 = bf.results()[1]
+    bf.close()
     b = gpu.BatchSolver(ctx, [s])
     b.reset()
     ms = b.run()
@@ -326,8 +332,11 @@ def shell_leg(ctx, args, fp64_peak):
                         f"{dims[1]}, first {args.shell_steps} of 20 load steps",
             "newton_solves": int(st[0][0]), "newton_passes": int(st[0][1]), "ms": ms,
             "solves_per_s": st[0][0] / (ms / 1e3), "ms_per_pass": ms / max(1, st[0][1]),
+            "wide_update": "tensor cores: FP64 products from exact bf16 slices (Ozaki), mma.sync m16n8k16",
             "wide_lu_tflops": lu.value / (ms / 1e3) / 1e12, "fp64_peak_tflops": fp64_peak,
             "wide_lu_frac_of_measured_fp64": lu.value / (ms / 1e3) / 1e12 / fp64_peak,
+            "fp64_fma_update": {"ms": ms_fp64, "ms_per_pass": ms_fp64 / max(1, st_fp64[0][1]),
+                                "same_counts": bool(tuple(st_fp64[0]) == tuple(st[0]))},
             "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
             "sparse_solve": sparse,
             "plate8": {"workload": "Shell_1 plate 8x8x2 (1,203 free DOFs), all 20 load steps",

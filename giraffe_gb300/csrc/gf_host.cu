@@ -997,6 +997,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
+  b.sh.wide_tc = B->opts.wide_update == GF_WIDE_TENSOR;
   b.max_refine = B->opts.max_refine;
   return GF_OK;
 }
@@ -1068,6 +1069,7 @@ void gf_default_opts(gf_solve_opts* o) {
   o->max_refine = 6;
   o->poll_every = 8;
   o->use_graph = 1;
+  o->wide_update = GF_WIDE_TENSOR;
 }
 
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts) {

@@ -26,6 +26,7 @@
 //                2 n kl^2 FP64 flops per factorization)
 // and the solves k_wb_fwd (y = L^-1 b, b in P, y in y) and k_wb_bwd
 // (x = U^-1 y into P), one launch per panel each.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -810,6 +811,211 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
   if (ri1 < m && cj1 < m) w.at(base + ri1, base + cj1) -= a11;
 }
 
+// ---- the same trailing update on the tensor cores (Ozaki scheme) ----
+// A22 -= L21 U12 for one 64x64 output tile with K = NB = 64, the FP64
+// products emulated by bf16 tensor-core products of exact slices.  Each
+// row of L21 (column of U12) gets the power of two 2^e just above its
+// largest magnitude; an entry x becomes the 56-bit integer
+// X = floor(|x| 2^(56 - e)), read off the FP64 bits with integer
+// operations, cut into OZ_S = 8 slices of 7 bits, v_q = bits 49-7q .. 55-7q
+// of X with the sign of x: x = 2^e sum_q v_q 2^-7(q+1) + r, |r| < 2^(e-56),
+// every |v_q| <= 127 exact in bf16.  The slice products with q + t = d all
+// weigh 2^-7(d+2); summed over k and over the d + 1 pairs they form an
+// integer of magnitude below 8 * 64 * 127^2 < 2^23, which the FP32
+// accumulators of mma.sync hold exactly.  The diagonals are combined
+// exactly as two 64-bit integers (Horner in powers of 2^7: d = 0..4 and
+// d = 5..7), joined by one FMA and scaled by the row and column powers of
+// two.  What
+// is left out (pairs with q + t > 7, the remainders r) weighs at most about
+// 2^-55 of sum_k |L| |U|, the FP64 rounding of the product itself.  All
+// slicing is integer work, so the FP64 pipe, the scarce one on this part,
+// only sees a handful of operations per output entry.
+constexpr int OZ_S = 8;    // slices per operand
+constexpr int OZ_T = 64;   // output tile (rows and columns)
+constexpr int OZ_LD = 72;  // bf16 row stride of the slice tiles: 144 B, so the 8 rows of an ldmatrix hit distinct banks
+constexpr int OZ_THREADS = 256;
+constexpr size_t OZ_SMEM = 2 * sizeof(double) * OZ_T * (NB + 1) + 2 * sizeof(__nv_bfloat16) * OZ_S * OZ_T * OZ_LD +
+                           2 * sizeof(int) * OZ_T;
+
+__device__ __forceinline__ void oz_ldmatrix_x4(unsigned (&r)[4], const __nv_bfloat16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+__device__ __forceinline__ void oz_mma(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Magnitude bits of x (monotonic in |x| for finite values).
+__device__ __forceinline__ unsigned long long oz_mag(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// Scale exponent from the largest magnitude's bits: e with max|x| < 2^e
+// (biased: the FP64 exponent field of the maximum plus one); 0 for zero.
+__device__ __forceinline__ int oz_exponent(unsigned long long mag) { return mag ? (int)(mag >> 52) + 1 : 0; }
+
+// The slices of x under the biased row exponent eb, written to
+// dst[q * stride] for q = 0..OZ_S-1.  Subnormal entries count as zero.
+__device__ __forceinline__ void oz_split(double x, int eb, __nv_bfloat16* dst, int stride) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int E2 = (int)((u >> 52) & 0x7FF);
+  unsigned long long X = 0;
+  if (E2 != 0) {
+    const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = E2 - eb + 4;  // X = floor(|x| 2^(56 - e)); sh <= 3
+    X = sh >= 0 ? mant << sh : (sh > -64 ? mant >> (-sh) : 0ull);
+  }
+  const bool neg = (u >> 63) != 0;
+#pragma unroll
+  for (int q = 0; q < OZ_S; ++q) {
+    const int v = (int)((X >> (49 - 7 * q)) & 127ull);
+    dst[q * stride] = __float2bfloat16_rn((float)(neg ? -v : v));
+  }
+}
+
+__global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int part) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
+  const int s = b.sh.wide_structs[blockIdx.z];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);
+  if (m <= 0) return;
+  const int r0 = blockIdx.x * OZ_T, c0 = blockIdx.y * OZ_T;
+  if (r0 >= m || c0 >= m) return;
+  const bool corner = r0 < NB && c0 < NB;
+  if ((part == 1 && !corner) || (part == 2 && corner)) return;
+  extern __shared__ __align__(16) unsigned char oz_raw[];
+  double* Lf = reinterpret_cast<double*>(oz_raw);  // [row][k], stride NB + 1
+  double* Uf = Lf + OZ_T * (NB + 1);               // [col][k]
+  __nv_bfloat16* Ls = reinterpret_cast<__nv_bfloat16*>(Uf + OZ_T * (NB + 1));  // [slice][row][k]
+  __nv_bfloat16* Us = Ls + OZ_S * OZ_T * OZ_LD;                                 // [slice][col][k]
+  int* eL = reinterpret_cast<int*>(Us + OZ_S * OZ_T * OZ_LD);
+  int* eU = eL + OZ_T;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int base = j0 + nb;
+  // 1. the FP64 tiles (consecutive threads walk a band column: coalesced)
+  for (int x = tid; x < OZ_T * NB; x += OZ_THREADS) {
+    const int i = x % OZ_T, k = x / OZ_T, gk = j0 + k;
+    const int gi = base + r0 + i, gj = base + c0 + i;
+    Lf[i * (NB + 1) + k] = (k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
+    Uf[i * (NB + 1) + k] = (k < nb && c0 + i < m && gj - gk <= w.kl) ? w.at(gk, gj) : 0.0;
+  }
+  __syncthreads();
+  // 2. row / column scales (each warp 8 rows of L21 and 8 columns of U12),
+  // from the magnitude bits
+  for (int q = 0; q < OZ_T / (OZ_THREADS / 32); ++q) {
+    const int i = warp * (OZ_T / (OZ_THREADS / 32)) + q;
+    unsigned long long ml = max(oz_mag(Lf[i * (NB + 1) + lane]), oz_mag(Lf[i * (NB + 1) + lane + 32]));
+    unsigned long long mu = max(oz_mag(Uf[i * (NB + 1) + lane]), oz_mag(Uf[i * (NB + 1) + lane + 32]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+      mu = max(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+    }
+    if (lane == 0) {
+      eL[i] = oz_exponent(ml);
+      eU[i] = oz_exponent(mu);
+    }
+  }
+  __syncthreads();
+  // 3. slices
+  for (int x = tid; x < OZ_T * NB; x += OZ_THREADS) {
+    const int i = x / NB, k = x % NB;
+    oz_split(Lf[i * (NB + 1) + k], eL[i], Ls + i * OZ_LD + k, OZ_T * OZ_LD);
+    oz_split(Uf[i * (NB + 1) + k], eU[i], Us + i * OZ_LD + k, OZ_T * OZ_LD);
+  }
+  __syncthreads();
+  // 4. slice products on the tensor cores: warp (wm, wn) owns rows
+  // 32 wm .. +31 and columns 16 wn .. +15 as 2 x 2 tiles of 16 x 8; the
+  // fragments of the next 16-wide k step load while this one multiplies
+  const int wm = warp >> 2, wn = warp & 3;
+  long long hi[2][2][4];  // diagonals 0..4: sum_d c_d 2^(7 (4 - d)), exact (< 2^52)
+  long long lo[2][2][4];  // diagonals 5..7: c_5 2^14 + c_6 2^7 + c_7, exact (< 2^38)
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hi[a][c][q] = lo[a][c][q] = 0;
+  // ldmatrix row addresses of this lane: A (rows x k) and B (stored as
+  // columns x k)
+  const int a_row = wm * 32 + (lane & 7) + ((lane >> 3) & 1) * 8, a_col = (lane >> 4) * 8;
+  const int b_row = wn * 16 + (lane & 7) + (lane >> 4) * 8, b_col = ((lane >> 3) & 1) * 8;
+#pragma unroll 1
+  for (int d = 0; d < OZ_S; ++d) {
+    float c32[2][2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c32[a][c][q] = 0.0f;
+#pragma unroll 1
+    for (int sa = 0; sa <= d; ++sa) {
+      const __nv_bfloat16* As = Ls + sa * OZ_T * OZ_LD + a_row * OZ_LD + a_col;
+      const __nv_bfloat16* Bs = Us + (d - sa) * OZ_T * OZ_LD + b_row * OZ_LD + b_col;
+      unsigned af[2][2][4], bf[2][4];  // [buffer][m tile][reg], [buffer][reg]
+      oz_ldmatrix_x4(af[0][0], As);
+      oz_ldmatrix_x4(af[0][1], As + 16 * OZ_LD);
+      oz_ldmatrix_x4(bf[0], Bs);
+#pragma unroll
+      for (int ks = 0; ks < NB / 16; ++ks) {
+        const int cur = ks & 1, nxt = cur ^ 1;
+        if (ks + 1 < NB / 16) {
+          oz_ldmatrix_x4(af[nxt][0], As + 16 * (ks + 1));
+          oz_ldmatrix_x4(af[nxt][1], As + 16 * OZ_LD + 16 * (ks + 1));
+          oz_ldmatrix_x4(bf[nxt], Bs + 16 * (ks + 1));
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int c = 0; c < 2; ++c) oz_mma(c32[a][c], af[cur][a], bf[cur][2 * c], bf[cur][2 * c + 1]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const long long v = __float2int_rn(c32[a][c][q]);  // |c| < 2^23: an exact 32-bit integer
+          if (d <= 4) hi[a][c][q] = hi[a][c][q] * 128 + v;
+          else lo[a][c][q] = lo[a][c][q] * 128 + v;
+        }
+  }
+  // 5. A22 -= the product, in units of 2^(e_i + e_j - 63): hi 2^21 + lo
+  // (accumulator entry q of tile (a, c): row lane / 4 (+ 8 for q >= 2),
+  // column 2 (lane % 4) + q % 2)
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = wm * 32 + 16 * a + (lane >> 2) + (q >= 2 ? 8 : 0);
+        const int j = wn * 16 + 8 * c + 2 * (lane & 3) + (q & 1);
+        if (r0 + i < m && c0 + j < m) {
+          const double v = fma((double)hi[a][c][q], 0x1p21, (double)lo[a][c][q]);
+          // eL, eU are biased exponents (1023 + e); the scale 2^(e_i + e_j - 63)
+          const int k = eL[i] + eU[j] - 2046 - 63;
+          const double scale = (k >= -1022 && k <= 1023) ? __longlong_as_double((long long)(k + 1023) << 52)
+                                                          : ldexp(1.0, k);
+          w.at(base + r0 + i, base + c0 + j) -= v * scale;
+        }
+      }
+}
+
 // Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
 // below the panel: P_i -= L21(i, :) y_p.  Every CTA solves the small
 // triangle redundantly; CTA 0 writes y_p.
@@ -929,6 +1135,27 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
 // The next panel's diagonal LU and the forward substitution run while the
 // bulk of the trailing update occupies the SMs; the backward substitution
 // follows the last panel.
+// The trailing update of panel p (part as in k_wb_update): on the tensor
+// cores (64x64 tiles) when the batch asks for it, else in FP64 (32x32).
+// The corner (the next panel's diagonal block, on the lookahead's critical
+// path) always takes the FP64 kernel: four small CTAs finish it sooner than
+// one tensor-core CTA's load, slice and multiply sequence.
+static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
+  const int nw = b.sh.n_wide, mr = b.sh.max_kl;
+  if (b.sh.wide_tc && part != 1) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_wb_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM);
+      attr = true;
+    }
+    const int t = part == 1 ? 1 : (mr + OZ_T - 1) / OZ_T;
+    k_wb_update_tc<<<dim3(t, t, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p, part);
+  } else {
+    const int t = part == 1 ? (NB + UT - 1) / UT : (mr + UT - 1) / UT;
+    k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
+  }
+}
+
 // Panel-loop control inside a captured pass: the counter's start value,
 // and the step at the end of each loop body, which also sets the loop's
 // condition (continue while the counter stays in [0, limit)).
@@ -979,7 +1206,7 @@ cudaError_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_
 static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide, mr = sd.max_kl, P = sd.max_panels;
-  const int tiles = (mr + UT - 1) / UT, ct = (NB + UT - 1) / UT, nrb = (mr + 15) / 16, rb = (mr + 255) / 256;
+  const int nrb = (mr + 15) / 16, rb = (mr + 255) / 256;
   cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1];
   cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
   if (P <= 0) return cudaSuccess;
@@ -996,12 +1223,12 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   cudaStreamWaitEvent(s3, e_trsm, 0);
   k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
   cudaEventRecord(e_fwd, s3);
-  k_wb_update<<<dim3(ct, ct, nw), 256, 0, sb>>>(b, -1, 1);
+  launch_wb_update(b, -1, 1, sb);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
   k_wb_diag<<<nw, 256, 0, s2>>>(b, -2);
   cudaEventRecord(e_diag, s2);
-  k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, sb>>>(b, -1, 2);
+  launch_wb_update(b, -1, 2, sb);
   cudaStreamWaitEvent(sb, e_diag, 0);
   cudaStreamWaitEvent(sb, e_fwd, 0);
   k_wb_loop_step<<<1, 1, 0, sb>>>(sd.panel, 1, P, h);
@@ -1028,8 +1255,6 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide;
   const int mr = sd.max_kl;  // largest kl over the wide structures
-  const int tiles = (mr + UT - 1) / UT;
-  const int ct = (NB + UT - 1) / UT;
   const int nrb = (mr + 15) / 16;
   const int rb = (mr + 255) / 256;
   cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1];
@@ -1044,15 +1269,15 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
     bool next = p + 1 < sd.max_panels;
     if (next) {
-      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(ct, ct, nw), 256, 0, st>>>(b, p, 1); }
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 1, st); }
       cudaEventRecord(e_corner, st);
       cudaStreamWaitEvent(s2, e_corner, 0);
       { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, s2>>>(b, p + 1); }
       cudaEventRecord(e_diag, s2);
-      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p, 2); }
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 2, st); }
       cudaStreamWaitEvent(st, e_diag, 0);
     } else {
-      { ProfScope q(prof, st, KC_WIDE_UPDATE); k_wb_update<<<dim3(tiles, tiles, nw), 256, 0, st>>>(b, p, 0); }
+      { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 0, st); }
     }
   }
   // join: every forward step is done before the backward substitution

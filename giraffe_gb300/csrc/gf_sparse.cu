@@ -127,6 +127,7 @@ struct WideBatch {
     sd.max_panels = inf.n_panels;
     sd.max_kl = w;
     sd.wband = wband;
+    sd.wide_tc = 1;  // the trailing update on the tensor cores, as gf_default_opts
     for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
     for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
     return true;

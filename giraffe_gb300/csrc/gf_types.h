@@ -234,6 +234,7 @@ struct ShellData {
   double* wband;
   int* panel;       // device panel counter of the captured panel loops
   int loops_in_graph;  // capture the panel loops as graph WHILE loops (served waves)
+  int wide_tc;         // trailing update on the tensor cores (Ozaki slices) instead of FP64 FMA
   // host handles of the wide-band lookahead: two helper streams and the
   // events that fork from and join into the pass's stream; aux[2] roots the
   // captured panel-loop bodies

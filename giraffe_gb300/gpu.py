@@ -15,6 +15,7 @@ from .model import Structure, gf_model_desc
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgiraffe_gpu.so")
 
 GF_PREC_FP64, GF_PREC_MIXED = 0, 1
+GF_WIDE_FP64, GF_WIDE_TENSOR = 0, 1
 
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_batch_create",
            "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",
@@ -28,7 +29,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
 
 class gf_solve_opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_refine", C.c_int), ("poll_every", C.c_int),
-                ("use_graph", C.c_int)]
+                ("use_graph", C.c_int), ("wide_update", C.c_int)]
 
 
 class gf_stats(C.Structure):
@@ -145,10 +146,12 @@ class Context:
         if rc != 0:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
-    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=6):
+    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=6, wide_update=None):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
         o.precision, o.use_graph, o.poll_every, o.max_refine = precision, int(use_graph), poll_every, max_refine
+        if wide_update is not None:
+            o.wide_update = wide_update
         return o
 
     def beam_elements(self, xyz, mat, sec, cs, hist_disp, disp):

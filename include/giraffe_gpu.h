@@ -63,7 +63,12 @@ typedef struct gf_solve_opts {
   int max_refine;  /* mixed: FP64 refinement sweeps before falling back to FP64 */
   int poll_every;  /* Newton passes between host checks for completion */
   int use_graph;   /* capture one Newton pass as a CUDA graph */
+  int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
+                      default: FP64 products from exact bf16 slices on the
+                      tensor cores, Ozaki scheme, error below the FP64
+                      rounding of the product) or GF_WIDE_FP64 (FP64 FMA) */
 } gf_solve_opts;
+enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1 };
 
 /* Per-structure result of a solution step. */
 typedef struct gf_stats {

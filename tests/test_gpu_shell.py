@@ -84,3 +84,35 @@ def test_plate_and_beams_in_one_batch_match_the_oracle(gpu_ctx):
         assert tuple(stats[k]) == tuple(so), k
         scale = np.abs(fo[:, :3]).max()
         assert np.abs(finals[k][:, :3] - fo[:, :3]).max() <= 1e-10 * scale, k
+
+
+@pytest.mark.parametrize("name,make", [
+    ("ref_plate.npz", lambda: configs.square_plate(4, steps=20)),
+    ("ref_plate_fixed_area.npz", lambda: configs.square_plate(3, steps=10, area_update=0)),
+])
+def test_plate_tensor_core_and_fp64_updates_match_reference(gpu_ctx, golden, name, make):
+    """The wide-band LU's trailing update on the tensor cores (FP64 products
+    from exact bf16 slices, GF_WIDE_TENSOR, the default) and in FP64 FMA
+    (GF_WIDE_FP64): both solve the plate as the reference does (1e-10, same
+    step and iteration counts) and agree to 1e-13."""
+    g = golden(name)
+    s = make()
+    b = gpu.BatchSolver(gpu_ctx, [s], gpu_ctx.opts(wide_update=gpu.GF_WIDE_TENSOR))
+    b.reset()
+    b.run()
+    finals, stats = b.results()
+    b.close()
+    ref = g["nodes"][-1]
+    scale = np.abs(ref[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref[:, :3]).max() <= 1e-10 * scale
+    steps = g["steps"]
+    conv = steps[steps[:, 2] == 0]
+    assert stats[0][0] == len(conv)
+    assert stats[0][1] == int(conv[:, 1].sum() + len(conv))
+    b = gpu.BatchSolver(gpu_ctx, [make()], gpu_ctx.opts(wide_update=gpu.GF_WIDE_FP64))
+    b.reset()
+    b.run()
+    f64, st64 = b.results()
+    b.close()
+    assert tuple(st64[0]) == tuple(stats[0])
+    assert np.abs(finals[0][:, :3] - f64[0][:, :3]).max() <= 1e-13 * scale
