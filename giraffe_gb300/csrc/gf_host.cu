@@ -948,6 +948,13 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total) ||
         !balloc(B, &sd.panel, 1))
       return GF_ERR_CUDA;
+    if (B->opts.wide_update == GF_WIDE_TENSOR) {
+      // slices of one panel per wide structure for the tensor-core update
+      sd.oz_rows = (max_wkl + 63) / 64 * 64;
+      const size_t nw = wide_structs.size(), R = (size_t)sd.oz_rows;
+      if (!balloc(B, &sd.oz_slices, nw * 2 * 8 * R * GF_WB_NB) || !balloc(B, &sd.oz_exp, nw * 2 * R))
+        return GF_ERR_CUDA;
+    }
     if (!B->count_only) {
       for (auto& a : sd.aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
       for (auto& e : sd.evt) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -997,7 +1004,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
-  b.sh.wide_tc = B->opts.wide_update == GF_WIDE_TENSOR;
+  b.sh.wide_tc = B->opts.wide_update == GF_WIDE_TENSOR && b.sh.oz_slices != nullptr;
   b.max_refine = B->opts.max_refine;
   return GF_OK;
 }

@@ -831,11 +831,13 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 // slicing is integer work, so the FP64 pipe, the scarce one on this part,
 // only sees a handful of operations per output entry.
 constexpr int OZ_S = 8;    // slices per operand
-constexpr int OZ_T = 64;   // output tile (rows and columns)
+constexpr int OZ_T = 64;   // slicing block (rows of L21, columns of U12); output tile columns
+constexpr int OZ_TR = 32;  // output tile rows: two CTAs fit on an SM
 constexpr int OZ_LD = 72;  // bf16 row stride of the slice tiles: 144 B, so the 8 rows of an ldmatrix hit distinct banks
 constexpr int OZ_THREADS = 256;
-constexpr size_t OZ_SMEM = 2 * sizeof(double) * OZ_T * (NB + 1) + 2 * sizeof(__nv_bfloat16) * OZ_S * OZ_T * OZ_LD +
-                           2 * sizeof(int) * OZ_T;
+constexpr size_t OZ_SMEM = sizeof(__nv_bfloat16) * OZ_S * (OZ_TR + OZ_T) * OZ_LD + sizeof(int) * (OZ_TR + OZ_T);
+// The slicing kernel's FP64 tile
+constexpr size_t OZ_SLICE_SMEM = sizeof(double) * OZ_T * (NB + 1) + sizeof(int) * OZ_T;
 
 __device__ __forceinline__ void oz_ldmatrix_x4(unsigned (&r)[4], const __nv_bfloat16* p) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(p);
@@ -880,6 +882,90 @@ __device__ __forceinline__ void oz_split(double x, int eb, __nv_bfloat16* dst, i
   }
 }
 
+// Slice buffers of wide structure slot z (a panel's L21 rows and U12
+// columns, each as OZ_S slices of 64 bf16 per row or column, and their
+// biased scale exponents).
+struct OzSlices {
+  __nv_bfloat16 *L, *U;  // [slice][row or column][k]
+  int *eL, *eU;
+};
+__device__ __forceinline__ OzSlices oz_slices(const Batch& b, int z) {
+  const int64_t R = b.sh.oz_rows;
+  OzSlices o;
+  o.L = b.sh.oz_slices + (int64_t)z * 2 * OZ_S * R * NB;
+  o.U = o.L + OZ_S * R * NB;
+  o.eL = b.sh.oz_exp + (int64_t)z * 2 * R;
+  o.eU = o.eL + R;
+  return o;
+}
+
+// Slices of panel p's L21 (blockIdx.y = 0: 64 rows) or U12 (blockIdx.y = 1:
+// 64 columns) into the structure's slice buffers: the FP64 block through
+// shared memory (consecutive threads walk a band column), the scale
+// exponent of every row or column, then its OZ_S slices.  Rows or columns
+// beyond the trailing window are zero.
+__global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
+  const int s = b.sh.wide_structs[blockIdx.z];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);
+  if (m <= 0) return;
+  const int r0 = blockIdx.x * OZ_T;
+  if (r0 >= m) return;
+  const bool lower = blockIdx.y == 0;
+  extern __shared__ __align__(16) unsigned char oz_raw[];
+  double* F = reinterpret_cast<double*>(oz_raw);  // [row or column][k], stride NB + 1
+  int* e = reinterpret_cast<int*>(F + OZ_T * (NB + 1));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int base = j0 + nb;
+  for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
+    const int i = x % OZ_T, k = x / OZ_T, gk = j0 + k, g = base + r0 + i;
+    const bool live = k < nb && r0 + i < m && g - gk <= w.kl;
+    F[i * (NB + 1) + k] = live ? (lower ? w.at(g, gk) : w.at(gk, g)) : 0.0;
+  }
+  __syncthreads();
+  for (int q = 0; q < OZ_T / 8; ++q) {
+    const int i = warp * (OZ_T / 8) + q;
+    unsigned long long mx = max(oz_mag(F[i * (NB + 1) + lane]), oz_mag(F[i * (NB + 1) + lane + 32]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) e[i] = oz_exponent(mx);
+  }
+  __syncthreads();
+  OzSlices o = oz_slices(b, blockIdx.z);
+  __nv_bfloat16* dst = lower ? o.L : o.U;
+  const int64_t R = b.sh.oz_rows;
+  for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
+    const int i = x / NB, k = x % NB;
+    oz_split(F[i * (NB + 1) + k], e[i], dst + (int64_t)(r0 + i) * NB + k, (int)(R * NB));
+  }
+  if (tid < OZ_T) (lower ? o.eL : o.eU)[r0 + tid] = e[tid];
+}
+
+__device__ __forceinline__ void oz_cp16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void oz_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+// Waits until at most `pending` of this thread's copy groups are in flight.
+__device__ __forceinline__ void oz_wait(int pending) {
+  switch (pending) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::); break;
+    case 3: asm volatile("cp.async.wait_group 3;\n" ::); break;
+    case 4: asm volatile("cp.async.wait_group 4;\n" ::); break;
+    case 5: asm volatile("cp.async.wait_group 5;\n" ::); break;
+    case 6: asm volatile("cp.async.wait_group 6;\n" ::); break;
+    default: asm volatile("cp.async.wait_group 7;\n" ::); break;
+  }
+}
+
 __global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int part) {
   p = wb_panel(b, p);
   if (p < 0) return;
@@ -891,129 +977,105 @@ __global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);
   if (m <= 0) return;
-  const int r0 = blockIdx.x * OZ_T, c0 = blockIdx.y * OZ_T;
+  const int r0 = blockIdx.x * OZ_TR, c0 = blockIdx.y * OZ_T;
   if (r0 >= m || c0 >= m) return;
   const bool corner = r0 < NB && c0 < NB;
   if ((part == 1 && !corner) || (part == 2 && corner)) return;
   extern __shared__ __align__(16) unsigned char oz_raw[];
-  double* Lf = reinterpret_cast<double*>(oz_raw);  // [row][k], stride NB + 1
-  double* Uf = Lf + OZ_T * (NB + 1);               // [col][k]
-  __nv_bfloat16* Ls = reinterpret_cast<__nv_bfloat16*>(Uf + OZ_T * (NB + 1));  // [slice][row][k]
-  __nv_bfloat16* Us = Ls + OZ_S * OZ_T * OZ_LD;                                 // [slice][col][k]
+  __nv_bfloat16* Ls = reinterpret_cast<__nv_bfloat16*>(oz_raw);  // [slice][row][k]
+  __nv_bfloat16* Us = Ls + OZ_S * OZ_TR * OZ_LD;                  // [slice][col][k]
   int* eL = reinterpret_cast<int*>(Us + OZ_S * OZ_T * OZ_LD);
-  int* eU = eL + OZ_T;
+  int* eU = eL + OZ_TR;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = j0 + nb;
-  // 1. the FP64 tiles (consecutive threads walk a band column: coalesced)
-  for (int x = tid; x < OZ_T * NB; x += OZ_THREADS) {
-    const int i = x % OZ_T, k = x / OZ_T, gk = j0 + k;
-    const int gi = base + r0 + i, gj = base + c0 + i;
-    Lf[i * (NB + 1) + k] = (k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
-    Uf[i * (NB + 1) + k] = (k < nb && c0 + i < m && gj - gk <= w.kl) ? w.at(gk, gj) : 0.0;
-  }
-  __syncthreads();
-  // 2. row / column scales (each warp 8 rows of L21 and 8 columns of U12),
-  // from the magnitude bits
-  for (int q = 0; q < OZ_T / (OZ_THREADS / 32); ++q) {
-    const int i = warp * (OZ_T / (OZ_THREADS / 32)) + q;
-    unsigned long long ml = max(oz_mag(Lf[i * (NB + 1) + lane]), oz_mag(Lf[i * (NB + 1) + lane + 32]));
-    unsigned long long mu = max(oz_mag(Uf[i * (NB + 1) + lane]), oz_mag(Uf[i * (NB + 1) + lane + 32]));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
-      mu = max(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+  // 1-3. the slices of this tile's rows and columns, one copy group per
+  // slice index, so that the products of the first diagonals start while
+  // the later slices are still on their way
+  {
+    const OzSlices o = oz_slices(b, blockIdx.z);
+    const int64_t R = b.sh.oz_rows;
+    for (int q = 0; q < OZ_S; ++q) {
+      // 32 rows of L21 and 64 columns of U12, 8 chunks of 16 bytes each
+      for (int x = tid; x < (OZ_TR + OZ_T) * 8; x += OZ_THREADS) {
+        const int op = x >= OZ_TR * 8, y = x - op * OZ_TR * 8, i = y >> 3, c = y & 7;
+        const __nv_bfloat16* src = (op ? o.U + (int64_t)q * R * NB + (int64_t)(c0 + i) * NB
+                                       : o.L + (int64_t)q * R * NB + (int64_t)(r0 + i) * NB) + 8 * c;
+        __nv_bfloat16* dst = (op ? Us + q * OZ_T * OZ_LD : Ls + q * OZ_TR * OZ_LD) + i * OZ_LD + 8 * c;
+        oz_cp16(dst, src);
+      }
+      oz_commit();
     }
-    if (lane == 0) {
-      eL[i] = oz_exponent(ml);
-      eU[i] = oz_exponent(mu);
-    }
+    if (tid < OZ_TR) eL[tid] = o.eL[r0 + tid];
+    if (tid < OZ_T) eU[tid] = o.eU[c0 + tid];
   }
-  __syncthreads();
-  // 3. slices
-  for (int x = tid; x < OZ_T * NB; x += OZ_THREADS) {
-    const int i = x / NB, k = x % NB;
-    oz_split(Lf[i * (NB + 1) + k], eL[i], Ls + i * OZ_LD + k, OZ_T * OZ_LD);
-    oz_split(Uf[i * (NB + 1) + k], eU[i], Us + i * OZ_LD + k, OZ_T * OZ_LD);
-  }
-  __syncthreads();
   // 4. slice products on the tensor cores: warp (wm, wn) owns rows
-  // 32 wm .. +31 and columns 16 wn .. +15 as 2 x 2 tiles of 16 x 8; the
+  // 16 wm .. +15 and columns 16 wn .. +15 as 1 x 2 tiles of 16 x 8; the
   // fragments of the next 16-wide k step load while this one multiplies
   const int wm = warp >> 2, wn = warp & 3;
-  long long hi[2][2][4];  // diagonals 0..4: sum_d c_d 2^(7 (4 - d)), exact (< 2^52)
-  long long lo[2][2][4];  // diagonals 5..7: c_5 2^14 + c_6 2^7 + c_7, exact (< 2^38)
+  long long hi[2][4];  // diagonals 0..4: sum_d c_d 2^(7 (4 - d)), exact (< 2^52)
+  long long lo[2][4];  // diagonals 5..7: c_5 2^14 + c_6 2^7 + c_7, exact (< 2^38)
 #pragma unroll
-  for (int a = 0; a < 2; ++a)
+  for (int c = 0; c < 2; ++c)
 #pragma unroll
-    for (int c = 0; c < 2; ++c)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) hi[a][c][q] = lo[a][c][q] = 0;
+    for (int q = 0; q < 4; ++q) hi[c][q] = lo[c][q] = 0;
   // ldmatrix row addresses of this lane: A (rows x k) and B (stored as
   // columns x k)
-  const int a_row = wm * 32 + (lane & 7) + ((lane >> 3) & 1) * 8, a_col = (lane >> 4) * 8;
+  const int a_row = wm * 16 + (lane & 7) + ((lane >> 3) & 1) * 8, a_col = (lane >> 4) * 8;
   const int b_row = wn * 16 + (lane & 7) + (lane >> 4) * 8, b_col = ((lane >> 3) & 1) * 8;
 #pragma unroll 1
   for (int d = 0; d < OZ_S; ++d) {
-    float c32[2][2][4];
+    oz_wait(OZ_S - 1 - d);  // slices 0..d of both operands are in
+    __syncthreads();
+    float c32[2][4];
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+    for (int c = 0; c < 2; ++c)
 #pragma unroll
-      for (int c = 0; c < 2; ++c)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) c32[a][c][q] = 0.0f;
+      for (int q = 0; q < 4; ++q) c32[c][q] = 0.0f;
 #pragma unroll 1
     for (int sa = 0; sa <= d; ++sa) {
-      const __nv_bfloat16* As = Ls + sa * OZ_T * OZ_LD + a_row * OZ_LD + a_col;
+      const __nv_bfloat16* As = Ls + sa * OZ_TR * OZ_LD + a_row * OZ_LD + a_col;
       const __nv_bfloat16* Bs = Us + (d - sa) * OZ_T * OZ_LD + b_row * OZ_LD + b_col;
-      unsigned af[2][2][4], bf[2][4];  // [buffer][m tile][reg], [buffer][reg]
-      oz_ldmatrix_x4(af[0][0], As);
-      oz_ldmatrix_x4(af[0][1], As + 16 * OZ_LD);
+      unsigned af[2][4], bf[2][4];  // [buffer][reg]
+      oz_ldmatrix_x4(af[0], As);
       oz_ldmatrix_x4(bf[0], Bs);
 #pragma unroll
       for (int ks = 0; ks < NB / 16; ++ks) {
         const int cur = ks & 1, nxt = cur ^ 1;
         if (ks + 1 < NB / 16) {
-          oz_ldmatrix_x4(af[nxt][0], As + 16 * (ks + 1));
-          oz_ldmatrix_x4(af[nxt][1], As + 16 * OZ_LD + 16 * (ks + 1));
+          oz_ldmatrix_x4(af[nxt], As + 16 * (ks + 1));
           oz_ldmatrix_x4(bf[nxt], Bs + 16 * (ks + 1));
         }
 #pragma unroll
-        for (int a = 0; a < 2; ++a)
-#pragma unroll
-          for (int c = 0; c < 2; ++c) oz_mma(c32[a][c], af[cur][a], bf[cur][2 * c], bf[cur][2 * c + 1]);
+        for (int c = 0; c < 2; ++c) oz_mma(c32[c], af[cur], bf[cur][2 * c], bf[cur][2 * c + 1]);
       }
     }
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int c = 0; c < 2; ++c)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const long long v = __float2int_rn(c32[a][c][q]);  // |c| < 2^23: an exact 32-bit integer
-          if (d <= 4) hi[a][c][q] = hi[a][c][q] * 128 + v;
-          else lo[a][c][q] = lo[a][c][q] * 128 + v;
-        }
-  }
-  // 5. A22 -= the product, in units of 2^(e_i + e_j - 63): hi 2^21 + lo
-  // (accumulator entry q of tile (a, c): row lane / 4 (+ 8 for q >= 2),
-  // column 2 (lane % 4) + q % 2)
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
 #pragma unroll
     for (int c = 0; c < 2; ++c)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const int i = wm * 32 + 16 * a + (lane >> 2) + (q >= 2 ? 8 : 0);
-        const int j = wn * 16 + 8 * c + 2 * (lane & 3) + (q & 1);
-        if (r0 + i < m && c0 + j < m) {
-          const double v = fma((double)hi[a][c][q], 0x1p21, (double)lo[a][c][q]);
-          // eL, eU are biased exponents (1023 + e); the scale 2^(e_i + e_j - 63)
-          const int k = eL[i] + eU[j] - 2046 - 63;
-          const double scale = (k >= -1022 && k <= 1023) ? __longlong_as_double((long long)(k + 1023) << 52)
-                                                          : ldexp(1.0, k);
-          w.at(base + r0 + i, base + c0 + j) -= v * scale;
-        }
+        const long long v = __float2int_rn(c32[c][q]);  // |c| < 2^23: an exact 32-bit integer
+        if (d <= 4) hi[c][q] = hi[c][q] * 128 + v;
+        else lo[c][q] = lo[c][q] * 128 + v;
       }
+  }
+  // 5. A22 -= the product, in units of 2^(e_i + e_j - 63): hi 2^21 + lo
+  // (accumulator entry q of tile c: row lane / 4 (+ 8 for q >= 2), column
+  // 2 (lane % 4) + q % 2)
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = wm * 16 + (lane >> 2) + (q >= 2 ? 8 : 0);
+      const int j = wn * 16 + 8 * c + 2 * (lane & 3) + (q & 1);
+      if (r0 + i < m && c0 + j < m) {
+        const double v = fma((double)hi[c][q], 0x1p21, (double)lo[c][q]);
+        // eL, eU are biased exponents (1023 + e); the scale 2^(e_i + e_j - 63)
+        const int k = eL[i] + eU[j] - 2046 - 63;
+        const double scale =
+            (k >= -1022 && k <= 1023) ? __longlong_as_double((long long)(k + 1023) << 52) : ldexp(1.0, k);
+        w.at(base + r0 + i, base + c0 + j) -= v * scale;
+      }
+    }
 }
 
 // Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
@@ -1146,10 +1208,13 @@ static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_wb_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM);
+      cudaFuncSetAttribute(k_wb_slice, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SLICE_SMEM);
       attr = true;
     }
-    const int t = part == 1 ? 1 : (mr + OZ_T - 1) / OZ_T;
-    k_wb_update_tc<<<dim3(t, t, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p, part);
+    // the panel's slices (L21 rows and U12 columns), then the tiles
+    k_wb_slice<<<dim3((mr + OZ_T - 1) / OZ_T, 2, nw), 256, OZ_SLICE_SMEM, st>>>(b, p);
+    k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
+                                                                                                      part);
   } else {
     const int t = part == 1 ? (NB + UT - 1) / UT : (mr + UT - 1) / UT;
     k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
@@ -1319,7 +1384,9 @@ int shell_launches_per_pass(const Batch& b) {
   // update corner + next diagonal + update rest (or one update for the
   // last), backward step; graph loops: two loop-control kernels, the first
   // diagonal LU, six kernels per forward iteration and two per backward one
-  if (b.sh.n_wide) n += b.sh.loops_in_graph ? 3 + 8 * b.sh.max_panels : 1 + 6 * b.sh.max_panels;
+  if (b.sh.n_wide)
+    n += (b.sh.loops_in_graph ? 3 + 8 * b.sh.max_panels : 1 + 6 * b.sh.max_panels) +
+         (b.sh.wide_tc ? b.sh.max_panels : 0);  // the tensor-core update's slicing kernel
   return n;
 }
 }  // namespace gf

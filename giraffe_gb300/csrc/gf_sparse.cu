@@ -13,6 +13,7 @@
 // The CSR path picks the narrower of the natural ordering and reverse
 // Cuthill-McKee on the symmetrised pattern, as the batch path does for
 // shells.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -109,7 +110,12 @@ struct WideBatch {
     st0.phase = PH_ITER;
     st0.need_solve = 1;
     const int zero = 0;
-    if (!mem.get(&dinf, 1) || !mem.get(&dst, 1) || !mem.get(&dws, 1) || !hl.create()) return false;
+    const int R = (w + 63) / 64 * 64;
+    __nv_bfloat16* sl = nullptr;
+    int* se = nullptr;
+    if (!mem.get(&dinf, 1) || !mem.get(&dst, 1) || !mem.get(&dws, 1) || !hl.create() ||
+        !mem.get(&sl, (size_t)2 * 8 * R * GF_WB_NB) || !mem.get(&se, (size_t)2 * R))
+      return false;
     cudaStream_t s = ctx->stream;
     if (cudaMemcpyAsync(dinf, &inf, sizeof(inf), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(dst, &st0, sizeof(st0), cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -128,6 +134,9 @@ struct WideBatch {
     sd.max_kl = w;
     sd.wband = wband;
     sd.wide_tc = 1;  // the trailing update on the tensor cores, as gf_default_opts
+    sd.oz_rows = R;
+    sd.oz_slices = sl;
+    sd.oz_exp = se;
     for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
     for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
     return true;

@@ -16,6 +16,7 @@
 //             reference src/BandMatrix.cpp:214,246), FP64 and an FP32 copy
 //   factor    U rows: n_free x (GF_KB+1), [j][c] = U(j, j+c)
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -235,6 +236,11 @@ struct ShellData {
   int* panel;       // device panel counter of the captured panel loops
   int loops_in_graph;  // capture the panel loops as graph WHILE loops (served waves)
   int wide_tc;         // trailing update on the tensor cores (Ozaki slices) instead of FP64 FMA
+  // the tensor-core update's slices of a panel: per wide structure slot,
+  // [2 operands][8 slices][oz_rows][64] bf16 and [2][oz_rows] exponents
+  int oz_rows;         // max_kl rounded up to 64
+  __nv_bfloat16* oz_slices;
+  int* oz_exp;
   // host handles of the wide-band lookahead: two helper streams and the
   // events that fork from and join into the pass's stream; aux[2] roots the
   // captured panel-loop bodies
