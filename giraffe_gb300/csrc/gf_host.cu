@@ -1200,6 +1200,85 @@ int gf_batch_run(gf_batch* B) {
   return GF_OK;
 }
 
+int gf_batch_step(gf_batch* B, int max_passes, int* running) {
+  if (!B || max_passes <= 0) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  cudaStream_t st = B->stream;
+  int r = ensure_graph(B);
+  if (r != GF_OK) return r;
+  for (int k = 0; k < max_passes; ++k) {
+    if (B->graph) {
+      CK(cudaGraphLaunch(B->graph, st));
+    } else {
+      launch_iteration(B->b, st);
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(B->h_running, B->b.running, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (running) *running = *B->h_running;
+  return GF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// The device state a batch carries from one Newton pass to the next: nodal
+// increments, configurations, velocities and accelerations (current and
+// converged), Gauss-point histories, the per-structure step machine, and
+// the Rayleigh matrices when they are formed once per step.  Everything
+// else is rebuilt by every pass.
+std::vector<std::pair<void*, size_t>> state_parts(const gf_batch* B) {
+  const Batch& b = B->b;
+  const size_t nn = (size_t)b.n_nodes, ne = (size_t)b.n_elem, ns = (size_t)b.sh.n_shells;
+  std::vector<std::pair<void*, size_t>> v = {
+      {b.disp, 8 * 6 * nn},      {b.copy, 8 * 6 * nn},      {b.Qn, 8 * 9 * nn},
+      {b.vel, 8 * 6 * nn},       {b.accel, 8 * 6 * nn},     {b.copy_vel, 8 * 6 * nn},
+      {b.copy_accel, 8 * 6 * nn}, {b.bhist, sizeof(BeamHist) * ne}, {b.baux, sizeof(BeamHistAux) * ne},
+      {b.state, sizeof(StructState) * (size_t)b.n_struct}};
+  if (ns) {
+    v.push_back({b.sh.shist, sizeof(ShellHist) * ns});
+    v.push_back({b.sh.saux, sizeof(ShellHistAux) * ns});
+  }
+  if (b.any_rayleigh) v.push_back({b.RD, 8 * 324 * ne});
+  return v;
+}
+}  // namespace
+
+extern "C" {
+
+int gf_batch_snapshot_bytes(const gf_batch* B, size_t* bytes) {
+  if (!B || !bytes) return GF_ERR_ARG;
+  size_t n = 0;
+  for (const auto& p : state_parts(B)) n += p.second;
+  *bytes = n;
+  return GF_OK;
+}
+
+int gf_batch_snapshot(gf_batch* B, void* host) {
+  if (!B || !host) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  char* h = static_cast<char*>(host);
+  for (const auto& p : state_parts(B)) {
+    if (p.second) CK(cudaMemcpyAsync(h, p.first, p.second, cudaMemcpyDeviceToHost, B->stream));
+    h += p.second;
+  }
+  CK(cudaStreamSynchronize(B->stream));
+  return GF_OK;
+}
+
+int gf_batch_restore(gf_batch* B, const void* host) {
+  if (!B || !host) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  const char* h = static_cast<const char*>(host);
+  for (const auto& p : state_parts(B)) {
+    if (p.second) CK(cudaMemcpyAsync(p.first, h, p.second, cudaMemcpyHostToDevice, B->stream));
+    h += p.second;
+  }
+  CK(cudaStreamSynchronize(B->stream));
+  return GF_OK;
+}
+
 int gf_batch_solve_timed(gf_batch* B, int steps, double* ms_out) {
   if (!B || steps <= 0) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;

@@ -21,7 +21,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",
            "gf_batch_last_ms", "gf_batch_last_launches", "gf_batch_assemble", "gf_solve",
            "gf_beam_elements", "gf_band_solve", "gf_batch_solve_timed", "gf_batch_profile",
-           "gf_kernel_name", "gf_batch_bytes", "gf_batch_host_ms", "gf_batch_work", "gf_device_fp_peaks",
+           "gf_kernel_name", "gf_batch_bytes", "gf_batch_host_ms", "gf_batch_step", "gf_batch_snapshot_bytes",
+           "gf_batch_snapshot", "gf_batch_restore", "gf_batch_work", "gf_device_fp_peaks",
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_sparse_solve", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
            "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr"]
@@ -81,6 +82,10 @@ def lib():
         L.gf_batch_last_launches.restype = C.c_longlong
         L.gf_batch_last_launches.argtypes = [vp]
         L.gf_batch_host_ms.argtypes = [vp, dp, C.c_int]
+        L.gf_batch_step.argtypes = [vp, C.c_int, ip]
+        L.gf_batch_snapshot_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+        L.gf_batch_snapshot.argtypes = [vp, vp]
+        L.gf_batch_restore.argtypes = [vp, vp]
         L.gf_batch_assemble.argtypes = [vp, C.c_int, dp, dp, ip]
         L.gf_solve.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts),
                                C.POINTER(dp), C.POINTER(gf_stats)]
@@ -263,6 +268,24 @@ class BatchSolver:
         ms = (C.c_double * 5)()
         self.ctx.check(self.ctx.L.gf_batch_host_ms(self.h, ms, 5), "gf_batch_host_ms")
         return dict(zip(("build", "alloc", "upload", "graph", "results"), list(ms)))
+
+    def step(self, passes: int) -> int:
+        """Runs up to `passes` Newton passes; returns the structures still running."""
+        r = C.c_int(0)
+        self.ctx.check(self.ctx.L.gf_batch_step(self.h, passes, C.byref(r)), "gf_batch_step")
+        return r.value
+
+    def snapshot(self) -> np.ndarray:
+        """The batch's device state between passes, as host bytes."""
+        n = C.c_size_t(0)
+        self.ctx.check(self.ctx.L.gf_batch_snapshot_bytes(self.h, C.byref(n)), "gf_batch_snapshot_bytes")
+        buf = np.empty(n.value, dtype=np.uint8)
+        self.ctx.check(self.ctx.L.gf_batch_snapshot(self.h, buf.ctypes.data), "gf_batch_snapshot")
+        return buf
+
+    def restore(self, buf: np.ndarray) -> None:
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self.ctx.check(self.ctx.L.gf_batch_restore(self.h, buf.ctypes.data), "gf_batch_restore")
 
     def launches(self):
         return self.ctx.L.gf_batch_last_launches(self.h)

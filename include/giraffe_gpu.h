@@ -98,6 +98,19 @@ void gf_batch_destroy(gf_batch* batch);
 int gf_batch_reset(gf_batch* batch);
 /* Runs every structure's solution step to its end (or abort) on the device. */
 int gf_batch_run(gf_batch* batch);
+/* Runs at most max_passes Newton passes (fewer only in effect: passes after
+ * every structure finished change nothing); *running receives the number of
+ * structures still running.  gf_batch_run continues from where it stops. */
+int gf_batch_step(gf_batch* batch, int max_passes, int* running);
+/* Checkpoint / resume of a batch between passes (the in-memory counterpart
+ * of the reference's last converged configuration, Solution::
+ * SaveConfiguration / RestoreConfiguration, src/Solution.cpp:426-575, here
+ * with the step machine and the Gauss-point histories, so a restore resumes
+ * exactly): gf_batch_snapshot copies the batch's device state into `host`
+ * (gf_batch_snapshot_bytes long), gf_batch_restore puts it back. */
+int gf_batch_snapshot_bytes(const gf_batch* batch, size_t* bytes);
+int gf_batch_snapshot(gf_batch* batch, void* host);
+int gf_batch_restore(gf_batch* batch, const void* host);
 /* Final nodal state per structure: final_nodes[s] holds n_nodes x 15 doubles
  * (copy_coordinates: position and accumulated Rodrigues vector, then the
  * nodal rotation tensor Q row-major); stats may be NULL. */
