@@ -1090,6 +1090,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
   B->stream = ctx->stream;
   if (opts) B->opts = *opts; else gf_default_opts(&B->opts);
   if (B->opts.poll_every <= 0) B->opts.poll_every = 8;
+  NvtxRange range("gf_batch_create");
   const double t0 = host_now_ms();
   if (build_batch(B, n, models) != GF_OK || cudaMallocHost(&B->h_running, sizeof(int)) != cudaSuccess ||
       cudaEventCreate(&B->ev0) != cudaSuccess || cudaEventCreate(&B->ev1) != cudaSuccess) {
@@ -1136,6 +1137,7 @@ int ensure_graph(gf_batch* B) {
   gf_ctx* ctx = B->ctx;
   cudaStream_t st = B->stream;
   if (B->opts.use_graph && !B->graph) {
+    NvtxRange range("capture Newton pass");
     const double t0 = host_now_ms();
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1183,6 +1185,7 @@ extern "C" {
 
 int gf_batch_run(gf_batch* B) {
   if (!B) return GF_ERR_ARG;
+  NvtxRange range("gf_batch_run");
   gf_ctx* ctx = B->ctx;
   cudaStream_t st = B->stream;
   int r = ensure_graph(B);
@@ -1406,6 +1409,7 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
   if (!B) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
   const Batch& b = B->b;
+  NvtxRange range("gf_batch_results");
   const double t0 = host_now_ms();
   int n = b.n_struct;
   std::vector<StructState> st(n);

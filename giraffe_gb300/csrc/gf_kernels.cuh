@@ -21,6 +21,8 @@
 // sequence (captured as a CUDA graph) serves structures at different load
 // steps.
 #pragma once
+#include <nvtx3/nvToolsExt.h>
+
 #include "gf_types.h"
 
 namespace gf {
@@ -40,7 +42,16 @@ enum KernelClass {
 };
 const char* kernel_class_name(int k);
 
-// Brackets one launch with profiling events (no-op when p is null).
+// A named NVTX range for timeline tools (Nsight Systems): host phases of the
+// library, and each kernel class of a profiled (launched, not replayed)
+// pass.  Without an attached tool the calls return at once.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
+// Brackets one launch with profiling events and an NVTX range of its
+// kernel class (no-op when p is null).
 struct ProfScope {
   LaunchProf* p;
   cudaStream_t st;
@@ -49,11 +60,15 @@ struct ProfScope {
     if (p && p->n < p->cap) {
       idx = p->n++;
       p->cls[idx] = k;
+      nvtxRangePushA(kernel_class_name(k));
       cudaEventRecord(p->ev[2 * idx], st);
     }
   }
   ~ProfScope() {
-    if (idx >= 0) cudaEventRecord(p->ev[2 * idx + 1], st);
+    if (idx >= 0) {
+      cudaEventRecord(p->ev[2 * idx + 1], st);
+      nvtxRangePop();
+    }
   }
 };
 

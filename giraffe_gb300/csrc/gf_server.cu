@@ -391,6 +391,7 @@ int admit_kind(gf_server* S, bool kind, bool* admitted) {
 // Builder thread: the device batch of one admitted wave, built and captured
 // on the capture stream, reset on the wave's slot stream.
 void build_wave(gf_server* S, Wave& w) {
+  NvtxRange range("build wave");
   const int take = (int)w.reqs.size();
   std::vector<gf_model_desc> models(take);
   for (int i = 0; i < take; ++i) models[i] = w.reqs[i].model;
