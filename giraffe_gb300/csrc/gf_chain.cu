@@ -396,14 +396,15 @@ __global__ void k_corner_scatter(Batch b, ChainData c) {
 
 void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
   if (c.n_chain_elems == 0) return;
-  static bool attr = false;
   const int smem = 6 * NC * CT * (int)sizeof(double);
-  if (!attr) {
+  // once per process (a function-local static is initialised by one thread)
+  static const bool attr = [smem] {
     cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_cr_eliminate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_cr_root, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   k_condense<<<(c.n_chain_elems + CT - 1) / CT, CT, smem, st>>>(b, c);
   if (c.n_corners > 0) {
     k_corner_system<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);

@@ -1007,7 +1007,6 @@ void launch_init_state(const Batch& b, cudaStream_t st) {
   k_init_state<<<(b.n_struct + 127) / 128, 128, 0, st>>>(b);
 }
 
-static bool g_attr_set = false;
 
 static void set_attrs();
 
@@ -1027,14 +1026,18 @@ void launch_iteration_partial(const Batch& b_in, cudaStream_t st) {
   k_residual<<<b.n_chunks, 256, 0, st>>>(b);
 }
 
+// Shared-memory limits of the large kernels, once per process (the served
+// path's builder thread and the caller's thread may both get here first; a
+// function-local static is initialised by exactly one of them).
 static void set_attrs() {
-  if (!g_attr_set) {
+  static const bool done = [] {
     cudaFuncSetAttribute(k_beam_tangent<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
     cudaFuncSetAttribute(k_beam_tangent<f2>, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
     cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (RING * GF_LDB + RING) * (int)sizeof(double));
-    g_attr_set = true;
-  }
+    return true;
+  }();
+  (void)done;
 }
 
 const char* kernel_class_name(int k) {
@@ -1113,11 +1116,9 @@ void launch_band_solve(const Batch& b, cudaStream_t st) {
 void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const double* d, double* K,
                           double* f, cudaStream_t st) {
   if (n <= 0) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_beam_elements, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM);
-    attr = true;
-  }
+  static const bool attr =
+      cudaFuncSetAttribute(k_beam_elements, cudaFuncAttributeMaxDynamicSharedMemorySize, MOUNT_SMEM) == cudaSuccess;
+  (void)attr;
   k_beam_elements<<<(n + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(n, c, h, d, K, f);
 }
 

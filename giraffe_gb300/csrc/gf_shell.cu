@@ -1205,12 +1205,12 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
 static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
   const int nw = b.sh.n_wide, mr = b.sh.max_kl;
   if (b.sh.wide_tc && part != 1) {
-    static bool attr = false;
-    if (!attr) {
+    static const bool attr = [] {  // once per process, thread-safe
       cudaFuncSetAttribute(k_wb_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM);
       cudaFuncSetAttribute(k_wb_slice, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SLICE_SMEM);
-      attr = true;
-    }
+      return true;
+    }();
+    (void)attr;
     // the panel's slices (L21 rows and U12 columns), then the tiles
     k_wb_slice<<<dim3((mr + OZ_T - 1) / OZ_T, 2, nw), 256, OZ_SLICE_SMEM, st>>>(b, p);
     k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
