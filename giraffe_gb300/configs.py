@@ -116,6 +116,26 @@ def tutorial10(rayleigh_alpha: float = 0.0, rayleigh_beta: float = 0.0, update_r
     return s
 
 
+def rotating_base(angular: str = "EulerAngles", steps: int = 10) -> Structure:
+    """tutorial01's cantilever (10 Beam_1 along z) whose clamped base is turned
+    by a prescribed rotation with components (0.4, -0.3, 1.2) at t = 1, read
+    as Euler angles or as an Euler rotation vector (NodalDisplacement
+    AngularParameters), with a tip force, in `steps` load steps."""
+    s = Structure(nodes=straight_chain(10, 1.0, (0.0, 0.0, 1.0)))
+    mat = s.add_material(1e7, 0.3, 2000)
+    sec = s.add_rectangle(0.1, 0.1)
+    cs = s.add_cs((1, 0, 0), (0, 0, 1))
+    _chain_beams(s, 10, mat, sec, cs)
+    s.clamp(0)
+    s.displacements.append(NodalDisplacement([0], cs, Table(
+        np.array([0.0, 1.0]), np.array([[0.0] * 6, [0.0, 0.0, 0.0, 0.4, -0.3, 1.2]])), angular=angular))
+    s.loads.append(NodalLoad([20], cs, Table(np.array([0.0, 1.0]), np.array([[0.0] * 6, [50.0, 0, 0, 0, 0, 0]]))))
+    dt = 1.0 / steps
+    s.solution = Solution(GF_STATIC, 0.0, 1.0, dt, dt, dt / 64, 20, 3, 4, 1.0)
+    s.criteria.update(force_tol=1e-8, moment_tol=1e-8, force_min=1.0, moment_min=1.0)
+    return s
+
+
 def pipe_chain(n_el: int, De: float, wall: float, tip_force, steps: int = 10,
                element_length: float = 1.0, tol: float = 1e-8) -> Structure:
     s = Structure(nodes=straight_chain(n_el, n_el * element_length, (0.0, 0.0, 1.0)))

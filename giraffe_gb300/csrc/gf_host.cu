@@ -776,6 +776,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
         de.structure = s;
         de.node = node_off + D.nodes[q];
         de.table = t;
+        de.angular = D.angular == GF_ANGLES_VECTOR ? GF_ANGLES_VECTOR : GF_ANGLES_EULER;
         std::memcpy(de.CQ, CQ, sizeof(CQ));
         disps.push_back(de);
       }

@@ -6,6 +6,7 @@
 #include "gf_beam.cuh"
 #include "gf_df64.cuh"
 #include "gf_chain.cuh"
+#include "../../include/giraffe_model.h"
 #include "gf_kernels.cuh"
 
 namespace gf {
@@ -211,15 +212,30 @@ __global__ void k_step_begin(Batch b) {
     double th = cons[4] == 1 ? table_at(b, D.table, time, 4) : 0.0;
     double psi = cons[5] == 1 ? table_at(b, D.table, time, 5) : 0.0;
     M3<double> Q;
-    Q[0] = cos(th) * cos(psi);
-    Q[1] = sin(phi) * sin(th) * cos(psi) - cos(phi) * sin(psi);
-    Q[2] = cos(phi) * sin(th) * cos(psi) + sin(phi) * sin(psi);
-    Q[3] = cos(th) * sin(psi);
-    Q[4] = sin(phi) * sin(th) * sin(psi) + cos(phi) * cos(psi);
-    Q[5] = cos(phi) * sin(th) * sin(psi) - sin(phi) * cos(psi);
-    Q[6] = -sin(th);
-    Q[7] = sin(phi) * cos(th);
-    Q[8] = cos(phi) * cos(th);
+    if (D.angular == GF_ANGLES_VECTOR) {
+      // Euler rotation vector (phi, th, psi): Rodrigues parameters of length
+      // 2 tan(|e| / 2) along e (reference src/NodalDisplacement.cpp:330-350)
+      const double en = sqrt(phi * phi + th * th + psi * psi);
+      const double inv = en != 0.0 ? 1.0 / en : 0.0;
+      const double rod = 2.0 * tan(en / 2.0);
+      const V3<double> r = {{rod * (inv * phi), rod * (inv * th), rod * (inv * psi)}};
+      const M3<double> A = skew(r), A2 = mul(A, A);
+      const double g = 4.0 / (4.0 + rod * rod);
+      for (int k = 0; k < 9; ++k) Q[k] = g * (A[k] + 0.5 * A2[k]);
+      Q[0] += 1.0;
+      Q[4] += 1.0;
+      Q[8] += 1.0;
+    } else {
+      Q[0] = cos(th) * cos(psi);
+      Q[1] = sin(phi) * sin(th) * cos(psi) - cos(phi) * sin(psi);
+      Q[2] = cos(phi) * sin(th) * cos(psi) + sin(phi) * sin(psi);
+      Q[3] = cos(th) * sin(psi);
+      Q[4] = sin(phi) * sin(th) * sin(psi) + cos(phi) * cos(psi);
+      Q[5] = cos(phi) * sin(th) * sin(psi) - sin(phi) * cos(psi);
+      Q[6] = -sin(th);
+      Q[7] = sin(phi) * cos(th);
+      Q[8] = cos(phi) * cos(th);
+    }
     M3<double> CQ, Qi;
     for (int k = 0; k < 9; ++k) { CQ[k] = D.CQ[k]; Qi[k] = b.Qn[(int64_t)node * 9 + k]; }
     Q = tmul(CQ, mul(Q, CQ));

@@ -162,7 +162,7 @@ struct DispEntry {
   int structure;
   int node;
   int table;
-  int pad;
+  int angular;  // GF_ANGLES_EULER or GF_ANGLES_VECTOR
   double CQ[9];
 };
 

@@ -21,7 +21,7 @@ for the blocks of a Beam_1 / Shell_1 Static or Dynamic solution step:
   Loads           NodalLoad id NodeSet CS NTimes n + n rows (t, 6 values);
                   ShellLoad id ElementSet AreaUpdate NTimes n + n rows (t, p)
   Displacements   NodalDisplacement id NodeSet CS [AngularParameters
-                  EulerAngles] [BoolTable ...] NTimes n + n rows
+                  EulerAngles | EulerVector] [BoolTable ...] NTimes n + n rows
                   (src/NodalDisplacement.cpp:40-120)
   Constraints     NodalConstraint id NodeSet + UX..ROTZ BoolTable ...
   ConvergenceCriteria  the twelve tolerances and references
@@ -308,10 +308,11 @@ def read_deck(text: str, step: int = 1) -> Structure:
                 ns = tk.int()
                 tk.expect("CS")
                 c = tk.int()
+                ap = "EulerAngles"
                 if tk.peek() == "AngularParameters":
                     tk.next()
                     ap = tk.next()
-                    if ap != "EulerAngles":
+                    if ap not in ("EulerAngles", "EulerVector"):
                         raise DeckError(f"NodalDisplacement: AngularParameters '{ap}' is not supported")
                 active = [True]
                 if tk.peek() == "BoolTable":
@@ -319,7 +320,7 @@ def read_deck(text: str, step: int = 1) -> Structure:
                     active = tk.bool_table()
                 if tk.next() != "NTimes":
                     raise DeckError("NodalDisplacement: only tabulated displacements (NTimes) are supported")
-                disps.append((ns, c, active, _table(tk, tk.int(), 6)))
+                disps.append((ns, c, active, _table(tk, tk.int(), 6), ap))
         elif kw == "Constraints":
             for _ in range(tk.int()):
                 kind = tk.next()
@@ -406,10 +407,10 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
             if any(e not in shell_of for e in members):
                 raise DeckError(f"ShellLoad on element set {es}: every element must be a Shell_1")
             s.loads.append(PressureLoad([shell_of[e] for e in members], table, area_update=au))
-    for ns, c, active, table in disps:
+    for ns, c, active, table, ap in disps:
         if _step_value(active, step):
             s.displacements.append(NodalDisplacement([n - 1 for n in lookup(node_sets, ns, "node set")],
-                                                     lookup(cs_ix, c, "coordinate system"), table))
+                                                     lookup(cs_ix, c, "coordinate system"), table, ap))
     s.solution = steps[step - 1]
     s.criteria = dict(criteria)
     return s

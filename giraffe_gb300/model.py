@@ -71,7 +71,7 @@ class gf_load(C.Structure):
 
 
 class gf_displacement(C.Structure):
-    _fields_ = [("n_nodes", C.c_int), ("nodes", _vp), ("cs", C.c_int), ("table", gf_table)]
+    _fields_ = [("n_nodes", C.c_int), ("nodes", _vp), ("cs", C.c_int), ("table", gf_table), ("angular", C.c_int)]
 
 
 class gf_solution(C.Structure):
@@ -206,6 +206,7 @@ class NodalDisplacement:
     nodes: list
     cs: int
     table: Table
+    angular: str = "EulerAngles"  # or "EulerVector": how the rotation columns are read
 
 
 @dataclass
@@ -387,7 +388,7 @@ class Structure:
             rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
                              for t, vals in zip(D.table.times, D.table.values))
             disp_lines.append(f"NodalDisplacement\t{len(disp_lines) + 1}\tNodeSet\t{ns}\tCS\t{D.cs + 1}"
-                              f"\tNTimes\t{len(D.table.times)}\n{rows}")
+                              f"\tAngularParameters\t{D.angular}\tNTimes\t{len(D.table.times)}\n{rows}")
         if sets:
             o.append(f"NodeSets\t{len(sets)}")
             for i, nodes in enumerate(sets):
@@ -465,6 +466,7 @@ class DescHandle:
             disps[k].n_nodes = len(nd)
             disps[k].nodes = _ptr(nd, _ip)
             disps[k].cs = D.cs
+            disps[k].angular = 1 if D.angular == "EulerVector" else 0
             disps[k].table = gf_table(len(tt), tv.shape[1], _ptr(tt, _dp), _ptr(tv, _dp))
         self.keep += [loads, disps]
         so = s.solution

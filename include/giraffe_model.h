@@ -44,12 +44,17 @@ typedef struct gf_load {
 } gf_load;
 
 /* NodalDisplacement (reference src/NodalDisplacement.cpp:158-208): the six
- * table columns are prescribed UX UY UZ ROTX ROTY ROTZ in cs. */
+ * table columns are prescribed UX UY UZ ROTX ROTY ROTZ in cs; the rotation
+ * columns are Euler angles (AngularParameters EulerAngles, the default) or
+ * the components of an Euler rotation vector (EulerVector,
+ * src/NodalDisplacement.cpp:327-350). */
+enum { GF_ANGLES_EULER = 0, GF_ANGLES_VECTOR = 1 };
 typedef struct gf_displacement {
   int n_nodes;
   const int* nodes;
   int cs;
   gf_table table;
+  int angular; /* GF_ANGLES_EULER or GF_ANGLES_VECTOR */
 } gf_displacement;
 
 /* Static (reference src/Static.cpp:43-130) and Dynamic

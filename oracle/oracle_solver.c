@@ -12,7 +12,7 @@
  *   reference src/Solution.cpp:798-849      Zeros, Clear
  *   reference src/ConvergenceCriteria.cpp:187-618
  *   reference src/NodalLoad.cpp:230-401     (UpdateforSolutionStep, Mount)
- *   reference src/NodalDisplacement.cpp:158-208, 327-410 (EulerAngles)
+ *   reference src/NodalDisplacement.cpp:158-208, 327-410 (EulerAngles, EulerVector)
  *   reference src/Node.cpp:325-370          SaveConfiguration
  * The linear solve (PARDISO in the reference, src/SparseMatrix.cpp:74-166)
  * is an FP64 banded LU with partial pivoting on the same K_AA.
@@ -416,7 +416,20 @@ static void mount_displacements(ost* s) {
       double th = s->cons[6 * node + 4] == 1 ? table_at(&D->table, time, 4) : 0.0;
       double psi = s->cons[6 * node + 5] == 1 ? table_at(&D->table, time, 5) : 0.0;
       double Q[9], t[9], Qd[9];
-      euler_angles_Q(Q, phi, th, psi);
+      if (D->angular == GF_ANGLES_VECTOR) {
+        /* EulerVector: Rodrigues parameters of length 2 tan(|e|/2) along e
+         * (reference src/NodalDisplacement.cpp:330-350) */
+        double en = sqrt(phi * phi + th * th + psi * psi), inv = en != 0.0 ? 1.0 / en : 0.0;
+        double rod = 2.0 * tan(en / 2.0);
+        double rv[3] = {rod * (inv * phi), rod * (inv * th), rod * (inv * psi)}, A[9], A2[9];
+        double g = 4.0 / (4.0 + rod * rod);
+        m3_skew(A, rv);
+        m3_mul(A2, A, A);
+        for (int k = 0; k < 9; ++k) Q[k] = g * (A[k] + 0.5 * A2[k]);
+        Q[0] += 1.0; Q[4] += 1.0; Q[8] += 1.0;
+      } else {
+        euler_angles_Q(Q, phi, th, psi);
+      }
       m3_mul(t, Q, CQ);
       m3_tmul(Q, CQ, t);
       m3_mult(Qd, Q, s->Qn + 9 * node);

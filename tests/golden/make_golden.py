@@ -26,6 +26,10 @@ stores what the reference computes:
 * ref_riser_rayleigh.npz a 12-element riser under a prescribed top motion
                          with Rayleigh damping (alpha 0.3, beta 0.004,
                          Update 1), 120 steps.
+* ref_rotating_base_angles.npz, ref_rotating_base_vector.npz
+                         a cantilever whose base turns by a prescribed rotation
+                         read as Euler angles / as an Euler rotation vector
+                         (NodalDisplacement AngularParameters), 10 steps.
 * ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
                          single elements (Beam_1::MountMass) with random
                          history, increments, nodal velocities/accelerations.
@@ -306,6 +310,8 @@ DECKS = {
     "ref_tutorial10.npz": configs.tutorial10,
     "ref_plate.npz": lambda: configs.square_plate(4, steps=20),
     "ref_plate_fixed_area.npz": lambda: configs.square_plate(3, steps=10, area_update=0),
+    "ref_rotating_base_angles.npz": lambda: configs.rotating_base("EulerAngles"),
+    "ref_rotating_base_vector.npz": lambda: configs.rotating_base("EulerVector"),
     "ref_tutorial10_rayleigh.npz": lambda: configs.tutorial10(0.2, 0.002, 0),
     "ref_tutorial10_rayleigh_update.npz": lambda: configs.tutorial10(0.2, 0.002, 1),
     "ref_riser_rayleigh.npz": lambda: configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0,

@@ -37,7 +37,7 @@ def same_structure(a, b):
         assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
     assert len(a.displacements) == len(b.displacements)
     for x, y in zip(a.displacements, b.displacements):
-        assert list(x.nodes) == list(y.nodes) and x.cs == y.cs
+        assert list(x.nodes) == list(y.nodes) and x.cs == y.cs and x.angular == y.angular
         assert np.array_equal(x.table.times, y.table.times)
         assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
     assert a.solution == b.solution
@@ -47,7 +47,7 @@ def same_structure(a, b):
 @pytest.mark.parametrize("make", [
     configs.tutorial01, configs.cantilever_rollup, lambda: configs.tutorial10(0.2, 0.002, 1),
     lambda: configs.pipe_chain(25, 0.4, 0.03, [1e5, -2e4, 3e4]),
-    lambda: configs.riser_chain(15, 0.35, 0.025, 1.0, 6.0, steps=30),
+    lambda: configs.riser_chain(15, 0.35, 0.025, 1.0, 6.0, steps=30), lambda: configs.rotating_base("EulerVector"),
     lambda: configs.square_plate(3, steps=10, area_update=0), lambda: configs.square_plate(4, steps=20),
 ])
 def test_written_deck_reads_back_the_same(make):

@@ -236,3 +236,19 @@ def test_assembly_csr_matches_oracle(gpu_ctx):
         assert rel(dense, ref) < 1e-13
         assert rel(P, P_o) < 1e-13
     b.close()
+
+
+@pytest.mark.parametrize("name,angular", [("ref_rotating_base_angles.npz", "EulerAngles"),
+                                          ("ref_rotating_base_vector.npz", "EulerVector")])
+def test_prescribed_base_rotation_matches_reference(gpu_ctx, golden, name, angular):
+    """Prescribed rotations as Euler angles and as an Euler rotation vector
+    (NodalDisplacement AngularParameters) against the reference's runs."""
+    s = configs.rotating_base(angular)
+    g = golden(name)
+    finals, stats = _solve_gpu(gpu_ctx, [s])
+    ref = g["nodes"][-1]
+    scale = np.abs(ref[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(finals[0][:, 6:] - ref[:, 6:]).max() <= 1e-9
+    _, so, _ = oracle.solve(s)
+    assert list(stats[0]) == list(so)
