@@ -116,6 +116,16 @@ def tutorial10(rayleigh_alpha: float = 0.0, rayleigh_beta: float = 0.0, update_r
     return s
 
 
+def pretensioned_chain(n_el: int = 20, T0: float = 2e5, steps: int = 10) -> Structure:
+    """A pipe chain like the benchmark's (10 m, tube 0.4 x 0.03) whose
+    elements carry a PreTension T0 (reference length shortened by
+    1 + T0 / EA, Gauss points starting stretched), under a lateral tip
+    force."""
+    s = pipe_chain(n_el, 0.4, 0.03, [4e4, -2e4, 0.0], steps=steps, element_length=10.0 / n_el)
+    s.pretension = {e: T0 for e in range(n_el)}
+    return s
+
+
 def rotating_base(angular: str = "EulerAngles", steps: int = 10) -> Structure:
     """tutorial01's cantilever (10 Beam_1 along z) whose clamped base is turned
     by a prescribed rotation with components (0.4, -0.3, 1.2) at t = 1, read

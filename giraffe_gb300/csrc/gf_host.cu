@@ -67,7 +67,7 @@ void cs_rows(double* Q, const double* e1e3) {
 }
 
 void beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec, const double* cs,
-                  BeamConst& c, BeamHist& h, BeamHistAux& x) {
+                  BeamConst& c, BeamHist& h, BeamHistAux& x, double T0 = 0.0) {
   std::memset(&c, 0, sizeof(c));
   std::memset(&h, 0, sizeof(h));
   std::memset(&x, 0, sizeof(x));
@@ -93,7 +93,11 @@ void beam_precalc(const double* x0, const double* x2, const double* mat, const d
   double inv = 1.0 / len;
   for (int k = 0; k < 3; ++k) e3[k] = inv * e3[k];
   for (int i = 0; i < 3; ++i) c.e3r[i] = c.T3[i * 3] * e3[0] + c.T3[i * 3 + 1] * e3[1] + c.T3[i * 3 + 2] * e3[2];
-  c.jac = len / 2.0;
+  // pre-strain of a pre-tension T0: the reference length is the distance of
+  // the end nodes shortened by 1 + T0 / EA, and the Gauss points start
+  // stretched (reference src/Beam_1.cpp:616-621)
+  const double du0 = T0 / c.Dd[2];
+  c.jac = (len / (1.0 + du0)) / 2.0;
   for (int g = 0; g < 2; ++g) {
     double xi = g == 0 ? -0.577350269189626 : +0.577350269189626;
     c.N[g][0] = 0.5 * xi * (xi - 1.0);
@@ -105,7 +109,7 @@ void beam_precalc(const double* x0, const double* x2, const double* mat, const d
   }
   for (int g = 0; g < 2; ++g) {
     h.Q[g][0] = h.Q[g][4] = h.Q[g][8] = 1.0;
-    h.dz[g][2] = 1.0;
+    h.dz[g][2] = 1.0 + du0;
   }
 }
 
@@ -650,7 +654,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     for (int e = 0; e < m.n_beams; ++e) {
       const int* be = m.beams + 6 * e;
       beam_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.materials + 3 * be[3], m.sections + 6 * be[4],
-                   m.cs + 6 * be[5], bconst[eo + e], bhist[eo + e], baux[eo + e]);
+                   m.cs + 6 * be[5], bconst[eo + e], bhist[eo + e], baux[eo + e],
+                   m.beam_pretension ? m.beam_pretension[e] : 0.0);
       for (int j = 0; j < 3; ++j) enodes[(size_t)(eo + e) * 3 + j] = no + be[j];
       estruct[eo + e] = s;
       unsigned used = node_colors[be[0]] | node_colors[be[1]] | node_colors[be[2]];

@@ -205,11 +205,11 @@ def read_deck(text: str, step: int = 1) -> Structure:
                     c = tk.int()
                     tk.expect("Nodes")
                     nd = [tk.int() for _ in range(3)]
+                    t0 = 0.0
                     if tk.peek() == "PreTension":
                         tk.next()
-                        if tk.float() != 0.0:
-                            raise DeckError(f"Beam_1 {eid}: PreTension is not supported")
-                    elems.append(("Beam_1", eid, m, sc, c, nd))
+                        t0 = tk.float()
+                    elems.append(("Beam_1", eid, m, sc, c, nd, t0))
                 elif kind == "Shell_1":
                     tk.expect("Mat")
                     m = tk.int()
@@ -221,7 +221,7 @@ def read_deck(text: str, step: int = 1) -> Structure:
                         c = tk.int()
                     tk.expect("Nodes")
                     nd = [tk.int() for _ in range(6)]
-                    elems.append(("Shell_1", eid, m, sc, c, nd))
+                    elems.append(("Shell_1", eid, m, sc, c, nd, 0.0))
                 else:
                     raise DeckError(f"element type '{kind}' is not solved by this library")
         elif kw == "Materials":
@@ -382,10 +382,12 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
         return table[i]
 
     shell_of = {}
-    for kind, eid, m, sc, c, nd in sorted(elems, key=lambda e: e[1]):
+    for kind, eid, m, sc, c, nd, t0 in sorted(elems, key=lambda e: e[1]):
         if any(n not in nodes for n in nd):
             raise DeckError(f"element {eid} refers to a missing node")
         if kind == "Beam_1":
+            if t0 != 0.0:
+                s.pretension[len(s.beams)] = t0
             s.beams.append((nd[0] - 1, nd[1] - 1, nd[2] - 1, lookup(mat_ix, m, "material"),
                             lookup(sec_ix, sc, "section"), lookup(cs_ix, c, "coordinate system")))
         else:

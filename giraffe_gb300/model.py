@@ -100,7 +100,7 @@ class gf_model_desc(C.Structure):
                 ("constraints", _vp),
                 ("n_loads", C.c_int), ("loads", _vp),
                 ("n_displacements", C.c_int), ("displacements", _vp),
-                ("solution", gf_solution), ("criteria", gf_criteria)]
+                ("solution", gf_solution), ("criteria", gf_criteria), ("beam_pretension", _vp)]
 
 
 def _r(v):
@@ -250,6 +250,7 @@ class Structure:
     displacements: list = field(default_factory=list)
     solution: Solution = field(default_factory=Solution)
     criteria: dict = field(default_factory=lambda: dict(DEFAULT_CRITERIA))
+    pretension: dict = field(default_factory=dict)     # beam index -> Beam_1 PreTension T0
 
     def __setattr__(self, name, value):
         # element rows assigned as lists become ElementTables
@@ -332,10 +333,11 @@ class Structure:
             o.append(f"Node\t{i + 1}\t{_r(x[0])}\t{_r(x[1])}\t{_r(x[2])}")
         o.append(f"Elements\t{len(self.beams) + len(self.shells)}")
         k = 0
-        for b in self.beams:
+        for e, b in enumerate(self.beams):
             k += 1
+            t0 = float(self.pretension.get(e, 0.0))
             o.append(f"Beam_1\t{k}\tMat\t{b[3] + 1}\tSec\t{b[4] + 1}\tCS\t{b[5] + 1}\tNodes\t"
-                     f"{b[0] + 1}\t{b[1] + 1}\t{b[2] + 1}")
+                     f"{b[0] + 1}\t{b[1] + 1}\t{b[2] + 1}" + (f"\tPreTension\t{_r(t0)}" if t0 != 0.0 else ""))
         for sh in self.shells:
             k += 1
             nodes = "\t".join(str(v + 1) for v in sh[:6])
@@ -474,11 +476,17 @@ class DescHandle:
                           so.min_time_step, so.max_it, so.min_it, so.conv_increase, so.inc_factor,
                           so.beta, so.gamma, so.rayleigh_alpha, so.rayleigh_beta, so.update_rayleigh)
         crit = gf_criteria(**{k: float(v) for k, v in s.criteria.items()})
+        pre = None
+        if s.pretension:
+            pre = np.zeros(max(1, len(s.beams)))
+            for e, t0 in s.pretension.items():
+                pre[int(e)] = float(t0)
+            self.keep.append(pre)
         self.desc = gf_model_desc(
             len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
             len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
             len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), C.addressof(loads),
-            len(s.displacements), C.addressof(disps), sol, crit)
+            len(s.displacements), C.addressof(disps), sol, crit, _ptr(pre))
 
     @property
     def ref(self):

@@ -108,6 +108,8 @@ typedef struct gf_model_desc {
   const gf_displacement* displacements;
   gf_solution solution;
   gf_criteria criteria;
+  const double* beam_pretension; /* [n_beams]: Beam_1 PreTension T0 (force), or NULL
+                                    (reference src/Beam_1.cpp:420-428, 616-621) */
 } gf_model_desc;
 
 #ifdef __cplusplus

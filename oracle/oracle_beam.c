@@ -15,7 +15,7 @@
 
 /* reference src/Beam_1.cpp:501-692 (Hooke material, non-special section) */
 void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec,
-                         const double* cs, ob_const* c, ob_hist* h) {
+                         const double* cs, double T0, ob_const* c, ob_hist* h) {
   double E = mat[0], nu = mat[1], rho = mat[2];
   double G = E / (2 * (1 + nu));
   double sf = 1.0;
@@ -40,8 +40,10 @@ void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, 
   double inv = 1.0 / v3_norm(e3);
   for (int k = 0; k < 3; ++k) e3[k] = inv * e3[k];
   m3_vec(c->e3r, c->T3, e3);
-  /* no pre-tension: du0 = 0, dz_i = e3 (reference src/Beam_1.cpp:616-621) */
-  c->jac = len / 2.0;
+  /* pre-tension T0: du0 = T0 / EA, reference length |x2 - x0| / (1 + du0),
+   * dz_i = (1 + du0) e3 (reference src/Beam_1.cpp:616-621) */
+  double du0 = T0 / c->D[2 * 6 + 2];
+  c->jac = (len / (1.0 + du0)) / 2.0;
   for (int g = 0; g < 2; ++g) {
     double xi = g == 0 ? -0.577350269189626 : +0.577350269189626;
     c->N[g][0] = 0.5 * xi * (xi - 1.0);
@@ -55,7 +57,7 @@ void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, 
     memset(h, 0, sizeof(*h));
     for (int g = 0; g < 2; ++g) {
       m3_eye(h->Q[g]);
-      h->dz[g][2] = 1.0;
+      h->dz[g][2] = 1.0 + du0;
     }
   }
 }

@@ -25,7 +25,7 @@ typedef struct ob_hist {
 } ob_hist;
 
 void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec,
-                         const double* cs, ob_const* c, ob_hist* h);
+                         const double* cs, double pretension, ob_const* c, ob_hist* h);
 void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
                        double* strain_energy);
 void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);

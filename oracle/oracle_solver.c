@@ -125,7 +125,8 @@ static int ost_init(ost* s, const gf_model_desc* m) {
   for (int e = 0; e < s->nb; ++e) {
     const int* b = m->beams + 6 * e;
     oracle_beam_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->materials + 3 * b[3],
-                        m->sections + 6 * b[4], m->cs + 6 * b[5], s->bc + e, s->bh + e);
+                        m->sections + 6 * b[4], m->cs + 6 * b[5], m->beam_pretension ? m->beam_pretension[e] : 0.0,
+                        s->bc + e, s->bh + e);
   }
   /* Shell_1::PreCalc */
   for (int e = 0; e < s->ns; ++e) {
@@ -734,7 +735,7 @@ int oracle_beam_element(const double* xyz9, const double* mat3, const double* se
                         int n_hist, const double* hist_disp, const double* disp18, double* K, double* f) {
   ob_const c;
   ob_hist h;
-  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, &c, &h);
+  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, 0.0, &c, &h);
   for (int q = 0; q < n_hist; ++q) oracle_beam_commit(&c, &h, hist_disp + 18 * q);
   oracle_beam_mount(&c, &h, disp18, K, f, NULL);
   return 0;
@@ -777,7 +778,7 @@ int oracle_beam_inertia_element(const double* xyz9, const double* mat3, const do
                                 double* ke) {
   ob_const c;
   ob_hist h;
-  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, &c, &h);
+  oracle_beam_precalc(xyz9, xyz9 + 6, mat3, sec6, cs6, 0.0, &c, &h);
   for (int q = 0; q < n_hist; ++q) oracle_beam_commit(&c, &h, hist_disp + 18 * q);
   double a[6];
   newmark_coeff(dt, beta, gamma, a);

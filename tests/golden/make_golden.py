@@ -30,6 +30,8 @@ stores what the reference computes:
                          a cantilever whose base turns by a prescribed rotation
                          read as Euler angles / as an Euler rotation vector
                          (NodalDisplacement AngularParameters), 10 steps.
+* ref_pretension.npz     a 20-element pipe chain with PreTension 2e5 N in every
+                         element under a lateral tip force, 10 steps.
 * ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
                          single elements (Beam_1::MountMass) with random
                          history, increments, nodal velocities/accelerations.
@@ -310,6 +312,7 @@ DECKS = {
     "ref_tutorial10.npz": configs.tutorial10,
     "ref_plate.npz": lambda: configs.square_plate(4, steps=20),
     "ref_plate_fixed_area.npz": lambda: configs.square_plate(3, steps=10, area_update=0),
+    "ref_pretension.npz": configs.pretensioned_chain,
     "ref_rotating_base_angles.npz": lambda: configs.rotating_base("EulerAngles"),
     "ref_rotating_base_vector.npz": lambda: configs.rotating_base("EulerVector"),
     "ref_tutorial10_rayleigh.npz": lambda: configs.tutorial10(0.2, 0.002, 0),

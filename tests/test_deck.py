@@ -41,6 +41,7 @@ def same_structure(a, b):
         assert np.array_equal(x.table.times, y.table.times)
         assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
     assert a.solution == b.solution
+    assert {int(k): float(v) for k, v in a.pretension.items()} == {int(k): float(v) for k, v in b.pretension.items()}
     assert {k: float(v) for k, v in a.criteria.items()} == {k: float(v) for k, v in b.criteria.items()}
 
 
@@ -48,6 +49,7 @@ def same_structure(a, b):
     configs.tutorial01, configs.cantilever_rollup, lambda: configs.tutorial10(0.2, 0.002, 1),
     lambda: configs.pipe_chain(25, 0.4, 0.03, [1e5, -2e4, 3e4]),
     lambda: configs.riser_chain(15, 0.35, 0.025, 1.0, 6.0, steps=30), lambda: configs.rotating_base("EulerVector"),
+    configs.pretensioned_chain,
     lambda: configs.square_plate(3, steps=10, area_update=0), lambda: configs.square_plate(4, steps=20),
 ])
 def test_written_deck_reads_back_the_same(make):

@@ -252,3 +252,14 @@ def test_prescribed_base_rotation_matches_reference(gpu_ctx, golden, name, angul
     assert np.abs(finals[0][:, 6:] - ref[:, 6:]).max() <= 1e-9
     _, so, _ = oracle.solve(s)
     assert list(stats[0]) == list(so)
+
+
+def test_pretensioned_chain_matches_reference(gpu_ctx, golden):
+    s = configs.pretensioned_chain()
+    g = golden("ref_pretension.npz")
+    finals, stats = _solve_gpu(gpu_ctx, [s])
+    ref = g["nodes"][-1]
+    scale = np.abs(ref[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref[:, :3]).max() <= 1e-10 * scale
+    _, so, _ = oracle.solve(s)
+    assert list(stats[0]) == list(so)

@@ -145,3 +145,9 @@ def test_prescribed_base_rotation_matches_reference(golden, name, angular):
     final, _, _ = _check_run(golden(name), configs.rotating_base(angular), tol=1e-10)
     other = golden("ref_rotating_base_vector.npz" if angular == "EulerAngles" else "ref_rotating_base_angles.npz")
     assert np.abs(final[:, :3] - other["nodes"][-1][:, :3]).max() > 0.1
+
+
+def test_pretensioned_chain_matches_reference(golden):
+    """Beam_1 PreTension: reference length shortened by 1 + T0 / EA and the
+    Gauss points starting stretched (Beam_1::PreCalc)."""
+    _check_run(golden("ref_pretension.npz"), configs.pretensioned_chain(), tol=1e-10)
