@@ -269,6 +269,24 @@ def square_plate(n: int = 64, side: float = 1.0, thickness: float = 0.01, E: flo
     return s
 
 
+def plate_dynamics(n: int = 4, pressure: float = 1e5, rise: float = 0.002, dt: float = 0.001, steps: int = 30,
+                   area_update: int = 1, rayleigh_alpha: float = 0.0, rayleigh_beta: float = 0.0,
+                   update_rayleigh: int = 0, beta: float = 0.25, gamma: float = 0.5, tol: float = 1e-8,
+                   **plate) -> Structure:
+    """The clamped square plate of square_plate in a Dynamic step (Newmark
+    beta, gamma, time step dt, `steps` steps): the follower pressure rises
+    linearly to `pressure` over `rise` seconds and then stays, so the plate
+    vibrates about its static deflection (the first mode of the 1 m, 10 mm
+    aluminium plate has a period near 11 ms).  Optional Rayleigh damping
+    C = alpha M + beta K, formed once or (update_rayleigh 1) every
+    iteration."""
+    s = square_plate(n, pressure=pressure, steps=steps, area_update=area_update, tol=tol, **plate)
+    s.loads[0].table = Table(np.array([0.0, rise]), np.array([[0.0], [pressure]]))
+    s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 4096, 30, 3, 4, 1.0, beta=beta, gamma=gamma,
+                          rayleigh_alpha=rayleigh_alpha, rayleigh_beta=rayleigh_beta, update_rayleigh=update_rayleigh)
+    return s
+
+
 def served_mixed(n_requests: int, seed: int = 0, plate_share: float = 0.3, chain_dof=(1000, 50000),
                  plate_dof=(10000, 200000), steps: int = 10, tol: float = 1e-8) -> list:
     """The mixed served stream: each request is a pipe chain (free DOFs

@@ -59,6 +59,14 @@ int oracle_beam_element(const double* xyz9, const double* mat3, const double* se
 int oracle_shell_element(const double* xyz18, const double* mat3, double thickness, int n_hist,
                          const double* hist_disp, const double* disp27, int with_pressure, double pressure,
                          int area_update, double* K, double* f);
+/* Shell_1 MountMass of one element after n_hist committed increments:
+ * vel36 / acc36 = [6][6] converged nodal velocities and accelerations
+ * (global), Newmark time step and parameters; M: 27x27 column-major,
+ * F: 27, *ke. */
+int oracle_shell_inertia_element(const double* xyz18, const double* mat3, double thickness, int n_hist,
+                                 const double* hist_disp, const double* disp27, const double* vel36,
+                                 const double* acc36, double dt, double beta, double gamma, double* M, double* F,
+                                 double* ke);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,8 @@ def lib():
                                               dp, dp]
         _lib.oracle_beam_inertia_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double,
                                                      C.c_double, dp, dp, dp]
+        _lib.oracle_shell_inertia_element.argtypes = [dp, dp, C.c_double, C.c_int, dp, dp, dp, dp, C.c_double,
+                                                      C.c_double, C.c_double, dp, dp, dp]
     return _lib
 
 
@@ -122,3 +124,18 @@ def beam_inertia(xyz9, mat3, sec6, cs6, hist_disp, disp18, vel18, acc18, dt, bet
                                       _dp(args[4]), _dp(args[5]), _dp(args[6]), dt, beta, gamma, _dp(M), _dp(F),
                                       _dp(ke))
     return M.reshape(18, 18).T, F, ke[0]
+
+
+def shell_inertia(xyz18, mat3, thickness, hist_disp, disp27, vel36, acc36, dt, beta, gamma):
+    """Shell_1 MountMass of one element (oracle_shell_inertia_element): the
+    mass/gyroscopic tangent row-major [r][s], the inertial force, the kinetic
+    energy."""
+    M = np.zeros(729)
+    F = np.zeros(27)
+    ke = np.zeros(1)
+    nh = 0 if hist_disp is None else len(hist_disp)
+    hd = np.ascontiguousarray(hist_disp if nh else np.zeros((1, 27)), dtype=np.float64)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz18, mat3, disp27, vel36, acc36)]
+    lib().oracle_shell_inertia_element(_dp(args[0]), _dp(args[1]), float(thickness), nh, _dp(hd), _dp(args[2]),
+                                       _dp(args[3]), _dp(args[4]), dt, beta, gamma, _dp(M), _dp(F), _dp(ke))
+    return M.reshape(27, 27).T, F, ke[0]

@@ -283,13 +283,69 @@ void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d) {
  *                   - g^2/2 (h + da x h / 2) da^T - g/2 skew(h).
  * The element sums wJ N^T dT and wJ N^T DdT N and turns them to the global
  * frame. */
+void oracle_gp_inertia(double Mr, const double* Jr, const double* alpha_i, const double* du, const double* da,
+                       const double* vi, const double* ai, const double* wi, const double* dwi, const double* a,
+                       double* dT, double* DdT, double* ke) {
+  const double a1 = a[0], a2 = a[1], a3 = a[2], a4 = a[3], a5 = a[4], a6 = a[5];
+  memset(DdT, 0, 36 * sizeof(double));
+  for (int i = 0; i < 3; ++i) {
+    dT[i] = Mr * (a1 * du[i] - a2 * vi[i] - a3 * ai[i]);
+    DdT[i * 6 + i] = a1 * Mr;
+  }
+  double Qi[9], Ji[9], t[9];
+  rodrigues_Q(Qi, alpha_i);
+  m3_mul(t, Qi, Jr);
+  m3_mult(Ji, t, Qi);
+  double w1[3], w2[3], Jw1[3], Jw2[3], cr[3], hv[3];
+  for (int i = 0; i < 3; ++i) {
+    w1[i] = a4 * da[i] + a5 * wi[i] + a6 * dwi[i];
+    w2[i] = a1 * da[i] - a2 * wi[i] - a3 * dwi[i];
+  }
+  m3_vec(Jw1, Ji, w1);
+  m3_vec(Jw2, Ji, w2);
+  v3_cross(cr, w1, Jw1);
+  for (int i = 0; i < 3; ++i) hv[i] = Jw2[i] + cr[i];
+  double n2 = v3_dot(da, da);
+  double gg = 4.0 / (4.0 + n2);
+  double A[9], Xi[9];
+  m3_skew(A, da);
+  for (int q = 0; q < 9; ++q) Xi[q] = gg * 0.5 * A[q];
+  Xi[0] += gg; Xi[4] += gg; Xi[8] += gg;
+  double m[3];
+  m3_vec(m, Xi, hv);
+  for (int i = 0; i < 3; ++i) dT[3 + i] = m[i];
+  /* dh/dda = a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)) */
+  double Sw1[9], SJw1[9], Dh[9];
+  m3_skew(Sw1, w1);
+  m3_skew(SJw1, Jw1);
+  m3_mul(t, Sw1, Ji);
+  for (int q = 0; q < 9; ++q) Dh[q] = a1 * Ji[q] + a4 * (t[q] - SJw1[q]);
+  double XDh[9], axh[3], hh[3], Sh[9];
+  m3_mul(XDh, Xi, Dh);
+  v3_cross(axh, da, hv);
+  for (int i = 0; i < 3; ++i) hh[i] = hv[i] + 0.5 * axh[i];
+  m3_skew(Sh, hv);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      DdT[(3 + i) * 6 + 3 + j] = XDh[i * 3 + j] - 0.5 * gg * gg * hh[i] * da[j] - 0.5 * gg * Sh[i * 3 + j];
+  /* kinetic energy at the end of the step */
+  double v1[3], om[3], Qd[9], Jom[3], Q[9], J[9];
+  for (int i = 0; i < 3; ++i) v1[i] = a4 * du[i] + a5 * vi[i] + a6 * ai[i];
+  rodrigues_Q(Qd, da);
+  m3_vec(om, Qd, w1);
+  m3_mul(Q, Qd, Qi);
+  m3_mul(t, Q, Jr);
+  m3_mult(J, t, Q);
+  m3_vec(Jom, J, om);
+  *ke = 0.5 * Mr * v3_dot(v1, v1) + 0.5 * v3_dot(om, Jom);
+}
+
 void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, const double* vel,
                          const double* acc, const double* a, double* K, double* f, double* kinetic) {
   double Kl[18 * 18], fl[18];
   memset(Kl, 0, sizeof(Kl));
   memset(fl, 0, sizeof(fl));
   double ke = 0.0;
-  const double a1 = a[0], a2 = a[1], a3 = a[2], a4 = a[3], a5 = a[4], a6 = a[5];
   for (int g = 0; g < 2; ++g) {
     const double* N = c->N[g];
     double da[3] = {0, 0, 0}, du[3] = {0, 0, 0}, wi[3] = {0, 0, 0}, dwi[3] = {0, 0, 0}, vi[3] = {0, 0, 0},
@@ -309,48 +365,8 @@ void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, c
     m3_vec(dwi, c->T3, dwi);
     m3_vec(vi, c->T3, vi);
     m3_vec(ai, c->T3, ai);
-    double dT[6], DdT[36];
-    memset(DdT, 0, sizeof(DdT));
-    for (int i = 0; i < 3; ++i) {
-      dT[i] = c->Mr * (a1 * du[i] - a2 * vi[i] - a3 * ai[i]);
-      DdT[i * 6 + i] = a1 * c->Mr;
-    }
-    double Qi[9], Ji[9], t[9];
-    rodrigues_Q(Qi, h->alpha[g]);
-    m3_mul(t, Qi, c->Jr);
-    m3_mult(Ji, t, Qi);
-    double w1[3], w2[3], Jw1[3], Jw2[3], cr[3], hv[3];
-    for (int i = 0; i < 3; ++i) {
-      w1[i] = a4 * da[i] + a5 * wi[i] + a6 * dwi[i];
-      w2[i] = a1 * da[i] - a2 * wi[i] - a3 * dwi[i];
-    }
-    m3_vec(Jw1, Ji, w1);
-    m3_vec(Jw2, Ji, w2);
-    v3_cross(cr, w1, Jw1);
-    for (int i = 0; i < 3; ++i) hv[i] = Jw2[i] + cr[i];
-    double n2 = v3_dot(da, da);
-    double gg = 4.0 / (4.0 + n2);
-    double A[9], Xi[9];
-    m3_skew(A, da);
-    for (int q = 0; q < 9; ++q) Xi[q] = gg * 0.5 * A[q];
-    Xi[0] += gg; Xi[4] += gg; Xi[8] += gg;
-    double m[3];
-    m3_vec(m, Xi, hv);
-    for (int i = 0; i < 3; ++i) dT[3 + i] = m[i];
-    /* dh/dda = a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)) */
-    double Sw1[9], SJw1[9], Dh[9];
-    m3_skew(Sw1, w1);
-    m3_skew(SJw1, Jw1);
-    m3_mul(t, Sw1, Ji);
-    for (int q = 0; q < 9; ++q) Dh[q] = a1 * Ji[q] + a4 * (t[q] - SJw1[q]);
-    double XDh[9], axh[3], hh[3], Sh[9];
-    m3_mul(XDh, Xi, Dh);
-    v3_cross(axh, da, hv);
-    for (int i = 0; i < 3; ++i) hh[i] = hv[i] + 0.5 * axh[i];
-    m3_skew(Sh, hv);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
-        DdT[(3 + i) * 6 + 3 + j] = XDh[i * 3 + j] - 0.5 * gg * gg * hh[i] * da[j] - 0.5 * gg * Sh[i * 3 + j];
+    double dT[6], DdT[36], kg;
+    oracle_gp_inertia(c->Mr, c->Jr, h->alpha[g], du, da, vi, ai, wi, dwi, a, dT, DdT, &kg);
     double wJ = 1.0 * c->jac;
     for (int I = 0; I < 3; ++I) {
       for (int i = 0; i < 6; ++i) fl[6 * I + i] += wJ * N[I] * dT[i];
@@ -358,18 +374,7 @@ void oracle_beam_inertia(const ob_const* c, const ob_hist* h, const double* d, c
         for (int i = 0; i < 6; ++i)
           for (int j = 0; j < 6; ++j) Kl[(6 * I + i) + 18 * (6 * J + j)] += wJ * N[I] * N[J] * DdT[i * 6 + j];
     }
-    /* kinetic energy of the Gauss point at the end of the step */
-    double v1[3], om[3], Qd[9], Jom[3];
-    for (int i = 0; i < 3; ++i) v1[i] = a4 * du[i] + a5 * vi[i] + a6 * ai[i];
-    rodrigues_Q(Qd, da);
-    m3_vec(om, Qd, w1);
-    double Q[9];
-    m3_mul(Q, Qd, Qi);
-    m3_mul(t, Q, c->Jr);
-    double J[9];
-    m3_mult(J, t, Q);
-    m3_vec(Jom, J, om);
-    ke += wJ * (0.5 * c->Mr * v3_dot(v1, v1) + 0.5 * v3_dot(om, Jom));
+    ke += wJ * kg;
   }
   const double* T = c->T3;
   for (int bi = 0; bi < 6; ++bi)

@@ -29,6 +29,16 @@ void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, 
 void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
                        double* strain_energy);
 void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);
+/* One Gauss point of the inertia of a rigid cross-section (Beam_1) or
+ * director fibre (Shell_1), in the element frame: mass Mr per unit length or
+ * area, rotary inertia Jr in the reference frame, committed rotation vector
+ * alpha_i, increments du / da, converged translational velocity and
+ * acceleration vi / ai, angular velocity and acceleration wi / dwi, Newmark
+ * coefficients a[6].  dT: 6 inertial forces, DdT: 6x6 row-major tangent,
+ * *ke: kinetic energy density at the end of the step. */
+void oracle_gp_inertia(double Mr, const double* Jr, const double* alpha_i, const double* du, const double* da,
+                       const double* vi, const double* ai, const double* wi, const double* dwi, const double* a,
+                       double* dT, double* DdT, double* ke);
 /* Inertial force and its tangent (MountMass, Newmark coefficients a[6]);
  * vel/acc: [3][6] converged nodal velocities and accelerations. Adds to K
  * (18x18 column-major, global frame) and f. */

@@ -13,9 +13,15 @@
  *   1392-1467  MountShellSpecialLoads (follower pressure and its tangent)
  *   1650-1664  SaveLagrange
  *   1470-1510  TransformMatrix
+ *   2406-2498  MountMass (through the Gauss-point inertia shared with
+ *              Beam_1: a director fibre of mass coef1 per unit area and
+ *              rotary inertia coef2 (I - e3r e3r^T), whose inertial moment
+ *              coef2 d x (d'') equals J w' + w x J w with J = Q Jr Q^T)
+ *   2368-2396  MountMassModal and EvaluateMassModal (3171-)
  */
 #include "oracle_shell.h"
 #include "giraffe_oracle.h"
+#include "oracle_beam.h"
 
 #include <string.h>
 
@@ -80,6 +86,9 @@ void oracle_shell_precalc(const double* xyz, const double* mat, double thickness
   c->lambda = 2.0 * c->mu * nu / (1 - 2.0 * nu);
   c->stiff_drill = E * thickness * thickness * thickness;
   c->thick = thickness;
+  c->coef1 = thickness * mat[2];
+  c->coef2 = (1.0 / 12.0) * thickness * thickness * thickness * mat[2];
+  c->coef3 = mat[2] * thickness * A / (3 * 3.1415926535897932384626433832795);
   /* area-coordinate derivatives in the local frame */
   double d23[3], d31[3], d12[3], d32[3], d13[3], d21[3];
   for (int k = 0; k < 3; ++k) {
@@ -105,6 +114,9 @@ void oracle_shell_precalc(const double* xyz, const double* mat, double thickness
   for (int k = 0; k < 6; ++k) {
     c->w4[k] = A * (k < 3 ? wa : wb);
     shape_u(Lc[k], Lx1, Lx2, c->N4[k], c->N41[k], c->N42[k]);
+    c->Na4[k][0] = 1 - 2 * Lc[k][2];
+    c->Na4[k][1] = 1 - 2 * Lc[k][0];
+    c->Na4[k][2] = 1 - 2 * Lc[k][1];
   }
   c->alpha1 = A / 3.0;
   for (int g = 0; g < 3; ++g) {
@@ -496,4 +508,122 @@ int oracle_shell_element(const double* xyz18, const double* mat3, double thickne
     oracle_shell_pressure(&c, pu, pressure, area_update, K, f);
   }
   return 0;
+}
+
+/* TransformMatrix (reference src/Shell_1.cpp:1470-1510) applied to a local
+ * 27x27 (row-major Kl) and 27-vector: T^T Kl T added to K (column-major). */
+static void shell_to_global(const os_const* c, const double* Kl, const double* fl, double* K, double* f) {
+  for (int a = 0; a < 9; ++a)
+    for (int b = 0; b < 9; ++b) {
+      double Bl[9], t[9], o[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Bl[i * 3 + j] = Kl[(3 * a + i) * 27 + 3 * b + j];
+      m3_mul(t, Bl, c->T3);
+      m3_tmul(o, c->T3, t);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) K[(3 * a + i) + 27 * (3 * b + j)] += o[i * 3 + j];
+    }
+  if (f)
+    for (int a = 0; a < 9; ++a) {
+      double t3[3];
+      m3_tvec(t3, c->T3, fl + 3 * a);
+      for (int i = 0; i < 3; ++i) f[3 * a + i] += t3[i];
+    }
+}
+
+/* rows of the 6x27 interpolation N (translations of the six nodes, rotations
+ * of the midside nodes): N[i][col] for row i < 3 at col 3n+i with Nu[n], for
+ * row 3+i at col 18+3m+i with Na[m] */
+static void shell_add_NtDN(const double* Nu, const double* Na, const double* D, double w, double* Kl) {
+  int col[6][6];
+  double val[6][6];
+  for (int i = 0; i < 3; ++i)
+    for (int n = 0; n < 6; ++n) { col[i][n] = 3 * n + i; val[i][n] = Nu[n]; }
+  for (int i = 0; i < 3; ++i)
+    for (int n = 0; n < 6; ++n) {
+      col[3 + i][n] = n < 3 ? 18 + 3 * n + i : -1;
+      val[3 + i][n] = n < 3 ? Na[n] : 0.0;
+    }
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double dij = D[i * 6 + j];
+      if (dij == 0.0) continue;
+      for (int p = 0; p < 6; ++p) {
+        if (col[i][p] < 0) continue;
+        for (int q = 0; q < 6; ++q) {
+          if (col[j][q] < 0) continue;
+          Kl[col[i][p] * 27 + col[j][q]] += w * val[i][p] * dij * val[j][q];
+        }
+      }
+    }
+}
+
+void oracle_shell_inertia(const os_const* c, const os_hist* h, const double* d, const double* vel,
+                          const double* acc, const double* a, double* K, double* f, double* kinetic) {
+  double Kl[27 * 27], fl[27];
+  memset(Kl, 0, sizeof(Kl));
+  memset(fl, 0, sizeof(fl));
+  const double Jr[9] = {c->coef2, 0, 0, 0, c->coef2, 0, 0, 0, 0};
+  double ke = 0.0;
+  for (int g = 0; g < 3; ++g) {
+    const double* Nu = c->Nu[g];
+    const double* Na = c->Na[g];
+    double du[3] = {0, 0, 0}, da[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, ai[3] = {0, 0, 0}, wi[3] = {0, 0, 0},
+           dwi[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i) {
+      for (int n = 0; n < 6; ++n) {
+        du[i] += d[3 * n + i] * Nu[n];
+        vi[i] += vel[6 * n + i] * Nu[n];
+        ai[i] += acc[6 * n + i] * Nu[n];
+      }
+      for (int m = 0; m < 3; ++m) {
+        da[i] += d[18 + 3 * m + i] * Na[m];
+        wi[i] += vel[6 * (3 + m) + 3 + i] * Na[m];
+        dwi[i] += acc[6 * (3 + m) + 3 + i] * Na[m];
+      }
+    }
+    m3_vec(du, c->T3, du);
+    m3_vec(da, c->T3, da);
+    m3_vec(vi, c->T3, vi);
+    m3_vec(ai, c->T3, ai);
+    m3_vec(wi, c->T3, wi);
+    m3_vec(dwi, c->T3, dwi);
+    double dT[6], DdT[36], kg;
+    oracle_gp_inertia(c->coef1, Jr, h->alpha[g], du, da, vi, ai, wi, dwi, a, dT, DdT, &kg);
+    for (int i = 0; i < 3; ++i) {
+      for (int n = 0; n < 6; ++n) fl[3 * n + i] += c->alpha1 * Nu[n] * dT[i];
+      for (int m = 0; m < 3; ++m) fl[18 + 3 * m + i] += c->alpha1 * Na[m] * dT[3 + i];
+    }
+    shell_add_NtDN(Nu, Na, DdT, c->alpha1, Kl);
+    ke += c->alpha1 * kg;
+  }
+  shell_to_global(c, Kl, fl, K, f);
+  if (kinetic) *kinetic = ke;
+}
+
+void oracle_shell_modal_mass(const os_const* c, const double* rot, double* M) {
+  double Ml[27 * 27];
+  memset(Ml, 0, sizeof(Ml));
+  memset(M, 0, sizeof(double) * 27 * 27);
+  for (int k = 0; k < 6; ++k) {
+    double al[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int m = 0; m < 3; ++m) al[i] += rot[3 * m + i] * c->Na4[k][m];
+    m3_vec(al, c->T3, al);
+    /* director d = Q(alpha) e3r; rotation block coef2 (|d|^2 I - d d^T) +
+     * coef3 d d^T (EvaluateMassModal) */
+    double Q[9], dv[3];
+    rodrigues_Q(Q, al);
+    for (int i = 0; i < 3; ++i) dv[i] = Q[i * 3 + 2];
+    double d2 = v3_dot(dv, dv);
+    double D[36];
+    memset(D, 0, sizeof(D));
+    for (int i = 0; i < 3; ++i) {
+      D[i * 6 + i] = c->coef1;
+      for (int j = 0; j < 3; ++j)
+        D[(3 + i) * 6 + 3 + j] = (i == j ? c->coef2 * d2 : 0.0) + (c->coef3 - c->coef2) * dv[i] * dv[j];
+    }
+    shell_add_NtDN(c->N4[k], c->Na4[k], D, c->w4[k], Ml);
+  }
+  shell_to_global(c, Ml, NULL, M, NULL);
 }

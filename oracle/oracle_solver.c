@@ -69,13 +69,14 @@ typedef struct {
   int ray, ray_update, ray_init;
   double ray_alpha, ray_beta;
   double* rd;   /* [nb][18x18] column-major */
+  double* rds;  /* [ns][27x27] column-major (Shell_1::MountDamping) */
 } ost;
 
 static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
   free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
-  free(s->rd);
+  free(s->rd); free(s->rds);
 }
 
 /* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
@@ -265,6 +266,37 @@ static void assemble(ost* s) {
           pu[a] = s->copy[6 * node + k] - m->node_xyz[3 * node + k] + s->disp[6 * node + k];
         }
         oracle_shell_pressure(s->sc + e, pu, table_at(&L->table, time, 0), L->area_update, Ks, fs);
+      }
+    }
+    if (s->dynamic) {
+      /* MountMass + MountDamping + MountDyn (reference
+       * src/Shell_1.cpp:2406-2544): C from the stiffness that includes the
+       * follower-pressure tangent, then K += M (+ a4 C), f += f_inertial
+       * (+ C v) */
+      const int* nd = m->shells + 9 * e;
+      double v[36], ac[36];
+      for (int j = 0; j < 6; ++j) {
+        memcpy(v + 6 * j, s->copy_vel + 6 * nd[j], 6 * sizeof(double));
+        memcpy(ac + 6 * j, s->copy_accel + 6 * nd[j], 6 * sizeof(double));
+      }
+      double* rd = s->ray ? s->rds + (size_t)729 * e : NULL;
+      if (rd && (s->ray_update || !s->ray_init)) {
+        double Mm[729], rot[9];
+        for (int j = 0; j < 3; ++j) memcpy(rot + 3 * j, s->copy + 6 * nd[3 + j] + 3, 3 * sizeof(double));
+        oracle_shell_modal_mass(s->sc + e, rot, Mm);
+        for (int x = 0; x < 729; ++x) rd[x] = s->ray_alpha * Mm[x] + s->ray_beta * Ks[x];
+      }
+      oracle_shell_inertia(s->sc + e, s->sh + e, ds, v, ac, s->a, Ks, fs, NULL);
+      if (rd) {
+        double vi[27];
+        for (int a = 0; a < 18; ++a) vi[a] = s->vel[6 * nd[a / 3] + a % 3];
+        for (int a = 0; a < 9; ++a) vi[18 + a] = s->vel[6 * nd[3 + a / 3] + 3 + a % 3];
+        for (int x = 0; x < 729; ++x) Ks[x] += s->a[3] * rd[x];
+        for (int q = 0; q < 27; ++q) {
+          double acc = 0.0;
+          for (int k = 0; k < 27; ++k) acc += rd[q + 27 * k] * vi[k];
+          fs[q] += acc;
+        }
       }
     }
     int g[27];
@@ -617,7 +649,7 @@ static void update_dyn(ost* s) {
 }
 
 /* reference src/Dynamic.cpp:255-468 (no contact, no special constraints,
- * Rayleigh alpha = beta = 0, zero initial conditions) */
+ * zero initial conditions) */
 static int dynamic_solve(ost* s, oracle_record* rec, int* stats) {
   const gf_solution* so = &s->m->solution;
   int aborted = 0, convergence_counter = 0, converged_number = 0, total_it = 0, bisections = 0;
@@ -704,7 +736,6 @@ static void final_state(ost* s, double* out) {
 }
 
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
-  if (m->n_shells && m->solution.type == GF_DYNAMIC) return -1;
   ost s;
   ost_init(&s, m);
   s.dynamic = m->solution.type == GF_DYNAMIC;
@@ -714,6 +745,7 @@ int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes
     s.ray_beta = m->solution.rayleigh_beta;
     s.ray_update = m->solution.update_rayleigh;
     s.rd = calloc((size_t)324 * (s.nb ? s.nb : 1), sizeof(double));
+    s.rds = calloc((size_t)729 * (s.ns ? s.ns : 1), sizeof(double));
   }
   int r = s.dynamic ? dynamic_solve(&s, rec, stats) : static_solve(&s, rec, stats);
   final_state(&s, final_nodes);
@@ -785,5 +817,21 @@ int oracle_beam_inertia_element(const double* xyz9, const double* mat3, const do
   memset(M, 0, sizeof(double) * 324);
   memset(F, 0, sizeof(double) * 18);
   oracle_beam_inertia(&c, &h, disp18, vel18, acc18, a, M, F, ke);
+  return 0;
+}
+
+int oracle_shell_inertia_element(const double* xyz18, const double* mat3, double thickness, int n_hist,
+                                 const double* hist_disp, const double* disp27, const double* vel36,
+                                 const double* acc36, double dt, double beta, double gamma, double* M, double* F,
+                                 double* ke) {
+  os_const c;
+  os_hist h;
+  oracle_shell_precalc(xyz18, mat3, thickness, &c, &h);
+  for (int q = 0; q < n_hist; ++q) oracle_shell_commit(&c, &h, hist_disp + 27 * q);
+  double a[6];
+  newmark_coeff(dt, beta, gamma, a);
+  memset(M, 0, sizeof(double) * 729);
+  memset(F, 0, sizeof(double) * 27);
+  oracle_shell_inertia(&c, &h, disp27, vel36, acc36, a, M, F, ke);
   return 0;
 }

@@ -358,3 +358,25 @@ extern "C" int giraffe_ref_shell_pressure(int e, int l, double t, double* K, dou
   memcpy(P, s->P_loading->getMatrix(), sizeof(double) * 27);
   return 27;
 }
+
+// Shell_1 inertial contributions of the first solution step, which must be
+// Dynamic: Newmark coefficients for time step dt, then Zeros, Mount
+// (Gauss-point increments) and MountMass (reference
+// src/Shell_1.cpp:2406-2498).  M: 27x27 column-major mass/gyroscopic
+// tangent, F: inertial_loading, *ke: kinetic energy.
+extern "C" int giraffe_ref_shell_inertia(int e, double dt, double* M, double* F, double* ke) {
+  if (typeid(*db.solution[0]) != typeid(Dynamic)) return 0;
+  Dynamic* d = static_cast<Dynamic*>(db.solution[0]);
+  d->CalculateNewmarkCoeff(dt);
+  db.current_solution_number = 1;
+  Element* el = db.elements[e - 1];
+  if (typeid(*el) != typeid(Shell_1)) return 0;
+  Shell_1* s = static_cast<Shell_1*>(el);
+  s->Zeros();
+  s->Mount();
+  s->MountMass();
+  memcpy(M, s->mass->getMatrix(), sizeof(double) * 27 * 27);
+  memcpy(F, s->inertial_loading->getMatrix(), sizeof(double) * 27);
+  *ke = s->kinetic_energy;
+  return 27;
+}

@@ -44,6 +44,15 @@ stores what the reference computes:
 * ref_plate.npz          a clamped 4x4x2 Shell_1 plate under follower
                          pressure (AreaUpdate 1), 20 steps, every step.
 * ref_plate_fixed_area.npz  a clamped 3x3x2 plate, AreaUpdate 0, 10 steps.
+* ref_shell_inertia.npz  Shell_1 inertial force and mass/gyroscopic tangent of
+                         single elements (Shell_1::MountMass) with random
+                         history, increments, nodal velocities/accelerations.
+* ref_plate_dynamic.npz  the clamped 3x3x2 plate in a Dynamic step: follower
+                         pressure raised over 2 ms, Newmark, 20 steps of 1 ms.
+* ref_plate_dynamic_rayleigh.npz, ref_plate_dynamic_rayleigh_update.npz
+                         the same with Rayleigh damping (alpha 8 1/s, beta
+                         2e-5 s), AreaUpdate 0 with C formed once, and
+                         AreaUpdate 1 with C formed at every iteration.
 
 Node records hold copy_coordinates (position and accumulated Rodrigues
 vector) then the nodal Q (row-major); Gauss-point records hold Q_i
@@ -301,6 +310,63 @@ def run_shell_elements(L, rng, n, tmp):
     return res
 
 
+def run_shell_inertia(L, rng, n, tmp):
+    dp = C.POINTER(C.c_double)
+    L.giraffe_ref_set_vel_accel.argtypes = [C.c_int, dp, dp]
+    L.giraffe_ref_shell_inertia.argtypes = [C.c_int, C.c_double, dp, dp, dp]
+    out = {k: [] for k in ("xyz", "mat", "thick", "hist", "disp", "vel", "acc", "dt", "beta", "gamma", "M", "F", "ke")}
+    nh_list = []
+    for i in range(n):
+        c = rng.normal(size=(3, 3))
+        if i % 4 == 0:
+            c[:, 2] = 0.0  # in the x-y plane
+        xyz = np.vstack([c, 0.5 * (c[0] + c[1]), 0.5 * (c[1] + c[2]), 0.5 * (c[2] + c[0])])
+        s = Structure(nodes=xyz)
+        matv = (rng.uniform(5e10, 2.1e11), rng.uniform(0.2, 0.4), rng.uniform(2000.0, 8000.0))
+        mat = s.add_material(*matv)
+        t = rng.uniform(0.005, 0.05)
+        sec = s.add_shell_section(t)
+        cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+        s.shells.append((0, 1, 2, 3, 4, 5, mat, sec, cs))
+        beta, gamma, dt = rng.uniform(0.25, 0.35), rng.uniform(0.5, 0.6), rng.uniform(1e-3, 2e-2)
+        s.solution = Solution(1, 0.0, 1.0, dt, dt, dt / 100, 20, 3, 4, 1.0, beta=beta, gamma=gamma)
+        deck = os.path.join(tmp, f"si{i}.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        L.giraffe_ref_prepare()
+        nh = int(rng.integers(0, 4))
+        scale = np.array([0.01] * 3 + [0.1] * 3)
+        hist = np.zeros((3, 27))
+        vel = rng.normal(size=(6, 6))
+        acc = rng.normal(size=(6, 6)) * 5
+        vel[:3, 3:] = 0.0  # corner nodes carry no rotation
+        acc[:3, 3:] = 0.0
+        for q in range(nh + 1):
+            dn = rng.normal(size=(6, 6)) * scale
+            dn[:3, 3:] = 0.0
+            for nd in range(6):
+                L.giraffe_ref_set_increment(nd + 1, _dp(np.ascontiguousarray(dn[nd])))
+            d27 = np.concatenate([dn[:, :3].ravel(), dn[3:, 3:].ravel()])
+            if q < nh:
+                L.giraffe_ref_commit()
+                hist[q] = d27
+        for nd in range(6):
+            L.giraffe_ref_set_vel_accel(nd + 1, _dp(np.ascontiguousarray(vel[nd])), _dp(np.ascontiguousarray(acc[nd])))
+        M = np.zeros(729)
+        F = np.zeros(27)
+        ke = np.zeros(1)
+        assert L.giraffe_ref_shell_inertia(1, dt, _dp(M), _dp(F), _dp(ke)) == 27
+        for k, v in (("xyz", xyz.ravel()), ("mat", np.array(matv)), ("thick", t), ("hist", hist), ("disp", d27),
+                     ("vel", vel.ravel()), ("acc", acc.ravel()), ("dt", dt), ("beta", beta), ("gamma", gamma),
+                     ("M", M.reshape(27, 27).T), ("F", F), ("ke", ke[0])):
+            out[k].append(v)
+        nh_list.append(nh)
+    res = {k: np.array(v) for k, v in out.items()}
+    res["n_hist"] = np.array(nh_list)
+    return res
+
+
 def small_chain():
     return configs.pipe_chain(30, 0.4, 0.03, [1.5e5, -1.0e5, 0.8e5], element_length=10.0 / 30)
 
@@ -317,6 +383,11 @@ DECKS = {
     "ref_rotating_base_vector.npz": lambda: configs.rotating_base("EulerVector"),
     "ref_tutorial10_rayleigh.npz": lambda: configs.tutorial10(0.2, 0.002, 0),
     "ref_tutorial10_rayleigh_update.npz": lambda: configs.tutorial10(0.2, 0.002, 1),
+    "ref_plate_dynamic.npz": lambda: configs.plate_dynamics(3, steps=20),
+    "ref_plate_dynamic_rayleigh.npz": lambda: configs.plate_dynamics(3, steps=20, area_update=0, rayleigh_alpha=8.0,
+                                                                     rayleigh_beta=2e-5),
+    "ref_plate_dynamic_rayleigh_update.npz": lambda: configs.plate_dynamics(3, steps=20, rayleigh_alpha=8.0,
+                                                                            rayleigh_beta=2e-5, update_rayleigh=1),
     "ref_riser_rayleigh.npz": lambda: configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0,
                                                           rayleigh_alpha=0.3, rayleigh_beta=0.004,
                                                           update_rayleigh=1),
@@ -331,6 +402,7 @@ def make_elements():
         np.savez_compressed(os.path.join(HERE, "ref_beam_inertia.npz"),
                             **run_inertia(L, element_cases(rng, 16), tmp, rng))
         np.savez_compressed(os.path.join(HERE, "ref_shell_elements.npz"), **run_shell_elements(L, rng, 24, tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_shell_inertia.npz"), **run_shell_inertia(L, rng, 16, tmp))
 
 
 def make_deck(name):

@@ -151,3 +151,37 @@ def test_pretensioned_chain_matches_reference(golden):
     """Beam_1 PreTension: reference length shortened by 1 + T0 / EA and the
     Gauss points starting stretched (Beam_1::PreCalc)."""
     _check_run(golden("ref_pretension.npz"), configs.pretensioned_chain(), tol=1e-10)
+
+
+def test_shell_inertia_matches_reference(golden):
+    """Shell_1 MountMass: the director-fibre inertia.  The rotational blocks
+    are four to six orders below the translational ones, so they are checked
+    on their own scale."""
+    g = golden("ref_shell_inertia.npz")
+    for i in range(len(g["M"])):
+        nh = int(g["n_hist"][i])
+        M, F, ke = oracle.shell_inertia(g["xyz"][i], g["mat"][i], float(g["thick"][i]), g["hist"][i][:nh],
+                                        g["disp"][i], g["vel"][i], g["acc"][i], float(g["dt"][i]),
+                                        float(g["beta"][i]), float(g["gamma"][i]))
+        R = g["M"][i]
+        assert rel(M, R) < 1e-12, i
+        assert rel(M[18:, 18:], R[18:, 18:]) < 1e-12, i
+        assert np.abs(R[:18, 18:]).max() == 0.0 and np.abs(M[:18, 18:]).max() == 0.0
+        assert rel(F, g["F"][i]) < 1e-12, i
+        assert rel(F[18:], g["F"][i][18:]) < 1e-12, i
+        assert abs(ke - g["ke"][i]) <= 1e-12 * abs(g["ke"][i]), i
+
+
+@pytest.mark.parametrize("name,kw", [
+    ("ref_plate_dynamic.npz", {}),
+    ("ref_plate_dynamic_rayleigh.npz", dict(area_update=0, rayleigh_alpha=8.0, rayleigh_beta=2e-5)),
+    ("ref_plate_dynamic_rayleigh_update.npz", dict(rayleigh_alpha=8.0, rayleigh_beta=2e-5, update_rayleigh=1)),
+])
+def test_plate_dynamics_matches_reference(golden, name, kw):
+    """Shell_1 in a Dynamic step (MountMass, MountDamping with the modal mass
+    of EvaluateMassModal, MountDyn): a clamped plate set vibrating by a
+    quickly applied follower pressure, with and without Rayleigh damping."""
+    final, _, _ = _check_run(golden(name), configs.plate_dynamics(3, steps=20, **kw), tol=1e-10)
+    if kw:
+        undamped = golden("ref_plate_dynamic.npz")["nodes"][-1]
+        assert np.abs(final[:, 2] - undamped[:, 2]).max() > 1e-2 * np.abs(undamped[:, 2]).max()
