@@ -201,6 +201,16 @@ void shell_precalc(const double* xyz, const double* mat, double thick, ShellCons
     shell_shapes(Lc[k], Lx1, Lx2, c.N4[k], c.N41[k], c.N42[k]);
   }
   c.alpha1 = A / 3.0;
+  // inertia of the director fibre and drilling inertia of the modal mass
+  // (reference src/Shell_1.cpp:2022-2024); PI as reference src/Geometry.h:4
+  c.coef1 = thick * mat[2];
+  c.coef2 = (1.0 / 12.0) * thick * thick * thick * mat[2];
+  c.coef3 = mat[2] * thick * A / (3 * 3.1415926535897932384626433832795);
+  for (int k = 0; k < 6; ++k) {
+    c.Na4[k][0] = 1 - 2 * Lc[k][2];
+    c.Na4[k][1] = 1 - 2 * Lc[k][0];
+    c.Na4[k][2] = 1 - 2 * Lc[k][1];
+  }
   for (int g = 0; g < 3; ++g) {
     h.Q[g][0] = h.Q[g][4] = h.Q[g][8] = 1.0;
     h.z1[g][0] = 1.0;
@@ -374,10 +384,6 @@ void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
   }
   if (m.n_shells && m.n_beams) {
     P.err = strf("structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
-    return;
-  }
-  if (m.n_shells && m.solution.type == GF_DYNAMIC) {
-    P.err = strf("structure %d: Shell_1 structures are supported in Static steps only", s);
     return;
   }
   const int nn = m.n_nodes;
@@ -815,7 +821,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       p.ray_alpha = so.rayleigh_alpha;
       p.ray_beta = so.rayleigh_beta;
       p.ray_update = so.update_rayleigh ? 1 : 0;
-      b.any_rayleigh = 1;
+      if (m.n_beams) b.any_rayleigh = 1;
+      if (m.n_shells) b.sh.any_rayleigh = 1;
     }
   }
   b.n_struct = n;
@@ -947,7 +954,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
         !upload(B, &sd.saux, saux) || !dup(B, &B->shist0, sd.shist, shist.size()) ||
         !dup(B, &B->saux0, sd.saux, saux.size()) ||
         !upload(B, &sd.color_elems, scolor_elems) || !balloc(B, &sd.Ke, (size_t)shell_off * 729) ||
-        !balloc(B, &sd.Fe, (size_t)shell_off * 27))
+        !balloc(B, &sd.Fe, (size_t)shell_off * 27) ||
+        (sd.any_rayleigh && !balloc(B, &sd.RD, (size_t)shell_off * 729)))
       return GF_ERR_CUDA;
   }
   if (!wide_structs.empty()) {
@@ -1250,6 +1258,7 @@ std::vector<std::pair<void*, size_t>> state_parts(const gf_batch* B) {
     v.push_back({b.sh.saux, sizeof(ShellHistAux) * ns});
   }
   if (b.any_rayleigh) v.push_back({b.RD, 8 * 324 * ne});
+  if (b.sh.any_rayleigh) v.push_back({b.sh.RD, 8 * 729 * ns});
   return v;
 }
 }  // namespace
@@ -1698,6 +1707,61 @@ int gf_shell_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, 
     }
   }
   cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dpu); cudaFree(dp); cudaFree(dK); cudaFree(df);
+  return rc;
+}
+
+int gf_shell_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick,
+                              int n_hist, const double* hist_disp, const double* disp, const double* vel,
+                              const double* acc, double dt, double beta, double gamma, double* M, double* F) {
+  if (!ctx || n <= 0 || !xyz || !mat || !thick || !disp || !vel || !acc || !M || !F || n_hist < 0 ||
+      (n_hist && !hist_disp) || !(dt > 0.0) || !(beta > 0.0)) {
+    set_err(ctx, "gf_shell_inertia_elements: invalid arguments");
+    return GF_ERR_ARG;
+  }
+  std::vector<ShellConst> c(n);
+  std::vector<ShellHist> h(n);
+  std::vector<ShellHistAux> x(n);
+  for (int e = 0; e < n; ++e) shell_precalc(xyz + 18 * (size_t)e, mat + 3 * (size_t)e, thick[e], c[e], h[e], x[e]);
+  double a[6] = {1.0 / (dt * dt * beta), 1.0 / (dt * beta), 1.0 / (2.0 * beta) - 1.0, gamma / (dt * beta),
+                 1.0 - gamma / beta, dt * (1.0 - gamma / (2.0 * beta))};
+  ShellConst* dc = nullptr;
+  ShellHist* dh = nullptr;
+  ShellHistAux* dx = nullptr;
+  double *dd = nullptr, *dv = nullptr, *da = nullptr, *dA = nullptr, *dM = nullptr, *dF = nullptr;
+  int rc = GF_OK;
+  if (!dmalloc(ctx, &dc, n) || !dmalloc(ctx, &dh, n) || !dmalloc(ctx, &dx, n) || !dmalloc(ctx, &dd, (size_t)n * 27) ||
+      !dmalloc(ctx, &dv, (size_t)n * 36) || !dmalloc(ctx, &da, (size_t)n * 36) || !dmalloc(ctx, &dA, 6) ||
+      !dmalloc(ctx, &dM, (size_t)n * 729) || !dmalloc(ctx, &dF, (size_t)n * 27)) {
+    rc = GF_ERR_CUDA;
+  } else {
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(dc, c.data(), sizeof(ShellConst) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dh, h.data(), sizeof(ShellHist) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dx, x.data(), sizeof(ShellHistAux) * n, cudaMemcpyHostToDevice, st);
+    std::vector<double> step((size_t)n * 27);
+    for (int q = 0; q < n_hist; ++q) {
+      for (int e = 0; e < n; ++e)
+        std::memcpy(&step[(size_t)e * 27], hist_disp + ((size_t)e * n_hist + q) * 27, 27 * sizeof(double));
+      cudaMemcpyAsync(dd, step.data(), sizeof(double) * step.size(), cudaMemcpyHostToDevice, st);
+      launch_shell_commit_elements(n, dc, dh, dx, dd, st);
+      cudaStreamSynchronize(st);
+    }
+    cudaMemcpyAsync(dd, disp, sizeof(double) * (size_t)n * 27, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dv, vel, sizeof(double) * (size_t)n * 36, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(da, acc, sizeof(double) * (size_t)n * 36, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dA, a, sizeof(a), cudaMemcpyHostToDevice, st);
+    launch_shell_inertia_elements(n, dc, dx, dd, dv, da, dA, dM, dF, st);
+    cudaMemcpyAsync(M, dM, sizeof(double) * (size_t)n * 729, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(F, dF, sizeof(double) * (size_t)n * 27, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_err(ctx, "gf_shell_inertia_elements: %s", cudaGetErrorString(e));
+      rc = GF_ERR_CUDA;
+    }
+  }
+  cudaFree(dc); cudaFree(dh); cudaFree(dx); cudaFree(dd); cudaFree(dv); cudaFree(da); cudaFree(dA);
+  cudaFree(dM); cudaFree(dF);
   return rc;
 }
 

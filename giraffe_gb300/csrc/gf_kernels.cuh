@@ -104,6 +104,9 @@ void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const
                            const double* p, int area_update, double* K, double* f, cudaStream_t st);
 void launch_shell_commit_elements(int n, const ShellConst* c, ShellHist* h, ShellHistAux* x, const double* d,
                                   cudaStream_t st);
+void launch_shell_inertia_elements(int n, const ShellConst* c, const ShellHistAux* x, const double* d,
+                                   const double* v, const double* a_acc, const double* a, double* M, double* F,
+                                   cudaStream_t st);
 // Kernel launches of one pass of the shell and wide-band kernels.
 int shell_launches_per_pass(const Batch& b);
 

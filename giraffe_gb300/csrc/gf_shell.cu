@@ -1,7 +1,9 @@
 // Shell_1 structures on the device: element tangent and internal force with
-// the follower pressure (k_shell_tangent), colour scatter into the wide band
-// (k_shell_scatter), SaveLagrange (k_shell_commit), and the wide-band LU with
-// its triangular solves for the K_AA of those structures.
+// the follower pressure and, in Dynamic steps, the inertial terms
+// (k_shell_tangent), Rayleigh damping (k_shell_rayleigh), colour scatter
+// into the wide band (k_shell_scatter), SaveLagrange (k_shell_commit), and
+// the wide-band LU with its triangular solves for the K_AA of those
+// structures.
 //
 // Element math restates reference src/Shell_1.cpp:
 //   899-1332   Mount: incremental Rodrigues kinematics at the three midside
@@ -11,6 +13,7 @@
 //              K = T^T sum_g w (dN^T (Psi^T D Psi + G) dN) T
 //   1392-1467  MountShellSpecialLoads: follower pressure and its tangent
 //   1650-1664  SaveLagrange
+//   2368-2544  MountMassModal, MountMass, MountDamping, MountDyn
 // dN is block-sparse (each 3x3 block a scalar times I), so the products run
 // over the 3x3 blocks that are not zero.
 //
@@ -477,6 +480,131 @@ __device__ void shell_pressure(const ShellConst& c, const double* pu, double p, 
   }
 }
 
+// MountMass and the mass part of MountDyn (reference
+// src/Shell_1.cpp:2406-2498, 2536-2541).  At each of the three midside
+// Gauss points (weight alpha1) the director fibre has mass coef1 per unit
+// area and, about the midsurface, rotary inertia J_i = coef2 (I - d d^T)
+// with d = Q(alpha_i) e3r; its inertial moment coef2 d x d'' equals
+// J w' + w x J w.  In the element frame, with a[0..5] = a1..a6:
+//   dT_u = coef1 (a1 du - a2 v_i - a3 acc_i)
+//   dT_a = Xi(da) h,  h = J_i w2 + w1 x J_i w1,
+//   w1 = a4 da + a5 w_i + a6 dw_i,  w2 = a1 da - a2 w_i - a3 dw_i
+// (Newmark in the tangent space transported by Q_delta, as for Beam_1), and
+// the exact tangent d dT_u/d du = a1 coef1 I,
+//   d dT_a/d da = Xi (a1 J_i + a4 (skew(w1) J_i - skew(J_i w1)))
+//                 - g^2/2 (h + da x h / 2) da^T - g/2 skew(h).
+// The element adds alpha1 N^T dT to f and alpha1 N^T DdT N to K (global
+// frame, column-major), N the 6x27 interpolation of the translations of the
+// six nodes and the rotations of the midside nodes.  vel / acc: [6][6]
+// converged nodal velocities and accelerations (global).
+__device__ __noinline__ void shell_inertia(const ShellConst& c, const ShellHistAux& x, const double* d,
+                                           const double* vel, const double* acc, const double* a, double* K,
+                                           double* f) {
+  const m3 T = ld3(c.T3);
+  const double a1 = a[0], a2 = a[1], a3 = a[2], a4 = a[3], a5 = a[4], a6 = a[5];
+  double wt[6][6];  // alpha1 sum_g Nu_n Nu_p
+#pragma unroll
+  for (int n = 0; n < 6; ++n)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) wt[n][q] = 0.0;
+#pragma unroll 1
+  for (int g = 0; g < 3; ++g) {
+    const double* Nu = c.Nu[g];
+    const double* Na = c.Na[g];
+    v3 du = {{0, 0, 0}}, vi = {{0, 0, 0}}, ai = {{0, 0, 0}}, da = {{0, 0, 0}}, wi = {{0, 0, 0}}, dwi = {{0, 0, 0}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int n = 0; n < 6; ++n) {
+        du[i] += d[3 * n + i] * Nu[n];
+        vi[i] += vel[6 * n + i] * Nu[n];
+        ai[i] += acc[6 * n + i] * Nu[n];
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        da[i] += d[18 + 3 * m + i] * Na[m];
+        wi[i] += vel[6 * (3 + m) + 3 + i] * Na[m];
+        dwi[i] += acc[6 * (3 + m) + 3 + i] * Na[m];
+      }
+    }
+    du = mv(T, du);
+    vi = mv(T, vi);
+    ai = mv(T, ai);
+    da = mv(T, da);
+    wi = mv(T, wi);
+    dwi = mv(T, dwi);
+    v3 fu;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) fu[i] = c.coef1 * (a1 * du[i] - a2 * vi[i] - a3 * ai[i]);
+    const m3 Qi = rodrigues(v3{{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}});
+    m3 Ji;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Ji[i * 3 + j] = c.coef2 * ((i == j ? 1.0 : 0.0) - Qi[i * 3 + 2] * Qi[j * 3 + 2]);
+    v3 w1, w2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      w1[i] = a4 * da[i] + a5 * wi[i] + a6 * dwi[i];
+      w2[i] = a1 * da[i] - a2 * wi[i] - a3 * dwi[i];
+    }
+    const v3 Jw1 = mv(Ji, w1), Jw2 = mv(Ji, w2), cr = cross(w1, Jw1);
+    v3 h;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) h[i] = Jw2[i] + cr[i];
+    const double gg = 4.0 / (4.0 + dot(da, da));
+    m3 Xi = skew(da);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) Xi[q] *= 0.5 * gg;
+    Xi[0] += gg;
+    Xi[4] += gg;
+    Xi[8] += gg;
+    const v3 mom = mv(Xi, h);
+    const m3 t = mul(skew(w1), Ji), SJw1 = skew(Jw1);
+    m3 Dh;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) Dh[q] = a1 * Ji[q] + a4 * (t[q] - SJw1[q]);
+    m3 D = mul(Xi, Dh);
+    const v3 axh = cross(da, h);
+    const m3 Sh = skew(h);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        D[i * 3 + j] += -0.5 * gg * gg * (h[i] + 0.5 * axh[i]) * da[j] - 0.5 * gg * Sh[i * 3 + j];
+    const m3 Dg = tmul(T, mul(D, T));
+    const v3 gu = tmv(T, fu), ga = tmv(T, mom);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int n = 0; n < 6; ++n) f[3 * n + i] += c.alpha1 * Nu[n] * gu[i];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) f[18 + 3 * m + i] += c.alpha1 * Na[m] * ga[i];
+    }
+#pragma unroll 1
+    for (int m = 0; m < 3; ++m)
+#pragma unroll 1
+      for (int q = 0; q < 3; ++q) {
+        const double w = c.alpha1 * Na[m] * Na[q];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) K[(18 + 3 * m + i) + 27 * (18 + 3 * q + j)] += w * Dg[i * 3 + j];
+      }
+#pragma unroll
+    for (int n = 0; n < 6; ++n)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) wt[n][q] += c.alpha1 * Nu[n] * Nu[q];
+  }
+  const double a1m = a1 * c.coef1;
+#pragma unroll 1
+  for (int n = 0; n < 6; ++n)
+#pragma unroll 1
+    for (int q = 0; q < 6; ++q)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) K[(3 * n + i) + 27 * (3 * q + i)] += wt[n][q] * a1m;
+}
+
 // One thread per Shell_1 element of an iterating structure: Mount +
 // MountElementLoads + the element's ShellLoad at the step's time; K (27x27,
 // column-major, global frame) and f (P_loading) go to the element scratch.
@@ -500,9 +628,145 @@ __global__ void __launch_bounds__(64) k_shell_tangent(Batch b) {
     }
     shell_pressure(b.sh.sconst[e], pu, table_value(b, pt, st.time), b.sh.sarea[e] != 0, K, f);
   }
+  const StructParams& pr = b.params[s];
+  if (pr.dynamic) {
+    // Rayleigh damping: on the iterations that form C_e, the stiffness
+    // (with the pressure tangent, as MountLoads precedes MountDamping) goes
+    // to the damping scratch, where k_shell_rayleigh turns it into
+    // C_e = alpha M_modal + beta K_e
+    if (pr.ray_on && (pr.ray_update || !st.ray_init)) {
+      double* C = b.sh.RD + e;
+      const int64_t ns = b.sh.n_shells;
+#pragma unroll 1
+      for (int q = 0; q < 729; ++q) C[q * ns] = K[q];
+    }
+    const int* nd = b.sh.snodes + 6 * e;
+    double vel[36], acc[36];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        vel[6 * j + q] = b.copy_vel[(int64_t)nd[j] * 6 + q];
+        acc[6 * j + q] = b.copy_accel[(int64_t)nd[j] * 6 + q];
+      }
+    shell_inertia(b.sh.sconst[e], b.sh.saux[e], d, vel, acc, st.a, K, f);
+  }
   double* F = b.sh.Fe + (int64_t)e * 27;
 #pragma unroll
   for (int a = 0; a < 27; ++a) F[a] = f[a];
+}
+
+// MountDamping and the damping part of MountDyn (reference
+// src/Shell_1.cpp:2501-2541).  On the iterations that form it (the step's
+// first, or every one with Update 1), C_e = alpha M_modal + beta K_e.  The
+// modal mass is MountMassModal (src/Shell_1.cpp:2368-2396) over the
+// six-point rule: at each point the rotation vector interpolated from the
+// midside nodes' accumulated rotations (copy_coordinates 3..5) gives the
+// director d = Q e3r, and EvaluateMassModal (src/Shell_1.cpp:3171-) the
+// 6x6 operator blockdiag(coef1 I, coef2 (|d|^2 I - d d^T) + coef3 d d^T);
+// the element sums w N^T D N and turns it to the global frame.  Every
+// iteration then adds a4 C_e to K_e and C_e v to f_e, v the nodes' current
+// velocities.  One thread per element; C_e is structure-of-arrays.
+__global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= b.sh.n_shells) return;
+  const int s = b.sh.sstruct[e];
+  const StructState& st = b.state[s];
+  if (!iterating_s(st)) return;
+  const StructParams& p = b.params[s];
+  if (!p.dynamic || !p.ray_on) return;
+  const int64_t ns = b.sh.n_shells;
+  double* C = b.sh.RD + e;
+  const int* nd = b.sh.snodes + 6 * e;
+  if (p.ray_update || !st.ray_init) {
+    const ShellConst& c = b.sh.sconst[e];
+    const m3 T = ld3(c.T3);
+    double wt[6][6], R[3][3][9];  // translation weights; local rotation blocks
+#pragma unroll
+    for (int n = 0; n < 6; ++n)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) wt[n][q] = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[m][q][k] = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) {
+      v3 al = {{0, 0, 0}};
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) al[i] += b.copy[(int64_t)nd[3 + m] * 6 + 3 + i] * c.Na4[k][m];
+      al = mv(T, al);
+      const m3 Q = rodrigues(al);
+      const v3 dv = {{Q[2], Q[5], Q[8]}};
+      const double d2 = dot(dv, dv);
+      m3 D;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          D[i * 3 + j] = (i == j ? c.coef2 * d2 : 0.0) + (c.coef3 - c.coef2) * dv[i] * dv[j];
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const double w = c.w4[k] * c.Na4[k][m] * c.Na4[k][q];
+#pragma unroll
+          for (int x = 0; x < 9; ++x) R[m][q][x] += w * D[x];
+        }
+#pragma unroll
+      for (int n = 0; n < 6; ++n)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) wt[n][q] += c.w4[k] * c.N4[k][n] * c.N4[k][q];
+    }
+    // translations: coef1 times the weights on the diagonal of each 3x3
+    // node block (T^T I T = I); rotations: T^T R T
+#pragma unroll 1
+    for (int q = 0; q < 9; ++q)
+#pragma unroll 1
+      for (int n = 0; n < 9; ++n) {
+        m3 blk;
+        if (n < 6 && q < 6) {
+#pragma unroll
+          for (int x = 0; x < 9; ++x) blk[x] = (x % 4 == 0) ? c.coef1 * wt[n][q] : 0.0;
+        } else if (n >= 6 && q >= 6) {
+          m3 r;
+#pragma unroll
+          for (int x = 0; x < 9; ++x) r[x] = R[n - 6][q - 6][x];
+          blk = tmul(T, mul(r, T));
+        } else {
+#pragma unroll
+          for (int x = 0; x < 9; ++x) blk[x] = 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const int64_t xi = (3 * n + i) + 27 * (3 * q + j);
+            C[xi * ns] = p.ray_alpha * blk[i * 3 + j] + p.ray_beta * C[xi * ns];
+          }
+      }
+  }
+  const double a4 = st.a[3];
+  double v[27];
+#pragma unroll
+  for (int a = 0; a < 18; ++a) v[a] = b.vel[(int64_t)nd[a / 3] * 6 + a % 3];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) v[18 + a] = b.vel[(int64_t)nd[3 + a / 3] * 6 + 3 + a % 3];
+  double* K = b.sh.Ke + (int64_t)e * 729;
+  double* F = b.sh.Fe + (int64_t)e * 27;
+#pragma unroll 1
+  for (int q = 0; q < 27; ++q) {
+    double acc = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < 27; ++k) acc += C[(q + 27 * k) * ns] * v[k];
+    F[q] += acc;
+  }
+#pragma unroll 1
+  for (int x = 0; x < 729; ++x) K[x] += a4 * C[x * ns];
 }
 
 // Standalone elements (gf_shell_elements): n elements with their own
@@ -1177,6 +1441,7 @@ __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
 void launch_shell_mount(const Batch& b, cudaStream_t st) {
   if (b.sh.n_shells == 0) return;
   k_shell_tangent<<<(b.sh.n_shells + 63) / 64, 64, 0, st>>>(b);
+  if (b.sh.any_rayleigh) k_shell_rayleigh<<<(b.sh.n_shells + 127) / 128, 128, 0, st>>>(b);
   for (int c = 0; c < b.sh.n_colors; ++c) {
     int cnt = b.sh.color_off[c + 1] - b.sh.color_off[c];
     if (cnt <= 0) continue;
@@ -1360,6 +1625,36 @@ void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const
   k_shell_elements<<<(n + 63) / 64, 64, 0, st>>>(n, c, h, d, pu, p, area_update, K, f);
 }
 
+// Standalone inertia (gf_shell_inertia_elements): n elements with their own
+// constants, history, increments d ([n][27]), converged nodal velocities v
+// and accelerations a_acc ([n][36]) and Newmark coefficients a[6].
+__global__ void __launch_bounds__(64) k_shell_inertia_elements(int n, const ShellConst* cs, const ShellHistAux* xs,
+                                                               const double* ds, const double* vs, const double* as,
+                                                               const double* a, double* Ms, double* Fs) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double d[27], vel[36], acc[36], f[27], an[6];
+  for (int q = 0; q < 27; ++q) {
+    d[q] = ds[(int64_t)e * 27 + q];
+    f[q] = 0.0;
+  }
+  for (int q = 0; q < 36; ++q) {
+    vel[q] = vs[(int64_t)e * 36 + q];
+    acc[q] = as[(int64_t)e * 36 + q];
+  }
+  for (int q = 0; q < 6; ++q) an[q] = a[q];
+  double* M = Ms + (int64_t)e * 729;
+  for (int q = 0; q < 729; ++q) M[q] = 0.0;
+  shell_inertia(cs[e], xs[e], d, vel, acc, an, M, f);
+  for (int q = 0; q < 27; ++q) Fs[(int64_t)e * 27 + q] = f[q];
+}
+
+void launch_shell_inertia_elements(int n, const ShellConst* c, const ShellHistAux* x, const double* d,
+                                   const double* v, const double* a_acc, const double* a, double* M, double* F,
+                                   cudaStream_t st) {
+  if (n > 0) k_shell_inertia_elements<<<(n + 63) / 64, 64, 0, st>>>(n, c, x, d, v, a_acc, a, M, F);
+}
+
 void launch_shell_commit_elements(int n, const ShellConst* c, ShellHist* h, ShellHistAux* x, const double* d,
                                   cudaStream_t st) {
   if (n <= 0) return;
@@ -1377,7 +1672,7 @@ namespace gf {
 int shell_launches_per_pass(const Batch& b) {
   int n = 0;
   if (b.sh.n_shells) {
-    n += 2;  // tangent + commit
+    n += 2 + (b.sh.any_rayleigh ? 1 : 0);  // tangent (+ Rayleigh damping) + commit
     for (int c = 0; c < b.sh.n_colors; ++c) n += b.sh.color_off[c + 1] > b.sh.color_off[c];
   }
   // unrolled: the first diagonal LU, then per panel trsm, forward step,

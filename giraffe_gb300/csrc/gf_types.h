@@ -58,10 +58,12 @@ struct BeamHistAux {
 struct ShellConst {
   double T3[9];
   double mu, lambda, stiff_drill, thick, alpha1;
+  double coef1, coef2, coef3;  // fibre mass per area, its rotary inertia, drilling inertia (modal mass)
   double Nu[3][6], Nu1[3][6], Nu2[3][6];
   double Na[3][3], Na1[3][3], Na2[3][3];
   double w4[6];
   double N4[6][6], N41[6][6], N42[6][6];
+  double Na4[6][3];  // midside rotation shape functions at the six points
 };
 
 // Shell_1 Gauss-point history read by Mount: Q_i, kappa_r1_i, kappa_r2_i,
@@ -229,6 +231,11 @@ struct ShellData {
   ShellHistAux* saux;
   double* Ke;       // [n_shells][27 x 27] column-major (global frame)
   double* Fe;       // [n_shells][27]
+  // Rayleigh damping matrix per element (27x27 column-major,
+  // structure-of-arrays: entry x of element e at [x * n_shells + e]);
+  // allocated when any_rayleigh
+  double* RD;
+  int any_rayleigh;
   int* color_elems;
   int color_off[17];
   int n_colors;

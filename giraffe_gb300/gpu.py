@@ -25,7 +25,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_batch_snapshot", "gf_batch_restore", "gf_batch_work", "gf_device_fp_peaks",
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_sparse_solve", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
-           "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr"]
+           "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr",
+           "gf_shell_inertia_elements"]
 
 
 class gf_solve_opts(C.Structure):
@@ -97,6 +98,8 @@ def lib():
                                                C.c_double, C.c_double, dp, dp]
         L.gf_batch_assemble_csr.argtypes = [vp, C.c_int, ip, ip, dp, dp, ip]
         L.gf_shell_elements.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int, dp, dp, dp, C.c_int, dp, dp]
+        L.gf_shell_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
+                                                C.c_double, C.c_double, dp, dp]
         L.gf_batch_device_bytes.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(C.c_size_t)]
         L.gf_server_default_opts.argtypes = [C.POINTER(gf_server_opts)]
         L.gf_server_create.restype = vp
@@ -195,6 +198,19 @@ class Context:
                                             _dp(arrs[3]), None if pr is None else _dp(pr), int(area_update), _dp(K),
                                             _dp(f)), "gf_shell_elements")
         return K.reshape(n, 27, 27).transpose(0, 2, 1), f
+
+    def shell_inertia(self, xyz, mat, thick, hist_disp, disp, vel, acc, dt, beta, gamma):
+        """gf_shell_inertia_elements: M [n][27][27] (row-major [r][s]) and F [n][27]."""
+        n = len(disp)
+        nh = 0 if hist_disp is None else hist_disp.shape[1]
+        M = np.zeros((n, 729))
+        F = np.zeros((n, 27))
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz, mat, thick, disp, vel, acc)]
+        hd = np.ascontiguousarray(hist_disp if nh else np.zeros((n, 1, 27)), dtype=np.float64)
+        self.check(self.L.gf_shell_inertia_elements(self.h, n, _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]), nh, _dp(hd),
+                                                    _dp(arrs[3]), _dp(arrs[4]), _dp(arrs[5]), dt, beta, gamma,
+                                                    _dp(M), _dp(F)), "gf_shell_inertia_elements")
+        return M.reshape(n, 27, 27).transpose(0, 2, 1), F
 
     def band_solve(self, ab, kl, ku, b):
         ab = np.ascontiguousarray(ab, dtype=np.float64)  # [n][ldab] (column j contiguous)

@@ -19,6 +19,7 @@
  *                           ConvergenceCriteria checks
  *                           (src/ConvergenceCriteria.cpp:187-618)
  *   gf_beam_inertia_elements Beam_1::MountMass (src/Beam_1.cpp:1564-1638)
+ *   gf_shell_inertia_elements Shell_1::MountMass (src/Shell_1.cpp:2406-2498)
  *   gf_shell_elements       Shell_1::PreCalc + SaveLagrange + Mount +
  *                           MountElementLoads + MountShellSpecialLoads
  *                           (src/Shell_1.cpp:899-1467, 1650-2365)
@@ -200,6 +201,17 @@ int gf_beam_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double
                              const double* cs, int n_hist, const double* hist_disp, const double* disp,
                              const double* vel, const double* acc, double dt, double beta, double gamma,
                              double* M, double* F);
+
+/* Inertial contributions of n independent Shell_1 elements (replaces
+ * Shell_1::MountMass, reference src/Shell_1.cpp:2406-2498): geometry,
+ * material, thickness, history and increments as gf_shell_elements, plus the
+ * converged nodal velocities and accelerations of the six nodes (n x 36
+ * each, six per node, global frame) and the Newmark step (dt, beta, gamma;
+ * reference src/Dynamic.cpp:582-590).  M: n x 729 mass/gyroscopic tangent
+ * (column-major), F: n x 27 inertial force. */
+int gf_shell_inertia_elements(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick,
+                              int n_hist, const double* hist_disp, const double* disp, const double* vel,
+                              const double* acc, double dt, double beta, double gamma, double* M, double* F);
 
 /* Solves A x = b for a banded matrix given in the reference's BandMatrix
  * storage (LAPACK GB: entry (i,j) at ab[(kl+ku+i-j) + j*ldab], ldab >=
