@@ -287,6 +287,41 @@ def plate_dynamics(n: int = 4, pressure: float = 1e5, rise: float = 0.002, dt: f
     return s
 
 
+def plate_release(n: int = 3, pressure: float = 1e5, static_steps: int = 5, dt: float = 0.001,
+                  dynamic_steps: int = 15, area_update: int = 1, tol: float = 1e-8) -> Structure:
+    """Two solution steps, as the reference's Shell_1 tutorial: a Static step
+    loads the clamped plate of square_plate with a follower pressure over
+    [0, 1], the pressure is released at t = 1.0001, and a Dynamic step (beta
+    0.3, gamma 0.5) follows the free vibration from the deformed state for
+    `dynamic_steps` steps of dt."""
+    s = square_plate(n, pressure=pressure, steps=static_steps, area_update=area_update, tol=tol)
+    s.loads[0].table = Table(np.array([0.0, 1.0, 1.0001]), np.array([[0.0], [pressure], [0.0]]))
+    s.next_steps = [Solution(GF_DYNAMIC, 1.0, 1.0 + dynamic_steps * dt, dt, dt, dt / 4096, 30, 3, 4, 1.0,
+                             beta=0.3, gamma=0.5)]
+    return s
+
+
+def chain_sequence(n_el: int = 20, tip_force=(2e5, 0.0, 1e5), tol: float = 1e-8) -> Structure:
+    """Four solution steps on a 10 m clamped pipe chain (first bending period
+    near 0.26 s): Static [0, 1] raises a tip force; at t = 1.0001 it drops to
+    half and a damped Dynamic step [1, 1.5] (Rayleigh alpha 0.5 1/s, beta
+    0.002 s) follows the motion; a Dynamic step [1.5, 2] restarts from rest
+    in the deformed shape (ZeroIC); a Static step [2, 2.5] raises the force
+    back to its full value."""
+    s = pipe_chain(n_el, 0.4, 0.03, list(tip_force), steps=5, element_length=10.0 / n_el, tol=tol)
+    f = np.asarray(tip_force, dtype=np.float64)
+    s.loads[0].table = Table(np.array([0.0, 1.0, 1.0001, 2.0, 2.5]),
+                             np.array([[0.0] * 6, [*f, 0.0, 0.0, 0.0], [*(0.5 * f), 0.0, 0.0, 0.0],
+                                       [*(0.5 * f), 0.0, 0.0, 0.0], [*f, 0.0, 0.0, 0.0]]))
+    s.next_steps = [
+        Solution(GF_DYNAMIC, 1.0, 1.5, 0.02, 0.02, 0.02 / 64, 30, 3, 4, 1.0, beta=0.25, gamma=0.5,
+                 rayleigh_alpha=0.5, rayleigh_beta=0.002),
+        Solution(GF_DYNAMIC, 1.5, 2.0, 0.025, 0.025, 0.025 / 64, 30, 3, 4, 1.0, beta=0.3, gamma=0.55, zero_ic=1),
+        Solution(GF_STATIC, 2.0, 2.5, 0.1, 0.1, 0.1 / 64, 30, 3, 4, 1.0),
+    ]
+    return s
+
+
 def served_mixed(n_requests: int, seed: int = 0, plate_share: float = 0.3, chain_dof=(1000, 50000),
                  plate_dof=(10000, 200000), steps: int = 10, tol: float = 1e-8) -> list:
     """The mixed served stream: each request is a pipe chain (free DOFs

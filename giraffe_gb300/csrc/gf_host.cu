@@ -382,6 +382,18 @@ void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
     P.err = strf("structure %d: unknown solution type", s);
     return;
   }
+  if (m.n_next_steps < 0 || (m.n_next_steps > 0 && !m.next_steps)) {
+    P.err = strf("structure %d: invalid solution step list", s);
+    return;
+  }
+  bool any_dynamic = m.solution.type == GF_DYNAMIC;
+  for (int k = 0; k < m.n_next_steps; ++k) {
+    if (m.next_steps[k].type != GF_STATIC && m.next_steps[k].type != GF_DYNAMIC) {
+      P.err = strf("structure %d: unknown solution type in step %d", s, k + 2);
+      return;
+    }
+    any_dynamic = any_dynamic || m.next_steps[k].type == GF_DYNAMIC;
+  }
   if (m.n_shells && m.n_beams) {
     P.err = strf("structure %d: structures mixing Beam_1 and Shell_1 elements are not supported", s);
     return;
@@ -515,7 +527,7 @@ void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
     return;
   }
   P.kb = wide ? P.kl_nat : kbs;
-  if (m.solution.type == GF_DYNAMIC)
+  if (any_dynamic)
     for (int i = 0; i < nn; ++i) {
       int fr = (g6[6 * i + 3] >= 0) + (g6[6 * i + 4] >= 0) + (g6[6 * i + 5] >= 0);
       if (fr != 0 && fr != 3) {
@@ -709,7 +721,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     max_scolor = std::max(max_scolor, plan[s].n_scolors);
   }
   // ---- tables, loads, prescribed displacements, step parameters (serial) ----
-  std::vector<StructParams> params(n);
+  std::vector<StructParams> params(n), step_params;
   std::vector<LoadEntry> loads;
   std::vector<DispEntry> disps;
   std::vector<TableDev> tables;
@@ -792,38 +804,49 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
         disps.push_back(de);
       }
     }
-    StructParams& p = params[s];
-    const gf_solution& so = m.solution;
-    p.start_time = so.start_time;
-    p.end_time = so.end_time;
-    p.time_step0 = so.time_step;
-    p.max_time_step = so.max_time_step;
-    p.min_time_step = so.min_time_step;
-    p.inc_factor = so.inc_factor;
-    p.max_it = so.max_it;
-    p.min_it = so.min_it;
-    p.conv_increase = so.conv_increase;
-    p.dynamic = so.type == GF_DYNAMIC;
-    p.beta = so.beta;
-    p.gamma = so.gamma;
-    const gf_criteria& cr = m.criteria;
-    p.force_tol = cr.force_tol;
-    p.moment_tol = cr.moment_tol;
-    p.force_min = cr.force_min;
-    p.moment_min = cr.moment_min;
-    p.disp_tol = cr.disp_tol;
-    p.rot_tol = cr.rot_tol;
-    p.disp_min = cr.disp_min;
-    p.rot_min = cr.rot_min;
-    p.divergence_ref = cr.divergence_ref;
-    if (so.type == GF_DYNAMIC && (so.rayleigh_alpha != 0.0 || so.rayleigh_beta != 0.0)) {
-      p.ray_on = 1;
-      p.ray_alpha = so.rayleigh_alpha;
-      p.ray_beta = so.rayleigh_beta;
-      p.ray_update = so.update_rayleigh ? 1 : 0;
-      if (m.n_beams) b.any_rayleigh = 1;
-      if (m.n_shells) b.sh.any_rayleigh = 1;
+    // the structure's solution steps: each starts where the previous one
+    // ends (reference src/Database.cpp:759-768)
+    inf.step_off = (int)step_params.size();
+    inf.n_steps = 1 + m.n_next_steps;
+    double start = m.solution.start_time;
+    for (int k = 0; k < inf.n_steps; ++k) {
+      const gf_solution& so = k == 0 ? m.solution : m.next_steps[k - 1];
+      StructParams p{};
+      p.start_time = start;
+      p.end_time = so.end_time;
+      p.time_step0 = so.time_step;
+      p.max_time_step = so.max_time_step;
+      p.min_time_step = so.min_time_step;
+      p.inc_factor = so.inc_factor;
+      p.max_it = so.max_it;
+      p.min_it = so.min_it;
+      p.conv_increase = so.conv_increase;
+      p.dynamic = so.type == GF_DYNAMIC;
+      p.zero_va = !p.dynamic || so.zero_ic;
+      p.beta = so.beta;
+      p.gamma = so.gamma;
+      const gf_criteria& cr = m.criteria;
+      p.force_tol = cr.force_tol;
+      p.moment_tol = cr.moment_tol;
+      p.force_min = cr.force_min;
+      p.moment_min = cr.moment_min;
+      p.disp_tol = cr.disp_tol;
+      p.rot_tol = cr.rot_tol;
+      p.disp_min = cr.disp_min;
+      p.rot_min = cr.rot_min;
+      p.divergence_ref = cr.divergence_ref;
+      if (so.type == GF_DYNAMIC && (so.rayleigh_alpha != 0.0 || so.rayleigh_beta != 0.0)) {
+        p.ray_on = 1;
+        p.ray_alpha = so.rayleigh_alpha;
+        p.ray_beta = so.rayleigh_beta;
+        p.ray_update = so.update_rayleigh ? 1 : 0;
+        if (m.n_beams) b.any_rayleigh = 1;
+        if (m.n_shells) b.sh.any_rayleigh = 1;
+      }
+      step_params.push_back(p);
+      start = so.end_time;
     }
+    params[s] = step_params[inf.step_off];
   }
   b.n_struct = n;
   b.n_nodes = node_off;
@@ -982,7 +1005,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !upload(B, &b.cons, cons) || !upload(B, &b.node_struct, node_struct) || !upload(B, &b.enodes, enodes) ||
       !upload(B, &b.estruct, estruct) || !upload(B, &b.bconst, bconst) || !upload(B, &b.bhist, bhist) ||
       !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
-      !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.loads, loads) ||
+      !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.step_params, step_params) ||
+      !upload(B, &b.loads, loads) ||
       !upload(B, &b.disps, disps) || !upload(B, &b.tables, tables) || !upload(B, &b.table_data, tdata) ||
       !dup(B, &B->copy0, b.copy, copy.size()) || !dup(B, &B->Qn0, b.Qn, Qn.size()) ||
       !dup(B, &B->bhist0, b.bhist, bhist.size()) || !dup(B, &B->baux0, b.baux, baux.size()))
@@ -1252,7 +1276,7 @@ std::vector<std::pair<void*, size_t>> state_parts(const gf_batch* B) {
       {b.disp, 8 * 6 * nn},      {b.copy, 8 * 6 * nn},      {b.Qn, 8 * 9 * nn},
       {b.vel, 8 * 6 * nn},       {b.accel, 8 * 6 * nn},     {b.copy_vel, 8 * 6 * nn},
       {b.copy_accel, 8 * 6 * nn}, {b.bhist, sizeof(BeamHist) * ne}, {b.baux, sizeof(BeamHistAux) * ne},
-      {b.state, sizeof(StructState) * (size_t)b.n_struct}};
+      {b.state, sizeof(StructState) * (size_t)b.n_struct}, {b.params, sizeof(StructParams) * (size_t)b.n_struct}};
   if (ns) {
     v.push_back({b.sh.shist, sizeof(ShellHist) * ns});
     v.push_back({b.sh.saux, sizeof(ShellHistAux) * ns});

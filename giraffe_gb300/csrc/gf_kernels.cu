@@ -127,11 +127,12 @@ __device__ void update_dyn_node(const Batch& b, const double* a, int node) {
 }
 
 // ---------------------------------------------------------------------------
-// initial state: reference src/Static.cpp:140-170
+// initial state: the first solution step (reference src/Static.cpp:140-170)
 __global__ void k_init_state(Batch b) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= b.n_struct) return;
-  const StructParams& p = b.params[s];
+  const StructParams p = b.step_params[b.info[s].step_off];
+  b.params[s] = p;
   StructState& st = b.state[s];
   StructState z = {};
   z.phase = PH_START;
@@ -145,11 +146,13 @@ __global__ void k_init_state(Batch b) {
 __global__ void k_step_begin(Batch b) {
   int s = blockIdx.x;
   StructState& st = b.state[s];
-  __shared__ int go;
+  __shared__ int go, zero_va;
   if (threadIdx.x == 0) {
     if (s == 0) *b.running = 0;
     go = st.phase == PH_START;
+    zero_va = go && st.zero_va;
     if (go) {
+      st.zero_va = 0;
       const StructParams& p = b.params[s];
       st.last_converged_time = st.time;
       st.time += st.time_step;
@@ -183,6 +186,7 @@ __global__ void k_step_begin(Batch b) {
   for (int i = threadIdx.x; i < inf.n_nodes * 6; i += blockDim.x) {
     int64_t q = (int64_t)inf.node_off * 6 + i;
     b.disp[q] = 0.0;
+    if (zero_va) b.vel[q] = b.accel[q] = b.copy_vel[q] = b.copy_accel[q] = 0.0;
     if (dyn) {  // back to the converged velocities (a no-op after a commit)
       b.vel[q] = b.copy_vel[q];
       b.accel[q] = b.copy_accel[q];
@@ -890,6 +894,28 @@ __global__ void k_control(Batch b) {
     st.bisections++;
   }
   if ((st.time < p.end_time || st.diverged) && !st.aborted) {
+    st.phase = PH_START;
+    atomicAdd(b.running, 1);
+  } else if (!st.aborted && st.step + 1 < b.info[s].n_steps) {
+    // the next solution step (reference src/main.cpp:52-60) starts from
+    // this state: its own step control, a fresh residual-criterion average
+    // (src/Static.cpp:146, src/Dynamic.cpp:261), Rayleigh matrices formed
+    // anew (Dynamic::Solve's `first`), and zero nodal velocities for a
+    // Static step (ZerosVelAccel) or a Dynamic one with ZeroIC.  The commit
+    // kernels of this pass still save the converged state of the step that
+    // ended; of the new parameters they read only the Dynamic flag (whether
+    // to save the velocities), and in every sequence the velocities it
+    // decides on are zero or zeroed before they are read again.
+    st.step++;
+    const StructParams np = b.step_params[b.info[s].step_off + st.step];
+    b.params[s] = np;
+    st.time = np.start_time;
+    st.last_converged_time = np.start_time;
+    st.time_step = np.time_step0;
+    st.convergence_counter = 0;
+    st.n_conv_evaluated = 0;
+    st.ray_init = 0;
+    st.zero_va = np.zero_va;
     st.phase = PH_START;
     atomicAdd(b.running, 1);
   } else {

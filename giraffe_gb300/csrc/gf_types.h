@@ -97,6 +97,10 @@ struct StructParams {
   // (or at every iteration with ray_update)
   double ray_alpha, ray_beta;
   int ray_on, ray_update;
+  // the step starts from zero nodal velocities and accelerations: a Static
+  // step (Solution::ZerosVelAccel) or a Dynamic one with ZeroIC
+  int zero_va;
+  int pad_p;
 };
 
 // Per-structure ranges in the batch arrays.
@@ -115,6 +119,8 @@ struct StructInfo {
   int wkl;
   int n_panels;  // ceil(n_free / GF_WB_NB)
   int pad_w;
+  // solution steps: Batch::step_params[step_off .. step_off + n_steps)
+  int step_off, n_steps;
   int64_t wb_off;    // into ShellData::wband
 };
 
@@ -143,6 +149,8 @@ struct StructState {
   int solve_sweeps;  // refinement sweeps of the last solve (mixed path)
   int fp64_fallback;  // mixed path: this structure factors in FP64
   int ray_init;       // Rayleigh matrices formed (after the step's first iteration)
+  int step;           // current solution step of the structure
+  int zero_va;        // zero the nodal velocities / accelerations before the next time step
   double time, time_step, last_converged_time, current_time_step;
   double force_crit, moment_crit, disp_crit, rot_crit;
   double last_res, last_inc;
@@ -295,7 +303,8 @@ struct Batch {
   float* U32;
   // structures
   StructInfo* info;
-  StructParams* params;
+  StructParams* params;       // the current solution step's parameters
+  StructParams* step_params;  // every solution step of every structure
   StructState* state;
   // loads
   LoadEntry* loads;

@@ -3,7 +3,8 @@
 The reference reads a deck token by token (fscanf "%s") in IO::ReadFile
 (reference src/IO.cpp:193-657), each top-level keyword handing the stream to
 the block's own reader.  This reader follows the same keywords and layouts
-for the blocks of a Beam_1 / Shell_1 Static or Dynamic solution step:
+for the blocks of a sequence of Beam_1 / Shell_1 Static and Dynamic
+solution steps:
 
   SolutionSteps   Static / Dynamic (src/Static.cpp:40-130,
                   src/Dynamic.cpp:60-215: EndTime ... Sample, RayleighDamping,
@@ -159,16 +160,18 @@ def _solution(tk: _Tokens, kind: str) -> Solution:
         s.beta = tk.float()
         tk.expect("Gamma")
         s.gamma = tk.float()
-        if tk.peek() == "ZeroIC":
+        if tk.peek() == "ZeroIC":  # a bare keyword (src/Dynamic.cpp:209-216)
             tk.next()
-            tk.int()
+            s.zero_ic = 1
     return s
 
 
-def read_deck(text: str, step: int = 1) -> Structure:
-    """The structure and solution step `step` (1-based) of a deck.  Only the
-    first step starts from the undeformed configuration, as a fresh solve of
-    this library does; later steps of a multi-step deck raise DeckError."""
+def read_deck(text: str, step: int = None) -> Structure:
+    """The structure of a deck with its solution steps: the first as
+    `solution`, the others in `next_steps`, run in sequence as the
+    reference's main loop does.  `step` = 1 keeps the first step alone;
+    later steps on their own raise DeckError (only the first starts from the
+    undeformed configuration)."""
     tk = _Tokens(text)
     steps, nodes, elems, mats, secs, shell_secs, css = [], {}, [], {}, {}, {}, {}
     node_sets, elem_sets, loads, disps, cons = {}, {}, [], [], []
@@ -356,10 +359,12 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
            criteria) -> Structure:
     if not steps:
         raise DeckError("the deck has no solution step")
-    if not 1 <= step <= len(steps):
-        raise DeckError(f"the deck has {len(steps)} solution step(s), not {step}")
-    if step != 1:
-        raise DeckError("only the first solution step starts from the undeformed configuration")
+    if step is not None:
+        if not 1 <= step <= len(steps):
+            raise DeckError(f"the deck has {len(steps)} solution step(s), not {step}")
+        if step != 1:
+            raise DeckError("only the first solution step starts from the undeformed configuration")
+    n_steps = len(steps) if step is None else 1
     if not nodes:
         raise DeckError("the deck has no nodes")
     ids = sorted(nodes)
@@ -395,7 +400,10 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
             s.shells.append((*[n - 1 for n in nd], lookup(mat_ix, m, "material"),
                              lookup(ssec_ix, sc, "shell section"), cs_ix.get(c, 0)))
     for ns, tables in cons:
-        mask = [1 if _step_value(t, step) else 0 for t in tables]
+        mask = [1 if _step_value(t, 1) else 0 for t in tables]
+        if any([1 if _step_value(t, k) else 0 for t in tables] != mask for k in range(2, n_steps + 1)):
+            raise DeckError(f"NodalConstraint on node set {ns}: constraints that change between solution steps "
+                            "are not supported")
         for n in lookup(node_sets, ns, "node set"):
             s.clamp(n - 1, mask)
     for ld in loads:
@@ -410,14 +418,23 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
                 raise DeckError(f"ShellLoad on element set {es}: every element must be a Shell_1")
             s.loads.append(PressureLoad([shell_of[e] for e in members], table, area_update=au))
     for ns, c, active, table, ap in disps:
-        if _step_value(active, step):
+        on = [_step_value(active, k) for k in range(1, n_steps + 1)]
+        if any(x != on[0] for x in on):
+            raise DeckError(f"NodalDisplacement on node set {ns}: displacements active in some solution steps "
+                            "only are not supported")
+        if on[0]:
             s.displacements.append(NodalDisplacement([n - 1 for n in lookup(node_sets, ns, "node set")],
                                                      lookup(cs_ix, c, "coordinate system"), table, ap))
-    s.solution = steps[step - 1]
+    start = 0.0  # each step starts where the previous one ends (src/Database.cpp:759-768)
+    for so in steps[:n_steps]:
+        so.start_time = start
+        start = so.end_time
+    s.solution = steps[0]
+    s.next_steps = list(steps[1:n_steps])
     s.criteria = dict(criteria)
     return s
 
 
-def read_deck_file(path: str, step: int = 1) -> Structure:
+def read_deck_file(path: str, step: int = None) -> Structure:
     with open(path, encoding="latin-1") as f:
         return read_deck(f.read(), step)

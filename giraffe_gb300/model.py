@@ -3,8 +3,8 @@
 A :class:`Structure` holds what a GIRAFFE input deck holds for this path
 (nodes, Hooke materials, sections, coordinate systems, Beam_1 / Shell_1
 elements, nodal constraints, nodal loads, shell pressure loads, prescribed
-nodal displacements, one Static or Dynamic solution step and the convergence
-criteria; reference src/IO.cpp:288-657).  It can
+nodal displacements, a sequence of Static and Dynamic solution steps and the
+convergence criteria; reference src/IO.cpp:288-657).  It can
 
 * produce the flat C description ``gf_model_desc`` (include/giraffe_model.h)
   that both the CUDA library and the CPU oracle take, and
@@ -80,7 +80,7 @@ class gf_solution(C.Structure):
                 ("min_time_step", C.c_double), ("max_it", C.c_int), ("min_it", C.c_int),
                 ("conv_increase", C.c_int), ("inc_factor", C.c_double), ("beta", C.c_double),
                 ("gamma", C.c_double), ("rayleigh_alpha", C.c_double),
-                ("rayleigh_beta", C.c_double), ("update_rayleigh", C.c_int)]
+                ("rayleigh_beta", C.c_double), ("update_rayleigh", C.c_int), ("zero_ic", C.c_int)]
 
 
 class gf_criteria(C.Structure):
@@ -100,7 +100,8 @@ class gf_model_desc(C.Structure):
                 ("constraints", _vp),
                 ("n_loads", C.c_int), ("loads", _vp),
                 ("n_displacements", C.c_int), ("displacements", _vp),
-                ("solution", gf_solution), ("criteria", gf_criteria), ("beam_pretension", _vp)]
+                ("solution", gf_solution), ("criteria", gf_criteria), ("beam_pretension", _vp),
+                ("n_next_steps", C.c_int), ("next_steps", _vp)]
 
 
 def _r(v):
@@ -227,6 +228,7 @@ class Solution:
     rayleigh_alpha: float = 0.0
     rayleigh_beta: float = 0.0
     update_rayleigh: int = 0
+    zero_ic: int = 0          # Dynamic: ZeroIC
 
 
 # reference src/ConvergenceCriteria.cpp:15-60
@@ -249,6 +251,7 @@ class Structure:
     loads: list = field(default_factory=list)
     displacements: list = field(default_factory=list)
     solution: Solution = field(default_factory=Solution)
+    next_steps: list = field(default_factory=list)     # Solution steps run after `solution`
     criteria: dict = field(default_factory=lambda: dict(DEFAULT_CRITERIA))
     pretension: dict = field(default_factory=dict)     # beam index -> Beam_1 PreTension T0
 
@@ -305,29 +308,31 @@ class Structure:
 
     # ---- deck in the reference's syntax ----
     @staticmethod
-    def from_inp(text: str, step: int = 1) -> "Structure":
-        """The structure and solution step of a deck in the reference's .inp
+    def from_inp(text: str, step: int = None) -> "Structure":
+        """The structure and solution steps of a deck in the reference's .inp
         syntax (giraffe_gb300.deck.read_deck)."""
         from .deck import read_deck
         return read_deck(text, step)
 
     def to_inp(self) -> str:
         o = []
-        s = self.solution
-        o.append("SolutionSteps\t1")
-        if s.type == GF_STATIC:
-            o.append(f"Static\t1\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
-                     f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
-                     f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
-                     f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}")
-        else:
-            o.append(f"Dynamic\t1\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
-                     f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
-                     f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
-                     f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}\n"
-                     f"RayleighDamping\tAlpha\t{_r(s.rayleigh_alpha)}\tBeta\t{_r(s.rayleigh_beta)}"
-                     f"\tUpdate\t{s.update_rayleigh}\n"
-                     f"NewmarkCoefficients\tBeta\t{_r(s.beta)}\tGamma\t{_r(s.gamma)}")
+        steps = [self.solution] + list(self.next_steps)
+        o.append(f"SolutionSteps\t{len(steps)}")
+        for k, s in enumerate(steps, 1):
+            if s.type == GF_STATIC:
+                o.append(f"Static\t{k}\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
+                         f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
+                         f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
+                         f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}")
+            else:
+                o.append(f"Dynamic\t{k}\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"
+                         f"MaxTimeStep\t{_r(s.max_time_step)}\nMinTimeStep\t{_r(s.min_time_step)}\n"
+                         f"MaxIt\t{s.max_it}\nMinIt\t{s.min_it}\nConvIncrease\t{s.conv_increase}\n"
+                         f"IncFactor\t{_r(s.inc_factor)}\nSample\t{s.sample}\n"
+                         f"RayleighDamping\tAlpha\t{_r(s.rayleigh_alpha)}\tBeta\t{_r(s.rayleigh_beta)}"
+                         f"\tUpdate\t{s.update_rayleigh}\n"
+                         f"NewmarkCoefficients\tBeta\t{_r(s.beta)}\tGamma\t{_r(s.gamma)}"
+                         + ("\nZeroIC" if s.zero_ic else ""))
         o.append(f"Nodes\t{self.n_nodes}")
         for i, x in enumerate(np.asarray(self.nodes, dtype=np.float64)):
             o.append(f"Node\t{i + 1}\t{_r(x[0])}\t{_r(x[1])}\t{_r(x[2])}")
@@ -471,10 +476,15 @@ class DescHandle:
             disps[k].angular = 1 if D.angular == "EulerVector" else 0
             disps[k].table = gf_table(len(tt), tv.shape[1], _ptr(tt, _dp), _ptr(tv, _dp))
         self.keep += [loads, disps]
-        so = s.solution
-        sol = gf_solution(so.type, so.start_time, so.end_time, so.time_step, so.max_time_step,
-                          so.min_time_step, so.max_it, so.min_it, so.conv_increase, so.inc_factor,
-                          so.beta, so.gamma, so.rayleigh_alpha, so.rayleigh_beta, so.update_rayleigh)
+        def csol(so):
+            return gf_solution(so.type, so.start_time, so.end_time, so.time_step, so.max_time_step,
+                               so.min_time_step, so.max_it, so.min_it, so.conv_increase, so.inc_factor,
+                               so.beta, so.gamma, so.rayleigh_alpha, so.rayleigh_beta, so.update_rayleigh,
+                               int(so.zero_ic))
+
+        sol = csol(s.solution)
+        nxt = (gf_solution * max(1, len(s.next_steps)))(*[csol(so) for so in s.next_steps])
+        self.keep.append(nxt)
         crit = gf_criteria(**{k: float(v) for k, v in s.criteria.items()})
         pre = None
         if s.pretension:
@@ -486,7 +496,8 @@ class DescHandle:
             len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
             len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
             len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), C.addressof(loads),
-            len(s.displacements), C.addressof(disps), sol, crit, _ptr(pre))
+            len(s.displacements), C.addressof(disps), sol, crit, _ptr(pre), len(s.next_steps),
+            C.addressof(nxt) if s.next_steps else None)
 
     @property
     def ref(self):

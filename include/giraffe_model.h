@@ -4,8 +4,8 @@
  * deck for that path (reference src/IO.cpp:288-657): nodes, Hooke materials,
  * beam sections, shell sections, coordinate systems, Beam_1 and Shell_1
  * elements, nodal constraints, nodal loads, shell pressure loads, nodal
- * prescribed displacements, one Static or Dynamic solution step and the
- * convergence criteria.  All indices are 0-based; all arrays are row-major
+ * prescribed displacements, a sequence of Static and Dynamic solution steps
+ * and the convergence criteria.  All indices are 0-based; all arrays are row-major
  * and owned by the caller for the duration of the call that takes them.
  *
  * Both the CUDA library (libgiraffe_gpu.so) and the CPU oracle take this
@@ -76,6 +76,8 @@ typedef struct gf_solution {
   double rayleigh_alpha;
   double rayleigh_beta;
   int update_rayleigh;
+  int zero_ic;         /* Dynamic: ZeroIC, start from zero nodal velocities and
+                          accelerations (reference src/Dynamic.cpp:209-216) */
 } gf_solution;
 
 /* ConvergenceCriteria (reference src/ConvergenceCriteria.cpp:15-60 gives the
@@ -110,6 +112,16 @@ typedef struct gf_model_desc {
   gf_criteria criteria;
   const double* beam_pretension; /* [n_beams]: Beam_1 PreTension T0 (force), or NULL
                                     (reference src/Beam_1.cpp:420-428, 616-621) */
+  /* Solution steps after `solution`, run in sequence from the state the
+   * previous one ends in (reference src/main.cpp:52-60).  Each starts at the
+   * previous step's end time (src/Database.cpp:759-768; their start_time is
+   * not read), restarts the residual-criterion average and the step control
+   * (src/Static.cpp:143-166, src/Dynamic.cpp:257-287); a Static step zeroes
+   * the nodal velocities and accelerations (Solution::ZerosVelAccel), a
+   * Dynamic step keeps them unless zero_ic.  Constraints and prescribed
+   * displacements apply to every step. */
+  int n_next_steps;
+  const gf_solution* next_steps;
 } gf_model_desc;
 
 #ifdef __cplusplus

@@ -43,6 +43,7 @@ typedef struct {
   int* active;   /* [nn][6] */
   int* cons;     /* [nn][6] */
   int n_free, n_fixed, kl, ku, ldab;
+  int kl_nat;    /* half-bandwidth under the reference's numbering */
   double* disp;  /* increments in the step (Node::displacements) */
   double* copy;  /* Node::copy_coordinates */
   double* Qn;    /* Node::Q */
@@ -53,6 +54,7 @@ typedef struct {
   os_const* sc;
   os_hist* sh;
   double* ab; int* ipiv; double* PA;
+  int* pf;      /* free DOF (GL - 1) -> row / column of the band solver */
   /* criteria state */
   double force_crit, moment_crit, disp_crit, rot_crit;
   int n_conv_evaluated;
@@ -76,7 +78,7 @@ static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
   free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
-  free(s->rd); free(s->rds);
+  free(s->rd); free(s->rds); free(s->pf);
 }
 
 /* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
@@ -181,6 +183,38 @@ static int ost_init(ost* s, const gf_model_desc* m) {
             if (ga > 0 && gb > 0 && ga - gb > kl) kl = ga - gb;
           }
       }
+  s->kl_nat = kl;
+  /* the band solver's order of the free DOFs: the reference's numbering,
+   * or reverse Cuthill-McKee when that gives a narrower band */
+  s->pf = malloc(sizeof(int) * (size_t)(fr ? fr : 1));
+  for (int i = 0; i < fr; ++i) s->pf[i] = i;
+  if (fr > 1) {
+    size_t np = 0, cap = (size_t)s->nb * 324 + (size_t)s->ns * 729 + 1;
+    int* pi = malloc(sizeof(int) * cap);
+    int* pj = malloc(sizeof(int) * cap);
+    for (int e = 0; e < s->nb; ++e)
+      for (int a = 0; a < 18; ++a)
+        for (int b = 0; b < 18; ++b) {
+          int ga = s->GL[6 * m->beams[6 * e + a / 6] + a % 6], gb = s->GL[6 * m->beams[6 * e + b / 6] + b % 6];
+          if (ga > 0 && gb > 0 && ga < gb) { pi[np] = ga - 1; pj[np] = gb - 1; np++; }
+        }
+    for (int e = 0; e < s->ns; ++e) {
+      int g[27];
+      shell_dofs(s, e, g);
+      for (int a = 0; a < 27; ++a)
+        for (int b = 0; b < 27; ++b)
+          if (g[a] > 0 && g[b] > 0 && g[a] < g[b]) { pi[np] = g[a] - 1; pj[np] = g[b] - 1; np++; }
+    }
+    int *xadj, *adj;
+    oracle_graph(fr, np, pi, pj, &xadj, &adj);
+    int* perm = malloc(sizeof(int) * (size_t)fr);
+    oracle_rcm(fr, xadj, adj, perm);
+    if (oracle_perm_bandwidth(fr, xadj, adj, perm) < kl) {
+      memcpy(s->pf, perm, sizeof(int) * (size_t)fr);
+      kl = oracle_perm_bandwidth(fr, xadj, adj, perm);
+    }
+    free(perm); free(xadj); free(adj); free(pi); free(pj);
+  }
   s->kl = s->ku = kl;
   s->ldab = 2 * kl + kl + 1;
   s->ab = malloc(sizeof(double) * (size_t)s->ldab * (size_t)(fr ? fr : 1));
@@ -201,7 +235,7 @@ static int ost_init(ost* s, const gf_model_desc* m) {
 
 /* ---- global assembly ---- */
 static void add_K(ost* s, int ga, int gb, double v) {
-  if (ga > 0 && gb > 0) GB_AT(s->ab, s->ldab, s->kl, s->ku, ga - 1, gb - 1) += v;
+  if (ga > 0 && gb > 0) GB_AT(s->ab, s->ldab, s->kl, s->ku, s->pf[ga - 1], s->pf[gb - 1]) += v;
 }
 
 static void assemble(ost* s) {
@@ -533,22 +567,26 @@ static void record(ost* s, oracle_record* rec, double time, int iterations) {
 }
 
 static int solve_linear(ost* s) {
-  if (s->n_free == 0) return 0;
-  int info = oracle_gbtrf(s->n_free, s->kl, s->ku, s->ab, s->ldab, s->ipiv);
+  const int n = s->n_free;
+  if (n == 0) return 0;
+  int info = oracle_gbtrf(n, s->kl, s->ku, s->ab, s->ldab, s->ipiv);
   if (info) return 1;
-  oracle_gbtrs(s->n_free, s->kl, s->ku, s->ab, s->ldab, s->ipiv, s->PA);
-  for (int i = 0; i < s->n_free; ++i)
+  double* w = malloc(sizeof(double) * (size_t)n);
+  for (int i = 0; i < n; ++i) w[s->pf[i]] = s->PA[i];
+  oracle_gbtrs(n, s->kl, s->ku, s->ab, s->ldab, s->ipiv, w);
+  for (int i = 0; i < n; ++i) s->PA[i] = w[s->pf[i]];
+  free(w);
+  for (int i = 0; i < n; ++i)
     if (!(s->PA[i] == s->PA[i])) return 1;
   return 0;
 }
 
 /* reference src/Static.cpp:140-311 */
-static int static_solve(ost* s, oracle_record* rec, int* stats) {
-  const gf_solution* so = &s->m->solution;
+static int static_solve(ost* s, const gf_solution* so, double start_time, oracle_record* rec, int* stats) {
   int aborted = 0, convergence_counter = 0, converged_number = 0, total_it = 0, bisections = 0;
   s->n_conv_evaluated = 0;
-  s->last_converged_time = so->start_time;
-  record(s, rec, so->start_time, 0);
+  s->last_converged_time = start_time;
+  record(s, rec, start_time, 0);
   double time_step = so->time_step, time = s->last_converged_time;
   s->diverged = 0;
   for (int i = 0; i < s->nn * 6; ++i) s->copy_vel[i] = s->copy_accel[i] = s->vel[i] = s->accel[i] = 0.0;
@@ -649,18 +687,21 @@ static void update_dyn(ost* s) {
 }
 
 /* reference src/Dynamic.cpp:255-468 (no contact, no special constraints,
- * zero initial conditions) */
-static int dynamic_solve(ost* s, oracle_record* rec, int* stats) {
-  const gf_solution* so = &s->m->solution;
+ * no InitialConditions blocks) */
+static int dynamic_solve(ost* s, const gf_solution* so, double start_time, oracle_record* rec, int* stats) {
   int aborted = 0, convergence_counter = 0, converged_number = 0, total_it = 0, bisections = 0;
   s->n_conv_evaluated = 0;
-  s->last_converged_time = so->start_time;
-  record(s, rec, so->start_time, 0);
+  s->last_converged_time = start_time;
+  record(s, rec, start_time, 0);
   double time_step = so->time_step, time = s->last_converged_time;
-  /* ComputeInitialConditions with zero initial conditions: Zeros() and a
-   * SaveConfiguration that leaves every node unchanged */
+  /* ComputeInitialConditions (reference src/Solution.cpp:866-885): Zeros(),
+   * ZeroIC when asked, then a SaveConfiguration that leaves every node's
+   * configuration unchanged and makes the velocities the converged ones */
   memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
+  if (so->zero_ic)
+    for (int i = 0; i < s->nn * 6; ++i) s->vel[i] = s->accel[i] = 0.0;
   for (int i = 0; i < s->nn * 6; ++i) { s->copy_vel[i] = s->vel[i]; s->copy_accel[i] = s->accel[i]; }
+  s->ray_init = 0; /* Dynamic::Solve's `first`: C is formed anew */
   s->diverged = 0;
   while ((time < so->end_time || s->diverged) && !aborted) {
     s->last_converged_time = time;
@@ -735,19 +776,31 @@ static void final_state(ost* s, double* out) {
   }
 }
 
+/* The solution steps in sequence (reference src/main.cpp:52-60), each
+ * starting at the previous one's end time (src/Database.cpp:759-768);
+ * stats add up over the steps. */
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
   ost s;
   ost_init(&s, m);
-  s.dynamic = m->solution.type == GF_DYNAMIC;
-  if (s.dynamic && (m->solution.rayleigh_alpha != 0.0 || m->solution.rayleigh_beta != 0.0)) {
-    s.ray = 1;
-    s.ray_alpha = m->solution.rayleigh_alpha;
-    s.ray_beta = m->solution.rayleigh_beta;
-    s.ray_update = m->solution.update_rayleigh;
-    s.rd = calloc((size_t)324 * (s.nb ? s.nb : 1), sizeof(double));
-    s.rds = calloc((size_t)729 * (s.ns ? s.ns : 1), sizeof(double));
+  int r = 0, total[4] = {0, 0, 0, 0};
+  double start = m->solution.start_time;
+  for (int k = 0; k <= m->n_next_steps && r == 0; ++k) {
+    const gf_solution* so = k == 0 ? &m->solution : m->next_steps + (k - 1);
+    s.dynamic = so->type == GF_DYNAMIC;
+    s.ray = s.dynamic && (so->rayleigh_alpha != 0.0 || so->rayleigh_beta != 0.0);
+    if (s.ray) {
+      s.ray_alpha = so->rayleigh_alpha;
+      s.ray_beta = so->rayleigh_beta;
+      s.ray_update = so->update_rayleigh;
+      if (!s.rd) s.rd = calloc((size_t)324 * (s.nb ? s.nb : 1), sizeof(double));
+      if (!s.rds) s.rds = calloc((size_t)729 * (s.ns ? s.ns : 1), sizeof(double));
+    }
+    int st[4] = {0, 0, 0, 0};
+    r = s.dynamic ? dynamic_solve(&s, so, start, rec, st) : static_solve(&s, so, start, rec, st);
+    for (int q = 0; q < 4; ++q) total[q] += st[q];
+    start = so->end_time;
   }
-  int r = s.dynamic ? dynamic_solve(&s, rec, stats) : static_solve(&s, rec, stats);
+  if (stats) memcpy(stats, total, sizeof(total));
   final_state(&s, final_nodes);
   ost_free(&s);
   return r;
@@ -780,15 +833,22 @@ int oracle_beam_element(const double* xyz9, const double* mat3, const double* se
 int oracle_first_tangent(const gf_model_desc* m, double* ab, double* PA, int* dims) {
   ost s;
   ost_init(&s, m);
-  dims[0] = s.n_free;
-  dims[1] = s.kl;
+  const int n = s.n_free, kn = s.kl_nat, ld = 3 * kn + 1;
+  dims[0] = n;
+  dims[1] = kn;
   if (ab) {
     s.last_converged_time = m->solution.start_time;
     s.current_time_step = m->solution.time_step;
     mount_displacements(&s);
     assemble(&s);
-    memcpy(ab, s.ab, sizeof(double) * (size_t)s.ldab * (size_t)s.n_free);
-    memcpy(PA, s.PA, sizeof(double) * (size_t)s.n_free);
+    /* back to the reference's numbering */
+    memset(ab, 0, sizeof(double) * (size_t)ld * (size_t)n);
+    for (int j = 0; j < n; ++j)
+      for (int i = j - kn < 0 ? 0 : j - kn; i <= j + kn && i < n; ++i) {
+        int pi = s.pf[i], pj = s.pf[j], d = pi - pj;
+        if (d <= s.kl && -d <= s.ku) GB_AT(ab, ld, kn, kn, i, j) = GB_AT(s.ab, s.ldab, s.kl, s.ku, pi, pj);
+      }
+    memcpy(PA, s.PA, sizeof(double) * (size_t)n);
   }
   ost_free(&s);
   return 0;

@@ -138,8 +138,10 @@ Matrix operator*(SparseMatrix& A, Matrix& x) {
   return y;
 }
 
-// PARDISO substitute: FP64 band LU with partial pivoting over the CSR
-// pattern's own bandwidth.  info_fail follows the reference convention
+// PARDISO substitute: FP64 band LU with partial pivoting, in the CSR
+// numbering or, where that narrows the band, in reverse Cuthill-McKee order
+// (PARDISO reorders too: nested dissection, reference
+// src/SparseMatrix.cpp:93-94).  info_fail follows the reference convention
 // (0 ok, 1 failure).
 Matrix sparsesystem(SparseMatrix& A, Matrix& b, int* info_fail, int, int) {
   if (!A.mounted) A.Mount();
@@ -150,6 +152,8 @@ Matrix sparsesystem(SparseMatrix& A, Matrix& b, int* info_fail, int, int) {
   const double* a = A.m_matrix.valuePtr();
   const int* ia = A.m_matrix.outerIndexPtr();
   const int* ja = A.m_matrix.innerIndexPtr();
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
   int kl = 0, ku = 0;
   for (int i = 0; i < n; ++i)
     for (int p = ia[i]; p < ia[i + 1]; ++p) {
@@ -157,15 +161,32 @@ Matrix sparsesystem(SparseMatrix& A, Matrix& b, int* info_fail, int, int) {
       if (d > ku) ku = d;
       if (-d > kl) kl = -d;
     }
+  if (n > 1) {
+    std::vector<int> pi, pj;
+    for (int i = 0; i < n; ++i)
+      for (int p = ia[i]; p < ia[i + 1]; ++p) { pi.push_back(i); pj.push_back(ja[p]); }
+    int *xadj, *adj;
+    oracle_graph(n, pi.size(), pi.data(), pj.data(), &xadj, &adj);
+    std::vector<int> rcm(n);
+    oracle_rcm(n, xadj, adj, rcm.data());
+    int bw = oracle_perm_bandwidth(n, xadj, adj, rcm.data());
+    if (bw < (kl > ku ? kl : ku)) {
+      perm = rcm;
+      kl = ku = bw;
+    }
+    free(xadj);
+    free(adj);
+  }
   int ldab = 2 * kl + ku + 1;
-  std::vector<double> ab((size_t)ldab * n, 0.0);
+  std::vector<double> ab((size_t)ldab * n, 0.0), w(n);
   std::vector<int> ipiv(n);
   for (int i = 0; i < n; ++i)
-    for (int p = ia[i]; p < ia[i + 1]; ++p) GB_AT(ab.data(), ldab, kl, ku, i, ja[p]) += a[p];
-  for (int i = 0; i < n; ++i) x(i, 0) = b(i, 0);
+    for (int p = ia[i]; p < ia[i + 1]; ++p) GB_AT(ab.data(), ldab, kl, ku, perm[i], perm[ja[p]]) += a[p];
+  for (int i = 0; i < n; ++i) w[perm[i]] = b(i, 0);
   int info = oracle_gbtrf(n, kl, ku, ab.data(), ldab, ipiv.data());
   if (info != 0) { *info_fail = 1; return x; }
-  oracle_gbtrs(n, kl, ku, ab.data(), ldab, ipiv.data(), x.getMatrix());
+  oracle_gbtrs(n, kl, ku, ab.data(), ldab, ipiv.data(), w.data());
+  for (int i = 0; i < n; ++i) x(i, 0) = w[perm[i]];
   for (int i = 0; i < n; ++i)
     if (!(x(i, 0) == x(i, 0))) *info_fail = 1;
   return x;

@@ -53,6 +53,11 @@ stores what the reference computes:
                          the same with Rayleigh damping (alpha 8 1/s, beta
                          2e-5 s), AreaUpdate 0 with C formed once, and
                          AreaUpdate 1 with C formed at every iteration.
+* ref_plate_release.npz  two solution steps: the 3x3x2 plate loaded in a Static
+                         step, then released into a Dynamic step (15 steps).
+* ref_chain_sequence.npz four solution steps on a pipe chain: Static, damped
+                         Dynamic after a load drop, Dynamic from rest (ZeroIC),
+                         Static reloading.
 
 Node records hold copy_coordinates (position and accumulated Rodrigues
 vector) then the nodal Q (row-major); Gauss-point records hold Q_i
@@ -388,6 +393,8 @@ DECKS = {
                                                                      rayleigh_beta=2e-5),
     "ref_plate_dynamic_rayleigh_update.npz": lambda: configs.plate_dynamics(3, steps=20, rayleigh_alpha=8.0,
                                                                             rayleigh_beta=2e-5, update_rayleigh=1),
+    "ref_plate_release.npz": lambda: configs.plate_release(3),
+    "ref_chain_sequence.npz": configs.chain_sequence,
     "ref_riser_rayleigh.npz": lambda: configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0,
                                                           rayleigh_alpha=0.3, rayleigh_beta=0.004,
                                                           update_rayleigh=1),

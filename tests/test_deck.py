@@ -41,6 +41,7 @@ def same_structure(a, b):
         assert np.array_equal(x.table.times, y.table.times)
         assert np.array_equal(np.asarray(x.table.values, dtype=float), np.asarray(y.table.values, dtype=float))
     assert a.solution == b.solution
+    assert a.next_steps == b.next_steps
     assert {int(k): float(v) for k, v in a.pretension.items()} == {int(k): float(v) for k, v in b.pretension.items()}
     assert {k: float(v) for k, v in a.criteria.items()} == {k: float(v) for k, v in b.criteria.items()}
 
@@ -49,7 +50,8 @@ def same_structure(a, b):
     configs.tutorial01, configs.cantilever_rollup, lambda: configs.tutorial10(0.2, 0.002, 1),
     lambda: configs.pipe_chain(25, 0.4, 0.03, [1e5, -2e4, 3e4]),
     lambda: configs.riser_chain(15, 0.35, 0.025, 1.0, 6.0, steps=30), lambda: configs.rotating_base("EulerVector"),
-    configs.pretensioned_chain,
+    configs.pretensioned_chain, configs.chain_sequence, lambda: configs.plate_release(3),
+    lambda: configs.plate_dynamics(3, steps=10, rayleigh_alpha=8.0, rayleigh_beta=2e-5, update_rayleigh=1),
     lambda: configs.square_plate(3, steps=10, area_update=0), lambda: configs.square_plate(4, steps=20),
 ])
 def test_written_deck_reads_back_the_same(make):
@@ -94,13 +96,31 @@ def test_reference_tutorial10_reads_as_the_built_config():
     same_structure(read_deck_file(_ref_deck("tutorial10")), configs.tutorial10())
 
 
-def test_reference_tutorial05_first_step():
-    """A Shell_1 plate with a nodal load: the Static first step reads; the
-    Dynamic second step would start from the first one's end state."""
+def test_reference_tutorial05_steps():
+    """A Shell_1 strip with a tip load: a Static step, then a Dynamic step
+    that starts from the first one's end state; the first step can be read
+    alone, a later one cannot."""
     path = _ref_deck("tutorial05")
     s = read_deck_file(path)
     assert len(s.shells) == 400 and len(s.beams) == 0 and s.n_nodes == 861
     assert s.solution.type == 0 and s.solution.end_time == 1.0
+    assert len(s.next_steps) == 1 and s.next_steps[0].type == 1 and s.next_steps[0].end_time == 1.4
+    assert s.next_steps[0].beta == 0.3 and s.next_steps[0].time_step == 0.005
     assert int(np.asarray(s.constraints).sum()) == 21 * 6
+    assert read_deck_file(path, step=1).next_steps == []
     with pytest.raises(DeckError, match="first solution step"):
         read_deck_file(path, step=2)
+    same_structure(read_deck(s.to_inp()), s)
+
+
+def test_zero_ic_and_step_dependent_tables():
+    s = configs.chain_sequence()
+    text = s.to_inp()
+    assert "ZeroIC" in text
+    r = read_deck(text)
+    assert [x.zero_ic for x in r.next_steps] == [0, 1, 0]
+    # a constraint released in the second step is refused
+    k = text.index("NodalConstraint")
+    bad = text[:k] + text[k:].replace("BoolTable\t1", "BoolTable\t1\t0", 1)
+    with pytest.raises(DeckError, match="change between solution steps"):
+        read_deck(bad)

@@ -1,8 +1,9 @@
 """Checkpoint / resume of a device batch (gf_batch_step, gf_batch_snapshot,
 gf_batch_restore) through the C ABI: a batch of static chains, a damped
-dynamic riser, a static and a damped vibrating Shell_1 plate is stopped
-between Newton passes, snapshotted, run to the end, restored and run to the
-end again; both ends and a run without a stop are bit-identical."""
+dynamic riser, a static and a damped vibrating Shell_1 plate and a chain
+running four solution steps in sequence is stopped between Newton passes,
+snapshotted, run to the end, restored and run to the end again; both ends
+and a run without a stop are bit-identical."""
 import numpy as np
 import pytest
 
@@ -16,6 +17,7 @@ def _mixed():
         configs.riser_chain(25, 0.4, 0.03, 1.0, 5.0, steps=30, rayleigh_alpha=0.2, rayleigh_beta=0.003),
         configs.square_plate(3, steps=10, area_update=0),
         configs.plate_dynamics(3, steps=10, rayleigh_alpha=8.0, rayleigh_beta=2e-5),
+        configs.chain_sequence(10),
     ]
 
 

@@ -1,0 +1,70 @@
+"""Solution steps in sequence on the CUDA path (gf_model_desc.next_steps):
+each step starts from the state the previous one ends in, with its own step
+control, Newmark parameters, Rayleigh matrices and initial velocities, as the
+reference's main loop runs them.  Against the reference's goldens (1e-10
+relative on positions) and the oracle (same counts)."""
+import numpy as np
+import pytest
+
+from giraffe_gb300 import configs, gpu
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(ctx, structs):
+    b = gpu.BatchSolver(ctx, structs)
+    b.reset()
+    b.run()
+    out = b.results()
+    b.close()
+    return out
+
+
+@pytest.mark.parametrize("name,make", [("ref_plate_release.npz", lambda: configs.plate_release(3)),
+                                       ("ref_chain_sequence.npz", configs.chain_sequence)])
+def test_sequences_match_reference(gpu_ctx, golden, name, make):
+    s = make()
+    g = golden(name)
+    finals, stats = _solve(gpu_ctx, [s])
+    ref = g["nodes"][-1]
+    scale = np.abs(ref[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(finals[0][:, 6:] - ref[:, 6:]).max() <= 1e-9
+    assert stats[0][0] == len(g["steps"]) and stats[0][3] == 0
+    _, so, _ = oracle.solve(s)
+    assert list(stats[0]) == list(so)
+
+
+def test_sequences_share_a_batch_with_single_steps(gpu_ctx):
+    """Multi-step and single-step structures of both element families in one
+    batch, each bit-identical to its run alone and equal to the oracle."""
+    mix = [configs.chain_sequence(), configs.riser_chain(25, 0.4, 0.03, 1.0, 5.0, steps=30),
+           configs.plate_release(3, static_steps=3, dynamic_steps=8), configs.chain_sequence(12),
+           configs.cantilever_rollup()]
+    finals, stats = _solve(gpu_ctx, mix)
+    for k, s in enumerate(mix):
+        fo, so, _ = oracle.solve(s)
+        assert list(stats[k]) == list(so), k
+        scale = np.abs(fo[:, :3]).max()
+        assert np.abs(finals[k][:, :3] - fo[:, :3]).max() <= 1e-10 * scale, k
+        alone, st1 = _solve(gpu_ctx, [s])
+        assert np.array_equal(alone[0], finals[k]), k
+
+
+def test_zero_ic_is_honoured(gpu_ctx):
+    """Dropping ZeroIC from the third step changes the motion of that step."""
+    a = configs.chain_sequence()
+    b = configs.chain_sequence()
+    b.next_steps = b.next_steps[:2]
+    c = configs.chain_sequence()
+    c.next_steps = c.next_steps[:2]
+    c.next_steps[1].zero_ic = 0
+    fa, _ = _solve(gpu_ctx, [b])
+    fc, _ = _solve(gpu_ctx, [c])
+    fo_b, _, _ = oracle.solve(b)
+    fo_c, _, _ = oracle.solve(c)
+    scale = np.abs(fo_b[:, :3]).max()
+    assert np.abs(fa[0][:, :3] - fo_b[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(fc[0][:, :3] - fo_c[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(fo_b[:, :3] - fo_c[:, :3]).max() > 1e-3
