@@ -59,6 +59,8 @@ def parse():
                     help="largest plate (free DOFs) in the mixed served leg")
     ap.add_argument("--mixed-steps", type=int, default=3,
                     help="timed solves of the mixed-precision leg (0 = skip)")
+    ap.add_argument("--shell-n", type=int, default=64,
+                    help="squares per side of the plate of the shell leg (64: the 64x64x2 benchmark plate)")
     ap.add_argument("--shell-steps", type=int, default=2,
                     help="load steps (of 20) of the 64x64x2 Shell_1 plate leg (0 = skip)")
     ap.add_argument("--dyn-steps", type=int, default=50,
@@ -283,7 +285,7 @@ def shell_leg(ctx, args, fp64_peak):
     from oracle import oracle
 
     L = ctx.L
-    s = configs.square_plate(64, steps=20)
+    s = configs.square_plate(args.shell_n, steps=20)
     s.solution.end_time = args.shell_steps / 20.0
     # the same steps with the trailing update in FP64 FMA, for comparison
     bf = gpu.BatchSolver(ctx, [s], ctx.opts(wide_update=gpu.GF_WIDE_FP64))
@@ -312,7 +314,8 @@ def shell_leg(ctx, args, fp64_peak):
         times.append(time.perf_counter() - t0)
     t_sp = statistics.median(times)
     n_sp, kl_sp = len(P), dims[1]
-    sparse = {"workload": f"first-pass K_AA of the 64x64x2 plate as host CSR: n {n_sp}, nnz {len(v)}, "
+    sparse = {"workload": f"first-pass K_AA of the {args.shell_n}x{args.shell_n}x2 plate as host CSR: n {n_sp}, "
+                          f"nnz {len(v)}, "
                           f"half-bandwidth {kl_sp}", "ms": t_sp * 1e3, "linear_solves_per_s": 1.0 / t_sp,
               "info": int(info), "lu_tflops_end_to_end": 2.0 * n_sp * kl_sp * kl_sp / t_sp / 1e12,
               "note": "host CSR in, x out; includes the RCM trial, CSR upload, scatter, factor and "
@@ -328,7 +331,8 @@ def shell_leg(ctx, args, fp64_peak):
     t0 = time.perf_counter()
     _, so, _ = oracle.solve(small, 0)
     cpu_s = time.perf_counter() - t0
-    return {"workload": f"Shell_1 plate 64x64x2, {dims[0]} free DOFs, natural numbering half-bandwidth "
+    return {"workload": f"Shell_1 plate {args.shell_n}x{args.shell_n}x2, {dims[0]} free DOFs, natural numbering "
+                        f"half-bandwidth "
                         f"{dims[1]}, first {args.shell_steps} of 20 load steps",
             "newton_solves": int(st[0][0]), "newton_passes": int(st[0][1]), "ms": ms,
             "solves_per_s": st[0][0] / (ms / 1e3), "ms_per_pass": ms / max(1, st[0][1]),
