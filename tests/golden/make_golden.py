@@ -58,6 +58,9 @@ stores what the reference computes:
 * ref_chain_sequence.npz four solution steps on a pipe chain: Static, damped
                          Dynamic after a load drop, Dynamic from rest (ZeroIC),
                          Static reloading.
+* ref_tutorial05.npz     the reference's tutorial05 deck itself (400 Shell_1,
+                         a Static then a Dynamic step), every 10th
+                         configuration; the reference needs tens of minutes.
 
 Node records hold copy_coordinates (position and accumulated Rodrigues
 vector) then the nodal Q (row-major); Gauss-point records hold Q_i
@@ -401,6 +404,32 @@ DECKS = {
 }
 
 
+REF_INPUTS = "/root/reference/inputs"
+
+
+def make_tutorial05(stride: int = 10):
+    """The reference's own Shell_1 deck, tutorial05 (a strip loaded at its tip
+    in a Static step, then released into a Dynamic step), run from its file.
+    The deck writes every step; every `stride`-th configuration and the last
+    are kept.  The stored deck is the same structure written by
+    Structure.to_inp, which reads back identically."""
+    from giraffe_gb300.deck import read_deck_file
+
+    path = os.path.join(REF_INPUTS, "tutorial05", "tutorial05.inp")
+    L = ref_lib()
+    s = read_deck_file(path)
+    with tempfile.TemporaryDirectory() as tmp:
+        assert L.giraffe_ref_load(path.encode()) == 0
+        rec = os.path.join(tmp, "t05.rec")
+        log = os.path.join(tmp, "t05.log")
+        rc = L.giraffe_ref_solve(rec.encode(), log.encode())
+        times, nodes, gq = parse_rec(rec)
+        steps = parse_log(log)
+    keep = sorted(set(range(0, len(times), stride)) | {len(times) - 1})
+    np.savez_compressed(os.path.join(HERE, "ref_tutorial05.npz"), rc=np.array(rc), times=times[keep],
+                        nodes=nodes[keep], gp_Q=gq[keep], steps=steps, deck=np.array(s.to_inp()))
+
+
 def make_elements():
     L = ref_lib()
     rng = np.random.default_rng(20261203)
@@ -425,11 +454,13 @@ def main():
     if len(sys.argv) > 1:
         if sys.argv[1] == "elements":
             make_elements()
+        elif sys.argv[1] == "ref_tutorial05.npz":
+            make_tutorial05()
         else:
             make_deck(sys.argv[1])
         return
     ref_lib()
-    for job in ["elements"] + list(DECKS):
+    for job in ["elements"] + list(DECKS) + ["ref_tutorial05.npz"]:
         subprocess.run([sys.executable, os.path.abspath(__file__), job], check=True)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -68,3 +68,23 @@ def test_zero_ic_is_honoured(gpu_ctx):
     assert np.abs(fa[0][:, :3] - fo_b[:, :3]).max() <= 1e-10 * scale
     assert np.abs(fc[0][:, :3] - fo_c[:, :3]).max() <= 1e-10 * scale
     assert np.abs(fo_b[:, :3] - fo_c[:, :3]).max() > 1e-3
+
+
+def test_reference_tutorial05(gpu_ctx, golden):
+    """The reference's own Shell_1 deck: a strip of 400 six-node triangles
+    loaded at its tip in a Static step (with bisections), then released into
+    a Dynamic step of 80 Newmark steps.  The final configuration and the
+    step counts as the reference writes them."""
+    from giraffe_gb300.deck import read_deck
+
+    g = golden("ref_tutorial05.npz")
+    s = read_deck(str(g["deck"]))
+    assert len(s.shells) == 400 and len(s.next_steps) == 1
+    finals, stats = _solve(gpu_ctx, [s])
+    steps = g["steps"]
+    assert stats[0][0] == int((steps[:, 2] == 0).sum())
+    assert stats[0][2] == int((steps[:, 2] == 1).sum()) and stats[0][3] == 0
+    ref = g["nodes"][-1]
+    scale = np.abs(ref[:, :3]).max()
+    assert np.abs(finals[0][:, :3] - ref[:, :3]).max() <= 1e-10 * scale
+    assert np.abs(finals[0][:, 6:] - ref[:, 6:]).max() <= 1e-9
