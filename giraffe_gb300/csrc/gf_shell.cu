@@ -666,10 +666,12 @@ __global__ void __launch_bounds__(64) k_shell_tangent(Batch b) {
 // 6x6 operator blockdiag(coef1 I, coef2 (|d|^2 I - d d^T) + coef3 d d^T);
 // the element sums w N^T D N and turns it to the global frame.  Every
 // iteration then adds a4 C_e to K_e and C_e v to f_e, v the nodes' current
-// velocities.  One thread per element; C_e is structure-of-arrays.
+// velocities.  One warp per element, lane r < 27 owning row r of C_e, K_e
+// and f_e (no lane reads another's row); C_e is structure-of-arrays.
 __global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= b.sh.n_shells) return;
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int r = threadIdx.x & 31;
+  if (e >= b.sh.n_shells || r >= 27) return;
   const int s = b.sh.sstruct[e];
   const StructState& st = b.state[s];
   if (!iterating_s(st)) return;
@@ -678,95 +680,80 @@ __global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
   const int64_t ns = b.sh.n_shells;
   double* C = b.sh.RD + e;
   const int* nd = b.sh.snodes + 6 * e;
+  const int n = r / 3, i = r % 3;  // row block (node 0..5 translations, 6..8 midside rotations), row in it
   if (p.ray_update || !st.ray_init) {
     const ShellConst& c = b.sh.sconst[e];
-    const m3 T = ld3(c.T3);
-    double wt[6][6], R[3][3][9];  // translation weights; local rotation blocks
+    double row[27];
 #pragma unroll
-    for (int n = 0; n < 6; ++n)
+    for (int x = 0; x < 27; ++x) row[x] = 0.0;
+    if (n < 6) {
+      // translations: coef1 times the weights on the diagonal of each 3x3
+      // node block (T^T I T = I)
+#pragma unroll 1
+      for (int q = 0; q < 6; ++q) {
+        double w = 0.0;
 #pragma unroll
-      for (int q = 0; q < 6; ++q) wt[n][q] = 0.0;
-#pragma unroll
-    for (int m = 0; m < 3; ++m)
+        for (int k = 0; k < 6; ++k) w += c.w4[k] * c.N4[k][n] * c.N4[k][q];
+        row[3 * q + i] = c.coef1 * w;
+      }
+    } else {
+      // rotations of midside node m: row i of T^T R[m][q] T for q = 0..2
+      const int m = n - 6;
+      const m3 T = ld3(c.T3);
+      double R[3][9];
 #pragma unroll
       for (int q = 0; q < 3; ++q)
 #pragma unroll
-        for (int k = 0; k < 9; ++k) R[m][q][k] = 0.0;
+        for (int x = 0; x < 9; ++x) R[q][x] = 0.0;
 #pragma unroll 1
-    for (int k = 0; k < 6; ++k) {
-      v3 al = {{0, 0, 0}};
+      for (int k = 0; k < 6; ++k) {
+        v3 al = {{0, 0, 0}};
 #pragma unroll
-      for (int m = 0; m < 3; ++m)
+        for (int mm = 0; mm < 3; ++mm)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) al[i] += b.copy[(int64_t)nd[3 + m] * 6 + 3 + i] * c.Na4[k][m];
-      al = mv(T, al);
-      const m3 Q = rodrigues(al);
-      const v3 dv = {{Q[2], Q[5], Q[8]}};
-      const double d2 = dot(dv, dv);
-      m3 D;
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          D[i * 3 + j] = (i == j ? c.coef2 * d2 : 0.0) + (c.coef3 - c.coef2) * dv[i] * dv[j];
-#pragma unroll
-      for (int m = 0; m < 3; ++m)
+          for (int j = 0; j < 3; ++j) al[j] += b.copy[(int64_t)nd[3 + mm] * 6 + 3 + j] * c.Na4[k][mm];
+        al = mv(T, al);
+        const m3 Q = rodrigues(al);
+        const v3 dv = {{Q[2], Q[5], Q[8]}};
+        const double d2 = dot(dv, dv);
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
           const double w = c.w4[k] * c.Na4[k][m] * c.Na4[k][q];
 #pragma unroll
-          for (int x = 0; x < 9; ++x) R[m][q][x] += w * D[x];
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              R[q][a * 3 + j] += w * ((a == j ? c.coef2 * d2 : 0.0) + (c.coef3 - c.coef2) * dv[a] * dv[j]);
         }
-#pragma unroll
-      for (int n = 0; n < 6; ++n)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) wt[n][q] += c.w4[k] * c.N4[k][n] * c.N4[k][q];
-    }
-    // translations: coef1 times the weights on the diagonal of each 3x3
-    // node block (T^T I T = I); rotations: T^T R T
-#pragma unroll 1
-    for (int q = 0; q < 9; ++q)
-#pragma unroll 1
-      for (int n = 0; n < 9; ++n) {
-        m3 blk;
-        if (n < 6 && q < 6) {
-#pragma unroll
-          for (int x = 0; x < 9; ++x) blk[x] = (x % 4 == 0) ? c.coef1 * wt[n][q] : 0.0;
-        } else if (n >= 6 && q >= 6) {
-          m3 r;
-#pragma unroll
-          for (int x = 0; x < 9; ++x) r[x] = R[n - 6][q - 6][x];
-          blk = tmul(T, mul(r, T));
-        } else {
-#pragma unroll
-          for (int x = 0; x < 9; ++x) blk[x] = 0.0;
-        }
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            const int64_t xi = (3 * n + i) + 27 * (3 * q + j);
-            C[xi * ns] = p.ray_alpha * blk[i * 3 + j] + p.ray_beta * C[xi * ns];
-          }
       }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        m3 Rq;
+#pragma unroll
+        for (int x = 0; x < 9; ++x) Rq[x] = R[q][x];
+        const m3 G = tmul(T, mul(Rq, T));
+#pragma unroll
+        for (int j = 0; j < 3; ++j) row[18 + 3 * q + j] = G[i * 3 + j];
+      }
+    }
+#pragma unroll 1
+    for (int x = 0; x < 27; ++x) {
+      const int64_t xi = r + 27 * x;
+      C[xi * ns] = p.ray_alpha * row[x] + p.ray_beta * C[xi * ns];
+    }
   }
   const double a4 = st.a[3];
-  double v[27];
-#pragma unroll
-  for (int a = 0; a < 18; ++a) v[a] = b.vel[(int64_t)nd[a / 3] * 6 + a % 3];
-#pragma unroll
-  for (int a = 0; a < 9; ++a) v[18 + a] = b.vel[(int64_t)nd[3 + a / 3] * 6 + 3 + a % 3];
   double* K = b.sh.Ke + (int64_t)e * 729;
-  double* F = b.sh.Fe + (int64_t)e * 27;
+  double acc = 0.0;
 #pragma unroll 1
-  for (int q = 0; q < 27; ++q) {
-    double acc = 0.0;
-#pragma unroll 1
-    for (int k = 0; k < 27; ++k) acc += C[(q + 27 * k) * ns] * v[k];
-    F[q] += acc;
+  for (int x = 0; x < 27; ++x) {
+    const int node = x < 18 ? nd[x / 3] : nd[3 + (x - 18) / 3];
+    const int k = x < 18 ? x % 3 : 3 + (x - 18) % 3;
+    const double cx = C[(int64_t)(r + 27 * x) * ns];
+    acc += cx * b.vel[(int64_t)node * 6 + k];
+    K[r + 27 * x] += a4 * cx;
   }
-#pragma unroll 1
-  for (int x = 0; x < 729; ++x) K[x] += a4 * C[x * ns];
+  b.sh.Fe[(int64_t)e * 27 + r] += acc;
 }
 
 // Standalone elements (gf_shell_elements): n elements with their own
@@ -1441,7 +1428,7 @@ __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
 void launch_shell_mount(const Batch& b, cudaStream_t st) {
   if (b.sh.n_shells == 0) return;
   k_shell_tangent<<<(b.sh.n_shells + 63) / 64, 64, 0, st>>>(b);
-  if (b.sh.any_rayleigh) k_shell_rayleigh<<<(b.sh.n_shells + 127) / 128, 128, 0, st>>>(b);
+  if (b.sh.any_rayleigh) k_shell_rayleigh<<<(b.sh.n_shells + 3) / 4, 128, 0, st>>>(b);
   for (int c = 0; c < b.sh.n_colors; ++c) {
     int cnt = b.sh.color_off[c + 1] - b.sh.color_off[c];
     if (cnt <= 0) continue;
