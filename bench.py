@@ -190,7 +190,27 @@ def cpu_baseline(structs, sample_n, rank):
     solves = int(stats[:, 0].sum())
     return {"value": solves / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(sample)} of the {len(structs)} chains (every size stratum), "
-                      f"{solves} Newton solves in {dt:.2f} s on {threads} host threads"}, sample
+                      f"{solves} Newton solves in {dt:.2f} s on {threads} host threads"}, (idx, finals, stats)
+
+
+def oracle_parity(structs, idx, finals, stats, o_finals, o_stats):
+    """The headline's own results against the oracle's, chain by chain, on
+    the chains the CPU baseline solved: relative error of the converged
+    nodal translations (2-norm), largest deviation of the nodal rotation
+    tensors, and whether converged steps, Newton iterations and bisections
+    are the same."""
+    rel, dq, same = [], 0.0, 0
+    for k, i in enumerate(idx):
+        s = structs[i]
+        u, uo = finals[i][:, :3] - s.nodes, o_finals[k][:, :3] - s.nodes
+        rel.append(float(np.linalg.norm(u - uo) / np.linalg.norm(uo)))
+        dq = max(dq, float(np.abs(finals[i][:, 6:] - o_finals[k][:, 6:]).max()))
+        same += int(np.array_equal(np.asarray(stats[i]), np.asarray(o_stats[k])))
+    worst = int(np.argmax(rel))
+    return {"chains": len(idx), "max_rel_err_displacement": max(rel), "median_rel_err_displacement":
+            float(np.median(rel)), "worst_chain_elements": len(structs[idx[worst]].beams),
+            "max_abs_err_rotation": dq, "counts_match": same,
+            "tolerance": 1e-10, "within_tolerance": int(sum(r <= 1e-10 for r in rel))}
 
 
 def run_reference(args, rank, world):
@@ -538,8 +558,10 @@ def run_ours(args, rank, world):
         serving = served_leg(ctx, args, rank)
     serving_mixed = served_mixed_leg(ctx, args, rank) if args.serve_mixed_requests > 0 else None
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, _ = cpu_baseline(structs, args.cpu_sample, rank)
+        cpu, (idx, o_finals, o_stats) = cpu_baseline(structs, args.cpu_sample, rank)
+        parity = oracle_parity(structs, idx, f64_finals, stats, o_finals, o_stats)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -569,7 +591,8 @@ def run_ours(args, rank, world):
                 "dynamics": dyn,
                 "serving": serving,
                 "serving_mixed": serving_mixed,
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu,
+                "parity_vs_oracle": parity}
         print(json.dumps(line), flush=True)
     ctx.close()
 

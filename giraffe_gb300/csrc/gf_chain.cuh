@@ -16,8 +16,10 @@
 //   4. back substitution level by level, then the midside nodes.
 // The critical path is O(log m) small dense solves instead of the O(n)
 // column recurrence of a banded LU, which on a GPU with slow FP64 latency
-// (~64 cycles per dependent FP64 operation) dominates long chains.  The same
-// K_AA is read from the batch's band storage.  Equations follow from block
+// (~64 cycles per dependent FP64 operation) dominates long chains.  The
+// solver never reads an assembled K_AA: it takes each element's tangent K_e
+// from the element scratch (plus the nodal load stiffness), which is the
+// same K_AA term by term.  Equations follow from block
 // Gaussian elimination on the assembled matrix; the reference solves the
 // same K_AA with PARDISO (reference src/SparseMatrix.cpp:74-166).
 #pragma once

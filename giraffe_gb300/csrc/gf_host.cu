@@ -989,7 +989,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       // slices of one panel per wide structure for the tensor-core update
       sd.oz_rows = (max_wkl + 63) / 64 * 64;
       const size_t nw = wide_structs.size(), R = (size_t)sd.oz_rows;
-      if (!balloc(B, &sd.oz_slices, nw * 2 * 8 * R * GF_WB_NB) || !balloc(B, &sd.oz_exp, nw * 2 * R))
+      if (!balloc(B, &sd.oz_slices, nw * 2 * 8 * R * GF_WB_NB) || !balloc(B, &sd.oz_exp, nw * 2 * R) ||
+          !zeroed(B, &sd.oz_kmax, nw * 2 * 2 * GF_WB_NB))
         return GF_ERR_CUDA;
     }
     if (!B->count_only) {
@@ -1109,12 +1110,22 @@ void gf_destroy(gf_ctx* ctx) {
 
 const char* gf_last_error(const gf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
+int gf_ctx_set_opts(gf_ctx* ctx, const gf_solve_opts* opts) {
+  if (!ctx || !opts || (opts->wide_update != GF_WIDE_FP64 && opts->wide_update != GF_WIDE_TENSOR)) {
+    set_err(ctx, "gf_ctx_set_opts: invalid arguments");
+    return GF_ERR_ARG;
+  }
+  ctx->wide_update = opts->wide_update;
+  return GF_OK;
+}
+
 void gf_default_opts(gf_solve_opts* o) {
   o->precision = GF_PREC_FP64;
   o->max_refine = 6;
   o->poll_every = 8;
   o->use_graph = 1;
   o->wide_update = GF_WIDE_TENSOR;
+  o->max_passes = 0;
 }
 
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts) {
@@ -1195,7 +1206,7 @@ int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
   cudaStream_t st = B->stream;
   const Batch& b = B->b;
   long long passes = 0;
-  const long long cap = 4000000;
+  const long long cap = B->opts.max_passes > 0 ? B->opts.max_passes : 4000000;
   for (;;) {
     for (int k = 0; k < B->opts.poll_every; ++k) {
       if (B->graph && !prof) {
@@ -1209,7 +1220,7 @@ int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
     CK(cudaMemcpyAsync(B->h_running, b.running, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (*B->h_running == 0) break;
-    if (passes > cap) {
+    if (passes >= cap) {
       set_err(ctx, "gf_batch_run: %lld Newton passes without completion", passes);
       return GF_ERR_TIMEOUT;
     }
@@ -1285,22 +1296,52 @@ std::vector<std::pair<void*, size_t>> state_parts(const gf_batch* B) {
   if (b.sh.any_rayleigh) v.push_back({b.sh.RD, 8 * 729 * ns});
   return v;
 }
+
+// Header at the start of a snapshot: what the batch's layout depends on,
+// so a snapshot is restored only into a batch laid out the same way.
+struct SnapshotHeader {
+  unsigned long long magic;  // kSnapshotMagic
+  unsigned version;
+  int n_struct;
+  long long n_nodes, n_elem, n_shells;
+  int rayleigh_beam, rayleigh_shell;
+  unsigned long long total_bytes;  // header included
+};
+constexpr unsigned long long kSnapshotMagic = 0x50414e5346524947ull;  // "GIRFSNAP"
+constexpr unsigned kSnapshotVersion = 1;
+
+SnapshotHeader snapshot_header(const gf_batch* B) {
+  const Batch& b = B->b;
+  SnapshotHeader h{};
+  h.magic = kSnapshotMagic;
+  h.version = kSnapshotVersion;
+  h.n_struct = b.n_struct;
+  h.n_nodes = b.n_nodes;
+  h.n_elem = b.n_elem;
+  h.n_shells = b.sh.n_shells;
+  h.rayleigh_beam = b.any_rayleigh ? 1 : 0;
+  h.rayleigh_shell = b.sh.any_rayleigh ? 1 : 0;
+  size_t n = sizeof(SnapshotHeader);
+  for (const auto& p : state_parts(B)) n += p.second;
+  h.total_bytes = n;
+  return h;
+}
 }  // namespace
 
 extern "C" {
 
 int gf_batch_snapshot_bytes(const gf_batch* B, size_t* bytes) {
   if (!B || !bytes) return GF_ERR_ARG;
-  size_t n = 0;
-  for (const auto& p : state_parts(B)) n += p.second;
-  *bytes = n;
+  *bytes = (size_t)snapshot_header(B).total_bytes;
   return GF_OK;
 }
 
 int gf_batch_snapshot(gf_batch* B, void* host) {
   if (!B || !host) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
-  char* h = static_cast<char*>(host);
+  const SnapshotHeader hd = snapshot_header(B);
+  std::memcpy(host, &hd, sizeof(hd));
+  char* h = static_cast<char*>(host) + sizeof(hd);
   for (const auto& p : state_parts(B)) {
     if (p.second) CK(cudaMemcpyAsync(h, p.first, p.second, cudaMemcpyDeviceToHost, B->stream));
     h += p.second;
@@ -1312,7 +1353,23 @@ int gf_batch_snapshot(gf_batch* B, void* host) {
 int gf_batch_restore(gf_batch* B, const void* host) {
   if (!B || !host) return GF_ERR_ARG;
   gf_ctx* ctx = B->ctx;
-  const char* h = static_cast<const char*>(host);
+  SnapshotHeader got;
+  std::memcpy(&got, host, sizeof(got));
+  const SnapshotHeader want = snapshot_header(B);
+  if (got.magic != kSnapshotMagic || got.version != kSnapshotVersion) {
+    set_err(ctx, "gf_batch_restore: not a batch snapshot (bad magic or version)");
+    return GF_ERR_ARG;
+  }
+  if (got.n_struct != want.n_struct || got.n_nodes != want.n_nodes || got.n_elem != want.n_elem ||
+      got.n_shells != want.n_shells || got.rayleigh_beam != want.rayleigh_beam ||
+      got.rayleigh_shell != want.rayleigh_shell || got.total_bytes != want.total_bytes) {
+    set_err(ctx, "gf_batch_restore: snapshot of a different batch (structures %d/%d, nodes %lld/%lld, "
+                 "elements %lld/%lld, shells %lld/%lld, bytes %llu/%llu)",
+            got.n_struct, want.n_struct, got.n_nodes, want.n_nodes, got.n_elem, want.n_elem, got.n_shells,
+            want.n_shells, got.total_bytes, want.total_bytes);
+    return GF_ERR_ARG;
+  }
+  const char* h = static_cast<const char*>(host) + sizeof(got);
   for (const auto& p : state_parts(B)) {
     if (p.second) CK(cudaMemcpyAsync(p.first, h, p.second, cudaMemcpyHostToDevice, B->stream));
     h += p.second;
@@ -1906,7 +1963,10 @@ constexpr size_t NA_INFO = NA_U + round256((size_t)GF_NOALLOC_MAX_N * GF_UW);
 constexpr size_t NA_STATE = NA_INFO + round256((sizeof(StructInfo) + 7) / 8);
 constexpr size_t NA_TOTAL = NA_STATE + round256((sizeof(StructState) + 7) / 8);
 constexpr int NA_MAX_DEVICES = 64;
-void* g_noalloc_base[NA_MAX_DEVICES] = {};
+// Per-device address of the scratch array, looked up on the first call on
+// that device.  Two threads making their first call at once both store the
+// same pointer; the atomics make that well defined.
+std::atomic<void*> g_noalloc_base[NA_MAX_DEVICES] = {};
 
 struct DeviceGuard {
   int prev = -1;
@@ -1954,7 +2014,7 @@ extern "C" int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const d
     CK(cudaSetDevice(ctx->device));
     guard.switched = true;
   }
-  double* base = static_cast<double*>(g_noalloc_base[ctx->device]);
+  double* base = static_cast<double*>(g_noalloc_base[ctx->device].load(std::memory_order_acquire));
   if (!base) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -1963,7 +2023,7 @@ extern "C" int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const d
               cudaGetErrorString(e));
       return GF_ERR_CUDA;
     }
-    g_noalloc_base[ctx->device] = p;
+    g_noalloc_base[ctx->device].store(p, std::memory_order_release);
     base = static_cast<double*>(p);
   }
   double* dband = base;

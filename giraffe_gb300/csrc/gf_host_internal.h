@@ -18,6 +18,9 @@ struct gf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
+  // options of the standalone solves (gf_band_solve, gf_sparse_solve):
+  // wide_update picks their wide-band trailing update
+  int wide_update = GF_WIDE_TENSOR;
 };
 
 // First-fit sub-allocator over one allocation (the served path's device

@@ -69,7 +69,7 @@ struct Wave {
 
 // Newton passes a wave may run before its unfinished structures are
 // reported as timed out (the batch path's cap).
-constexpr long long kMaxWavePasses = 4000000;
+constexpr long long kMaxWavePasses = 4000000;  // default of max_wave_passes
 // Slack added to each wave's size: the batch's own 256-byte roundings.
 constexpr size_t kWaveSlack = 1 << 16;
 // Pinned host staging shared by the uploads of new waves and the result
@@ -285,7 +285,7 @@ int read_chunk(gf_server* S, Wave& w, bool* progressed) {
   w.head ^= 1;
   w.inflight--;
   if (running == 0) w.finishing = true;
-  if (w.passes > kMaxWavePasses) {
+  if (w.passes >= (S->o.max_wave_passes > 0 ? (long long)S->o.max_wave_passes : kMaxWavePasses)) {
     w.finishing = true;
     for (int s = 0; s < (int)w.reqs.size(); ++s)
       if (!w.reported[s]) report(S, w, s, &st[s], GF_ERR_TIMEOUT);
@@ -491,7 +491,7 @@ void gf_server_default_opts(gf_server_opts* o) {
   o->max_waves = 4;
   o->max_wave_structs = 128;
   o->passes_per_chunk = 4;
-  o->pad = 0;
+  o->max_wave_passes = 0;
 }
 
 gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts) {

@@ -892,6 +892,12 @@ constexpr int NB = GF_WB_NB;
 __device__ __forceinline__ int wb_panel(const Batch& b, int p) { return p >= 0 ? p : *b.sh.panel + (-1 - p); }
 }  // namespace
 
+// Column / row maxima of panel p's L21 and U12 for wide structure slot z
+// (the tensor-core update balances k with them): [operand][k].
+__device__ __forceinline__ unsigned long long* wb_kmax(const Batch& b, int z, int p) {
+  return b.sh.oz_kmax + ((int64_t)z * 2 + (p & 1)) * 2 * NB;
+}
+
 // zero the wide band of iterating structures
 __global__ void k_wb_zero(Batch b) {
   int s = b.sh.wide_structs[blockIdx.y];
@@ -917,6 +923,9 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
   __shared__ int fail;
   const int tid = threadIdx.x;
   if (tid == 0) fail = 0;
+  // this panel's L21 / U12 maxima start at zero (the buffer of its parity
+  // was last read by the slicing of panel p - 2, which precedes this kernel)
+  if (b.sh.wide_tc && tid < 2 * NB) wb_kmax(b, blockIdx.x, p)[tid] = 0ull;
   for (int x = tid; x < NB * NB; x += blockDim.x) {
     int i = x % NB, j = x / NB;
     double v = 0.0;
@@ -1009,6 +1018,19 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
     if (lower) w.at(g, j0 + k) = X[r][k];
     else w.at(j0 + k, g) = X[r][k];
   }
+  if (b.sh.wide_tc && tid < nb) {
+    // largest magnitude of column k of this block's L21 rows (row k of its
+    // U12 columns), as FP64 bits, which order like the magnitudes; the
+    // maximum over the CTAs is exact and independent of their order
+    const int k = tid;
+    unsigned long long mx = 0;
+    for (int q = 0; q < 16; ++q) {
+      const int gq = j0 + nb + blk * 16 + q;
+      if (gq < j0 + nb + m && gq - (j0 + k) <= w.kl)
+        mx = max(mx, (unsigned long long)__double_as_longlong(X[q][k]) & 0x7FFFFFFFFFFFFFFFull);
+    }
+    if (mx) atomicMax(wb_kmax(b, blockIdx.y, p) + (lower ? 0 : NB) + k, mx);
+  }
 }
 
 // A22 -= L21 U12 over the (m x m) trailing window of panel p, 32x32 tiles
@@ -1064,7 +1086,10 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 
 // ---- the same trailing update on the tensor cores (Ozaki scheme) ----
 // A22 -= L21 U12 for one 64x64 output tile with K = NB = 64, the FP64
-// products emulated by bf16 tensor-core products of exact slices.  Each
+// products emulated by bf16 tensor-core products of exact slices.  First
+// every k of the panel is balanced: column k of L21 times 2^-f_k and row k
+// of U12 times 2^f_k (exact, the products unchanged), f_k half the exponent
+// difference of their largest entries.  Then each
 // row of L21 (column of U12) gets the power of two 2^e just above its
 // largest magnitude; an entry x becomes the 56-bit integer
 // X = floor(|x| 2^(56 - e)), read off the FP64 bits with integer
@@ -1076,9 +1101,11 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 // accumulators of mma.sync hold exactly.  The diagonals are combined
 // exactly as two 64-bit integers (Horner in powers of 2^7: d = 0..4 and
 // d = 5..7), joined by one FMA and scaled by the row and column powers of
-// two.  What
-// is left out (pairs with q + t > 7, the remainders r) weighs at most about
-// 2^-55 of sum_k |L| |U|, the FP64 rounding of the product itself.  All
+// two.  What is left out (pairs with q + t > 7, the remainders r) is
+// below about 2^-52 K max_k |L~_ik| max_k |U~_kj| for the balanced L~, U~:
+// the FP64 rounding of the product when the terms of a row and a column
+// are of like size, larger when a row holds entries far apart in
+// magnitude that the balancing cannot bring together.  All
 // slicing is integer work, so the FP64 pipe, the scarce one on this part,
 // only sees a handful of operations per output entry.
 constexpr int OZ_S = 8;    // slices per operand
@@ -1172,12 +1199,27 @@ __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
   extern __shared__ __align__(16) unsigned char oz_raw[];
   double* F = reinterpret_cast<double*>(oz_raw);  // [row or column][k], stride NB + 1
   int* e = reinterpret_cast<int*>(F + OZ_T * (NB + 1));
+  __shared__ double bal[NB];  // 2^-f_k for L21 columns, 2^f_k for U12 rows
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = j0 + nb;
+  if (tid < NB) {
+    // balance k: column k of L21 scaled by 2^-f_k and row k of U12 by 2^f_k
+    // leaves every product L_ik U_kj as it is (powers of two, exact) and
+    // brings the two maxima within a factor 2 of each other, so the
+    // per-row (per-column) slicing exponents below do not depend on how
+    // the DOFs of the panel are scaled
+    const unsigned long long* km = wb_kmax(b, blockIdx.z, p);
+    const unsigned long long ml = km[tid], mu = km[NB + tid];
+    int f = 0;
+    if (ml && mu) f = ((int)(ml >> 52) - (int)(mu >> 52)) >> 1;  // floor of half the exponent difference
+    f = max(-1000, min(1000, f));
+    bal[tid] = ldexp(1.0, lower ? -f : f);
+  }
+  __syncthreads();
   for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
     const int i = x % OZ_T, k = x / OZ_T, gk = j0 + k, g = base + r0 + i;
     const bool live = k < nb && r0 + i < m && g - gk <= w.kl;
-    F[i * (NB + 1) + k] = live ? (lower ? w.at(g, gk) : w.at(gk, g)) : 0.0;
+    F[i * (NB + 1) + k] = live ? (lower ? w.at(g, gk) : w.at(gk, g)) * bal[k] : 0.0;
   }
   __syncthreads();
   for (int q = 0; q < OZ_T / 8; ++q) {

@@ -113,8 +113,12 @@ struct WideBatch {
     const int R = (w + 63) / 64 * 64;
     __nv_bfloat16* sl = nullptr;
     int* se = nullptr;
+    unsigned long long* km = nullptr;
     if (!mem.get(&dinf, 1) || !mem.get(&dst, 1) || !mem.get(&dws, 1) || !hl.create() ||
-        !mem.get(&sl, (size_t)2 * 8 * R * GF_WB_NB) || !mem.get(&se, (size_t)2 * R))
+        !mem.get(&sl, (size_t)2 * 8 * R * GF_WB_NB) || !mem.get(&se, (size_t)2 * R) ||
+        !mem.get(&km, (size_t)2 * 2 * GF_WB_NB))
+      return false;
+    if (cudaMemsetAsync(km, 0, sizeof(unsigned long long) * 2 * 2 * GF_WB_NB, ctx->stream) != cudaSuccess)
       return false;
     cudaStream_t s = ctx->stream;
     if (cudaMemcpyAsync(dinf, &inf, sizeof(inf), cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -133,10 +137,11 @@ struct WideBatch {
     sd.max_panels = inf.n_panels;
     sd.max_kl = w;
     sd.wband = wband;
-    sd.wide_tc = 1;  // the trailing update on the tensor cores, as gf_default_opts
+    sd.wide_tc = ctx->wide_update == GF_WIDE_TENSOR;  // the context's choice (tensor cores by default)
     sd.oz_rows = R;
     sd.oz_slices = sl;
     sd.oz_exp = se;
+    sd.oz_kmax = km;
     for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
     for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
     return true;

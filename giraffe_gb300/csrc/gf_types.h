@@ -256,6 +256,11 @@ struct ShellData {
   int oz_rows;         // max_kl rounded up to 64
   __nv_bfloat16* oz_slices;
   int* oz_exp;
+  // per wide structure slot, [2 panel parities][2 operands][64]: the
+  // magnitude bits of the largest entry of each column k of a panel's L21
+  // and of each row k of its U12 (zeroed by the panel's diagonal LU, raised
+  // by its trsm), from which the slicing balances k by a power of two
+  unsigned long long* oz_kmax;
   // host handles of the wide-band lookahead: two helper streams and the
   // events that fork from and join into the pass's stream; aux[2] roots the
   // captured panel-loop bodies

@@ -26,12 +26,12 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_sparse_solve", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
            "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr",
-           "gf_shell_inertia_elements"]
+           "gf_shell_inertia_elements", "gf_ctx_set_opts"]
 
 
 class gf_solve_opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_refine", C.c_int), ("poll_every", C.c_int),
-                ("use_graph", C.c_int), ("wide_update", C.c_int)]
+                ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int)]
 
 
 class gf_stats(C.Structure):
@@ -42,7 +42,7 @@ class gf_stats(C.Structure):
 
 class gf_server_opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_waves", C.c_int), ("max_wave_structs", C.c_int),
-                ("passes_per_chunk", C.c_int), ("pad", C.c_int)]
+                ("passes_per_chunk", C.c_int), ("max_wave_passes", C.c_int)]
 
 
 class gf_server_result(C.Structure):
@@ -72,6 +72,7 @@ def lib():
         L.gf_last_error.restype = C.c_char_p
         L.gf_last_error.argtypes = [vp]
         L.gf_default_opts.argtypes = [C.POINTER(gf_solve_opts)]
+        L.gf_ctx_set_opts.argtypes = [vp, C.POINTER(gf_solve_opts)]
         L.gf_batch_create.restype = vp
         L.gf_batch_create.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts)]
         L.gf_batch_destroy.argtypes = [vp]
@@ -154,10 +155,13 @@ class Context:
         if rc != 0:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
-    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=6, wide_update=None):
+    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=None, wide_update=None,
+             max_passes=0):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
-        o.precision, o.use_graph, o.poll_every, o.max_refine = precision, int(use_graph), poll_every, max_refine
+        o.precision, o.use_graph, o.poll_every, o.max_passes = precision, int(use_graph), poll_every, max_passes
+        if max_refine is not None:
+            o.max_refine = max_refine
         if wide_update is not None:
             o.wide_update = wide_update
         return o
@@ -235,6 +239,12 @@ class Context:
         self.check(self.L.gf_sparse_solve(self.h, n, rp.ctypes.data_as(ip), ci.ctypes.data_as(ip), _dp(v), _dp(x),
                                           C.byref(info)), "gf_sparse_solve")
         return x, info.value
+
+    def set_standalone_opts(self, wide_update=GF_WIDE_TENSOR):
+        """gf_ctx_set_opts: the wide-band trailing update of this context's
+        standalone solves (band_solve, sparse_solve)."""
+        o = self.opts(wide_update=wide_update)
+        self.check(self.L.gf_ctx_set_opts(self.h, C.byref(o)), "gf_ctx_set_opts")
 
     def band_solve_noalloc(self, ab, kl, ku, b):
         """gf_band_solve_noalloc: band_solve through the static device scratch."""

@@ -1,6 +1,7 @@
 /*
  * giraffe_gpu.h — C ABI of the GB300 implementation of GIRAFFE's implicit
- * Beam_1 finite-element step.
+ * nonlinear finite-element step for Beam_1 and Shell_1 structures (Static and
+ * Dynamic solution steps).
  *
  * Every function is extern "C", takes plain pointers and sizes, returns an
  * int status (0 = success) unless stated otherwise, and records a message
@@ -65,9 +66,18 @@ typedef struct gf_solve_opts {
   int poll_every;  /* Newton passes between host checks for completion */
   int use_graph;   /* capture one Newton pass as a CUDA graph */
   int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
-                      default: FP64 products from exact bf16 slices on the
-                      tensor cores, Ozaki scheme, error below the FP64
-                      rounding of the product) or GF_WIDE_FP64 (FP64 FMA) */
+                      default: FP64 products emulated from exact bf16 slices
+                      on the tensor cores, Ozaki scheme) or GF_WIDE_FP64
+                      (FP64 FMA).  The emulated product of row i of L21 and
+                      column j of U12 (K = 64 terms) errs by at most about
+                      2^-52 K max_k |L_ik 2^-f_k| max_k |2^f_k U_kj|, where
+                      2^f_k is a power-of-two balancing of the panel's column
+                      k of L21 against row k of U12 (chosen per panel); for
+                      rows whose terms differ greatly in magnitude that can
+                      exceed the FP64 rounding of the product sum */
+  int max_passes;  /* host cap on the Newton passes of one gf_batch_run;
+                      beyond it the run stops with GF_ERR_TIMEOUT (0: the
+                      default of 4,000,000) */
 } gf_solve_opts;
 enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1 };
 
@@ -87,12 +97,18 @@ gf_ctx* gf_create(int device);
 void gf_destroy(gf_ctx* ctx);
 const char* gf_last_error(const gf_ctx* ctx);
 void gf_default_opts(gf_solve_opts* opts);
+/* Options of the context's standalone solves (gf_band_solve and
+ * gf_sparse_solve, which have no options argument, as bandsystem and
+ * sparsesystem have none): their wide-band trailing update follows
+ * opts->wide_update (GF_WIDE_TENSOR until set).  The batch entry points take
+ * their own options. */
+int gf_ctx_set_opts(gf_ctx* ctx, const gf_solve_opts* opts);
 
-/* Uploads n structures into one device batch: each a Static or Dynamic
- * step of Beam_1 elements, or a Static step of Shell_1 elements with
- * follower pressures, with nodal loads, constraints and prescribed
- * displacements.  Shell_1 structures are solved by the wide-band LU on
- * their reverse Cuthill-McKee numbering. */
+/* Uploads n structures into one device batch: each a sequence of Static and
+ * Dynamic solution steps of Beam_1 elements or of Shell_1 elements (with
+ * follower pressures), with nodal loads, constraints and prescribed
+ * displacements.  Shell_1 structures are solved by the wide-band LU on the
+ * narrower of the reference's numbering and reverse Cuthill-McKee. */
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts);
 void gf_batch_destroy(gf_batch* batch);
 /* Restores the initial configuration of every structure (device side). */
@@ -108,7 +124,11 @@ int gf_batch_step(gf_batch* batch, int max_passes, int* running);
  * SaveConfiguration / RestoreConfiguration, src/Solution.cpp:426-575, here
  * with the step machine and the Gauss-point histories, so a restore resumes
  * exactly): gf_batch_snapshot copies the batch's device state into `host`
- * (gf_batch_snapshot_bytes long), gf_batch_restore puts it back. */
+ * (gf_batch_snapshot_bytes long, a header first: structure, node, element
+ * and shell counts, damping flags, total size), gf_batch_restore puts it
+ * back.  A snapshot whose header does not match the batch (taken from a
+ * batch of other structures) is refused with GF_ERR_ARG and nothing is
+ * written. */
 int gf_batch_snapshot_bytes(const gf_batch* batch, size_t* bytes);
 int gf_batch_snapshot(gf_batch* batch, void* host);
 int gf_batch_restore(gf_batch* batch, const void* host);
@@ -257,7 +277,9 @@ typedef struct gf_server_opts {
   int max_waves;         /* batches in flight at once (each its own stream) */
   int max_wave_structs;  /* structures per batch */
   int passes_per_chunk;  /* Newton passes enqueued between two state reads */
-  int pad;
+  int max_wave_passes;   /* Newton passes after which a wave's unfinished
+                            structures are reported with GF_ERR_TIMEOUT
+                            (0: the default of 4,000,000) */
 } gf_server_opts;
 
 typedef struct gf_server_result {
@@ -295,18 +317,19 @@ int gf_server_submit(gf_server* srv, const gf_model_desc* model, double* final_n
 int gf_server_poll(gf_server* srv, gf_server_result* results, int max_results, int* n_results);
 int gf_server_get_status(const gf_server* srv, gf_server_status* status);
 
-/* No counterpart in the reference.  The same solve as gf_band_solve, same
- * arguments and results, for callers that must not allocate device memory
- * per call: a host loop that runs under another allocator's budget, or one
- * that cannot afford cudaMalloc/cudaFree, which synchronise the whole device.
- * Work arrays live in one static device array per device sized for
- * GF_NOALLOC_MAX_N unknowns (about 7 MB); no cudaMalloc, cudaFree or other
- * allocating routine is called.  n > GF_NOALLOC_MAX_N returns GF_ERR_ARG
- * (use gf_band_solve).  The first call on each device looks up the array's
+/* No counterpart in the reference.  The same solve as gf_band_solve for
+ * narrow bands (kl, ku <= GF_KB = 17, the bands of Beam_1 chains and
+ * frames), same arguments and results, for callers that must not allocate
+ * device memory per call: a host loop that runs under another allocator's
+ * budget, or one that cannot afford cudaMalloc/cudaFree, which synchronise
+ * the whole device.  Work arrays live in one static device array per device
+ * sized for GF_NOALLOC_MAX_N unknowns (about 7 MB); no cudaMalloc, cudaFree
+ * or other allocating routine is called.  n > GF_NOALLOC_MAX_N, kl > 17 or
+ * ku > 17 return GF_ERR_ARG (use gf_band_solve).  The first call on each device looks up the array's
  * address (cudaGetSymbolAddress); make that first call before any stream
  * capture.  Every context on a device shares the array: overlapping calls on
  * one device, from two threads or two contexts, race. */
-enum { GF_NOALLOC_MAX_N = 16384 };
+enum { GF_NOALLOC_MAX_N = 16384, GF_NOALLOC_MAX_KB = 17 };
 int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
 
 #ifdef __cplusplus

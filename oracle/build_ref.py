@@ -1,7 +1,7 @@
 """Builds oracle/_ref/libgiraffe_ref.so from the reference's own sources.
 
 TEST INFRASTRUCTURE.  The reference (C++14 written for MSVC + oneMKL) is
-compiled in place from /root/reference/src — nothing is copied — with the
+compiled in place from the reference tree's src/ — nothing is copied — with the
 headers in oracle/ref_shim/ (rvalue-binding overloads, BLAS/LAPACK
 declarations, a CSR stand-in for Eigen's sparse header) and linked with
 oracle/ref_blas.c, oracle/ref_support.cpp and oracle/ref_driver.cpp.  Symbols
@@ -12,7 +12,9 @@ generated stubs that abort if ever called.
 The library is x86-64 only and is built only where the reference tree is
 present; it never travels to or runs on the GPU host.  Usage:
 
-    python oracle/build_ref.py [--reference /root/reference] [--jobs N]
+    python oracle/build_ref.py [--reference <reference tree>] [--jobs N]
+
+The tree defaults to the environment variable GIRAFFE_REFERENCE.
 """
 import argparse
 import os
@@ -84,7 +86,7 @@ def stub_source(undefined):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("GIRAFFE_REFERENCE", "/root/reference"))
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
     ref_src = os.path.join(a.reference, "src")

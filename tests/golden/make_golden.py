@@ -58,6 +58,10 @@ stores what the reference computes:
 * ref_chain_sequence.npz four solution steps on a pipe chain: Static, damped
                          Dynamic after a load drop, Dynamic from rest (ZeroIC),
                          Static reloading.
+* ref_plate24.npz        a clamped 24x24x2 Shell_1 plate (11,667 free DOFs,
+                         half-bandwidth 506) under follower pressure ramped to
+                         1e5 Pa over 20 steps: the Newton solve counts, every
+                         5th configuration and the last (nodes only).
 * ref_tutorial05.npz     the reference's tutorial05 deck itself (400 Shell_1,
                          a Static then a Dynamic step), every 10th
                          configuration; the reference needs tens of minutes.
@@ -404,7 +408,7 @@ DECKS = {
 }
 
 
-REF_INPUTS = "/root/reference/inputs"
+REF_INPUTS = os.path.join(os.environ.get("GIRAFFE_REFERENCE", "/root/reference"), "inputs")
 
 
 def make_tutorial05(stride: int = 10):
@@ -428,6 +432,18 @@ def make_tutorial05(stride: int = 10):
     keep = sorted(set(range(0, len(times), stride)) | {len(times) - 1})
     np.savez_compressed(os.path.join(HERE, "ref_tutorial05.npz"), rc=np.array(rc), times=times[keep],
                         nodes=nodes[keep], gp_Q=gq[keep], steps=steps, deck=np.array(s.to_inp()))
+
+
+def make_plate24(stride: int = 5):
+    """The benchmark's plate family at a size whose band (half-bandwidth
+    506) spans many 64-wide tiles of the wide-band LU: every `stride`-th
+    configuration and the last, without the Gauss-point records."""
+    L = ref_lib()
+    with tempfile.TemporaryDirectory() as tmp:
+        r = run_deck(L, configs.square_plate(24, steps=20), "plate24", tmp)
+    keep = sorted(set(range(0, len(r["times"]), stride)) | {len(r["times"]) - 1})
+    np.savez_compressed(os.path.join(HERE, "ref_plate24.npz"), rc=r["rc"], times=r["times"][keep],
+                        nodes=r["nodes"][keep], steps=r["steps"], deck=r["deck"])
 
 
 def make_elements():
@@ -456,11 +472,13 @@ def main():
             make_elements()
         elif sys.argv[1] == "ref_tutorial05.npz":
             make_tutorial05()
+        elif sys.argv[1] == "ref_plate24.npz":
+            make_plate24()
         else:
             make_deck(sys.argv[1])
         return
     ref_lib()
-    for job in ["elements"] + list(DECKS) + ["ref_tutorial05.npz"]:
+    for job in ["elements"] + list(DECKS) + ["ref_tutorial05.npz", "ref_plate24.npz"]:
         subprocess.run([sys.executable, os.path.abspath(__file__), job], check=True)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -10,7 +10,7 @@ from giraffe_gb300 import configs
 from giraffe_gb300.deck import DeckError, read_deck, read_deck_file
 from giraffe_gb300.model import NodalLoad
 
-REF_INPUTS = "/root/reference/inputs"
+REF_INPUTS = os.path.join(os.environ.get("GIRAFFE_REFERENCE", "/root/reference"), "inputs")
 
 
 def same_structure(a, b):

@@ -57,3 +57,31 @@ def test_step_counts_down_to_zero(gpu_ctx):
     b.close()
     assert seen[0] > 0 and seen[-1] == 0
     assert all(x >= y for x, y in zip(seen, seen[1:]))
+
+
+def test_restore_refuses_a_snapshot_of_another_batch(gpu_ctx):
+    """A snapshot carries a header (counts, damping flags, size): restoring it
+    into a batch of other structures, or restoring bytes that are not a
+    snapshot, fails with GF_ERR_ARG and leaves the batch as it was."""
+    a = gpu.BatchSolver(gpu_ctx, configs.batched_static(3, seed=1, n_min=20, n_max=60))
+    other = gpu.BatchSolver(gpu_ctx, configs.batched_static(4, seed=2, n_min=20, n_max=60))
+    a.reset()
+    a.step(5)
+    snap = a.snapshot()
+    other.reset()
+    other.run()
+    before, st_before = other.results()
+    with pytest.raises(RuntimeError, match=r"gf_batch_restore failed \(1\).*different batch"):
+        other.restore(snap)
+    junk = np.zeros_like(snap)
+    with pytest.raises(RuntimeError, match=r"gf_batch_restore failed \(1\).*not a batch snapshot"):
+        a.restore(junk)
+    after, st_after = other.results()
+    for x, y in zip(before, after):
+        assert np.array_equal(x, y)
+    assert np.array_equal(st_before, st_after)
+    # the snapshot still restores into its own batch
+    a.restore(snap)
+    a.run()
+    a.close()
+    other.close()

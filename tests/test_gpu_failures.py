@@ -77,3 +77,38 @@ def test_failure_path_follows_the_step_control_of_the_oracle(gpu_ctx, make):
     _, so, _ = oracle.solve(s)
     assert list(stats[0]) == list(so)
     assert so[3] == 1
+
+
+def test_pass_cap_ends_the_run_with_timeout(gpu_ctx):
+    """The host cap on Newton passes (gf_solve_opts.max_passes) stops a run
+    that has not finished with GF_ERR_TIMEOUT; a fresh run with the default
+    cap then finishes as the oracle does."""
+    s = configs.pipe_chain(30, 0.4, 0.03, [1e5, -5e4, 2e4], element_length=10.0 / 30)
+    b = gpu.BatchSolver(gpu_ctx, [s], gpu_ctx.opts(poll_every=4, max_passes=8))
+    b.reset()
+    with pytest.raises(RuntimeError, match=r"gf_batch_run failed \(4\)"):
+        b.run()
+    b.close()
+    _, st = _solve(gpu_ctx, [s])
+    _, so, _ = oracle.solve(s)
+    assert list(st[0]) == list(so)
+
+
+def test_server_wave_pass_cap_reports_timeout(gpu_ctx):
+    """A served wave that runs past gf_server_opts.max_wave_passes reports its
+    unfinished structures with GF_ERR_TIMEOUT instead of running on; the
+    server stays usable and solves the next structure normally."""
+    from giraffe_gb300 import serve
+
+    s = configs.pipe_chain(30, 0.4, 0.03, [1e5, -5e4, 2e4], element_length=10.0 / 30)
+    srv = serve.Server(gpu_ctx, hbm_budget=1 << 30, passes_per_chunk=2, max_wave_passes=4)
+    srv.submit(s, tag=1)
+    res = srv.drain(timeout_s=120)
+    srv.close()
+    assert len(res) == 1 and res[0].status == 4  # GF_ERR_TIMEOUT
+    srv = serve.Server(gpu_ctx, hbm_budget=1 << 30)
+    srv.submit(s, tag=2)
+    res = srv.drain(timeout_s=120)
+    srv.close()
+    _, so, _ = oracle.solve(s)
+    assert res[0].status == 0 and list(res[0].stats) == list(so)
