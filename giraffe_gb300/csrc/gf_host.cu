@@ -1553,6 +1553,51 @@ namespace {
 // The first Newton pass of structure s from its initial configuration, read
 // back: K_AA in the solver's band layout (leading dimension W, half
 // bandwidth kw) and P_A, both in the solver's numbering.
+}  // namespace
+
+namespace gfh {
+// The CSR pattern of structure s's K_AA in the reference's free-DOF
+// numbering: row i holds the sorted columns j that some element couples to
+// i (the union of every element's free-DOF pattern, as SparseMatrix::setValue
+// of every element entry followed by setFromTriplets).  Returns nnz.
+int64_t csr_rows(const gf_batch* B, int s, std::vector<std::vector<int>>& rows) {
+  const StructInfo& inf = B->info[s];
+  const int nf = inf.n_free;
+  const std::vector<int>& perm = B->perm[s];
+  std::vector<int> inv(nf);  // solver index -> the reference's index
+  for (int i = 0; i < nf; ++i) inv[perm.empty() ? i : perm[i]] = i;
+  rows.assign(nf, {});
+  auto add_elem = [&](const int* dofs, int nd) {
+    for (int a = 0; a < nd; ++a) {
+      if (dofs[a] < 0) continue;
+      for (int c = 0; c < nd; ++c)
+        if (dofs[c] >= 0) rows[inv[dofs[a]]].push_back(inv[dofs[c]]);
+    }
+  };
+  for (int e = inf.elem_off; e < inf.elem_off + inf.n_elem; ++e) {
+    int d[18];
+    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_enodes[3 * e + a / 6] * 6 + a % 6];
+    add_elem(d, 18);
+  }
+  int s_lo = B->shell_off[s];
+  int s_hi = s + 1 < (int)B->shell_off.size() ? B->shell_off[s + 1] : B->b.sh.n_shells;
+  for (int e = s_lo; e < s_hi; ++e) {
+    int d[27];
+    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_snodes[6 * e + a / 3] * 6 + a % 3];
+    for (int a = 0; a < 9; ++a) d[18 + a] = B->h_gl[(size_t)B->h_snodes[6 * e + 3 + a / 3] * 6 + 3 + a % 3];
+    add_elem(d, 27);
+  }
+  int64_t nnz = 0;
+  for (auto& r : rows) {
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    nnz += (int64_t)r.size();
+  }
+  return nnz;
+}
+}  // namespace gfh
+
+namespace {
 int first_pass_band(gf_batch* B, int s, std::vector<double>& band, std::vector<double>& P, int64_t& W,
                     int64_t& kw) {
   gf_ctx* ctx = B->ctx;
@@ -1619,37 +1664,8 @@ int gf_batch_assemble_csr(gf_batch* B, int s, int* row_ptr, int* col_idx, double
   const StructInfo& inf = B->info[s];
   const int nf = inf.n_free;
   const std::vector<int>& perm = B->perm[s];
-  std::vector<int> inv(nf);  // solver index -> the reference's index
-  for (int i = 0; i < nf; ++i) inv[perm.empty() ? i : perm[i]] = i;
-  // pattern: the union of the element patterns over free DOF pairs
-  // (SparseMatrix::setValue of every element entry, summed by setFromTriplets)
-  std::vector<std::vector<int>> rows(nf);
-  auto add_elem = [&](const int* dofs, int nd) {
-    for (int a = 0; a < nd; ++a) {
-      if (dofs[a] < 0) continue;
-      for (int c = 0; c < nd; ++c)
-        if (dofs[c] >= 0) rows[inv[dofs[a]]].push_back(inv[dofs[c]]);
-    }
-  };
-  for (int e = inf.elem_off; e < inf.elem_off + inf.n_elem; ++e) {
-    int d[18];
-    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_enodes[3 * e + a / 6] * 6 + a % 6];
-    add_elem(d, 18);
-  }
-  int s_lo = B->shell_off[s];
-  int s_hi = s + 1 < (int)B->shell_off.size() ? B->shell_off[s + 1] : B->b.sh.n_shells;
-  for (int e = s_lo; e < s_hi; ++e) {
-    int d[27];
-    for (int a = 0; a < 18; ++a) d[a] = B->h_gl[(size_t)B->h_snodes[6 * e + a / 3] * 6 + a % 3];
-    for (int a = 0; a < 9; ++a) d[18 + a] = B->h_gl[(size_t)B->h_snodes[6 * e + 3 + a / 3] * 6 + 3 + a % 3];
-    add_elem(d, 27);
-  }
-  int64_t nnz = 0;
-  for (auto& r : rows) {
-    std::sort(r.begin(), r.end());
-    r.erase(std::unique(r.begin(), r.end()), r.end());
-    nnz += (int64_t)r.size();
-  }
+  std::vector<std::vector<int>> rows;
+  int64_t nnz = csr_rows(B, s, rows);
   if (nnz > INT32_MAX) {
     set_err(ctx, "gf_batch_assemble_csr: %lld nonzeros exceed 32-bit CSR indices", (long long)nnz);
     return GF_ERR_ARG;

@@ -167,6 +167,17 @@ std::vector<int> rcm_order(int nn, const std::vector<std::vector<int>>& adj);
 // gf_band_solve for half-bandwidths above 17: the blocked wide-band LU on a
 // one-structure batch (gf_sparse.cu).
 int wide_band_solve(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
+// Host PreCalc of one Beam_1 element (end nodes x0, x2; Hooke material E,
+// nu, rho; section A, I11, I22, I12, It, I33; CS rows E1, E3; pre-tension
+// T0) into its constants and initial Gauss-point history, and of one Shell_1
+// element (six nodes, material, thickness).
+void beam_precalc(const double* x0, const double* x2, const double* mat, const double* sec, const double* cs,
+                  gf::BeamConst& c, gf::BeamHist& h, gf::BeamHistAux& x, double T0);
+void shell_precalc(const double* xyz, const double* mat, double thick, gf::ShellConst& c, gf::ShellHist& h,
+                   gf::ShellHistAux& x);
+// CSR pattern of structure s's K_AA in the reference's free-DOF numbering
+// (sorted columns per row); returns nnz.
+int64_t csr_rows(const gf_batch* B, int s, std::vector<std::vector<int>>& rows);
 }  // namespace gfh
 
 #define GF_CK(call)                                                                          \

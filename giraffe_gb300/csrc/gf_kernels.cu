@@ -154,13 +154,20 @@ __global__ void k_step_begin(Batch b) {
     if (go) {
       st.zero_va = 0;
       const StructParams& p = b.params[s];
-      st.last_converged_time = st.time;
-      st.time += st.time_step;
-      if (st.time > 0.99999999 * p.end_time) {
-        st.time = p.end_time;
-        st.time_step = p.end_time - st.last_converged_time;
+      if (st.host_step) {
+        // gf_begin_step: the caller's Static::Solve / Dynamic::Solve loop
+        // advanced the time itself
+        st.time_step = st.current_time_step;
+        st.time = st.last_converged_time + st.current_time_step;
+      } else {
+        st.last_converged_time = st.time;
+        st.time += st.time_step;
+        if (st.time > 0.99999999 * p.end_time) {
+          st.time = p.end_time;
+          st.time_step = p.end_time - st.last_converged_time;
+        }
+        st.current_time_step = st.time_step;
       }
-      st.current_time_step = st.time_step;
       if (p.dynamic) {
         // reference src/Dynamic.cpp:582-590
         double dt = st.time_step;
@@ -1066,6 +1073,32 @@ void launch_iteration_partial(const Batch& b_in, cudaStream_t st) {
   launch_shell_mount(b, st);
   k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
   k_residual<<<b.n_chunks, 256, 0, st>>>(b);
+}
+
+// The stages of one Newton iteration for a caller that runs its own step
+// control (gf_begin_step, gf_assemble, gf_set_increment, gf_commit): every
+// structure's band is filled (the assembly view), as the caller reads K_AA.
+void launch_step_begin(const Batch& b, cudaStream_t st) { k_step_begin<<<b.n_struct, 256, 0, st>>>(b); }
+
+void launch_assembly(const Batch& b_in, cudaStream_t st) {
+  set_attrs();
+  Batch b = b_in;
+  b.full_band = 1;
+  int ns = b.n_struct;
+  k_zero<<<dim3(8, ns), 256, 0, st>>>(b);
+  launch_wide_zero(b, st);
+  launch_mount(b, st, nullptr);
+  launch_shell_mount(b, st);
+  k_loads<<<(ns + 63) / 64, 64, 0, st>>>(b);
+  k_residual<<<b.n_chunks, 256, 0, st>>>(b);
+}
+
+void launch_increment(const Batch& b, cudaStream_t st) { k_update<<<b.n_chunks, 256, 0, st>>>(b); }
+
+void launch_commit(const Batch& b, cudaStream_t st) {
+  if (b.n_elem) k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
+  if (b.sh.n_shells) launch_shell_commit(b, st);
+  if (b.n_nodes) k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b);
 }
 
 // Shared-memory limits of the large kernels, once per process (the served

@@ -81,6 +81,15 @@ void launch_iteration_partial(const Batch& b, cudaStream_t st);
 // Commit of n standalone elements with nodal increments d ([n][18]).
 void launch_beam_commit(int n, const BeamConst* c, BeamHist* h, BeamHistAux* x, const double* d, cudaStream_t st);
 void launch_init_state(const Batch& b, cudaStream_t st);
+// Stages of one Newton iteration driven by the caller's own step control:
+// step start (prescribed displacements, Newmark predictor), assembly into
+// every structure's band and P (P = -P at the end), the increment P added
+// to the nodal displacements (UpdateDisps, UpdateDyn), SaveConfiguration of
+// the structures whose commit flag is set.
+void launch_step_begin(const Batch& b, cudaStream_t st);
+void launch_assembly(const Batch& b, cudaStream_t st);
+void launch_increment(const Batch& b, cudaStream_t st);
+void launch_commit(const Batch& b, cudaStream_t st);
 // Inertial force and tangent of n standalone elements; a: 6 Newmark
 // coefficients in device memory.
 void launch_beam_inertia(int n, const BeamConst* c, const BeamHistAux* x, const double* d, const double* v,

@@ -151,6 +151,9 @@ struct StructState {
   int ray_init;       // Rayleigh matrices formed (after the step's first iteration)
   int step;           // current solution step of the structure
   int zero_va;        // zero the nodal velocities / accelerations before the next time step
+  int host_step;      // the caller's step control set last_converged_time and
+                      // current_time_step (gf_begin_step): step_begin keeps them
+  int pad_st;
   double time, time_step, last_converged_time, current_time_step;
   double force_crit, moment_crit, disp_crit, rot_crit;
   double last_res, last_inc;

@@ -26,7 +26,13 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_beam_inertia_elements", "gf_band_solve_noalloc", "gf_sparse_solve", "gf_batch_device_bytes",
            "gf_server_default_opts", "gf_server_create", "gf_server_destroy", "gf_server_submit",
            "gf_server_poll", "gf_server_get_status", "gf_shell_elements", "gf_batch_assemble_csr",
-           "gf_shell_inertia_elements", "gf_ctx_set_opts"]
+           "gf_shell_inertia_elements", "gf_ctx_set_opts", "gf_upload_structure", "gf_structure_destroy",
+           "gf_structure_dims", "gf_structure_dofs", "gf_structure_pattern", "gf_structure_set_step", "gf_begin_step",
+           "gf_assemble", "gf_set_increment", "gf_commit", "gf_rollback", "gf_structure_nodes", "gf_beam_mount",
+           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange"]
+
+GF_LAYOUT_CSR, GF_LAYOUT_GB = 0, 1
+GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
 
 
 class gf_solve_opts(C.Structure):
@@ -102,6 +108,23 @@ def lib():
         L.gf_shell_inertia_elements.argtypes = [vp, C.c_int, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double,
                                                 C.c_double, C.c_double, dp, dp]
         L.gf_batch_device_bytes.argtypes = [vp, C.c_int, C.POINTER(gf_model_desc), C.POINTER(C.c_size_t)]
+        L.gf_upload_structure.restype = vp
+        L.gf_upload_structure.argtypes = [vp, C.POINTER(gf_model_desc), C.POINTER(gf_solve_opts)]
+        L.gf_structure_destroy.argtypes = [vp]
+        L.gf_structure_dims.argtypes = [vp, ip]
+        L.gf_structure_dofs.argtypes = [vp, ip]
+        L.gf_structure_pattern.argtypes = [vp, ip, ip]
+        L.gf_structure_set_step.argtypes = [vp, C.c_int]
+        L.gf_begin_step.argtypes = [vp, C.c_double, C.c_double]
+        L.gf_assemble.argtypes = [vp, C.c_int, dp, dp]
+        L.gf_set_increment.argtypes = [vp, dp]
+        L.gf_commit.argtypes = [vp]
+        L.gf_rollback.argtypes = [vp]
+        L.gf_structure_nodes.argtypes = [vp, dp, dp]
+        L.gf_beam_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.gf_beam_save_lagrange.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp]
+        L.gf_shell_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.c_int, dp, dp]
+        L.gf_shell_save_lagrange.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp]
         L.gf_server_default_opts.argtypes = [C.POINTER(gf_server_opts)]
         L.gf_server_create.restype = vp
         L.gf_server_create.argtypes = [vp, C.POINTER(gf_server_opts)]
@@ -246,6 +269,47 @@ class Context:
         o = self.opts(wide_update=wide_update)
         self.check(self.L.gf_ctx_set_opts(self.h, C.byref(o)), "gf_ctx_set_opts")
 
+    def beam_mount(self, xyz, mat, sec, cs, lag, disp):
+        """gf_beam_mount: K [n][18][18] (row r, column s) and P_loading on the
+        reference's LagrangeSave state lag [n][2][21]."""
+        n = xyz.shape[0]
+        K = np.zeros((n, 324))
+        f = np.zeros((n, 18))
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (xyz, mat, sec, cs, lag, disp)]
+        self.check(self.L.gf_beam_mount(self.h, n, *[_dp(v) for v in a], _dp(K), _dp(f)), "gf_beam_mount")
+        return K.reshape(n, 18, 18).transpose(0, 2, 1), f
+
+    def beam_save_lagrange(self, xyz, mat, sec, cs, lag, disp):
+        """gf_beam_save_lagrange: the state after committing disp (a new array)."""
+        n = xyz.shape[0]
+        out = np.ascontiguousarray(lag, dtype=np.float64).copy()
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (xyz, mat, sec, cs)]
+        d = np.ascontiguousarray(disp, dtype=np.float64)
+        self.check(self.L.gf_beam_save_lagrange(self.h, n, *[_dp(v) for v in a], _dp(out), _dp(d)),
+                   "gf_beam_save_lagrange")
+        return out
+
+    def shell_mount(self, xyz, mat, thick, lag, disp, cur_xyz=None, pressure=None, area_update=1):
+        n = xyz.shape[0]
+        K = np.zeros((n, 729))
+        f = np.zeros((n, 27))
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (xyz, mat, thick, lag, disp)]
+        cur = None if cur_xyz is None else np.ascontiguousarray(cur_xyz, dtype=np.float64)
+        p = None if pressure is None else np.ascontiguousarray(pressure, dtype=np.float64)
+        self.check(self.L.gf_shell_mount(self.h, n, *[_dp(v) for v in a], _dp(cur) if cur is not None else None,
+                                         _dp(p) if p is not None else None, area_update, _dp(K), _dp(f)),
+                   "gf_shell_mount")
+        return K.reshape(n, 27, 27).transpose(0, 2, 1), f
+
+    def shell_save_lagrange(self, xyz, mat, thick, lag, disp):
+        n = xyz.shape[0]
+        out = np.ascontiguousarray(lag, dtype=np.float64).copy()
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (xyz, mat, thick)]
+        d = np.ascontiguousarray(disp, dtype=np.float64)
+        self.check(self.L.gf_shell_save_lagrange(self.h, n, *[_dp(v) for v in a], _dp(out), _dp(d)),
+                   "gf_shell_save_lagrange")
+        return out
+
     def band_solve_noalloc(self, ab, kl, ku, b):
         """gf_band_solve_noalloc: band_solve through the static device scratch."""
         ab = np.ascontiguousarray(ab, dtype=np.float64)
@@ -255,6 +319,75 @@ class Context:
         self.check(self.L.gf_band_solve_noalloc(self.h, n, kl, ku, _dp(ab), ldab, _dp(x), C.byref(info)),
                    "gf_band_solve_noalloc")
         return x, info.value
+
+
+class DeviceStructure:
+    """One device-resident structure driven one Newton stage at a time
+    (gf_upload_structure ... gf_rollback): the calls a caller's own
+    Static::Solve / Dynamic::Solve loop makes.  Vectors are in the
+    reference's free-DOF numbering."""
+
+    def __init__(self, ctx: Context, structure: Structure, opts=None):
+        self.ctx = ctx
+        self.L = ctx.L
+        self.structure = structure
+        self.handle = structure.desc()
+        o = opts or ctx.opts()
+        self.h = self.L.gf_upload_structure(ctx.h, C.byref(self.handle.desc), C.byref(o))
+        if not self.h:
+            raise RuntimeError("gf_upload_structure failed: " + ctx.error())
+        dims = (C.c_int * 4)()
+        self.L.gf_structure_dims(self.h, dims)
+        self.n, self.nnz, self.kb, self.n_nodes = list(dims)
+        ip = C.POINTER(C.c_int)
+        self.dof = np.zeros(self.n, dtype=np.int32)
+        self.L.gf_structure_dofs(self.h, self.dof.ctypes.data_as(ip))
+        self.row_ptr = np.zeros(self.n + 1, dtype=np.int32)
+        self.col_idx = np.zeros(max(self.nnz, 1), dtype=np.int32)
+        self.L.gf_structure_pattern(self.h, self.row_ptr.ctypes.data_as(ip), self.col_idx.ctypes.data_as(ip))
+        self.col_idx = self.col_idx[:self.nnz]
+
+    def close(self):
+        if self.h:
+            self.L.gf_structure_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_step(self, k: int):
+        self.ctx.check(self.L.gf_structure_set_step(self.h, k), "gf_structure_set_step")
+
+    def begin_step(self, last_converged_time: float, time_step: float):
+        self.ctx.check(self.L.gf_begin_step(self.h, last_converged_time, time_step), "gf_begin_step")
+
+    def assemble(self, layout=GF_LAYOUT_CSR):
+        """(K, P_A): CSR values in the pattern's order, or GB storage
+        [n][3 kb + 1] (column j contiguous), and the residual f_ext - f_int."""
+        K = np.zeros(self.nnz if layout == GF_LAYOUT_CSR else (self.n, 3 * self.kb + 1))
+        P = np.zeros(self.n)
+        self.ctx.check(self.L.gf_assemble(self.h, layout, _dp(K), _dp(P)), "gf_assemble")
+        return K, P
+
+    def set_increment(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self.ctx.check(self.L.gf_set_increment(self.h, _dp(x)), "gf_set_increment")
+
+    def commit(self):
+        self.ctx.check(self.L.gf_commit(self.h), "gf_commit")
+
+    def rollback(self):
+        self.ctx.check(self.L.gf_rollback(self.h), "gf_rollback")
+
+    def nodes(self):
+        """(nodes [n_nodes x 15], increments [n_nodes x 6])."""
+        nodes = np.zeros((self.n_nodes, 15))
+        inc = np.zeros((self.n_nodes, 6))
+        self.ctx.check(self.L.gf_structure_nodes(self.h, _dp(nodes), _dp(inc)), "gf_structure_nodes")
+        return nodes, inc
 
 
 class BatchSolver:

@@ -36,6 +36,12 @@
  *   gf_band_solve           bandsystem (src/BandMatrix.cpp:257-287)
  *   gf_sparse_solve         the Newton solve sparsesystem
  *                           (src/SparseMatrix.cpp:74-166) on SparseMatrix's CSR
+ *   gf_upload_structure ... Solution's per-iteration helpers on one device-
+ *   gf_rollback             resident structure (section "Newton-iteration
+ *                           boundary" below)
+ *   gf_beam_mount,          Beam_1::Mount / SaveLagrange and Shell_1::Mount /
+ *   gf_*_save_lagrange,     SaveLagrange on the reference's stored Gauss-point
+ *   gf_shell_mount          state
  */
 #ifndef GIRAFFE_GPU_H
 #define GIRAFFE_GPU_H
@@ -331,6 +337,94 @@ int gf_server_get_status(const gf_server* srv, gf_server_status* status);
  * one device, from two threads or two contexts, race. */
 enum { GF_NOALLOC_MAX_N = 16384, GF_NOALLOC_MAX_KB = 17 };
 int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const double* ab, int ldab, double* b, int* info);
+
+/* ---- Newton-iteration boundary ----
+ * A device-resident structure driven by the caller's own Static::Solve /
+ * Dynamic::Solve loop, one call per stage of an iteration, in the order of
+ * reference src/Static.cpp:176-298:
+ *
+ *   gf_begin_step(t_last, dt)   Zeros + MountDisplacements (+ the Newmark
+ *                               predictor of a Dynamic step)
+ *   loop: gf_assemble           Clear + MountLocal + MountElementLoads +
+ *                               MountLoads + MountGlobal + P_A = -P_A +
+ *                               MountSparse (src/Static.cpp:206-216)
+ *         (the caller's criteria and sparsesystem / gf_sparse_solve)
+ *         gf_set_increment(x)   UpdateDisps (src/Solution.cpp:390-423; Dynamic:
+ *                               UpdateDyn, src/Dynamic.cpp:480-580)
+ *   gf_commit                   SaveConfiguration (src/Solution.cpp:426-500)
+ *   or gf_rollback              RestoreConfiguration (src/Solution.cpp:502-575)
+ *
+ * Every vector is in the reference's free-DOF numbering (SetGlobalDOFs,
+ * src/Solution.cpp:40-118: node by node, DOF by DOF, fixed and inactive DOFs
+ * skipped); gf_structure_dofs gives node * 6 + DOF of each free index.  The
+ * structure's nodal configuration and Gauss-point histories stay on the
+ * device between calls. */
+typedef struct gf_structure gf_structure;
+enum { GF_LAYOUT_CSR = 0, GF_LAYOUT_GB = 1 };
+
+/* Uploads one structure (its first solution step's parameters; see
+ * gf_structure_set_step), numbers its DOFs and runs the elements' PreCalc:
+ * replaces DOFsActive + SetGlobalDOFs + SetGlobalSize (src/Solution.cpp:
+ * 40-224, 577-654).  NULL on failure (gf_last_error). */
+gf_structure* gf_upload_structure(gf_ctx* ctx, const gf_model_desc* model, const gf_solve_opts* opts);
+void gf_structure_destroy(gf_structure* s);
+/* dims[0] free DOFs n, dims[1] nonzeros of K_AA's CSR pattern, dims[2] its
+ * half-bandwidth kb (GB storage has ldab = 3 kb + 1), dims[3] nodes. */
+int gf_structure_dims(const gf_structure* s, int* dims);
+/* dof_node[i] = node * 6 + DOF (0-based) of free index i. */
+int gf_structure_dofs(const gf_structure* s, int* dof_node);
+/* K_AA's CSR pattern (SparseMatrix::m_matrix: row-major, 0-based, the union
+ * of the element patterns, zeros kept): row_ptr (n + 1), col_idx (nnz). */
+int gf_structure_pattern(const gf_structure* s, int* row_ptr, int* col_idx);
+/* Makes solution step k of the description (0: `solution`, k > 0:
+ * next_steps[k - 1]) the current one (src/main.cpp:52-60). */
+int gf_structure_set_step(gf_structure* s, int k);
+/* Starts a load / time step at last_converged_time + time_step. */
+int gf_begin_step(gf_structure* s, double last_converged_time, double time_step);
+/* Assembles at the current iterate: K (CSR values in gf_structure_pattern's
+ * order, nnz doubles, or GB storage, ldab x n doubles, ldab = 3 kb + 1, per
+ * layout; may be NULL) and P_A (n, after the sign flip: f_ext - f_int; may be
+ * NULL). */
+int gf_assemble(gf_structure* s, int layout, double* K, double* P_A);
+/* Adds the Newton increment x (n) to the nodal displacements. */
+int gf_set_increment(gf_structure* s, const double* x);
+int gf_commit(gf_structure* s);
+int gf_rollback(gf_structure* s);
+/* Current state: nodes (n_nodes x 15: the committed copy_coordinates, then
+ * the nodal rotation tensor row-major) and increments (n_nodes x 6, the
+ * step's Node::displacements); either may be NULL. */
+int gf_structure_nodes(gf_structure* s, double* nodes, double* increments);
+
+/* ---- Element entries on the reference's stored Gauss-point state ----
+ * gf_beam_mount replaces Beam_1::Mount + MountElementLoads
+ * (src/Beam_1.cpp:695-843) for n elements; their state is given as the
+ * reference's LagrangeSave holds it (src/LagrangeSave.h:11-17), per element
+ * and Gauss point GF_BEAM_LAG doubles: Q_i (3x3 column-major, as Matrix
+ * stores it), alpha_i, kappa_i_ref, u_i, dz_i (3 each; LagrangeSave's
+ * d_alpha_i and theta_i are not read by Mount or SaveLagrange).  Geometry,
+ * material, section and CS as gf_beam_elements (no pre-tension); disp
+ * (n x 18) are the nodes' Node::displacements.  gf_beam_save_lagrange
+ * replaces Beam_1::SaveLagrange (src/Beam_1.cpp:1494-1506): it updates lag
+ * in place.  The state of a new element is Q_i = I, dz_i = (0, 0, 1), the
+ * rest zero (src/LagrangeSave.cpp). */
+enum { GF_BEAM_LAG = 21, GF_SHELL_LAG = 27 };
+int gf_beam_mount(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec, const double* cs,
+                  const double* lag, const double* disp, double* K, double* f);
+int gf_beam_save_lagrange(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* sec,
+                          const double* cs, double* lag, const double* disp);
+/* The same for Shell_1 (Shell_1::Mount + MountElementLoads +
+ * MountShellSpecialLoads, src/Shell_1.cpp:899-1467; SaveLagrange, 1650-1664):
+ * per element and Gauss point GF_SHELL_LAG doubles of Shell_1's own state
+ * (src/Shell_1.h:117-127): Q_i (3x3 column-major), u_i, alpha_i, kappa_r1_i,
+ * kappa_r2_i, z_x1_i, z_x2_i (3 each); a new element has Q_i = I,
+ * z_x1_i = (1, 0, 0), z_x2_i = (0, 1, 0), the rest zero.  With a follower
+ * pressure (pressure[n], NULL for none), cur_xyz (n x 18) gives the six nodes'
+ * current positions (copy_coordinates) before this iteration's increments. */
+int gf_shell_mount(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick, const double* lag,
+                   const double* disp, const double* cur_xyz, const double* pressure, int area_update, double* K,
+                   double* f);
+int gf_shell_save_lagrange(gf_ctx* ctx, int n, const double* xyz, const double* mat, const double* thick, double* lag,
+                           const double* disp);
 
 #ifdef __cplusplus
 }

@@ -147,9 +147,12 @@ def test_plate_64_first_solve_tensor_and_fp64_by_backward_error(gpu_ctx):
     be = {k: _backward_error(rp, ci, v, x, P) for k, x in xs.items()}
     be["cpu"] = _backward_error(rp, ci, v, x_cpu, P)
     assert be["tensor"] <= 1e-14 and be["fp64"] <= 1e-14, be
+    # forward differences are bounded by the condition number times the
+    # backward error (the plate's K_AA is near 1e9 conditioned): the two
+    # GPU updates and the pivoting CPU solve agree to about 1e-9
     for k in ("tensor", "fp64"):
-        assert np.linalg.norm(xs[k] - x_cpu) / np.linalg.norm(x_cpu) <= 1e-9, k
-    assert np.linalg.norm(xs["tensor"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]) <= 1e-9
+        assert np.linalg.norm(xs[k] - x_cpu) / np.linalg.norm(x_cpu) <= 1e-8, k
+    assert np.linalg.norm(xs["tensor"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]) <= 1e-8
 
 
 def _scaled_band(rng, n, w, spread):

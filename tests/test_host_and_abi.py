@@ -65,3 +65,18 @@ def test_deck_roundtrip_keywords():
                "NodeSets", "NodalLoad", "NodalConstraint", "ConvergenceCriteria"):
         assert kw in txt
     assert "np.float64" not in txt
+
+
+def test_reference_loop_driver_compiles_against_the_header(tmp_path):
+    """The C++ Static::Solve loop that drives the Newton-iteration boundary
+    (tests/iteration_abi/static_loop.cpp) compiles against include/ alone:
+    the boundary is plain C, usable from the reference's C++."""
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = os.path.join(ROOT, "tests", "iteration_abi", "static_loop.cpp")
+    subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src],
+                   check=True)
