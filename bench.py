@@ -12,9 +12,11 @@ src/Static.cpp:200-250); the metric counts converged load steps.
 
 --impl ours (default) runs the CUDA library; --impl reference times the
 reference's CPU algorithm for the path (the oracle restatement, on all host
-threads, on a bounded sample of the same chains).  Under torchrun every rank
-solves its own 512-chain batch (weak scaling, no collective on the data
-path) and rank 0 prints one JSON line.
+threads, on a bounded sample of the same chains).  Under torchrun with N
+ranks the workload is N x 512 chains of the same family (seed 0), split
+across the ranks by greedy LPT on each chain's estimated Newton-pass cost
+(giraffe_gb300.partition): about 512 chains of work per GPU (weak
+scaling), no collective on the data path; rank 0 prints one JSON line.
 """
 import argparse
 import json
@@ -445,14 +447,28 @@ def served_mixed_leg(ctx, args, rank):
             "aborted": int(sum(r.stats[3] for r in res)), "gpu_launches": st["launches"]}
 
 
+def rank_structures(args, rank, world):
+    """This rank's chains: the N x --chains workload of seed --seed split by
+    LPT on estimated Newton-pass cost (all of it at N = 1), and the
+    estimated load of every rank (None at N = 1)."""
+    from giraffe_gb300 import configs, partition
+
+    allc = configs.batched_static(args.chains * world, seed=args.seed)
+    if world == 1:
+        return allc, None
+    mine, loads = partition.shard(allc, rank, world)
+    return [allc[i] for i in mine], loads
+
+
 def run_ours(args, rank, world):
     import ctypes as C
 
-    from giraffe_gb300 import build, configs, gpu
+    from giraffe_gb300 import build, gpu
 
     build.build()
-    structs = configs.batched_static(args.chains, seed=args.seed + rank)
-    ctx = gpu.Context(0)
+    structs, rank_loads = rank_structures(args, rank, world)
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = gpu.Context(device)
     L = ctx.L
     b = gpu.BatchSolver(ctx, structs, ctx.opts())
     # warm-up
@@ -465,7 +481,7 @@ def run_ours(args, rank, world):
     L.gf_batch_solve_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
     ms = C.c_double(0.0)
     barrier(world)
-    with Clocks() as clk:
+    with Clocks(device) as clk:
         ctx.check(L.gf_batch_solve_timed(b.h, args.steps, C.byref(ms)), "gf_batch_solve_timed")
     barrier(world)
     launches = b.launches()
@@ -495,7 +511,7 @@ def run_ours(args, rank, world):
         barrier(world)
         split = {}
         t0 = time.perf_counter()
-        finals, st = gpu.solve(structs, timings=split)
+        finals, st = gpu.solve(structs, device=device, timings=split)
         e2e_times.append(time.perf_counter() - t0)
         e2e_split.append(split)
     e2e_t = max_over_ranks(statistics.median(e2e_times), world)
@@ -568,7 +584,10 @@ def run_ours(args, rank, world):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
                 "config": {"workload": f"batched static: {args.chains} Beam_1 pipe chains per GPU, "
                                        f"50-2000 elements log-uniform, 10 load steps, seed {args.seed}",
-                           "chains_per_gpu": args.chains, "load_steps": 10,
+                           "chains": args.chains * world, "chains_per_gpu": args.chains, "load_steps": 10,
+                           "sharding": "one workload of N x chains split by greedy LPT on estimated Newton-pass "
+                                       "cost (giraffe_gb300.partition)" if world > 1 else "single GPU",
+                           "estimated_rank_loads": rank_loads,
                            "newton_solves_per_step": solves_per_step,
                            "precision": "plain FP64 (element tangent and force, chain/band solver, residual)",
                            "l2": "working set larger than L2: element tangent scratch 0.62 GB and chain-solver "
