@@ -315,6 +315,12 @@ def shell_leg(ctx, args, fp64_peak):
     ms_fp64 = bf.run()
     st_fp64 = bf.results()[1]
     bf.close()
+    # and with the warp-level mma.sync form of the tensor-core update
+    bsy = gpu.BatchSolver(ctx, [s], ctx.opts(wide_update=gpu.GF_WIDE_TENSOR_SYNC))
+    bsy.reset()
+    ms_sync = bsy.run()
+    f_sync, st_sync = bsy.results()
+    bsy.close()
     b = gpu.BatchSolver(ctx, [s])
     b.reset()
     ms = b.run()
@@ -324,6 +330,19 @@ def shell_leg(ctx, args, fp64_peak):
     dims = (C.c_int * 2)()
     L.gf_batch_assemble(b.h, 0, None, None, dims)
     launches = b.launches()
+    # per-kernel-class device time of a pass over the first load step (events
+    # around every launch, no graph; classes on the lookahead's helper
+    # streams overlap the main stream, so the classes sum to more than a pass)
+    L.gf_batch_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.gf_kernel_name.restype = C.c_char_p
+    s1 = configs.square_plate(args.shell_n, steps=20)
+    s1.solution.end_time = 1.0 / 20.0
+    bp = gpu.BatchSolver(ctx, [s1])
+    kms, kl = (C.c_double * 17)(), (C.c_longlong * 17)()
+    ctx.check(L.gf_batch_profile(bp.h, kms, kl), "gf_batch_profile")
+    passes = max(1, int(bp.results()[1][0][1]))
+    bp.close()
+    split = {L.gf_kernel_name(i).decode(): round(kms[i] / passes, 3) for i in range(17) if kl[i]}
     # the sparsesystem drop-in on the same plate: the first pass's K_AA as a
     # host CSR, solved through gf_sparse_solve (ordering, upload, wide-band
     # LU, solution back to the host)
@@ -358,12 +377,17 @@ def shell_leg(ctx, args, fp64_peak):
                         f"{dims[1]}, first {args.shell_steps} of 20 load steps",
             "newton_solves": int(st[0][0]), "newton_passes": int(st[0][1]), "ms": ms,
             "solves_per_s": st[0][0] / (ms / 1e3), "ms_per_pass": ms / max(1, st[0][1]),
-            "wide_update": "tensor cores: FP64 products from exact bf16 slices (Ozaki), mma.sync m16n8k16",
+            "wide_update": "tensor cores: FP64 products from exact bf16 slices (Ozaki), tcgen05.mma 128x64x16 with "
+                           "TMEM accumulators, bulk-copy (TMA) staged slices",
             "wide_lu_tflops": lu.value / (ms / 1e3) / 1e12, "fp64_peak_tflops": fp64_peak,
             "wide_lu_frac_of_measured_fp64": lu.value / (ms / 1e3) / 1e12 / fp64_peak,
             "fp64_fma_update": {"ms": ms_fp64, "ms_per_pass": ms_fp64 / max(1, st_fp64[0][1]),
                                 "same_counts": bool(tuple(st_fp64[0]) == tuple(st[0]))},
+            "mma_sync_update": {"ms": ms_sync, "ms_per_pass": ms_sync / max(1, st_sync[0][1]),
+                                "same_counts": bool(tuple(st_sync[0]) == tuple(st[0])),
+                                "max_abs_diff_m": float(np.abs(f_sync[0][:, :3] - fin[0][:, :3]).max())},
             "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
+            "pass_split_ms": split,
             "sparse_solve": sparse,
             "plate8": {"workload": "Shell_1 plate 8x8x2 (1,203 free DOFs), all 20 load steps",
                         "gpu_solves_per_s": st_small[0] / (ms_small / 1e3), "gpu_ms": ms_small,

@@ -985,12 +985,12 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total) ||
         !balloc(B, &sd.panel, 1))
       return GF_ERR_CUDA;
-    if (B->opts.wide_update == GF_WIDE_TENSOR) {
+    if (B->opts.wide_update == GF_WIDE_TENSOR || B->opts.wide_update == GF_WIDE_TENSOR_SYNC) {
       // slices of one panel per wide structure for the tensor-core update
-      sd.oz_rows = (max_wkl + 63) / 64 * 64;
+      sd.oz_rows = (max_wkl + 127) / 128 * 128;  // whole 128-row tiles of the tensor-core update
       const size_t nw = wide_structs.size(), R = (size_t)sd.oz_rows;
-      if (!balloc(B, &sd.oz_slices, nw * 2 * 8 * R * GF_WB_NB) || !balloc(B, &sd.oz_exp, nw * 2 * R) ||
-          !zeroed(B, &sd.oz_kmax, nw * 2 * 2 * GF_WB_NB))
+      if (!zeroed(B, &sd.oz_slices, nw * 2 * 8 * R * GF_WB_NB) || !balloc(B, &sd.oz_exp, nw * 2 * R) ||
+          !zeroed(B, &sd.oz_kmax, nw * 2 * 2 * GF_WB_NB) || !zeroed(B, &sd.oz_error, 1))
         return GF_ERR_CUDA;
     }
     if (!B->count_only) {
@@ -1043,7 +1043,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
-  b.sh.wide_tc = B->opts.wide_update == GF_WIDE_TENSOR && b.sh.oz_slices != nullptr;
+  b.sh.wide_tc = b.sh.oz_slices != nullptr ? B->opts.wide_update : GF_WIDE_FP64;
   b.max_refine = B->opts.max_refine;
   return GF_OK;
 }
@@ -1111,7 +1111,9 @@ void gf_destroy(gf_ctx* ctx) {
 const char* gf_last_error(const gf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 int gf_ctx_set_opts(gf_ctx* ctx, const gf_solve_opts* opts) {
-  if (!ctx || !opts || (opts->wide_update != GF_WIDE_FP64 && opts->wide_update != GF_WIDE_TENSOR)) {
+  if (!ctx || !opts ||
+      (opts->wide_update != GF_WIDE_FP64 && opts->wide_update != GF_WIDE_TENSOR &&
+       opts->wide_update != GF_WIDE_TENSOR_SYNC)) {
     set_err(ctx, "gf_ctx_set_opts: invalid arguments");
     return GF_ERR_ARG;
   }

@@ -956,8 +956,11 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
 
 // L21 = A21 U11^-1 (row blocks) and U12 = L11^-1 A12 (column blocks) of
 // panel p.  16 rows (or columns) per CTA, 16 threads each splitting the
-// panel width; blockIdx.x < nrb: L21 row block, else U12 column block.
-__global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
+// panel width.  The launch covers blocks blk0 .. blk0 + nblk - 1 of both:
+// blockIdx.x < nblk an L21 row block, else a U12 column block.  The first
+// four blocks (the rows and columns of the next panel's diagonal block) are
+// a launch of their own on the lookahead's critical path; the rest follow.
+__global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int nblk) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
@@ -969,8 +972,8 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p) {
   const int m = min(w.kl, w.n - j0 - nb);  // rows below / columns right of the panel
   if (m <= 0) return;
   const int nrb = (m + 15) / 16;
-  const bool lower = blockIdx.x < nrb;
-  const int blk = lower ? blockIdx.x : blockIdx.x - nrb;
+  const bool lower = (int)blockIdx.x < nblk;
+  const int blk = blk0 + (lower ? (int)blockIdx.x : (int)blockIdx.x - nblk);
   if (blk >= nrb) return;
   __shared__ double T[NB][NB + 1];  // the diagonal block's LU
   __shared__ double X[16][NB + 1];
@@ -1235,7 +1238,10 @@ __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
   const int64_t R = b.sh.oz_rows;
   for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
     const int i = x / NB, k = x % NB;
-    oz_split(F[i * (NB + 1) + k], e[i], dst + (int64_t)(r0 + i) * NB + k, (int)(R * NB));
+    // the 128-byte swizzle: 16-byte chunk k / 8 of row r stored at chunk
+    // (k / 8) ^ (r & 7)
+    const int r = r0 + i, ks = (((k >> 3) ^ (r & 7)) << 3) | (k & 7);
+    oz_split(F[i * (NB + 1) + k], e[i], dst + (int64_t)r * NB + ks, (int)(R * NB));
   }
   if (tid < OZ_T) (lower ? o.eL : o.eU)[r0 + tid] = e[tid];
 }
@@ -1291,8 +1297,10 @@ __global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int
       // 32 rows of L21 and 64 columns of U12, 8 chunks of 16 bytes each
       for (int x = tid; x < (OZ_TR + OZ_T) * 8; x += OZ_THREADS) {
         const int op = x >= OZ_TR * 8, y = x - op * OZ_TR * 8, i = y >> 3, c = y & 7;
+        // chunk c of a row sits at chunk c ^ (row & 7) in global memory (r0
+        // and c0 are multiples of 8)
         const __nv_bfloat16* src = (op ? o.U + (int64_t)q * R * NB + (int64_t)(c0 + i) * NB
-                                       : o.L + (int64_t)q * R * NB + (int64_t)(r0 + i) * NB) + 8 * c;
+                                       : o.L + (int64_t)q * R * NB + (int64_t)(r0 + i) * NB) + 8 * (c ^ (i & 7));
         __nv_bfloat16* dst = (op ? Us + q * OZ_T * OZ_LD : Ls + q * OZ_TR * OZ_LD) + i * OZ_LD + 8 * c;
         oz_cp16(dst, src);
       }
@@ -1369,6 +1377,246 @@ __global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int
         w.at(base + r0 + i, base + c0 + j) -= v * scale;
       }
     }
+}
+
+// ---- the same trailing update on the 5th-generation tensor cores ----
+// One CTA per 128 x 64 output tile.  The eight diagonals of slice products
+// accumulate in tensor memory (8 x 64 FP32 columns: the whole 512 columns
+// of the SM), issued by one thread as tcgen05.mma (M 128, N 64, K 16, bf16
+// in, FP32 out) on shared-memory operands in the 128-byte swizzled K-major
+// layout; the slices arrive by bulk copies (the TMA engine) completing on
+// mbarriers: the tile's eight U12 slices (64 KB) at once, its L21 slices
+// (16 KB each) through three stages, so slice q + 2 loads while the products
+// of slice q run.  Accumulator d (q + t = d) gets (d + 1) products of K = 64,
+// an exact integer below 2^23, as in the mma.sync version.  While the
+// products run, four warps load the tile's A22 into registers (a row per
+// thread); then they read tensor memory (warp w owns rows 32 w .. 32 w + 31,
+// a row per lane), join the diagonals exactly in 64-bit integers, convert
+// once, scale by the row and column powers of two through the exponent bits
+// and write A22 back (column by column, so a warp writes 32 consecutive
+// doubles).  Every wait is bounded; a wait that gives up marks the
+// structure's solve failed and sets the batch's error word, and the CTA
+// still waits (bounded) for its copies and products before it frees tensor
+// memory.
+constexpr int T5_M = 128;
+constexpr int T5_N = 64;
+constexpr int T5_STAGES = 3;
+constexpr int T5_THREADS = 128;
+constexpr uint32_t T5_A_BYTES = T5_M * NB * 2;  // one L21 slice of a tile
+constexpr uint32_t T5_B_BYTES = T5_N * NB * 2;  // one U12 slice of a tile
+constexpr uint32_t T5_TMEM_COLS = OZ_S * T5_N;  // 512
+constexpr size_t T5_SMEM = 1024 + OZ_S * T5_B_BYTES + T5_STAGES * T5_A_BYTES + 128 + T5_N * sizeof(int);
+// instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28
+constexpr uint32_t T5_IDESC =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_N >> 3) << 17) | ((uint32_t)(T5_M >> 4) << 24);
+constexpr long long T5_WAIT_CYCLES = 2000000000ll;  // about a second at the SM clock
+
+__device__ __forceinline__ uint32_t t5_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t t5_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void t5_mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void t5_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool t5_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of parity `parity` to complete, for about a second at
+// most; false if it did not.
+__device__ __forceinline__ bool t5_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!t5_try_wait(bar, parity))
+    if (clock64() - t0 > T5_WAIT_CYCLES) return false;
+  return true;
+}
+__device__ __forceinline__ void t5_bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void t5_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(T5_IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ void t5_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void t5_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void t5_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// Eight consecutive FP32 columns of this warp's 32 TMEM lanes (a lane each).
+__device__ __forceinline__ void t5_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void t5_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, int part) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
+  const int s = b.sh.wide_structs[blockIdx.z];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(w.kl, w.n - j0 - nb);
+  if (m <= 0) return;
+  const int r0 = blockIdx.x * T5_M, c0 = blockIdx.y * T5_N;
+  if (r0 >= m || c0 >= m) return;
+  extern __shared__ __align__(16) unsigned char t5_raw[];
+  unsigned char* base = t5_raw + ((1024u - (t5_smem(t5_raw) & 1023u)) & 1023u);
+  unsigned char* Bs = base;                              // [slice][64 columns][128 B]
+  unsigned char* As = Bs + OZ_S * T5_B_BYTES;            // [stage][128 rows][128 B]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(As + T5_STAGES * T5_A_BYTES);  // fullB, fullA[3], emptyA[3], done
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 8);
+  int* okflag = reinterpret_cast<int*>(holder + 1);
+  int* eU = reinterpret_cast<int*>(bars + 16);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const OzSlices o = oz_slices(b, blockIdx.z);
+  const int64_t R = b.sh.oz_rows;
+  const uint32_t bar0 = t5_smem(bars);
+  const uint32_t fullB = bar0, fullA = bar0 + 8, emptyA = bar0 + 32, done = bar0 + 56;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(t5_smem(holder)),
+                 "r"(T5_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 8; ++i) t5_mbar_init(bar0 + 8 * i, 1);
+    *okflag = 1;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (tid < T5_N) eU[tid] = o.eU[c0 + tid];
+  const int eLr = o.eL[r0 + tid];  // r0 + 127 < oz_rows
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  const uint32_t tmem = *holder;
+  if (tid == 0) {
+    // issue the loads, then the products slice by slice
+    const uint32_t sA = t5_smem(As), sB = t5_smem(Bs);
+    const unsigned char* gU = reinterpret_cast<const unsigned char*>(o.U + (int64_t)c0 * NB);
+    const unsigned char* gL = reinterpret_cast<const unsigned char*>(o.L + (int64_t)r0 * NB);
+    const int64_t slice_bytes = R * NB * 2;
+    t5_expect_tx(fullB, OZ_S * T5_B_BYTES);
+    for (int q = 0; q < OZ_S; ++q) t5_bulk_load(sB + q * T5_B_BYTES, gU + q * slice_bytes, T5_B_BYTES, fullB);
+    for (int q = 0; q < T5_STAGES; ++q) {
+      t5_expect_tx(fullA + 8 * q, T5_A_BYTES);
+      t5_bulk_load(sA + q * T5_A_BYTES, gL + q * slice_bytes, T5_A_BYTES, fullA + 8 * q);
+    }
+    int issued[T5_STAGES] = {1, 1, 1}, landed[T5_STAGES] = {0, 0, 0};
+    bool okB = false, ok = true;
+    for (int q = 0; q < OZ_S && ok; ++q) {
+      const int st = q % T5_STAGES;
+      if (!t5_wait(fullA + 8 * st, (q / T5_STAGES) & 1)) { ok = false; break; }
+      landed[st]++;
+      if (!okB) {
+        if (!t5_wait(fullB, 0)) { ok = false; break; }
+        okB = true;
+      }
+      t5_fence_after();
+      for (int t = 0; t + q < OZ_S; ++t)
+        for (int kk = 0; kk < NB / 16; ++kk)
+          t5_mma(tmem + (uint32_t)((q + t) * T5_N), t5_desc(sA + st * T5_A_BYTES + 32 * kk),
+                 t5_desc(sB + t * T5_B_BYTES + 32 * kk), (q | kk) != 0);
+      t5_commit(emptyA + 8 * st);
+      if (q >= 1 && q + 2 < OZ_S) {
+        // the stage of slice q - 1 takes slice q + 2 once its products ran
+        const int sp = (q - 1) % T5_STAGES;
+        if (!t5_wait(emptyA + 8 * sp, ((q - 1) / T5_STAGES) & 1)) { ok = false; break; }
+        t5_expect_tx(fullA + 8 * sp, T5_A_BYTES);
+        t5_bulk_load(sA + sp * T5_A_BYTES, gL + (q + 2) * slice_bytes, T5_A_BYTES, fullA + 8 * sp);
+        issued[sp]++;
+      }
+    }
+    t5_commit(done);  // arrives once every product issued so far has run
+    if (!ok) {
+      // let the copies in flight land before the CTA's shared memory goes
+      *okflag = 0;
+      for (int st = 0; st < T5_STAGES; ++st)
+        for (int k = landed[st]; k < issued[st]; ++k) t5_wait(fullA + 8 * st, k & 1);
+      if (!okB) t5_wait(fullB, 0);
+    }
+  }
+  // epilogue: while the products run, every thread loads its row of the
+  // tile's A22 into registers (64 independent loads, so the L2 latency is
+  // paid once, not once per column); then it waits for the products and
+  // reads its row of the accumulators
+  const int base_row = j0 + nb;
+  const int r = r0 + tid;  // this thread's row of the window
+  const bool row_live = r < m;
+  double a22[T5_N];
+#pragma unroll
+  for (int c = 0; c < T5_N; ++c)
+    a22[c] = (row_live && c0 + c < m) ? w.at(base_row + r, base_row + c0 + c) : 0.0;
+  const bool ready = t5_wait(done, 0);
+  if (!ready && tid == 0) t5_wait(done, 0);  // once more before tensor memory is freed
+  __syncthreads();
+  const bool good = ready && *okflag;
+  if (!good && tid == 0) {
+    atomicOr(b.sh.oz_error, 1);
+    b.state[s].info_fail = 1;
+  }
+  t5_fence_after();
+  if (good) {
+    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int j = 0; j < T5_N / 8; ++j) {
+      uint32_t v[OZ_S][8];
+#pragma unroll
+      for (int d = 0; d < OZ_S; ++d) t5_ld8(tl + (uint32_t)(d * T5_N + 8 * j), v[d]);
+      t5_wait_ld();
+      if (!row_live) continue;
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) {
+        const int c = c0 + 8 * j + cc;
+        if (c >= m || (part == 2 && r < NB && c < NB)) continue;
+        int ci[OZ_S];
+#pragma unroll
+        for (int d = 0; d < OZ_S; ++d) ci[d] = __float2int_rn(__uint_as_float(v[d][cc]));
+        // S = sum_d c_d 2^(7 (7 - d)), |S| < 2^73; T = floor(S / 2^10) in
+        // 64 bits: pairs of diagonals first (|c_d 2^7 + c_(d+1)| < 2^31);
+        // the bits dropped weigh below 2^-62 of the largest |S|, far under
+        // the slicing's own truncation
+        const int P0 = ci[0] * 128 + ci[1], P1 = ci[2] * 128 + ci[3], P2 = ci[4] * 128 + ci[5];
+        const int P3 = (ci[6] * 128 + ci[7]) >> 10;
+        const long long T = ((long long)P0 << 32) + ((long long)P1 << 18) + ((long long)P2 << 4) + (long long)P3;
+        double dv = (double)T;
+        // times 2^(e_i + e_j - 2046 - 53) through the exponent field
+        const int k = eLr + eU[8 * j + cc] - 2046 - 53;
+        if (dv != 0.0) {
+          const long long bits = __double_as_longlong(dv);
+          const int e = (int)((bits >> 52) & 0x7FF) + k;
+          dv = (e > 0 && e < 2047) ? __longlong_as_double(bits + ((long long)k << 52)) : ldexp(dv, k);
+        }
+        w.at(base_row + r, base_row + c) = a22[8 * j + cc] - dv;
+      }
+    }
+  }
+  t5_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    t5_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(T5_TMEM_COLS));
+  }
 }
 
 // Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
@@ -1483,6 +1731,10 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
   k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
 }
 
+// Row (column) blocks of 16 in the first trsm launch of a panel: the 64
+// rows and columns that the next panel's diagonal block needs.
+constexpr int TRSM_FIRST = NB / 16;
+
 // Panel loop with lookahead on two helper streams (fork / join by events,
 // so a captured pass keeps the same dependencies):
 //   main   trsm(p) -> update corner(p) -> update rest(p) -> [join diag(p+1)]
@@ -1501,14 +1753,19 @@ static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
   if (b.sh.wide_tc && part != 1) {
     static const bool attr = [] {  // once per process, thread-safe
       cudaFuncSetAttribute(k_wb_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM);
+      cudaFuncSetAttribute(k_wb_update_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
       cudaFuncSetAttribute(k_wb_slice, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SLICE_SMEM);
       return true;
     }();
     (void)attr;
     // the panel's slices (L21 rows and U12 columns), then the tiles
     k_wb_slice<<<dim3((mr + OZ_T - 1) / OZ_T, 2, nw), 256, OZ_SLICE_SMEM, st>>>(b, p);
-    k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
-                                                                                                      part);
+    if (b.sh.wide_tc == 1)  // GF_WIDE_TENSOR: tcgen05; 2, GF_WIDE_TENSOR_SYNC: mma.sync
+      k_wb_update_t5<<<dim3((mr + T5_M - 1) / T5_M, (mr + T5_N - 1) / T5_N, nw), T5_THREADS, T5_SMEM, st>>>(b, p,
+                                                                                                         part);
+    else
+      k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
+                                                                                                        part);
   } else {
     const int t = part == 1 ? (NB + UT - 1) / UT : (mr + UT - 1) / UT;
     k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
@@ -1577,16 +1834,17 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
   if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
-  k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, sb>>>(b, -1);
-  cudaEventRecord(e_trsm, sb);
-  cudaStreamWaitEvent(s3, e_trsm, 0);
-  k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
-  cudaEventRecord(e_fwd, s3);
+  k_wb_trsm<<<dim3(2 * TRSM_FIRST, nw), 256, 0, sb>>>(b, -1, 0, TRSM_FIRST);
   launch_wb_update(b, -1, 1, sb);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
   k_wb_diag<<<nw, 256, 0, s2>>>(b, -2);
   cudaEventRecord(e_diag, s2);
+  if (nrb > TRSM_FIRST) k_wb_trsm<<<dim3(2 * (nrb - TRSM_FIRST), nw), 256, 0, sb>>>(b, -1, TRSM_FIRST, nrb - TRSM_FIRST);
+  cudaEventRecord(e_trsm, sb);
+  cudaStreamWaitEvent(s3, e_trsm, 0);
+  k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
+  cudaEventRecord(e_fwd, s3);
   launch_wb_update(b, -1, 2, sb);
   cudaStreamWaitEvent(sb, e_diag, 0);
   cudaStreamWaitEvent(sb, e_fwd, 0);
@@ -1622,17 +1880,27 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
   { ProfScope q(prof, st, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, st>>>(b, 0); }
   for (int p = 0; p < sd.max_panels; ++p) {
-    { ProfScope q(prof, st, KC_WIDE_TRSM); k_wb_trsm<<<dim3(2 * nrb, nw), 256, 0, st>>>(b, p); }
-    cudaEventRecord(e_trsm, st);
-    cudaStreamWaitEvent(s3, e_trsm, 0);
-    { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
     bool next = p + 1 < sd.max_panels;
+    // the first row and column blocks of L21 / U12, the corner update and
+    // the next diagonal LU form the lookahead's critical path; the rest of
+    // the trsm, the forward step and the bulk of the update run beside the
+    // next diagonal LU
+    { ProfScope q(prof, st, KC_WIDE_TRSM); k_wb_trsm<<<dim3(2 * TRSM_FIRST, nw), 256, 0, st>>>(b, p, 0, TRSM_FIRST); }
     if (next) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 1, st); }
       cudaEventRecord(e_corner, st);
       cudaStreamWaitEvent(s2, e_corner, 0);
       { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, s2>>>(b, p + 1); }
       cudaEventRecord(e_diag, s2);
+    }
+    if (nrb > TRSM_FIRST) {
+      ProfScope q(prof, st, KC_WIDE_TRSM);
+      k_wb_trsm<<<dim3(2 * (nrb - TRSM_FIRST), nw), 256, 0, st>>>(b, p, TRSM_FIRST, nrb - TRSM_FIRST);
+    }
+    cudaEventRecord(e_trsm, st);
+    cudaStreamWaitEvent(s3, e_trsm, 0);
+    { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
+    if (next) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 2, st); }
       cudaStreamWaitEvent(st, e_diag, 0);
     } else {
@@ -1704,13 +1972,17 @@ int shell_launches_per_pass(const Batch& b) {
     n += 2 + (b.sh.any_rayleigh ? 1 : 0);  // tangent (+ Rayleigh damping) + commit
     for (int c = 0; c < b.sh.n_colors; ++c) n += b.sh.color_off[c + 1] > b.sh.color_off[c];
   }
-  // unrolled: the first diagonal LU, then per panel trsm, forward step,
-  // update corner + next diagonal + update rest (or one update for the
-  // last), backward step; graph loops: two loop-control kernels, the first
-  // diagonal LU, six kernels per forward iteration and two per backward one
-  if (b.sh.n_wide)
-    n += (b.sh.loops_in_graph ? 3 + 8 * b.sh.max_panels : 1 + 6 * b.sh.max_panels) +
-         (b.sh.wide_tc ? b.sh.max_panels : 0);  // the tensor-core update's slicing kernel
+  // unrolled: the first diagonal LU, then per panel the first trsm blocks,
+  // update corner + next diagonal, the other trsm blocks, forward step,
+  // update rest, backward step (the last panel has no corner or next
+  // diagonal); graph loops: two loop-control kernels, the first diagonal
+  // LU, the same six or seven kernels and a counter step per forward
+  // iteration, and two kernels per backward one
+  if (b.sh.n_wide) {
+    const int P = b.sh.max_panels, per = 6 + ((b.sh.max_kl + 15) / 16 > TRSM_FIRST ? 1 : 0);
+    n += (b.sh.loops_in_graph ? 3 + (per + 2) * P : 1 + per * P - 2) +
+         (b.sh.wide_tc ? P : 0);  // the tensor-core update's slicing kernel
+  }
   return n;
 }
 }  // namespace gf

@@ -110,15 +110,18 @@ struct WideBatch {
     st0.phase = PH_ITER;
     st0.need_solve = 1;
     const int zero = 0;
-    const int R = (w + 63) / 64 * 64;
+    const int R = (w + 127) / 128 * 128;
     __nv_bfloat16* sl = nullptr;
     int* se = nullptr;
     unsigned long long* km = nullptr;
+    int* err = nullptr;
     if (!mem.get(&dinf, 1) || !mem.get(&dst, 1) || !mem.get(&dws, 1) || !hl.create() ||
         !mem.get(&sl, (size_t)2 * 8 * R * GF_WB_NB) || !mem.get(&se, (size_t)2 * R) ||
-        !mem.get(&km, (size_t)2 * 2 * GF_WB_NB))
+        !mem.get(&km, (size_t)2 * 2 * GF_WB_NB) || !mem.get(&err, 1))
       return false;
-    if (cudaMemsetAsync(km, 0, sizeof(unsigned long long) * 2 * 2 * GF_WB_NB, ctx->stream) != cudaSuccess)
+    if (cudaMemsetAsync(km, 0, sizeof(unsigned long long) * 2 * 2 * GF_WB_NB, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(sl, 0, sizeof(__nv_bfloat16) * 2 * 8 * R * GF_WB_NB, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(err, 0, sizeof(int), ctx->stream) != cudaSuccess)
       return false;
     cudaStream_t s = ctx->stream;
     if (cudaMemcpyAsync(dinf, &inf, sizeof(inf), cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -137,11 +140,12 @@ struct WideBatch {
     sd.max_panels = inf.n_panels;
     sd.max_kl = w;
     sd.wband = wband;
-    sd.wide_tc = ctx->wide_update == GF_WIDE_TENSOR;  // the context's choice (tensor cores by default)
+    sd.wide_tc = ctx->wide_update;  // the context's choice (tcgen05 tensor cores by default)
     sd.oz_rows = R;
     sd.oz_slices = sl;
     sd.oz_exp = se;
     sd.oz_kmax = km;
+    sd.oz_error = err;
     for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
     for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
     return true;

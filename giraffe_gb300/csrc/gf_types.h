@@ -253,10 +253,13 @@ struct ShellData {
   double* wband;
   int* panel;       // device panel counter of the captured panel loops
   int loops_in_graph;  // capture the panel loops as graph WHILE loops (served waves)
-  int wide_tc;         // trailing update on the tensor cores (Ozaki slices) instead of FP64 FMA
+  int wide_tc;         // trailing update: 0 FP64 FMA, 1 tcgen05 Ozaki slices, 2 mma.sync Ozaki slices
   // the tensor-core update's slices of a panel: per wide structure slot,
-  // [2 operands][8 slices][oz_rows][64] bf16 and [2][oz_rows] exponents
-  int oz_rows;         // max_kl rounded up to 64
+  // [2 operands][8 slices][oz_rows][64] bf16 and [2][oz_rows] exponents;
+  // every 128-byte row of 64 slices is stored with its eight 16-byte chunks
+  // permuted (chunk c at c ^ (row & 7)), the 128-byte swizzle of the tensor
+  // cores' shared-memory operands, so a tile of rows is one bulk copy
+  int oz_rows;         // max_kl rounded up to 128
   __nv_bfloat16* oz_slices;
   int* oz_exp;
   // per wide structure slot, [2 panel parities][2 operands][64]: the
@@ -264,6 +267,9 @@ struct ShellData {
   // and of each row k of its U12 (zeroed by the panel's diagonal LU, raised
   // by its trsm), from which the slicing balances k by a power of two
   unsigned long long* oz_kmax;
+  // nonzero when a bounded wait of the tensor-core update gave up (its
+  // structures are then reported as failed solves)
+  int* oz_error;
   // host handles of the wide-band lookahead: two helper streams and the
   // events that fork from and join into the pass's stream; aux[2] roots the
   // captured panel-loop bodies

@@ -15,7 +15,7 @@ from .model import Structure, gf_model_desc
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgiraffe_gpu.so")
 
 GF_PREC_FP64, GF_PREC_MIXED = 0, 1
-GF_WIDE_FP64, GF_WIDE_TENSOR = 0, 1
+GF_WIDE_FP64, GF_WIDE_TENSOR, GF_WIDE_TENSOR_SYNC = 0, 1, 2
 
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_batch_create",
            "gf_batch_destroy", "gf_batch_reset", "gf_batch_run", "gf_batch_results",

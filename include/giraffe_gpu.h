@@ -73,7 +73,9 @@ typedef struct gf_solve_opts {
   int use_graph;   /* capture one Newton pass as a CUDA graph */
   int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
                       default: FP64 products emulated from exact bf16 slices
-                      on the tensor cores, Ozaki scheme) or GF_WIDE_FP64
+                      on the tensor cores, Ozaki scheme, tcgen05.mma with
+                      tensor-memory accumulators), GF_WIDE_TENSOR_SYNC (the
+                      same emulation on warp-level mma.sync) or GF_WIDE_FP64
                       (FP64 FMA).  The emulated product of row i of L21 and
                       column j of U12 (K = 64 terms) errs by at most about
                       2^-52 K max_k |L_ik 2^-f_k| max_k |2^f_k U_kj|, where
@@ -85,7 +87,7 @@ typedef struct gf_solve_opts {
                       beyond it the run stops with GF_ERR_TIMEOUT (0: the
                       default of 4,000,000) */
 } gf_solve_opts;
-enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1 };
+enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1, GF_WIDE_TENSOR_SYNC = 2 };
 
 /* Per-structure result of a solution step. */
 typedef struct gf_stats {
