@@ -1412,7 +1412,7 @@ int gf_batch_profile(gf_batch* B, double* ms_out, long long* launches_out) {
   cudaStream_t st = B->stream;
   int r = batch_reset(B);
   if (r != GF_OK) return r;
-  const int cap = 1 << 16;
+  const int cap = 1 << 18;
   std::vector<cudaEvent_t> ev(2 * cap);
   std::vector<int> cls(cap);
   for (auto& e : ev) CK(cudaEventCreate(&e));

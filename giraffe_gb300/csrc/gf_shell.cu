@@ -1389,19 +1389,20 @@ __global__ void __launch_bounds__(OZ_THREADS) k_wb_update_tc(Batch b, int p, int
 // (16 KB each) through three stages, so slice q + 2 loads while the products
 // of slice q run.  Accumulator d (q + t = d) gets (d + 1) products of K = 64,
 // an exact integer below 2^23, as in the mma.sync version.  While the
-// products run, four warps load the tile's A22 into registers (a row per
-// thread); then they read tensor memory (warp w owns rows 32 w .. 32 w + 31,
-// a row per lane), join the diagonals exactly in 64-bit integers, convert
-// once, scale by the row and column powers of two through the exponent bits
-// and write A22 back (column by column, so a warp writes 32 consecutive
-// doubles).  Every wait is bounded; a wait that gives up marks the
+// products run, sixteen warps load the tile's A22 into registers (warp w
+// owns rows 32 (w % 4) .. + 31, the TMEM lanes it may read, a row per lane,
+// and columns 16 (w / 4) .. + 15); then they read tensor memory, join the
+// diagonals exactly in 64-bit integers, convert once, scale by the row and
+// column powers of two through the exponent bits and write A22 back (column
+// by column, so a warp writes 32 consecutive doubles).  Every wait is bounded; a wait that gives up marks the
 // structure's solve failed and sets the batch's error word, and the CTA
 // still waits (bounded) for its copies and products before it frees tensor
 // memory.
 constexpr int T5_M = 128;
 constexpr int T5_N = 64;
 constexpr int T5_STAGES = 3;
-constexpr int T5_THREADS = 128;
+constexpr int T5_THREADS = 512;
+constexpr int T5_COLS_PER_WARP = T5_N / (T5_THREADS / 128);  // 16
 constexpr uint32_t T5_A_BYTES = T5_M * NB * 2;  // one L21 slice of a tile
 constexpr uint32_t T5_B_BYTES = T5_N * NB * 2;  // one U12 slice of a tile
 constexpr uint32_t T5_TMEM_COLS = OZ_S * T5_N;  // 512
@@ -1505,7 +1506,9 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, 
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (tid < T5_N) eU[tid] = o.eU[c0 + tid];
-  const int eLr = o.eL[r0 + tid];  // r0 + 127 < oz_rows
+  const int lg = warp & 3, cq = warp >> 2;      // TMEM lane group, column group
+  const int row = 32 * lg + (tid & 31);         // this thread's row of the tile
+  const int eLr = o.eL[r0 + row];               // r0 + 127 < oz_rows
   t5_fence_before();
   __syncthreads();
   t5_fence_after();
@@ -1556,17 +1559,18 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, 
       if (!okB) t5_wait(fullB, 0);
     }
   }
-  // epilogue: while the products run, every thread loads its row of the
-  // tile's A22 into registers (64 independent loads, so the L2 latency is
-  // paid once, not once per column); then it waits for the products and
-  // reads its row of the accumulators
+  // epilogue: while the products run, every thread loads its part of its
+  // row of the tile's A22 into registers (16 independent loads, so the L2
+  // latency is paid once, not once per column); then it waits for the
+  // products and reads its part of the accumulators
   const int base_row = j0 + nb;
-  const int r = r0 + tid;  // this thread's row of the window
+  const int r = r0 + row;  // this thread's row of the window
   const bool row_live = r < m;
-  double a22[T5_N];
+  const int cb = T5_COLS_PER_WARP * cq;  // first tile column of this thread
+  double a22[T5_COLS_PER_WARP];
 #pragma unroll
-  for (int c = 0; c < T5_N; ++c)
-    a22[c] = (row_live && c0 + c < m) ? w.at(base_row + r, base_row + c0 + c) : 0.0;
+  for (int c = 0; c < T5_COLS_PER_WARP; ++c)
+    a22[c] = (row_live && c0 + cb + c < m) ? w.at(base_row + r, base_row + c0 + cb + c) : 0.0;
   const bool ready = t5_wait(done, 0);
   if (!ready && tid == 0) t5_wait(done, 0);  // once more before tensor memory is freed
   __syncthreads();
@@ -1577,17 +1581,17 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, 
   }
   t5_fence_after();
   if (good) {
-    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16);
 #pragma unroll
-    for (int j = 0; j < T5_N / 8; ++j) {
+    for (int j = 0; j < T5_COLS_PER_WARP / 8; ++j) {
       uint32_t v[OZ_S][8];
 #pragma unroll
-      for (int d = 0; d < OZ_S; ++d) t5_ld8(tl + (uint32_t)(d * T5_N + 8 * j), v[d]);
+      for (int d = 0; d < OZ_S; ++d) t5_ld8(tl + (uint32_t)(d * T5_N + cb + 8 * j), v[d]);
       t5_wait_ld();
       if (!row_live) continue;
 #pragma unroll
       for (int cc = 0; cc < 8; ++cc) {
-        const int c = c0 + 8 * j + cc;
+        const int c = c0 + cb + 8 * j + cc;
         if (c >= m || (part == 2 && r < NB && c < NB)) continue;
         int ci[OZ_S];
 #pragma unroll
@@ -1601,7 +1605,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, 
         const long long T = ((long long)P0 << 32) + ((long long)P1 << 18) + ((long long)P2 << 4) + (long long)P3;
         double dv = (double)T;
         // times 2^(e_i + e_j - 2046 - 53) through the exponent field
-        const int k = eLr + eU[8 * j + cc] - 2046 - 53;
+        const int k = eLr + eU[cb + 8 * j + cc] - 2046 - 53;
         if (dv != 0.0) {
           const long long bits = __double_as_longlong(dv);
           const int e = (int)((bits >> 52) & 0x7FF) + k;
