@@ -933,17 +933,22 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
     A[i][j] = v;
   }
   __syncthreads();
+  // warp 0 forms the pivot's reciprocal and the multipliers of column k
+  // (the FP64 pipe is scarce: one warp, not every thread, computes the
+  // reciprocal); then the 16 x 16 threads update the trailing block, thread
+  // (ty, tx) on rows k + 1 + ty + 16 a and columns k + 1 + tx + 16 c
+  const int tx = tid & 15, ty = tid >> 4;
   for (int k = 0; k < nb; ++k) {
-    double piv = A[k][k];
-    if (tid == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
-    double r = wb_recip(piv);
+    if (tid < 32) {
+      const double piv = A[k][k];
+      if (tid == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
+      const double r = wb_recip(piv);
+      for (int i = k + 1 + tid; i < nb; i += 32) A[i][k] *= r;
+    }
     __syncthreads();
-    for (int i = k + 1 + tid; i < nb; i += blockDim.x) A[i][k] *= r;
-    __syncthreads();
-    int m = nb - k - 1;
-    for (int x = tid; x < m * m; x += blockDim.x) {
-      int i = k + 1 + x % m, j = k + 1 + x / m;
-      A[i][j] -= A[i][k] * A[k][j];
+    for (int i = k + 1 + ty; i < nb; i += 16) {
+      const double l = A[i][k];
+      for (int j = k + 1 + tx; j < nb; j += 16) A[i][j] -= l * A[k][j];
     }
     __syncthreads();
   }
@@ -955,11 +960,14 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
 }
 
 // L21 = A21 U11^-1 (row blocks) and U12 = L11^-1 A12 (column blocks) of
-// panel p.  16 rows (or columns) per CTA, 16 threads each splitting the
-// panel width.  The launch covers blocks blk0 .. blk0 + nblk - 1 of both:
-// blockIdx.x < nblk an L21 row block, else a U12 column block.  The first
-// four blocks (the rows and columns of the next panel's diagonal block) are
-// a launch of their own on the lookahead's critical path; the rest follow.
+// panel p.  TRSM_RB rows (or columns) per CTA, a warp each splitting the
+// panel width; lane 0 forms each multiplier once and the warp reads it from
+// shared memory (the FP64 pipe is scarce).  The launch covers blocks
+// blk0 .. blk0 + nblk - 1 of both: blockIdx.x < nblk an L21 row block, else
+// a U12 column block.  The first blocks (the rows and columns of the next
+// panel's diagonal block) are a launch of their own on the lookahead's
+// critical path; the rest follow.
+constexpr int TRSM_RB = 8;
 __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int nblk) {
   p = wb_panel(b, p);
   if (p < 0) return;
@@ -971,12 +979,12 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);  // rows below / columns right of the panel
   if (m <= 0) return;
-  const int nrb = (m + 15) / 16;
+  const int nrb = (m + TRSM_RB - 1) / TRSM_RB;
   const bool lower = (int)blockIdx.x < nblk;
   const int blk = blk0 + (lower ? (int)blockIdx.x : (int)blockIdx.x - nblk);
   if (blk >= nrb) return;
   __shared__ double T[NB][NB + 1];  // the diagonal block's LU
-  __shared__ double X[16][NB + 1];
+  __shared__ double X[TRSM_RB][NB + 1];
   __shared__ double rd[NB];         // reciprocals of U11's diagonal
   const int tid = threadIdx.x;
   for (int x = tid; x < NB * NB; x += blockDim.x) {
@@ -984,10 +992,10 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
     T[i][j] = (i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
   }
   if (tid < nb) rd[tid] = wb_recip(w.at(j0 + tid, j0 + tid));
-  const int r = tid >> 4, c = tid & 15;  // row (or column) r of the block, lane c of its 16
-  const int g = j0 + nb + blk * 16 + r;  // global row (lower) or column (upper)
+  const int r = tid >> 5, c = tid & 31;  // row (or column) r of the block, lane c
+  const int g = j0 + nb + blk * TRSM_RB + r;  // global row (lower) or column (upper)
   const bool live = g < j0 + nb + m;
-  for (int k = c; k < NB; k += 16) {
+  for (int k = c; k < NB; k += 32) {
     double v = 0.0;
     if (live && k < nb) {
       if (lower) { if (g - (j0 + k) <= w.kl) v = w.at(g, j0 + k); }
@@ -996,27 +1004,25 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
     X[r][k] = v;
   }
   __syncthreads();
-  const unsigned gm = 0xffffu << (16 * ((tid >> 4) & 1));
   if (lower) {
     // x U11 = a: x_k = a_k / u_kk, then a_j -= x_k u_kj (j > k)
     for (int k = 0; k < nb; ++k) {
-      double xk = X[r][k] * rd[k];
-      __syncwarp(gm);
-      for (int j = k + 1 + c; j < nb; j += 16) X[r][j] -= xk * T[k][j];
-      if (c == 0) X[r][k] = xk;
-      __syncwarp(gm);
+      if (c == 0) X[r][k] = X[r][k] * rd[k];
+      __syncwarp();
+      const double xk = X[r][k];
+      for (int j = k + 1 + c; j < nb; j += 32) X[r][j] -= xk * T[k][j];
+      __syncwarp();
     }
   } else {
     // L11 y = a (unit lower): y_k = a_k, then a_i -= l_ik y_k (i > k)
     for (int k = 0; k < nb; ++k) {
-      double yk = X[r][k];
-      __syncwarp(gm);
-      for (int i = k + 1 + c; i < nb; i += 16) X[r][i] -= T[i][k] * yk;
-      __syncwarp(gm);
+      const double yk = X[r][k];
+      for (int i = k + 1 + c; i < nb; i += 32) X[r][i] -= T[i][k] * yk;
+      __syncwarp();
     }
   }
   __syncthreads();
-  for (int k = c; k < nb; k += 16) {
+  for (int k = c; k < nb; k += 32) {
     if (!live || g - (j0 + k) > w.kl) continue;
     if (lower) w.at(g, j0 + k) = X[r][k];
     else w.at(j0 + k, g) = X[r][k];
@@ -1027,8 +1033,8 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
     // maximum over the CTAs is exact and independent of their order
     const int k = tid;
     unsigned long long mx = 0;
-    for (int q = 0; q < 16; ++q) {
-      const int gq = j0 + nb + blk * 16 + q;
+    for (int q = 0; q < TRSM_RB; ++q) {
+      const int gq = j0 + nb + blk * TRSM_RB + q;
       if (gq < j0 + nb + m && gq - (j0 + k) <= w.kl)
         mx = max(mx, (unsigned long long)__double_as_longlong(X[q][k]) & 0x7FFFFFFFFFFFFFFFull);
     }
@@ -1735,9 +1741,9 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
   k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
 }
 
-// Row (column) blocks of 16 in the first trsm launch of a panel: the 64
+// Row (column) blocks of TRSM_RB in the first trsm launch of a panel: the 64
 // rows and columns that the next panel's diagonal block needs.
-constexpr int TRSM_FIRST = NB / 16;
+constexpr int TRSM_FIRST = NB / TRSM_RB;
 
 // Panel loop with lookahead on two helper streams (fork / join by events,
 // so a captured pass keeps the same dependencies):
@@ -1826,7 +1832,7 @@ cudaError_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_
 static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide, mr = sd.max_kl, P = sd.max_panels;
-  const int nrb = (mr + 15) / 16, rb = (mr + 255) / 256;
+  const int nrb = (mr + TRSM_RB - 1) / TRSM_RB, rb = (mr + 255) / 256;
   cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1];
   cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
   if (P <= 0) return cudaSuccess;
@@ -1876,7 +1882,7 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide;
   const int mr = sd.max_kl;  // largest kl over the wide structures
-  const int nrb = (mr + 15) / 16;
+  const int nrb = (mr + TRSM_RB - 1) / TRSM_RB;
   const int rb = (mr + 255) / 256;
   cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1];
   // the helpers fork from the main stream at their first wait and join it
@@ -1983,7 +1989,7 @@ int shell_launches_per_pass(const Batch& b) {
   // LU, the same six or seven kernels and a counter step per forward
   // iteration, and two kernels per backward one
   if (b.sh.n_wide) {
-    const int P = b.sh.max_panels, per = 6 + ((b.sh.max_kl + 15) / 16 > TRSM_FIRST ? 1 : 0);
+    const int P = b.sh.max_panels, per = 6 + ((b.sh.max_kl + TRSM_RB - 1) / TRSM_RB > TRSM_FIRST ? 1 : 0);
     n += (b.sh.loops_in_graph ? 3 + (per + 2) * P : 1 + per * P - 2) +
          (b.sh.wide_tc ? P : 0);  // the tensor-core update's slicing kernel
   }
