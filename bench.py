@@ -63,10 +63,16 @@ def parse():
                     help="timed solves of the mixed-precision leg (0 = skip)")
     ap.add_argument("--shell-n", type=int, default=64,
                     help="squares per side of the plate of the shell leg (64: the 64x64x2 benchmark plate)")
-    ap.add_argument("--shell-steps", type=int, default=2,
-                    help="load steps (of 20) of the 64x64x2 Shell_1 plate leg (0 = skip)")
-    ap.add_argument("--dyn-steps", type=int, default=50,
+    ap.add_argument("--shell-steps", type=int, default=20,
+                    help="load steps (of 20) of the 64x64x2 Shell_1 plate leg (0 = skip); its FP64-FMA and "
+                         "mma.sync comparisons run the first two")
+    ap.add_argument("--dyn-steps", type=int, default=1000,
                     help="time steps (of 1000) of the batched-dynamics leg (0 = skip)")
+    ap.add_argument("--rollup", type=int, default=1, help="time the 20-element roll-up (config 1) (0 = skip)")
+    ap.add_argument("--serve-saturated", type=int, default=1,
+                    help="the 512-chain workload submitted at once through the server (0 = skip)")
+    ap.add_argument("--serve-full-requests", type=int, default=12,
+                    help="requests of the mixed served stream with the full 10k-200k plate range (0 = skip)")
     return ap.parse_args()
 
 
@@ -309,14 +315,22 @@ def shell_leg(ctx, args, fp64_peak):
     L = ctx.L
     s = configs.square_plate(args.shell_n, steps=20)
     s.solution.end_time = args.shell_steps / 20.0
-    # the same steps with the trailing update in FP64 FMA, for comparison
-    bf = gpu.BatchSolver(ctx, [s], ctx.opts(wide_update=gpu.GF_WIDE_FP64))
+    # the first two steps with the trailing update in FP64 FMA and in the
+    # mma.sync form, for comparison
+    s2 = configs.square_plate(args.shell_n, steps=20)
+    s2.solution.end_time = min(args.shell_steps, 2) / 20.0
+    b2 = gpu.BatchSolver(ctx, [s2])
+    b2.reset()
+    ms_tc2 = b2.run()
+    f_tc2, st_tc2 = b2.results()
+    b2.close()
+    bf = gpu.BatchSolver(ctx, [s2], ctx.opts(wide_update=gpu.GF_WIDE_FP64))
     bf.reset()
     ms_fp64 = bf.run()
     st_fp64 = bf.results()[1]
     bf.close()
     # and with the warp-level mma.sync form of the tensor-core update
-    bsy = gpu.BatchSolver(ctx, [s], ctx.opts(wide_update=gpu.GF_WIDE_TENSOR_SYNC))
+    bsy = gpu.BatchSolver(ctx, [s2], ctx.opts(wide_update=gpu.GF_WIDE_TENSOR_SYNC))
     bsy.reset()
     ms_sync = bsy.run()
     f_sync, st_sync = bsy.results()
@@ -381,11 +395,12 @@ def shell_leg(ctx, args, fp64_peak):
                            "TMEM accumulators, bulk-copy (TMA) staged slices",
             "wide_lu_tflops": lu.value / (ms / 1e3) / 1e12, "fp64_peak_tflops": fp64_peak,
             "wide_lu_frac_of_measured_fp64": lu.value / (ms / 1e3) / 1e12 / fp64_peak,
-            "fp64_fma_update": {"ms": ms_fp64, "ms_per_pass": ms_fp64 / max(1, st_fp64[0][1]),
-                                "same_counts": bool(tuple(st_fp64[0]) == tuple(st[0]))},
-            "mma_sync_update": {"ms": ms_sync, "ms_per_pass": ms_sync / max(1, st_sync[0][1]),
-                                "same_counts": bool(tuple(st_sync[0]) == tuple(st[0])),
-                                "max_abs_diff_m": float(np.abs(f_sync[0][:, :3] - fin[0][:, :3]).max())},
+            "first_two_steps": {"tcgen05_ms_per_pass": ms_tc2 / max(1, st_tc2[0][1]),
+                                "fp64_fma_update_ms_per_pass": ms_fp64 / max(1, st_fp64[0][1]),
+                                "mma_sync_update_ms_per_pass": ms_sync / max(1, st_sync[0][1]),
+                                "same_counts": bool(tuple(st_fp64[0]) == tuple(st_tc2[0]) == tuple(st_sync[0])),
+                                "max_abs_diff_m_sync_vs_tcgen05":
+                                    float(np.abs(f_sync[0][:, :3] - f_tc2[0][:, :3]).max())},
             "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
             "pass_split_ms": split,
             "sparse_solve": sparse,
@@ -407,16 +422,93 @@ def dynamics_leg(ctx, args):
         s.solution.end_time = args.dyn_steps * 0.01
     b = gpu.BatchSolver(ctx, structs)
     b.reset()
-    b.run()
-    b.reset()
-    ms = b.run()
+    ms = b.run()  # device time after the pass graph's capture
     _, st = b.results()
     launches = b.launches()
     b.close()
     solves = int(st[:, 0].sum())
-    return {"workload": f"256 pipe chains, 100-1000 elements uniform (seed {args.seed}), Newmark, first "
+    return {"workload": f"256 pipe chains, 100-1000 elements uniform (seed {args.seed}), Newmark, "
                         f"{args.dyn_steps} of 1000 time steps", "newton_solves": solves, "ms": ms,
             "solves_per_s": solves / (ms / 1e3), "aborted": int(st[:, 3].sum()), "gpu_launches": launches}
+
+
+def rollup_leg(ctx):
+    """Config 1: the 20-element cantilever rolled into a circle by a tip
+    moment over 20 load steps (plain FP64 path, one structure), device time
+    after a warm-up run, beside the oracle on one host core."""
+    from giraffe_gb300 import configs, gpu
+    from oracle import oracle
+
+    s = configs.cantilever_rollup(n_el=20, steps=20)
+    b = gpu.BatchSolver(ctx, [s])
+    b.reset()
+    b.run()
+    b.reset()
+    ms = b.run()
+    fin, st = b.results()
+    b.close()
+    t0 = time.perf_counter()
+    fo, so, _ = oracle.solve(s)
+    cpu_s = time.perf_counter() - t0
+    u, uo = fin[0][:, :3] - s.nodes, fo[:, :3] - s.nodes
+    return {"workload": "20 Beam_1 cantilever (246 DOF), tip moment 2 pi EI/L over 20 load steps, FP64",
+            "newton_solves": int(st[0][0]), "newton_passes": int(st[0][1]), "gpu_ms": ms,
+            "gpu_solves_per_s": st[0][0] / (ms / 1e3), "cpu_oracle_ms": cpu_s * 1e3,
+            "cpu_oracle_solves_per_s": so[0] / cpu_s, "cpu_cores": 1,
+            "same_counts": bool(tuple(st[0]) == tuple(so)),
+            "rel_err_vs_oracle": float(np.linalg.norm(u - uo) / np.linalg.norm(uo)),
+            "tip_x_m": float(fin[0][-1, 0])}
+
+
+def served_saturated_leg(ctx, args, structs, plain_value):
+    """Config 2 through the server: all 512 chains submitted at once, the
+    server admitting them in waves under its budget; sustained Newton solves
+    per second from the first submission to the last result, against the
+    plain single-structure path."""
+    from giraffe_gb300 import serve
+
+    srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30)
+    out = serve.run_stream(srv, structs, np.zeros(len(structs)))
+    srv.close()
+    res = out["results"]
+    r = {"workload": f"the {len(structs)}-chain batched-static workload submitted at t = 0 through gf_server_*",
+         "solves_per_s": out["solves"] / out["wall_s"], "wall_s": out["wall_s"],
+         "p50_latency_ms": out["p50_ms"], "p99_latency_ms": out["p99_ms"],
+         "aborted": int(sum(x.stats[3] for x in res))}
+    if plain_value:
+        r["over_plain_single_structure"] = r["solves_per_s"] / plain_value
+    return r
+
+
+def served_full_leg(ctx, args, rank):
+    """Config 5 with the description's full plate range: 70 % pipe chains
+    (1k-50k DOF), 30 % Shell_1 plates of 10k-200k DOF (log-uniform), Poisson
+    arrivals at 200/s.  One GPU cannot sustain the plates' share of the
+    offered load; the leg reports what it sustains and the queueing."""
+    from giraffe_gb300 import configs, serve
+
+    seed = args.seed + 4000 + rank
+    reqs = configs.served_mixed(args.serve_full_requests, seed=seed, plate_dof=(10000, 200000))
+    arrivals = serve.poisson_arrivals(len(reqs), args.serve_rate, seed=seed)
+    srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30)
+    out = serve.run_stream(srv, reqs, arrivals, timeout_s=1200.0)
+    srv.close()
+    res = out["results"]
+    is_plate = np.array([bool(s.shells) for s in reqs])
+    lat = out["latency_ms"]
+    dofs = [int(s.n_free) for s in reqs]
+    return {"workload": f"{len(reqs)} requests: {int((~is_plate).sum())} pipe chains 1k-50k DOF and "
+                        f"{int(is_plate.sum())} Shell_1 plates of 10k-200k DOF (largest "
+                        f"{max([d for d, p in zip(dofs, is_plate) if p], default=0)}), 10 load steps each, "
+                        f"Poisson arrivals at {args.serve_rate:g}/s",
+            "p50_latency_ms": out["p50_ms"], "p99_latency_ms": out["p99_ms"],
+            "chain_p50_ms": float(np.percentile(lat[~is_plate], 50)) if (~is_plate).any() else None,
+            "plate_p50_ms": float(np.percentile(lat[is_plate], 50)) if is_plate.any() else None,
+            "plate_max_ms": float(lat[is_plate].max()) if is_plate.any() else None,
+            "solves_per_s": out["solves_per_s"], "requests_per_s": out["requests_per_s"], "wall_s": out["wall_s"],
+            "offered_requests_per_s": args.serve_rate,
+            "mean_queued_ms": float(np.mean([r.queued_ms for r in res])),
+            "aborted": int(sum(r.stats[3] for r in res))}
 
 
 def served_leg(ctx, args, rank):
@@ -597,6 +689,10 @@ def run_ours(args, rank, world):
     if args.serve_requests > 0:
         serving = served_leg(ctx, args, rank)
     serving_mixed = served_mixed_leg(ctx, args, rank) if args.serve_mixed_requests > 0 else None
+    serving_full = served_full_leg(ctx, args, rank) if args.serve_full_requests > 0 else None
+    saturated = (served_saturated_leg(ctx, args, structs, plain["value"] if plain else None)
+                 if args.serve_saturated else None)
+    rollup = rollup_leg(ctx) if args.rollup else None
     cpu = None
     parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -634,6 +730,9 @@ def run_ours(args, rank, world):
                 "dynamics": dyn,
                 "serving": serving,
                 "serving_mixed": serving_mixed,
+                "serving_full_plate_range": serving_full,
+                "serving_saturated_config2": saturated,
+                "rollup_config1": rollup,
                 "cpu_baseline": cpu,
                 "parity_vs_oracle": parity}
         print(json.dumps(line), flush=True)

@@ -946,10 +946,26 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
       for (int i = k + 1 + tid; i < nb; i += 32) A[i][k] *= r;
     }
     __syncthreads();
-    for (int i = k + 1 + ty; i < nb; i += 16) {
-      const double l = A[i][k];
-      for (int j = k + 1 + tx; j < nb; j += 16) A[i][j] -= l * A[k][j];
+    // thread (ty, tx) owns rows ty + 16 a and columns tx + 16 c of the block;
+    // every operand is loaded before any store, so the 16 updates are
+    // independent and only the FP64 pipe bounds them
+    double l[4], u[4], v[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      l[q] = A[ty + 16 * q][k];
+      u[q] = A[k][tx + 16 * q];
     }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) v[a][c] = A[ty + 16 * a][tx + 16 * c];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int i = ty + 16 * a, j = tx + 16 * c;
+        if (i > k && j > k && i < nb && j < nb) A[i][j] = fma(-l[a], u[c], v[a][c]);
+      }
     __syncthreads();
   }
   for (int x = tid; x < nb * nb; x += blockDim.x) {
