@@ -22,6 +22,10 @@
   T ~ U(5, 15) s (tabulated at every time step, so exact at step times), its
   rotations held; bottom free.  E = 210 GPa and 0.5 m elements (chains of
   50-500 m) are this generator's choices; the description fixes neither.
+* :func:`pipe_riser` — Pipe_1 elements (PipeSection of a steel tube) pinned
+  at the bottom, the top driven laterally as in :func:`riser_chain`, under
+  an internal pressure (PipeLoad) raised over the first quarter of the run;
+  Newmark dynamics.
 
 Every generator is deterministic in its seed (numpy default_rng).
 """
@@ -31,8 +35,8 @@ import math
 
 import numpy as np
 
-from .model import (GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PressureLoad, Solution, Structure,
-                    Table)
+from .model import (GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PipeLoad, PressureLoad, Solution,
+                    Structure, Table)
 
 E_STEEL = 210e9
 NU_STEEL = 0.3
@@ -209,6 +213,37 @@ def riser_chain(n_el: int, De: float, wall: float, amp: float, period: float, st
     vals = np.zeros((steps + 1, 6))
     vals[:, 0] = amp * np.sin(2.0 * math.pi * t / period)
     s.displacements.append(NodalDisplacement([top], cs, Table(t, vals)))
+    s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 64, 20, 3, 4, 1.0, beta=0.25, gamma=0.5,
+                          rayleigh_alpha=rayleigh_alpha, rayleigh_beta=rayleigh_beta, update_rayleigh=update_rayleigh)
+    s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, force_min=1.0, moment_min=1.0)
+    return s
+
+
+def pipe_riser(n_el: int = 16, De: float = 0.3, wall: float = 0.02, amp: float = 0.5, period: float = 2.0,
+               pressure: float = 2e7, steps: int = 100, dt: float = 0.01, element_length: float = 1.0,
+               tol: float = 1e-8, rayleigh_alpha: float = 0.0, rayleigh_beta: float = 0.0,
+               update_rayleigh: int = 0) -> Structure:
+    L = n_el * element_length
+    s = Structure(nodes=straight_chain(n_el, L, (0.0, 0.0, 1.0)))
+    Di = De - 2.0 * wall
+    A = math.pi / 4.0 * (De * De - Di * Di)
+    I = math.pi / 64.0 * (De ** 4 - Di ** 4)
+    G = E_STEEL / (2.0 * (1.0 + NU_STEEL))
+    ps = s.add_pipe_section(E_STEEL * A, E_STEEL * I, G * 2.0 * I, G * A, RHO_STEEL * A, De, Di)
+    cs = s.add_cs((1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+    for e in range(n_el):
+        s.add_pipe(2 * e, 2 * e + 1, 2 * e + 2, ps, cs)
+    s.clamp(0, (1, 1, 1, 0, 0, 0))
+    top = 2 * n_el
+    s.clamp(top)
+    t = np.arange(steps + 1) * dt
+    vals = np.zeros((steps + 1, 6))
+    vals[:, 0] = amp * np.sin(2.0 * math.pi * t / period)
+    s.displacements.append(NodalDisplacement([top], cs, Table(t, vals)))
+    ramp = max(steps // 4, 1) * dt
+    s.loads.append(PipeLoad(list(range(n_el)), Table(np.array([0.0, ramp, steps * dt]),
+                                                     np.array([[0.0] * 4, [pressure, 0, 0, 0],
+                                                               [pressure, 0, 0, 0]]))))
     s.solution = Solution(GF_DYNAMIC, 0.0, steps * dt, dt, dt, dt / 64, 20, 3, 4, 1.0, beta=0.25, gamma=0.5,
                           rayleigh_alpha=rayleigh_alpha, rayleigh_beta=rayleigh_beta, update_rayleigh=update_rayleigh)
     s.criteria.update(force_tol=tol, moment_tol=tol, disp_tol=tol, rot_tol=tol, force_min=1.0, moment_min=1.0)

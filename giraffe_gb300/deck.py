@@ -11,16 +11,21 @@ solution steps:
                   NewmarkCoefficients, optional ZeroIC)
   Nodes           Node id x y z
   Elements        Beam_1 id Mat Sec CS Nodes a b c [PreTension p]
-                  (src/Beam_1.cpp:371-430); Shell_1 id Mat Sec [CS] Nodes
+                  (src/Beam_1.cpp:371-430); Pipe_1 id PipeSec CS Nodes a b c
+                  (src/Pipe_1.cpp:535-572); Shell_1 id Mat Sec [CS] Nodes
                   six ids (src/Shell_1.cpp:538-590)
   Materials       Hooke id E Nu Rho
   Sections        Rectangle id B H; Tube id De Di
+  PipeSections    PS id EA EI GJ GA Rho CDt CDn CAt CAn De Di
+                  (src/PipeSection.cpp:19-131)
   ShellSections   Homogeneous id Thickness
   CoordinateSystems  CS id E1 x y z E3 x y z
   NodeSets / ElementSets  List ids | Sequence Initial i Increment d
                   (src/NodeSet.cpp:30-95)
   Loads           NodalLoad id NodeSet CS NTimes n + n rows (t, 6 values);
-                  ShellLoad id ElementSet AreaUpdate NTimes n + n rows (t, p)
+                  ShellLoad id ElementSet AreaUpdate NTimes n + n rows (t, p);
+                  PipeLoad id ElementSet NTimes n + n rows (t, P0I, P0E,
+                  RhoI, RhoE) (src/PipeLoad.cpp:45-88)
   Displacements   NodalDisplacement id NodeSet CS [AngularParameters
                   EulerAngles | EulerVector] [BoolTable ...] NTimes n + n rows
                   (src/NodalDisplacement.cpp:40-120)
@@ -39,8 +44,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PressureLoad, Solution,
-                    Structure, Table)
+from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PipeLoad, PressureLoad,
+                    Solution, Structure, Table)
 
 # Every top-level keyword of IO::ReadFile: a block reader stops at the next one.
 TOP = {
@@ -173,7 +178,7 @@ def read_deck(text: str, step: int = None) -> Structure:
     later steps on their own raise DeckError (only the first starts from the
     undeformed configuration)."""
     tk = _Tokens(text)
-    steps, nodes, elems, mats, secs, shell_secs, css = [], {}, [], {}, {}, {}, {}
+    steps, nodes, elems, mats, secs, shell_secs, css, pipe_secs = [], {}, [], {}, {}, {}, {}, {}
     node_sets, elem_sets, loads, disps, cons = {}, {}, [], [], []
     criteria = dict(DEFAULT_CRITERIA)
     while tk.more():
@@ -213,6 +218,14 @@ def read_deck(text: str, step: int = None) -> Structure:
                         tk.next()
                         t0 = tk.float()
                     elems.append(("Beam_1", eid, m, sc, c, nd, t0))
+                elif kind == "Pipe_1":
+                    tk.expect("PipeSec")
+                    ps = tk.int()
+                    tk.expect("CS")
+                    c = tk.int()
+                    tk.expect("Nodes")
+                    nd = [tk.int() for _ in range(3)]
+                    elems.append(("Pipe_1", eid, None, ps, c, nd, 0.0))
                 elif kind == "Shell_1":
                     tk.expect("Mat")
                     m = tk.int()
@@ -255,6 +268,15 @@ def read_deck(text: str, step: int = None) -> Structure:
                     secs[i] = ("tube", de, tk.float())
                 else:
                     raise DeckError(f"section '{kind}' is not supported")
+        elif kw == "PipeSections":
+            for _ in range(tk.int()):
+                tk.expect("PS")
+                i = tk.int()
+                row = {}
+                for name in ("EA", "EI", "GJ", "GA", "Rho", "CDt", "CDn", "CAt", "CAn", "De", "Di"):
+                    tk.expect(name)
+                    row[name] = tk.float()
+                pipe_secs[i] = row
         elif kw == "ShellSections":
             for _ in range(tk.int()):
                 kind = tk.next()
@@ -299,6 +321,12 @@ def read_deck(text: str, step: int = None) -> Structure:
                     if tk.next() != "NTimes":
                         raise DeckError("ShellLoad: only tabulated pressures (NTimes) are supported")
                     loads.append(("shell", es, au, _table(tk, tk.int(), 1)))
+                elif kind == "PipeLoad":
+                    tk.expect("ElementSet")
+                    es = tk.int()
+                    if tk.next() != "NTimes":
+                        raise DeckError("PipeLoad: only tabulated pressures (NTimes) are supported")
+                    loads.append(("pipe", es, 0, _table(tk, tk.int(), 4)))
                 else:
                     raise DeckError(f"load '{kind}' is not supported")
         elif kw == "Displacements":
@@ -352,11 +380,11 @@ def read_deck(text: str, step: int = None) -> Structure:
         else:
             raise DeckError(f"unknown keyword '{kw}' (token {tk.i})")
     return _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, elem_sets, loads, disps, cons,
-                  criteria)
+                  criteria, pipe_secs)
 
 
 def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, elem_sets, loads, disps, cons,
-           criteria) -> Structure:
+           criteria, pipe_secs=None) -> Structure:
     if not steps:
         raise DeckError("the deck has no solution step")
     if step is not None:
@@ -380,17 +408,26 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
         sec_ix[i] = s.add_rectangle(x, y) if kind == "rect" else s.add_tube(x, y)
     ssec_ix = {i: s.add_shell_section(shell_secs[i]) for i in sorted(shell_secs)}
     cs_ix = {i: s.add_cs(*css[i]) for i in sorted(css)}
+    pipe_secs = pipe_secs or {}
+    psec_ix = {}
+    for i in sorted(pipe_secs):
+        r = pipe_secs[i]
+        psec_ix[i] = s.add_pipe_section(r["EA"], r["EI"], r["GJ"], r["GA"], r["Rho"], r["De"], r["Di"],
+                                        r["CDt"], r["CDn"], r["CAt"], r["CAn"])
 
     def lookup(table, i, what):
         if i not in table:
             raise DeckError(f"{what} {i} is not defined")
         return table[i]
 
-    shell_of = {}
+    shell_of, pipe_of = {}, {}
     for kind, eid, m, sc, c, nd, t0 in sorted(elems, key=lambda e: e[1]):
         if any(n not in nodes for n in nd):
             raise DeckError(f"element {eid} refers to a missing node")
-        if kind == "Beam_1":
+        if kind == "Pipe_1":
+            pipe_of[eid] = s.add_pipe(nd[0] - 1, nd[1] - 1, nd[2] - 1, lookup(psec_ix, sc, "pipe section"),
+                                      lookup(cs_ix, c, "coordinate system"))
+        elif kind == "Beam_1":
             if t0 != 0.0:
                 s.pretension[len(s.beams)] = t0
             s.beams.append((nd[0] - 1, nd[1] - 1, nd[2] - 1, lookup(mat_ix, m, "material"),
@@ -411,6 +448,12 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
             _, ns, c, table = ld
             s.loads.append(NodalLoad([n - 1 for n in lookup(node_sets, ns, "node set")],
                                      lookup(cs_ix, c, "coordinate system"), table))
+        elif ld[0] == "pipe":
+            _, es, _, table = ld
+            members = lookup(elem_sets, es, "element set")
+            if any(e not in pipe_of for e in members):
+                raise DeckError(f"PipeLoad on element set {es}: every element must be a Pipe_1")
+            s.loads.append(PipeLoad([pipe_of[e] for e in members], table))
         else:
             _, es, au, table = ld
             members = lookup(elem_sets, es, "element set")

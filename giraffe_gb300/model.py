@@ -24,7 +24,7 @@ import numpy as np
 PI = 3.1415926535897932384626433832795
 
 GF_STATIC, GF_DYNAMIC = 0, 1
-GF_LOAD_NODAL, GF_LOAD_SHELL_PRESSURE = 0, 1
+GF_LOAD_NODAL, GF_LOAD_SHELL_PRESSURE, GF_LOAD_PIPE_PRESSURE = 0, 1, 2
 
 
 # --------------------------------------------------------------------------
@@ -101,7 +101,8 @@ class gf_model_desc(C.Structure):
                 ("n_loads", C.c_int), ("loads", _vp),
                 ("n_displacements", C.c_int), ("displacements", _vp),
                 ("solution", gf_solution), ("criteria", gf_criteria), ("beam_pretension", _vp),
-                ("n_next_steps", C.c_int), ("next_steps", _vp)]
+                ("n_next_steps", C.c_int), ("next_steps", _vp),
+                ("n_pipe_sections", C.c_int), ("pipe_sections", _vp), ("beam_pipe_section", _vp)]
 
 
 def _r(v):
@@ -203,6 +204,15 @@ class PressureLoad:
 
 
 @dataclass
+class PipeLoad:
+    """PipeLoad (reference src/PipeLoad.cpp): pressure on Pipe_1 elements
+    (beam indices); table columns P0I P0E RhoI RhoE, of which the internal
+    pressure P0I acts on the section's internal area."""
+    pipes: list
+    table: Table
+
+
+@dataclass
 class NodalDisplacement:
     nodes: list
     cs: int
@@ -254,6 +264,10 @@ class Structure:
     next_steps: list = field(default_factory=list)     # Solution steps run after `solution`
     criteria: dict = field(default_factory=lambda: dict(DEFAULT_CRITERIA))
     pretension: dict = field(default_factory=dict)     # beam index -> Beam_1 PreTension T0
+    # Pipe_1: PipeSection rows (EA, EI, GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di)
+    # and the pipe section of each beam that is a Pipe_1 element
+    pipe_sections: list = field(default_factory=list)
+    pipe_of: dict = field(default_factory=dict)        # beam index -> pipe section
 
     def __setattr__(self, name, value):
         # element rows assigned as lists become ElementTables
@@ -275,6 +289,17 @@ class Structure:
         self.sections.append(section_tube(De, Di))
         self.section_decks.append(f"Tube\t{len(self.sections)}\tDe\t{_r(De)}\tDi\t{_r(Di)}")
         return len(self.sections) - 1
+
+    def add_pipe_section(self, EA, EI, GJ, GA, Rho, De, Di, CDt=0.0, CDn=0.0, CAt=0.0, CAn=0.0):
+        self.pipe_sections.append(tuple(float(v) for v in (EA, EI, GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di)))
+        return len(self.pipe_sections) - 1
+
+    def add_pipe(self, n0, n1, n2, pipe_section, cs):
+        """A Pipe_1 element: Beam_1 kinematics with the pipe section's
+        stiffness and mass; its material and section columns are -1."""
+        self.pipe_of[len(self.beams)] = int(pipe_section)
+        self.beams.append((n0, n1, n2, -1, -1, cs))
+        return len(self.beams) - 1
 
     def add_shell_section(self, thickness):
         self.shell_sections.append(float(thickness))
@@ -340,6 +365,10 @@ class Structure:
         k = 0
         for e, b in enumerate(self.beams):
             k += 1
+            if e in self.pipe_of:
+                o.append(f"Pipe_1\t{k}\tPipeSec\t{self.pipe_of[e] + 1}\tCS\t{b[5] + 1}\tNodes\t"
+                         f"{b[0] + 1}\t{b[1] + 1}\t{b[2] + 1}")
+                continue
             t0 = float(self.pretension.get(e, 0.0))
             o.append(f"Beam_1\t{k}\tMat\t{b[3] + 1}\tSec\t{b[4] + 1}\tCS\t{b[5] + 1}\tNodes\t"
                      f"{b[0] + 1}\t{b[1] + 1}\t{b[2] + 1}" + (f"\tPreTension\t{_r(t0)}" if t0 != 0.0 else ""))
@@ -347,12 +376,18 @@ class Structure:
             k += 1
             nodes = "\t".join(str(v + 1) for v in sh[:6])
             o.append(f"Shell_1\t{k}\tMat\t{sh[6] + 1}\tSec\t{sh[7] + 1}\tCS\t{sh[8] + 1}\tNodes\t{nodes}")
-        o.append(f"Materials\t{len(self.materials)}")
+        if self.materials:
+            o.append(f"Materials\t{len(self.materials)}")
         for i, (E, nu, rho) in enumerate(self.materials):
             o.append(f"Hooke\t{i + 1}\tE\t{_r(E)}\tNu\t{_r(nu)}\tRho\t{_r(rho)}")
         if self.sections:
             o.append(f"Sections\t{len(self.section_decks)}")
             o.extend(self.section_decks)
+        if self.pipe_sections:
+            o.append(f"PipeSections\t{len(self.pipe_sections)}")
+            names = ("EA", "EI", "GJ", "GA", "Rho", "CDt", "CDn", "CAt", "CAn", "De", "Di")
+            for i, row in enumerate(self.pipe_sections):
+                o.append(f"PS\t{i + 1}\t" + "\t".join(f"{n}\t{_r(v)}" for n, v in zip(names, row)))
         if self.shell_sections:
             o.append(f"ShellSections\t{len(self.shell_sections)}")
             for i, t in enumerate(self.shell_sections):
@@ -383,6 +418,12 @@ class Structure:
                 rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
                                  for t, vals in zip(L.table.times, L.table.values))
                 load_lines.append(f"NodalLoad\t{len(load_lines) + 1}\tNodeSet\t{ns}\tCS\t{L.cs + 1}"
+                                  f"\tNTimes\t{len(L.table.times)}\n{rows}")
+            elif isinstance(L, PipeLoad):
+                rows = "\n".join("\t".join(repr(float(v)) for v in (t, *vals))
+                                  for t, vals in zip(L.table.times, L.table.values))
+                elem_sets.append(list(L.pipes))
+                load_lines.append(f"PipeLoad\t{len(load_lines) + 1}\tElementSet\t{len(elem_sets)}"
                                   f"\tNTimes\t{len(L.table.times)}\n{rows}")
             else:
                 rows = "\n".join(f"{_r(float(t))}\t{_r(float(v[0]))}"
@@ -456,10 +497,13 @@ class DescHandle:
         cons = i(s.constraints) if s.constraints is not None else None
         loads = (gf_load * max(1, len(s.loads)))()
         for k, L in enumerate(s.loads):
-            items = i(np.asarray(L.nodes if isinstance(L, NodalLoad) else L.shells))
+            kind = (GF_LOAD_NODAL if isinstance(L, NodalLoad) else
+                    GF_LOAD_PIPE_PRESSURE if isinstance(L, PipeLoad) else GF_LOAD_SHELL_PRESSURE)
+            items = i(np.asarray(L.nodes if kind == GF_LOAD_NODAL else
+                                 L.pipes if kind == GF_LOAD_PIPE_PRESSURE else L.shells))
             tt = d(L.table.times)
             tv = d(np.asarray(L.table.values, dtype=np.float64).reshape(len(tt), -1))
-            loads[k].type = GF_LOAD_NODAL if isinstance(L, NodalLoad) else GF_LOAD_SHELL_PRESSURE
+            loads[k].type = kind
             loads[k].n_items = len(items)
             loads[k].items = _ptr(items, _ip)
             loads[k].cs = L.cs if isinstance(L, NodalLoad) else 0
@@ -492,12 +536,20 @@ class DescHandle:
             for e, t0 in s.pretension.items():
                 pre[int(e)] = float(t0)
             self.keep.append(pre)
+        psec, bps = None, None
+        if s.pipe_of:
+            psec = d(np.asarray(s.pipe_sections, dtype=np.float64).reshape(-1, 11))
+            bps = np.full(max(1, len(s.beams)), -1, dtype=np.int32)
+            for e, p in s.pipe_of.items():
+                bps[int(e)] = int(p)
+            self.keep.append(bps)
         self.desc = gf_model_desc(
             len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
             len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
             len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), C.addressof(loads),
             len(s.displacements), C.addressof(disps), sol, crit, _ptr(pre), len(s.next_steps),
-            C.addressof(nxt) if s.next_steps else None)
+            C.addressof(nxt) if s.next_steps else None,
+            len(psec) if psec is not None else 0, _ptr(psec, _dp), _ptr(bps, _ip))
 
     @property
     def ref(self):

@@ -18,7 +18,7 @@ extern "C" {
 #endif
 
 enum { GF_STATIC = 0, GF_DYNAMIC = 1 };
-enum { GF_LOAD_NODAL = 0, GF_LOAD_SHELL_PRESSURE = 1 };
+enum { GF_LOAD_NODAL = 0, GF_LOAD_SHELL_PRESSURE = 1, GF_LOAD_PIPE_PRESSURE = 2 };
 
 /* A time table (reference src/Table.cpp:73-102: piecewise linear, clamped
  * to the first/last row outside its range).  values is [n_times][n_cols]. */
@@ -33,7 +33,10 @@ typedef struct gf_table {
  * coordinate system cs, split evenly over the nodes of the set, six table
  * columns (FX FY FZ MX MY MZ).  ShellLoad (reference src/ShellLoad.cpp:133-148
  * and src/Shell_1.cpp:1392-1467): follower pressure on a set of Shell_1
- * elements, one table column. */
+ * elements, one table column.  PipeLoad (reference src/PipeLoad.cpp,
+ * src/Pipe_1.cpp:1441-1494): pressure on a set of Pipe_1 elements (items are
+ * beam indices of Pipe_1 elements), four table columns P0I P0E RhoI RhoE, of
+ * which the internal pressure P0I acts (on the section's internal area). */
 typedef struct gf_load {
   int type;            /* GF_LOAD_NODAL or GF_LOAD_SHELL_PRESSURE */
   int n_items;         /* nodes (nodal) or shell elements (pressure) */
@@ -122,6 +125,16 @@ typedef struct gf_model_desc {
    * displacements apply to every step. */
   int n_next_steps;
   const gf_solution* next_steps;
+  /* Pipe_1 elements (reference src/Pipe_1.cpp): Beam_1's kinematics with a
+   * PipeSection's stiffness and mass (src/Pipe_1.cpp:1106-1156) and PipeLoad
+   * pressures.  A Pipe_1 element is an entry of `beams` whose
+   * beam_pipe_section is >= 0: its material and section columns are not read,
+   * its stiffness is D = diag(GA, GA, EA, EI, EI, GJ), its mass Rho per unit
+   * length and its rotary inertia Rho ((De/2)^2 - (Di/2)^2) diag(1/4, 1/4,
+   * 1/2). */
+  int n_pipe_sections;
+  const double* pipe_sections;   /* [n][11]: EA, EI, GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di */
+  const int* beam_pipe_section;  /* [n_beams]: -1 for Beam_1, else the pipe section; or NULL */
 } gf_model_desc;
 
 #ifdef __cplusplus

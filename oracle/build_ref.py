@@ -27,12 +27,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 OBJ = os.path.join(OUT, "obj")
 
-# Reference translation units of the implicit Beam_1/Shell_1 path.
+# Reference translation units of the implicit Beam_1/Pipe_1/Shell_1 path.
 SOURCES = [
     "Matrix", "Beam_1", "Shell_1", "Node", "LagrangeSave", "Hooke", "SecTube", "SecRectangle",
     "ShellSectionHomogeneous", "CoordinateSystem", "Table", "Static", "Dynamic", "Solution",
     "ConvergenceCriteria", "NodalLoad", "NodalConstraint", "NodeSet", "ElementSet", "BoolTable", "Load",
-    "Element", "NodalDisplacement", "ShellLoad", "SolverOptions", "SolidSection",
+    "Element", "NodalDisplacement", "ShellLoad", "SolverOptions", "SolidSection", "Pipe_1", "PipeSection",
+    "PipeLoad",
 ]
 
 CXXFLAGS = ["-std=c++14", "-O2", "-fPIC", "-fpermissive", "-w", "-fno-fast-math",

@@ -50,6 +50,12 @@ int oracle_solve_batch(int n, const gf_model_desc* models, double** final_nodes,
 int oracle_beam_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
                         int n_hist, const double* hist_disp, const double* disp18, double* K, double* f);
 
+/* One Pipe_1 element: as oracle_beam_element with a pipe section (EA, EI,
+ * GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di) and, when p0i != 0, the
+ * internal-pressure load of MountPipeSpecialLoads added to K and f. */
+int oracle_pipe_element(const double* xyz9, const double* ps11, const double* cs6, int n_hist,
+                        const double* hist_disp, const double* disp18, double p0i, double* K, double* f);
+
 /* One Shell_1 element: PreCalc from nodal coordinates (6x3), material
  * (E, nu, rho) and thickness; n_hist committed increments (each 27 values in
  * element DOF order: translations of nodes 1..6, rotations of nodes 4..6)

@@ -24,6 +24,7 @@ def lib():
         _lib.oracle_solve_batch.argtypes = [C.c_int, C.c_void_p, C.POINTER(dp), ip, C.c_int]
         _lib.oracle_beam_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         _lib.oracle_first_tangent.argtypes = [C.c_void_p, dp, dp, ip]
+        _lib.oracle_pipe_element.argtypes = [dp, dp, dp, C.c_int, dp, dp, C.c_double, dp, dp]
         _lib.oracle_shell_element.argtypes = [dp, dp, C.c_double, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int,
                                               dp, dp]
         _lib.oracle_beam_inertia_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double,
@@ -57,7 +58,8 @@ def solve(structure, record_cap: int = 0):
         nodes = np.zeros((record_cap, structure.n_nodes, 15))
         gq = np.zeros((record_cap, max(1, len(structure.beams)), 2, 9))
         rec = Record(record_cap, 0, _dp(t), it.ctypes.data_as(C.POINTER(C.c_int)), _dp(nodes), _dp(gq))
-    lib().oracle_solve(C.cast(h.ref, C.c_void_p), C.byref(rec) if rec else None, _dp(final), stats)
+    if lib().oracle_solve(C.cast(h.ref, C.c_void_p), C.byref(rec) if rec else None, _dp(final), stats) < 0:
+        raise ValueError("oracle: invalid structure description")
     if rec:
         n = rec.n
         rd = dict(time=t[:n], iterations=it[:n], nodes=nodes[:n], gp_Q=gq[:n])
@@ -85,6 +87,19 @@ def beam_element(xyz9, mat3, sec6, cs6, hist_disp, disp18):
     args = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz9, mat3, sec6, cs6, disp18)]
     lib().oracle_beam_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), _dp(args[3]), nh, _dp(hd),
                               _dp(args[4]), _dp(K), _dp(f))
+    return K.reshape(18, 18).T, f  # row-major [r][s]
+
+
+def pipe_element(xyz9, ps11, cs6, hist_disp, disp18, p0i=0.0):
+    """One Pipe_1 element with an internal pressure p0i
+    (oracle_pipe_element): K row-major [r][s], f."""
+    K = np.zeros(324)
+    f = np.zeros(18)
+    nh = 0 if hist_disp is None else len(hist_disp)
+    hd = np.ascontiguousarray(hist_disp if nh else np.zeros((1, 18)), dtype=np.float64)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (xyz9, ps11, cs6, disp18)]
+    lib().oracle_pipe_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), nh, _dp(hd), _dp(args[3]), float(p0i),
+                              _dp(K), _dp(f))
     return K.reshape(18, 18).T, f  # row-major [r][s]
 
 

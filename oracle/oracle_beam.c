@@ -437,3 +437,132 @@ void oracle_beam_modal_mass(const ob_const* c, const ob_hist* h, double* M) {
         for (int j = 0; j < 3; ++j) M[(3 * bi + i) + 18 * (3 * bj + j)] = blk[i * 3 + j];
     }
 }
+
+/* Pipe_1::PreCalc (reference src/Pipe_1.cpp:1106-1156): Beam_1's geometry
+ * and shape functions with the PipeSection's constitutive matrix
+ * diag(GA, GA, EA, EI, EI, GJ), mass Rho per unit length and rotary
+ * inertia Rho ((De/2)^2 - (Di/2)^2) diag(1/4, 1/4, 1/2).  ps: EA, EI, GJ,
+ * GA, Rho, CDt, CDn, CAt, CAn, De, Di. */
+void oracle_pipe_precalc(const double* x0, const double* x2, const double* ps, const double* cs, ob_const* c,
+                         ob_hist* h) {
+  /* the geometry as Beam_1 without pre-tension; then the pipe's constants */
+  const double unit_mat[3] = {1.0, 0.0, 0.0}, unit_sec[6] = {1.0, 1.0, 1.0, 0.0, 1.0, 1.0};
+  oracle_beam_precalc(x0, x2, unit_mat, unit_sec, cs, 0.0, c, h);
+  const double EA = ps[0], EI = ps[1], GJ = ps[2], GA = ps[3], Rho = ps[4], De = ps[9], Di = ps[10];
+  memset(c->D, 0, sizeof(c->D));
+  c->D[0 * 6 + 0] = GA;
+  c->D[1 * 6 + 1] = GA;
+  c->D[2 * 6 + 2] = EA;
+  c->D[3 * 6 + 3] = EI;
+  c->D[4 * 6 + 4] = EI;
+  c->D[5 * 6 + 5] = GJ;
+  c->Mr = Rho;
+  m3_zero(c->Jr);
+  const double rr = (De / 2.0) * (De / 2.0) - (Di / 2.0) * (Di / 2.0);
+  c->Jr[0] = (Rho * rr / 4.0);
+  c->Jr[4] = (Rho * rr / 4.0);
+  c->Jr[8] = (Rho * rr / 2.0);
+}
+
+/* MountPipeSpecialLoads (reference src/Pipe_1.cpp:1441-1494): the internal
+ * pressure p0i on the internal area Aint of a Pipe_1 element at the current
+ * iterate.  At each Gauss point, with Q = Q_delta Q_i, k = Q kappa_r and
+ * e3 = Q e3r (local frame): the load f = -p0i Aint (k x e3), the moment
+ * m = -p0i Aint Xi^T (z' x e3), and the load stiffness Kext (6 x 12, on
+ * (u, alpha, u', alpha')).  P -= jac T^T N^T (f, m); K -= jac p0i Aint
+ * T^T N^T Kext Upsilon T.  K is 18x18 column-major, global frame. */
+void oracle_pipe_pressure(const ob_const* c, const ob_hist* h, const double* d, double p0i, double Aint, double* K,
+                          double* f) {
+  const double mult = 1.0 * c->jac;
+  /* The reference's O1 term reads the element's scalar member g, which
+   * Pipe_1::Mount leaves at the value of its last Gauss point
+   * (src/Pipe_1.cpp:890): both Gauss points use g of the second. */
+  gp_kin k1;
+  beam_gp_kinematics(c, h, d, 1, &k1);
+  const double g_last = k1.g;
+  for (int g = 0; g < 2; ++g) {
+    gp_kin k;
+    beam_gp_kinematics(c, h, d, g, &k);
+    double Q[9];
+    m3_transpose(Q, k.Qt);
+    double kip[3], e3ip[3];
+    m3_vec(kip, Q, k.kappa);
+    m3_vec(e3ip, Q, c->e3r);
+    const double pa = -p0i * Aint;
+    double cr[3], t1[3], tl[6];
+    v3_cross(cr, kip, e3ip);
+    for (int i = 0; i < 3; ++i) tl[i] = pa * cr[i];
+    v3_cross(cr, k.dz, e3ip);
+    m3_tvec(t1, k.Xi, cr);
+    for (int i = 0; i < 3; ++i) tl[3 + i] = pa * t1[i];
+    double E3[9], Kp[9];
+    m3_skew(E3, e3ip);
+    m3_skew(Kp, kip);
+    /* O1 = -0.5 g (Xi^T (e3 x z') alpha^T - skew(e3 x z')), g of the last
+   * Gauss point */
+    double c2[3], w[3], S2[9], O1[9];
+    v3_cross(c2, e3ip, k.dz);
+    m3_tvec(w, k.Xi, c2);
+    m3_skew(S2, c2);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) O1[i * 3 + j] = -0.5 * g_last * (w[i] * k.alpha[j] - S2[i * 3 + j]);
+    /* K1ua = Kp E3 Xi + E3 dXi - E3 Kp Xi; K1aa = O1 + Xi^T dZ E3 Xi;
+     * K2ua = E3 Xi; K2au = Xi^T E3 */
+    double a1[9], a2[9], K1ua[9], K1aa[9], K2ua[9], K2au[9];
+    m3_mul(a1, Kp, E3);
+    m3_mul(K1ua, a1, k.Xi);
+    m3_mul(a2, E3, k.dXi);
+    for (int q = 0; q < 9; ++q) K1ua[q] += a2[q];
+    m3_mul(a1, E3, Kp);
+    m3_mul(a2, a1, k.Xi);
+    for (int q = 0; q < 9; ++q) K1ua[q] -= a2[q];
+    m3_mul(a1, k.dZ, E3);
+    m3_mul(a2, a1, k.Xi);
+    m3_tmul(K1aa, k.Xi, a2);
+    for (int q = 0; q < 9; ++q) K1aa[q] += O1[q];
+    m3_mul(K2ua, E3, k.Xi);
+    m3_tmul(K2au, k.Xi, E3);
+    /* Kext (6 x 12, row-major): (0:3, 3:6) K1ua, (3:6, 3:6) K1aa,
+     * (0:3, 9:12) K2ua, (3:6, 6:9) K2au */
+    double Kx[6][12];
+    memset(Kx, 0, sizeof(Kx));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Kx[i][3 + j] = K1ua[i * 3 + j];
+        Kx[3 + i][3 + j] = K1aa[i * 3 + j];
+        Kx[i][9 + j] = K2ua[i * 3 + j];
+        Kx[3 + i][6 + j] = K2au[i * 3 + j];
+      }
+    /* force: P -= mult T^T N^T tl */
+    for (int a = 0; a < 3; ++a) {
+      const double Na = c->N[g][a];
+      for (int blk = 0; blk < 2; ++blk) {
+        double v[3], r[3];
+        for (int i = 0; i < 3; ++i) v[i] = Na * tl[3 * blk + i];
+        m3_tvec(r, c->T3, v);
+        for (int i = 0; i < 3; ++i) f[6 * a + 3 * blk + i] -= mult * r[i];
+      }
+    }
+    /* stiffness: K -= s T^T (N^T Kext Upsilon) T, node blocks (a, b):
+     * N_a (N_b Kext[:, 0:6] + dN_b Kext[:, 6:12]) */
+    const double s = mult * p0i * Aint;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        const double Na = c->N[g][a], Nb = c->N[g][b], dNb = c->dN[g][b];
+        for (int p = 0; p < 2; ++p)
+          for (int q = 0; q < 2; ++q) {
+            double X[9], Y[9], Z[9];
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j)
+                X[i * 3 + j] = Na * (Nb * Kx[3 * p + i][3 * q + j] + dNb * Kx[3 * p + i][6 + 3 * q + j]);
+            m3_tmul(Y, c->T3, X); /* T3^T X */
+            m3_mul(Z, Y, c->T3);  /* T3^T X T3 */
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j) {
+                const int r = 6 * a + 3 * p + i, col = 6 * b + 3 * q + j;
+                K[r + 18 * col] -= s * Z[i * 3 + j];
+              }
+          }
+      }
+  }
+}

@@ -28,6 +28,13 @@ void oracle_beam_precalc(const double* x0, const double* x2, const double* mat, 
                          const double* cs, double pretension, ob_const* c, ob_hist* h);
 void oracle_beam_mount(const ob_const* c, const ob_hist* h, const double* d, double* K, double* f,
                        double* strain_energy);
+/* Pipe_1::PreCalc from a PipeSection (EA, EI, GJ, GA, Rho, CDt, CDn, CAt,
+ * CAn, De, Di) and MountPipeSpecialLoads (internal pressure p0i on the
+ * internal area Aint; adds to K, 18x18 column-major, and f). */
+void oracle_pipe_precalc(const double* x0, const double* x2, const double* ps, const double* cs, ob_const* c,
+                         ob_hist* h);
+void oracle_pipe_pressure(const ob_const* c, const ob_hist* h, const double* d, double p0i, double Aint, double* K,
+                          double* f);
 void oracle_beam_commit(const ob_const* c, ob_hist* h, const double* d);
 /* One Gauss point of the inertia of a rigid cross-section (Beam_1) or
  * director fibre (Shell_1), in the element frame: mass Mr per unit length or

@@ -72,13 +72,17 @@ typedef struct {
   double ray_alpha, ray_beta;
   double* rd;   /* [nb][18x18] column-major */
   double* rds;  /* [ns][27x27] column-major (Shell_1::MountDamping) */
+  /* PipeLoads on each beam, in load order: load indices
+   * pp_load[pp_off[e] .. pp_off[e + 1]) */
+  int* pp_off;
+  int* pp_load;
 } ost;
 
 static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
   free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
-  free(s->rd); free(s->rds); free(s->pf);
+  free(s->rd); free(s->rds); free(s->pf); free(s->pp_off); free(s->pp_load);
 }
 
 /* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
@@ -124,12 +128,42 @@ static int ost_init(ost* s, const gf_model_desc* m) {
     m3_eye(s->Qn + 9 * i);
     for (int k = 0; k < 3; ++k) s->copy[6 * i + k] = m->node_xyz[3 * i + k];
   }
+  /* PipeLoad element lists (reference src/PipeLoad.cpp:123-138): the loads
+   * of each Pipe_1 element in load order */
+  s->pp_off = calloc((size_t)s->nb + 1, sizeof(int));
+  int n_pp = 0;
+  for (int l = 0; l < m->n_loads; ++l)
+    if (m->loads[l].type == GF_LOAD_PIPE_PRESSURE) {
+      for (int q = 0; q < m->loads[l].n_items; ++q) {
+        const int e = m->loads[l].items[q];
+        if (e < 0 || e >= s->nb || !m->beam_pipe_section || m->beam_pipe_section[e] < 0) return -1;
+        s->pp_off[e + 1]++;
+        ++n_pp;
+      }
+    }
+  for (int e = 0; e < s->nb; ++e) s->pp_off[e + 1] += s->pp_off[e];
+  s->pp_load = calloc((size_t)(n_pp ? n_pp : 1), sizeof(int));
+  {
+    int* fill = calloc((size_t)s->nb + 1, sizeof(int));
+    for (int l = 0; l < m->n_loads; ++l)
+      if (m->loads[l].type == GF_LOAD_PIPE_PRESSURE)
+        for (int q = 0; q < m->loads[l].n_items; ++q) {
+          const int e = m->loads[l].items[q];
+          s->pp_load[s->pp_off[e] + fill[e]++] = l;
+        }
+    free(fill);
+  }
   /* Beam_1::PreCalc */
   for (int e = 0; e < s->nb; ++e) {
     const int* b = m->beams + 6 * e;
-    oracle_beam_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->materials + 3 * b[3],
-                        m->sections + 6 * b[4], m->cs + 6 * b[5], m->beam_pretension ? m->beam_pretension[e] : 0.0,
-                        s->bc + e, s->bh + e);
+    const int ps = m->beam_pipe_section ? m->beam_pipe_section[e] : -1;
+    if (ps >= 0) /* Pipe_1::PreCalc */
+      oracle_pipe_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->pipe_sections + 11 * ps,
+                          m->cs + 6 * b[5], s->bc + e, s->bh + e);
+    else
+      oracle_beam_precalc(m->node_xyz + 3 * b[0], m->node_xyz + 3 * b[2], m->materials + 3 * b[3],
+                          m->sections + 6 * b[4], m->cs + 6 * b[5], m->beam_pretension ? m->beam_pretension[e] : 0.0,
+                          s->bc + e, s->bh + e);
   }
   /* Shell_1::PreCalc */
   for (int e = 0; e < s->ns; ++e) {
@@ -243,10 +277,19 @@ static void assemble(ost* s) {
   memset(s->ab, 0, sizeof(double) * (size_t)s->ldab * (size_t)(s->n_free ? s->n_free : 1));
   memset(s->PA, 0, sizeof(double) * (size_t)(s->n_free ? s->n_free : 1));
   double K[324], f[18], d[18];
+  const double tnow = s->last_converged_time + s->current_time_step;
   for (int e = 0; e < s->nb; ++e) {
     const int* b = m->beams + 6 * e;
     for (int j = 0; j < 3; ++j) memcpy(d + 6 * j, s->disp + 6 * b[j], 6 * sizeof(double));
     oracle_beam_mount(s->bc + e, s->bh + e, d, K, f, NULL);
+    /* PipeLoad on a Pipe_1 element (MountLoads, reference
+     * src/PipeLoad.cpp Mount -> src/Pipe_1.cpp:1441-1494) */
+    for (int q = s->pp_off[e]; q < s->pp_off[e + 1]; ++q) {
+      const gf_load* L = m->loads + s->pp_load[q];
+      const double* ps = m->pipe_sections + 11 * m->beam_pipe_section[e];
+      const double Aint = OR_PI * ps[10] * ps[10] / 4.0;
+      oracle_pipe_pressure(s->bc + e, s->bh + e, d, table_at(&L->table, tnow, 0), Aint, K, f);
+    }
     if (s->dynamic) {
       /* MountMass + MountDamping + MountDyn (reference
        * src/Beam_1.cpp:1564-1673): K += M (+ a4 C), f += f_inertial (+ C v) */
@@ -781,7 +824,10 @@ static void final_state(ost* s, double* out) {
  * stats add up over the steps. */
 int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes, int* stats) {
   ost s;
-  ost_init(&s, m);
+  if (ost_init(&s, m) != 0) {
+    ost_free(&s);
+    return -1;
+  }
   int r = 0, total[4] = {0, 0, 0, 0};
   double start = m->solution.start_time;
   for (int k = 0; k <= m->n_next_steps && r == 0; ++k) {
@@ -826,13 +872,31 @@ int oracle_beam_element(const double* xyz9, const double* mat3, const double* se
   return 0;
 }
 
+/* One Pipe_1 element: PreCalc from the pipe section ps11, the committed
+ * history, Mount at disp18 and, when p0i != 0, MountPipeSpecialLoads of an
+ * internal pressure p0i (reference src/Pipe_1.cpp:836-974, 1106-1156,
+ * 1441-1494).  K 18x18 column-major, f 18. */
+int oracle_pipe_element(const double* xyz9, const double* ps11, const double* cs6, int n_hist,
+                        const double* hist_disp, const double* disp18, double p0i, double* K, double* f) {
+  ob_const c;
+  ob_hist h;
+  oracle_pipe_precalc(xyz9, xyz9 + 6, ps11, cs6, &c, &h);
+  for (int q = 0; q < n_hist; ++q) oracle_beam_commit(&c, &h, hist_disp + 18 * q);
+  oracle_beam_mount(&c, &h, disp18, K, f, NULL);
+  if (p0i != 0.0) oracle_pipe_pressure(&c, &h, disp18, p0i, OR_PI * ps11[10] * ps11[10] / 4.0, K, f);
+  return 0;
+}
+
 /* Tangent and residual of the first Newton iteration of the first load step
  * (all increments zero): K_AA in GB storage (ldab = 3 kl + 1, column-major,
  * n_free columns) and P_A.  dims receives n_free and kl.  With ab == NULL only
  * dims is filled. */
 int oracle_first_tangent(const gf_model_desc* m, double* ab, double* PA, int* dims) {
   ost s;
-  ost_init(&s, m);
+  if (ost_init(&s, m) != 0) {
+    ost_free(&s);
+    return -1;
+  }
   const int n = s.n_free, kn = s.kl_nat, ld = 3 * kn + 1;
   dims[0] = n;
   dims[1] = kn;

@@ -21,6 +21,9 @@
 #include "NodalLoad.h"
 #include "Node.h"
 #include "NodeSet.h"
+#include "PipeLoad.h"
+#include "PipeSection.h"
+#include "Pipe_1.h"
 #include "SecRectangle.h"
 #include "SecTube.h"
 #include "Shell_1.h"
@@ -51,11 +54,13 @@ void ref_record_state(int solution, double time) {
     fprintf(f, "\n");
   }
   for (int e = 0; e < db.number_elements; ++e) {
-    if (typeid(*db.elements[e]) != typeid(Beam_1)) continue;
-    Beam_1* b = static_cast<Beam_1*>(db.elements[e]);
+    LagrangeSave* lag = nullptr;
+    if (typeid(*db.elements[e]) == typeid(Beam_1)) lag = static_cast<Beam_1*>(db.elements[e])->lag_save;
+    else if (typeid(*db.elements[e]) == typeid(Pipe_1)) lag = static_cast<Pipe_1*>(db.elements[e])->lag_save;
+    if (!lag) continue;
     for (int g = 0; g < 2; ++g) {
       fprintf(f, "G %d %d", e + 1, g);
-      for (int k = 0; k < 9; ++k) fprintf(f, " %.17g", b->lag_save->Q_i[g]->getMatrix()[k]);
+      for (int k = 0; k < 9; ++k) fprintf(f, " %.17g", lag->Q_i[g]->getMatrix()[k]);
       fprintf(f, "\n");
     }
   }
@@ -93,7 +98,7 @@ bool is_keyword(const char* s) {
   static const char* k[] = {"SolutionSteps", "Nodes", "Elements", "Materials", "Sections",
                             "ShellSections", "CoordinateSystems", "NodeSets", "Loads",
                             "Displacements", "Constraints", "ConvergenceCriteria", "SolverOptions",
-                            "Monitor", "PostFiles", "ElementSets", "Environment", nullptr};
+                            "Monitor", "PostFiles", "ElementSets", "Environment", "PipeSections", nullptr};
   for (int i = 0; k[i]; ++i)
     if (!strcmp(s, k[i])) return true;
   return false;
@@ -145,9 +150,21 @@ int giraffe_ref_load(const char* path) {
       ok = read_block<Element>(f, db.number_elements, db.elements, [](const char* t) -> Element* {
         if (!strcmp(t, "Beam_1")) return new Beam_1();
         if (!strcmp(t, "Shell_1")) return new Shell_1();
+        if (!strcmp(t, "Pipe_1")) return new Pipe_1();
         return nullptr;
       });
       db.elements_exist = true;
+    } else if (!strcmp(s, "PipeSections")) {
+      // reference src/IO.cpp:1282-1301: PipeSection::Read takes its own "PS"
+      if (fscanf(f, "%999s", s) != 1) { ok = false; break; }
+      db.number_pipe_sections = atoi(s);
+      db.pipe_sections = new PipeSection*[db.number_pipe_sections];
+      for (int i = 0; i < db.number_pipe_sections && ok; ++i) {
+        db.pipe_sections[i] = new PipeSection();
+        TryComment(f);
+        ok = db.pipe_sections[i]->Read(f);
+      }
+      db.pipe_sections_exist = true;
     } else if (!strcmp(s, "Materials")) {
       ok = read_block<Material>(f, db.number_materials, db.materials, [](const char* t) -> Material* {
         return !strcmp(t, "Hooke") ? new Hooke() : nullptr;
@@ -200,6 +217,7 @@ int giraffe_ref_load(const char* path) {
       ok = read_block<Load>(f, db.number_loads, db.loads, [](const char* t) -> Load* {
         if (!strcmp(t, "NodalLoad")) return new NodalLoad();
         if (!strcmp(t, "ShellLoad")) return new ShellLoad();
+        if (!strcmp(t, "PipeLoad")) return new PipeLoad();
         return nullptr;
       });
       db.loads_exist = true;
@@ -289,6 +307,9 @@ int giraffe_ref_element_mount(int e, double* K, double* P) {
   if (typeid(*el) == typeid(Beam_1)) {
     stiff = static_cast<Beam_1*>(el)->stiffness;
     load = static_cast<Beam_1*>(el)->P_loading;
+  } else if (typeid(*el) == typeid(Pipe_1)) {
+    stiff = static_cast<Pipe_1*>(el)->stiffness;
+    load = static_cast<Pipe_1*>(el)->P_loading;
   } else if (typeid(*el) == typeid(Shell_1)) {
     stiff = static_cast<Shell_1*>(el)->stiffness;
     load = static_cast<Shell_1*>(el)->P_loading;
@@ -379,4 +400,21 @@ extern "C" int giraffe_ref_shell_inertia(int e, double dt, double* M, double* F,
   memcpy(F, s->inertial_loading->getMatrix(), sizeof(double) * 27);
   *ke = s->kinetic_energy;
   return 27;
+}
+
+// Pipe_1 Mount + MountElementLoads + MountPipeSpecialLoads of load number l
+// (1-based) with the load evaluated at time t (reference
+// src/Pipe_1.cpp:1441-1494).  K: 18x18 column-major, P: P_loading.
+extern "C" int giraffe_ref_pipe_pressure(int e, int l, double t, double* K, double* P) {
+  Element* el = db.elements[e - 1];
+  if (typeid(*el) != typeid(Pipe_1)) return 0;
+  db.last_converged_time = t;
+  db.current_time_step = 0.0;
+  Pipe_1* p = static_cast<Pipe_1*>(el);
+  p->Mount();
+  p->MountElementLoads();
+  p->MountPipeSpecialLoads(l);
+  memcpy(K, p->stiffness->getMatrix(), sizeof(double) * 18 * 18);
+  memcpy(P, p->P_loading->getMatrix(), sizeof(double) * 18);
+  return 18;
 }

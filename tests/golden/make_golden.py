@@ -35,6 +35,19 @@ stores what the reference computes:
 * ref_beam_inertia.npz   Beam_1 inertial force and mass/gyroscopic tangent of
                          single elements (Beam_1::MountMass) with random
                          history, increments, nodal velocities/accelerations.
+* ref_pipe_elements.npz  Pipe_1 tangent K (18x18) and unbalanced force P (18)
+                         of single elements with random geometry, pipe
+                         section, frame, history and increment, half of them
+                         under an internal pressure (Pipe_1::PreCalc, Mount,
+                         MountPipeSpecialLoads).
+* ref_tutorial04.npz     the reference's tutorial04 deck itself (50 Pipe_1, a
+                         lateral perturbation, then internal pressure raised
+                         to 1.2 MPa over 200 Static steps), every step.
+* ref_pipe_riser.npz     a 16-element Pipe_1 riser, pinned at the bottom, its
+                         top driven laterally, under an internal pressure
+                         raised to 20 MPa: Dynamic (Newmark), 100 steps.
+* ref_pipe_riser_rayleigh.npz  the same with Rayleigh damping (alpha 0.3,
+                         beta 0.004, Update 1).
 * ref_shell_elements.npz Shell_1 tangent K (27x27) and unbalanced force P (27)
                          of single elements with random geometry, material,
                          thickness, committed history and increment, half of
@@ -87,7 +100,7 @@ ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, ROOT)
 
 from giraffe_gb300 import configs  # noqa: E402
-from giraffe_gb300.model import NodalLoad, PressureLoad, Solution, Structure, Table  # noqa: E402
+from giraffe_gb300.model import NodalLoad, PipeLoad, PressureLoad, Solution, Structure, Table  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "libgiraffe_ref.so")
 
@@ -102,6 +115,7 @@ def ref_lib():
     L.giraffe_ref_set_increment.argtypes = [C.c_int, dp]
     L.giraffe_ref_element_mount.argtypes = [C.c_int, dp, dp]
     L.giraffe_ref_shell_pressure.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp]
+    L.giraffe_ref_pipe_pressure.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp]
     return L
 
 
@@ -268,6 +282,54 @@ def run_inertia(L, cases, tmp, rng):
     return res
 
 
+def run_pipe_elements(L, rng, n, tmp):
+    """Single Pipe_1 elements: random geometry, pipe section, frame, history
+    and increment; half of them under an internal pressure (PipeLoad)."""
+    out = {k: [] for k in ("xyz", "ps", "cs", "hist", "disp", "pressure", "K", "P")}
+    nh_list = []
+    for i, c in enumerate(element_cases(rng, n)):
+        s = Structure(nodes=c["xyz"])
+        De = rng.uniform(0.2, 0.7)
+        Di = De - 2 * rng.uniform(0.01, 0.04)
+        E = rng.uniform(5e10, 2.1e11)
+        A = np.pi / 4 * (De * De - Di * Di)
+        I = np.pi / 64 * (De ** 4 - Di ** 4)
+        ps = s.add_pipe_section(E * A, E * I, 0.8 * E * I, 0.4 * E * A, 7850.0 * A, De, Di)
+        cs = s.add_cs(c["e1"], c["e3"])
+        s.add_pipe(0, 1, 2, ps, cs)
+        press = i % 2 == 1
+        p = rng.uniform(-2e6, 2e6)
+        if press:
+            s.loads.append(PipeLoad([0], Table(np.array([0.0, 10.0]), np.array([[p, 0, 0, 0], [p, 0, 0, 0]]))))
+        deck = os.path.join(tmp, f"pp{i}.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        L.giraffe_ref_prepare()
+        for h in c["hist"]:
+            for nd in range(3):
+                L.giraffe_ref_set_increment(nd + 1, _dp(np.ascontiguousarray(h[nd])))
+            L.giraffe_ref_commit()
+        for nd in range(3):
+            L.giraffe_ref_set_increment(nd + 1, _dp(np.ascontiguousarray(c["disp"][nd])))
+        K = np.zeros(324)
+        P = np.zeros(18)
+        if press:
+            assert L.giraffe_ref_pipe_pressure(1, 1, 1.0, _dp(K), _dp(P)) == 18
+        else:
+            assert L.giraffe_ref_element_mount(1, _dp(K), _dp(P)) == 18
+        hist = np.zeros((3, 18))
+        hist[: len(c["hist"])] = c["hist"].reshape(-1, 18)
+        for k, v in (("xyz", c["xyz"].ravel()), ("ps", np.array(s.pipe_sections[0])), ("cs", np.array(s.cs[0])),
+                     ("hist", hist), ("disp", c["disp"].ravel()), ("pressure", p if press else 0.0),
+                     ("K", K.reshape(18, 18).T), ("P", P)):
+            out[k].append(v)
+        nh_list.append(len(c["hist"]))
+    res = {k: np.array(v) for k, v in out.items()}
+    res["n_hist"] = np.array(nh_list)
+    return res
+
+
 def run_shell_elements(L, rng, n, tmp):
     out = {k: [] for k in ("xyz", "mat", "thick", "hist", "disp", "pressure", "area_update", "K", "P")}
     nh_list = []
@@ -402,6 +464,9 @@ DECKS = {
                                                                             rayleigh_beta=2e-5, update_rayleigh=1),
     "ref_plate_release.npz": lambda: configs.plate_release(3),
     "ref_chain_sequence.npz": configs.chain_sequence,
+    "ref_pipe_riser.npz": configs.pipe_riser,
+    "ref_pipe_riser_rayleigh.npz": lambda: configs.pipe_riser(rayleigh_alpha=0.3, rayleigh_beta=0.004,
+                                                              update_rayleigh=1),
     "ref_riser_rayleigh.npz": lambda: configs.riser_chain(12, 0.4, 0.03, 1.0, 4.0, steps=120, element_length=2.0,
                                                           rayleigh_alpha=0.3, rayleigh_beta=0.004,
                                                           update_rayleigh=1),
@@ -457,6 +522,33 @@ def make_elements():
         np.savez_compressed(os.path.join(HERE, "ref_shell_inertia.npz"), **run_shell_inertia(L, rng, 16, tmp))
 
 
+def make_pipe_elements():
+    L = ref_lib()
+    rng = np.random.default_rng(20261204)
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, "ref_pipe_elements.npz"), **run_pipe_elements(L, rng, 24, tmp))
+
+
+def make_tutorial04():
+    """The reference's own Pipe_1 deck, tutorial04 (a pinned pipe perturbed
+    by a lateral load, then under internal pressure raised to 1.2 MPa in 200
+    steps), run from its file; every converged configuration."""
+    from giraffe_gb300.deck import read_deck_file
+
+    path = os.path.join(REF_INPUTS, "tutorial04", "tutorial04.inp")
+    L = ref_lib()
+    s = read_deck_file(path)
+    with tempfile.TemporaryDirectory() as tmp:
+        assert L.giraffe_ref_load(path.encode()) == 0
+        rec = os.path.join(tmp, "t04.rec")
+        log = os.path.join(tmp, "t04.log")
+        rc = L.giraffe_ref_solve(rec.encode(), log.encode())
+        times, nodes, gq = parse_rec(rec)
+        steps = parse_log(log)
+    np.savez_compressed(os.path.join(HERE, "ref_tutorial04.npz"), rc=np.array(rc), times=times, nodes=nodes,
+                        gp_Q=gq, steps=steps, deck=np.array(s.to_inp()))
+
+
 def make_deck(name):
     L = ref_lib()
     with tempfile.TemporaryDirectory() as tmp:
@@ -472,13 +564,18 @@ def main():
             make_elements()
         elif sys.argv[1] == "ref_tutorial05.npz":
             make_tutorial05()
+        elif sys.argv[1] == "ref_tutorial04.npz":
+            make_tutorial04()
+        elif sys.argv[1] == "ref_pipe_elements.npz":
+            make_pipe_elements()
         elif sys.argv[1] == "ref_plate24.npz":
             make_plate24()
         else:
             make_deck(sys.argv[1])
         return
     ref_lib()
-    for job in ["elements"] + list(DECKS) + ["ref_tutorial05.npz", "ref_plate24.npz"]:
+    for job in (["elements", "ref_pipe_elements.npz"] + list(DECKS) +
+                ["ref_tutorial04.npz", "ref_tutorial05.npz", "ref_plate24.npz"]):
         subprocess.run([sys.executable, os.path.abspath(__file__), job], check=True)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

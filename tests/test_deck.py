@@ -73,8 +73,13 @@ def test_sets_by_sequence_comments_and_skipped_blocks():
 
 def test_unsupported_content_is_refused():
     base = configs.pipe_chain(4, 0.4, 0.03, [1e5, 0.0, 0.0]).to_inp()
-    with pytest.raises(DeckError, match="Pipe_1"):
-        read_deck(base.replace("Beam_1\t2\t", "Pipe_1\t2\t"))
+    with pytest.raises(DeckError, match="Truss_1"):
+        read_deck(base.replace("Beam_1\t2\t", "Truss_1\t2\t"))
+    mixed = configs.pipe_riser(4, steps=4)  # element 2 a Beam_1 inside the PipeLoad's set
+    mixed.beams[1] = (2, 3, 4, mixed.add_material(2.1e11, 0.3, 7850.0), mixed.add_tube(0.3, 0.26), 0)
+    del mixed.pipe_of[1]
+    with pytest.raises(DeckError, match="every element must be a Pipe_1"):
+        read_deck(mixed.to_inp())
     with pytest.raises(DeckError, match="Contacts"):
         read_deck(base + "Contacts\t1\nNSSS\t1\n")
     with pytest.raises(DeckError, match="solution step"):
@@ -124,3 +129,23 @@ def test_zero_ic_and_step_dependent_tables():
     bad = text[:k] + text[k:].replace("BoolTable\t1", "BoolTable\t1\t0", 1)
     with pytest.raises(DeckError, match="change between solution steps"):
         read_deck(bad)
+
+
+def test_pipe_deck_round_trip():
+    """Pipe_1 elements, PipeSections and PipeLoad written by to_inp read back
+    into the same structure."""
+    s = configs.pipe_riser(6, steps=8)
+    r = read_deck(s.to_inp())
+    assert r.pipe_of == s.pipe_of and r.pipe_sections == s.pipe_sections
+    assert r.beams.array().tolist() == s.beams.array().tolist()
+    assert len(r.loads) == 1 and r.loads[0].pipes == s.loads[0].pipes
+    assert np.array_equal(r.loads[0].table.values, s.loads[0].table.values)
+    assert r.to_inp() == s.to_inp()
+
+
+def test_reference_tutorial04_reads():
+    s = read_deck_file(_ref_deck("tutorial04"))
+    assert len(s.beams) == 50 and len(s.pipe_of) == 50 and len(s.pipe_sections) == 1
+    assert s.pipe_sections[0][-2:] == (0.65, 0.62)
+    assert len(s.loads) == 2 and s.loads[1].pipes == list(range(50))
+    assert [so.end_time for so in [s.solution] + s.next_steps] == [1.0, 2.0]

@@ -197,3 +197,47 @@ def test_solution_step_sequences_match_reference(golden, name, make):
     Static for a pipe chain."""
     final, stats, _ = _check_run(golden(name), make(), tol=1e-10)
     assert stats[0] == len(golden(name)["steps"])
+
+
+def test_pipe_elements_match_reference(golden):
+    """Pipe_1: Beam_1 kinematics with a PipeSection's stiffness, and the
+    internal-pressure load of MountPipeSpecialLoads with its load
+    stiffness (half of the elements)."""
+    g = golden("ref_pipe_elements.npz")
+    pressed = 0
+    for i in range(len(g["K"])):
+        nh = int(g["n_hist"][i])
+        p = float(g["pressure"][i])
+        K, f = oracle.pipe_element(g["xyz"][i], g["ps"][i], g["cs"][i], g["hist"][i][:nh], g["disp"][i], p)
+        assert rel(K, g["K"][i]) < 1e-12, i
+        assert rel(f, g["P"][i]) < 1e-12, i
+        if p != 0.0:
+            pressed += 1
+            K0, _ = oracle.pipe_element(g["xyz"][i], g["ps"][i], g["cs"][i], g["hist"][i][:nh], g["disp"][i])
+            # the load stiffness itself, on its own scale
+            assert rel(K - K0, g["K"][i] - K0) < 1e-9, i
+    assert pressed == len(g["K"]) // 2
+
+
+def test_tutorial04_pressurized_pipe_matches_reference(golden):
+    """The reference's tutorial04 deck (read back from the fixture's deck
+    text): 50 Pipe_1 elements, a lateral perturbation, then internal
+    pressure raised to 1.2 MPa in 200 Static steps."""
+    from giraffe_gb300.model import Structure
+    g = golden("ref_tutorial04.npz")
+    s = Structure.from_inp(str(g["deck"]))
+    assert len(s.pipe_of) == 50 and len(s.next_steps) == 1
+    _check_run(g, s, tol=1e-10)
+
+
+@pytest.mark.parametrize("name,kw", [("ref_pipe_riser.npz", {}),
+                                     ("ref_pipe_riser_rayleigh.npz",
+                                      dict(rayleigh_alpha=0.3, rayleigh_beta=0.004, update_rayleigh=1))])
+def test_pipe_riser_dynamics_matches_reference(golden, name, kw):
+    """Pipe_1 in a Dynamic step (the pipe section's mass and rotary inertia)
+    under a rising internal pressure, with and without Rayleigh damping."""
+    final, _, _ = _check_run(golden(name), configs.pipe_riser(**kw), tol=1e-10)
+    # the pressure changes the motion by far more than the tolerance
+    s = configs.pipe_riser(pressure=0.0, **kw)
+    f0, _, _ = oracle.solve(s)
+    assert np.abs(final[:, :3] - f0[:, :3]).max() > 1e-6 * np.abs(final[:, :3]).max()
