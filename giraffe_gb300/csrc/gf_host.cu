@@ -113,6 +113,31 @@ void beam_precalc(const double* x0, const double* x2, const double* mat, const d
   }
 }
 
+// Pipe_1::PreCalc (reference src/Pipe_1.cpp:1106-1156): Beam_1's frame, e3r,
+// length and shape functions (no pre-tension), with the PipeSection's
+// constitutive matrix diag(GA, GA, EA, EI, EI, GJ), mass Rho per unit length
+// and rotary inertia Rho ((De/2)^2 - (Di/2)^2) diag(1/4, 1/4, 1/2).  ps:
+// EA, EI, GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di.
+void pipe_precalc(const double* x0, const double* x2, const double* ps, const double* cs, BeamConst& c, BeamHist& h,
+                  BeamHistAux& x) {
+  const double unit_mat[3] = {1.0, 0.0, 0.0}, unit_sec[6] = {1.0, 1.0, 1.0, 0.0, 1.0, 1.0};
+  beam_precalc(x0, x2, unit_mat, unit_sec, cs, c, h, x, 0.0);
+  const double EA = ps[0], EI = ps[1], GJ = ps[2], GA = ps[3], Rho = ps[4], De = ps[9], Di = ps[10];
+  c.Dd[0] = GA;
+  c.Dd[1] = GA;
+  c.Dd[2] = EA;
+  c.Dd[3] = EI;
+  c.Dd[4] = EI;
+  c.Dd[5] = GJ;
+  c.D34 = 0.0;
+  c.Mr = Rho;
+  for (int k = 0; k < 9; ++k) c.Jr[k] = 0.0;
+  const double rr = (De / 2.0) * (De / 2.0) - (Di / 2.0) * (Di / 2.0);
+  c.Jr[0] = (Rho * rr / 4.0);
+  c.Jr[4] = (Rho * rr / 4.0);
+  c.Jr[8] = (Rho * rr / 2.0);
+}
+
 template <typename T> bool dmalloc(gf_ctx* ctx, T** p, size_t n) {
   if (n == 0) n = 1;
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
@@ -432,8 +457,15 @@ void plan_structure(const gf_model_desc& m, int s, StructPlan& P) {
       }
       for (int k = 0; k < 6; ++k) active[6 * nd + k] = 1;
     }
-    if (m.beams[6 * e + 3] < 0 || m.beams[6 * e + 3] >= m.n_materials || m.beams[6 * e + 4] < 0 ||
-        m.beams[6 * e + 4] >= m.n_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
+    const int ps = m.beam_pipe_section ? m.beam_pipe_section[e] : -1;
+    if (ps >= 0) {
+      // a Pipe_1 element: its pipe section and CS (material and section unused)
+      if (ps >= m.n_pipe_sections || !m.pipe_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
+        P.err = strf("structure %d: pipe %d refers to a missing pipe section or CS", s, e);
+        return;
+      }
+    } else if (m.beams[6 * e + 3] < 0 || m.beams[6 * e + 3] >= m.n_materials || m.beams[6 * e + 4] < 0 ||
+               m.beams[6 * e + 4] >= m.n_sections || m.beams[6 * e + 5] < 0 || m.beams[6 * e + 5] >= m.n_cs) {
       P.err = strf("structure %d: beam %d refers to a missing material, section or CS", s, e);
       return;
     }
@@ -671,9 +703,14 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     std::vector<unsigned> node_colors(nn, 0u);
     for (int e = 0; e < m.n_beams; ++e) {
       const int* be = m.beams + 6 * e;
-      beam_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.materials + 3 * be[3], m.sections + 6 * be[4],
-                   m.cs + 6 * be[5], bconst[eo + e], bhist[eo + e], baux[eo + e],
-                   m.beam_pretension ? m.beam_pretension[e] : 0.0);
+      const int ps = m.beam_pipe_section ? m.beam_pipe_section[e] : -1;
+      if (ps >= 0)
+        pipe_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.pipe_sections + 11 * ps, m.cs + 6 * be[5],
+                     bconst[eo + e], bhist[eo + e], baux[eo + e]);
+      else
+        beam_precalc(m.node_xyz + 3 * be[0], m.node_xyz + 3 * be[2], m.materials + 3 * be[3],
+                     m.sections + 6 * be[4], m.cs + 6 * be[5], bconst[eo + e], bhist[eo + e], baux[eo + e],
+                     m.beam_pretension ? m.beam_pretension[e] : 0.0);
       for (int j = 0; j < 3; ++j) enodes[(size_t)(eo + e) * 3 + j] = no + be[j];
       estruct[eo + e] = s;
       unsigned used = node_colors[be[0]] | node_colors[be[1]] | node_colors[be[2]];
@@ -723,6 +760,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   // ---- tables, loads, prescribed displacements, step parameters (serial) ----
   std::vector<StructParams> params(n), step_params;
   std::vector<LoadEntry> loads;
+  std::vector<int> pp_elem, pp_table;
+  std::vector<double> pp_aint;
   std::vector<DispEntry> disps;
   std::vector<TableDev> tables;
   std::vector<double> tdata;
@@ -743,6 +782,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       return (int)tables.size() - 1;
     };
     inf.load_off = (int)loads.size();
+    std::vector<char> pipe_pressed;
     for (int l = 0; l < m.n_loads; ++l) {
       const gf_load& L = m.loads[l];
       if (L.type == GF_LOAD_SHELL_PRESSURE) {
@@ -759,6 +799,29 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
           }
           spress[shell_off + e] = t;
           sarea[shell_off + e] = L.area_update ? 1 : 0;
+        }
+        continue;
+      }
+      if (L.type == GF_LOAD_PIPE_PRESSURE) {
+        // PipeLoad (reference src/PipeLoad.cpp:123-138): the internal
+        // pressure P0I of its table on each Pipe_1 of the set, one PipeLoad
+        // per element
+        if (L.table.n_cols < 1) { set_err(ctx, "structure %d: PipeLoad table needs P0I", s); return GF_ERR_ARG; }
+        int t = add_table(L.table);
+        for (int q = 0; q < L.n_items; ++q) {
+          const int e = L.items[q];
+          const int ps = e >= 0 && e < m.n_beams && m.beam_pipe_section ? m.beam_pipe_section[e] : -1;
+          if (ps < 0) { set_err(ctx, "structure %d: PipeLoad on %d, which is not a Pipe_1", s, e); return GF_ERR_ARG; }
+          if (pipe_pressed.empty()) pipe_pressed.assign((size_t)m.n_beams, 0);
+          if (pipe_pressed[e]) {
+            set_err(ctx, "structure %d: pipe %d carries more than one PipeLoad", s, e);
+            return GF_ERR_ARG;
+          }
+          pipe_pressed[e] = 1;
+          const double Di = m.pipe_sections[11 * ps + 10];
+          pp_elem.push_back(elem_offs[s] + e);
+          pp_table.push_back(t);
+          pp_aint.push_back(3.1415926535897932384626433832795 * Di * Di / 4.0);
         }
         continue;
       }
@@ -853,6 +916,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.n_elem = elem_off;
   b.n_free = dof_off;
   b.n_loads = (int)loads.size();
+  b.n_pipe_press = (int)pp_elem.size();
   b.n_disps = (int)disps.size();
   b.n_tables = (int)tables.size();
   // chain solver data: sizes and offsets per structure (serial), then the
@@ -1007,7 +1071,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !upload(B, &b.estruct, estruct) || !upload(B, &b.bconst, bconst) || !upload(B, &b.bhist, bhist) ||
       !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
       !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.step_params, step_params) ||
-      !upload(B, &b.loads, loads) ||
+      !upload(B, &b.loads, loads) || !upload(B, &b.pp_elem, pp_elem) || !upload(B, &b.pp_table, pp_table) ||
+      !upload(B, &b.pp_aint, pp_aint) ||
       !upload(B, &b.disps, disps) || !upload(B, &b.tables, tables) || !upload(B, &b.table_data, tdata) ||
       !dup(B, &B->copy0, b.copy, copy.size()) || !dup(B, &B->Qn0, b.Qn, Qn.size()) ||
       !dup(B, &B->bhist0, b.bhist, bhist.size()) || !dup(B, &B->baux0, b.baux, baux.size()))
@@ -1061,7 +1126,8 @@ int count_launches_per_pass(const gf_batch* B) {
         chain_launches += 2 * (cd.odd_off[l + 1] > cd.odd_off[l]) + (cd.even_off[l + 1] > cd.even_off[l]);
     }
   }
-  return 10 + colors + chain_launches + shell_launches_per_pass(B->b) + (B->b.any_rayleigh ? 1 : 0);
+  return 10 + colors + chain_launches + shell_launches_per_pass(B->b) + (B->b.any_rayleigh ? 1 : 0) +
+         (B->b.n_pipe_press ? 1 : 0);
 }
 
 int batch_reset(gf_batch* B) {

@@ -499,6 +499,110 @@ __global__ void k_beam_rayleigh(Batch b) {
   }
 }
 
+// Pipe_1::MountPipeSpecialLoads (reference src/Pipe_1.cpp:1441-1494): the
+// internal pressure p0i of a PipeLoad acting on the internal area Aint, at
+// the current iterate.  At each Gauss point, with Q = Q_delta Q_i,
+// kappa = Q kappa_r and e3 = Q e3r (element frame), the line load
+// (f, m) = -p0i Aint (kappa x e3, Xi^T (z' x e3)) and its stiffness Kext
+// (6 x 12 on (u, alpha, u', alpha'): K1ua, K1aa, K2ua, K2au) enter as
+// f_e -= jac T^T N^T (f, m) and K_e -= jac p0i Aint T^T N^T Kext Upsilon T.
+// Its O1 term reads the element's scalar g, which the reference's Mount
+// leaves at the second Gauss point's value (src/Pipe_1.cpp:890), for both
+// points.  One thread per pressurized element, after k_beam_tangent has
+// written K_e and f_e.
+__global__ void k_pipe_pressure(Batch b) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= b.n_pipe_press) return;
+  const int e = b.pp_elem[q];
+  const StructState& st = b.state[b.estruct[e]];
+  if (!iterating(st)) return;
+  const double p0i = table_at(b, b.pp_table[q], st.last_converged_time + st.current_time_step, 0);
+  const double Aint = b.pp_aint[q];
+  const BeamConst& c = b.bconst[e];
+  const BeamHist& h = b.bhist[e];
+  double d[18];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const int64_t nd = b.enodes[3 * e + j];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) d[6 * j + k] = b.disp[nd * 6 + k];
+  }
+  M3<double> T;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) T[i] = c.T3[i];
+  const V3<double> e3r = {{c.e3r[0], c.e3r[1], c.e3r[2]}};
+  const BeamInterp ip1 = beam_interp(c, d, 1);
+  const double g_last = 4.0 / (4.0 + dot(ip1.alpha, ip1.alpha));
+  const double pa = -p0i * Aint, sK = c.jac * p0i * Aint;
+  const int64_t ne = b.n_elem;
+  double* Ke = b.Ke + e;
+  double* Fe = b.Fe + e;
+#pragma unroll 1
+  for (int g = 0; g < 2; ++g) {
+    const BeamInterp ip = beam_interp(c, d, g);
+    double gg;
+    M3<double> Qd, Xi, Qi;
+    beam_rot(ip.alpha, gg, Qd, Xi);
+    const M3<double> dA = skew(ip.dalpha);
+    const double ad = dot(ip.alpha, ip.dalpha);
+    M3<double> dXi;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) dXi[i] = -0.5 * gg * (ad * Xi[i] - dA[i]);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Qi[i] = h.Q[g][i];
+    V3<double> dz;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dz[i] = ip.du[i] + h.dz[g][i];
+    const M3<double> Q = mul(Qd, Qi);
+    V3<double> kap = tmv(Qi, tmv(Xi, ip.dalpha));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) kap[i] += h.kap[g][i];
+    const V3<double> kip = mv(Q, kap), e3 = mv(Q, e3r);
+    const V3<double> fl = cross(kip, e3), ml = tmv(Xi, cross(dz, e3));
+    const M3<double> E3 = skew(e3), Kp = skew(kip), dZ = skew(dz);
+    const V3<double> c2 = cross(e3, dz), w = tmv(Xi, c2);
+    const M3<double> S2 = skew(c2);
+    const M3<double> A1 = mul(mul(Kp, E3), Xi), A2 = mul(E3, dXi), A3 = mul(mul(E3, Kp), Xi);
+    const M3<double> B1 = tmul(Xi, mul(mul(dZ, E3), Xi));
+    M3<double> K1ua, K1aa;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        K1ua[i * 3 + j] = A1[i * 3 + j] + A2[i * 3 + j] - A3[i * 3 + j];
+        K1aa[i * 3 + j] = -0.5 * g_last * (w[i] * ip.alpha[j] - S2[i * 3 + j]) + B1[i * 3 + j];
+      }
+    // blocks of Kext in the global frame: T^T X T
+    const M3<double> G1 = tmul(T, mul(K1ua, T)), G2 = tmul(T, mul(mul(E3, Xi), T));
+    const M3<double> G3 = tmul(T, mul(tmul(Xi, E3), T)), G4 = tmul(T, mul(K1aa, T));
+    const V3<double> fg = tmv(T, fl), mg = tmv(T, ml);
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+      const double Na = c.N[g][a];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        Fe[(int64_t)(6 * a + i) * ne] -= c.jac * Na * (pa * fg[i]);
+        Fe[(int64_t)(6 * a + 3 + i) * ne] -= c.jac * Na * (pa * mg[i]);
+      }
+#pragma unroll 1
+      for (int n = 0; n < 3; ++n) {
+        const double Nb = c.N[g][n], dNb = c.dN[g][n];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const int x = i * 3 + j;
+            // (u_a, alpha_b): K1ua Nb + K2ua dNb; (alpha_a, u_b): K2au dNb;
+            // (alpha_a, alpha_b): K1aa Nb
+            Ke[(int64_t)((6 * a + i) + 18 * (6 * n + 3 + j)) * ne] -= sK * (Na * (Nb * G1[x] + dNb * G2[x]));
+            Ke[(int64_t)((6 * a + 3 + i) + 18 * (6 * n + j)) * ne] -= sK * (Na * (dNb * G3[x]));
+            Ke[(int64_t)((6 * a + 3 + i) + 18 * (6 * n + 3 + j)) * ne] -= sK * (Na * (Nb * G4[x]));
+          }
+      }
+    }
+  }
+}
+
 __global__ void k_beam_scatter(Batch b, int color) {
   int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
@@ -1134,6 +1238,7 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     else
       k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
     if (b.any_rayleigh) k_beam_rayleigh<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
+    if (b.n_pipe_press) k_pipe_pressure<<<(b.n_pipe_press + 127) / 128, 128, 0, st>>>(b);
   }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];

@@ -5,7 +5,8 @@
 // HBM layout (all structure-of-arrays over the batch):
 //   nodes     disp[6], copy[6] (position + accumulated Rodrigues vector),
 //             Qn[9], gl[6] (local free index or -1), node_struct
-//   elements  enodes[3], estruct, BeamConst (PreCalc constants),
+//   elements  enodes[3], estruct, BeamConst (PreCalc constants of Beam_1 or
+//             of a Pipe_1 from its PipeSection),
 //             BeamHist (Gauss-point history read by Mount), BeamHistAux
 //             (u_i, alpha_i written at commit)
 //   DOFs      dof_node6 (node*6 + k of each free DOF), P (residual, then the
@@ -320,6 +321,12 @@ struct Batch {
   StructParams* params;       // the current solution step's parameters
   StructParams* step_params;  // every solution step of every structure
   StructState* state;
+  // PipeLoad internal pressures: one entry per pressurized Pipe_1 element
+  // (batch element index, table of P0I P0E RhoI RhoE, internal area)
+  int n_pipe_press;
+  int* pp_elem;
+  int* pp_table;
+  double* pp_aint;
   // loads
   LoadEntry* loads;
   DispEntry* disps;
