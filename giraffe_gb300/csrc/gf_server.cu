@@ -83,8 +83,8 @@ constexpr size_t kHostStage = (size_t)256 << 20;
 // running waves.
 struct Parked {
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t evt[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t aux[GF_WB_STREAMS] = {};
+  cudaEvent_t evt[GF_WB_EVENTS] = {};
 };
 // Parked handles beyond this many are destroyed at once, waiting or not.
 constexpr size_t kMaxParked = 64;
@@ -316,8 +316,8 @@ void retire(gf_server* S, size_t i) {
   if (B->b.sh.loops_in_graph) {
     Parked p;
     std::swap(p.graph, B->graph);
-    for (int k = 0; k < 3; ++k) std::swap(p.aux[k], B->b.sh.aux[k]);
-    for (int k = 0; k < 5; ++k) std::swap(p.evt[k], B->b.sh.evt[k]);
+    for (int k = 0; k < GF_WB_STREAMS; ++k) std::swap(p.aux[k], B->b.sh.aux[k]);
+    for (int k = 0; k < GF_WB_EVENTS; ++k) std::swap(p.evt[k], B->b.sh.evt[k]);
     S->parked.push_back(p);
     if (S->parked.size() > kMaxParked) {
       destroy_parked(S->parked.front());

@@ -909,7 +909,18 @@ __global__ void k_wb_zero(Batch b) {
     a[i] = 0.0;
 }
 
-// LU (no pivoting) of the diagonal block of panel p, in place.
+// LU (no pivoting) of the diagonal block of panel p, in place, right-looking
+// on a column-major copy in shared memory.  FP64 issue is the bound on this
+// part (about two FMA lanes per clock per SM), and a warp instruction costs
+// its full issue time however few of its lanes are live, so step k gives
+// each warp whole columns j = k + 1 + warp + 8 q of the trailing block with
+// its lanes on consecutive rows: a step issues about (m / 8) (1 + [m > 32])
+// FMA instructions per warp for a trailing size m, not a fixed 4 x 4 grid.
+// Warp 0 updates column k + 1 first and forms that column's multipliers
+// (pivot reciprocal, scaled entries) at once, so one barrier per step
+// suffices.  Each entry sees the same operations in the same order as the
+// textbook kij loop: multiplier l = a_ik * (1 / a_kk), then a_ij =
+// fma(-l, a_kj, a_ij) for k = 0, 1, ...
 __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
@@ -919,72 +930,70 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
   if (p >= inf.n_panels) return;
   WB w = wb_of(b, inf);
   const int j0 = p * NB, nb = min(NB, w.n - j0);
-  __shared__ double A[NB][NB + 1];
+  __shared__ double Ac[NB][NB + 1];  // Ac[j][i] = A(i, j)
   __shared__ int fail;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) fail = 0;
   // this panel's L21 / U12 maxima start at zero (the buffer of its parity
   // was last read by the slicing of panel p - 2, which precedes this kernel)
   if (b.sh.wide_tc && tid < 2 * NB) wb_kmax(b, blockIdx.x, p)[tid] = 0ull;
   for (int x = tid; x < NB * NB; x += blockDim.x) {
-    int i = x % NB, j = x / NB;
+    const int i = x % NB, j = x / NB;
     double v = 0.0;
     if (i < nb && j < nb && abs(i - j) <= w.kl) v = w.at(j0 + i, j0 + j);
-    A[i][j] = v;
+    Ac[j][i] = v;
   }
   __syncthreads();
-  // warp 0 forms the pivot's reciprocal and the multipliers of column k
-  // (the FP64 pipe is scarce: one warp, not every thread, computes the
-  // reciprocal); then the 16 x 16 threads update the trailing block, thread
-  // (ty, tx) on rows k + 1 + ty + 16 a and columns k + 1 + tx + 16 c
-  const int tx = tid & 15, ty = tid >> 4;
-  for (int k = 0; k < nb; ++k) {
-    if (tid < 32) {
-      const double piv = A[k][k];
-      if (tid == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
-      const double r = wb_recip(piv);
-      for (int i = k + 1 + tid; i < nb; i += 32) A[i][k] *= r;
-    }
-    __syncthreads();
-    // thread (ty, tx) owns rows ty + 16 a and columns tx + 16 c of the block;
-    // every operand is loaded before any store, so the 16 updates are
-    // independent and only the FP64 pipe bounds them
-    double l[4], u[4], v[4][4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      l[q] = A[ty + 16 * q][k];
-      u[q] = A[k][tx + 16 * q];
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) v[a][c] = A[ty + 16 * a][tx + 16 * c];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int i = ty + 16 * a, j = tx + 16 * c;
-        if (i > k && j > k && i < nb && j < nb) A[i][j] = fma(-l[a], u[c], v[a][c]);
+  if (warp == 0 && nb > 0) {  // the multipliers of column 0
+    const double piv = Ac[0][0];
+    if (lane == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
+    const double r = wb_recip(piv);
+    if (1 + lane < nb) Ac[0][1 + lane] *= r;
+    if (33 + lane < nb) Ac[0][33 + lane] *= r;
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < nb; ++k) {
+    const int i0 = k + 1 + lane, i1 = i0 + 32;
+    const bool two = k + 33 < nb;  // warp-uniform: a second chunk of rows
+    const double l0 = i0 < nb ? Ac[k][i0] : 0.0;
+    const double l1 = two && i1 < nb ? Ac[k][i1] : 0.0;
+    for (int j = k + 1 + warp; j < nb; j += 8) {
+      const double u = Ac[j][k];
+      if (i0 < nb) Ac[j][i0] = fma(-l0, u, Ac[j][i0]);
+      if (two && i1 < nb) Ac[j][i1] = fma(-l1, u, Ac[j][i1]);
+      if (j == k + 1) {
+        // warp 0: column k + 1 is final; its pivot and multipliers
+        __syncwarp();
+        const double piv = Ac[j][j];
+        if (lane == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
+        const double r = wb_recip(piv);
+        if (i0 > j && i0 < nb) Ac[j][i0] *= r;
+        if (two && i1 < nb) Ac[j][i1] *= r;
       }
+    }
     __syncthreads();
   }
   for (int x = tid; x < nb * nb; x += blockDim.x) {
-    int i = x % nb, j = x / nb;
-    if (abs(i - j) <= w.kl) w.at(j0 + i, j0 + j) = A[i][j];
+    const int i = x % nb, j = x / nb;
+    if (abs(i - j) <= w.kl) w.at(j0 + i, j0 + j) = Ac[j][i];
   }
   if (tid == 0 && fail) b.state[s].info_fail = 1;
 }
 
 // L21 = A21 U11^-1 (row blocks) and U12 = L11^-1 A12 (column blocks) of
-// panel p.  TRSM_RB rows (or columns) per CTA, a warp each splitting the
-// panel width; lane 0 forms each multiplier once and the warp reads it from
-// shared memory (the FP64 pipe is scarce).  The launch covers blocks
-// blk0 .. blk0 + nblk - 1 of both: blockIdx.x < nblk an L21 row block, else
-// a U12 column block.  The first blocks (the rows and columns of the next
-// panel's diagonal block) are a launch of their own on the lookahead's
-// critical path; the rest follow.
+// panel p.  RB rows (or columns) per CTA, a warp each splitting the panel
+// width; lane 0 forms each multiplier once and the warp reads it from shared
+// memory (the FP64 pipe is scarce).  The launch covers rows (columns)
+// row0 .. row0 + nblk RB - 1 below (right of) the panel's diagonal block:
+// blockIdx.x < nblk an L21 row block, else a U12 column block.  The first
+// NB rows and columns (the next panel's diagonal block, on the lookahead's
+// critical path) are a launch of their own with two rows per CTA, spread
+// over 64 SMs; the bulk runs beside it with eight.  Each CTA loads the half
+// of the diagonal block its side reads (U11 for L21, L11 for U12).
 constexpr int TRSM_RB = 8;
-__global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int nblk) {
+constexpr int TRSM_RB_FIRST = 2;
+template <int RB>
+__global__ void __launch_bounds__(32 * RB) k_wb_trsm(Batch b, int p, int row0, int nblk) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
@@ -995,21 +1004,20 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);  // rows below / columns right of the panel
   if (m <= 0) return;
-  const int nrb = (m + TRSM_RB - 1) / TRSM_RB;
   const bool lower = (int)blockIdx.x < nblk;
-  const int blk = blk0 + (lower ? (int)blockIdx.x : (int)blockIdx.x - nblk);
-  if (blk >= nrb) return;
-  __shared__ double T[NB][NB + 1];  // the diagonal block's LU
-  __shared__ double X[TRSM_RB][NB + 1];
+  const int rowb = row0 + RB * (lower ? (int)blockIdx.x : (int)blockIdx.x - nblk);
+  if (rowb >= m) return;
+  __shared__ double T[NB][NB + 1];  // the diagonal block's LU (the half this side reads)
+  __shared__ double X[RB][NB + 1];
   __shared__ double rd[NB];         // reciprocals of U11's diagonal
   const int tid = threadIdx.x;
   for (int x = tid; x < NB * NB; x += blockDim.x) {
     int i = x % NB, j = x / NB;
-    T[i][j] = (i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
+    T[i][j] = ((lower ? i <= j : i > j) && i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : 0.0;
   }
-  if (tid < nb) rd[tid] = wb_recip(w.at(j0 + tid, j0 + tid));
+  if (lower && tid < nb) rd[tid] = wb_recip(w.at(j0 + tid, j0 + tid));
   const int r = tid >> 5, c = tid & 31;  // row (or column) r of the block, lane c
-  const int g = j0 + nb + blk * TRSM_RB + r;  // global row (lower) or column (upper)
+  const int g = j0 + nb + rowb + r;      // global row (lower) or column (upper)
   const bool live = g < j0 + nb + m;
   for (int k = c; k < NB; k += 32) {
     double v = 0.0;
@@ -1049,8 +1057,8 @@ __global__ void __launch_bounds__(256) k_wb_trsm(Batch b, int p, int blk0, int n
     // maximum over the CTAs is exact and independent of their order
     const int k = tid;
     unsigned long long mx = 0;
-    for (int q = 0; q < TRSM_RB; ++q) {
-      const int gq = j0 + nb + blk * TRSM_RB + q;
+    for (int q = 0; q < RB; ++q) {
+      const int gq = j0 + nb + rowb + q;
       if (gq < j0 + nb + m && gq - (j0 + k) <= w.kl)
         mx = max(mx, (unsigned long long)__double_as_longlong(X[q][k]) & 0x7FFFFFFFFFFFFFFFull);
     }
@@ -1109,6 +1117,45 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
   if (ri1 < m && cj1 < m) w.at(base + ri1, base + cj1) -= a11;
 }
 
+// The corner of panel p's trailing update: the next panel's diagonal block
+// (the first NB rows and columns of the window), on the lookahead's critical
+// path.  8 x 8 output tiles, one output per thread: the 262 k FMAs spread
+// over 64 CTAs instead of the four of k_wb_update's 32 x 32 tiles, and each
+// output is the same fma chain over k = 0..NB-1 as there.
+constexpr int CT8 = 8;
+__global__ void __launch_bounds__(CT8 * CT8) k_wb_corner(Batch b, int p) {
+  p = wb_panel(b, p);
+  if (p < 0) return;
+  int s = b.sh.wide_structs[blockIdx.z];
+  if (!wide_active(b, s)) return;
+  const StructInfo& inf = b.info[s];
+  if (p >= inf.n_panels) return;
+  WB w = wb_of(b, inf);
+  const int j0 = p * NB, nb = min(NB, w.n - j0);
+  const int m = min(min(w.kl, w.n - j0 - nb), NB);
+  const int r0 = blockIdx.x * CT8, c0 = blockIdx.y * CT8;
+  if (r0 >= m || c0 >= m) return;
+  __shared__ double Ls[NB][CT8 + 1];  // [k][row]
+  __shared__ double Us[NB][CT8 + 1];  // [k][col]
+  const int tid = threadIdx.x;
+  const int base = j0 + nb;
+  for (int x = tid; x < NB * CT8; x += blockDim.x) {
+    // rows of L21 along a band column are contiguous; U12's k along a
+    // band column too
+    const int i = x % CT8, k = x / CT8;
+    const int gk = j0 + k, gi = base + r0 + i;
+    Ls[k][i] = (k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
+    const int kk = x % NB, c = x / NB, gj = base + c0 + c;
+    Us[kk][c] = (kk < nb && c0 + c < m && gj - (j0 + kk) <= w.kl) ? w.at(j0 + kk, gj) : 0.0;
+  }
+  __syncthreads();
+  const int ty = tid / CT8, tx = tid % CT8;
+  double a = 0.0;
+#pragma unroll 16
+  for (int k = 0; k < NB; ++k) a = fma(Ls[k][ty], Us[k][tx], a);
+  if (r0 + ty < m && c0 + tx < m) w.at(base + r0 + ty, base + c0 + tx) -= a;
+}
+
 // ---- the same trailing update on the tensor cores (Ozaki scheme) ----
 // A22 -= L21 U12 for one 64x64 output tile with K = NB = 64, the FP64
 // products emulated by bf16 tensor-core products of exact slices.  First
@@ -1139,8 +1186,6 @@ constexpr int OZ_TR = 32;  // output tile rows: two CTAs fit on an SM
 constexpr int OZ_LD = 72;  // bf16 row stride of the slice tiles: 144 B, so the 8 rows of an ldmatrix hit distinct banks
 constexpr int OZ_THREADS = 256;
 constexpr size_t OZ_SMEM = sizeof(__nv_bfloat16) * OZ_S * (OZ_TR + OZ_T) * OZ_LD + sizeof(int) * (OZ_TR + OZ_T);
-// The slicing kernel's FP64 tile
-constexpr size_t OZ_SLICE_SMEM = sizeof(double) * OZ_T * (NB + 1) + sizeof(int) * OZ_T;
 
 __device__ __forceinline__ void oz_ldmatrix_x4(unsigned (&r)[4], const __nv_bfloat16* p) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(p);
@@ -1202,11 +1247,14 @@ __device__ __forceinline__ OzSlices oz_slices(const Batch& b, int z) {
   return o;
 }
 
-// Slices of panel p's L21 (blockIdx.y = 0: 64 rows) or U12 (blockIdx.y = 1:
-// 64 columns) into the structure's slice buffers: the FP64 block through
-// shared memory (consecutive threads walk a band column), the scale
-// exponent of every row or column, then its OZ_S slices.  Rows or columns
-// beyond the trailing window are zero.
+// Slices of panel p's L21 (blockIdx.y = 0: SL_ROWS rows) or U12
+// (blockIdx.y = 1: SL_ROWS columns) into the structure's slice buffers: the
+// FP64 block through shared memory (consecutive threads walk a band column:
+// down the rows of L21, along k for U12), the scale exponent of every row or
+// column, then its OZ_S slices.  Rows or columns beyond the trailing window
+// are zero.  Small blocks spread the panel over about a hundred CTAs: the
+// work is a few loads and integer operations per entry, bound by latency.
+constexpr int SL_ROWS = 16;
 __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
@@ -1218,12 +1266,11 @@ __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);
   if (m <= 0) return;
-  const int r0 = blockIdx.x * OZ_T;
+  const int r0 = blockIdx.x * SL_ROWS;
   if (r0 >= m) return;
   const bool lower = blockIdx.y == 0;
-  extern __shared__ __align__(16) unsigned char oz_raw[];
-  double* F = reinterpret_cast<double*>(oz_raw);  // [row or column][k], stride NB + 1
-  int* e = reinterpret_cast<int*>(F + OZ_T * (NB + 1));
+  __shared__ double F[SL_ROWS][NB + 1];  // [row or column][k]
+  __shared__ int e[SL_ROWS];
   __shared__ double bal[NB];  // 2^-f_k for L21 columns, 2^f_k for U12 rows
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int base = j0 + nb;
@@ -1241,15 +1288,15 @@ __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
     bal[tid] = ldexp(1.0, lower ? -f : f);
   }
   __syncthreads();
-  for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
-    const int i = x % OZ_T, k = x / OZ_T, gk = j0 + k, g = base + r0 + i;
+  for (int x = tid; x < SL_ROWS * NB; x += blockDim.x) {
+    const int i = lower ? x % SL_ROWS : x / NB, k = lower ? x / SL_ROWS : x % NB;
+    const int gk = j0 + k, g = base + r0 + i;
     const bool live = k < nb && r0 + i < m && g - gk <= w.kl;
-    F[i * (NB + 1) + k] = live ? (lower ? w.at(g, gk) : w.at(gk, g)) * bal[k] : 0.0;
+    F[i][k] = live ? (lower ? w.at(g, gk) : w.at(gk, g)) * bal[k] : 0.0;
   }
   __syncthreads();
-  for (int q = 0; q < OZ_T / 8; ++q) {
-    const int i = warp * (OZ_T / 8) + q;
-    unsigned long long mx = max(oz_mag(F[i * (NB + 1) + lane]), oz_mag(F[i * (NB + 1) + lane + 32]));
+  for (int i = warp; i < SL_ROWS; i += 8) {
+    unsigned long long mx = max(oz_mag(F[i][lane]), oz_mag(F[i][lane + 32]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) e[i] = oz_exponent(mx);
@@ -1258,14 +1305,14 @@ __global__ void __launch_bounds__(256) k_wb_slice(Batch b, int p) {
   OzSlices o = oz_slices(b, blockIdx.z);
   __nv_bfloat16* dst = lower ? o.L : o.U;
   const int64_t R = b.sh.oz_rows;
-  for (int x = tid; x < OZ_T * NB; x += blockDim.x) {
+  for (int x = tid; x < SL_ROWS * NB; x += blockDim.x) {
     const int i = x / NB, k = x % NB;
     // the 128-byte swizzle: 16-byte chunk k / 8 of row r stored at chunk
     // (k / 8) ^ (r & 7)
     const int r = r0 + i, ks = (((k >> 3) ^ (r & 7)) << 3) | (k & 7);
-    oz_split(F[i * (NB + 1) + k], e[i], dst + (int64_t)r * NB + ks, (int)(R * NB));
+    oz_split(F[i][k], e[i], dst + (int64_t)r * NB + ks, (int)(R * NB));
   }
-  if (tid < OZ_T) (lower ? o.eL : o.eU)[r0 + tid] = e[tid];
+  if (tid < SL_ROWS) (lower ? o.eL : o.eU)[r0 + tid] = e[tid];
 }
 
 __device__ __forceinline__ void oz_cp16(void* dst, const void* src) {
@@ -1757,43 +1804,49 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
   k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
 }
 
-// Row (column) blocks of TRSM_RB in the first trsm launch of a panel: the 64
-// rows and columns that the next panel's diagonal block needs.
-constexpr int TRSM_FIRST = NB / TRSM_RB;
+// The trsm of a panel: the first NB rows and columns (the next panel's
+// diagonal block needs them) in CTAs of TRSM_RB_FIRST, the rest in CTAs of
+// TRSM_RB.
+constexpr int TRSM_FIRST = NB / TRSM_RB_FIRST;
+__host__ __device__ constexpr int trsm_rest_blocks(int kl) { return kl > NB ? (kl - NB + TRSM_RB - 1) / TRSM_RB : 0; }
 
-// Panel loop with lookahead on two helper streams (fork / join by events,
+// Panel loop with lookahead on three helper streams (fork / join by events,
 // so a captured pass keeps the same dependencies):
-//   main   trsm(p) -> update corner(p) -> update rest(p) -> [join diag(p+1)]
+//   main   trsm first(p) -> corner(p) -> [join trsm rest(p)] -> update rest(p)
+//          -> [join diag(p+1)]
+//   s4     [at the panel's start] trsm rest(p)
 //   s2     [after corner(p)] diag(p+1)
-//   s3     [after trsm(p)]   forward substitution of panel p
-// The next panel's diagonal LU and the forward substitution run while the
-// bulk of the trailing update occupies the SMs; the backward substitution
-// follows the last panel.
+//   s3     [after all trsm(p)] forward substitution of panel p
+// The critical path per panel is the first trsm blocks, the corner and the
+// next diagonal LU; the bulk trsm runs beside them, and the next diagonal LU
+// and the forward substitution beside the bulk of the trailing update.  The
+// backward substitution follows the last panel.
 // The trailing update of panel p (part as in k_wb_update): on the tensor
 // cores (64x64 tiles) when the batch asks for it, else in FP64 (32x32).
 // The corner (the next panel's diagonal block, on the lookahead's critical
-// path) always takes the FP64 kernel: four small CTAs finish it sooner than
-// one tensor-core CTA's load, slice and multiply sequence.
+// path) always takes the FP64 kernel k_wb_corner: 64 small CTAs finish it
+// sooner than one tensor-core CTA's load, slice and multiply sequence.
 static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
   const int nw = b.sh.n_wide, mr = b.sh.max_kl;
   if (b.sh.wide_tc && part != 1) {
     static const bool attr = [] {  // once per process, thread-safe
       cudaFuncSetAttribute(k_wb_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM);
       cudaFuncSetAttribute(k_wb_update_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
-      cudaFuncSetAttribute(k_wb_slice, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SLICE_SMEM);
       return true;
     }();
     (void)attr;
     // the panel's slices (L21 rows and U12 columns), then the tiles
-    k_wb_slice<<<dim3((mr + OZ_T - 1) / OZ_T, 2, nw), 256, OZ_SLICE_SMEM, st>>>(b, p);
+    k_wb_slice<<<dim3((mr + SL_ROWS - 1) / SL_ROWS, 2, nw), 256, 0, st>>>(b, p);
     if (b.sh.wide_tc == 1)  // GF_WIDE_TENSOR: tcgen05; 2, GF_WIDE_TENSOR_SYNC: mma.sync
       k_wb_update_t5<<<dim3((mr + T5_M - 1) / T5_M, (mr + T5_N - 1) / T5_N, nw), T5_THREADS, T5_SMEM, st>>>(b, p,
                                                                                                          part);
     else
       k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
                                                                                                         part);
+  } else if (part == 1) {
+    k_wb_corner<<<dim3(NB / CT8, NB / CT8, nw), CT8 * CT8, 0, st>>>(b, p);
   } else {
-    const int t = part == 1 ? (NB + UT - 1) / UT : (mr + UT - 1) / UT;
+    const int t = (mr + UT - 1) / UT;
     k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
   }
 }
@@ -1848,9 +1901,10 @@ cudaError_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_
 static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide, mr = sd.max_kl, P = sd.max_panels;
-  const int nrb = (mr + TRSM_RB - 1) / TRSM_RB, rb = (mr + 255) / 256;
-  cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1];
-  cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
+  const int nrest = trsm_rest_blocks(mr), rb = (mr + 255) / 256;
+  cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1], s4 = sd.aux[3];
+  cudaEvent_t e_start = sd.evt[0], e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4],
+              e_rest = sd.evt[5];
   if (P <= 0) return cudaSuccess;
   cudaError_t e;
   cudaGraphConditionalHandle h;
@@ -1860,13 +1914,19 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
   if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
-  k_wb_trsm<<<dim3(2 * TRSM_FIRST, nw), 256, 0, sb>>>(b, -1, 0, TRSM_FIRST);
+  if (nrest) {
+    cudaEventRecord(e_start, sb);
+    cudaStreamWaitEvent(s4, e_start, 0);
+    k_wb_trsm<TRSM_RB><<<dim3(2 * nrest, nw), 32 * TRSM_RB, 0, s4>>>(b, -1, NB, nrest);
+    cudaEventRecord(e_rest, s4);
+  }
+  k_wb_trsm<TRSM_RB_FIRST><<<dim3(2 * TRSM_FIRST, nw), 32 * TRSM_RB_FIRST, 0, sb>>>(b, -1, 0, TRSM_FIRST);
   launch_wb_update(b, -1, 1, sb);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
   k_wb_diag<<<nw, 256, 0, s2>>>(b, -2);
   cudaEventRecord(e_diag, s2);
-  if (nrb > TRSM_FIRST) k_wb_trsm<<<dim3(2 * (nrb - TRSM_FIRST), nw), 256, 0, sb>>>(b, -1, TRSM_FIRST, nrb - TRSM_FIRST);
+  if (nrest) cudaStreamWaitEvent(sb, e_rest, 0);
   cudaEventRecord(e_trsm, sb);
   cudaStreamWaitEvent(s3, e_trsm, 0);
   k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
@@ -1898,20 +1958,27 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide;
   const int mr = sd.max_kl;  // largest kl over the wide structures
-  const int nrb = (mr + TRSM_RB - 1) / TRSM_RB;
+  const int nrest = trsm_rest_blocks(mr);
   const int rb = (mr + 255) / 256;
-  cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1];
+  cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1], s4 = sd.aux[3];
   // the helpers fork from the main stream at their first wait and join it
   // again before the backward substitution
-  cudaEvent_t e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4];
+  cudaEvent_t e_start = sd.evt[0], e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4],
+              e_rest = sd.evt[5];
   { ProfScope q(prof, st, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, st>>>(b, 0); }
   for (int p = 0; p < sd.max_panels; ++p) {
     bool next = p + 1 < sd.max_panels;
-    // the first row and column blocks of L21 / U12, the corner update and
-    // the next diagonal LU form the lookahead's critical path; the rest of
-    // the trsm, the forward step and the bulk of the update run beside the
-    // next diagonal LU
-    { ProfScope q(prof, st, KC_WIDE_TRSM); k_wb_trsm<<<dim3(2 * TRSM_FIRST, nw), 256, 0, st>>>(b, p, 0, TRSM_FIRST); }
+    if (nrest) {
+      cudaEventRecord(e_start, st);
+      cudaStreamWaitEvent(s4, e_start, 0);
+      ProfScope q(prof, s4, KC_WIDE_TRSM);
+      k_wb_trsm<TRSM_RB><<<dim3(2 * nrest, nw), 32 * TRSM_RB, 0, s4>>>(b, p, NB, nrest);
+      cudaEventRecord(e_rest, s4);
+    }
+    {
+      ProfScope q(prof, st, KC_WIDE_TRSM);
+      k_wb_trsm<TRSM_RB_FIRST><<<dim3(2 * TRSM_FIRST, nw), 32 * TRSM_RB_FIRST, 0, st>>>(b, p, 0, TRSM_FIRST);
+    }
     if (next) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 1, st); }
       cudaEventRecord(e_corner, st);
@@ -1919,10 +1986,7 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
       { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, s2>>>(b, p + 1); }
       cudaEventRecord(e_diag, s2);
     }
-    if (nrb > TRSM_FIRST) {
-      ProfScope q(prof, st, KC_WIDE_TRSM);
-      k_wb_trsm<<<dim3(2 * (nrb - TRSM_FIRST), nw), 256, 0, st>>>(b, p, TRSM_FIRST, nrb - TRSM_FIRST);
-    }
+    if (nrest) cudaStreamWaitEvent(st, e_rest, 0);
     cudaEventRecord(e_trsm, st);
     cudaStreamWaitEvent(s3, e_trsm, 0);
     { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
@@ -2005,7 +2069,7 @@ int shell_launches_per_pass(const Batch& b) {
   // LU, the same six or seven kernels and a counter step per forward
   // iteration, and two kernels per backward one
   if (b.sh.n_wide) {
-    const int P = b.sh.max_panels, per = 6 + ((b.sh.max_kl + TRSM_RB - 1) / TRSM_RB > TRSM_FIRST ? 1 : 0);
+    const int P = b.sh.max_panels, per = 6 + (trsm_rest_blocks(b.sh.max_kl) ? 1 : 0);
     n += (b.sh.loops_in_graph ? 3 + (per + 2) * P : 1 + per * P - 2) +
          (b.sh.wide_tc ? P : 0);  // the tensor-core update's slicing kernel
   }

@@ -75,8 +75,8 @@ struct DevBufs {
 // Helper streams and events of the wide LU's lookahead; destroyed on scope
 // exit.
 struct Helpers {
-  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t evt[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t aux[GF_WB_STREAMS] = {};
+  cudaEvent_t evt[GF_WB_EVENTS] = {};
   ~Helpers() {
     for (auto& a : aux)
       if (a) cudaStreamDestroy(a);
@@ -146,8 +146,8 @@ struct WideBatch {
     sd.oz_exp = se;
     sd.oz_kmax = km;
     sd.oz_error = err;
-    for (int k = 0; k < 3; ++k) sd.aux[k] = hl.aux[k];
-    for (int k = 0; k < 5; ++k) sd.evt[k] = hl.evt[k];
+    for (int k = 0; k < GF_WB_STREAMS; ++k) sd.aux[k] = hl.aux[k];
+    for (int k = 0; k < GF_WB_EVENTS; ++k) sd.evt[k] = hl.evt[k];
     return true;
   }
   // Factor and solve on the context's stream; *fail = the pivot status.

@@ -24,6 +24,8 @@
 #define GF_KB 17
 #define GF_LDB (2 * GF_KB + 1)
 #define GF_UW (GF_KB + 1)
+#define GF_WB_STREAMS 4  // helper streams of the wide-band lookahead
+#define GF_WB_EVENTS 6
 
 namespace gf {
 
@@ -271,11 +273,14 @@ struct ShellData {
   // nonzero when a bounded wait of the tensor-core update gave up (its
   // structures are then reported as failed solves)
   int* oz_error;
-  // host handles of the wide-band lookahead: two helper streams and the
-  // events that fork from and join into the pass's stream; aux[2] roots the
-  // captured panel-loop bodies
-  cudaStream_t aux[3];
-  cudaEvent_t evt[5];  // [1] after trsm, [2] after the corner update, [3] after diag, [4] end of forward
+  // host handles of the wide-band lookahead: helper streams and the events
+  // that fork from and join into the pass's stream; aux[2] roots the
+  // captured panel-loop bodies, aux[3] runs the bulk trsm beside the first
+  // blocks and the corner update
+  cudaStream_t aux[GF_WB_STREAMS];
+  // [0] panel start, [1] after trsm, [2] after the corner update, [3] after
+  // diag, [4] end of forward, [5] after the bulk trsm
+  cudaEvent_t evt[GF_WB_EVENTS];
 };
 
 // Device pointers of a batch.
