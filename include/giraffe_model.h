@@ -38,8 +38,8 @@ typedef struct gf_table {
  * beam indices of Pipe_1 elements), four table columns P0I P0E RhoI RhoE, of
  * which the internal pressure P0I acts (on the section's internal area). */
 typedef struct gf_load {
-  int type;            /* GF_LOAD_NODAL or GF_LOAD_SHELL_PRESSURE */
-  int n_items;         /* nodes (nodal) or shell elements (pressure) */
+  int type;            /* GF_LOAD_NODAL, GF_LOAD_SHELL_PRESSURE or GF_LOAD_PIPE_PRESSURE */
+  int n_items;         /* nodes (nodal), shell elements or Pipe_1 beams (pressure) */
   const int* items;
   int cs;              /* coordinate system of a nodal load */
   int area_update;     /* pressure: 1 = follow the current area */

@@ -27,12 +27,24 @@ def _solve(ctx, structs):
     return out
 
 
+def _static_pipes(n_el, pressure, steps=10):
+    """A Static pipe chain clamped at one end under a tip force, its Pipe_1
+    elements all under an internal pressure raised with the load factor."""
+    s = configs.pipe_chain(n_el, 0.4, 0.03, [4e4, -1e4, 2e4], steps=steps)
+    ps = s.add_pipe_section(2e9, 4e8, 3e8, 8e8, 300.0, 0.4, 0.34)
+    for e in range(len(s.beams)):
+        s.pipe_of[e] = ps
+    s.loads.append(PipeLoad(list(range(n_el)), Table(np.array([0.0, 1.0]),
+                                                    np.array([[0.0] * 4, [pressure, 0.0, 0.0, 0.0]]))))
+    return s
+
+
 def test_first_assembly_with_pressure_matches_oracle(gpu_ctx):
-    """K_AA and P_A of the first Newton iteration: pressurized pipes (the
-    pressure is already nonzero at the first step's time), one under
-    external-like negative pressure, and a Beam_1 chain in the same batch."""
-    structs = [configs.pipe_riser(), configs.pipe_riser(9, pressure=-5e6, steps=20),
-               configs.pipe_chain(23, 0.35, 0.025, [1e5, 2e4, -3e4])]
+    """K_AA and P_A of the first Newton iteration of Static steps:
+    pressurized pipes (the pressure is already nonzero at the first step's
+    time), one under a negative pressure, and a Beam_1 chain in the same
+    batch."""
+    structs = [_static_pipes(12, 8e6), _static_pipes(7, -5e6), configs.pipe_chain(23, 0.35, 0.025, [1e5, 2e4, -3e4])]
     b = gpu.BatchSolver(gpu_ctx, structs)
     for s, st in enumerate(structs):
         ab, P, kb = b.assemble(s)
@@ -84,12 +96,8 @@ def test_pressurized_pipes_beside_beams_match_the_oracle(gpu_ctx):
                                           amp=float(rng.uniform(0.2, 1.0)), steps=40,
                                           rayleigh_alpha=0.2 if k % 3 == 2 else 0.0,
                                           rayleigh_beta=0.003 if k % 3 == 2 else 0.0))
-    st = configs.pipe_chain(16, 0.4, 0.03, [4e4, 0.0, 0.0], steps=8)
-    ps = st.add_pipe_section(2e9, 4e8, 3e8, 8e8, 300.0, 0.4, 0.34)
-    for e in range(len(st.beams)):
-        st.pipe_of[e] = ps
-    st.loads.append(PipeLoad(list(range(0, 16, 2)), Table(np.array([0.0, 1.0]),
-                                                          np.array([[0.0] * 4, [8e6, 0.0, 0.0, 0.0]]))))
+    st = _static_pipes(16, 8e6, steps=8)
+    st.loads[1].pipes = list(range(0, 16, 2))  # every other element pressurized
     structs.append(st)
     structs += [configs.riser_chain(int(n), 0.4, 0.03, 1.0, 6.0, steps=40) for n in (15, 31)]
     finals, stats = _solve(gpu_ctx, structs)
