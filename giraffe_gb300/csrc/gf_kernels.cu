@@ -509,13 +509,19 @@ __global__ void k_beam_rayleigh(Batch b) {
 // Its O1 term reads the element's scalar g, which the reference's Mount
 // leaves at the second Gauss point's value (src/Pipe_1.cpp:890), for both
 // points.  One thread per pressurized element, after k_beam_tangent has
-// written K_e and f_e.
+// written K_e and f_e and before k_beam_rayleigh: in a Dynamic step the
+// reference mounts loads before damping, so on the iterations that form
+// C_e the load stiffness also goes into the stiffness part that C_e is
+// made from.
 __global__ void k_pipe_pressure(Batch b) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= b.n_pipe_press) return;
   const int e = b.pp_elem[q];
-  const StructState& st = b.state[b.estruct[e]];
+  const int s = b.estruct[e];
+  const StructState& st = b.state[s];
   if (!iterating(st)) return;
+  const StructParams& pr = b.params[s];
+  const bool form_c = pr.dynamic && pr.ray_on && (pr.ray_update || !st.ray_init);
   const double p0i = table_at(b, b.pp_table[q], st.last_converged_time + st.current_time_step, 0);
   const double Aint = b.pp_aint[q];
   const BeamConst& c = b.bconst[e];
@@ -537,6 +543,7 @@ __global__ void k_pipe_pressure(Batch b) {
   const int64_t ne = b.n_elem;
   double* Ke = b.Ke + e;
   double* Fe = b.Fe + e;
+  double* Ce = form_c ? b.RD + e : nullptr;
 #pragma unroll 1
   for (int g = 0; g < 2; ++g) {
     const BeamInterp ip = beam_interp(c, d, g);
@@ -594,9 +601,18 @@ __global__ void k_pipe_pressure(Batch b) {
             const int x = i * 3 + j;
             // (u_a, alpha_b): K1ua Nb + K2ua dNb; (alpha_a, u_b): K2au dNb;
             // (alpha_a, alpha_b): K1aa Nb
-            Ke[(int64_t)((6 * a + i) + 18 * (6 * n + 3 + j)) * ne] -= sK * (Na * (Nb * G1[x] + dNb * G2[x]));
-            Ke[(int64_t)((6 * a + 3 + i) + 18 * (6 * n + j)) * ne] -= sK * (Na * (dNb * G3[x]));
-            Ke[(int64_t)((6 * a + 3 + i) + 18 * (6 * n + 3 + j)) * ne] -= sK * (Na * (Nb * G4[x]));
+            const int64_t x1 = (6 * a + i) + 18 * (6 * n + 3 + j), x2 = (6 * a + 3 + i) + 18 * (6 * n + j),
+                          x3 = (6 * a + 3 + i) + 18 * (6 * n + 3 + j);
+            const double v1 = sK * (Na * (Nb * G1[x] + dNb * G2[x])), v2 = sK * (Na * (dNb * G3[x])),
+                         v3 = sK * (Na * (Nb * G4[x]));
+            Ke[x1 * ne] -= v1;
+            Ke[x2 * ne] -= v2;
+            Ke[x3 * ne] -= v3;
+            if (Ce) {
+              Ce[x1 * ne] -= v1;
+              Ce[x2 * ne] -= v2;
+              Ce[x3 * ne] -= v3;
+            }
           }
       }
     }
@@ -1237,8 +1253,10 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
       k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
     else
       k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
-    if (b.any_rayleigh) k_beam_rayleigh<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
+    // the pressure's load stiffness is part of the K_e that Rayleigh damping
+    // reads (the reference mounts loads before damping)
     if (b.n_pipe_press) k_pipe_pressure<<<(b.n_pipe_press + 127) / 128, 128, 0, st>>>(b);
+    if (b.any_rayleigh) k_beam_rayleigh<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
   }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];
