@@ -148,6 +148,26 @@ struct gf_batch {
   double host_ms[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 };
 
+// A device-resident structure driven one Newton iteration at a time
+// (gf_iter.cu) and its modal analysis (gf_modal.cu).
+struct gf_structure {
+  gf_ctx* ctx = nullptr;
+  gf_batch* B = nullptr;
+  int nf = 0;            // free DOFs
+  int kb = 0;            // half-bandwidth of K_AA in the reference's numbering
+  int n_nodes = 0;
+  std::vector<int> perm;      // reference free index -> solver index (empty: the same)
+  std::vector<int> dof_node;  // reference free index -> node * 6 + DOF
+  std::vector<int> rp, ci;    // CSR pattern (reference numbering)
+  int64_t* d_src = nullptr;   // per CSR entry: offset into the structure's band, or -1
+  double* d_val = nullptr;    // CSR values on the device
+  double* d_band = nullptr;   // the structure's band (solver numbering)
+  int64_t W = 0, kw = 0;      // band rows and half-bandwidth (solver numbering)
+  int iteration = 0;
+  bool in_step = false;
+  std::vector<double> h_tmp;
+};
+
 namespace gfh {
 bool set_err(gf_ctx* ctx, const char* fmt, ...);
 // Builds the device batch of n structures (or, with B->count_only, only
@@ -178,6 +198,9 @@ void shell_precalc(const double* xyz, const double* mat, double thick, gf::Shell
 // CSR pattern of structure s's K_AA in the reference's free-DOF numbering
 // (sorted columns per row); returns nnz.
 int64_t csr_rows(const gf_batch* B, int s, std::vector<std::vector<int>>& rows);
+// K_AA of a device-resident structure's current configuration, static, with
+// the loads at `time`, into its band (gf_iter.cu).
+int structure_static_tangent(gf_structure* S, double time);
 }  // namespace gfh
 
 #define GF_CK(call)                                                                          \

@@ -38,23 +38,6 @@
 using namespace gf;
 using namespace gfh;
 
-struct gf_structure {
-  gf_ctx* ctx = nullptr;
-  gf_batch* B = nullptr;
-  int nf = 0;            // free DOFs
-  int kb = 0;            // half-bandwidth of K_AA in the reference's numbering
-  int n_nodes = 0;
-  std::vector<int> perm;      // reference free index -> solver index (empty: the same)
-  std::vector<int> dof_node;  // reference free index -> node * 6 + DOF
-  std::vector<int> rp, ci;    // CSR pattern (reference numbering)
-  int64_t* d_src = nullptr;   // per CSR entry: offset into the structure's band, or -1
-  double* d_val = nullptr;    // CSR values on the device
-  double* d_band = nullptr;   // the structure's band (solver numbering)
-  int64_t W = 0, kw = 0;      // band rows and half-bandwidth (solver numbering)
-  int iteration = 0;
-  bool in_step = false;
-  std::vector<double> h_tmp;
-};
 
 namespace {
 
@@ -90,6 +73,20 @@ __global__ void k_iter_step(Batch b, int k) {
   st.step = k;
   st.ray_init = 0;
   st.zero_va = np.zero_va;
+}
+
+// The static tangent of the structure's current configuration, as a Modal
+// step mounts it (reference src/Modal.cpp:157-166): the step's parameters
+// with inertia and damping off for the assembly (restore = 0), then the
+// step's own parameters again (restore = 1).
+__global__ void k_iter_static(Batch b, int restore) {
+  StructParams& p = b.params[0];
+  if (restore) {
+    p = b.step_params[b.info[0].step_off + b.state[0].step];
+  } else {
+    p.dynamic = 0;
+    p.ray_on = 0;
+  }
 }
 
 __global__ void k_csr_gather(int64_t nnz, const int64_t* src, const double* band, double* val) {
@@ -172,6 +169,28 @@ void shell_state_out(const ShellHist& h, const ShellHistAux& x, double* L3) {
 }
 
 }  // namespace
+
+namespace gfh {
+// K_AA of the structure's current configuration with zero increments and
+// the loads at `time`, statically (no inertia or damping), in the
+// structure's band (S->d_band, solver numbering).  Ends any step the caller
+// had begun: a new gf_begin_step follows.
+int structure_static_tangent(gf_structure* S, double time) {
+  gf_ctx* ctx = S->ctx;
+  gf_batch* B = S->B;
+  cudaStream_t st = B->stream;
+  k_iter_static<<<1, 1, 0, st>>>(B->b, 0);
+  k_iter_begin<<<1, 1, 0, st>>>(B->b, time, 0.0);
+  launch_step_begin(B->b, st);
+  k_iter_set<<<1, 1, 0, st>>>(B->b, 1, -1, -1, -1);
+  launch_assembly(B->b, st);
+  k_iter_static<<<1, 1, 0, st>>>(B->b, 1);
+  k_iter_set<<<1, 1, 0, st>>>(B->b, 0, -1, PH_START, 0);
+  S->in_step = false;
+  GF_CK(cudaGetLastError());
+  return GF_OK;
+}
+}  // namespace gfh
 
 extern "C" {
 
@@ -341,6 +360,7 @@ int gf_assemble(gf_structure* S, int layout, double* K, double* P_A) {
   }
   return GF_OK;
 }
+
 
 int gf_set_increment(gf_structure* S, const double* x) {
   if (!S || !x) return GF_ERR_ARG;

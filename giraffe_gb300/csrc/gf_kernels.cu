@@ -400,6 +400,61 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
 // turned to the global frame block by block (T3^T B T3).  Every iteration
 // then adds a4 C_e to K_e and C_e v to f_e, v the nodes' current
 // velocities.  One thread per element; C_e is structure-of-arrays like K_e.
+// The modal mass of a Beam_1 / Pipe_1 element: per Gauss point D[g][0] =
+// Q Mr Q^T and D[g][1] = Q Jr Q^T (3x3 row-major) with Q = Q(alpha_i).
+__device__ void beam_modal_D(const BeamConst& c, const BeamHistAux& x, double (*D)[2][9]) {
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    M3<double> Q = rodrigues(V3<double>{{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}});
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double mt = 0.0, jt = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          double qm = 0.0, qj = 0.0;
+#pragma unroll
+          for (int l = 0; l < 3; ++l) {
+            qm += Q[i * 3 + l] * (l == k ? c.Mr : 0.0);
+            qj += Q[i * 3 + l] * c.Jr[l * 3 + k];
+          }
+          mt += qm * Q[j * 3 + k];
+          jt += qj * Q[j * 3 + k];
+        }
+        D[g][0][i * 3 + j] = mt;
+        D[g][1][i * 3 + j] = jt;
+      }
+  }
+}
+
+// Block (node I, node J, translation/rotation bi, bj) of the element's modal
+// mass in the global frame, 3x3 row-major: sum_g jac N_gI N_gJ D[g][bi]
+// turned by T^T (.) T on the diagonal blocks bi == bj, zero off them.
+__device__ void beam_modal_block(const BeamConst& c, const double (*D)[2][9], int I, int J, int bi, int bj,
+                                 double* m) {
+#pragma unroll
+  for (int q = 0; q < 9; ++q) m[q] = 0.0;
+  if (bi != bj) return;
+  const double* T = c.T3;
+  double loc[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    loc[q] = 0.0;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) loc[q] += ((c.jac * c.N[g][I]) * D[g][bi][q]) * c.N[g][J];
+  }
+  double t2[9];  // loc T, then T^T (loc T)
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) t2[i * 3 + j] = loc[i * 3] * T[j] + loc[i * 3 + 1] * T[3 + j] + loc[i * 3 + 2] * T[6 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) m[i * 3 + j] = T[i] * t2[j] + T[3 + i] * t2[3 + j] + T[6 + i] * t2[6 + j];
+}
+
 __global__ void k_beam_rayleigh(Batch b) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= b.n_elem) return;
@@ -412,32 +467,8 @@ __global__ void k_beam_rayleigh(Batch b) {
   double* C = b.RD + e;
   if (p.ray_update || !st.ray_init) {
     const BeamConst& c = b.bconst[e];
-    const BeamHistAux& x = b.baux[e];
     double D[2][2][9];  // [Gauss point][translation, rotation][3x3 row-major]
-#pragma unroll
-    for (int g = 0; g < 2; ++g) {
-      M3<double> Q = rodrigues(V3<double>{{x.alpha[g][0], x.alpha[g][1], x.alpha[g][2]}});
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          double mt = 0.0, jt = 0.0;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            double qm = 0.0, qj = 0.0;
-#pragma unroll
-            for (int l = 0; l < 3; ++l) {
-              qm += Q[i * 3 + l] * (l == k ? c.Mr : 0.0);
-              qj += Q[i * 3 + l] * c.Jr[l * 3 + k];
-            }
-            mt += qm * Q[j * 3 + k];
-            jt += qj * Q[j * 3 + k];
-          }
-          D[g][0][i * 3 + j] = mt;
-          D[g][1][i * 3 + j] = jt;
-        }
-    }
-    const double* T = c.T3;
+    beam_modal_D(c, b.baux[e], D);
 #pragma unroll 1
     for (int I = 0; I < 3; ++I)
 #pragma unroll 1
@@ -447,28 +478,7 @@ __global__ void k_beam_rayleigh(Batch b) {
 #pragma unroll 1
           for (int bj = 0; bj < 2; ++bj) {
             double m[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) m[q] = 0.0;
-            if (bi == bj) {
-              double loc[9];
-#pragma unroll
-              for (int q = 0; q < 9; ++q) {
-                loc[q] = 0.0;
-#pragma unroll
-                for (int g = 0; g < 2; ++g) loc[q] += ((c.jac * c.N[g][I]) * D[g][bi][q]) * c.N[g][J];
-              }
-              double t2[9];  // loc T, then T^T (loc T)
-#pragma unroll
-              for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                  t2[i * 3 + j] = loc[i * 3] * T[j] + loc[i * 3 + 1] * T[3 + j] + loc[i * 3 + 2] * T[6 + j];
-#pragma unroll
-              for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                  m[i * 3 + j] = T[i] * t2[j] + T[3 + i] * t2[3 + j] + T[6 + i] * t2[6 + j];
-            }
+            beam_modal_block(c, D, I, J, bi, bj, m);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -617,6 +627,37 @@ __global__ void k_pipe_pressure(Batch b) {
       }
     }
   }
+}
+
+// The modal mass of every Beam_1 / Pipe_1 element of colour class `color`
+// added into the band M (entry (i, j) at (kw + i - j) + j W, free indices of
+// b.gl): one thread per element, elements of a colour share no node.
+__global__ void k_modal_mass_beam(Batch b, int color, double* M, int64_t W, int kw) {
+  const int k = b.color_off[color] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.color_off[color + 1]) return;
+  const int e = b.color_elems[k];
+  const BeamConst& c = b.bconst[e];
+  double D[2][2][9];
+  beam_modal_D(c, b.baux[e], D);
+  int g[18];
+#pragma unroll
+  for (int a = 0; a < 18; ++a) g[a] = b.gl[(int64_t)b.enodes[3 * e + a / 6] * 6 + a % 6];
+#pragma unroll 1
+  for (int I = 0; I < 3; ++I)
+#pragma unroll 1
+    for (int J = 0; J < 3; ++J)
+#pragma unroll 1
+      for (int bi = 0; bi < 2; ++bi) {
+        double m[9];
+        beam_modal_block(c, D, I, J, bi, bi, m);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const int gr = g[6 * I + 3 * bi + i], gq = g[6 * J + 3 * bi + j];
+            if (gr >= 0 && gq >= 0 && abs(gr - gq) <= kw) M[(kw + gr - gq) + (int64_t)gq * W] += m[i * 3 + j];
+          }
+      }
 }
 
 __global__ void k_beam_scatter(Batch b, int color) {
@@ -1160,6 +1201,15 @@ __global__ void k_beam_commit(int n, const BeamConst* cs, BeamHist* hs, BeamHist
 }
 
 }  // namespace
+
+void launch_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st) {
+  for (int c = 0; c < b.n_colors; ++c) {
+    const int cnt = b.color_off[c + 1] - b.color_off[c];
+    if (cnt > 0) k_modal_mass_beam<<<(cnt + 63) / 64, 64, 0, st>>>(b, c, M, W, kw);
+  }
+  if (b.sh.n_shells) launch_shell_modal_mass(b, M, W, kw, st);
+}
+
 
 // ---------------------------------------------------------------------------
 void launch_beam_inertia(int n, const BeamConst* c, const BeamHistAux* x, const double* d, const double* v,

@@ -106,6 +106,11 @@ void launch_beam_elements(int n, const BeamConst* c, const BeamHist* h, const do
 void launch_shell_mount(const Batch& b, cudaStream_t st);
 void launch_wide_zero(const Batch& b, cudaStream_t st);
 void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof = nullptr);
+void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st);
+// The modal mass (MountMassModal) of every element added into a band of the
+// structure's layout: entry (i, j) at (kw + i - j) + j W.
+void launch_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st);
+void launch_shell_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st);
 void launch_shell_commit(const Batch& b, cudaStream_t st);
 // Standalone Shell_1 elements (gf_shell_elements): d [n][27], pu [n][18],
 // p [n] (NaN: no pressure); K [n][729] column-major, f [n][27].

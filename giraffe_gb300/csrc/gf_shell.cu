@@ -668,6 +668,66 @@ __global__ void __launch_bounds__(64) k_shell_tangent(Batch b) {
 // iteration then adds a4 C_e to K_e and C_e v to f_e, v the nodes' current
 // velocities.  One warp per element, lane r < 27 owning row r of C_e, K_e
 // and f_e (no lane reads another's row); C_e is structure-of-arrays.
+// Row r of element e's modal mass (MountMassModal over the six-point rule,
+// reference src/Shell_1.cpp:2368-2396, 3171-), global frame, into row[27].
+__device__ void shell_modal_row(const Batch& b, int e, int r, double* row) {
+  const ShellConst& c = b.sh.sconst[e];
+  const int* nd = b.sh.snodes + 6 * e;
+  const int n = r / 3, i = r % 3;  // row block (node 0..5 translations, 6..8 midside rotations), row in it
+#pragma unroll
+  for (int x = 0; x < 27; ++x) row[x] = 0.0;
+  if (n < 6) {
+    // translations: coef1 times the weights on the diagonal of each 3x3
+    // node block (T^T I T = I)
+#pragma unroll 1
+    for (int q = 0; q < 6; ++q) {
+      double w = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) w += c.w4[k] * c.N4[k][n] * c.N4[k][q];
+      row[3 * q + i] = c.coef1 * w;
+    }
+  } else {
+    // rotations of midside node m: row i of T^T R[m][q] T for q = 0..2
+    const int m = n - 6;
+    const m3 T = ld3(c.T3);
+    double R[3][9];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+      for (int x = 0; x < 9; ++x) R[q][x] = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) {
+      v3 al = {{0, 0, 0}};
+#pragma unroll
+      for (int mm = 0; mm < 3; ++mm)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) al[j] += b.copy[(int64_t)nd[3 + mm] * 6 + 3 + j] * c.Na4[k][mm];
+      al = mv(T, al);
+      const m3 Q = rodrigues(al);
+      const v3 dv = {{Q[2], Q[5], Q[8]}};
+      const double d2 = dot(dv, dv);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const double w = c.w4[k] * c.Na4[k][m] * c.Na4[k][q];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            R[q][a * 3 + j] += w * ((a == j ? c.coef2 * d2 : 0.0) + (c.coef3 - c.coef2) * dv[a] * dv[j]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      m3 Rq;
+#pragma unroll
+      for (int x = 0; x < 9; ++x) Rq[x] = R[q][x];
+      const m3 G = tmul(T, mul(Rq, T));
+#pragma unroll
+      for (int j = 0; j < 3; ++j) row[18 + 3 * q + j] = G[i * 3 + j];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
   const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int r = threadIdx.x & 31;
@@ -680,62 +740,9 @@ __global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
   const int64_t ns = b.sh.n_shells;
   double* C = b.sh.RD + e;
   const int* nd = b.sh.snodes + 6 * e;
-  const int n = r / 3, i = r % 3;  // row block (node 0..5 translations, 6..8 midside rotations), row in it
   if (p.ray_update || !st.ray_init) {
-    const ShellConst& c = b.sh.sconst[e];
     double row[27];
-#pragma unroll
-    for (int x = 0; x < 27; ++x) row[x] = 0.0;
-    if (n < 6) {
-      // translations: coef1 times the weights on the diagonal of each 3x3
-      // node block (T^T I T = I)
-#pragma unroll 1
-      for (int q = 0; q < 6; ++q) {
-        double w = 0.0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) w += c.w4[k] * c.N4[k][n] * c.N4[k][q];
-        row[3 * q + i] = c.coef1 * w;
-      }
-    } else {
-      // rotations of midside node m: row i of T^T R[m][q] T for q = 0..2
-      const int m = n - 6;
-      const m3 T = ld3(c.T3);
-      double R[3][9];
-#pragma unroll
-      for (int q = 0; q < 3; ++q)
-#pragma unroll
-        for (int x = 0; x < 9; ++x) R[q][x] = 0.0;
-#pragma unroll 1
-      for (int k = 0; k < 6; ++k) {
-        v3 al = {{0, 0, 0}};
-#pragma unroll
-        for (int mm = 0; mm < 3; ++mm)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) al[j] += b.copy[(int64_t)nd[3 + mm] * 6 + 3 + j] * c.Na4[k][mm];
-        al = mv(T, al);
-        const m3 Q = rodrigues(al);
-        const v3 dv = {{Q[2], Q[5], Q[8]}};
-        const double d2 = dot(dv, dv);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const double w = c.w4[k] * c.Na4[k][m] * c.Na4[k][q];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-              R[q][a * 3 + j] += w * ((a == j ? c.coef2 * d2 : 0.0) + (c.coef3 - c.coef2) * dv[a] * dv[j]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        m3 Rq;
-#pragma unroll
-        for (int x = 0; x < 9; ++x) Rq[x] = R[q][x];
-        const m3 G = tmul(T, mul(Rq, T));
-#pragma unroll
-        for (int j = 0; j < 3; ++j) row[18 + 3 * q + j] = G[i * 3 + j];
-      }
-    }
+    shell_modal_row(b, e, r, row);
 #pragma unroll 1
     for (int x = 0; x < 27; ++x) {
       const int64_t xi = r + 27 * x;
@@ -754,6 +761,38 @@ __global__ void __launch_bounds__(128) k_shell_rayleigh(Batch b) {
     K[r + 27 * x] += a4 * cx;
   }
   b.sh.Fe[(int64_t)e * 27 + r] += acc;
+}
+
+// The modal mass of every Shell_1 element of colour class `color` added into
+// the band M (entry (i, j) at (kw + i - j) + j W, free indices of b.gl):
+// one thread per element, elements of a colour share no node.
+__global__ void k_modal_mass_shell(Batch b, int color, double* M, int64_t W, int kw) {
+  const int k = b.sh.color_off[color] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.sh.color_off[color + 1]) return;
+  const int e = b.sh.color_elems[k];
+  const int* nd = b.sh.snodes + 6 * e;
+  int g[27];
+#pragma unroll 1
+  for (int x = 0; x < 27; ++x) {
+    const int node = x < 18 ? nd[x / 3] : nd[3 + (x - 18) / 3];
+    g[x] = b.gl[(int64_t)node * 6 + (x < 18 ? x % 3 : 3 + (x - 18) % 3)];
+  }
+#pragma unroll 1
+  for (int r = 0; r < 27; ++r) {
+    if (g[r] < 0) continue;
+    double row[27];
+    shell_modal_row(b, e, r, row);
+#pragma unroll 1
+    for (int x = 0; x < 27; ++x)
+      if (g[x] >= 0 && abs(g[r] - g[x]) <= kw) M[(kw + g[r] - g[x]) + (int64_t)g[x] * W] += row[x];
+  }
+}
+
+void launch_shell_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st) {
+  for (int c = 0; c < b.sh.n_colors; ++c) {
+    const int cnt = b.sh.color_off[c + 1] - b.sh.color_off[c];
+    if (cnt > 0) k_modal_mass_shell<<<(cnt + 63) / 64, 64, 0, st>>>(b, c, M, W, kw);
+  }
 }
 
 // Standalone elements (gf_shell_elements): n elements with their own
@@ -1705,8 +1744,9 @@ __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
   WB w = wb_of(b, inf);
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(w.kl, w.n - j0 - nb);
-  double* P = b.P + inf.dof_off;
-  double* Y = b.y + inf.dof_off;
+  // right-hand side blockIdx.z of a multi-column solve (columns rhs_ld apart)
+  double* P = b.P + inf.dof_off + (int64_t)blockIdx.z * b.rhs_ld;
+  double* Y = b.y + inf.dof_off + (int64_t)blockIdx.z * b.rhs_ld;
   __shared__ double T[NB][NB + 1];  // the panel's diagonal block (L11 below the diagonal)
   __shared__ double ys[NB];
   const int tid = threadIdx.x;
@@ -1749,8 +1789,9 @@ __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
   if (p >= inf.n_panels) return;
   WB w = wb_of(b, inf);
   const int j0 = p * NB, nb = min(NB, w.n - j0);
-  double* P = b.P + inf.dof_off;
-  double* Y = b.y + inf.dof_off;
+  // right-hand side blockIdx.z of a multi-column solve (columns rhs_ld apart)
+  double* P = b.P + inf.dof_off + (int64_t)blockIdx.z * b.rhs_ld;
+  double* Y = b.y + inf.dof_off + (int64_t)blockIdx.z * b.rhs_ld;
   __shared__ double T[NB][NB + 1];  // the panel's diagonal block (U11 on and above the diagonal)
   __shared__ double rdiag[NB];
   __shared__ double xs[NB];
@@ -2004,6 +2045,17 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     ProfScope q(prof, st, KC_WIDE_SUBST);
     k_wb_bwd<<<dim3(rb, nw), 256, 0, st>>>(b, p);
   }
+}
+
+// Forward and backward substitution alone on a wide band that already holds
+// its LU (a factor from launch_wide_solve), for nrhs right-hand sides at
+// b.P + q b.rhs_ld (q < nrhs, scratch alike in b.y): the panel loops of
+// launch_wide_solve without the factor, every column per launch.
+void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st) {
+  if (b.sh.n_wide == 0 || nrhs <= 0) return;
+  const int nw = b.sh.n_wide, rb = (b.sh.max_kl + 255) / 256;
+  for (int p = 0; p < b.sh.max_panels; ++p) k_wb_fwd<<<dim3(rb, nw, nrhs), 256, 0, st>>>(b, p);
+  for (int p = b.sh.max_panels - 1; p >= 0; --p) k_wb_bwd<<<dim3(rb, nw, nrhs), 256, 0, st>>>(b, p);
 }
 
 void launch_shell_elements(int n, const ShellConst* c, const ShellHist* h, const double* d, const double* pu,

@@ -312,6 +312,7 @@ struct Batch {
   int* dof_node6;
   double* P;
   double* y;
+  int64_t rhs_ld;  // column stride of a multi-column wide-band substitution (0: one column)
   double* xr;  // refinement: accumulated solution
   double* r;   // refinement: residual
   // band and factor

@@ -8,7 +8,9 @@ solution steps:
 
   SolutionSteps   Static / Dynamic (src/Static.cpp:40-130,
                   src/Dynamic.cpp:60-215: EndTime ... Sample, RayleighDamping,
-                  NewmarkCoefficients, optional ZeroIC)
+                  NewmarkCoefficients, optional ZeroIC); a deck's only step
+                  may be Modal (src/Modal.cpp:42-108: ExportMatrices,
+                  NumberModes, Tolerance, ComputeEigenvectors, NumberFrames)
   Nodes           Node id x y z
   Elements        Beam_1 id Mat Sec CS Nodes a b c [PreTension p]
                   (src/Beam_1.cpp:371-430); Pipe_1 id PipeSec CS Nodes a b c
@@ -44,8 +46,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, NodalDisplacement, NodalLoad, PipeLoad, PressureLoad,
-                    Solution, Structure, Table)
+from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, ModalStep, NodalDisplacement, NodalLoad, PipeLoad,
+                    PressureLoad, Solution, Structure, Table)
 
 # Every top-level keyword of IO::ReadFile: a block reader stops at the next one.
 TOP = {
@@ -192,6 +194,21 @@ def read_deck(text: str, step: int = None) -> Structure:
         if kw == "SolutionSteps":
             for _ in range(tk.int()):
                 kind = tk.next()
+                if kind == "Modal":
+                    tk.int()
+                    md = ModalStep()
+                    tk.expect("ExportMatrices")
+                    md.export_matrices = tk.int()
+                    tk.expect("NumberModes")
+                    md.number_modes = tk.int()
+                    tk.expect("Tolerance")
+                    md.tolerance = tk.float()
+                    tk.expect("ComputeEigenvectors")
+                    md.compute_eigenvectors = tk.int()
+                    tk.expect("NumberFrames")
+                    md.number_frames = tk.int()
+                    steps.append(md)
+                    continue
                 if kind not in ("Static", "Dynamic"):
                     raise DeckError(f"solution type '{kind}' is not solved by this library")
                 steps.append(_solution(tk, kind))
@@ -387,6 +404,12 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
            criteria, pipe_secs=None) -> Structure:
     if not steps:
         raise DeckError("the deck has no solution step")
+    modal = None
+    if any(isinstance(x, ModalStep) for x in steps):
+        if len(steps) != 1:
+            raise DeckError("a Modal step is solved only as a deck's only solution step")
+        modal = steps[0]
+        steps = [Solution()]
     if step is not None:
         if not 1 <= step <= len(steps):
             raise DeckError(f"the deck has {len(steps)} solution step(s), not {step}")
@@ -475,6 +498,7 @@ def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, el
     s.solution = steps[0]
     s.next_steps = list(steps[1:n_steps])
     s.criteria = dict(criteria)
+    s.modal = modal
     return s
 
 

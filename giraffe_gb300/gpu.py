@@ -29,7 +29,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_shell_inertia_elements", "gf_ctx_set_opts", "gf_upload_structure", "gf_structure_destroy",
            "gf_structure_dims", "gf_structure_dofs", "gf_structure_pattern", "gf_structure_set_step", "gf_begin_step",
            "gf_assemble", "gf_set_increment", "gf_commit", "gf_rollback", "gf_structure_nodes", "gf_beam_mount",
-           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange"]
+           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange", "gf_structure_modal", "gf_modal"]
 
 GF_LAYOUT_CSR, GF_LAYOUT_GB = 0, 1
 GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
@@ -121,6 +121,8 @@ def lib():
         L.gf_commit.argtypes = [vp]
         L.gf_rollback.argtypes = [vp]
         L.gf_structure_nodes.argtypes = [vp, dp, dp]
+        L.gf_structure_modal.argtypes = [vp, C.c_double, C.c_int, C.c_double, dp, dp, ip]
+        L.gf_modal.argtypes = [vp, C.POINTER(gf_model_desc), C.c_int, C.c_double, dp, dp, ip]
         L.gf_beam_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
         L.gf_beam_save_lagrange.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp]
         L.gf_shell_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.c_int, dp, dp]
@@ -310,6 +312,17 @@ class Context:
                    "gf_shell_save_lagrange")
         return out
 
+    def modal(self, structure: Structure, n_modes: int, tol: float = 0.0, modes: bool = True):
+        """A Modal step of the structure at its start (gf_modal): (eigenvalues
+        ascending, modes [n_modes x n free DOFs] or None, iterations)."""
+        h = structure.desc()
+        eig = np.zeros(n_modes)
+        V = np.zeros((n_modes, structure.n_free)) if modes else None
+        it = C.c_int(0)
+        self.check(self.L.gf_modal(self.h, C.byref(h.desc), n_modes, tol, _dp(eig), _dp(V) if modes else None,
+                                   C.byref(it)), "gf_modal")
+        return eig, V, it.value
+
     def band_solve_noalloc(self, ab, kl, ku, b):
         """gf_band_solve_noalloc: band_solve through the static device scratch."""
         ab = np.ascontiguousarray(ab, dtype=np.float64)
@@ -381,6 +394,17 @@ class DeviceStructure:
 
     def rollback(self):
         self.ctx.check(self.L.gf_rollback(self.h), "gf_rollback")
+
+    def modal(self, time: float, n_modes: int, tol: float = 0.0):
+        """Modal analysis at the structure's current configuration with the
+        loads at `time` (gf_structure_modal): (eigenvalues, modes
+        [n_modes x n] in the reference's free-DOF numbering, iterations)."""
+        eig = np.zeros(n_modes)
+        modes = np.zeros((n_modes, self.n))
+        it = C.c_int(0)
+        self.ctx.check(self.L.gf_structure_modal(self.h, time, n_modes, tol, _dp(eig), _dp(modes), C.byref(it)),
+                       "gf_structure_modal")
+        return eig, modes, it.value
 
     def nodes(self):
         """(nodes [n_nodes x 15], increments [n_nodes x 6])."""

@@ -221,6 +221,18 @@ class NodalDisplacement:
 
 
 @dataclass
+class ModalStep:
+    """A Modal solution step (reference src/Modal.cpp:42-108): the
+    number_modes smallest eigenvalues of K x = lambda M x at the structure's
+    start, by shift-invert with shift 0 (src/SparseMatrix.cpp:270-)."""
+    number_modes: int = 10
+    tolerance: float = 1e-6
+    export_matrices: int = 0
+    compute_eigenvectors: int = 0
+    number_frames: int = 0
+
+
+@dataclass
 class Solution:
     type: int = GF_STATIC
     start_time: float = 0.0
@@ -268,6 +280,7 @@ class Structure:
     # and the pipe section of each beam that is a Pipe_1 element
     pipe_sections: list = field(default_factory=list)
     pipe_of: dict = field(default_factory=dict)        # beam index -> pipe section
+    modal: ModalStep | None = None                     # a deck whose step is Modal
 
     def __setattr__(self, name, value):
         # element rows assigned as lists become ElementTables
@@ -342,7 +355,14 @@ class Structure:
     def to_inp(self) -> str:
         o = []
         steps = [self.solution] + list(self.next_steps)
-        o.append(f"SolutionSteps\t{len(steps)}")
+        if self.modal is not None:
+            md = self.modal
+            o.append(f"SolutionSteps\t1\nModal\t1\nExportMatrices\t{int(md.export_matrices)}\n"
+                     f"NumberModes\t{int(md.number_modes)}\nTolerance\t{_r(md.tolerance)}\n"
+                     f"ComputeEigenvectors\t{int(md.compute_eigenvectors)}\nNumberFrames\t{int(md.number_frames)}")
+            steps = []
+        else:
+            o.append(f"SolutionSteps\t{len(steps)}")
         for k, s in enumerate(steps, 1):
             if s.type == GF_STATIC:
                 o.append(f"Static\t{k}\nEndTime\t{_r(s.end_time)}\nTimeStep\t{_r(s.time_step)}\n"

@@ -397,6 +397,27 @@ int gf_rollback(gf_structure* s);
  * step's Node::displacements); either may be NULL. */
 int gf_structure_nodes(gf_structure* s, double* nodes, double* increments);
 
+/* ---- Modal analysis ----
+ * gf_structure_modal replaces Modal::Solve (src/Modal.cpp:131-199) with its
+ * eigen solve sparseeigen (src/SparseMatrix.cpp:270-420, ARPACK shift-invert
+ * with shift 0): the n_modes smallest eigenvalues of K_AA x = lambda M_AA x,
+ * K_AA the static tangent of the structure's current configuration with the
+ * loads at `time` (MountLocal + MountElementLoads + MountLoads) and M_AA the
+ * modal mass (MountMassModal).  Subspace iteration on K^-1 M with the
+ * wide-band factor of K on the device, until the n_modes smallest Ritz values
+ * change by at most tol relative (tol <= 0: 1e-12); at most 300 iterations
+ * (ARPACK's iparam[2] in the reference), else GF_ERR_TIMEOUT.  eig receives
+ * the n_modes eigenvalues ascending (real: the reference's Im column is 0 for
+ * these symmetric problems); modes (may be NULL) the M-orthonormal modes,
+ * n_modes x n free DOFs in the reference's numbering; iterations (may be
+ * NULL) the iterations taken.  A nonsymmetric K_AA (follower loads) is
+ * refused with GF_ERR_ARG, a singular one with GF_ERR_SINGULAR.  gf_modal is
+ * the Modal step of a structure at its start (solution.start_time). */
+int gf_structure_modal(gf_structure* s, double time, int n_modes, double tol, double* eig, double* modes,
+                       int* iterations);
+int gf_modal(gf_ctx* ctx, const gf_model_desc* model, int n_modes, double tol, double* eig, double* modes,
+             int* iterations);
+
 /* ---- Element entries on the reference's stored Gauss-point state ----
  * gf_beam_mount replaces Beam_1::Mount + MountElementLoads
  * (src/Beam_1.cpp:695-843) for n elements; their state is given as the

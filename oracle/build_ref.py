@@ -33,7 +33,7 @@ SOURCES = [
     "ShellSectionHomogeneous", "CoordinateSystem", "Table", "Static", "Dynamic", "Solution",
     "ConvergenceCriteria", "NodalLoad", "NodalConstraint", "NodeSet", "ElementSet", "BoolTable", "Load",
     "Element", "NodalDisplacement", "ShellLoad", "SolverOptions", "SolidSection", "Pipe_1", "PipeSection",
-    "PipeLoad",
+    "PipeLoad", "Modal",
 ]
 
 CXXFLAGS = ["-std=c++14", "-O2", "-fPIC", "-fpermissive", "-w", "-fno-fast-math",

@@ -50,6 +50,11 @@ int oracle_solve_batch(int n, const gf_model_desc* models, double** final_nodes,
 int oracle_beam_element(const double* xyz9, const double* mat3, const double* sec6, const double* cs6,
                         int n_hist, const double* hist_disp, const double* disp18, double* K, double* f);
 
+/* K_AA (static tangent at the step's start) and M_AA (the modal mass of
+ * MountMassModal) of a Modal solution step, GB storage as
+ * oracle_first_tangent; K == NULL fills dims only. */
+int oracle_modal_matrices(const gf_model_desc* m, double* K, double* M, int* dims);
+
 /* One Pipe_1 element: as oracle_beam_element with a pipe section (EA, EI,
  * GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di) and, when p0i != 0, the
  * internal-pressure load of MountPipeSpecialLoads added to K and f. */

@@ -24,6 +24,7 @@ def lib():
         _lib.oracle_solve_batch.argtypes = [C.c_int, C.c_void_p, C.POINTER(dp), ip, C.c_int]
         _lib.oracle_beam_element.argtypes = [dp, dp, dp, dp, C.c_int, dp, dp, dp, dp]
         _lib.oracle_first_tangent.argtypes = [C.c_void_p, dp, dp, ip]
+        _lib.oracle_modal_matrices.argtypes = [C.c_void_p, dp, dp, ip]
         _lib.oracle_pipe_element.argtypes = [dp, dp, dp, C.c_int, dp, dp, C.c_double, dp, dp]
         _lib.oracle_shell_element.argtypes = [dp, dp, C.c_double, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int,
                                               dp, dp]
@@ -88,6 +89,41 @@ def beam_element(xyz9, mat3, sec6, cs6, hist_disp, disp18):
     lib().oracle_beam_element(_dp(args[0]), _dp(args[1]), _dp(args[2]), _dp(args[3]), nh, _dp(hd),
                               _dp(args[4]), _dp(K), _dp(f))
     return K.reshape(18, 18).T, f  # row-major [r][s]
+
+
+def _gb_dense(ab, kl):
+    """Dense n x n of GB storage [n][3 kl + 1] (entry (i, j) at ab[j][2 kl + i - j])."""
+    n = ab.shape[0]
+    A = np.zeros((n, n))
+    for j in range(n):
+        i0, i1 = max(0, j - kl), min(n, j + kl + 1)
+        A[i0:i1, j] = ab[j, 2 * kl + np.arange(i0, i1) - j]
+    return A
+
+
+def modal_matrices(structure):
+    """K_AA and M_AA of a Modal step at the structure's start (dense, the
+    reference's numbering): oracle_modal_matrices."""
+    h = structure.desc()
+    dims = (C.c_int * 2)()
+    if lib().oracle_modal_matrices(C.cast(h.ref, C.c_void_p), None, None, dims) < 0:
+        raise ValueError("oracle: invalid structure description")
+    n, kl = dims[0], dims[1]
+    K = np.zeros((n, 3 * kl + 1))
+    M = np.zeros((n, 3 * kl + 1))
+    lib().oracle_modal_matrices(C.cast(h.ref, C.c_void_p), _dp(K), _dp(M), dims)
+    return _gb_dense(K, kl), _gb_dense(M, kl)
+
+
+def modal(structure, n_modes: int):
+    """The n_modes smallest eigenvalues of K x = lambda M x (Modal::Solve's
+    shift-invert problem with sigma 0), by LAPACK's symmetric-definite
+    generalized solver on the assembled matrices, and the M-normalized
+    modes (columns, the reference's numbering)."""
+    import scipy.linalg
+    K, M = modal_matrices(structure)
+    w, V = scipy.linalg.eigh(K, M, subset_by_index=[0, n_modes - 1])
+    return w, V
 
 
 def pipe_element(xyz9, ps11, cs6, hist_disp, disp18, p0i=0.0):

@@ -918,6 +918,63 @@ int oracle_first_tangent(const gf_model_desc* m, double* ab, double* PA, int* di
   return 0;
 }
 
+/* The two matrices of a Modal solution step (reference
+ * src/Modal.cpp:131-166): K_AA of MountLocal + MountElementLoads +
+ * MountLoads at the step's start with zero increments (the static tangent),
+ * and M_AA of MountMassModal (Beam_1 / Pipe_1 src/Beam_1.cpp:1538-1553 and
+ * Shell_1 src/Shell_1.cpp:3171-), both in GB storage (ldab = 3 kl + 1,
+ * column-major, n_free columns) in the reference's numbering.  dims
+ * receives n_free and kl; with K == NULL only dims is filled. */
+int oracle_modal_matrices(const gf_model_desc* m, double* K, double* M, int* dims) {
+  ost s;
+  if (ost_init(&s, m) != 0) {
+    ost_free(&s);
+    return -1;
+  }
+  const int n = s.n_free, kn = s.kl_nat, ld = 3 * kn + 1;
+  dims[0] = n;
+  dims[1] = kn;
+  if (K) {
+    s.last_converged_time = m->solution.start_time;
+    s.current_time_step = 0.0;
+    assemble(&s);
+    for (int pass = 0; pass < 2; ++pass) {
+      double* out = pass == 0 ? K : M;
+      if (pass == 1) {
+        /* the modal mass of every element, scattered as the tangent is */
+        memset(s.ab, 0, sizeof(double) * (size_t)s.ldab * (size_t)(s.n_free ? s.n_free : 1));
+        double Mm[729];
+        for (int e = 0; e < s.nb; ++e) {
+          const int* b = m->beams + 6 * e;
+          oracle_beam_modal_mass(s.bc + e, s.bh + e, Mm);
+          int g[18];
+          for (int a = 0; a < 18; ++a) g[a] = s.GL[6 * b[a / 6] + a % 6];
+          for (int a = 0; a < 18; ++a)
+            for (int c = 0; c < 18; ++c) add_K(&s, g[a], g[c], Mm[a + 18 * c]);
+        }
+        for (int e = 0; e < s.ns; ++e) {
+          const int* nd = m->shells + 9 * e;
+          double rot[9];
+          for (int j = 0; j < 3; ++j) memcpy(rot + 3 * j, s.copy + 6 * nd[3 + j] + 3, 3 * sizeof(double));
+          oracle_shell_modal_mass(s.sc + e, rot, Mm);
+          int g[27];
+          shell_dofs(&s, e, g);
+          for (int a = 0; a < 27; ++a)
+            for (int c = 0; c < 27; ++c) add_K(&s, g[a], g[c], Mm[a + 27 * c]);
+        }
+      }
+      memset(out, 0, sizeof(double) * (size_t)ld * (size_t)n);
+      for (int j = 0; j < n; ++j)
+        for (int i = j - kn < 0 ? 0 : j - kn; i <= j + kn && i < n; ++i) {
+          int pi = s.pf[i], pj = s.pf[j], d = pi - pj;
+          if (d <= s.kl && -d <= s.ku) GB_AT(out, ld, kn, kn, i, j) = GB_AT(s.ab, s.ldab, s.kl, s.ku, pi, pj);
+        }
+    }
+  }
+  ost_free(&s);
+  return 0;
+}
+
 /* Newmark coefficients (reference src/Dynamic.cpp:582-590). */
 static void newmark_coeff(double dt, double beta, double gamma, double* a) {
   a[0] = 1.0 / (dt * dt * beta);

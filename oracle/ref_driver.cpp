@@ -16,6 +16,7 @@
 #include "Dynamic.h"
 #include "Hooke.h"
 #include "LagrangeSave.h"
+#include "Modal.h"
 #include "NodalConstraint.h"
 #include "NodalDisplacement.h"
 #include "NodalLoad.h"
@@ -127,6 +128,7 @@ int giraffe_ref_load(const char* path) {
       ok = read_block<Solution>(f, db.number_solutions, db.solution, [](const char* t) -> Solution* {
         if (!strcmp(t, "Static")) return new Static();
         if (!strcmp(t, "Dynamic")) return new Dynamic();
+        if (!strcmp(t, "Modal")) return new Modal();
         return nullptr;
       });
       db.solution_exist = true;
@@ -417,4 +419,50 @@ extern "C" int giraffe_ref_pipe_pressure(int e, int l, double t, double* K, doub
   memcpy(K, p->stiffness->getMatrix(), sizeof(double) * 18 * 18);
   memcpy(P, p->P_loading->getMatrix(), sizeof(double) * 18);
   return 18;
+}
+
+// The two matrices of a Modal step (reference src/Modal.cpp:131-166,
+// without the ARPACK eigen solve that follows them): the modal mass M_AA
+// (MountMassModal, MountDynModal, MountGlobal, MountSparse), then the
+// tangent K_AA (MountLocal, MountElementLoads, MountSpecialConstraints,
+// MountContacts, MountLoads, MountGlobal, MountSparse), both written dense
+// and column-major (n x n) in the reference's own DOF numbering.  Returns n,
+// or 0 when n exceeds n_max.
+static void ref_dense(SparseMatrix& A, double* out, int n) {
+  if (!A.mounted) A.Mount();
+  for (int i = 0; i < n * n; ++i) out[i] = 0.0;
+  const double* a = A.m_matrix.valuePtr();
+  const int* ia = A.m_matrix.outerIndexPtr();
+  const int* ja = A.m_matrix.innerIndexPtr();
+  for (int i = 0; i < A.m_matrix.rows(); ++i)
+    for (int p = ia[i]; p < ia[i + 1]; ++p) out[i + (size_t)n * ja[p]] += a[p];
+}
+
+extern "C" int giraffe_ref_modal_matrices(double* K, double* M, int n_max) {
+  Modal md;
+  db.current_solution_number = 1;
+  md.DOFsActive();
+  md.SetGlobalDOFs();
+  md.SetGlobalSize();
+  const int n = db.global_stiffness_AA.rows;
+  if (n > n_max) return 0;
+  md.Zeros();
+  md.Clear();
+  md.ZerosLocalMatrices();
+  md.MountMassModal();
+  md.MountDynModal();
+  md.MountGlobal();
+  md.MountSparse();
+  ref_dense(db.global_stiffness_AA, M, n);
+  md.Clear();
+  md.ZerosLocalMatrices();
+  md.MountLocal();
+  md.MountElementLoads();
+  md.MountSpecialConstraints();
+  md.MountContacts();
+  md.MountLoads();
+  md.MountGlobal();
+  md.MountSparse();
+  ref_dense(db.global_stiffness_AA, K, n);
+  return n;
 }

@@ -48,6 +48,11 @@ stores what the reference computes:
                          raised to 20 MPa: Dynamic (Newmark), 100 steps.
 * ref_pipe_riser_rayleigh.npz  the same with Rayleigh damping (alpha 0.3,
                          beta 0.004, Update 1).
+* ref_modal_cantilever.npz, ref_modal_plate.npz, ref_modal_riser.npz
+                         the two matrices of a Modal step (K_AA and the modal
+                         mass M_AA, dense) from the reference build for
+                         tutorial01's cantilever, a 3x3x2 plate and the
+                         Pipe_1 riser, and their ten smallest eigenvalues.
 * ref_shell_elements.npz Shell_1 tangent K (27x27) and unbalanced force P (27)
                          of single elements with random geometry, material,
                          thickness, committed history and increment, half of
@@ -522,6 +527,44 @@ def make_elements():
         np.savez_compressed(os.path.join(HERE, "ref_shell_inertia.npz"), **run_shell_inertia(L, rng, 16, tmp))
 
 
+MODAL_DECKS = {
+    "ref_modal_cantilever.npz": configs.tutorial01,
+    "ref_modal_plate.npz": lambda: configs.square_plate(3, steps=10),
+    "ref_modal_riser.npz": configs.pipe_riser,
+}
+
+
+def make_modal(name, n_modes: int = 10):
+    """The two matrices of a Modal step from the reference build (K_AA and
+    the modal mass M_AA, dense, the reference's numbering) and the n_modes
+    smallest eigenvalues of K x = lambda M x from them.  The reference's own
+    eigen solve is ARPACK's shift-invert Arnoldi (arpack-ng, a vcpkg
+    dependency not in the reference tree); LAPACK's symmetric-definite
+    solver stands in for it on these symmetric matrices."""
+    import scipy.linalg
+    from giraffe_gb300.model import ModalStep
+
+    L = ref_lib()
+    dp = C.POINTER(C.c_double)
+    L.giraffe_ref_modal_matrices.argtypes = [dp, dp, C.c_int]
+    s = MODAL_DECKS[name]()
+    s.modal = ModalStep(number_modes=n_modes, tolerance=0.0)
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "modal.inp")
+        with open(deck, "w") as f:
+            f.write(s.to_inp())
+        assert L.giraffe_ref_load(deck.encode()) == 0
+        nmax = 4096
+        K = np.zeros(nmax * nmax)
+        M = np.zeros(nmax * nmax)
+        n = L.giraffe_ref_modal_matrices(_dp(K), _dp(M), nmax)
+        assert n > 0
+    K = K[: n * n].reshape(n, n).T.copy()
+    M = M[: n * n].reshape(n, n).T.copy()
+    w = scipy.linalg.eigh(K, M, eigvals_only=True, subset_by_index=[0, n_modes - 1])
+    np.savez_compressed(os.path.join(HERE, name), K=K, M=M, eig=w, deck=np.array(s.to_inp()))
+
+
 def make_pipe_elements():
     L = ref_lib()
     rng = np.random.default_rng(20261204)
@@ -568,13 +611,15 @@ def main():
             make_tutorial04()
         elif sys.argv[1] == "ref_pipe_elements.npz":
             make_pipe_elements()
+        elif sys.argv[1] in MODAL_DECKS:
+            make_modal(sys.argv[1])
         elif sys.argv[1] == "ref_plate24.npz":
             make_plate24()
         else:
             make_deck(sys.argv[1])
         return
     ref_lib()
-    for job in (["elements", "ref_pipe_elements.npz"] + list(DECKS) +
+    for job in (["elements", "ref_pipe_elements.npz"] + list(DECKS) + list(MODAL_DECKS) +
                 ["ref_tutorial04.npz", "ref_tutorial05.npz", "ref_plate24.npz"]):
         subprocess.run([sys.executable, os.path.abspath(__file__), job], check=True)
     for f in sorted(os.listdir(HERE)):

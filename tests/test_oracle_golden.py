@@ -241,3 +241,23 @@ def test_pipe_riser_dynamics_matches_reference(golden, name, kw):
     s = configs.pipe_riser(pressure=0.0, **kw)
     f0, _, _ = oracle.solve(s)
     assert np.abs(final[:, :3] - f0[:, :3]).max() > 1e-6 * np.abs(final[:, :3]).max()
+
+
+@pytest.mark.parametrize("name", ["ref_modal_cantilever.npz", "ref_modal_plate.npz", "ref_modal_riser.npz"])
+def test_modal_matrices_match_reference(golden, name):
+    """The two matrices of a Modal step (K_AA, and M_AA of MountMassModal)
+    equal the reference's own to rounding, and the oracle's eigenvalues (LAPACK's
+    symmetric-definite solver, standing in for the reference's ARPACK
+    shift-invert) equal the golden ones to 1e-7 relative: the smallest
+    eigenvalues of these stiff problems carry an error of about
+    eps |lambda_max| / |lambda| from any dense solver."""
+    from giraffe_gb300.model import Structure
+    g = golden(name)
+    s = Structure.from_inp(str(g["deck"]))
+    assert s.modal is not None and s.modal.number_modes == len(g["eig"])
+    K, M = oracle.modal_matrices(s)
+    assert rel(K, g["K"]) < 1e-14
+    assert rel(M, g["M"]) < 1e-14
+    w, V = oracle.modal(s, len(g["eig"]))
+    assert np.abs(w - g["eig"]).max() <= 1e-7 * np.abs(g["eig"]).max()
+    assert np.allclose(V.T @ g["M"] @ V, np.eye(len(w)), atol=1e-9)
