@@ -949,18 +949,21 @@ __global__ void k_wb_zero(Batch b) {
 }
 
 // LU (no pivoting) of the diagonal block of panel p, in place, right-looking
-// on a column-major copy in shared memory.  FP64 issue is the bound on this
-// part (about two FMA lanes per clock per SM), and a warp instruction costs
-// its full issue time however few of its lanes are live, so step k gives
-// each warp whole columns j = k + 1 + warp + 8 q of the trailing block with
-// its lanes on consecutive rows: a step issues about (m / 8) (1 + [m > 32])
-// FMA instructions per warp for a trailing size m, not a fixed 4 x 4 grid.
-// Warp 0 updates column k + 1 first and forms that column's multipliers
-// (pivot reciprocal, scaled entries) at once, so one barrier per step
-// suffices.  Each entry sees the same operations in the same order as the
-// textbook kij loop: multiplier l = a_ik * (1 / a_kk), then a_ij =
-// fma(-l, a_kj, a_ij) for k = 0, 1, ...
-__global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
+// on a column-major copy in shared memory.  On this part an FP64 warp
+// instruction occupies its sub-partition's FP64 unit for about 64 cycles
+// and a dependent FP64 result takes as long, so the kernel is built around
+// two costs: the FP64 issue of the trailing updates (about m^2 / 2 cycles per
+// step for a trailing size m on one SM) and the dependent chain of each pivot
+// (update the pivot, its reciprocal, the multipliers: about six FP64
+// latencies).  The pivot warp (warp 8) owns column k + 1 at step k: it
+// updates it, forms the next pivot's reciprocal and multipliers, while warps
+// 0-7 update the other m (m - 1) entries of the trailing block packed
+// densely over their lanes (entry e: column e / m, row e % m, so no lane
+// idles until the last round), and one barrier closes the step.  Each entry
+// sees the same operations in the same order as the textbook kij loop:
+// multiplier l = a_ik * (1 / a_kk), then a_ij = fma(-l, a_kj, a_ij).
+constexpr int DIAG_THREADS = 288;
+__global__ void __launch_bounds__(DIAG_THREADS) k_wb_diag(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.x];
@@ -983,7 +986,7 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
     Ac[j][i] = v;
   }
   __syncthreads();
-  if (warp == 0 && nb > 0) {  // the multipliers of column 0
+  if (warp == 8 && nb > 0) {  // the multipliers of column 0
     const double piv = Ac[0][0];
     if (lane == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
     const double r = wb_recip(piv);
@@ -992,22 +995,28 @@ __global__ void __launch_bounds__(256) k_wb_diag(Batch b, int p) {
   }
   __syncthreads();
   for (int k = 0; k + 1 < nb; ++k) {
-    const int i0 = k + 1 + lane, i1 = i0 + 32;
-    const bool two = k + 33 < nb;  // warp-uniform: a second chunk of rows
-    const double l0 = i0 < nb ? Ac[k][i0] : 0.0;
-    const double l1 = two && i1 < nb ? Ac[k][i1] : 0.0;
-    for (int j = k + 1 + warp; j < nb; j += 8) {
+    const int m = nb - 1 - k;  // trailing rows and columns
+    if (warp == 8) {
+      // column k + 1: its update, then the next pivot and multipliers
+      const int j = k + 1, i0 = j + lane, i1 = i0 + 32;
       const double u = Ac[j][k];
-      if (i0 < nb) Ac[j][i0] = fma(-l0, u, Ac[j][i0]);
-      if (two && i1 < nb) Ac[j][i1] = fma(-l1, u, Ac[j][i1]);
-      if (j == k + 1) {
-        // warp 0: column k + 1 is final; its pivot and multipliers
-        __syncwarp();
-        const double piv = Ac[j][j];
-        if (lane == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
-        const double r = wb_recip(piv);
-        if (i0 > j && i0 < nb) Ac[j][i0] *= r;
-        if (two && i1 < nb) Ac[j][i1] *= r;
+      if (i0 < nb) Ac[j][i0] = fma(-Ac[k][i0], u, Ac[j][i0]);
+      if (i1 < nb) Ac[j][i1] = fma(-Ac[k][i1], u, Ac[j][i1]);
+      __syncwarp();
+      const double piv = Ac[j][j];
+      if (lane == 0 && (!(piv != 0.0) || !isfinite(piv))) fail = 1;
+      const double r = wb_recip(piv);
+      if (i0 > j && i0 < nb) Ac[j][i0] *= r;
+      if (i1 < nb) Ac[j][i1] *= r;
+    } else {
+      // columns k + 2 .. nb - 1, m (m - 1) entries over 256 lanes
+      const int tot = m * (m - 1);
+      const float inv_m = 1.0f / (float)m;
+      for (int e = tid; e < tot; e += 256) {
+        const int jj = __float2int_rz(((float)e + 0.5f) * inv_m);  // e / m, exact for e < 4096
+        const int ii = e - jj * m;
+        const int i = k + 1 + ii, j = k + 2 + jj;
+        Ac[j][i] = fma(-Ac[k][i], Ac[j][k], Ac[j][i]);
       }
     }
     __syncthreads();
@@ -1067,23 +1076,34 @@ __global__ void __launch_bounds__(32 * RB) k_wb_trsm(Batch b, int p, int row0, i
     X[r][k] = v;
   }
   __syncthreads();
+  // the row in registers, lane c holding entries c and c + 32: each step
+  // broadcasts the finished entry k by shuffle (a dependent FP64 result
+  // takes about 64 cycles on this part, a shuffle far less), and the half
+  // with no live entry left (k >= 31 for the first) is skipped by a
+  // warp-uniform branch instead of issued masked
+  double v0 = X[r][c], v1 = X[r][c + 32];
   if (lower) {
     // x U11 = a: x_k = a_k / u_kk, then a_j -= x_k u_kj (j > k)
     for (int k = 0; k < nb; ++k) {
-      if (c == 0) X[r][k] = X[r][k] * rd[k];
-      __syncwarp();
-      const double xk = X[r][k];
-      for (int j = k + 1 + c; j < nb; j += 32) X[r][j] -= xk * T[k][j];
-      __syncwarp();
+      const double xk = __shfl_sync(0xffffffffu, k < 32 ? v0 : v1, k & 31) * rd[k];
+      if (k < 32) {
+        if (c == k) v0 = xk;
+      } else if (c == k - 32) {
+        v1 = xk;
+      }
+      if (k < 31 && c > k) v0 -= xk * T[k][c];
+      if (c + 32 > k && c + 32 < nb) v1 -= xk * T[k][c + 32];
     }
   } else {
     // L11 y = a (unit lower): y_k = a_k, then a_i -= l_ik y_k (i > k)
     for (int k = 0; k < nb; ++k) {
-      const double yk = X[r][k];
-      for (int i = k + 1 + c; i < nb; i += 32) X[r][i] -= T[i][k] * yk;
-      __syncwarp();
+      const double yk = __shfl_sync(0xffffffffu, k < 32 ? v0 : v1, k & 31);
+      if (k < 31 && c > k) v0 -= T[c][k] * yk;
+      if (c + 32 > k && c + 32 < nb) v1 -= T[c + 32][k] * yk;
     }
   }
+  X[r][c] = v0;
+  X[r][c + 32] = v1;
   __syncthreads();
   for (int k = c; k < nb; k += 32) {
     if (!live || g - (j0 + k) > w.kl) continue;
@@ -1158,11 +1178,14 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 
 // The corner of panel p's trailing update: the next panel's diagonal block
 // (the first NB rows and columns of the window), on the lookahead's critical
-// path.  8 x 8 output tiles, one output per thread: the 262 k FMAs spread
-// over 64 CTAs instead of the four of k_wb_update's 32 x 32 tiles, and each
-// output is the same fma chain over k = 0..NB-1 as there.
+// path.  8 x 8 output tiles over 64 CTAs; in a CTA four warps each sum a
+// quarter of k (16 terms) for all 64 outputs of the tile, and the quarters
+// are added in a fixed order: an FP64 warp instruction holds its
+// sub-partition's FP64 unit for about 64 cycles, so four warps on four
+// sub-partitions finish the 64 terms four times sooner than one.
 constexpr int CT8 = 8;
-__global__ void __launch_bounds__(CT8 * CT8) k_wb_corner(Batch b, int p) {
+constexpr int CORNER_THREADS = 256;
+__global__ void __launch_bounds__(CORNER_THREADS) k_wb_corner(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.z];
@@ -1176,6 +1199,7 @@ __global__ void __launch_bounds__(CT8 * CT8) k_wb_corner(Batch b, int p) {
   if (r0 >= m || c0 >= m) return;
   __shared__ double Ls[NB][CT8 + 1];  // [k][row]
   __shared__ double Us[NB][CT8 + 1];  // [k][col]
+  __shared__ double part[4][CT8 * CT8];
   const int tid = threadIdx.x;
   const int base = j0 + nb;
   for (int x = tid; x < NB * CT8; x += blockDim.x) {
@@ -1188,11 +1212,15 @@ __global__ void __launch_bounds__(CT8 * CT8) k_wb_corner(Batch b, int p) {
     Us[kk][c] = (kk < nb && c0 + c < m && gj - (j0 + kk) <= w.kl) ? w.at(j0 + kk, gj) : 0.0;
   }
   __syncthreads();
-  const int ty = tid / CT8, tx = tid % CT8;
+  const int o = tid & 63, q = tid >> 6;  // output, quarter of k
+  const int ty = o / CT8, tx = o % CT8;
   double a = 0.0;
-#pragma unroll 16
-  for (int k = 0; k < NB; ++k) a = fma(Ls[k][ty], Us[k][tx], a);
-  if (r0 + ty < m && c0 + tx < m) w.at(base + r0 + ty, base + c0 + tx) -= a;
+#pragma unroll
+  for (int k = 16 * q; k < 16 * q + 16; ++k) a = fma(Ls[k][ty], Us[k][tx], a);
+  part[q][o] = a;
+  __syncthreads();
+  if (q == 0 && r0 + ty < m && c0 + tx < m)
+    w.at(base + r0 + ty, base + c0 + tx) -= (part[0][o] + part[1][o]) + (part[2][o] + part[3][o]);
 }
 
 // ---- the same trailing update on the tensor cores (Ozaki scheme) ----
@@ -1885,7 +1913,7 @@ static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
       k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
                                                                                                         part);
   } else if (part == 1) {
-    k_wb_corner<<<dim3(NB / CT8, NB / CT8, nw), CT8 * CT8, 0, st>>>(b, p);
+    k_wb_corner<<<dim3(NB / CT8, NB / CT8, nw), CORNER_THREADS, 0, st>>>(b, p);
   } else {
     const int t = (mr + UT - 1) / UT;
     k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
@@ -1951,7 +1979,7 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   cudaGraphConditionalHandle h;
   cudaGraph_t body, done;
   k_wb_loop_set<<<1, 1, 0, st>>>(sd.panel, 0);
-  k_wb_diag<<<nw, 256, 0, st>>>(b, 0);
+  k_wb_diag<<<nw, DIAG_THREADS, 0, st>>>(b, 0);
   if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
   if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
@@ -1965,7 +1993,7 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   launch_wb_update(b, -1, 1, sb);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
-  k_wb_diag<<<nw, 256, 0, s2>>>(b, -2);
+  k_wb_diag<<<nw, DIAG_THREADS, 0, s2>>>(b, -2);
   cudaEventRecord(e_diag, s2);
   if (nrest) cudaStreamWaitEvent(sb, e_rest, 0);
   cudaEventRecord(e_trsm, sb);
@@ -2006,7 +2034,7 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
   // again before the backward substitution
   cudaEvent_t e_start = sd.evt[0], e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4],
               e_rest = sd.evt[5];
-  { ProfScope q(prof, st, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, st>>>(b, 0); }
+  { ProfScope q(prof, st, KC_WIDE_DIAG); k_wb_diag<<<nw, DIAG_THREADS, 0, st>>>(b, 0); }
   for (int p = 0; p < sd.max_panels; ++p) {
     bool next = p + 1 < sd.max_panels;
     if (nrest) {
@@ -2024,7 +2052,7 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); launch_wb_update(b, p, 1, st); }
       cudaEventRecord(e_corner, st);
       cudaStreamWaitEvent(s2, e_corner, 0);
-      { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, 256, 0, s2>>>(b, p + 1); }
+      { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<<<nw, DIAG_THREADS, 0, s2>>>(b, p + 1); }
       cudaEventRecord(e_diag, s2);
     }
     if (nrest) cudaStreamWaitEvent(st, e_rest, 0);
