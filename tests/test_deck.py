@@ -149,3 +149,12 @@ def test_reference_tutorial04_reads():
     assert s.pipe_sections[0][-2:] == (0.65, 0.62)
     assert len(s.loads) == 2 and s.loads[1].pipes == list(range(50))
     assert [so.end_time for so in [s.solution] + s.next_steps] == [1.0, 2.0]
+
+
+def test_reference_tutorial02_modal_step_reads():
+    """tutorial02: 3,036 Shell_1 and a Modal step (12 modes)."""
+    s = read_deck_file(_ref_deck("tutorial02"))
+    assert s.modal is not None and s.modal.number_modes == 12 and s.modal.compute_eigenvectors == 1
+    assert len(s.shells) == 3036 and s.n_free == 31323
+    r = read_deck(s.to_inp())
+    assert r.modal == s.modal
