@@ -35,7 +35,8 @@ solution steps:
   ConvergenceCriteria  the twelve tolerances and references
                   (src/ConvergenceCriteria.cpp:60-165)
 
-Output and run-control blocks (Monitor, PostFiles, SolverOptions,
+Monitor blocks are read (Sample and MonitorNodes; the other monitor lists
+are read past).  Output and run-control blocks (PostFiles, SolverOptions,
 ExecutionData, ConfigurationSave) are skipped.  A block this library does not
 solve (contact, particles, other elements, environment loads, special
 constraints, ...) raises DeckError naming it, instead of being ignored.
@@ -46,8 +47,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, ModalStep, NodalDisplacement, NodalLoad, PipeLoad,
-                    PressureLoad, Solution, Structure, Table)
+from .model import (DEFAULT_CRITERIA, GF_DYNAMIC, GF_STATIC, ModalStep, MonitorSpec, NodalDisplacement, NodalLoad,
+                    PipeLoad, PressureLoad, Solution, Structure, Table)
 
 # Every top-level keyword of IO::ReadFile: a block reader stops at the next one.
 TOP = {
@@ -59,7 +60,7 @@ TOP = {
     "ConcomitantSolution", "ConvergenceCriteria", "PostFiles", "ExecutionData", "PSYCoupling", "CADData",
     "ContactInterfaces", "Boundaries", "Geometries", "BodyGeometries", "EOF",
 }
-SKIPPED = {"Monitor", "PostFiles", "SolverOptions", "ExecutionData", "ConfigurationSave", "ConcomitantSolution"}
+SKIPPED = {"PostFiles", "SolverOptions", "ExecutionData", "ConfigurationSave", "ConcomitantSolution"}
 CRITERIA_KEYS = {
     "ForceTolerance": "force_tol", "MomentTolerance": "moment_tol", "ForceMinimumReference": "force_min",
     "MomentMinimumReference": "moment_min", "ConstraintMinimumReference": "constraint_min",
@@ -183,6 +184,7 @@ def read_deck(text: str, step: int = None) -> Structure:
     steps, nodes, elems, mats, secs, shell_secs, css, pipe_secs = [], {}, [], {}, {}, {}, {}, {}
     node_sets, elem_sets, loads, disps, cons = {}, {}, [], [], []
     criteria = dict(DEFAULT_CRITERIA)
+    mon_sample, mon_nodes = None, []
     while tk.more():
         kw = tk.next()
         if kw == "EOF":
@@ -190,6 +192,20 @@ def read_deck(text: str, step: int = None) -> Structure:
         if kw in SKIPPED:
             while tk.more() and tk.peek() not in TOP:
                 tk.next()
+            continue
+        if kw == "Monitor":
+            # Sample n, then MonitorNodes / MonitorElements / ... id lists;
+            # the nodes are kept (their monitor files are what this library
+            # writes), the other lists are read past
+            tk.expect("Sample")
+            mon_sample = tk.int()
+            while tk.more() and (tk.peek() or "").startswith("Monitor") and tk.peek() not in TOP:
+                which = tk.next()
+                ids = []
+                while tk.more() and (tk.peek() or "").isdigit():
+                    ids.append(tk.int())
+                if which == "MonitorNodes":
+                    mon_nodes += ids
             continue
         if kw == "SolutionSteps":
             for _ in range(tk.int()):
@@ -396,8 +412,13 @@ def read_deck(text: str, step: int = None) -> Structure:
             raise DeckError(f"block '{kw}' is not solved by this library")
         else:
             raise DeckError(f"unknown keyword '{kw}' (token {tk.i})")
-    return _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, elem_sets, loads, disps, cons,
-                  criteria, pipe_secs)
+    s = _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, elem_sets, loads, disps, cons,
+               criteria, pipe_secs)
+    if mon_sample is not None:
+        if any(n not in nodes for n in mon_nodes):
+            raise DeckError("Monitor: a monitored node is not defined")
+        s.monitor = MonitorSpec(mon_sample, [n - 1 for n in mon_nodes])
+    return s
 
 
 def _build(steps, step, nodes, elems, mats, secs, shell_secs, css, node_sets, elem_sets, loads, disps, cons,

@@ -221,6 +221,15 @@ class NodalDisplacement:
 
 
 @dataclass
+class MonitorSpec:
+    """A deck's Monitor block (reference src/Monitor.cpp:112-195): the nodes
+    whose state is written after every `sample`-th converged step (and at a
+    solution step's end)."""
+    sample: int = 1
+    nodes: list = field(default_factory=list)  # 0-based node indices
+
+
+@dataclass
 class ModalStep:
     """A Modal solution step (reference src/Modal.cpp:42-108): the
     number_modes smallest eigenvalues of K x = lambda M x at the structure's
@@ -281,6 +290,7 @@ class Structure:
     pipe_sections: list = field(default_factory=list)
     pipe_of: dict = field(default_factory=dict)        # beam index -> pipe section
     modal: ModalStep | None = None                     # a deck whose step is Modal
+    monitor: MonitorSpec | None = None                 # the deck's monitored nodes
 
     def __setattr__(self, name, value):
         # element rows assigned as lists become ElementTables
@@ -476,6 +486,10 @@ class Structure:
         if cons_lines:
             o.append(f"Constraints\t{len(cons_lines)}")
             o.extend(cons_lines)
+        if self.monitor is not None:
+            o.append(f"Monitor\tSample\t{int(self.monitor.sample)}" +
+                     ("\nMonitorNodes\t" + "\t".join(str(int(n) + 1) for n in self.monitor.nodes)
+                      if self.monitor.nodes else ""))
         c = self.criteria
         o.append("ConvergenceCriteria\n"
                  f"ForceTolerance\t{_r(c['force_tol'])}\nMomentTolerance\t{_r(c['moment_tol'])}\n"

@@ -30,6 +30,17 @@ typedef struct oracle_record {
   int* iterations;
   double* nodes;
   double* gp_Q;
+  /* Monitor lines (optional): for the mon_n nodes mon_nodes, every
+   * mon_sample-th converged step of a solution step and its end (and the
+   * start of the first step), Node::WriteMonitor's 31 columns per node:
+   * monitor[row][node][31], at most mon_cap rows; mon_rows receives the
+   * count. */
+  int mon_n;
+  const int* mon_nodes;
+  int mon_sample;
+  int mon_cap;
+  int mon_rows;
+  double* monitor;
 } oracle_record;
 
 /* Runs the structure's solution step.  final_nodes (n_nodes x 15, optional)

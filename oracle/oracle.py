@@ -38,7 +38,9 @@ def lib():
 class Record(C.Structure):
     _fields_ = [("cap", C.c_int), ("n", C.c_int), ("time", C.POINTER(C.c_double)),
                 ("iterations", C.POINTER(C.c_int)), ("nodes", C.POINTER(C.c_double)),
-                ("gp_Q", C.POINTER(C.c_double))]
+                ("gp_Q", C.POINTER(C.c_double)), ("mon_n", C.c_int), ("mon_nodes", C.POINTER(C.c_int)),
+                ("mon_sample", C.c_int), ("mon_cap", C.c_int), ("mon_rows", C.c_int),
+                ("monitor", C.POINTER(C.c_double))]
 
 
 def _dp(a):
@@ -53,17 +55,25 @@ def solve(structure, record_cap: int = 0):
     stats = (C.c_int * 4)()
     rec = None
     rd = None
+    mon = structure.monitor if getattr(structure, "monitor", None) is not None else None
     if record_cap:
         t = np.zeros(record_cap)
         it = np.zeros(record_cap, np.int32)
         nodes = np.zeros((record_cap, structure.n_nodes, 15))
         gq = np.zeros((record_cap, max(1, len(structure.beams)), 2, 9))
-        rec = Record(record_cap, 0, _dp(t), it.ctypes.data_as(C.POINTER(C.c_int)), _dp(nodes), _dp(gq))
+        mon_nodes = np.asarray(mon.nodes if mon else [0], dtype=np.int32)
+        mon_rows = np.zeros((record_cap + 1, max(1, len(mon_nodes)), 31))
+        rec = Record(record_cap, 0, _dp(t), it.ctypes.data_as(C.POINTER(C.c_int)), _dp(nodes), _dp(gq),
+                     len(mon.nodes) if mon else 0, mon_nodes.ctypes.data_as(C.POINTER(C.c_int)),
+                     int(mon.sample) if mon else 1, record_cap + 1, 0, _dp(mon_rows))
     if lib().oracle_solve(C.cast(h.ref, C.c_void_p), C.byref(rec) if rec else None, _dp(final), stats) < 0:
         raise ValueError("oracle: invalid structure description")
     if rec:
         n = rec.n
         rd = dict(time=t[:n], iterations=it[:n], nodes=nodes[:n], gp_Q=gq[:n])
+        if mon and mon.nodes:
+            # [node][row][31], as the reference writes one file per node
+            rd["monitor"] = np.transpose(mon_rows[:rec.mon_rows], (1, 0, 2)).copy()
     return final, np.array(list(stats)), rd
 
 

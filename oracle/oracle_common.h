@@ -58,6 +58,21 @@ static inline void m3_tvec(double* y, const double* a, const double* x) {
   double t2 = a[2] * x[0] + a[5] * x[1] + a[8] * x[2];
   y[0] = t0; y[1] = t1; y[2] = t2;
 }
+/* Inverse of a 3x3 matrix (row-major) by its adjugate over the determinant. */
+static inline void m3_inverse(double* r, const double* a) {
+  const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8], c02 = a[3] * a[7] - a[4] * a[6];
+  const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  const double id = 1.0 / det;
+  r[0] = c00 * id;
+  r[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+  r[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+  r[3] = c01 * id;
+  r[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+  r[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+  r[6] = c02 * id;
+  r[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+  r[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+}
 static inline void m3_skew(double* a, const double* v) {
   a[0] = 0.0;   a[1] = -v[2]; a[2] = v[1];
   a[3] = v[2];  a[4] = 0.0;   a[5] = -v[0];

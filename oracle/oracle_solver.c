@@ -76,13 +76,20 @@ typedef struct {
    * pp_load[pp_off[e] .. pp_off[e + 1]) */
   int* pp_off;
   int* pp_load;
+  /* Node::WriteMonitor's load vector per node and DOF at the last assembly:
+   * the element P_loading summed into every active DOF (global_I_A for the
+   * free ones, global_P_B for the fixed ones, which also carries -f of a
+   * NodalLoad on them), and the monitor's persistent load rows */
+  double* nload;
+  double* mon_load;
+  int sol_index;  /* index of the running solution step (the monitor starts with the first) */
 } ost;
 
 static void ost_free(ost* s) {
   free(s->GL); free(s->active); free(s->cons); free(s->disp); free(s->copy); free(s->Qn);
   free(s->vel); free(s->accel); free(s->copy_vel); free(s->copy_accel);
   free(s->bc); free(s->bh); free(s->sc); free(s->sh); free(s->ab); free(s->ipiv); free(s->PA); free(s->mult);
-  free(s->rd); free(s->rds); free(s->pf); free(s->pp_off); free(s->pp_load);
+  free(s->rd); free(s->rds); free(s->pf); free(s->pp_off); free(s->pp_load); free(s->nload); free(s->mon_load);
 }
 
 /* global DOF numbers (GLs) of a Shell_1 element's 27 DOFs: translations of
@@ -122,6 +129,8 @@ static int ost_init(ost* s, const gf_model_desc* m) {
   s->sc = calloc((size_t)(s->ns ? s->ns : 1), sizeof(os_const));
   s->sh = calloc((size_t)(s->ns ? s->ns : 1), sizeof(os_hist));
   s->mult = calloc((size_t)(m->n_loads ? m->n_loads : 1), sizeof(*s->mult));
+  s->nload = calloc((size_t)nn * 6, sizeof(double));
+  s->mon_load = calloc((size_t)nn * 6, sizeof(double));
   /* Node::Read sets copy_coordinates to the reference position
    * (reference src/Node.cpp:160-175); rotations start at zero */
   for (int i = 0; i < nn; ++i) {
@@ -276,6 +285,7 @@ static void assemble(ost* s) {
   const gf_model_desc* m = s->m;
   memset(s->ab, 0, sizeof(double) * (size_t)s->ldab * (size_t)(s->n_free ? s->n_free : 1));
   memset(s->PA, 0, sizeof(double) * (size_t)(s->n_free ? s->n_free : 1));
+  memset(s->nload, 0, sizeof(double) * 6 * (size_t)s->nn);
   double K[324], f[18], d[18];
   const double tnow = s->last_converged_time + s->current_time_step;
   for (int e = 0; e < s->nb; ++e) {
@@ -319,6 +329,7 @@ static void assemble(ost* s) {
     int g[18];
     for (int a = 0; a < 18; ++a) g[a] = s->GL[6 * b[a / 6] + a % 6];
     for (int a = 0; a < 18; ++a) {
+      if (g[a] != 0) s->nload[6 * b[a / 6] + a % 6] += f[a];
       if (g[a] > 0) s->PA[g[a] - 1] += f[a];
       for (int c = 0; c < 18; ++c) add_K(s, g[a], g[c], K[a + 18 * c]);
     }
@@ -379,6 +390,11 @@ static void assemble(ost* s) {
     int g[27];
     shell_dofs(s, e, g);
     for (int a = 0; a < 27; ++a) {
+      if (g[a] != 0) {
+        const int* nd = m->shells + 9 * e;
+        const int node = a < 18 ? nd[a / 3] : nd[3 + (a - 18) / 3], k = a < 18 ? a % 3 : 3 + (a - 18) % 3;
+        s->nload[6 * node + k] += fs[a];
+      }
       if (g[a] > 0) s->PA[g[a] - 1] += fs[a];
       for (int c = 0; c < 27; ++c) add_K(s, g[a], g[c], Ks[a + 27 * c]);
     }
@@ -410,10 +426,12 @@ static void assemble(ost* s) {
       for (int i = 0; i < 3; ++i) {
         int gi = s->GL[6 * node + i];
         if (s->active[6 * node + i] == 1 && gi > 0) s->PA[gi - 1] += -1.0 * fv[i];
+        if (s->active[6 * node + i] == 1 && gi < 0) s->nload[6 * node + i] += -1.0 * fv[i];
       }
       for (int i = 0; i < 3; ++i) {
         int gi = s->GL[6 * node + 3 + i];
         if (s->active[6 * node + 3 + i] == 1 && gi > 0) s->PA[gi - 1] += -1.0 * mm[i];
+        if (s->active[6 * node + 3 + i] == 1 && gi < 0) s->nload[6 * node + 3 + i] += -1.0 * mm[i];
         for (int j = 0; j < 3; ++j)
           if (s->active[6 * node + 3 + j] == 1) add_K(s, gi, s->GL[6 * node + 3 + j], -1.0 * V[i * 3 + j]);
       }
@@ -609,6 +627,47 @@ static void record(ost* s, oracle_record* rec, double time, int iterations) {
   }
 }
 
+/* One monitor line per monitored node (Node::WriteMonitor, reference
+ * src/Node.cpp:227-320): time, copy_coordinates 0..2, the Euler rotation
+ * vector of the accumulated Rodrigues vector (2 atan(|a| / 2) a / |a|,
+ * src/Node.cpp:350-358), the load of every active DOF (I_A free, P_B fixed,
+ * kept from the previous line where a DOF has no number yet), its moments
+ * turned from pseudo-moments by Xi(alpha)^-T with alpha the node's last
+ * rotation increment, the same six again (the local columns equal the
+ * global ones in the spatial description), copy_vel and copy_accel. */
+static void monitor_row(ost* s, oracle_record* rec, double time, int numbered) {
+  if (!rec || !rec->monitor || rec->mon_n <= 0 || rec->mon_rows >= rec->mon_cap) return;
+  double* row = rec->monitor + (size_t)rec->mon_rows * rec->mon_n * 31;
+  rec->mon_rows++;
+  for (int q = 0; q < rec->mon_n; ++q) {
+    const int i = rec->mon_nodes[q];
+    double* o = row + 31 * q;
+    double* L = s->mon_load + 6 * i;
+    if (numbered)
+      for (int k = 0; k < 6; ++k)
+        if (s->active[6 * i + k] == 1 && s->GL[6 * i + k] != 0) L[k] = s->nload[6 * i + k];
+    const double* a = s->disp + 6 * i + 3;
+    const double an = v3_norm(a), g = 4.0 / (4.0 + an * an);
+    double A[9], Xt[9], inv[9], mo[3];
+    m3_skew(A, a);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) Xt[r * 3 + c] = g * ((r == c ? 1.0 : 0.0) + 0.5 * A[c * 3 + r]);
+    m3_inverse(inv, Xt);
+    m3_vec(mo, inv, L + 3);
+    for (int k = 0; k < 3; ++k) L[3 + k] = mo[k];
+    o[0] = time;
+    for (int k = 0; k < 3; ++k) o[1 + k] = s->copy[6 * i + k];
+    const double* r3 = s->copy + 6 * i + 3;
+    const double rn = v3_norm(r3), th = 2.0 * atan(rn / 2.0);
+    for (int k = 0; k < 3; ++k) o[4 + k] = rn != 0.0 ? (th / rn) * r3[k] : 0.0;
+    for (int k = 0; k < 6; ++k) o[7 + k] = o[13 + k] = L[k];
+    for (int k = 0; k < 6; ++k) {
+      o[19 + k] = s->copy_vel[6 * i + k];
+      o[25 + k] = s->copy_accel[6 * i + k];
+    }
+  }
+}
+
 static int solve_linear(ost* s) {
   const int n = s->n_free;
   if (n == 0) return 0;
@@ -630,6 +689,7 @@ static int static_solve(ost* s, const gf_solution* so, double start_time, oracle
   s->n_conv_evaluated = 0;
   s->last_converged_time = start_time;
   record(s, rec, start_time, 0);
+  if (s->sol_index == 0) monitor_row(s, rec, start_time, 0);
   double time_step = so->time_step, time = s->last_converged_time;
   s->diverged = 0;
   for (int i = 0; i < s->nn * 6; ++i) s->copy_vel[i] = s->copy_accel[i] = s->vel[i] = s->accel[i] = 0.0;
@@ -679,6 +739,9 @@ static int static_solve(ost* s, const gf_solution* so, double start_time, oracle
         convergence_counter = 0;
       }
       if (!aborted) record(s, rec, time, it - 1);
+      if (!aborted && rec && rec->mon_n > 0 &&
+          (converged_number % (rec->mon_sample > 0 ? rec->mon_sample : 1) == 0 || time == so->end_time))
+        monitor_row(s, rec, time, 1);
     } else {
       memset(s->disp, 0, sizeof(double) * 6 * (size_t)s->nn);
       for (int i = 0; i < s->nn * 6; ++i) { s->vel[i] = s->copy_vel[i]; s->accel[i] = s->copy_accel[i]; }
@@ -736,6 +799,7 @@ static int dynamic_solve(ost* s, const gf_solution* so, double start_time, oracl
   s->n_conv_evaluated = 0;
   s->last_converged_time = start_time;
   record(s, rec, start_time, 0);
+  if (s->sol_index == 0) monitor_row(s, rec, start_time, 0);
   double time_step = so->time_step, time = s->last_converged_time;
   /* ComputeInitialConditions (reference src/Solution.cpp:866-885): Zeros(),
    * ZeroIC when asked, then a SaveConfiguration that leaves every node's
@@ -787,6 +851,9 @@ static int dynamic_solve(ost* s, const gf_solution* so, double start_time, oracl
       save_configuration(s);
       convergence_counter++;
       if (!aborted) record(s, rec, time, it - 1);
+      if (!aborted && rec && rec->mon_n > 0 &&
+          (converged_number % (rec->mon_sample > 0 ? rec->mon_sample : 1) == 0 || time == so->end_time))
+        monitor_row(s, rec, time, 1);
       if (it <= so->min_it || convergence_counter >= so->conv_increase) {
         time_step = time_step * so->inc_factor;
         if (time_step > so->max_time_step) time_step = so->max_time_step;
@@ -832,6 +899,7 @@ int oracle_solve(const gf_model_desc* m, oracle_record* rec, double* final_nodes
   double start = m->solution.start_time;
   for (int k = 0; k <= m->n_next_steps && r == 0; ++k) {
     const gf_solution* so = k == 0 ? &m->solution : m->next_steps + (k - 1);
+    s.sol_index = k;
     s.dynamic = so->type == GF_DYNAMIC;
     s.ray = s.dynamic && (so->rayleigh_alpha != 0.0 || so->rayleigh_beta != 0.0);
     if (s.ray) {

@@ -17,6 +17,7 @@
 #include "Hooke.h"
 #include "LagrangeSave.h"
 #include "Modal.h"
+#include "Monitor.h"
 #include "NodalConstraint.h"
 #include "NodalDisplacement.h"
 #include "NodalLoad.h"
@@ -240,7 +241,13 @@ int giraffe_ref_load(const char* path) {
     } else if (!strcmp(s, "SolverOptions")) {
       TryComment(f);
       ok = db.solver_options->Read(f);
-    } else if (!strcmp(s, "Monitor") || !strcmp(s, "PostFiles")) {
+    } else if (!strcmp(s, "Monitor")) {
+      // the reference's own reader (src/Monitor.cpp:112-195); the recording
+      // hook writes the monitored nodes' lines
+      db.monitor = new Monitor();
+      ok = db.monitor->Read(f);
+      db.monitor_exist = true;
+    } else if (!strcmp(s, "PostFiles")) {
       while (fscanf(f, "%999s", s) == 1) {
         if (is_keyword(s)) { have = true; break; }
       }

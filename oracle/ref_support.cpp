@@ -88,7 +88,18 @@ void PostFiles::UpdateSinglePartPostFiles(int solution, double time, int file_in
   ref_record_state(solution, time);
 }
 void PostFiles::WriteConfigurationResults(int, double, int) {}
-void Monitor::UpdateMonitor(double) {}
+// Monitor::UpdateMonitor: each monitored node's own monitor line
+// (Node::WriteMonitor, reference src/Node.cpp:227-320, the reference's code
+// and format) into the record, tagged "M <node>".
+void Monitor::UpdateMonitor(double time) {
+  FILE* f = ref_hooks_storage.rec;
+  if (!f) return;
+  for (size_t i = 0; i < nodes.size(); ++i) {
+    fprintf(f, "M %d\t", nodes[i]);
+    db.nodes[nodes[i] - 1]->WriteMonitor(f, false, time);
+  }
+  first_record = false;
+}
 
 // ---- SparseMatrix over the CSR stand-in ----
 SparseMatrix::SparseMatrix() {

@@ -48,6 +48,11 @@ stores what the reference computes:
                          raised to 20 MPa: Dynamic (Newmark), 100 steps.
 * ref_pipe_riser_rayleigh.npz  the same with Rayleigh damping (alpha 0.3,
                          beta 0.004, Update 1).
+* ref_monitor_tutorial10.npz, ref_monitor_chain.npz, ref_monitor_plate.npz,
+  ref_monitor_sequence.npz
+                         runs with a Monitor block: besides the configurations,
+                         the reference's own monitor line of every monitored
+                         node at every monitored time (Node::WriteMonitor).
 * ref_modal_cantilever.npz, ref_modal_plate.npz, ref_modal_riser.npz
                          the two matrices of a Modal step (K_AA and the modal
                          mass M_AA, dense) from the reference build for
@@ -128,11 +133,26 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def parse_monitor(path):
+    """Monitor lines "M <node>" + Node::WriteMonitor's 31 columns (TIME, X..Z,
+    ROTX..ROTZ, FX..MZ, FXloc..MZloc, dX..dROTZ, ddX..ddROTZ): (0-based node
+    ids, [node][record][31])."""
+    rows = {}
+    for line in open(path):
+        p = line.split()
+        if p and p[0] == "M":
+            rows.setdefault(int(p[1]), []).append([float(x) for x in p[2:]])
+    ids = list(rows)
+    return np.array([i - 1 for i in ids], dtype=np.int32), np.array([rows[i] for i in ids])
+
+
 def parse_rec(path):
     recs = []
     cur = None
     for line in open(path):
         p = line.split()
+        if p[0] == "M":
+            continue
         if p[0] == "T":
             cur = {"t": float(p[2]), "N": [], "G": []}
             recs.append(cur)
@@ -173,7 +193,10 @@ def run_deck(L, s, tag, tmp):
     rc = L.giraffe_ref_solve(rec.encode(), log.encode())
     times, nodes, gq = parse_rec(rec)
     steps = parse_log(log)
-    return dict(rc=np.array(rc), times=times, nodes=nodes, gp_Q=gq, steps=steps, deck=np.array(s.to_inp()))
+    out = dict(rc=np.array(rc), times=times, nodes=nodes, gp_Q=gq, steps=steps, deck=np.array(s.to_inp()))
+    if s.monitor is not None and s.monitor.nodes:
+        out["monitor_nodes"], out["monitor"] = parse_monitor(rec)
+    return out
 
 
 def element_cases(rng, n):
@@ -527,6 +550,29 @@ def make_elements():
         np.savez_compressed(os.path.join(HERE, "ref_shell_inertia.npz"), **run_shell_inertia(L, rng, 16, tmp))
 
 
+def _monitored(make, nodes, sample=1, end_steps=None):
+    """A configuration with a Monitor block on `nodes` (optionally cut to its
+    first `end_steps` time steps)."""
+    def build():
+        from giraffe_gb300.model import MonitorSpec
+        s = make()
+        if end_steps is not None:
+            s.solution.end_time = s.solution.start_time + end_steps * s.solution.time_step
+        s.monitor = MonitorSpec(sample, list(nodes))
+        return s
+    return build
+
+
+DECKS.update({
+    # monitored nodes: Node::WriteMonitor's columns after each converged
+    # step (positions, Euler rotation vectors, the internal-force / reaction
+    # vector with pseudo-moments turned to moments, velocities, accelerations)
+    "ref_monitor_tutorial10.npz": _monitored(configs.tutorial10, [0, 5, 10], sample=3, end_steps=150),
+    "ref_monitor_chain.npz": _monitored(small_chain, [0, 1, 30, 60]),
+    "ref_monitor_plate.npz": _monitored(lambda: configs.square_plate(3, steps=10), [0, 3, 24, 23]),
+    "ref_monitor_sequence.npz": _monitored(configs.chain_sequence, [0, 20, 40], sample=2),
+})
+
 MODAL_DECKS = {
     "ref_modal_cantilever.npz": configs.tutorial01,
     "ref_modal_plate.npz": lambda: configs.square_plate(3, steps=10),
@@ -588,8 +634,9 @@ def make_tutorial04():
         rc = L.giraffe_ref_solve(rec.encode(), log.encode())
         times, nodes, gq = parse_rec(rec)
         steps = parse_log(log)
+        mon_ids, mon = parse_monitor(rec)
     np.savez_compressed(os.path.join(HERE, "ref_tutorial04.npz"), rc=np.array(rc), times=times, nodes=nodes,
-                        gp_Q=gq, steps=steps, deck=np.array(s.to_inp()))
+                        gp_Q=gq, steps=steps, deck=np.array(s.to_inp()), monitor_nodes=mon_ids, monitor=mon)
 
 
 def make_deck(name):
