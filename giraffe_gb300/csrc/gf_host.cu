@@ -762,6 +762,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   std::vector<LoadEntry> loads;
   std::vector<int> pp_elem, pp_table;
   std::vector<double> pp_aint;
+  std::vector<int> mon_node, mon_struct, mon_adj_off(1, 0);
+  std::vector<int2> mon_adj;
+  B->mon_first.clear();
   std::vector<DispEntry> disps;
   std::vector<TableDev> tables;
   std::vector<double> tdata;
@@ -851,6 +854,31 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       }
     }
     inf.n_loads = (int)loads.size() - inf.load_off;
+    // monitored nodes (Monitor: Sample, MonitorNodes) and the elements that
+    // meet at each
+    inf.mon_off = (int)mon_node.size();
+    inf.mon_n = 0;
+    inf.mon_sample = std::max(m.monitor_sample, 1);
+    if (B->opts.monitor_rows > 0 && m.n_monitor_nodes > 0 && m.monitor_nodes) {
+      for (int q = 0; q < m.n_monitor_nodes; ++q) {
+        const int nd = m.monitor_nodes[q];
+        if (nd < 0 || nd >= m.n_nodes) { set_err(ctx, "structure %d: monitored node %d out of range", s, nd); return GF_ERR_ARG; }
+        mon_node.push_back(node_off + nd);
+        mon_struct.push_back(s);
+        for (int e = 0; e < m.n_beams; ++e)
+          for (int j = 0; j < 3; ++j)
+            if (m.beams[6 * e + j] == nd) mon_adj.push_back(make_int2(elem_offs[s] + e, j));
+        for (int e = 0; e < m.n_shells; ++e)
+          for (int j = 0; j < 6; ++j)
+            if (m.shells[9 * e + j] == nd) mon_adj.push_back(make_int2(shell_off + e, 64 + j));
+        mon_adj_off.push_back((int)mon_adj.size());
+        B->mon_first.push_back(m.node_xyz[3 * nd]);
+        B->mon_first.push_back(m.node_xyz[3 * nd + 1]);
+        B->mon_first.push_back(m.node_xyz[3 * nd + 2]);
+        B->mon_first.push_back(m.solution.start_time);
+        inf.mon_n++;
+      }
+    }
     for (int l = 0; l < m.n_displacements; ++l) {
       const gf_displacement& D = m.displacements[l];
       if (D.table.n_cols < 6) { set_err(ctx, "structure %d: displacement table needs 6 columns", s); return GF_ERR_ARG; }
@@ -917,6 +945,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.n_free = dof_off;
   b.n_loads = (int)loads.size();
   b.n_pipe_press = (int)pp_elem.size();
+  b.mon_total = (int)mon_node.size();
+  b.mon_cap = b.mon_total ? B->opts.monitor_rows : 0;
   b.n_disps = (int)disps.size();
   b.n_tables = (int)tables.size();
   // chain solver data: sizes and offsets per structure (serial), then the
@@ -1072,7 +1102,10 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !upload(B, &b.baux, baux) || !upload(B, &b.color_elems, color_elems) || !upload(B, &b.dof_node6, dof_node6) ||
       !upload(B, &b.info, B->info) || !upload(B, &b.params, params) || !upload(B, &b.step_params, step_params) ||
       !upload(B, &b.loads, loads) || !upload(B, &b.pp_elem, pp_elem) || !upload(B, &b.pp_table, pp_table) ||
-      !upload(B, &b.pp_aint, pp_aint) ||
+      !upload(B, &b.pp_aint, pp_aint) || !upload(B, &b.mon_node, mon_node) ||
+      !upload(B, &b.mon_struct, mon_struct) || !upload(B, &b.mon_adj_off, mon_adj_off) ||
+      !upload(B, &b.mon_adj, mon_adj) || !balloc(B, &b.mon_load, (size_t)b.mon_total * 6) ||
+      !balloc(B, &b.mon_rec, (size_t)b.mon_total * b.mon_cap * 25) ||
       !upload(B, &b.disps, disps) || !upload(B, &b.tables, tables) || !upload(B, &b.table_data, tdata) ||
       !dup(B, &B->copy0, b.copy, copy.size()) || !dup(B, &B->Qn0, b.Qn, Qn.size()) ||
       !dup(B, &B->bhist0, b.bhist, bhist.size()) || !dup(B, &B->baux0, b.baux, baux.size()))
@@ -1127,7 +1160,7 @@ int count_launches_per_pass(const gf_batch* B) {
     }
   }
   return 10 + colors + chain_launches + shell_launches_per_pass(B->b) + (B->b.any_rayleigh ? 1 : 0) +
-         (B->b.n_pipe_press ? 1 : 0);
+         (B->b.n_pipe_press ? 1 : 0) + (B->b.mon_total ? 1 : 0);
 }
 
 int batch_reset(gf_batch* B) {
@@ -1148,6 +1181,7 @@ int batch_reset(gf_batch* B) {
   CK(cudaMemsetAsync(b.accel, 0, n6, st));
   CK(cudaMemsetAsync(b.copy_vel, 0, n6, st));
   CK(cudaMemsetAsync(b.copy_accel, 0, n6, st));
+  if (b.mon_total) CK(cudaMemsetAsync(b.mon_load, 0, sizeof(double) * (size_t)b.mon_total * 6, st));
   launch_init_state(b, st);
   CK(cudaGetLastError());
   return GF_OK;
@@ -1194,6 +1228,7 @@ void gf_default_opts(gf_solve_opts* o) {
   o->use_graph = 1;
   o->wide_update = GF_WIDE_TENSOR;
   o->max_passes = 0;
+  o->monitor_rows = 0;
 }
 
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts) {
@@ -1606,6 +1641,45 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
     });
   }
   B->host_ms[4] = host_now_ms() - t0;
+  return GF_OK;
+}
+
+int gf_batch_monitor(gf_batch* B, int s, double* out, int* dims) {
+  if (!B || !dims || s < 0 || s >= B->b.n_struct) return GF_ERR_ARG;
+  gf_ctx* ctx = B->ctx;
+  const StructInfo& inf = B->info[s];
+  StructState st{};
+  GF_CK(cudaMemcpy(&st, B->b.state + s, sizeof(st), cudaMemcpyDeviceToHost));
+  const int made = inf.mon_n ? st.mon_rows : 0, kept = std::min(made, B->b.mon_cap);
+  dims[0] = inf.mon_n;
+  dims[1] = inf.mon_n ? 1 + kept : 0;
+  dims[2] = inf.mon_n ? 1 + made : 0;
+  if (!out || !inf.mon_n) return GF_OK;
+  std::vector<double> rec((size_t)inf.mon_n * B->b.mon_cap * 25);
+  GF_CK(cudaMemcpy(rec.data(), B->b.mon_rec + (size_t)inf.mon_off * B->b.mon_cap * 25, sizeof(double) * rec.size(),
+                   cudaMemcpyDeviceToHost));
+  const int rows = 1 + kept;
+  for (int q = 0; q < inf.mon_n; ++q) {
+    const double* first = &B->mon_first[4 * (size_t)(inf.mon_off + q)];
+    double* o = out + (size_t)q * rows * 31;
+    std::memset(o, 0, sizeof(double) * 31);
+    o[0] = first[3];
+    for (int k = 0; k < 3; ++k) o[1 + k] = first[k];
+    for (int r = 0; r < kept; ++r) {
+      const double* x = &rec[((size_t)q * B->b.mon_cap + r) * 25];
+      double* L = o + (size_t)(r + 1) * 31;
+      L[0] = x[0];
+      for (int k = 0; k < 3; ++k) L[1 + k] = x[1 + k];
+      // the Euler rotation vector of the accumulated Rodrigues vector
+      // (reference src/Node.cpp:350-358)
+      const double an = std::sqrt(x[4] * x[4] + x[5] * x[5] + x[6] * x[6]);
+      const double th = 2.0 * std::atan(an / 2.0);
+      for (int k = 0; k < 3; ++k) L[4 + k] = an != 0.0 ? (th / an) * x[4 + k] : 0.0;
+      for (int k = 0; k < 6; ++k) L[7 + k] = L[13 + k] = x[7 + k];
+      for (int k = 0; k < 6; ++k) L[19 + k] = x[13 + k];
+      for (int k = 0; k < 6; ++k) L[25 + k] = x[19 + k];
+    }
+  }
   return GF_OK;
 }
 

@@ -134,6 +134,10 @@ struct gf_batch {
   // offsets
   hvec<int> h_gl, h_enodes, h_snodes;
   std::vector<int> shell_off;
+  // the monitor's first line of each monitored entry (the first solution
+  // step's start: the reference coordinates; loads, rotations, velocities
+  // zero): x, y, z and the start time
+  std::vector<double> mon_first;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;

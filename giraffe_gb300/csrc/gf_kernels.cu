@@ -1045,10 +1045,19 @@ __global__ void k_control(Batch b) {
     atomicAdd(b.running, 1);
     return;
   }
+  st.mon_now = 0;
   if (!st.diverged) {
     st.converged_number++;
     st.commit = 1;
     st.convergence_counter++;
+    // the monitor's rule, on the solution step that converged (reference
+    // src/Static.cpp:268-276, src/Dynamic.cpp:392-399)
+    st.conv_in_step++;
+    const StructInfo& mi = b.info[s];
+    if (mi.mon_n > 0 && !st.aborted && (st.conv_in_step % mi.mon_sample == 0 || st.time == p.end_time)) {
+      st.mon_now = 1;
+      st.mon_rows++;
+    }
     if (st.it <= p.min_it || st.convergence_counter >= p.conv_increase) {
       st.time_step = st.time_step * p.inc_factor;
       if (st.time_step > p.max_time_step) st.time_step = p.max_time_step;
@@ -1075,6 +1084,7 @@ __global__ void k_control(Batch b) {
     // to save the velocities), and in every sequence the velocities it
     // decides on are zero or zeroed before they are read again.
     st.step++;
+    st.conv_in_step = 0;
     const StructParams np = b.step_params[b.info[s].step_off + st.step];
     b.params[s] = np;
     st.time = np.start_time;
@@ -1129,6 +1139,80 @@ __global__ void k_commit_nodes(Batch b) {
       b.copy_vel[(int64_t)i * 6 + k] = b.vel[(int64_t)i * 6 + k];
       b.copy_accel[(int64_t)i * 6 + k] = b.accel[(int64_t)i * 6 + k];
     }
+}
+
+// Monitor line of one monitored node (Node::WriteMonitor, reference
+// src/Node.cpp:227-320) after a committed step the monitor records: time,
+// copy_coordinates, the load of every numbered DOF -- the elements'
+// P_loading summed at the node (global_I_A at a free DOF, global_P_B at a
+// constrained one; a DOF without a number keeps its last value) with the
+// moments turned from pseudo-moments by Xi(alpha)^-T, alpha the node's
+// rotation increment -- and the converged velocities and accelerations.
+// One thread per monitored node.
+__global__ void k_monitor_record(Batch b) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= b.mon_total) return;
+  const int s = b.mon_struct[q];
+  const StructState& st = b.state[s];
+  if (!st.commit || !st.mon_now) return;
+  const int row = st.mon_rows - 1;
+  const int i = b.mon_node[q];
+  double* L = b.mon_load + (int64_t)q * 6;
+  double sum[6] = {0, 0, 0, 0, 0, 0};
+  const int64_t ne = b.n_elem;
+  for (int k = b.mon_adj_off[q]; k < b.mon_adj_off[q + 1]; ++k) {
+    const int2 a = b.mon_adj[k];
+    const int kind = a.y >> 6, at = a.y & 63;
+    if (kind == 0) {
+#pragma unroll
+      for (int d = 0; d < 6; ++d) sum[d] += b.Fe[(int64_t)(6 * at + d) * ne + a.x];
+    } else {
+      const double* F = b.sh.Fe + (int64_t)a.x * 27;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sum[d] += F[3 * at + d];
+      if (at >= 3)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sum[3 + d] += F[18 + 3 * (at - 3) + d];
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 6; ++d)
+    if (b.gl[(int64_t)i * 6 + d] != -2) L[d] = sum[d];
+  // pseudo-moment -> moment: m = Xi(alpha)^-T m
+  const V3<double> al = {{b.disp[(int64_t)i * 6 + 3], b.disp[(int64_t)i * 6 + 4], b.disp[(int64_t)i * 6 + 5]}};
+  const double g = 4.0 / (4.0 + dot(al, al));
+  M3<double> A = skew(al), Xt;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Xt[r * 3 + c] = g * ((r == c ? 1.0 : 0.0) + 0.5 * A[c * 3 + r]);
+  const double c00 = Xt[4] * Xt[8] - Xt[5] * Xt[7], c01 = Xt[5] * Xt[6] - Xt[3] * Xt[8],
+               c02 = Xt[3] * Xt[7] - Xt[4] * Xt[6];
+  const double id = 1.0 / (Xt[0] * c00 + Xt[1] * c01 + Xt[2] * c02);
+  M3<double> inv;
+  inv[0] = c00 * id;
+  inv[1] = (Xt[2] * Xt[7] - Xt[1] * Xt[8]) * id;
+  inv[2] = (Xt[1] * Xt[5] - Xt[2] * Xt[4]) * id;
+  inv[3] = c01 * id;
+  inv[4] = (Xt[0] * Xt[8] - Xt[2] * Xt[6]) * id;
+  inv[5] = (Xt[2] * Xt[3] - Xt[0] * Xt[5]) * id;
+  inv[6] = c02 * id;
+  inv[7] = (Xt[1] * Xt[6] - Xt[0] * Xt[7]) * id;
+  inv[8] = (Xt[0] * Xt[4] - Xt[1] * Xt[3]) * id;
+  const V3<double> m = mv(inv, V3<double>{{L[3], L[4], L[5]}});
+  L[3] = m[0];
+  L[4] = m[1];
+  L[5] = m[2];
+  if (row < 0 || row >= b.mon_cap) return;
+  double* o = b.mon_rec + ((int64_t)q * b.mon_cap + row) * 25;
+  o[0] = st.time;
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    o[1 + d] = b.copy[(int64_t)i * 6 + d];
+    o[7 + d] = L[d];
+    o[13 + d] = b.copy_vel[(int64_t)i * 6 + d];
+    o[19 + d] = b.copy_accel[(int64_t)i * 6 + d];
+  }
 }
 
 // Element-level entry (no batch): tangent and internal force, FP64.
@@ -1335,6 +1419,7 @@ void launch_iteration(const Batch& b, cudaStream_t st, bool commit_kernels, Laun
     if (b.n_elem) { ProfScope q(prof, st, KC_COMMIT_ELEMS); k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b); }
     if (b.sh.n_shells) { ProfScope q(prof, st, KC_COMMIT_ELEMS); launch_shell_commit(b, st); }
     if (b.n_nodes) { ProfScope q(prof, st, KC_COMMIT_NODES); k_commit_nodes<<<(b.n_nodes + 127) / 128, 128, 0, st>>>(b); }
+    if (b.mon_total) k_monitor_record<<<(b.mon_total + 127) / 128, 128, 0, st>>>(b);
   }
 }
 

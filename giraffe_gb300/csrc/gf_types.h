@@ -125,6 +125,10 @@ struct StructInfo {
   // solution steps: Batch::step_params[step_off .. step_off + n_steps)
   int step_off, n_steps;
   int64_t wb_off;    // into ShellData::wband
+  // monitored nodes (a deck's Monitor block): Batch::mon_* entries
+  // [mon_off, mon_off + mon_n), a line after every mon_sample-th converged
+  // step of a solution step and at its end
+  int mon_off, mon_n, mon_sample, pad_m;
 };
 
 // Per-structure Newton / load-step control state (reference
@@ -154,6 +158,10 @@ struct StructState {
   int ray_init;       // Rayleigh matrices formed (after the step's first iteration)
   int step;           // current solution step of the structure
   int zero_va;        // zero the nodal velocities / accelerations before the next time step
+  int conv_in_step;   // steps converged in the current solution step (the monitor's sample count)
+  int mon_rows;       // monitor lines recorded so far
+  int mon_now;        // this pass committed a step that the monitor records
+  int pad_mon;
   int host_step;      // the caller's step control set last_converged_time and
                       // current_time_step (gf_begin_step): step_begin keeps them
   int pad_st;
@@ -333,6 +341,18 @@ struct Batch {
   int* pp_elem;
   int* pp_table;
   double* pp_aint;
+  // monitored nodes: batch node, structure, element incidences
+  // mon_adj[mon_adj_off[q] .. mon_adj_off[q + 1]) (x: element, y: 64 * kind
+  // + the node's place in it; kind 0 Beam_1 / Pipe_1, 1 Shell_1), the load
+  // each keeps between lines (Node::load) and the lines, [q][mon_cap][25]:
+  // time, copy_coordinates (6), load (6), copy_vel (6), copy_accel (6)
+  int mon_total, mon_cap;
+  int* mon_node;
+  int* mon_struct;
+  int* mon_adj_off;
+  int2* mon_adj;
+  double* mon_load;
+  double* mon_rec;
   // loads
   LoadEntry* loads;
   DispEntry* disps;

@@ -29,7 +29,7 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_shell_inertia_elements", "gf_ctx_set_opts", "gf_upload_structure", "gf_structure_destroy",
            "gf_structure_dims", "gf_structure_dofs", "gf_structure_pattern", "gf_structure_set_step", "gf_begin_step",
            "gf_assemble", "gf_set_increment", "gf_commit", "gf_rollback", "gf_structure_nodes", "gf_beam_mount",
-           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange", "gf_structure_modal", "gf_modal"]
+           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange", "gf_structure_modal", "gf_modal", "gf_batch_monitor"]
 
 GF_LAYOUT_CSR, GF_LAYOUT_GB = 0, 1
 GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
@@ -37,7 +37,8 @@ GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
 
 class gf_solve_opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_refine", C.c_int), ("poll_every", C.c_int),
-                ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int)]
+                ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int),
+                ("monitor_rows", C.c_int)]
 
 
 class gf_stats(C.Structure):
@@ -123,6 +124,7 @@ def lib():
         L.gf_structure_nodes.argtypes = [vp, dp, dp]
         L.gf_structure_modal.argtypes = [vp, C.c_double, C.c_int, C.c_double, dp, dp, ip]
         L.gf_modal.argtypes = [vp, C.POINTER(gf_model_desc), C.c_int, C.c_double, dp, dp, ip]
+        L.gf_batch_monitor.argtypes = [vp, C.c_int, dp, ip]
         L.gf_beam_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
         L.gf_beam_save_lagrange.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp]
         L.gf_shell_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.c_int, dp, dp]
@@ -181,10 +183,11 @@ class Context:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
     def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=None, wide_update=None,
-             max_passes=0):
+             max_passes=0, monitor_rows=0):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
         o.precision, o.use_graph, o.poll_every, o.max_passes = precision, int(use_graph), poll_every, max_passes
+        o.monitor_rows = monitor_rows
         if max_refine is not None:
             o.max_refine = max_refine
         if wide_update is not None:
@@ -480,6 +483,17 @@ class BatchSolver:
         self.ctx.check(self.ctx.L.gf_batch_results(self.h, ptrs, stats), "gf_batch_results")
         st = np.array([[x.converged_steps, x.newton_iterations, x.bisections, x.aborted] for x in stats])
         return outs, st
+
+    def monitor(self, s: int):
+        """Structure s's monitor lines (gf_batch_monitor): [node][line][31]
+        in Node::WriteMonitor's columns, and the number of lines the run
+        produced (more than returned when monitor_rows ran out)."""
+        dims = (C.c_int * 3)()
+        self.ctx.check(self.ctx.L.gf_batch_monitor(self.h, s, None, dims), "gf_batch_monitor")
+        out = np.zeros((dims[0], dims[1], 31))
+        if dims[0]:
+            self.ctx.check(self.ctx.L.gf_batch_monitor(self.h, s, _dp(out), dims), "gf_batch_monitor")
+        return out, dims[2]
 
     def assemble(self, s: int):
         dims = (C.c_int * 2)()

@@ -102,7 +102,8 @@ class gf_model_desc(C.Structure):
                 ("n_displacements", C.c_int), ("displacements", _vp),
                 ("solution", gf_solution), ("criteria", gf_criteria), ("beam_pretension", _vp),
                 ("n_next_steps", C.c_int), ("next_steps", _vp),
-                ("n_pipe_sections", C.c_int), ("pipe_sections", _vp), ("beam_pipe_section", _vp)]
+                ("n_pipe_sections", C.c_int), ("pipe_sections", _vp), ("beam_pipe_section", _vp),
+                ("n_monitor_nodes", C.c_int), ("monitor_nodes", _vp), ("monitor_sample", C.c_int)]
 
 
 def _r(v):
@@ -577,13 +578,16 @@ class DescHandle:
             for e, p in s.pipe_of.items():
                 bps[int(e)] = int(p)
             self.keep.append(bps)
+        mon_nodes = i(np.asarray(s.monitor.nodes)) if s.monitor is not None and s.monitor.nodes else None
         self.desc = gf_model_desc(
             len(nodes), _ptr(nodes, _dp), len(mats), _ptr(mats, _dp), len(secs), _ptr(secs, _dp),
             len(ssec), _ptr(ssec, _dp), len(cs), _ptr(cs, _dp), len(beams), _ptr(beams, _ip),
             len(shells), _ptr(shells, _ip), _ptr(cons, _ip), len(s.loads), C.addressof(loads),
             len(s.displacements), C.addressof(disps), sol, crit, _ptr(pre), len(s.next_steps),
             C.addressof(nxt) if s.next_steps else None,
-            len(psec) if psec is not None else 0, _ptr(psec, _dp), _ptr(bps, _ip))
+            len(psec) if psec is not None else 0, _ptr(psec, _dp), _ptr(bps, _ip),
+            len(mon_nodes) if mon_nodes is not None else 0, _ptr(mon_nodes, _ip),
+            int(s.monitor.sample) if s.monitor is not None else 1)
 
     @property
     def ref(self):

@@ -86,6 +86,8 @@ typedef struct gf_solve_opts {
   int max_passes;  /* host cap on the Newton passes of one gf_batch_run;
                       beyond it the run stops with GF_ERR_TIMEOUT (0: the
                       default of 4,000,000) */
+  int monitor_rows; /* monitor lines kept per structure with a Monitor
+                      (gf_model_desc monitor_nodes; 0: none recorded) */
 } gf_solve_opts;
 enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1, GF_WIDE_TENSOR_SYNC = 2 };
 
@@ -396,6 +398,22 @@ int gf_rollback(gf_structure* s);
  * the nodal rotation tensor row-major) and increments (n_nodes x 6, the
  * step's Node::displacements); either may be NULL. */
 int gf_structure_nodes(gf_structure* s, double* nodes, double* increments);
+
+/* ---- Monitor ----
+ * gf_batch_monitor returns structure s's monitor lines after a run: for
+ * each of its monitor_nodes, the lines Node::WriteMonitor writes (reference
+ * src/Node.cpp:227-320; src/Monitor.cpp:384-401 calls it at the first
+ * solution step's start, after every monitor_sample-th converged step of a
+ * solution step and at a step's end): 31 columns TIME, X Y Z (position),
+ * ROTX ROTY ROTZ (Euler rotation vector), FX FY FZ MX MY MZ (the elements'
+ * internal force at a free DOF, the reaction at a constrained one; moments
+ * from the pseudo-moments), the same six as the local columns (equal in the
+ * spatial description), the velocities and the accelerations.  out is
+ * [node][line][31] (NULL: dims only); dims[0] monitored nodes, dims[1]
+ * lines returned, dims[2] lines the run produced (more than dims[1] when
+ * gf_solve_opts.monitor_rows ran out).  A NodalLoad acting on a constrained
+ * DOF is not added to its reaction column. */
+int gf_batch_monitor(gf_batch* b, int s, double* out, int* dims);
 
 /* ---- Modal analysis ----
  * gf_structure_modal replaces Modal::Solve (src/Modal.cpp:131-199) with its

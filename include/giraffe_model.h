@@ -135,6 +135,11 @@ typedef struct gf_model_desc {
   int n_pipe_sections;
   const double* pipe_sections;   /* [n][11]: EA, EI, GJ, GA, Rho, CDt, CDn, CAt, CAn, De, Di */
   const int* beam_pipe_section;  /* [n_beams]: -1 for Beam_1, else the pipe section; or NULL */
+  /* Monitor (reference src/Monitor.cpp:112-195): MonitorNodes (0-based) and
+   * Sample; lines are kept when gf_solve_opts.monitor_rows > 0 */
+  int n_monitor_nodes;
+  const int* monitor_nodes;
+  int monitor_sample;
 } gf_model_desc;
 
 #ifdef __cplusplus

@@ -158,3 +158,16 @@ def test_reference_tutorial02_modal_step_reads():
     assert len(s.shells) == 3036 and s.n_free == 31323
     r = read_deck(s.to_inp())
     assert r.modal == s.modal
+
+
+def test_monitor_file_text_round_trips():
+    """The monitor writer's text: Node::WriteMonitor's header and %.6e
+    columns, which read back as the values to that precision."""
+    from giraffe_gb300.monitor import HEADER, node_lines
+    rng = np.random.default_rng(3)
+    lines = rng.normal(size=(5, 31)) * 10.0 ** rng.integers(-8, 6, size=(5, 31))
+    text = node_lines(lines)
+    rows = text.strip().split("\n")
+    assert rows[0] == HEADER and len(rows[0].split("\t")) == 31
+    back = np.array([[float(v) for v in r.split("\t")] for r in rows[1:]])
+    assert np.allclose(back, lines, rtol=6e-7, atol=0)
