@@ -1142,7 +1142,6 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
   b.sh.wide_tc = b.sh.oz_slices != nullptr ? B->opts.wide_update : GF_WIDE_FP64;
-  b.max_refine = B->opts.max_refine;
   return GF_OK;
 }
 
@@ -1223,7 +1222,6 @@ int gf_ctx_set_opts(gf_ctx* ctx, const gf_solve_opts* opts) {
 
 void gf_default_opts(gf_solve_opts* o) {
   o->precision = GF_PREC_FP64;
-  o->max_refine = 6;
   o->poll_every = 8;
   o->use_graph = 1;
   o->wide_update = GF_WIDE_TENSOR;
@@ -1620,7 +1618,6 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       z.newton_iterations = st[s].total_it;
       z.bisections = st[s].bisections;
       z.aborted = st[s].phase == PH_ABORTED || st[s].aborted;
-      z.fp64_fallback = st[s].fp64_fallback;
       z.linear_solves = st[s].n_solves;
       stats[s] = z;
     }

@@ -51,7 +51,10 @@ __global__ void k_iter_set(Batch b, int it, int need_solve, int phase, int commi
   if (it < 0 && b.params[0].ray_on) st.ray_init = 1;
   if (need_solve >= 0) st.need_solve = need_solve;
   if (phase >= 0) st.phase = phase;
-  if (commit >= 0) st.commit = commit;
+  if (commit >= 0) {
+    st.commit = commit;
+    st.commit_dyn = b.params[0].dynamic;
+  }
 }
 
 // Starts the step at (last_converged_time, time_step) of the caller.

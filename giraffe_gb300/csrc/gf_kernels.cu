@@ -1049,6 +1049,7 @@ __global__ void k_control(Batch b) {
   if (!st.diverged) {
     st.converged_number++;
     st.commit = 1;
+    st.commit_dyn = p.dynamic;
     st.convergence_counter++;
     // the monitor's rule, on the solution step that converged (reference
     // src/Static.cpp:268-276, src/Dynamic.cpp:392-399)
@@ -1080,9 +1081,8 @@ __global__ void k_control(Batch b) {
     // anew (Dynamic::Solve's `first`), and zero nodal velocities for a
     // Static step (ZerosVelAccel) or a Dynamic one with ZeroIC.  The commit
     // kernels of this pass still save the converged state of the step that
-    // ended; of the new parameters they read only the Dynamic flag (whether
-    // to save the velocities), and in every sequence the velocities it
-    // decides on are zero or zeroed before they are read again.
+    // ended, with the ended step's Dynamic flag (commit_dyn) deciding
+    // whether its velocities are saved, as SaveConfiguration does.
     st.step++;
     st.conv_in_step = 0;
     const StructParams np = b.step_params[b.info[s].step_off + st.step];
@@ -1134,7 +1134,9 @@ __global__ void k_commit_nodes(Batch b) {
   for (int k = 0; k < 3; ++k) c[3 + k] = a3[k];
   M3<double> Q = rodrigues(a3);
   for (int k = 0; k < 9; ++k) b.Qn[(int64_t)i * 9 + k] = Q[k];
-  if (b.params[s].dynamic)
+  // the converged velocities of a Dynamic step, also of its last step when
+  // the next solution step's parameters are already in place
+  if (b.state[s].commit_dyn)
     for (int k = 0; k < 6; ++k) {
       b.copy_vel[(int64_t)i * 6 + k] = b.vel[(int64_t)i * 6 + k];
       b.copy_accel[(int64_t)i * 6 + k] = b.accel[(int64_t)i * 6 + k];

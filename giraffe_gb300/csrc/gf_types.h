@@ -153,15 +153,13 @@ struct StructState {
   int convergence_counter, converged_number, n_conv_evaluated, total_it, bisections;
   int commit;  // set by control for the commit kernel
   int n_solves;  // linear solves performed
-  int solve_sweeps;  // refinement sweeps of the last solve (mixed path)
-  int fp64_fallback;  // mixed path: this structure factors in FP64
   int ray_init;       // Rayleigh matrices formed (after the step's first iteration)
   int step;           // current solution step of the structure
   int zero_va;        // zero the nodal velocities / accelerations before the next time step
   int conv_in_step;   // steps converged in the current solution step (the monitor's sample count)
   int mon_rows;       // monitor lines recorded so far
   int mon_now;        // this pass committed a step that the monitor records
-  int pad_mon;
+  int commit_dyn;     // the committed step's solution step was Dynamic (its velocities are saved)
   int host_step;      // the caller's step control set last_converged_time and
                       // current_time_step (gf_begin_step): step_begin keeps them
   int pad_st;
@@ -366,7 +364,6 @@ struct Batch {
   double* nodeK;
   int full_band;
   int mixed;  // 1: Beam_1 tangent operator in FP32-pair arithmetic
-  int max_refine;
   int* running;  // structures still running after the last pass
   // Rayleigh damping matrix per element (18x18, structure-of-arrays: entry
   // x of element e at [x * n_elem + e]); allocated when any_rayleigh

@@ -36,14 +36,14 @@ GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
 
 
 class gf_solve_opts(C.Structure):
-    _fields_ = [("precision", C.c_int), ("max_refine", C.c_int), ("poll_every", C.c_int),
+    _fields_ = [("precision", C.c_int), ("poll_every", C.c_int),
                 ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int),
                 ("monitor_rows", C.c_int)]
 
 
 class gf_stats(C.Structure):
     _fields_ = [("converged_steps", C.c_int), ("newton_iterations", C.c_int), ("bisections", C.c_int),
-                ("aborted", C.c_int), ("linear_solves", C.c_int), ("fp64_fallback", C.c_int),
+                ("aborted", C.c_int), ("linear_solves", C.c_int),
                 ("pad", C.c_int * 2)]
 
 
@@ -182,14 +182,12 @@ class Context:
         if rc != 0:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
-    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, max_refine=None, wide_update=None,
+    def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, wide_update=None,
              max_passes=0, monitor_rows=0):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
         o.precision, o.use_graph, o.poll_every, o.max_passes = precision, int(use_graph), poll_every, max_passes
         o.monitor_rows = monitor_rows
-        if max_refine is not None:
-            o.max_refine = max_refine
         if wide_update is not None:
             o.wide_update = wide_update
         return o

@@ -68,7 +68,6 @@ enum { GF_PREC_FP64 = 0, GF_PREC_MIXED = 1 };
 
 typedef struct gf_solve_opts {
   int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED */
-  int max_refine;  /* mixed: FP64 refinement sweeps before falling back to FP64 */
   int poll_every;  /* Newton passes between host checks for completion */
   int use_graph;   /* capture one Newton pass as a CUDA graph */
   int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
@@ -98,7 +97,6 @@ typedef struct gf_stats {
   int bisections;         /* rolled-back steps */
   int aborted;            /* 1 when the step size fell below MinTimeStep */
   int linear_solves;      /* linear solves performed */
-  int fp64_fallback;      /* mixed precision: structure switched to FP64 */
   int pad[2];
 } gf_stats;
 
