@@ -352,11 +352,11 @@ def shell_leg(ctx, args, fp64_peak):
     s1 = configs.square_plate(args.shell_n, steps=20)
     s1.solution.end_time = 1.0 / 20.0
     bp = gpu.BatchSolver(ctx, [s1])
-    kms, kl = (C.c_double * 17)(), (C.c_longlong * 17)()
+    kms, kl = (C.c_double * gpu.GF_N_KERNELS)(), (C.c_longlong * gpu.GF_N_KERNELS)()
     ctx.check(L.gf_batch_profile(bp.h, kms, kl), "gf_batch_profile")
     passes = max(1, int(bp.results()[1][0][1]))
     bp.close()
-    split = {L.gf_kernel_name(i).decode(): round(kms[i] / passes, 3) for i in range(17) if kl[i]}
+    split = {L.gf_kernel_name(i).decode(): round(kms[i] / passes, 3) for i in range(gpu.GF_N_KERNELS) if kl[i]}
     # the sparsesystem drop-in on the same plate: the first pass's K_AA as a
     # host CSR, solved through gf_sparse_solve (ordering, upload, wide-band
     # LU, solution back to the host)
@@ -375,6 +375,38 @@ def shell_leg(ctx, args, fp64_peak):
               "info": int(info), "lu_tflops_end_to_end": 2.0 * n_sp * kl_sp * kl_sp / t_sp / 1e12,
               "note": "host CSR in, x out; includes the RCM trial, CSR upload, scatter, factor and "
                       "substitutions (2 n kl^2 flops counted)"}
+    # spec precision pattern: FP32 band factor with FP64 iterative
+    # refinement (GF_PREC_MIXED), the same plate and load steps
+    sm_ = configs.square_plate(args.shell_n, steps=20)
+    sm_.solution.end_time = args.shell_steps / 20.0
+    bm = gpu.BatchSolver(ctx, [sm_], ctx.opts(gpu.GF_PREC_MIXED))
+    bm.reset()
+    ms_mx = bm.run()
+    fin_mx, st_mx = bm.results()
+    ex_mx = bm.solve_stats()[0]
+    launches_mx = bm.launches()
+    bm.close()
+    s1m = configs.square_plate(args.shell_n, steps=20)
+    s1m.solution.end_time = 1.0 / 20.0
+    bpm = gpu.BatchSolver(ctx, [s1m], ctx.opts(gpu.GF_PREC_MIXED))
+    ctx.check(L.gf_batch_profile(bpm.h, kms, kl), "gf_batch_profile")
+    passes_m = max(1, int(bpm.results()[1][0][1]))
+    bpm.close()
+    split_mx = {L.gf_kernel_name(i).decode(): round(kms[i] / passes_m, 3) for i in range(gpu.GF_N_KERNELS) if kl[i]}
+    u64 = fin[0][:, :3] - s.nodes
+    mixed = {"precision": "FP32 wide-band LU (FP32 FMA panel kernels and trailing update) beside the FP64 K_AA; "
+                          "FP64 residual b - K x and x += K32^-1 r until a correction is below 2^-52 |x| or "
+                          "shrinks by less than half; FP64 refactor when refinement stalls above 2^-30 |x| or "
+                          "exceeds 30 sweeps",
+             "ms": ms_mx, "ms_per_pass": ms_mx / max(1, st_mx[0][1]),
+             "solves_per_s": st_mx[0][0] / (ms_mx / 1e3),
+             "speedup_vs_fp64_per_pass": (ms / max(1, st[0][1])) / (ms_mx / max(1, st_mx[0][1])),
+             "linear_solves": int(ex_mx[0]), "refine_sweeps": int(ex_mx[1]),
+             "sweeps_per_solve": float(ex_mx[1]) / max(1, int(ex_mx[0])), "fp64_fallbacks": int(ex_mx[2]),
+             "same_step_and_iteration_counts_as_fp64": bool(tuple(st_mx[0]) == tuple(st[0])),
+             "max_rel_err_displacement_vs_fp64":
+                 float(np.abs(fin_mx[0][:, :3] - fin[0][:, :3]).max() / max(np.abs(u64).max(), 1e-300)),
+             "gpu_launches": launches_mx, "pass_split_ms_first_step": split_mx}
     small = configs.square_plate(8, steps=20)
     bs = gpu.BatchSolver(ctx, [small])
     bs.reset()
@@ -404,6 +436,7 @@ def shell_leg(ctx, args, fp64_peak):
             "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
             "pass_split_ms": split,
             "sparse_solve": sparse,
+            "mixed_precision": mixed,
             "plate8": {"workload": "Shell_1 plate 8x8x2 (1,203 free DOFs), all 20 load steps",
                         "gpu_solves_per_s": st_small[0] / (ms_small / 1e3), "gpu_ms": ms_small,
                         "cpu_oracle_solves_per_s": so[0] / cpu_s, "cpu_cores": 1,
@@ -607,10 +640,10 @@ def run_ours(args, rank, world):
     # per-kernel device times (one profiled solve, events around every launch)
     L.gf_batch_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.gf_kernel_name.restype = C.c_char_p
-    kms = (C.c_double * 17)()
-    kl = (C.c_longlong * 17)()
+    kms = (C.c_double * gpu.GF_N_KERNELS)()
+    kl = (C.c_longlong * gpu.GF_N_KERNELS)()
     ctx.check(L.gf_batch_profile(b.h, kms, kl), "gf_batch_profile")
-    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(17) if kl[i]}
+    kernels = {L.gf_kernel_name(i).decode(): {"ms": kms[i], "launches": kl[i]} for i in range(gpu.GF_N_KERNELS) if kl[i]}
     L.gf_batch_work.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
     lu_f, asm_b, mnt_f = C.c_double(), C.c_double(), C.c_double()
     ctx.check(L.gf_batch_work(b.h, C.byref(lu_f), C.byref(asm_b), C.byref(mnt_f)), "gf_batch_work")

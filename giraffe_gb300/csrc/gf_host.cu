@@ -1079,6 +1079,14 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
     if (!upload(B, &sd.wide_structs, wide_structs) || !balloc(B, &sd.wband, (size_t)wb_total) ||
         !balloc(B, &sd.panel, 1))
       return GF_ERR_CUDA;
+    if (B->opts.precision == GF_PREC_MIXED) {
+      // the FP32 LU beside the FP64 K_AA, its right-hand side and scratch,
+      // the saved Newton right-hand side and the refinement state
+      if (!balloc(B, &sd.wband32, (size_t)wb_total) || !balloc(B, &sd.r32, (size_t)dof_off) ||
+          !balloc(B, &sd.y32, (size_t)dof_off) || !balloc(B, &sd.ir_rhs, (size_t)dof_off) ||
+          !zeroed(B, &sd.ir, wide_structs.size()) || !zeroed(B, &sd.ir_more, 4))
+        return GF_ERR_CUDA;
+    }
     if (B->opts.wide_update == GF_WIDE_TENSOR || B->opts.wide_update == GF_WIDE_TENSOR_SYNC) {
       // slices of one panel per wide structure for the tensor-core update
       sd.oz_rows = (max_wkl + 127) / 128 * 128;  // whole 128-row tiles of the tensor-core update
@@ -1141,6 +1149,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   CK(cudaMemsetAsync(b.P, 0, sizeof(double) * (size_t)std::max(dof_off, 1), B->stream));
   CK(cudaMemsetAsync(b.nodeK, 0, sizeof(double) * (size_t)std::max(node_off, 1) * 9, B->stream));
   b.mixed = B->opts.precision == GF_PREC_MIXED;
+  b.sh.ir_max = B->opts.max_refine > 0 ? B->opts.max_refine : GF_IR_MAX;
   b.sh.wide_tc = b.sh.oz_slices != nullptr ? B->opts.wide_update : GF_WIDE_FP64;
   return GF_OK;
 }
@@ -1291,8 +1300,15 @@ int ensure_graph(gf_batch* B) {
     const double t0 = host_now_ms();
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    wide_capture_error();  // clear
     launch_iteration(B->b, st);
+    const cudaError_t ce = wide_capture_error();
     CK(cudaStreamEndCapture(st, &g));
+    if (ce != cudaSuccess) {
+      cudaGraphDestroy(g);
+      set_err(ctx, "capture of the wide-band loops failed: %s", cudaGetErrorString(ce));
+      return GF_ERR_CUDA;
+    }
     CK(cudaGraphInstantiate(&B->graph, g, 0));
     CK(cudaGraphDestroy(g));
     B->host_ms[3] = host_now_ms() - t0;
@@ -1331,6 +1347,19 @@ int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
 }
 }  // namespace gfh
 
+// Launches of the mixed path's refinement sweeps and FP64 fallbacks since
+// the last call, from the device counters (the stream is idle here).
+static long long refine_launches(gf_batch* B) {
+  const int* cnt = B->b.sh.ir_more;
+  if (!cnt) return 0;
+  int c[4];
+  if (cudaMemcpy(c, cnt, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  const long long n = gf::wide_refine_launches(B->b, c[2] - B->ir_seen[0], c[3] - B->ir_seen[1]);
+  B->ir_seen[0] = c[2];
+  B->ir_seen[1] = c[3];
+  return n;
+}
+
 extern "C" {
 
 int gf_batch_run(gf_batch* B) {
@@ -1349,7 +1378,7 @@ int gf_batch_run(gf_batch* B) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
   B->last_ms = ms;
-  B->last_launches = passes * B->launches_per_pass;
+  B->last_launches = passes * B->launches_per_pass + refine_launches(B);
   return GF_OK;
 }
 
@@ -1501,9 +1530,11 @@ int gf_batch_solve_timed(gf_batch* B, int steps, double* ms_out) {
   CK(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
   *ms_out = ms;
   B->last_ms = ms / steps;
-  B->last_launches = launches;
+  B->last_launches = launches + refine_launches(B);
   return GF_OK;
 }
+
+static_assert(GF_N_KERNELS == KC_COUNT, "the ABI's kernel class count");
 
 int gf_batch_profile(gf_batch* B, double* ms_out, long long* launches_out) {
   if (!B) return GF_ERR_ARG;
@@ -1619,6 +1650,8 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       z.bisections = st[s].bisections;
       z.aborted = st[s].phase == PH_ABORTED || st[s].aborted;
       z.linear_solves = st[s].n_solves;
+      z.refine_sweeps = st[s].ir_sweeps;
+      z.fp64_fallbacks = st[s].ir_fallbacks;
       stats[s] = z;
     }
   if (final_nodes) {

@@ -142,6 +142,7 @@ struct gf_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   long long last_launches = 0;
+  int ir_seen[2] = {0, 0};  // refinement sweeps and FP64 fallbacks counted so far (mixed path)
   int launches_per_pass = 0;
   int* h_running = nullptr;  // pinned
   long long h2d_bytes = 0;

@@ -1374,7 +1374,8 @@ static void set_attrs() {
 const char* kernel_class_name(int k) {
   static const char* names[KC_COUNT] = {"step_begin", "zero", "beam_tangent", "loads", "residual", "band_solve",
                                         "update", "control", "commit_elems", "commit_nodes", "chain_solve", "scatter",
-                                        "shell_mount", "wide_diag", "wide_trsm", "wide_update", "wide_subst"};
+                                        "shell_mount", "wide_diag", "wide_trsm", "wide_update", "wide_subst",
+                                        "wide_refine"};
   return k >= 0 && k < KC_COUNT ? names[k] : "?";
 }
 

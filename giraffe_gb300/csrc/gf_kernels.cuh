@@ -38,7 +38,7 @@ struct LaunchProf {
 enum KernelClass {
   KC_STEP_BEGIN = 0, KC_ZERO, KC_MOUNT, KC_LOADS, KC_RESIDUAL, KC_SOLVE, KC_UPDATE, KC_CONTROL,
   KC_COMMIT_ELEMS, KC_COMMIT_NODES, KC_CHAIN, KC_SCATTER, KC_SHELL, KC_WIDE_DIAG, KC_WIDE_TRSM, KC_WIDE_UPDATE,
-  KC_WIDE_SUBST, KC_COUNT
+  KC_WIDE_SUBST, KC_WIDE_REFINE, KC_COUNT
 };
 const char* kernel_class_name(int k);
 
@@ -107,6 +107,9 @@ void launch_shell_mount(const Batch& b, cudaStream_t st);
 void launch_wide_zero(const Batch& b, cudaStream_t st);
 void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof = nullptr);
 void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st);
+// The first error of a wide-band capture step (a conditional node or body
+// capture) since the last call on this thread; clears it.
+cudaError_t wide_capture_error();
 // The modal mass (MountMassModal) of every element added into a band of the
 // structure's layout: entry (i, j) at (kw + i - j) + j W.
 void launch_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st);
@@ -123,6 +126,8 @@ void launch_shell_inertia_elements(int n, const ShellConst* c, const ShellHistAu
                                    cudaStream_t st);
 // Kernel launches of one pass of the shell and wide-band kernels.
 int shell_launches_per_pass(const Batch& b);
+int wide_launches_per_pass(const Batch& b);
+long long wide_refine_launches(const Batch& b, long long sweeps, long long fallbacks);
 
 // Band factor + solve of independent systems in the batch layout
 // (GF_LDB rows); FP64.  Returns per-system info in state[].info_fail.

@@ -165,6 +165,8 @@ void report(gf_server* S, Wave& w, int s, const StructState* st, int status) {
     res.stats.bisections = st->bisections;
     res.stats.aborted = st->phase == PH_ABORTED || st->aborted;
     res.stats.linear_solves = st->n_solves;
+    res.stats.refine_sweeps = st->ir_sweeps;
+    res.stats.fp64_fallbacks = st->ir_fallbacks;
   }
   double t = now_ms();
   res.queued_ms = r.t_admit - r.t_submit;

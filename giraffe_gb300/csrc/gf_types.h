@@ -24,7 +24,7 @@
 #define GF_KB 17
 #define GF_LDB (2 * GF_KB + 1)
 #define GF_UW (GF_KB + 1)
-#define GF_WB_STREAMS 4  // helper streams of the wide-band lookahead
+#define GF_WB_STREAMS 5  // helper streams of the wide-band lookahead
 #define GF_WB_EVENTS 6
 
 namespace gf {
@@ -85,6 +85,7 @@ struct ShellHistAux {
 
 // Wide-band LU panel width (columns per panel).
 #define GF_WB_NB 64
+#define GF_IR_MAX 30  // default FP64 refinement sweeps of the FP32 wide-band factor before the FP64 fallback
 
 enum Phase : int { PH_START = 0, PH_ITER = 1, PH_DONE = 2, PH_ABORTED = 3 };
 
@@ -162,7 +163,9 @@ struct StructState {
   int commit_dyn;     // the committed step's solution step was Dynamic (its velocities are saved)
   int host_step;      // the caller's step control set last_converged_time and
                       // current_time_step (gf_begin_step): step_begin keeps them
-  int pad_st;
+  int ir_sweeps;      // FP64 refinement sweeps of the FP32 wide-band factor (all solves)
+  int ir_fallbacks;   // solves that refinement did not finish: refactored in FP64
+  int ir_fb;          // this solve takes the FP64 fallback
   double time, time_step, last_converged_time, current_time_step;
   double force_crit, moment_crit, disp_crit, rot_crit;
   double last_res, last_inc;
@@ -236,6 +239,15 @@ struct ChainData {
 };
 
 // Shell_1 elements and the wide-band storage of their structures.
+// Refinement state of one wide structure slot (mixed precision): the
+// largest |correction| and |x| of the current sweep (FP64 bits, raised by
+// atomicMax), the previous sweep's |correction|, sweeps of this solve.
+struct WideIr {
+  unsigned long long dn, xn;
+  double dprev;
+  int k, done;
+};
+
 struct ShellData {
   int n_shells;
   int n_wide;       // structures solved by the wide-band LU
@@ -260,6 +272,21 @@ struct ShellData {
   int color_off[17];
   int n_colors;
   double* wband;
+  // mixed precision (GF_PREC_MIXED): K_AA stays in wband (FP64) for the
+  // residuals; its LU is formed in wband32 (FP32, same geometry) and the
+  // solution refined in FP64: r32 / y32 the FP32 right-hand side and the
+  // forward-substitution scratch, ir_rhs the Newton right-hand side, ir the
+  // per-slot refinement state.  fp64_pass is set on the host's copy of the
+  // batch for the FP64 fallback launches (only structures with ir_fb run).
+  float* wband32;
+  float* r32;
+  float* y32;
+  double* ir_rhs;
+  struct WideIr* ir;
+  int* ir_more;      // [0] a slot still refines, [1] a slot needs the FP64 fallback,
+                     // [2] sweeps run, [3] fallbacks run (both cumulative)
+  int fp64_pass;
+  int ir_max;        // refinement sweeps before the FP64 fallback
   int* panel;       // device panel counter of the captured panel loops
   int loops_in_graph;  // capture the panel loops as graph WHILE loops (served waves)
   int wide_tc;         // trailing update: 0 FP64 FMA, 1 tcgen05 Ozaki slices, 2 mma.sync Ozaki slices
@@ -282,7 +309,8 @@ struct ShellData {
   // host handles of the wide-band lookahead: helper streams and the events
   // that fork from and join into the pass's stream; aux[2] roots the
   // captured panel-loop bodies, aux[3] runs the bulk trsm beside the first
-  // blocks and the corner update
+  // blocks and the corner update, aux[4] roots the captured bodies of the
+  // refinement loop and of the FP64 fallback
   cudaStream_t aux[GF_WB_STREAMS];
   // [0] panel start, [1] after trsm, [2] after the corner update, [3] after
   // diag, [4] end of forward, [5] after the bulk trsm

@@ -15,6 +15,7 @@ from .model import Structure, gf_model_desc
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgiraffe_gpu.so")
 
 GF_PREC_FP64, GF_PREC_MIXED = 0, 1
+GF_N_KERNELS = 18  # kernel classes of gf_batch_profile
 GF_WIDE_FP64, GF_WIDE_TENSOR, GF_WIDE_TENSOR_SYNC = 0, 1, 2
 
 EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_batch_create",
@@ -38,13 +39,13 @@ GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
 class gf_solve_opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("poll_every", C.c_int),
                 ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int),
-                ("monitor_rows", C.c_int)]
+                ("monitor_rows", C.c_int), ("max_refine", C.c_int)]
 
 
 class gf_stats(C.Structure):
     _fields_ = [("converged_steps", C.c_int), ("newton_iterations", C.c_int), ("bisections", C.c_int),
                 ("aborted", C.c_int), ("linear_solves", C.c_int),
-                ("pad", C.c_int * 2)]
+                ("refine_sweeps", C.c_int), ("fp64_fallbacks", C.c_int)]
 
 
 class gf_server_opts(C.Structure):
@@ -183,11 +184,11 @@ class Context:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
     def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, wide_update=None,
-             max_passes=0, monitor_rows=0):
+             max_passes=0, monitor_rows=0, max_refine=0):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
         o.precision, o.use_graph, o.poll_every, o.max_passes = precision, int(use_graph), poll_every, max_passes
-        o.monitor_rows = monitor_rows
+        o.monitor_rows, o.max_refine = monitor_rows, max_refine
         if wide_update is not None:
             o.wide_update = wide_update
         return o
@@ -480,7 +481,15 @@ class BatchSolver:
         stats = (gf_stats * len(outs))()
         self.ctx.check(self.ctx.L.gf_batch_results(self.h, ptrs, stats), "gf_batch_results")
         st = np.array([[x.converged_steps, x.newton_iterations, x.bisections, x.aborted] for x in stats])
+        self.last_stats = stats
         return outs, st
+
+    def solve_stats(self):
+        """Per structure, after results(): linear solves, FP64 refinement
+        sweeps of the FP32 wide-band factor and solves refactored in FP64
+        (GF_PREC_MIXED), as rows [linear_solves, refine_sweeps,
+        fp64_fallbacks]."""
+        return np.array([[x.linear_solves, x.refine_sweeps, x.fp64_fallbacks] for x in self.last_stats])
 
     def monitor(self, s: int):
         """Structure s's monitor lines (gf_batch_monitor): [node][line][31]

@@ -67,7 +67,15 @@ enum {
 enum { GF_PREC_FP64 = 0, GF_PREC_MIXED = 1 };
 
 typedef struct gf_solve_opts {
-  int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED */
+  int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED: Beam_1 tangent
+                      operators in FP32-pair arithmetic, and Shell_1 wide-band
+                      K_AA factored in FP32 (its LU beside the FP64 K_AA) with
+                      FP64 iterative refinement (x += K32^-1 (b - K x)) until
+                      a correction is below 2^-52 |x| or shrinks by less than
+                      half; a solve that stalls above 2^-30 |x|, or is still
+                      refining after max_refine sweeps, is refactored in FP64
+                      (reference: src/SparseMatrix.cpp:74-166, PARDISO with
+                      iterative refinement) */
   int poll_every;  /* Newton passes between host checks for completion */
   int use_graph;   /* capture one Newton pass as a CUDA graph */
   int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
@@ -87,6 +95,8 @@ typedef struct gf_solve_opts {
                       default of 4,000,000) */
   int monitor_rows; /* monitor lines kept per structure with a Monitor
                       (gf_model_desc monitor_nodes; 0: none recorded) */
+  int max_refine;  /* GF_PREC_MIXED: FP64 refinement sweeps of a wide-band
+                      solve before its FP64 fallback (0: the default of 30) */
 } gf_solve_opts;
 enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1, GF_WIDE_TENSOR_SYNC = 2 };
 
@@ -97,7 +107,8 @@ typedef struct gf_stats {
   int bisections;         /* rolled-back steps */
   int aborted;            /* 1 when the step size fell below MinTimeStep */
   int linear_solves;      /* linear solves performed */
-  int pad[2];
+  int refine_sweeps;      /* GF_PREC_MIXED: FP64 refinement sweeps of the FP32 wide-band factor */
+  int fp64_fallbacks;     /* GF_PREC_MIXED: wide-band solves refactored in FP64 */
 } gf_stats;
 
 /* Context on CUDA device `device`; NULL on failure. */
@@ -170,7 +181,7 @@ int gf_batch_solve_timed(gf_batch* batch, int steps, double* ms);
  * kernel; per kernel class k (0 <= k < GF_N_KERNELS, names from
  * gf_kernel_name) *ms_out[k] receives the summed device time and
  * launches_out[k] the launch count. */
-enum { GF_N_KERNELS = 17 };
+enum { GF_N_KERNELS = 18 };
 int gf_batch_profile(gf_batch* batch, double* ms_out, long long* launches_out);
 const char* gf_kernel_name(int k);
 /* Bytes the batch moved host->device when it was created, and bytes
