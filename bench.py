@@ -344,6 +344,7 @@ def shell_leg(ctx, args, fp64_peak):
     dims = (C.c_int * 2)()
     L.gf_batch_assemble(b.h, 0, None, None, dims)
     launches = b.launches()
+    tiles = b.wide_tiles()
     # per-kernel-class device time of a pass over the first load step (events
     # around every launch, no graph; classes on the lookahead's helper
     # streams overlap the main stream, so the classes sum to more than a pass)
@@ -431,9 +432,16 @@ def shell_leg(ctx, args, fp64_peak):
                                 "fp64_fma_update_ms_per_pass": ms_fp64 / max(1, st_fp64[0][1]),
                                 "mma_sync_update_ms_per_pass": ms_sync / max(1, st_sync[0][1]),
                                 "same_counts": bool(tuple(st_fp64[0]) == tuple(st_tc2[0]) == tuple(st_sync[0])),
+                                "counts_steps_iterations_bisections":
+                                    {"tcgen05": [int(v) for v in st_tc2[0][:3]],
+                                     "fp64_fma": [int(v) for v in st_fp64[0][:3]],
+                                     "mma_sync": [int(v) for v in st_sync[0][:3]]},
                                 "max_abs_diff_m_sync_vs_tcgen05":
                                     float(np.abs(f_sync[0][:, :3] - f_tc2[0][:, :3]).max())},
             "gpu_launches": launches, "center_deflection_m": float(fin[0][:, 2].min()),
+            "wide_tiles": {"trsm_rows": tiles[0], "first_trsm_rows": tiles[1], "corner_tile": tiles[2],
+                           "solve_rows": tiles[3], "how": "picked by the library's autotuner (timed on a "
+                                                         "synthetic band of the plate's half-bandwidth)"},
             "pass_split_ms": split,
             "sparse_solve": sparse,
             "mixed_precision": mixed,

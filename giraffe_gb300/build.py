@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgiraffe_gpu.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["gf_kernels.cu", "gf_chain.cu", "gf_shell.cu", "gf_wideband.cu", "gf_host.cu", "gf_server.cu", "gf_sparse.cu", "gf_iter.cu", "gf_modal.cu"]
+SOURCES = ["gf_kernels.cu", "gf_chain.cu", "gf_shell.cu", "gf_wideband.cu", "gf_host.cu", "gf_server.cu", "gf_sparse.cu", "gf_iter.cu", "gf_modal.cu", "gf_tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -610,6 +610,14 @@ template <typename T> bool zeroed(gf_batch* B, T** p, size_t n) {
 int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   gf_ctx* ctx = B->ctx;
   Batch& b = B->b;
+  {
+    const int* wt = B->opts.wide_tiles;
+    if ((wt[0] && wt[0] != 4 && wt[0] != 8 && wt[0] != 16) || (wt[1] && wt[1] != 1 && wt[1] != 2 && wt[1] != 4) ||
+        (wt[2] && wt[2] != 4 && wt[2] != 8) || (wt[3] && wt[3] != 32 && wt[3] != 64)) {
+      set_err(ctx, "wide_tiles: bulk trsm rows 4/8/16, first trsm rows 1/2/4, corner tile 4/8, solve rows 32/64");
+      return GF_ERR_ARG;
+    }
+  }
   // ---- numbering pass (parallel over structures) ----
   std::vector<StructPlan> plan(n);
   size_t work = 0;
@@ -1151,6 +1159,19 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
   b.mixed = B->opts.precision == GF_PREC_MIXED;
   b.sh.ir_max = B->opts.max_refine > 0 ? B->opts.max_refine : GF_IR_MAX;
   b.sh.wide_tc = b.sh.oz_slices != nullptr ? B->opts.wide_update : GF_WIDE_FP64;
+  if (b.sh.n_wide) {
+    // tile shapes: the caller's entries, the others from the autotuner
+    // (served waves, whose device memory comes from the server's budget,
+    // take the defaults rather than time a synthetic band beside it)
+    const int* wt = B->opts.wide_tiles;
+    WideTiles t;
+    if (!(wt[0] && wt[1] && wt[2] && wt[3]) && !B->arena) t = tune_wide_tiles(B->ctx, b.sh.max_kl, b.sh.wide_tc);
+    if (wt[0]) t.trsm_rb = wt[0];
+    if (wt[1]) t.trsm_first = wt[1];
+    if (wt[2]) t.corner = wt[2];
+    if (wt[3]) t.sub_rows = wt[3];
+    b.sh.tiles = t;
+  }
   return GF_OK;
 }
 
@@ -1236,6 +1257,8 @@ void gf_default_opts(gf_solve_opts* o) {
   o->wide_update = GF_WIDE_TENSOR;
   o->max_passes = 0;
   o->monitor_rows = 0;
+  o->max_refine = 0;
+  for (int& t : o->wide_tiles) t = 0;
 }
 
 gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts) {
@@ -1671,6 +1694,17 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
     });
   }
   B->host_ms[4] = host_now_ms() - t0;
+  return GF_OK;
+}
+
+int gf_batch_wide_tiles(const gf_batch* B, int* tiles) {
+  if (!B || !tiles) return GF_ERR_ARG;
+  const WideTiles& t = B->b.sh.tiles;
+  const bool w = B->b.sh.n_wide > 0;
+  tiles[0] = w ? t.trsm_rb : 0;
+  tiles[1] = w ? t.trsm_first : 0;
+  tiles[2] = w ? t.corner : 0;
+  tiles[3] = w ? t.sub_rows : 0;
   return GF_OK;
 }
 

@@ -21,6 +21,8 @@ struct gf_ctx {
   // options of the standalone solves (gf_band_solve, gf_sparse_solve):
   // wide_update picks their wide-band trailing update
   int wide_update = GF_WIDE_TENSOR;
+  // the autotuner's wide-band tile shapes, per half-bandwidth and update kind
+  std::map<long long, gf::WideTiles> tiles;
 };
 
 // First-fit sub-allocator over one allocation (the served path's device
@@ -184,6 +186,10 @@ int batch_reset(gf_batch* B);
 int ensure_graph(gf_batch* B);
 // Kernel launches of one Newton pass.
 int count_launches_per_pass(const gf_batch* B);
+// The wide-band LU's tile shapes for half-bandwidth kl and trailing-update
+// kind wide_update, timed on a synthetic band once per context (gf_tune.cu);
+// the defaults when tuning cannot run.
+gf::WideTiles tune_wide_tiles(gf_ctx* ctx, int kl, int wide_update);
 // Host wall clock in milliseconds.
 double host_now_ms();
 // Reverse Cuthill-McKee order of a graph given by adjacency lists

@@ -239,6 +239,19 @@ struct ChainData {
 };
 
 // Shell_1 elements and the wide-band storage of their structures.
+// Tile shapes of the wide-band LU that leave every entry's arithmetic as it
+// is (so any choice gives the same bits): rows per CTA of the bulk trsm (4,
+// 8 or 16) and of the first trsm on the critical path (1, 2 or 4), the
+// output tile edge of the corner update (4 or 8), rows per CTA of the
+// triangular solves (32 or 64).  Picked by timing (the autotuner) or pinned
+// by the caller.
+struct WideTiles {
+  int trsm_rb = 8;
+  int trsm_first = 2;
+  int corner = 8;
+  int sub_rows = 64;
+};
+
 // Refinement state of one wide structure slot (mixed precision): the
 // largest |correction| and |x| of the current sweep (FP64 bits, raised by
 // atomicMax), the previous sweep's |correction|, sweeps of this solve.
@@ -283,6 +296,7 @@ struct ShellData {
   float* y32;
   double* ir_rhs;
   struct WideIr* ir;
+  WideTiles tiles;   // tile shapes of this batch's wide-band LU
   int* ir_more;      // [0] a slot still refines, [1] a slot needs the FP64 fallback,
                      // [2] sweeps run, [3] fallbacks run (both cumulative)
   int fp64_pass;

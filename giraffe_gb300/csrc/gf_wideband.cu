@@ -223,8 +223,6 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_wb_diag(Batch b, int p) {
 // critical path) are a launch of their own with two rows per CTA, spread
 // over 64 SMs; the bulk runs beside it with eight.  Each CTA loads the half
 // of the diagonal block its side reads (U11 for L21, L11 for U12).
-constexpr int TRSM_RB = 8;
-constexpr int TRSM_RB_FIRST = 2;
 template <typename F, int RB>
 __global__ void __launch_bounds__(32 * RB) k_wb_trsm(Batch b, int p, int row0, int nblk) {
   p = wb_panel(b, p);
@@ -248,7 +246,8 @@ __global__ void __launch_bounds__(32 * RB) k_wb_trsm(Batch b, int p, int row0, i
     int i = x % NB, j = x / NB;
     T[i][j] = ((lower ? i <= j : i > j) && i < nb && j < nb && abs(i - j) <= w.kl) ? w.at(j0 + i, j0 + j) : F(0);
   }
-  if (lower && tid < nb) rd[tid] = wb_rcp(w.at(j0 + tid, j0 + tid));
+  if (lower)
+    for (int k = tid; k < nb; k += blockDim.x) rd[k] = wb_rcp(w.at(j0 + k, j0 + k));
   const int r = tid >> 5, c = tid & 31;  // row (or column) r of the block, lane c
   const int g = j0 + nb + rowb + r;      // global row (lower) or column (upper)
   const bool live = g < j0 + nb + m;
@@ -295,11 +294,11 @@ __global__ void __launch_bounds__(32 * RB) k_wb_trsm(Batch b, int p, int row0, i
     if (lower) w.at(g, j0 + k) = X[r][k];
     else w.at(j0 + k, g) = X[r][k];
   }
-  if (sizeof(F) == 8 && b.sh.wide_tc && tid < nb) {
+  if (sizeof(F) == 8 && b.sh.wide_tc)
+  for (int k = tid; k < nb; k += blockDim.x) {
     // largest magnitude of column k of this block's L21 rows (row k of its
     // U12 columns), as FP64 bits, which order like the magnitudes; the
     // maximum over the CTAs is exact and independent of their order
-    const int k = tid;
     unsigned long long mx = 0;
     for (int q = 0; q < RB; ++q) {
       const int gq = j0 + nb + rowb + q;
@@ -363,14 +362,13 @@ __global__ void __launch_bounds__(256) k_wb_update(Batch b, int p, int part) {
 
 // The corner of panel p's trailing update: the next panel's diagonal block
 // (the first NB rows and columns of the window), on the lookahead's critical
-// path.  8 x 8 output tiles over 64 CTAs; in a CTA four warps each sum a
-// quarter of k (16 terms) for all 64 outputs of the tile, and the quarters
-// are added in a fixed order: an FP64 warp instruction holds its
+// path.  CT x CT output tiles (8 x 8 by default: 64 CTAs); in a CTA four
+// thread groups each sum a quarter of k (16 terms) for every output of the
+// tile, and the quarters are added in a fixed order: an FP64 warp instruction holds its
 // sub-partition's FP64 unit for about 64 cycles, so four warps on four
 // sub-partitions finish the 64 terms four times sooner than one.
-constexpr int CT8 = 8;
-constexpr int CORNER_THREADS = 256;
-__global__ void __launch_bounds__(CORNER_THREADS) k_wb_corner(Batch b, int p) {
+template <int CT>
+__global__ void __launch_bounds__(4 * CT * CT) k_wb_corner(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.z];
@@ -380,25 +378,25 @@ __global__ void __launch_bounds__(CORNER_THREADS) k_wb_corner(Batch b, int p) {
   WB w = wb_of(b, inf);
   const int j0 = p * NB, nb = min(NB, w.n - j0);
   const int m = min(min(w.kl, w.n - j0 - nb), NB);
-  const int r0 = blockIdx.x * CT8, c0 = blockIdx.y * CT8;
+  const int r0 = blockIdx.x * CT, c0 = blockIdx.y * CT;
   if (r0 >= m || c0 >= m) return;
-  __shared__ double Ls[NB][CT8 + 1];  // [k][row]
-  __shared__ double Us[NB][CT8 + 1];  // [k][col]
-  __shared__ double part[4][CT8 * CT8];
+  __shared__ double Ls[NB][CT + 1];  // [k][row]
+  __shared__ double Us[NB][CT + 1];  // [k][col]
+  __shared__ double part[4][CT * CT];
   const int tid = threadIdx.x;
   const int base = j0 + nb;
-  for (int x = tid; x < NB * CT8; x += blockDim.x) {
+  for (int x = tid; x < NB * CT; x += blockDim.x) {
     // rows of L21 along a band column are contiguous; U12's k along a
     // band column too
-    const int i = x % CT8, k = x / CT8;
+    const int i = x % CT, k = x / CT;
     const int gk = j0 + k, gi = base + r0 + i;
     Ls[k][i] = (k < nb && r0 + i < m && gi - gk <= w.kl) ? w.at(gi, gk) : 0.0;
     const int kk = x % NB, c = x / NB, gj = base + c0 + c;
     Us[kk][c] = (kk < nb && c0 + c < m && gj - (j0 + kk) <= w.kl) ? w.at(j0 + kk, gj) : 0.0;
   }
   __syncthreads();
-  const int o = tid & 63, q = tid >> 6;  // output, quarter of k
-  const int ty = o / CT8, tx = o % CT8;
+  const int o = tid % (CT * CT), q = tid / (CT * CT);  // output, quarter of k
+  const int ty = o / CT, tx = o % CT;
   double a = 0.0;
 #pragma unroll
   for (int k = 16 * q; k < 16 * q + 16; ++k) a = fma(Ls[k][ty], Us[k][tx], a);
@@ -945,19 +943,18 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_wb_update_t5(Batch b, int p, 
 }
 
 // The triangular solves run one launch per panel, so a launch's latency is
-// the solve's cost: each CTA takes SUB_ROWS rows of the panel's off-diagonal
-// block, its 256 threads four quarters (16 columns) of each row, and every
+// the solve's cost: each CTA takes SR rows of the panel's off-diagonal
+// block (64 by default), its 4 SR threads four quarters (16 columns) of each
+// row, and every
 // thread loads its 16 entries into registers before the small triangle's
 // dependent chain, so those loads hide behind it; the quarters are added in
 // a fixed order.
-constexpr int SUB_ROWS = 64;
-__host__ __device__ constexpr int sub_blocks(int kl) { return kl > 0 ? (kl + SUB_ROWS - 1) / SUB_ROWS : 1; }
 
 // Forward substitution for panel p: y_p = L11^-1 b_p into y; then the rows
 // below the panel: P_i -= L21(i, :) y_p.  Every CTA solves the small
 // triangle redundantly; CTA 0 writes y_p.
-template <typename F>
-__global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
+template <typename F, int SR>
+__global__ void __launch_bounds__(4 * SR) k_wb_fwd(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
@@ -972,9 +969,9 @@ __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
   F* Y = wb_scratch(b, inf, blockIdx.z, (F*)nullptr);
   __shared__ F T[NB][NB + 1];  // the panel's diagonal block (L11 below the diagonal)
   __shared__ F ys[NB];
-  __shared__ F part[4][SUB_ROWS];
-  const int tid = threadIdx.x, r = tid % SUB_ROWS, q = tid / SUB_ROWS;
-  const int row = blockIdx.x * SUB_ROWS + r, gi = j0 + nb + row;  // row below the panel
+  __shared__ F part[4][SR];
+  const int tid = threadIdx.x, r = tid % SR, q = tid / SR;
+  const int row = blockIdx.x * SR + r, gi = j0 + nb + row;  // row below the panel
   F lv[16];
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
@@ -1010,8 +1007,8 @@ __global__ void __launch_bounds__(256) k_wb_fwd(Batch b, int p) {
 
 // Backward substitution for panel p (last panel first): x_p = U11^-1 y_p into
 // P; then the rows above the panel: y_i -= U(i, panel) x_p.
-template <typename F>
-__global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
+template <typename F, int SR>
+__global__ void __launch_bounds__(4 * SR) k_wb_bwd(Batch b, int p) {
   p = wb_panel(b, p);
   if (p < 0) return;
   int s = b.sh.wide_structs[blockIdx.y];
@@ -1026,10 +1023,10 @@ __global__ void __launch_bounds__(256) k_wb_bwd(Batch b, int p) {
   __shared__ F T[NB][NB + 1];  // the panel's diagonal block (U11 on and above the diagonal)
   __shared__ F rdiag[NB];
   __shared__ F xs[NB];
-  __shared__ F part[4][SUB_ROWS];
-  const int tid = threadIdx.x, r = tid % SUB_ROWS, q = tid / SUB_ROWS;
+  __shared__ F part[4][SR];
+  const int tid = threadIdx.x, r = tid % SR, q = tid / SR;
   const int top = max(0, j0 - w.kl);
-  const int gi = top + blockIdx.x * SUB_ROWS + r;  // row above the panel
+  const int gi = top + blockIdx.x * SR + r;  // row above the panel
   F lv[16];
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
@@ -1321,11 +1318,52 @@ void launch_wide_zero(const Batch& b, cudaStream_t st) {
   k_wb_zero<<<dim3(4 * 152, b.sh.n_wide), 256, 0, st>>>(b);
 }
 
-// The trsm of a panel: the first NB rows and columns (the next panel's
-// diagonal block needs them) in CTAs of TRSM_RB_FIRST, the rest in CTAs of
-// TRSM_RB.
-constexpr int TRSM_FIRST = NB / TRSM_RB_FIRST;
-__host__ __device__ constexpr int trsm_rest_blocks(int kl) { return kl > NB ? (kl - NB + TRSM_RB - 1) / TRSM_RB : 0; }
+// Launches at the batch's tile shapes (b.sh.tiles).  The trsm of a panel:
+// the first NB rows and columns (the next panel's diagonal block needs them)
+// in CTAs of tiles.trsm_first rows, the rest in CTAs of tiles.trsm_rb.
+static int trsm_first_blocks(const Batch& b) { return NB / b.sh.tiles.trsm_first; }
+static int trsm_rest_blocks(const Batch& b) {
+  const int kl = b.sh.max_kl, rb = b.sh.tiles.trsm_rb;
+  return kl > NB ? (kl - NB + rb - 1) / rb : 0;
+}
+template <typename F, int RB>
+static void trsm_at(const Batch& b, int p, int row0, int nblk, cudaStream_t st) {
+  k_wb_trsm<F, RB><<<dim3(2 * nblk, b.sh.n_wide), 32 * RB, 0, st>>>(b, p, row0, nblk);
+}
+// rows row0 .. of panel p (and as many columns) in nblk CTAs of rb rows
+template <typename F>
+static void launch_trsm(const Batch& b, int p, int row0, int nblk, int rb, cudaStream_t st) {
+  switch (rb) {
+    case 1: trsm_at<F, 1>(b, p, row0, nblk, st); break;
+    case 2: trsm_at<F, 2>(b, p, row0, nblk, st); break;
+    case 4: trsm_at<F, 4>(b, p, row0, nblk, st); break;
+    case 16: trsm_at<F, 16>(b, p, row0, nblk, st); break;
+    default: trsm_at<F, 8>(b, p, row0, nblk, st); break;
+  }
+}
+template <typename F> static void launch_trsm_first(const Batch& b, int p, cudaStream_t st) {
+  launch_trsm<F>(b, p, 0, trsm_first_blocks(b), b.sh.tiles.trsm_first, st);
+}
+template <typename F> static void launch_trsm_rest(const Batch& b, int p, cudaStream_t st) {
+  launch_trsm<F>(b, p, NB, trsm_rest_blocks(b), b.sh.tiles.trsm_rb, st);
+}
+static void launch_corner(const Batch& b, int p, cudaStream_t st) {
+  const int nw = b.sh.n_wide;
+  if (b.sh.tiles.corner == 4) k_wb_corner<4><<<dim3(NB / 4, NB / 4, nw), 64, 0, st>>>(b, p);
+  else k_wb_corner<8><<<dim3(NB / 8, NB / 8, nw), 256, 0, st>>>(b, p);
+}
+// the triangular solves of panel p: rows of tiles.sub_rows per CTA, nrhs
+// right-hand sides
+template <typename F> static void launch_fwd(const Batch& b, int p, int nrhs, cudaStream_t st) {
+  const int sr = b.sh.tiles.sub_rows, kl = b.sh.max_kl, nb = kl > 0 ? (kl + sr - 1) / sr : 1;
+  if (sr == 32) k_wb_fwd<F, 32><<<dim3(nb, b.sh.n_wide, nrhs), 128, 0, st>>>(b, p);
+  else k_wb_fwd<F, 64><<<dim3(nb, b.sh.n_wide, nrhs), 256, 0, st>>>(b, p);
+}
+template <typename F> static void launch_bwd(const Batch& b, int p, int nrhs, cudaStream_t st) {
+  const int sr = b.sh.tiles.sub_rows, kl = b.sh.max_kl, nb = kl > 0 ? (kl + sr - 1) / sr : 1;
+  if (sr == 32) k_wb_bwd<F, 32><<<dim3(nb, b.sh.n_wide, nrhs), 128, 0, st>>>(b, p);
+  else k_wb_bwd<F, 64><<<dim3(nb, b.sh.n_wide, nrhs), 256, 0, st>>>(b, p);
+}
 
 // Panel loop with lookahead on three helper streams (fork / join by events,
 // so a captured pass keeps the same dependencies):
@@ -1361,7 +1399,7 @@ static void launch_wb_update(const Batch& b, int p, int part, cudaStream_t st) {
       k_wb_update_tc<<<dim3((mr + OZ_TR - 1) / OZ_TR, (mr + OZ_T - 1) / OZ_T, nw), OZ_THREADS, OZ_SMEM, st>>>(b, p,
                                                                                                         part);
   } else if (part == 1) {
-    k_wb_corner<<<dim3(NB / CT8, NB / CT8, nw), CORNER_THREADS, 0, st>>>(b, p);
+    launch_corner(b, p, st);
   } else {
     const int t = (mr + UT - 1) / UT;
     k_wb_update<<<dim3(t, t, nw), 256, 0, st>>>(b, p, part);
@@ -1443,7 +1481,8 @@ template <typename F>
 static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide, mr = sd.max_kl, P = sd.max_panels;
-  const int nrest = trsm_rest_blocks(mr), rb = sub_blocks(mr);
+  const int nrest = trsm_rest_blocks(b);
+  (void)mr;
   cudaStream_t sb = sd.aux[2], s2 = sd.aux[0], s3 = sd.aux[1], s4 = sd.aux[3];
   cudaEvent_t e_start = sd.evt[0], e_trsm = sd.evt[1], e_corner = sd.evt[2], e_diag = sd.evt[3], e_fwd = sd.evt[4],
               e_rest = sd.evt[5];
@@ -1459,10 +1498,10 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   if (nrest) {
     cudaEventRecord(e_start, sb);
     cudaStreamWaitEvent(s4, e_start, 0);
-    k_wb_trsm<F, TRSM_RB><<<dim3(2 * nrest, nw), 32 * TRSM_RB, 0, s4>>>(b, -1, NB, nrest);
+    launch_trsm_rest<F>(b, -1, s4);
     cudaEventRecord(e_rest, s4);
   }
-  k_wb_trsm<F, TRSM_RB_FIRST><<<dim3(2 * TRSM_FIRST, nw), 32 * TRSM_RB_FIRST, 0, sb>>>(b, -1, 0, TRSM_FIRST);
+  launch_trsm_first<F>(b, -1, sb);
   wb_update(b, -1, 1, sb, (F*)nullptr);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
@@ -1471,7 +1510,7 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   if (nrest) cudaStreamWaitEvent(sb, e_rest, 0);
   cudaEventRecord(e_trsm, sb);
   cudaStreamWaitEvent(s3, e_trsm, 0);
-  k_wb_fwd<F><<<dim3(rb, nw), 256, 0, s3>>>(b, -1);
+  launch_fwd<F>(b, -1, 1, s3);
   cudaEventRecord(e_fwd, s3);
   wb_update(b, -1, 2, sb, (F*)nullptr);
   cudaStreamWaitEvent(sb, e_diag, 0);
@@ -1482,7 +1521,7 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   if ((e = add_while(st, &h, &body)) != cudaSuccess) return e;
   if ((e = cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
-  k_wb_bwd<F><<<dim3(rb, nw), 256, 0, sb>>>(b, -1);
+  launch_bwd<F>(b, -1, 1, sb);
   k_wb_loop_step<<<1, 1, 0, sb>>>(sd.panel, -1, P, h);
   return cudaStreamEndCapture(sb, &done);
 }
@@ -1507,20 +1546,20 @@ cudaError_t wide_capture_error() {
 template <typename F>
 static void wide_factor_solve_serial(const Batch& b, cudaStream_t st) {
   const ShellData& sd = b.sh;
-  const int nw = sd.n_wide, mr = sd.max_kl, nrest = trsm_rest_blocks(mr), rb = sub_blocks(mr);
+  const int nw = sd.n_wide, nrest = trsm_rest_blocks(b);
   k_wb_diag<F><<<nw, DIAG_THREADS, 0, st>>>(b, 0);
   for (int p = 0; p < sd.max_panels; ++p) {
     const bool next = p + 1 < sd.max_panels;
-    if (nrest) k_wb_trsm<F, TRSM_RB><<<dim3(2 * nrest, nw), 32 * TRSM_RB, 0, st>>>(b, p, NB, nrest);
-    k_wb_trsm<F, TRSM_RB_FIRST><<<dim3(2 * TRSM_FIRST, nw), 32 * TRSM_RB_FIRST, 0, st>>>(b, p, 0, TRSM_FIRST);
+    if (nrest) launch_trsm_rest<F>(b, p, st);
+    launch_trsm_first<F>(b, p, st);
     if (next) {
       wb_update(b, p, 1, st, (F*)nullptr);
       k_wb_diag<F><<<nw, DIAG_THREADS, 0, st>>>(b, p + 1);
     }
-    k_wb_fwd<F><<<dim3(rb, nw), 256, 0, st>>>(b, p);
+    launch_fwd<F>(b, p, 1, st);
     wb_update(b, p, next ? 2 : 0, st, (F*)nullptr);
   }
-  for (int p = sd.max_panels - 1; p >= 0; --p) k_wb_bwd<F><<<dim3(rb, nw), 256, 0, st>>>(b, p);
+  for (int p = sd.max_panels - 1; p >= 0; --p) launch_bwd<F>(b, p, 1, st);
 }
 
 // Factor and solve in the factor's type F: FP64, the LU in place of K_AA
@@ -1538,8 +1577,8 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
   const ShellData& sd = b.sh;
   const int nw = sd.n_wide;
   const int mr = sd.max_kl;  // largest kl over the wide structures
-  const int nrest = trsm_rest_blocks(mr);
-  const int rb = sub_blocks(mr);
+  const int nrest = trsm_rest_blocks(b);
+  (void)mr;
   cudaStream_t s2 = sd.aux[0], s3 = sd.aux[1], s4 = sd.aux[3];
   // the helpers fork from the main stream at their first wait and join it
   // again before the backward substitution
@@ -1552,12 +1591,12 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
       cudaEventRecord(e_start, st);
       cudaStreamWaitEvent(s4, e_start, 0);
       ProfScope q(prof, s4, KC_WIDE_TRSM);
-      k_wb_trsm<F, TRSM_RB><<<dim3(2 * nrest, nw), 32 * TRSM_RB, 0, s4>>>(b, p, NB, nrest);
+      launch_trsm_rest<F>(b, p, s4);
       cudaEventRecord(e_rest, s4);
     }
     {
       ProfScope q(prof, st, KC_WIDE_TRSM);
-      k_wb_trsm<F, TRSM_RB_FIRST><<<dim3(2 * TRSM_FIRST, nw), 32 * TRSM_RB_FIRST, 0, st>>>(b, p, 0, TRSM_FIRST);
+      launch_trsm_first<F>(b, p, st);
     }
     if (next) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); wb_update(b, p, 1, st, (F*)nullptr); }
@@ -1569,7 +1608,7 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
     if (nrest) cudaStreamWaitEvent(st, e_rest, 0);
     cudaEventRecord(e_trsm, st);
     cudaStreamWaitEvent(s3, e_trsm, 0);
-    { ProfScope q(prof, s3, KC_WIDE_SUBST); k_wb_fwd<F><<<dim3(rb, nw), 256, 0, s3>>>(b, p); }
+    { ProfScope q(prof, s3, KC_WIDE_SUBST); launch_fwd<F>(b, p, 1, s3); }
     if (next) {
       { ProfScope q(prof, st, KC_WIDE_UPDATE); wb_update(b, p, 2, st, (F*)nullptr); }
       cudaStreamWaitEvent(st, e_diag, 0);
@@ -1582,7 +1621,7 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
   cudaStreamWaitEvent(st, e_fwd, 0);
   for (int p = sd.max_panels - 1; p >= 0; --p) {
     ProfScope q(prof, st, KC_WIDE_SUBST);
-    k_wb_bwd<F><<<dim3(rb, nw), 256, 0, st>>>(b, p);
+    launch_bwd<F>(b, p, 1, st);
   }
 }
 
@@ -1593,16 +1632,16 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
 // loops, are built with the FP64 options and never refine.)
 static void ir_sweep(const Batch& b, cudaStream_t st, cudaGraphConditionalHandle h, int use_h, LaunchProf* prof) {
   const ShellData& sd = b.sh;
-  const int nw = sd.n_wide, rb = sub_blocks(sd.max_kl), P = sd.max_panels;
+  const int nw = sd.n_wide, P = sd.max_panels;
   const int rows = (P * NB + 255) / 256;
   { ProfScope q(prof, st, KC_WIDE_REFINE); k_ir_residual<<<dim3(rows, nw), 256, 0, st>>>(b); }
   for (int p = 0; p < P; ++p) {
     ProfScope q(prof, st, KC_WIDE_SUBST);
-    k_wb_fwd<float><<<dim3(rb, nw), 256, 0, st>>>(b, p);
+    launch_fwd<float>(b, p, 1, st);
   }
   for (int p = P - 1; p >= 0; --p) {
     ProfScope q(prof, st, KC_WIDE_SUBST);
-    k_wb_bwd<float><<<dim3(rb, nw), 256, 0, st>>>(b, p);
+    launch_bwd<float>(b, p, 1, st);
   }
   {
     ProfScope q(prof, st, KC_WIDE_REFINE);
@@ -1686,9 +1725,8 @@ void launch_wide_solve(const Batch& b, cudaStream_t st, LaunchProf* prof) {
 // launch_wide_solve without the factor, every column per launch.
 void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st) {
   if (b.sh.n_wide == 0 || nrhs <= 0) return;
-  const int nw = b.sh.n_wide, rb = sub_blocks(b.sh.max_kl);
-  for (int p = 0; p < b.sh.max_panels; ++p) k_wb_fwd<double><<<dim3(rb, nw, nrhs), 256, 0, st>>>(b, p);
-  for (int p = b.sh.max_panels - 1; p >= 0; --p) k_wb_bwd<double><<<dim3(rb, nw, nrhs), 256, 0, st>>>(b, p);
+  for (int p = 0; p < b.sh.max_panels; ++p) launch_fwd<double>(b, p, nrhs, st);
+  for (int p = b.sh.max_panels - 1; p >= 0; --p) launch_bwd<double>(b, p, nrhs, st);
 }
 
 // Launches of the panel loops: unrolled, the first diagonal LU, then per
@@ -1699,7 +1737,7 @@ void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st) {
 // iteration, and two kernels per backward one; the FP64 tensor-core update
 // adds its slicing kernel per panel.
 static int wide_factor_launches(const Batch& b, bool fp64) {
-  const int P = b.sh.max_panels, per = 6 + (trsm_rest_blocks(b.sh.max_kl) ? 1 : 0);
+  const int P = b.sh.max_panels, per = 6 + (trsm_rest_blocks(b) ? 1 : 0);
   return (b.sh.loops_in_graph ? 3 + (per + 2) * P : 1 + per * P - 2) + (fp64 && b.sh.wide_tc ? P : 0);
 }
 

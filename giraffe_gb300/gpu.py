@@ -30,7 +30,8 @@ EXPORTS = ["gf_create", "gf_destroy", "gf_last_error", "gf_default_opts", "gf_ba
            "gf_shell_inertia_elements", "gf_ctx_set_opts", "gf_upload_structure", "gf_structure_destroy",
            "gf_structure_dims", "gf_structure_dofs", "gf_structure_pattern", "gf_structure_set_step", "gf_begin_step",
            "gf_assemble", "gf_set_increment", "gf_commit", "gf_rollback", "gf_structure_nodes", "gf_beam_mount",
-           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange", "gf_structure_modal", "gf_modal", "gf_batch_monitor"]
+           "gf_beam_save_lagrange", "gf_shell_mount", "gf_shell_save_lagrange", "gf_structure_modal", "gf_modal", "gf_batch_monitor",
+           "gf_batch_wide_tiles"]
 
 GF_LAYOUT_CSR, GF_LAYOUT_GB = 0, 1
 GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
@@ -39,7 +40,7 @@ GF_BEAM_LAG, GF_SHELL_LAG = 21, 27
 class gf_solve_opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("poll_every", C.c_int),
                 ("use_graph", C.c_int), ("wide_update", C.c_int), ("max_passes", C.c_int),
-                ("monitor_rows", C.c_int), ("max_refine", C.c_int)]
+                ("monitor_rows", C.c_int), ("max_refine", C.c_int), ("wide_tiles", C.c_int * 4)]
 
 
 class gf_stats(C.Structure):
@@ -126,6 +127,7 @@ def lib():
         L.gf_structure_modal.argtypes = [vp, C.c_double, C.c_int, C.c_double, dp, dp, ip]
         L.gf_modal.argtypes = [vp, C.POINTER(gf_model_desc), C.c_int, C.c_double, dp, dp, ip]
         L.gf_batch_monitor.argtypes = [vp, C.c_int, dp, ip]
+        L.gf_batch_wide_tiles.argtypes = [vp, ip]
         L.gf_beam_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
         L.gf_beam_save_lagrange.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp]
         L.gf_shell_mount.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.c_int, dp, dp]
@@ -184,11 +186,14 @@ class Context:
             raise RuntimeError(f"{what} failed ({rc}): {self.error()}")
 
     def opts(self, precision=GF_PREC_FP64, use_graph=True, poll_every=8, wide_update=None,
-             max_passes=0, monitor_rows=0, max_refine=0):
+             max_passes=0, monitor_rows=0, max_refine=0, wide_tiles=None):
         o = gf_solve_opts()
         self.L.gf_default_opts(C.byref(o))
         o.precision, o.use_graph, o.poll_every, o.max_passes = precision, int(use_graph), poll_every, max_passes
         o.monitor_rows, o.max_refine = monitor_rows, max_refine
+        if wide_tiles is not None:
+            for k, v in enumerate(wide_tiles):
+                o.wide_tiles[k] = v
         if wide_update is not None:
             o.wide_update = wide_update
         return o
@@ -483,6 +488,14 @@ class BatchSolver:
         st = np.array([[x.converged_steps, x.newton_iterations, x.bisections, x.aborted] for x in stats])
         self.last_stats = stats
         return outs, st
+
+    def wide_tiles(self):
+        """The wide-band LU tile shapes this batch runs with
+        (gf_batch_wide_tiles): [bulk trsm rows, first trsm rows, corner tile,
+        solve rows]."""
+        t = (C.c_int * 4)()
+        self.ctx.check(self.ctx.L.gf_batch_wide_tiles(self.h, t), "gf_batch_wide_tiles")
+        return list(t)
 
     def solve_stats(self):
         """Per structure, after results(): linear solves, FP64 refinement

@@ -97,6 +97,14 @@ typedef struct gf_solve_opts {
                       (gf_model_desc monitor_nodes; 0: none recorded) */
   int max_refine;  /* GF_PREC_MIXED: FP64 refinement sweeps of a wide-band
                       solve before its FP64 fallback (0: the default of 30) */
+  int wide_tiles[4]; /* Shell_1 wide-band LU tile shapes: rows per CTA of the
+                      bulk trsm (4, 8, 16) and of the first trsm (1, 2, 4),
+                      the corner update's tile edge (4, 8), rows per CTA of
+                      the triangular solves (32, 64).  An entry of 0 is picked
+                      by the autotuner, which times the shapes on a synthetic
+                      band of the structures' half-bandwidth once per context
+                      (served waves take the defaults 8, 2, 8, 64).  No
+                      choice changes any result. */
 } gf_solve_opts;
 enum { GF_WIDE_FP64 = 0, GF_WIDE_TENSOR = 1, GF_WIDE_TENSOR_SYNC = 2 };
 
@@ -423,6 +431,10 @@ int gf_structure_nodes(gf_structure* s, double* nodes, double* increments);
  * gf_solve_opts.monitor_rows ran out).  A NodalLoad acting on a constrained
  * DOF is not added to its reaction column. */
 int gf_batch_monitor(gf_batch* b, int s, double* out, int* dims);
+
+/* The wide-band LU tile shapes the batch runs with (gf_solve_opts.wide_tiles
+ * order; all 0 for a batch without Shell_1 structures). */
+int gf_batch_wide_tiles(const gf_batch* b, int* tiles);
 
 /* ---- Modal analysis ----
  * gf_structure_modal replaces Modal::Solve (src/Modal.cpp:131-199) with its
