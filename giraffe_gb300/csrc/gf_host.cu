@@ -1332,7 +1332,10 @@ int ensure_graph(gf_batch* B) {
       set_err(ctx, "capture of the wide-band loops failed: %s", cudaGetErrorString(ce));
       return GF_ERR_CUDA;
     }
-    CK(cudaGraphInstantiate(&B->graph, g, 0));
+    // per-node priorities (the wide-band LU's critical-path kernels) in a
+    // batch's own graph; a served wave's graph runs at its stream's priority,
+    // which orders the waves against each other
+    CK(cudaGraphInstantiate(&B->graph, g, B->arena ? 0 : cudaGraphInstantiateFlagUseNodePriority));
     CK(cudaGraphDestroy(g));
     B->host_ms[3] = host_now_ms() - t0;
   }

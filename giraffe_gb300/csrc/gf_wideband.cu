@@ -1459,6 +1459,28 @@ cudaError_t add_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_
 // with the batch's choice of kernel; FP32: k_wb_update32, the corner as its
 // single tile).
 void wb_update(const Batch& b, int p, int part, cudaStream_t st, double*) { launch_wb_update(b, p, part, st); }
+
+// The next panel's diagonal LU, one CTA per structure on the lookahead's
+// critical path, launched at the device's highest stream priority: the
+// block scheduler then gives it the first free SM ahead of the trailing
+// update's and the helper streams' CTAs (a captured launch keeps the
+// priority as a node attribute).
+template <typename F> void launch_diag(const Batch& b, int p, cudaStream_t st) {
+  static const int prio = [] {
+    int lo = 0, hi = 0;
+    return cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess ? hi : 0;
+  }();
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(b.sh.n_wide);
+  cfg.blockDim = dim3(DIAG_THREADS);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_wb_diag<F>, b, p);
+}
 void wb_update(const Batch& b, int p, int part, cudaStream_t st, float*) {
   const int t = part == 1 ? 1 : (b.sh.max_kl + U32T - 1) / U32T;
   k_wb_update32<<<dim3(t, t, b.sh.n_wide), 256, 0, st>>>(b, p, part);
@@ -1505,7 +1527,7 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   wb_update(b, -1, 1, sb, (F*)nullptr);
   cudaEventRecord(e_corner, sb);
   cudaStreamWaitEvent(s2, e_corner, 0);
-  k_wb_diag<F><<<nw, DIAG_THREADS, 0, s2>>>(b, -2);
+  launch_diag<F>(b, -2, s2);
   cudaEventRecord(e_diag, s2);
   if (nrest) cudaStreamWaitEvent(sb, e_rest, 0);
   cudaEventRecord(e_trsm, sb);
@@ -1602,7 +1624,7 @@ static void wide_factor_solve(const Batch& b, cudaStream_t st, LaunchProf* prof)
       { ProfScope q(prof, st, KC_WIDE_UPDATE); wb_update(b, p, 1, st, (F*)nullptr); }
       cudaEventRecord(e_corner, st);
       cudaStreamWaitEvent(s2, e_corner, 0);
-      { ProfScope q(prof, s2, KC_WIDE_DIAG); k_wb_diag<F><<<nw, DIAG_THREADS, 0, s2>>>(b, p + 1); }
+      { ProfScope q(prof, s2, KC_WIDE_DIAG); launch_diag<F>(b, p + 1, s2); }
       cudaEventRecord(e_diag, s2);
     }
     if (nrest) cudaStreamWaitEvent(st, e_rest, 0);
