@@ -2287,7 +2287,10 @@ extern "C" int gf_band_solve_noalloc(gf_ctx* ctx, int n, int kl, int ku, const d
   return GF_OK;
 }
 
-extern "C" int gf_batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, size_t* bytes) {
+namespace gfh {
+// Device bytes of a batch of these structures built with opts (NULL: the
+// defaults); no device work.
+int batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts, size_t* bytes) {
   if (n <= 0 || !models || !bytes) {
     set_err(ctx, "gf_batch_device_bytes: invalid arguments");
     return GF_ERR_ARG;
@@ -2295,9 +2298,14 @@ extern "C" int gf_batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* mo
   gf_batch B;
   B.ctx = ctx;
   B.count_only = true;
-  gf_default_opts(&B.opts);
+  if (opts) B.opts = *opts; else gf_default_opts(&B.opts);
   int r = build_batch(&B, n, models);
   if (r != GF_OK) return r;
   *bytes = B.counted_bytes;
   return GF_OK;
+}
+}  // namespace gfh
+
+extern "C" int gf_batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, size_t* bytes) {
+  return batch_device_bytes(ctx, n, models, nullptr, bytes);
 }

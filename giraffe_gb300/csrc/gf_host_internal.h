@@ -184,6 +184,9 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models);
 int batch_reset(gf_batch* B);
 // Captures one Newton pass as a CUDA graph on B->stream (opts.use_graph).
 int ensure_graph(gf_batch* B);
+// Device bytes of a batch of these structures built with opts (NULL: the
+// defaults), without touching the device.
+int batch_device_bytes(gf_ctx* ctx, int n, const gf_model_desc* models, const gf_solve_opts* opts, size_t* bytes);
 // Kernel launches of one Newton pass.
 int count_launches_per_pass(const gf_batch* B);
 // The wide-band LU's tile shapes for half-bandwidth kl and trailing-update

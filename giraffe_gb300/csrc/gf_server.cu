@@ -400,6 +400,7 @@ void build_wave(gf_server* S, Wave& w) {
   B->ctx = &S->build_ctx;
   gf_default_opts(&B->opts);
   B->opts.use_graph = 1;
+  B->opts.precision = S->o.precision;
   B->arena = &S->arena;
   B->host_stage = &S->stage;
   B->stream = S->capture_stream;
@@ -493,6 +494,7 @@ void gf_server_default_opts(gf_server_opts* o) {
   o->max_wave_structs = 128;
   o->passes_per_chunk = 4;
   o->max_wave_passes = 0;
+  o->precision = GF_PREC_FP64;
 }
 
 gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts) {
@@ -500,7 +502,8 @@ gf_server* gf_server_create(gf_ctx* ctx, const gf_server_opts* opts) {
   gf_server* S = new gf_server();
   S->ctx = ctx;
   if (opts) S->o = *opts; else gf_server_default_opts(&S->o);
-  if (S->o.max_waves <= 0 || S->o.max_wave_structs <= 0 || S->o.passes_per_chunk <= 0 || S->o.hbm_budget == 0) {
+  if (S->o.max_waves <= 0 || S->o.max_wave_structs <= 0 || S->o.passes_per_chunk <= 0 || S->o.hbm_budget == 0 ||
+      (S->o.precision != GF_PREC_FP64 && S->o.precision != GF_PREC_MIXED)) {
     set_err(ctx, "gf_server_create: invalid options");
     delete S;
     return nullptr;
@@ -578,7 +581,10 @@ int gf_server_submit(gf_server* S, const gf_model_desc* model, double* final_nod
   if (!S || !model) return GF_ERR_ARG;
   gf_ctx* ctx = S->ctx;
   size_t bytes = 0;
-  int r = gf_batch_device_bytes(ctx, 1, model, &bytes);
+  gf_solve_opts wo;  // the options the wave's batch is built with
+  gf_default_opts(&wo);
+  wo.precision = S->o.precision;
+  int r = batch_device_bytes(ctx, 1, model, &wo, &bytes);
   if (r != GF_OK) return r;
   if (bytes + kWaveSlack > S->arena.size) {
     set_err(ctx, "gf_server_submit: structure needs %zu device bytes, the budget is %zu", bytes, S->arena.size);

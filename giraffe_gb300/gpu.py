@@ -51,7 +51,7 @@ class gf_stats(C.Structure):
 
 class gf_server_opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_waves", C.c_int), ("max_wave_structs", C.c_int),
-                ("passes_per_chunk", C.c_int), ("max_wave_passes", C.c_int)]
+                ("passes_per_chunk", C.c_int), ("max_wave_passes", C.c_int), ("precision", C.c_int)]
 
 
 class gf_server_result(C.Structure):

@@ -30,7 +30,7 @@ class Result:
 
 class Server:
     def __init__(self, ctx: Context, hbm_budget: int = 8 << 30, max_waves: int = 4, max_wave_structs: int = 128,
-                 passes_per_chunk: int = 4, max_wave_passes: int = 0):
+                 passes_per_chunk: int = 4, max_wave_passes: int = 0, precision: int = 0):
         self.ctx = ctx
         self.L = lib()
         o = gf_server_opts()
@@ -38,6 +38,7 @@ class Server:
         o.hbm_budget, o.max_waves, o.max_wave_structs, o.passes_per_chunk = (hbm_budget, max_waves,
                                                                              max_wave_structs, passes_per_chunk)
         o.max_wave_passes = max_wave_passes
+        o.precision = precision  # GF_PREC_FP64 or GF_PREC_MIXED for every wave
         self.h = self.L.gf_server_create(ctx.h, C.byref(o))
         if not self.h:
             raise RuntimeError("gf_server_create failed: " + ctx.error())

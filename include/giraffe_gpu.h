@@ -307,6 +307,8 @@ typedef struct gf_server_opts {
   int max_wave_passes;   /* Newton passes after which a wave's unfinished
                             structures are reported with GF_ERR_TIMEOUT
                             (0: the default of 4,000,000) */
+  int precision;         /* the waves' gf_solve_opts.precision: GF_PREC_FP64
+                            (default) or GF_PREC_MIXED */
 } gf_server_opts;
 
 typedef struct gf_server_result {

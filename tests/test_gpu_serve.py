@@ -129,3 +129,35 @@ def test_mixed_chains_and_plates_equal_alone(gpu_ctx):
         assert time.perf_counter() - t0 < 300
     srv.close()
     _check_same_as_alone(gpu_ctx, structs, results)
+
+
+def test_mixed_precision_served_wave_equals_the_mixed_batch(gpu_ctx):
+    """gf_server_opts.precision = GF_PREC_MIXED: each wave is built with the
+    mixed options (FP32-pair Beam_1 tangents; an FP32 wide-band factor with
+    FP64 refinement for Shell_1, its panel loops as graph loops in the served
+    pass), and each served result is the mixed batch's result for that
+    structure, bit for bit and with the same counts."""
+    structs = configs.served_chains(5, seed=11, dof_min=600, dof_max=4000) + [configs.square_plate(6, steps=4)]
+    srv = serve.Server(gpu_ctx, hbm_budget=1 << 30, max_waves=2, max_wave_structs=3, passes_per_chunk=2,
+                       precision=gpu.GF_PREC_MIXED)
+    for i, s in enumerate(structs):
+        srv.submit(s, tag=i)
+    results = {}
+    t0 = time.perf_counter()
+    while len(results) < len(structs):
+        for r in srv.poll():
+            results[r.tag] = r
+        assert time.perf_counter() - t0 < 300
+    while srv.status()["waves"]:
+        assert not srv.poll()
+    srv.close()
+    for i, s in enumerate(structs):
+        b = gpu.BatchSolver(gpu_ctx, [s], gpu_ctx.opts(gpu.GF_PREC_MIXED))
+        b.reset()
+        b.run()
+        outs, st = b.results()
+        b.close()
+        r = results[i]
+        assert r.status == 0, i
+        assert tuple(int(v) for v in r.stats) == tuple(int(v) for v in st[0]), i
+        assert np.array_equal(r.final, outs[0]), i
