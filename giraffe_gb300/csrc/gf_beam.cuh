@@ -9,6 +9,8 @@
 // (T3^T M_pq T3) before the DeltaN expansion, which is the same linear map as
 // the reference's T^T (DeltaN^T M DeltaN) T on the 18x18 matrix.
 #pragma once
+#include <type_traits>
+
 #include "gf_math.cuh"
 #include "gf_types.h"
 
@@ -204,32 +206,42 @@ GF_HD void beam_gp_operator(const BeamConst& c, const BeamGP& k, TK* M, int ms =
   store_block(M, ms, 2, 1, V2, true);
 }
 
-// M'_pq = T3^T M_pq T3 for the 3x3 blocks, in place; M01 = M10 = 0 stay
-// zero and are skipped.
+// M'_pq = T3^T M_pq T3 for one 3x3 block, in place.
+template <typename TK> GF_HD void rotate_block9(const TK* T, TK* M, int ms, int p, int q) {
+  TK b[9], t[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) b[i * 3 + j] = M[((3 * p + i) * 9 + 3 * q + j) * ms];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) t[i * 3 + j] = b[i * 3] * T[j] + b[i * 3 + 1] * T[3 + j] + b[i * 3 + 2] * T[6 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      M[((3 * p + i) * 9 + 3 * q + j) * ms] = T[i] * t[j] + T[3 + i] * t[3 + j] + T[6 + i] * t[6 + j];
+}
+
+// M'_pq = T3^T M_pq T3 for the seven 3x3 blocks that are not zero (M01 = M10
+// = 0 stay zero), in place.  In FP64 the block loop is unrolled; in FP32-pair
+// arithmetic, whose operations are several instructions each, it is kept
+// rolled so the kernel's code stays within the instruction cache.
 template <typename TK> GF_HD void rotate_blocks9(const BeamConst& c, TK* M, int ms = 1) {
   TK T[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) T[i] = TK(c.T3[i]);
+  // blocks (0,0) (0,2) (1,1) (1,2) (2,0) (2,1) (2,2)
+  if constexpr (std::is_same<TK, double>::value) {
 #pragma unroll
-  for (int p = 0; p < 3; ++p)
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      if ((p == 0 && q == 1) || (p == 1 && q == 0)) continue;
-      TK b[9], t[9];
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) b[i * 3 + j] = M[((3 * p + i) * 9 + 3 * q + j) * ms];
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) t[i * 3 + j] = b[i * 3] * T[j] + b[i * 3 + 1] * T[3 + j] + b[i * 3 + 2] * T[6 + j];
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          M[((3 * p + i) * 9 + 3 * q + j) * ms] = T[i] * t[j] + T[3 + i] * t[3 + j] + T[6 + i] * t[6 + j];
-    }
+    for (int k = 0; k < 7; ++k)
+      rotate_block9(T, M, ms, k < 2 ? 0 : (k < 4 ? 1 : 2), k < 4 ? (k == 0 ? 0 : (k == 2 ? 1 : 2)) : k - 4);
+  } else {
+#pragma unroll 1
+    for (int k = 0; k < 7; ++k)
+      rotate_block9(T, M, ms, k < 2 ? 0 : (k < 4 ? 1 : 2), k < 4 ? (k == 0 ? 0 : (k == 2 ? 1 : 2)) : k - 4);
+  }
 }
 
 // Internal force contribution of one Gauss point, global frame, added to

@@ -6,9 +6,10 @@
 // Rounding is explicit (__fadd_rn / __fmul_rn / __fmaf_rn) so that the
 // compiler cannot contract the transformations.
 //
-// Used as the TK type of the Beam_1 tangent operator in the mixed-precision
-// path: the tangent only steers the Newton iteration, while the internal
-// force, the residual and the convergence checks stay FP64.
+// Used as the TK type of the Beam_1 tangent's rotation to the global frame
+// and K_e expansion in the mixed-precision path: the tangent only steers the
+// Newton iteration, while the Gauss-point operator, the internal force, the
+// residual and the convergence checks stay FP64.
 #pragma once
 #include <cuda_runtime.h>
 

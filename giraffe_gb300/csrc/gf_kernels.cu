@@ -340,8 +340,25 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     beam_kinematics(c, h, ip[g], g, kin);
     beam_gp_force(c, kin, g, f, MOUNT_THREADS);
     TK* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
-    beam_gp_operator<TK>(c, kin, M, MOUNT_THREADS);
-    rotate_blocks9<TK>(c, M, MOUNT_THREADS);
+    if constexpr (std::is_same<TK, double>::value) {
+      beam_gp_operator<TK>(c, kin, M, MOUNT_THREADS);
+      rotate_blocks9<TK>(c, M, MOUNT_THREADS);
+    } else {
+      // mixed precision: the operator in FP64, rounded to TK in place (a TK
+      // is as wide as a double), then its rotation and the K_e expansion in
+      // TK.  (Expanding in a kernel of its own, with many warps per SM, gains
+      // nothing here: its FP64 <-> FP32-pair conversions take the FP64 pipe
+      // as long as the products it moves off it.)
+      static_assert(sizeof(TK) == sizeof(double), "operator storage");
+      double* Md = reinterpret_cast<double*>(M);
+      beam_gp_operator<double>(c, kin, Md, MOUNT_THREADS);
+#pragma unroll 1
+      for (int q = 0; q < 81; ++q) {
+        const double v = Md[q * MOUNT_THREADS];
+        M[q * MOUNT_THREADS] = TK(v);
+      }
+      rotate_blocks9<TK>(c, M, MOUNT_THREADS);
+    }
   }
   double a1Mr = 0.0;
   if (dyn) {
@@ -368,6 +385,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
   // chain solver are coalesced
   double* Ke = b.Ke + e;
   const int64_t ne = b.n_elem;
+
 #pragma unroll 1
   for (int J = 0; J < 3; ++J)
 #pragma unroll 1

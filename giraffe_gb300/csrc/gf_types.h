@@ -361,13 +361,10 @@ struct Batch {
   double* P;
   double* y;
   int64_t rhs_ld;  // column stride of a multi-column wide-band substitution (0: one column)
-  double* xr;  // refinement: accumulated solution
-  double* r;   // refinement: residual
   // band and factor
   double* Ke;  // per-element tangent scratch (18x18 column-major)
   double* Fe;  // per-element internal force scratch
   double* band;
-  float* band32;
   double* U;
   float* U32;
   // structures

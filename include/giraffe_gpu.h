@@ -67,8 +67,9 @@ enum {
 enum { GF_PREC_FP64 = 0, GF_PREC_MIXED = 1 };
 
 typedef struct gf_solve_opts {
-  int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED: Beam_1 tangent
-                      operators in FP32-pair arithmetic, and Shell_1 wide-band
+  int precision;   /* GF_PREC_FP64 (plain) or GF_PREC_MIXED: the Beam_1
+                      tangent's rotation and K_e expansion in FP32-pair
+                      arithmetic (the operator itself FP64), and Shell_1 wide-band
                       K_AA factored in FP32 (its LU beside the FP64 K_AA) with
                       FP64 iterative refinement (x += K32^-1 (b - K x)) until
                       a correction is below 2^-52 |x| or shrinks by less than
