@@ -41,34 +41,45 @@ __device__ __forceinline__ double recip(double p) {
   return r;
 }
 
-// Gauss-Jordan on a thread's 6 x NCOLS augmented matrix A (row-major, entry
-// (r, c) at A[(r * NC + c) * CT]): on return columns 6.. hold D^{-1} RHS.
-// No pivoting; returns false on a zero or non-finite pivot.  Fully unrolled
-// so that the independent column updates of one pivot step overlap.
-template <int NCOLS>
-__device__ bool gauss_jordan6(double* A) {
+// Gauss-Jordan on a thread's augmented matrix [D | R]: D (6x6, row-major)
+// in registers, every index static under the full unroll, and the NR
+// right-hand sides R in shared memory (entry (r, c) at R[(r * NR + c) * CT]).
+// On return R holds D^{-1} R.  No pivoting; returns false on a zero or
+// non-finite pivot.  Only R takes shared memory (624 B per thread for 13
+// columns, against 912 B for the whole 6 x 19 system), so more CTAs share an
+// SM; the independent column updates of one pivot step overlap.
+template <int NR>
+__device__ bool gauss_jordan6(double (&D)[36], double* R) {
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    double p = A[(k * NC + k) * CT];
+    const double p = D[k * 6 + k];
     if (!(p != 0.0) || !isfinite(p)) ok = false;
-    double inv = recip(p);
-    double rk[NCOLS];
+    const double inv = recip(p);
+    double dk[6], rk[NR];
 #pragma unroll
-    for (int c = k + 1; c < NCOLS; ++c) {
-      rk[c] = A[(k * NC + c) * CT] * inv;
-      A[(k * NC + c) * CT] = rk[c];
+    for (int c = k + 1; c < 6; ++c) {
+      dk[c] = D[k * 6 + c] * inv;
+      D[k * 6 + c] = dk[c];
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+      rk[c] = R[(k * NR + c) * CT] * inv;
+      R[(k * NR + c) * CT] = rk[c];
     }
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
       if (i == k) continue;
-      double m = A[(i * NC + k) * CT];
+      const double m = D[i * 6 + k];
 #pragma unroll
-      for (int c = k + 1; c < NCOLS; ++c) A[(i * NC + c) * CT] = fma(-m, rk[c], A[(i * NC + c) * CT]);
+      for (int c = k + 1; c < 6; ++c) D[i * 6 + c] = fma(-m, dk[c], D[i * 6 + c]);
+#pragma unroll
+      for (int c = 0; c < NR; ++c) R[(i * NR + c) * CT] = fma(-m, rk[c], R[(i * NR + c) * CT]);
     }
   }
   return ok;
 }
+constexpr int NRHS = 13;  // right-hand sides of the chain eliminations: b, then 6 + 6 coupling columns
 
 // ---- 1. condensation of the midside node of every chain element ----
 __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
@@ -80,7 +91,8 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   if (!solving(b, s)) return;
   const StructInfo inf = b.info[s];
   const double* P = b.P + inf.dof_off;
-  double* A = smem + threadIdx.x;
+  double* R = smem + threadIdx.x;  // [P_m | K_ma | K_mb], 6 x 13
+  double D[36];                     // K_mm (+ the load stiffness)
   // K of the chain comes from the element tangents (column-major 18x18,
   // DOFs of the first corner, the midside node, the last corner) plus the
   // nodal load stiffness of the midside node: the midside rows belong to
@@ -94,23 +106,29 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   int gm[6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) gm[i] = b.gl[(int64_t)nm * 6 + i];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double kmm = K((6 + i) + 18 * (6 + j));
+      if (i >= 3 && j >= 3) kmm += nk[(i - 3) * 3 + j - 3];
+      D[i * 6 + j] = kmm;
+    }
+  }
 #pragma unroll 1
   for (int i = 0; i < 6; ++i) {
 #pragma unroll 1
     for (int j = 0; j < 6; ++j) {
-      double kmm = K((6 + i) + 18 * (6 + j));
-      if (i >= 3 && j >= 3) kmm += nk[(i - 3) * 3 + j - 3];
-      A[(i * NC + j) * CT] = kmm;
-      A[(i * NC + 7 + j) * CT] = fa ? K((6 + i) + 18 * j) : 0.0;
-      A[(i * NC + 13 + j) * CT] = fb ? K((6 + i) + 18 * (12 + j)) : 0.0;
+      R[(i * NRHS + 1 + j) * CT] = fa ? K((6 + i) + 18 * j) : 0.0;
+      R[(i * NRHS + 7 + j) * CT] = fb ? K((6 + i) + 18 * (12 + j)) : 0.0;
     }
-    A[(i * NC + 6) * CT] = P[gm[i]];
+    R[(i * NRHS) * CT] = P[gm[i]];
   }
-  if (!gauss_jordan6<NC>(A)) b.state[s].info_fail = 1;
+  if (!gauss_jordan6<NRHS>(D, R)) b.state[s].info_fail = 1;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
 #pragma unroll 1
-    for (int q = 0; q < 13; ++q) ELM(c.ez, t, i * 13 + q) = A[(i * NC + 6 + q) * CT];
+    for (int q = 0; q < 13; ++q) ELM(c.ez, t, i * 13 + q) = R[(i * NRHS + q) * CT];
   // -A_as Z and -A_bs Z (6 x 13 each)
 #pragma unroll 1
   for (int side = 0; side < 2; ++side) {
@@ -125,7 +143,7 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
       for (int q = 0; q < 13; ++q) {
         double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc = fma(row[j], A[(j * NC + 6 + q) * CT], acc);
+        for (int j = 0; j < 6; ++j) acc = fma(row[j], R[(j * NRHS + q) * CT], acc);
         ELM(c.ec, t, i * 26 + side * 13 + q) = -acc;
       }
     }
@@ -185,22 +203,24 @@ __global__ void __launch_bounds__(CT) k_cr_eliminate(Batch b, ChainData c, int l
   CrItem it = c.odd[t];
   if (!solving(b, it.structure)) return;
   int k = it.corner;
-  double* A = smem + threadIdx.x;
+  double* R = smem + threadIdx.x;  // [b | L | U], 6 x 13
+  double D[36];
+#pragma unroll
+  for (int q = 0; q < 36; ++q) D[q] = CRN(c.cD, k, q);
 #pragma unroll 1
   for (int i = 0; i < 6; ++i) {
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      A[(i * NC + j) * CT] = CRN(c.cD, k, i * 6 + j);
-      A[(i * NC + 7 + j) * CT] = it.prev >= 0 ? CRN(c.cL, k, i * 6 + j) : 0.0;
-      A[(i * NC + 13 + j) * CT] = it.next >= 0 ? CRN(c.cU, k, i * 6 + j) : 0.0;
+      R[(i * NRHS + 1 + j) * CT] = it.prev >= 0 ? CRN(c.cL, k, i * 6 + j) : 0.0;
+      R[(i * NRHS + 7 + j) * CT] = it.next >= 0 ? CRN(c.cU, k, i * 6 + j) : 0.0;
     }
-    A[(i * NC + 6) * CT] = CRN(c.cb, k, i);
+    R[(i * NRHS) * CT] = CRN(c.cb, k, i);
   }
-  if (!gauss_jordan6<NC>(A)) b.state[it.structure].info_fail = 1;
+  if (!gauss_jordan6<NRHS>(D, R)) b.state[it.structure].info_fail = 1;
 #pragma unroll 1
   for (int i = 0; i < 6; ++i)
 #pragma unroll 1
-    for (int q = 0; q < 13; ++q) CRN(c.cz, k, i * 13 + q) = A[(i * NC + 6 + q) * CT];
+    for (int q = 0; q < 13; ++q) CRN(c.cz, k, i * 13 + q) = R[(i * NRHS + q) * CT];
 }
 
 // Warp-per-item form of k_cr_eliminate for the small levels near the top of
@@ -321,13 +341,13 @@ __global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
   int k = c.roots[t];
   int s = c.corner_struct[k];
   if (!solving(b, s)) return;
-  double* A = smem + threadIdx.x;
-  for (int i = 0; i < 6; ++i) {
-    for (int j = 0; j < 6; ++j) A[(i * NC + j) * CT] = CRN(c.cD, k, i * 6 + j);
-    A[(i * NC + 6) * CT] = CRN(c.cb, k, i);
-  }
-  if (!gauss_jordan6<7>(A)) b.state[s].info_fail = 1;
-  for (int i = 0; i < 6; ++i) CRN(c.cx, k, i) = A[(i * NC + 6) * CT];
+  double* R = smem + threadIdx.x;  // b, 6 x 1
+  double D[36];
+#pragma unroll
+  for (int q = 0; q < 36; ++q) D[q] = CRN(c.cD, k, q);
+  for (int i = 0; i < 6; ++i) R[i * CT] = CRN(c.cb, k, i);
+  if (!gauss_jordan6<1>(D, R)) b.state[s].info_fail = 1;
+  for (int i = 0; i < 6; ++i) CRN(c.cx, k, i) = R[i * CT];
 }
 
 // ---- 4. back substitution: x = Zb - ZL x_prev - ZU x_next ----
@@ -396,7 +416,7 @@ __global__ void k_corner_scatter(Batch b, ChainData c) {
 
 void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
   if (c.n_chain_elems == 0) return;
-  const int smem = 6 * NC * CT * (int)sizeof(double);
+  const int smem = 6 * NRHS * CT * (int)sizeof(double);
   // once per process (a function-local static is initialised by one thread)
   static const bool attr = [smem] {
     cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
