@@ -102,7 +102,8 @@ GF_HD void beam_kinematics(const BeamConst& c, const BeamHist& h, const BeamInte
   beam_stress(c, eps, k.sig);
 }
 
-// Gauss-point operator M = B^T D B + G (9x9 row-major, local frame) in TK.
+// Gauss-point operator M = B^T D B + G (9x9, local frame, stored at op_idx)
+// in TK.
 // With B = [[Qt, 0, P], [0, R, S]] (P = Qt dZ Xi, R = Qt Xi, S = Qt dXi) and
 // D = diag(Dt, Dr), the blocks are M00 = Qt^T Dt Qt, M02 = Qt^T Dt P,
 // M11 = R^T Dr R, M12 = R^T Dr S, M22 = P^T Dt P + S^T Dr S, M20 = M02^T,
@@ -130,6 +131,15 @@ template <typename TK> GF_HD M3<TK> dr_rows(const M3<TK>& Y, TK d3, TK d4, TK d5
   return r;
 }
 
+// Storage of the 9x9 operator: its 3x3 blocks (0, 1) and (1, 0) are zero
+// and are not stored, the other 63 entries row by row: entry (r, c) at
+// op_idx(r, c) (rows 0-2 hold columns 0-2 and 6-8, rows 3-5 columns 3-8,
+// rows 6-8 all nine).
+constexpr int OP_N = 63;
+GF_HD constexpr int op_idx(int r, int c) {
+  return r < 3 ? r * 6 + (c < 3 ? c : c - 3) : (r < 6 ? 18 + (r - 3) * 6 + (c - 3) : 36 + (r - 6) * 9 + c);
+}
+
 template <typename TK>
 GF_HD void store_block(TK* M, int ms, int p, int q, const M3<TK>& X, bool add = false, bool transposed = false) {
 #pragma unroll
@@ -137,7 +147,7 @@ GF_HD void store_block(TK* M, int ms, int p, int q, const M3<TK>& X, bool add = 
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       TK v = transposed ? X[j * 3 + i] : X[i * 3 + j];
-      TK& dst = M[((3 * p + i) * 9 + 3 * q + j) * ms];
+      TK& dst = M[op_idx(3 * p + i, 3 * q + j) * ms];
       dst = add ? dst + v : v;
     }
 }
@@ -150,11 +160,6 @@ GF_HD void beam_gp_operator(const BeamConst& c, const BeamGP& k, TK* M, int ms =
   TK d3 = TK(c.Dd[3]), d4 = TK(c.Dd[4]), d5 = TK(c.Dd[5]), d34 = TK(c.D34);
   M3<TK> Qt = cvt<TK>(k.Qt);
   M3<TK> Xi = cvt<TK>(k.Xi);
-  M3<TK> Z;
-#pragma unroll
-  for (int i = 0; i < 9; ++i) Z[i] = TK(0);
-  store_block(M, ms, 0, 1, Z);
-  store_block(M, ms, 1, 0, Z);
   store_block(M, ms, 0, 0, tmul(Qt, diag_rows(Qt, d0, d1, d2)));
   {
     M3<TK> P = mul(Qt, mul(cvt<TK>(kdZ), Xi));
@@ -212,7 +217,7 @@ template <typename TK> GF_HD void rotate_block9(const TK* T, TK* M, int ms, int 
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) b[i * 3 + j] = M[((3 * p + i) * 9 + 3 * q + j) * ms];
+    for (int j = 0; j < 3; ++j) b[i * 3 + j] = M[op_idx(3 * p + i, 3 * q + j) * ms];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -221,7 +226,7 @@ template <typename TK> GF_HD void rotate_block9(const TK* T, TK* M, int ms, int 
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      M[((3 * p + i) * 9 + 3 * q + j) * ms] = T[i] * t[j] + T[3 + i] * t[3 + j] + T[6 + i] * t[6 + j];
+      M[op_idx(3 * p + i, 3 * q + j) * ms] = T[i] * t[j] + T[3 + i] * t[3 + j] + T[6 + i] * t[6 + j];
 }
 
 // M'_pq = T3^T M_pq T3 for the seven 3x3 blocks that are not zero (M01 = M10
@@ -301,19 +306,19 @@ GF_HD void beam_K_block(const BeamConst& c, const TK* M0, const TK* M1, int I, i
       for (int g = 0; g < 2; ++g) {
         const TK* M = g ? M1 : M0;
         if (a < 3 && b < 3) {
-          acc += cdd[g] * M[(a * 9 + b) * ms];
+          acc += cdd[g] * M[op_idx(a, b) * ms];
         } else if (a < 3) {
           // the operator's block (0, 1) is zero
           int bb = b - 3;
-          acc += cdn[g] * M[(a * 9 + 6 + bb) * ms];
+          acc += cdn[g] * M[op_idx(a, 6 + bb) * ms];
         } else if (b < 3) {
           // the operator's block (1, 0) is zero
           int aa = a - 3;
-          acc += cnd[g] * M[((6 + aa) * 9 + b) * ms];
+          acc += cnd[g] * M[op_idx(6 + aa, b) * ms];
         } else {
           int aa = a - 3, bb = b - 3;
-          acc += cdd[g] * M[((3 + aa) * 9 + 3 + bb) * ms] + cdn[g] * M[((3 + aa) * 9 + 6 + bb) * ms] +
-                 cnd[g] * M[((6 + aa) * 9 + 3 + bb) * ms] + cnn[g] * M[((6 + aa) * 9 + 6 + bb) * ms];
+          acc += cdd[g] * M[op_idx(3 + aa, 3 + bb) * ms] + cdn[g] * M[op_idx(3 + aa, 6 + bb) * ms] +
+                 cnd[g] * M[op_idx(6 + aa, 3 + bb) * ms] + cnn[g] * M[op_idx(6 + aa, 6 + bb) * ms];
         }
       }
       double k = double(acc);

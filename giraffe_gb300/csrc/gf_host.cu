@@ -921,6 +921,7 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       p.min_it = so.min_it;
       p.conv_increase = so.conv_increase;
       p.dynamic = so.type == GF_DYNAMIC;
+      if (p.dynamic) b.any_dynamic = 1;
       p.zero_va = !p.dynamic || so.zero_ic;
       p.beta = so.beta;
       p.gamma = so.gamma;

@@ -307,7 +307,11 @@ __global__ void k_zero(Batch b) {
 // contiguous.  Elements of one colour share no node, so the scatter needs no
 // atomics and is deterministic.
 constexpr int MOUNT_THREADS = 64;
-constexpr int MOUNT_SMEM = (2 * 81 + 18 + 18) * MOUNT_THREADS * (int)sizeof(double);
+// per thread: the two operators (OP_N stored entries each), the internal
+// force (18) and, in batches with Dynamic steps, the two inertial
+// rotational tangents (18); a static batch fits three CTAs on an SM
+constexpr int MOUNT_SMEM_STATIC = (2 * OP_N + 18) * MOUNT_THREADS * (int)sizeof(double);
+constexpr int MOUNT_SMEM = (2 * OP_N + 18 + 18) * MOUNT_THREADS * (int)sizeof(double);
 
 template <typename TK>
 __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
@@ -327,8 +331,8 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
 #pragma unroll
     for (int q = 0; q < 6; ++q) d[6 * j + q] = b.disp[(int64_t)nd[j] * 6 + q];
   BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
-  double* f = reinterpret_cast<double*>(sM + (size_t)2 * 81 * MOUNT_THREADS) + tid;
-  double* Dm = f + 18 * MOUNT_THREADS;  // inertial rotational tangents, 2 x 9
+  double* f = reinterpret_cast<double*>(sM + (size_t)2 * OP_N * MOUNT_THREADS) + tid;
+  double* Dm = f + 18 * MOUNT_THREADS;  // inertial rotational tangents, 2 x 9 (any_dynamic batches)
 #pragma unroll
   for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
   const StructParams& pr = b.params[s];
@@ -339,7 +343,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     BeamGP kin;
     beam_kinematics(c, h, ip[g], g, kin);
     beam_gp_force(c, kin, g, f, MOUNT_THREADS);
-    TK* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
+    TK* M = sM + (size_t)g * OP_N * MOUNT_THREADS + tid;
     if constexpr (std::is_same<TK, double>::value) {
       beam_gp_operator<TK>(c, kin, M, MOUNT_THREADS);
       rotate_blocks9<TK>(c, M, MOUNT_THREADS);
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
       double* Md = reinterpret_cast<double*>(M);
       beam_gp_operator<double>(c, kin, Md, MOUNT_THREADS);
 #pragma unroll 1
-      for (int q = 0; q < 81; ++q) {
+      for (int q = 0; q < OP_N; ++q) {
         const double v = Md[q * MOUNT_THREADS];
         M[q * MOUNT_THREADS] = TK(v);
       }
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
   for (int J = 0; J < 3; ++J)
 #pragma unroll 1
     for (int I = 0; I < 3; ++I)
-      beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
+      beam_K_block<TK>(c, sM + tid, sM + OP_N * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
                        Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, ne);
   // Rayleigh damping: on the iterations that form C_e, the stiffness part
   // of K_e alone (no inertial terms) goes to the damping scratch, where
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     for (int J = 0; J < 3; ++J)
 #pragma unroll 1
       for (int I = 0; I < 3; ++I)
-        beam_K_block<TK>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ce, false, Dm,
+        beam_K_block<TK>(c, sM + tid, sM + OP_N * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ce, false, Dm,
                          Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, 0.0, ne);
   }
 #pragma unroll
@@ -1248,14 +1252,14 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_elements(int n, const Be
   double d[18];
   for (int q = 0; q < 18; ++q) d[q] = ds[(int64_t)e * 18 + q];
   BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
-  double* f = sM + (size_t)2 * 81 * MOUNT_THREADS + tid;
+  double* f = sM + (size_t)2 * OP_N * MOUNT_THREADS + tid;
   for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
 #pragma unroll 1
   for (int g = 0; g < 2; ++g) {
     BeamGP kin;
     beam_kinematics(c, h, ip[g], g, kin);
     beam_gp_force(c, kin, g, f, MOUNT_THREADS);
-    double* M = sM + (size_t)g * 81 * MOUNT_THREADS + tid;
+    double* M = sM + (size_t)g * OP_N * MOUNT_THREADS + tid;
     beam_gp_operator<double>(c, kin, M, MOUNT_THREADS);
     rotate_blocks9<double>(c, M, MOUNT_THREADS);
   }
@@ -1263,7 +1267,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_elements(int n, const Be
 #pragma unroll 1
   for (int J = 0; J < 3; ++J)
 #pragma unroll 1
-    for (int I = 0; I < 3; ++I) beam_K_block<double>(c, sM + tid, sM + 81 * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, K);
+    for (int I = 0; I < 3; ++I) beam_K_block<double>(c, sM + tid, sM + OP_N * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, K);
   for (int q = 0; q < 18; ++q) fs[(int64_t)e * 18 + q] = f[q * MOUNT_THREADS];
 }
 
@@ -1404,10 +1408,11 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     ProfScope q(prof, st, KC_MOUNT);
     // mixed precision: the tangent operator in FP32-pair arithmetic on the
     // FP32 pipe; kinematics, internal force and everything after stay FP64
+    const int smem = b.any_dynamic ? MOUNT_SMEM : MOUNT_SMEM_STATIC;
     if (b.mixed)
-      k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+      k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, smem, st>>>(b);
     else
-      k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, MOUNT_SMEM, st>>>(b);
+      k_beam_tangent<double><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, smem, st>>>(b);
     // the pressure's load stiffness is part of the K_e that Rayleigh damping
     // reads (the reference mounts loads before damping)
     if (b.n_pipe_press) k_pipe_pressure<<<(b.n_pipe_press + 127) / 128, 128, 0, st>>>(b);

@@ -408,6 +408,7 @@ struct Batch {
   // x of element e at [x * n_elem + e]); allocated when any_rayleigh
   double* RD;
   int any_rayleigh;
+  int any_dynamic;  // a structure has a Dynamic solution step (the tangent kernel then stages inertial terms)
   // reduction chunks: chunk k covers free DOFs [chunk_start[k],
   // chunk_start[k] + GF_RED_CHUNK) of structure chunk_struct[k]
   int n_chunks;
