@@ -1132,7 +1132,8 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       !balloc(B, &b.state, (size_t)n) || !balloc(B, &b.running, 1) ||
       !balloc(B, &b.Ke, (size_t)elem_off * 324) || !balloc(B, &b.Fe, (size_t)elem_off * 18) ||
       !balloc(B, &b.nodeK, (size_t)std::max(node_off, 1) * 9) ||
-      !balloc(B, &b.RD, b.any_rayleigh ? (size_t)elem_off * 324 : 1))
+      !balloc(B, &b.RD, b.any_rayleigh ? (size_t)elem_off * 324 : 1) ||
+      !balloc(B, &b.Dm, b.any_dynamic ? (size_t)elem_off * 18 : 1))
     return GF_ERR_CUDA;
   // reduction chunks of k_residual / k_update
   {

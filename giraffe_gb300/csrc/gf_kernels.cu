@@ -307,11 +307,10 @@ __global__ void k_zero(Batch b) {
 // contiguous.  Elements of one colour share no node, so the scatter needs no
 // atomics and is deterministic.
 constexpr int MOUNT_THREADS = 64;
-// per thread: the two operators (OP_N stored entries each), the internal
-// force (18) and, in batches with Dynamic steps, the two inertial
-// rotational tangents (18); a static batch fits three CTAs on an SM
-constexpr int MOUNT_SMEM_STATIC = (2 * OP_N + 18) * MOUNT_THREADS * (int)sizeof(double);
-constexpr int MOUNT_SMEM = (2 * OP_N + 18 + 18) * MOUNT_THREADS * (int)sizeof(double);
+// per thread: the two operators (OP_N stored entries each) and the internal
+// force (18), so three CTAs fit on an SM; the inertial rotational tangents
+// of Dynamic steps go to the element scratch b.Dm instead
+constexpr int MOUNT_SMEM = (2 * OP_N + 18) * MOUNT_THREADS * (int)sizeof(double);
 
 template <typename TK>
 __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
@@ -332,7 +331,9 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     for (int q = 0; q < 6; ++q) d[6 * j + q] = b.disp[(int64_t)nd[j] * 6 + q];
   BeamInterp ip[2] = {beam_interp(c, d, 0), beam_interp(c, d, 1)};
   double* f = reinterpret_cast<double*>(sM + (size_t)2 * OP_N * MOUNT_THREADS) + tid;
-  double* Dm = f + 18 * MOUNT_THREADS;  // inertial rotational tangents, 2 x 9 (any_dynamic batches)
+  // inertial rotational tangents, 2 x 9, structure-of-arrays like K_e
+  double* Dm = b.Dm + e;
+  const int64_t dms = b.n_elem;
 #pragma unroll
   for (int q = 0; q < 18; ++q) f[q * MOUNT_THREADS] = 0.0;
   const StructParams& pr = b.params[s];
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
     const BeamHistAux& x = b.baux[e];
 #pragma unroll 1
     for (int g = 0; g < 2; ++g)
-      beam_gp_inertia(c, x, ip[g], vel, acc, a6, g, f, MOUNT_THREADS, Dm + (size_t)g * 9 * MOUNT_THREADS, MOUNT_THREADS);
+      beam_gp_inertia(c, x, ip[g], vel, acc, a6, g, f, MOUNT_THREADS, Dm + (int64_t)g * 9 * dms, (int)dms);
     a1Mr = a6[0] * c.Mr;
   }
   // element scratch is structure-of-arrays (entry x of element e at
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
 #pragma unroll 1
     for (int I = 0; I < 3; ++I)
       beam_K_block<TK>(c, sM + tid, sM + OP_N * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ke, dyn, Dm,
-                       Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, a1Mr, ne);
+                       Dm + 9 * dms, (int)dms, a1Mr, ne);
   // Rayleigh damping: on the iterations that form C_e, the stiffness part
   // of K_e alone (no inertial terms) goes to the damping scratch, where
   // k_beam_rayleigh turns it into C_e = alpha M_modal + beta K_e
@@ -406,7 +407,7 @@ __global__ void __launch_bounds__(MOUNT_THREADS) k_beam_tangent(Batch b) {
 #pragma unroll 1
       for (int I = 0; I < 3; ++I)
         beam_K_block<TK>(c, sM + tid, sM + OP_N * MOUNT_THREADS + tid, I, J, MOUNT_THREADS, Ce, false, Dm,
-                         Dm + 9 * MOUNT_THREADS, MOUNT_THREADS, 0.0, ne);
+                         Dm + 9 * dms, (int)dms, 0.0, ne);
   }
 #pragma unroll
   for (int q = 0; q < 18; ++q) b.Fe[q * ne + e] = f[q * MOUNT_THREADS];
@@ -1408,7 +1409,7 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     ProfScope q(prof, st, KC_MOUNT);
     // mixed precision: the tangent operator in FP32-pair arithmetic on the
     // FP32 pipe; kinematics, internal force and everything after stay FP64
-    const int smem = b.any_dynamic ? MOUNT_SMEM : MOUNT_SMEM_STATIC;
+    const int smem = MOUNT_SMEM;
     if (b.mixed)
       k_beam_tangent<f2><<<(b.n_elem + MOUNT_THREADS - 1) / MOUNT_THREADS, MOUNT_THREADS, smem, st>>>(b);
     else

@@ -408,7 +408,10 @@ struct Batch {
   // x of element e at [x * n_elem + e]); allocated when any_rayleigh
   double* RD;
   int any_rayleigh;
-  int any_dynamic;  // a structure has a Dynamic solution step (the tangent kernel then stages inertial terms)
+  int any_dynamic;  // a structure has a Dynamic solution step
+  // inertial rotational tangents of the Beam_1 Gauss points (2 x 9 per
+  // element, structure-of-arrays like Ke); allocated when any_dynamic
+  double* Dm;
   // reduction chunks: chunk k covers free DOFs [chunk_start[k],
   // chunk_start[k] + GF_RED_CHUNK) of structure chunk_struct[k]
   int n_chunks;
