@@ -36,7 +36,7 @@ METRIC = "Newton solves/sec (batched static Beam_1 chains, FP64, converged load 
 UNIT = "Newton solves/s"
 # DRAM bytes per element mount of k_beam_tangent, from one ncu capture on 128
 # chains: (54.9 MB read + 173.1 MB written) / 79,322 elements
-TANGENT_DRAM_BYTES_PER_ELEMENT = (54.875648e6 + 173.070848e6) / 79322
+TANGENT_DRAM_BYTES_PER_ELEMENT = (55.088384e6 + 202.853120e6) / 79322
 
 
 def parse():
