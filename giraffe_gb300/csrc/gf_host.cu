@@ -1003,34 +1003,50 @@ int build_batch(gf_batch* B, int n, const gf_model_desc* models) {
       const StructInfo& inf = B->info[s];
       const int mm = inf.n_elem, M = Mc[s], cbase = cb[s], tbase = tb[s];
       const std::vector<char>& fr = plan[s].node_free;
+      // corner slots: the chain's corners in the order of cyclic reduction,
+      // position 0, then the odd multiples of the largest power of two below
+      // M, ..., then the odd positions; at every level the items eliminated
+      // (the odd multiples of 2^l) are one contiguous run and the surviving
+      // ones the run before it, so a level's loads are contiguous in the
+      // structure-of-arrays scratch
+      std::vector<int> slot(std::max(M, 1));
+      {
+        int r = 0;
+        if (M > 0) slot[0] = r++;
+        int hmax = 1;
+        while (hmax * 2 < M) hmax *= 2;
+        for (int h = hmax; h >= 1 && M > 1; h /= 2)
+          for (int kp = h; kp < M; kp += 2 * h) slot[kp] = r++;
+      }
       std::vector<int> pos(mm + 1, -1);
       for (int ci = 0, k = 0; ci <= mm; ++ci)
-        if (fr[2 * ci]) pos[ci] = k++;
+        if (fr[2 * ci]) pos[ci] = slot[k++];
       for (int e = 0; e < mm; ++e) {
         elem_list[tbase + e] = inf.elem_off + e;
         eca[tbase + e] = pos[e] >= 0 ? cbase + pos[e] : -1;
         ecb[tbase + e] = pos[e + 1] >= 0 ? cbase + pos[e + 1] : -1;
       }
-      for (int ci = 0; ci <= mm; ++ci) {
+      for (int ci = 0, k = 0; ci <= mm; ++ci) {
         if (pos[ci] < 0) continue;
-        const int k = pos[ci], c = cbase + k;
+        const int c = cbase + pos[ci];
         cnode[c] = inf.node_off + 2 * ci;
         cstruct[c] = s;
         cleft[c] = ci >= 1 ? tbase + ci - 1 : -1;
         cright[c] = ci < mm ? tbase + ci : -1;
-        cprev[c] = k > 0 ? cbase + k - 1 : -1;
-        cnext[c] = k + 1 < M ? cbase + k + 1 : -1;
+        cprev[c] = k > 0 ? cbase + slot[k - 1] : -1;
+        cnext[c] = k + 1 < M ? cbase + slot[k + 1] : -1;
+        ++k;
       }
-      if (rpos[s] >= 0) roots[rpos[s]] = cbase;
+      if (rpos[s] >= 0) roots[rpos[s]] = cbase + slot[0];
       int l = 0;
       for (int h = 1; h < M; h *= 2, ++l) {
         CrItem* o = &odd[cd.odd_off[l] + opos[(size_t)s * NL + l]];
         for (int kp = h; kp < M; kp += 2 * h)
-          *o++ = CrItem{cbase + kp, cbase + kp - h, kp + h < M ? cbase + kp + h : -1, s};
+          *o++ = CrItem{cbase + slot[kp], cbase + slot[kp - h], kp + h < M ? cbase + slot[kp + h] : -1, s};
         CrItem* v = &even[cd.even_off[l] + epos[(size_t)s * NL + l]];
         for (int kp = 0; kp < M; kp += 2 * h) {
           bool hp = kp - h >= 0, hn = kp + h < M;
-          *v++ = CrItem{cbase + kp, hp ? cbase + kp - h : -1, hn ? cbase + kp + h : -1, s};
+          *v++ = CrItem{cbase + slot[kp], hp ? cbase + slot[kp - h] : -1, hn ? cbase + slot[kp + h] : -1, s};
         }
       }
     });
