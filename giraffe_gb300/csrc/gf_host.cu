@@ -1252,6 +1252,7 @@ gf_ctx* gf_create(int device) {
 void gf_destroy(gf_ctx* ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pin) cudaFreeHost(ctx->pin);
   delete ctx;
 }
 
@@ -1699,9 +1700,20 @@ int gf_batch_results(gf_batch* B, double* const* final_nodes, gf_stats* stats) {
       stats[s] = z;
     }
   if (final_nodes) {
-    hvec<double> copy((size_t)b.n_nodes * 6), Qn((size_t)b.n_nodes * 9);
-    CK(cudaMemcpy(copy.data(), b.copy, sizeof(double) * copy.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(Qn.data(), b.Qn, sizeof(double) * Qn.size(), cudaMemcpyDeviceToHost));
+    // through the context's pinned staging (a pageable copy when none)
+    const size_t nc = (size_t)b.n_nodes * 6, nq = (size_t)b.n_nodes * 9;
+    hvec<double> hc, hq;
+    double* copy = static_cast<double*>(ctx->pinned(sizeof(double) * (nc + nq)));
+    double* Qn = copy ? copy + nc : nullptr;
+    if (!copy) {
+      hc.resize(nc);
+      hq.resize(nq);
+      copy = hc.data();
+      Qn = hq.data();
+    }
+    CK(cudaMemcpyAsync(copy, b.copy, sizeof(double) * nc, cudaMemcpyDeviceToHost, B->stream));
+    CK(cudaMemcpyAsync(Qn, b.Qn, sizeof(double) * nq, cudaMemcpyDeviceToHost, B->stream));
+    CK(cudaStreamSynchronize(B->stream));
     parallel_structures(n, (size_t)b.n_nodes, [&](int s) {
       double* o = final_nodes[s];
       if (!o) return;

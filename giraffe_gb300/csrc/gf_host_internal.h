@@ -23,6 +23,23 @@ struct gf_ctx {
   int wide_update = GF_WIDE_TENSOR;
   // the autotuner's wide-band tile shapes, per half-bandwidth and update kind
   std::map<long long, gf::WideTiles> tiles;
+  // pinned staging of gf_batch_results' read-back (grown on demand, freed
+  // with the context)
+  void* pin = nullptr;
+  size_t pin_bytes = 0;
+  // a pinned block of at least n bytes, or nullptr when none can be had
+  void* pinned(size_t n) {
+    if (n <= pin_bytes) return pin;
+    if (pin) cudaFreeHost(pin);
+    pin = nullptr;
+    pin_bytes = 0;
+    if (cudaMallocHost(&pin, n) != cudaSuccess) {
+      pin = nullptr;
+      return nullptr;
+    }
+    pin_bytes = n;
+    return pin;
+  }
 };
 
 // First-fit sub-allocator over one allocation (the served path's device
