@@ -1300,17 +1300,7 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
     ctx->err = e.empty() ? "gf_batch_create failed" : e;
     return nullptr;
   }
-  if (B->opts.use_graph) {
-    // the device-side pass loop of the captured pass
-    if (cudaMalloc(&B->d_loop, 2 * sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(&B->h_loop, 2 * sizeof(int)) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&B->loop_stream, cudaStreamNonBlocking) != cudaSuccess) {
-      gf_batch_destroy(B);
-      set_err(ctx, "gf_batch_create: pass-loop buffers");
-      return nullptr;
-    }
-  }
-  B->launches_per_pass = count_launches_per_pass(B) + (B->d_loop ? 1 : 0);  // + the loop check
+  B->launches_per_pass = count_launches_per_pass(B);
   B->host_ms[0] = host_now_ms() - t0 - B->host_ms[1] - B->host_ms[2];
   return B;
 }
@@ -1318,9 +1308,6 @@ gf_batch* gf_batch_create(gf_ctx* ctx, int n, const gf_model_desc* models, const
 void gf_batch_destroy(gf_batch* B) {
   if (!B) return;
   if (B->graph) cudaGraphExecDestroy(B->graph);
-  if (B->d_loop) cudaFree(B->d_loop);
-  if (B->h_loop) cudaFreeHost(B->h_loop);
-  if (B->loop_stream) cudaStreamDestroy(B->loop_stream);
   for (auto& a : B->b.sh.aux)
     if (a) cudaStreamDestroy(a);
   for (auto& e : B->b.sh.evt)
@@ -1356,27 +1343,8 @@ int ensure_graph(gf_batch* B) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     wide_capture_error();  // clear
-    cudaError_t ce = cudaSuccess;
-    if (B->d_loop) {
-      // passes in a device-side loop: a WHILE node whose body is one pass and
-      // the loop check, so one launch runs up to d_loop[1] passes and stops
-      // when no structure runs
-      cudaGraphConditionalHandle h;
-      cudaGraph_t body = nullptr, done = nullptr;
-      launch_loop_begin(B->d_loop, st);
-      ce = capture_while(st, &h, &body);
-      if (ce == cudaSuccess)
-        ce = cudaStreamBeginCaptureToGraph(B->loop_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-      if (ce == cudaSuccess) {
-        launch_iteration(B->b, B->loop_stream);
-        launch_loop_check(B->b, B->d_loop, h, B->loop_stream);
-        ce = cudaStreamEndCapture(B->loop_stream, &done);
-      }
-    } else {
-      launch_iteration(B->b, st);
-    }
-    const cudaError_t we = wide_capture_error();
-    if (ce == cudaSuccess) ce = we;
+    launch_iteration(B->b, st);
+    const cudaError_t ce = wide_capture_error();
     CK(cudaStreamEndCapture(st, &g));
     if (ce != cudaSuccess) {
       cudaGraphDestroy(g);
@@ -1401,27 +1369,6 @@ int run_passes(gf_batch* B, long long* passes_out, LaunchProf* prof = nullptr) {
   const Batch& b = B->b;
   long long passes = 0;
   const long long cap = B->opts.max_passes > 0 ? B->opts.max_passes : 4000000;
-  if (B->graph && B->d_loop && !prof) {
-    // one graph launch runs up to chunk passes on the device, stopping when
-    // no structure runs; the host reads the pass count and the running flag
-    const long long chunk = 64LL * std::max(B->opts.poll_every, 1);
-    for (;;) {
-      B->h_loop[1] = (int)std::min(chunk, cap - passes);
-      CK(cudaMemcpyAsync(B->d_loop + 1, B->h_loop + 1, sizeof(int), cudaMemcpyHostToDevice, st));
-      CK(cudaGraphLaunch(B->graph, st));
-      CK(cudaMemcpyAsync(B->h_loop, B->d_loop, sizeof(int), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(B->h_running, b.running, sizeof(int), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      passes += B->h_loop[0];
-      if (*B->h_running == 0) break;
-      if (passes >= cap) {
-        set_err(ctx, "gf_batch_run: %lld Newton passes without completion", passes);
-        return GF_ERR_TIMEOUT;
-      }
-    }
-    *passes_out = passes;
-    return GF_OK;
-  }
   for (;;) {
     for (int k = 0; k < B->opts.poll_every; ++k) {
       if (B->graph && !prof) {
@@ -1486,19 +1433,11 @@ int gf_batch_step(gf_batch* B, int max_passes, int* running) {
   cudaStream_t st = B->stream;
   int r = ensure_graph(B);
   if (r != GF_OK) return r;
-  if (B->graph && B->d_loop) {
-    // up to max_passes passes on the device, fewer when every structure has
-    // finished (the passes left would change nothing)
-    B->h_loop[1] = max_passes;
-    CK(cudaMemcpyAsync(B->d_loop + 1, B->h_loop + 1, sizeof(int), cudaMemcpyHostToDevice, st));
-    CK(cudaGraphLaunch(B->graph, st));
-  } else {
-    for (int k = 0; k < max_passes; ++k) {
-      if (B->graph) {
-        CK(cudaGraphLaunch(B->graph, st));
-      } else {
-        launch_iteration(B->b, st);
-      }
+  for (int k = 0; k < max_passes; ++k) {
+    if (B->graph) {
+      CK(cudaGraphLaunch(B->graph, st));
+    } else {
+      launch_iteration(B->b, st);
     }
   }
   CK(cudaGetLastError());

@@ -158,12 +158,6 @@ struct gf_batch {
   // zero): x, y, z and the start time
   std::vector<double> mon_first;
   cudaGraphExec_t graph = nullptr;
-  // the device-side pass loop of a batch's graph (not served waves): [0]
-  // passes of the last launch, [1] the launch's pass limit; pinned mirror;
-  // the stream its body is captured on
-  int* d_loop = nullptr;
-  int* h_loop = nullptr;
-  cudaStream_t loop_stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   long long last_launches = 0;

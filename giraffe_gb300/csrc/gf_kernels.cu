@@ -1374,20 +1374,6 @@ void launch_assembly(const Batch& b_in, cudaStream_t st) {
 
 void launch_increment(const Batch& b, cudaStream_t st) { k_update<<<b.n_chunks, 256, 0, st>>>(b); }
 
-namespace {
-__global__ void k_loop_begin(int* loop) { loop[0] = 0; }
-__global__ void k_loop_check(const int* running, int* loop, cudaGraphConditionalHandle h) {
-  const int c = loop[0] + 1;
-  loop[0] = c;
-  cudaGraphSetConditional(h, (*running != 0 && c < loop[1]) ? 1u : 0u);
-}
-}  // namespace
-
-void launch_loop_begin(int* loop, cudaStream_t st) { k_loop_begin<<<1, 1, 0, st>>>(loop); }
-void launch_loop_check(const Batch& b, int* loop, cudaGraphConditionalHandle h, cudaStream_t st) {
-  k_loop_check<<<1, 1, 0, st>>>(b.running, loop, h);
-}
-
 void launch_commit(const Batch& b, cudaStream_t st) {
   if (b.n_elem) k_commit_elems<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
   if (b.sh.n_shells) launch_shell_commit(b, st);

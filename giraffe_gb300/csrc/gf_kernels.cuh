@@ -110,15 +110,6 @@ void launch_wide_subst(const Batch& b, int nrhs, cudaStream_t st);
 // The first error of a wide-band capture step (a conditional node or body
 // capture) since the last call on this thread; clears it.
 cudaError_t wide_capture_error();
-// A WHILE node appended to the capture of st (condition 1 at every launch);
-// *body receives its body graph.
-cudaError_t capture_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_t* body);
-// The device-side pass loop of a batch's graph: loop[0] counts the passes
-// of the current launch (launch_loop_begin zeroes it), loop[1] is the launch's
-// pass limit; launch_loop_check ends a pass and keeps the loop going while a
-// structure runs and the limit is not reached.
-void launch_loop_begin(int* loop, cudaStream_t st);
-void launch_loop_check(const Batch& b, int* loop, cudaGraphConditionalHandle h, cudaStream_t st);
 // The modal mass (MountMassModal) of every element added into a band of the
 // structure's layout: entry (i, j) at (kw + i - j) + j W.
 void launch_modal_mass(const Batch& b, double* M, int64_t W, int kw, cudaStream_t st);

@@ -1548,13 +1548,6 @@ static cudaError_t capture_wide_loops(const Batch& b, cudaStream_t st) {
   return cudaStreamEndCapture(sb, &done);
 }
 
-// A WHILE node appended to the capture of st, its condition 1 at every
-// launch of the graph; *body receives the node's body graph (for a capture
-// of the body on another stream).
-cudaError_t capture_while(cudaStream_t st, cudaGraphConditionalHandle* h, cudaGraph_t* body) {
-  return add_while(st, h, body);
-}
-
 // The first error of a wide-band capture step on this thread (a failed
 // conditional node or body capture), which the capturing caller reports:
 // capture_error() returns it and clears it.

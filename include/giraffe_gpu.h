@@ -77,10 +77,7 @@ typedef struct gf_solve_opts {
                       refining after max_refine sweeps, is refactored in FP64
                       (reference: src/SparseMatrix.cpp:74-166, PARDISO with
                       iterative refinement) */
-  int poll_every;  /* Newton passes between host checks for completion; with
-                      use_graph the pass loop runs on the device (a graph
-                      WHILE node), one launch running up to 64 x poll_every
-                      passes and stopping when no structure runs */
+  int poll_every;  /* Newton passes between host checks for completion */
   int use_graph;   /* capture one Newton pass as a CUDA graph */
   int wide_update; /* Shell_1 wide-band LU trailing update: GF_WIDE_TENSOR (the
                       default: FP64 products emulated from exact bf16 slices
