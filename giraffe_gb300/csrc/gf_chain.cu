@@ -129,21 +129,28 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   for (int i = 0; i < 6; ++i)
 #pragma unroll 1
     for (int q = 0; q < 13; ++q) ELM(c.ez, t, i * 13 + q) = R[(i * NRHS + q) * CT];
-  // -A_as Z and -A_bs Z (6 x 13 each)
+  // -A_as Z and -A_bs Z (6 x 13 each): a side's 6x6 block of K in
+  // registers, each column of Z read once from shared memory for all six
+  // rows (the same FMA chain over j for every entry)
 #pragma unroll 1
   for (int side = 0; side < 2; ++side) {
     bool free_side = side ? fb : fa;
     const int r0 = side ? 12 : 0;
-#pragma unroll 1
-    for (int i = 0; i < 6; ++i) {
-      double row[6];
+    double A[36];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) row[j] = free_side ? K((r0 + i) + 18 * (6 + j)) : 0.0;
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) A[i * 6 + j] = free_side ? K((r0 + i) + 18 * (6 + j)) : 0.0;
 #pragma unroll 1
-      for (int q = 0; q < 13; ++q) {
+    for (int q = 0; q < 13; ++q) {
+      double z[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) z[j] = R[(j * NRHS + q) * CT];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
         double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc = fma(row[j], R[(j * NRHS + q) * CT], acc);
+        for (int j = 0; j < 6; ++j) acc = fma(A[i * 6 + j], z[j], acc);
         ELM(c.ec, t, i * 26 + side * 13 + q) = -acc;
       }
     }
