@@ -1,7 +1,9 @@
 // Chain solver kernels (see gf_chain.cuh).  One thread per item (element or
 // corner): every FP64 warp instruction carries 32 independent items, which is
-// what the FP64 unit's throughput needs; the 6x19 augmented matrices of the
-// small dense solves are staged in shared memory.
+// what the FP64 unit's throughput needs.  The small dense solves factor the
+// 6x6 pivot block in registers (reciprocals and multipliers kept there too)
+// and then take the right-hand sides one column at a time, so no kernel here
+// uses shared memory.
 #include <cuda_runtime.h>
 
 #include "gf_chain.cuh"
@@ -41,49 +43,51 @@ __device__ __forceinline__ double recip(double p) {
   return r;
 }
 
-// Gauss-Jordan on a thread's augmented matrix [D | R]: D (6x6, row-major)
-// in registers, every index static under the full unroll, and the NR
-// right-hand sides R in shared memory (entry (r, c) at R[(r * NR + c) * CT]).
-// On return R holds D^{-1} R.  No pivoting; returns false on a zero or
-// non-finite pivot.  Only R takes shared memory (624 B per thread for 13
-// columns, against 912 B for the whole 6 x 19 system), so more CTAs share an
-// SM; the independent column updates of one pivot step overlap.
-template <int NR>
-__device__ bool gauss_jordan6(double (&D)[36], double* R) {
+// Gauss-Jordan on a thread's augmented matrix [D | R] in two phases, both in
+// registers: gj6_factor eliminates D (6x6, row-major, every index static under
+// the full unroll) and records each pivot's reciprocal and multipliers;
+// gj6_apply then takes one right-hand-side column through the same steps in
+// the same order (r_k *= 1/p_k, then r_i -= m_ik r_k), so each column needs
+// its six entries only and no shared memory.  The operations on every entry
+// are those of the joined elimination.  No pivoting; gj6_factor returns false
+// on a zero or non-finite pivot.
+__device__ __forceinline__ bool gj6_factor(double (&D)[36], double (&inv)[6], double (&mult)[36]) {
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     const double p = D[k * 6 + k];
     if (!(p != 0.0) || !isfinite(p)) ok = false;
-    const double inv = recip(p);
-    double dk[6], rk[NR];
+    inv[k] = recip(p);
+    double dk[6];
 #pragma unroll
     for (int c = k + 1; c < 6; ++c) {
-      dk[c] = D[k * 6 + c] * inv;
+      dk[c] = D[k * 6 + c] * inv[k];
       D[k * 6 + c] = dk[c];
-    }
-#pragma unroll
-    for (int c = 0; c < NR; ++c) {
-      rk[c] = R[(k * NR + c) * CT] * inv;
-      R[(k * NR + c) * CT] = rk[c];
     }
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
       if (i == k) continue;
       const double m = D[i * 6 + k];
+      mult[k * 6 + i] = m;
 #pragma unroll
       for (int c = k + 1; c < 6; ++c) D[i * 6 + c] = fma(-m, dk[c], D[i * 6 + c]);
-#pragma unroll
-      for (int c = 0; c < NR; ++c) R[(i * NR + c) * CT] = fma(-m, rk[c], R[(i * NR + c) * CT]);
     }
   }
   return ok;
 }
-constexpr int NRHS = 13;  // right-hand sides of the chain eliminations: b, then 6 + 6 coupling columns
+__device__ __forceinline__ void gj6_apply(const double (&inv)[6], const double (&mult)[36], double (&r)[6]) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double rk = r[k] * inv[k];
+    r[k] = rk;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      if (i != k) r[i] = fma(-mult[k * 6 + i], rk, r[i]);
+  }
+}
 
 // ---- 1. condensation of the midside node of every chain element ----
 __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
-  extern __shared__ double smem[];
   int t = blockIdx.x * CT + threadIdx.x;
   if (t >= c.n_chain_elems) return;
   int e = c.elem_list[t];
@@ -91,8 +95,7 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
   if (!solving(b, s)) return;
   const StructInfo inf = b.info[s];
   const double* P = b.P + inf.dof_off;
-  double* R = smem + threadIdx.x;  // [P_m | K_ma | K_mb], 6 x 13
-  double D[36];                     // K_mm (+ the load stiffness)
+  double D[36];  // K_mm (+ the load stiffness)
   // K of the chain comes from the element tangents (column-major 18x18,
   // DOFs of the first corner, the midside node, the last corner) plus the
   // nodal load stiffness of the midside node: the midside rows belong to
@@ -115,42 +118,32 @@ __global__ void __launch_bounds__(CT) k_condense(Batch b, ChainData c) {
       D[i * 6 + j] = kmm;
     }
   }
+  double inv[6], mult[36];
+  if (!gj6_factor(D, inv, mult)) b.state[s].info_fail = 1;
+  // Z = K_mm^-1 [P_m | K_ma | K_mb] a column at a time, and with each column
+  // its share of -A_as Z and -A_bs Z (6 x 13 each: the same FMA chain over j
+  // for every entry)
 #pragma unroll 1
-  for (int i = 0; i < 6; ++i) {
-#pragma unroll 1
-    for (int j = 0; j < 6; ++j) {
-      R[(i * NRHS + 1 + j) * CT] = fa ? K((6 + i) + 18 * j) : 0.0;
-      R[(i * NRHS + 7 + j) * CT] = fb ? K((6 + i) + 18 * (12 + j)) : 0.0;
+  for (int q = 0; q < 13; ++q) {
+    double r[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      if (q == 0) r[i] = P[gm[i]];
+      else if (q < 7) r[i] = fa ? K((6 + i) + 18 * (q - 1)) : 0.0;
+      else r[i] = fb ? K((6 + i) + 18 * (12 + q - 7)) : 0.0;
     }
-    R[(i * NRHS) * CT] = P[gm[i]];
-  }
-  if (!gauss_jordan6<NRHS>(D, R)) b.state[s].info_fail = 1;
-#pragma unroll 1
-  for (int i = 0; i < 6; ++i)
-#pragma unroll 1
-    for (int q = 0; q < 13; ++q) ELM(c.ez, t, i * 13 + q) = R[(i * NRHS + q) * CT];
-  // -A_as Z and -A_bs Z (6 x 13 each): a side's 6x6 block of K in
-  // registers, each column of Z read once from shared memory for all six
-  // rows (the same FMA chain over j for every entry)
-#pragma unroll 1
-  for (int side = 0; side < 2; ++side) {
-    bool free_side = side ? fb : fa;
-    const int r0 = side ? 12 : 0;
-    double A[36];
+    gj6_apply(inv, mult, r);
 #pragma unroll
-    for (int i = 0; i < 6; ++i)
+    for (int i = 0; i < 6; ++i) ELM(c.ez, t, i * 13 + q) = r[i];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) A[i * 6 + j] = free_side ? K((r0 + i) + 18 * (6 + j)) : 0.0;
-#pragma unroll 1
-    for (int q = 0; q < 13; ++q) {
-      double z[6];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) z[j] = R[(j * NRHS + q) * CT];
+    for (int side = 0; side < 2; ++side) {
+      const bool free_side = side ? fb : fa;
+      const int r0 = side ? 12 : 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
         double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc = fma(A[i * 6 + j], z[j], acc);
+        for (int j = 0; j < 6; ++j) acc = fma(free_side ? K((r0 + i) + 18 * (6 + j)) : 0.0, r[j], acc);
         ELM(c.ec, t, i * 26 + side * 13 + q) = -acc;
       }
     }
@@ -204,37 +197,37 @@ __global__ void k_corner_system(Batch b, ChainData c) {
 
 // ---- 3. cyclic reduction: eliminate odd positions ----
 __global__ void __launch_bounds__(CT) k_cr_eliminate(Batch b, ChainData c, int lo, int hi) {
-  extern __shared__ double smem[];
   int t = lo + blockIdx.x * CT + threadIdx.x;
   if (t >= hi) return;
   CrItem it = c.odd[t];
   if (!solving(b, it.structure)) return;
   int k = it.corner;
-  double* R = smem + threadIdx.x;  // [b | L | U], 6 x 13
   double D[36];
 #pragma unroll
   for (int q = 0; q < 36; ++q) D[q] = CRN(c.cD, k, q);
+  double inv[6], mult[36];
+  if (!gj6_factor(D, inv, mult)) b.state[it.structure].info_fail = 1;
+  // Z = D^-1 [b | L | U], a column at a time
 #pragma unroll 1
-  for (int i = 0; i < 6; ++i) {
+  for (int q = 0; q < 13; ++q) {
+    double r[6];
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      R[(i * NRHS + 1 + j) * CT] = it.prev >= 0 ? CRN(c.cL, k, i * 6 + j) : 0.0;
-      R[(i * NRHS + 7 + j) * CT] = it.next >= 0 ? CRN(c.cU, k, i * 6 + j) : 0.0;
+    for (int i = 0; i < 6; ++i) {
+      if (q == 0) r[i] = CRN(c.cb, k, i);
+      else if (q < 7) r[i] = it.prev >= 0 ? CRN(c.cL, k, i * 6 + q - 1) : 0.0;
+      else r[i] = it.next >= 0 ? CRN(c.cU, k, i * 6 + q - 7) : 0.0;
     }
-    R[(i * NRHS) * CT] = CRN(c.cb, k, i);
+    gj6_apply(inv, mult, r);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) CRN(c.cz, k, i * 13 + q) = r[i];
   }
-  if (!gauss_jordan6<NRHS>(D, R)) b.state[it.structure].info_fail = 1;
-#pragma unroll 1
-  for (int i = 0; i < 6; ++i)
-#pragma unroll 1
-    for (int q = 0; q < 13; ++q) CRN(c.cz, k, i * 13 + q) = R[(i * NRHS + q) * CT];
 }
 
 // Warp-per-item form of k_cr_eliminate for the small levels near the top of
 // the reduction, where one item per thread would leave most of the FP64
 // units idle: lane q holds column q of the augmented 6 x 19 matrix
 // [D | b | L | U] in registers and the pivot column is broadcast by shuffle.
-// The arithmetic is the same sequence as gauss_jordan6 (same products and
+// The arithmetic is the same sequence as gj6_factor / gj6_apply (same products and
 // FMAs on every entry), so both forms give the same bits.
 __global__ void k_cr_eliminate_w(Batch b, ChainData c, int lo, int hi) {
   const int lane = threadIdx.x & 31;
@@ -342,19 +335,21 @@ __global__ void k_cr_update_w(Batch b, ChainData c, int lo, int hi) {
 
 // ---- 3c. the last position of each chain ----
 __global__ void __launch_bounds__(CT) k_cr_root(Batch b, ChainData c) {
-  extern __shared__ double smem[];
   int t = blockIdx.x * CT + threadIdx.x;
   if (t >= c.n_roots) return;
   int k = c.roots[t];
   int s = c.corner_struct[k];
   if (!solving(b, s)) return;
-  double* R = smem + threadIdx.x;  // b, 6 x 1
-  double D[36];
+  double D[36], r[6];
 #pragma unroll
   for (int q = 0; q < 36; ++q) D[q] = CRN(c.cD, k, q);
-  for (int i = 0; i < 6; ++i) R[i * CT] = CRN(c.cb, k, i);
-  if (!gauss_jordan6<1>(D, R)) b.state[s].info_fail = 1;
-  for (int i = 0; i < 6; ++i) CRN(c.cx, k, i) = R[i * CT];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r[i] = CRN(c.cb, k, i);
+  double inv[6], mult[36];
+  if (!gj6_factor(D, inv, mult)) b.state[s].info_fail = 1;
+  gj6_apply(inv, mult, r);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) CRN(c.cx, k, i) = r[i];
 }
 
 // ---- 4. back substitution: x = Zb - ZL x_prev - ZU x_next ----
@@ -423,16 +418,7 @@ __global__ void k_corner_scatter(Batch b, ChainData c) {
 
 void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
   if (c.n_chain_elems == 0) return;
-  const int smem = 6 * NRHS * CT * (int)sizeof(double);
-  // once per process (a function-local static is initialised by one thread)
-  static const bool attr = [smem] {
-    cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_cr_eliminate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_cr_root, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    return true;
-  }();
-  (void)attr;
-  k_condense<<<(c.n_chain_elems + CT - 1) / CT, CT, smem, st>>>(b, c);
+  k_condense<<<(c.n_chain_elems + CT - 1) / CT, CT, 0, st>>>(b, c);
   if (c.n_corners > 0) {
     k_corner_system<<<(c.n_corners + 127) / 128, 128, 0, st>>>(b, c);
     // levels with fewer items than ~8 per FP64 unit take the lane-parallel
@@ -440,14 +426,14 @@ void launch_chain_solve(const Batch& b, const ChainData& c, cudaStream_t st) {
     const int small = 152 * 4 * 8;
     for (int l = 0; l < c.n_levels; ++l) {
       int lo = c.odd_off[l], hi = c.odd_off[l + 1];
-      if (hi - lo >= small) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, smem, st>>>(b, c, lo, hi);
+      if (hi - lo >= small) k_cr_eliminate<<<(hi - lo + CT - 1) / CT, CT, 0, st>>>(b, c, lo, hi);
       else if (hi > lo) k_cr_eliminate_w<<<(hi - lo + 3) / 4, 128, 0, st>>>(b, c, lo, hi);
       // the update runs row-per-lane at every level: the same FP64
       // instruction count as one item per thread, six times the warps
       int elo = c.even_off[l], ehi = c.even_off[l + 1];
       if (ehi > elo) k_cr_update_w<<<(ehi - elo + 19) / 20, 128, 0, st>>>(b, c, elo, ehi);
     }
-    k_cr_root<<<(c.n_roots + CT - 1) / CT, CT, smem, st>>>(b, c);
+    k_cr_root<<<(c.n_roots + CT - 1) / CT, CT, 0, st>>>(b, c);
     for (int l = c.n_levels - 1; l >= 0; --l) {
       int lo = c.odd_off[l], hi = c.odd_off[l + 1];
       if (hi > lo) k_cr_back<<<(hi - lo + 19) / 20, 128, 0, st>>>(b, c, lo, hi);
