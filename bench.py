@@ -68,7 +68,7 @@ def parse():
                          "mma.sync comparisons run the first two")
     ap.add_argument("--dyn-steps", type=int, default=1000,
                     help="time steps (of 1000) of the batched-dynamics leg (0 = skip)")
-    ap.add_argument("--rollup", type=int, default=1, help="time the 20-element roll-up (config 1) (0 = skip)")
+    ap.add_argument("--rollup", type=int, default=1, help="time the 20-element cantilever roll-up (0 = skip)")
     ap.add_argument("--serve-saturated", type=int, default=1,
                     help="the 512-chain workload submitted at once through the server (0 = skip)")
     ap.add_argument("--serve-full-requests", type=int, default=12,
@@ -378,8 +378,8 @@ def shell_leg(ctx, args, fp64_peak):
               "info": int(info), "lu_tflops_end_to_end": 2.0 * n_sp * kl_sp * kl_sp / t_sp / 1e12,
               "note": "host CSR in, x out; includes the RCM trial, CSR upload, scatter, factor and "
                       "substitutions (2 n kl^2 flops counted)"}
-    # spec precision pattern: FP32 band factor with FP64 iterative
-    # refinement (GF_PREC_MIXED), the same plate and load steps
+    # FP32 band factor with FP64 iterative refinement (GF_PREC_MIXED), the
+    # same plate and load steps
     sm_ = configs.square_plate(args.shell_n, steps=20)
     sm_.solution.end_time = args.shell_steps / 20.0
     bm = gpu.BatchSolver(ctx, [sm_], ctx.opts(gpu.GF_PREC_MIXED))
@@ -476,7 +476,7 @@ def dynamics_leg(ctx, args):
 
 
 def rollup_leg(ctx):
-    """Config 1: the 20-element cantilever rolled into a circle by a tip
+    """The 20-element cantilever rolled into a circle by a tip
     moment over 20 load steps (plain FP64 path, one structure), device time
     after a warm-up run, beside the oracle on one host core."""
     from giraffe_gb300 import configs, gpu
@@ -504,10 +504,10 @@ def rollup_leg(ctx):
 
 
 def served_saturated_leg(ctx, args, structs, plain_value):
-    """Config 2 through the server: all 512 chains submitted at once, the
-    server admitting them in waves under its budget; sustained Newton solves
-    per second from the first submission to the last result, against the
-    plain single-structure path."""
+    """The 512-chain batched-static workload through the server: all chains
+    submitted at once, the server admitting them in waves under its budget;
+    sustained Newton solves per second from the first submission to the last
+    result, against the plain single-structure path."""
     from giraffe_gb300 import serve
 
     srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30)
@@ -520,8 +520,8 @@ def served_saturated_leg(ctx, args, structs, plain_value):
          "aborted": int(sum(x.stats[3] for x in res))}
     if plain_value:
         r["over_plain_single_structure"] = r["solves_per_s"] / plain_value
-    # the benchmark spec's batched mixed-precision served path: the same
-    # submission with every wave built with GF_PREC_MIXED
+    # the batched mixed-precision served path: the same submission with
+    # every wave built with GF_PREC_MIXED
     from giraffe_gb300 import gpu
     srv = serve.Server(ctx, hbm_budget=args.serve_budget_gb << 30, precision=gpu.GF_PREC_MIXED)
     outm = serve.run_stream(srv, structs, np.zeros(len(structs)))
@@ -536,9 +536,9 @@ def served_saturated_leg(ctx, args, structs, plain_value):
 
 
 def served_full_leg(ctx, args, rank):
-    """Config 5 with the description's full plate range: 70 % pipe chains
-    (1k-50k DOF), 30 % Shell_1 plates of 10k-200k DOF (log-uniform), Poisson
-    arrivals at 200/s.  One GPU cannot sustain the plates' share of the
+    """The mixed served stream with plates over the full DOF range: 70 % pipe
+    chains (1k-50k DOF), 30 % Shell_1 plates of 10k-200k DOF (log-uniform),
+    Poisson arrivals at 200/s.  One GPU cannot sustain the plates' share of the
     offered load; the leg reports what it sustains and the queueing."""
     from giraffe_gb300 import configs, serve
 
@@ -803,8 +803,8 @@ def run_ours(args, rank, world):
                 "serving": serving,
                 "serving_mixed": serving_mixed,
                 "serving_full_plate_range": serving_full,
-                "serving_saturated_config2": saturated,
-                "rollup_config1": rollup,
+                "serving_saturated_512_chains": saturated,
+                "rollup_20_elements": rollup,
                 "cpu_baseline": cpu,
                 "parity_vs_oracle": parity}
         print(json.dumps(line), flush=True)

@@ -1,6 +1,6 @@
 /*
  * Banded LU with partial pivoting in LAPACK general-band (GB) storage, FP64.
- * TEST INFRASTRUCTURE (oracle): the checker's linear solver, never shipped on
+ * TEST INFRASTRUCTURE (oracle): the oracle's linear solver, never shipped on
  * the product path.
  *
  * Storage follows the reference's BandMatrix (reference src/BandMatrix.cpp:

@@ -1,7 +1,7 @@
 """Builds the CPU oracle library oracle/liboracle.so with gcc.
 
-TEST INFRASTRUCTURE: the oracle is the parity checker and the timed CPU
-baseline; the product never loads it.  FMA contraction is disabled so the
+TEST INFRASTRUCTURE: the oracle gives the parity tests' reference values and
+the timed CPU baseline; the product never loads it.  FMA contraction is disabled so the
 same sources give the same bits on x86-64 and aarch64 hosts.
 """
 import os

@@ -1,6 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so).
 
-TEST INFRASTRUCTURE: the checker and the timed CPU baseline; never used by
+TEST INFRASTRUCTURE: the values the CUDA path is tested against and the
+timed CPU baseline; never used by
 the product path.
 """
 from __future__ import annotations

@@ -1,6 +1,7 @@
 /*
  * Beam_1 element, CPU restatement.  TEST INFRASTRUCTURE (oracle): the
- * checker for the CUDA element kernels and part of the timed CPU baseline.
+ * reference values for the CUDA element kernels and part of the timed CPU
+ * baseline.
  *
  * Follows reference src/Beam_1.cpp: PreCalc 501-692 (constitutive matrix,
  * transformation, Gauss points, shape functions), Mount 695-835 (incremental

@@ -1,6 +1,6 @@
 /*
- * Shared helpers of the CPU oracle.  TEST INFRASTRUCTURE: the oracle is the
- * checker for the CUDA path and the timed CPU baseline; only tests/, the
+ * Shared helpers of the CPU oracle.  TEST INFRASTRUCTURE: the oracle gives
+ * the values the CUDA path is tested against and the timed CPU baseline; only tests/, the
  * smoke check and bench.py's CPU legs load it.  It is a plain restatement of
  * the reference's algorithm, not part of the product.
  *

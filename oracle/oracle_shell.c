@@ -1,6 +1,6 @@
 /*
  * Shell_1 element, CPU restatement.  TEST INFRASTRUCTURE (oracle): the
- * checker for the CUDA Shell_1 path.
+ * reference values the CUDA Shell_1 path is tested against.
  *
  * Follows reference src/Shell_1.cpp:
  *   1666-2365  PreCalc (local frame, Lame constants, drilling stiffness,

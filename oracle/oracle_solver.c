@@ -1,6 +1,7 @@
 /*
  * Static solution of one structure, CPU restatement.  TEST INFRASTRUCTURE
- * (oracle): the checker for the CUDA solver and the timed CPU baseline.
+ * (oracle): the reference values for the CUDA solver and the timed CPU
+ * baseline.
  *
  * Follows, for Beam_1 structures with nodal loads, constraints and prescribed
  * displacements:

@@ -3,7 +3,8 @@
  * (oracle/_ref) in place of Intel oneMKL, which the reference links
  * (reference src/Matrix.cpp:243-246 calls cblas_dgemm/cblas_dgemv with
  * CblasColMajor).  This is TEST INFRASTRUCTURE: it only serves the
- * reference-build checker and is never part of the product path.
+ * reference build that pins the oracle and is never part of the product
+ * path.
  *
  * Loop order is the textbook one (k innermost, ascending); MKL's blocked
  * order is unknown and unpinned, so results agree with an MKL build to

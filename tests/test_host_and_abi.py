@@ -53,7 +53,7 @@ def test_generators_are_seeded():
     assert ne.min() >= 50 and ne.max() <= 2000
 
 
-def test_config1_shape():
+def test_rollup_20_element_shape():
     s = configs.cantilever_rollup()
     assert s.n_nodes == 41 and len(s.beams) == 20
     assert s.n_nodes * 6 == 246 and s.n_free == 240
