@@ -1197,6 +1197,8 @@ int count_launches_per_pass(const gf_batch* B) {
   int colors = 0;
   for (int c = 0; c < B->b.n_colors; ++c) colors += B->b.color_off[c + 1] > B->b.color_off[c];
   const ChainData& cd = B->b.chain;
+  // chains only: one gather launch in place of the colour passes
+  if (B->b.n_elem && !B->b.full_band && cd.n_chain_elems == B->b.n_elem) colors = 1;
   int chain_launches = 0;
   if (cd.n_chain_elems) {
     chain_launches = 2;

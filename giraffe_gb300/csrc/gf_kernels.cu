@@ -714,6 +714,36 @@ __global__ void k_beam_scatter(Batch b, int color) {
   if (lane < 18 && myg >= 0) b.P[inf.dof_off + myg] += b.Fe[(int64_t)lane * ne + e];
 }
 
+// MountGlobal of the internal forces when every Beam_1 element of the batch
+// belongs to a chain and no band is filled (the chain solver reads K_e from
+// the element scratch): one thread per node DOF gathers the forces of the one
+// or two elements on its node in a single launch, in place of the two colour
+// passes of k_beam_scatter.  Chain element e of a structure sits on its local
+// nodes 2e, 2e+1, 2e+2.  k_zero has just cleared P, so the sum (0 + f_a) + f_b
+// formed here equals the colour-ordered scatter's, whichever element's colour
+// comes first (IEEE addition is commutative).
+__global__ void k_chain_gather_f(Batch b) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)b.n_nodes * 6) return;
+  const int g = b.gl[t];
+  if (g < 0) return;
+  const int i = (int)(t / 6), q = (int)(t - (int64_t)i * 6);
+  const int s = b.node_struct[i];
+  const StructInfo& inf = b.info[s];
+  if (!inf.is_chain || !iterating(b.state[s])) return;
+  const int ln = i - inf.node_off, eo = inf.elem_off;
+  const int64_t ne = b.n_elem;
+  double v = 0.0;
+  if (ln & 1) {
+    v += b.Fe[(int64_t)(6 + q) * ne + eo + (ln >> 1)];
+  } else {
+    const int el = ln >> 1;
+    if (el >= 1) v += b.Fe[(int64_t)(12 + q) * ne + eo + el - 1];
+    if (el < inf.n_elem) v += b.Fe[(int64_t)q * ne + eo + el];
+  }
+  b.P[inf.dof_off + g] = v;
+}
+
 // NodalLoad::Mount for every load entry of a structure, in entry order (one
 // thread per structure keeps the accumulation order fixed).
 __global__ void k_loads(Batch b) {
@@ -1418,6 +1448,13 @@ static void launch_mount(const Batch& b, cudaStream_t st, LaunchProf* prof) {
     // reads (the reference mounts loads before damping)
     if (b.n_pipe_press) k_pipe_pressure<<<(b.n_pipe_press + 127) / 128, 128, 0, st>>>(b);
     if (b.any_rayleigh) k_beam_rayleigh<<<(b.n_elem + 127) / 128, 128, 0, st>>>(b);
+  }
+  if (!b.full_band && b.chain.n_chain_elems == b.n_elem) {
+    // chains only: the residual is all the scatter would assemble
+    ProfScope q(prof, st, KC_SCATTER);
+    const int64_t nt = (int64_t)b.n_nodes * 6;
+    k_chain_gather_f<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(b);
+    return;
   }
   for (int c = 0; c < b.n_colors; ++c) {
     int cnt = b.color_off[c + 1] - b.color_off[c];
